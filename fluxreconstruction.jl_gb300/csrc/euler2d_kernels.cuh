@@ -1,0 +1,457 @@
+// euler2d.cu -- fused 2D Euler flux-reconstruction residual + SSPRK3 stage.
+//
+// One launch evaluates the residual of example/shock-vortex.jl:26-118 (the
+// dudt! closure: volume flux :48-55, face interpolation :57-71, interface
+// Riemann flux :73-89, derivative :91-100, correction :102-115) on every
+// element and applies one Shu-Osher SSPRK3 stage update to it.  The state
+// never leaves the Julia layout u[i, j, k, l, m] (element index fastest), so a
+// warp of 32 consecutive elements reads every (k, l, m) plane with one
+// 128-byte (FP32) or 256-byte (FP64) coalesced transaction.
+//
+// CTA = TX x TY elements.  Thread (ex, ln, ey) is first an "x-line" thread
+// (element ex, row s = ln: it owns the NP points along r) and later a
+// "y-line" thread (element ex, column r = ln).  Shared memory carries the
+// transposition between the two sweeps, the face traces and the interface
+// fluxes.  Faces on the tile edge use traces of the neighbouring elements,
+// recomputed from global memory (L2-resident) with the same arithmetic as the
+// owner, so both sides of every face see bit-identical fluxes.
+#pragma once
+#include "fr_common.cuh"
+#include "frgpu_internal.h"
+
+using namespace frk;
+
+namespace {
+
+enum { MODE_FP64 = 0, MODE_FP32K = 1 };
+
+template <class Real, int NP> struct E2DArgs {
+    int nx, ny;
+    const Real *uin;  // stage input (FP64) or u^n high part (FP32K)
+    const Real *din;  // FP32K: increment added to uin (stages 2, 3), else null
+    const Real *un;   // FP64 stages 2, 3: u^n
+    Real *out;        // residual (stage 0), next state (FP64) / increment or new high part (FP32K)
+    Real *ul;         // FP32K stage 3: low part, updated in place
+    const double *dtp;
+    Real iJx, iJy, gamma, gm1;
+    int bc[4];
+    Real fixed[4][4];
+    Ops<Real, NP> ops;
+    int *status;
+};
+
+template <class Real, int NP> struct Tile;
+// Tile shapes: TX elements along x (one warp), TY rows.
+// Shared memory per CTA (see Smem below) stays under 227 KB:
+// FP64 NP=3/TY=4 158 KB, NP=4/TY=2 122 KB, NP=5/TY=1 98 KB, NP=6/TY=1 130 KB;
+// FP32 NP=2/TY=8 86 KB, NP=4/TY=2 61 KB, NP=6/TY=1 65 KB.
+template <int NP> struct Tile<double, NP> {
+    static constexpr int TX = 32;
+    static constexpr int TY = NP <= 3 ? 4 : (NP == 4 ? 2 : 1);
+};
+template <int NP> struct Tile<float, NP> {
+    static constexpr int TX = 32;
+    static constexpr int TY = NP <= 2 ? 8 : (NP <= 4 ? 2 : 1);
+};
+
+template <class Real, int NP, int TX, int TY> struct Smem {
+    static constexpr int U = TY * NP * NP * 4 * TX;
+    static constexpr int TR = TY * NP * 4 * TX;
+    static constexpr int HY = 2 * NP * 4 * TX;
+    static constexpr int HX = 2 * TY * NP * 4;
+    static constexpr int FX = TY * NP * 4 * (TX + 1);
+    static constexpr int FY = (TY + 1) * NP * 4 * TX;
+    static constexpr int total = 2 * U + 4 * TR + HY + HX + FX + FY;
+    static constexpr size_t bytes = sizeof(Real) * total;
+};
+
+// Element (io, jo) whose trace stands in for the neighbour at (i, j) outside
+// the tile; false means the neighbour is a fixed ghost state.
+__device__ __forceinline__ bool resolve(int i, int n, int bc_lo, int bc_hi, int &io) {
+    if (i < 0) {
+        if (bc_lo == FRGPU_BC_PERIODIC) { io = n - 1; return true; }
+        if (bc_lo == FRGPU_BC_COPY) { io = 0; return true; }
+        return false;
+    }
+    if (i >= n) {
+        if (bc_hi == FRGPU_BC_PERIODIC) { io = 0; return true; }
+        if (bc_hi == FRGPU_BC_COPY) { io = n - 1; return true; }
+        return false;
+    }
+    io = i;
+    return true;
+}
+
+template <class Real>
+__device__ __forceinline__ Real ld_state(const Real *__restrict__ uin, const Real *__restrict__ din, size_t idx) {
+    Real v = __ldg(uin + idx);
+    if (din != nullptr) v += __ldg(din + idx);
+    return v;
+}
+
+template <class Real, int NP, int FLUX, int MODE, int STAGE>
+__global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
+    k_euler2d(const E2DArgs<Real, NP> a) {
+    constexpr int TX = Tile<Real, NP>::TX, TY = Tile<Real, NP>::TY;
+    constexpr int NT = TX * NP * TY;
+    using S = Smem<Real, NP, TX, TY>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Real *s_u = reinterpret_cast<Real *>(smem_raw);
+    Real *s_g = s_u + S::U;
+    Real *s_uxl = s_g + S::U;
+    Real *s_uxr = s_uxl + S::TR;
+    Real *s_uyb = s_uxr + S::TR;
+    Real *s_uyt = s_uyb + S::TR;
+    Real *s_hy = s_uyt + S::TR;
+    Real *s_hx = s_hy + S::HY;
+    Real *s_Fx = s_hx + S::HX;
+    Real *s_Fy = s_Fx + S::FX;
+#define SU(ey, l, k, m, ex) s_u[((((ey) * NP + (l)) * NP + (k)) * 4 + (m)) * TX + (ex)]
+#define SG(ey, l, k, m, ex) s_g[((((ey) * NP + (l)) * NP + (k)) * 4 + (m)) * TX + (ex)]
+#define STR(arr, ey, q, m, ex) arr[(((ey) * NP + (q)) * 4 + (m)) * TX + (ex)]
+#define SHY(side, k, m, ex) s_hy[(((side) * NP + (k)) * 4 + (m)) * TX + (ex)]
+#define SHX(side, ey, l, m) s_hx[(((side) * TY + (ey)) * NP + (l)) * 4 + (m)]
+#define SFX(ey, l, m, f) s_Fx[(((ey) * NP + (l)) * 4 + (m)) * (TX + 1) + (f)]
+#define SFY(fy, k, m, ex) s_Fy[(((fy) * NP + (k)) * 4 + (m)) * TX + (ex)]
+
+    const int tid = threadIdx.x;
+    const int ex = tid % TX, ln = (tid / TX) % NP, ey = tid / (TX * NP);
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+    const int nx = a.nx, ny = a.ny;
+    const int vx = min(TX, nx - i0), vy = min(TY, ny - j0);
+    const bool valid = ex < vx && ey < vy;
+    const size_t plane = (size_t)nx * ny;
+    const Real *__restrict__ uin = a.uin;
+    const Real *__restrict__ din = a.din;
+    const Ops<Real, NP> &op = a.ops;
+    int bad = 0;
+
+    // ---- halo: traces of the neighbours across the tile edges --------------
+    for (int t = tid; t < 2 * NP * (TX + TY); t += NT) {
+        if (t < 2 * NP * TX) {
+            const int hx = t % TX, hk = (t / TX) % NP, side = t / (TX * NP);
+            if (hx >= vx) continue;
+            // side 0: row below needs its top trace (lr along s);
+            // side 1: row above needs its bottom trace (ll along s)
+            const int jn = side == 0 ? j0 - 1 : j0 + vy;
+            const Real *w = side == 0 ? op.lr : op.ll;
+            int jo;
+            if (resolve(jn, ny, a.bc[2], a.bc[3], jo)) {
+                const size_t base = (size_t)(i0 + hx) + (size_t)nx * jo + plane * hk;
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    Real v[NP];
+#pragma unroll
+                    for (int l = 0; l < NP; ++l) v[l] = ld_state(uin, din, base + plane * (NP * (l + NP * m)));
+                    SHY(side, hk, m, hx) = dotw<Real, NP>(v, w);
+                }
+            } else {
+                const int s = side == 0 ? 2 : 3;
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    Real v[NP];
+#pragma unroll
+                    for (int l = 0; l < NP; ++l) v[l] = a.fixed[s][m];
+                    SHY(side, hk, m, hx) = dotw<Real, NP>(v, w);
+                }
+            }
+        } else {
+            const int u = t - 2 * NP * TX;
+            const int hy = u % TY, hl = (u / TY) % NP, side = u / (TY * NP);
+            if (hy >= vy) continue;
+            // side 0: left neighbour needs its right trace (lr along r);
+            // side 1: right neighbour needs its left trace (ll along r)
+            const int in_ = side == 0 ? i0 - 1 : i0 + vx;
+            const Real *w = side == 0 ? op.lr : op.ll;
+            int io;
+            if (resolve(in_, nx, a.bc[0], a.bc[1], io)) {
+                const size_t base = (size_t)io + (size_t)nx * (j0 + hy) + plane * (NP * hl);
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    Real v[NP];
+#pragma unroll
+                    for (int k = 0; k < NP; ++k) v[k] = ld_state(uin, din, base + plane * (k + NP * NP * m));
+                    SHX(side, hy, hl, m) = dotw<Real, NP>(v, w);
+                }
+            } else {
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    Real v[NP];
+#pragma unroll
+                    for (int k = 0; k < NP; ++k) v[k] = a.fixed[side][m];
+                    SHX(side, hy, hl, m) = dotw<Real, NP>(v, w);
+                }
+            }
+        }
+    }
+
+    // ---- phase A: x-line (element ex, row l = ln) --------------------------
+    const int i = i0 + ex, j = j0 + ey;
+    Real rx[NP][4], fxl[4], fxr[4];
+    {
+        const int l = ln;
+        Real u[NP][4];
+        if (valid) {
+            const size_t base = (size_t)i + (size_t)nx * j + plane * (NP * l);
+#pragma unroll
+            for (int m = 0; m < 4; ++m)
+#pragma unroll
+                for (int k = 0; k < NP; ++k) u[k][m] = ld_state(uin, din, base + plane * (k + NP * NP * m));
+        } else {
+#pragma unroll
+            for (int k = 0; k < NP; ++k) {
+                u[k][0] = Real(1); u[k][1] = Real(0); u[k][2] = Real(0); u[k][3] = Real(1);
+            }
+        }
+        Real fx[NP][4], gy[NP][4];
+#pragma unroll
+        for (int k = 0; k < NP; ++k) euler2d_flux<Real>(u[k], a.gm1, a.iJx, a.iJy, fx[k], gy[k], bad);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            Real uc[NP], fc[NP];
+#pragma unroll
+            for (int k = 0; k < NP; ++k) { uc[k] = u[k][m]; fc[k] = fx[k][m]; }
+#pragma unroll
+            for (int k = 0; k < NP; ++k) rx[k][m] = dotw<Real, NP>(fc, op.D[k]);
+            STR(s_uxl, ey, l, m, ex) = dotw<Real, NP>(uc, op.ll);
+            STR(s_uxr, ey, l, m, ex) = dotw<Real, NP>(uc, op.lr);
+            fxl[m] = dotw<Real, NP>(fc, op.ll);
+            fxr[m] = dotw<Real, NP>(fc, op.lr);
+#pragma unroll
+            for (int k = 0; k < NP; ++k) {
+                SU(ey, l, k, m, ex) = u[k][m];
+                SG(ey, l, k, m, ex) = gy[k][m];
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- phase B: y-line (element ex, column k = ln) + x interface flux ----
+    Real ry[NP][4], gyb[4], gyt[4];
+    {
+        const int k = ln;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            Real uc[NP], gc[NP];
+#pragma unroll
+            for (int l = 0; l < NP; ++l) { uc[l] = SU(ey, l, k, m, ex); gc[l] = SG(ey, l, k, m, ex); }
+#pragma unroll
+            for (int l = 0; l < NP; ++l) ry[l][m] = dotw<Real, NP>(gc, op.D[l]);
+            STR(s_uyb, ey, k, m, ex) = dotw<Real, NP>(uc, op.ll);
+            STR(s_uyt, ey, k, m, ex) = dotw<Real, NP>(uc, op.lr);
+            gyb[m] = dotw<Real, NP>(gc, op.ll);
+            gyt[m] = dotw<Real, NP>(gc, op.lr);
+        }
+        // x interface flux at the left face of element ex (row l = ln)
+        if (valid) {
+            const int l = ln;
+            Real wL[4], wR[4], F[4];
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                wL[m] = ex > 0 ? STR(s_uxr, ey, l, m, ex - 1) : SHX(0, ey, l, m);
+                wR[m] = STR(s_uxl, ey, l, m, ex);
+            }
+            riemann2d<Real, 0, FLUX>(wL, wR, a.gamma, a.gm1, F);
+#pragma unroll
+            for (int m = 0; m < 4; ++m) SFX(ey, l, m, ex) = F[m];
+            if (ex == vx - 1) {
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    wL[m] = STR(s_uxr, ey, l, m, ex);
+                    wR[m] = SHX(1, ey, l, m);
+                }
+                riemann2d<Real, 0, FLUX>(wL, wR, a.gamma, a.gm1, F);
+#pragma unroll
+                for (int m = 0; m < 4; ++m) SFX(ey, l, m, ex + 1) = F[m];
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- phase C: y interface flux; x correction into s_g -------------------
+    {
+        const int k = ln;
+        if (valid) {
+            Real wL[4], wR[4], F[4];
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                wL[m] = ey > 0 ? STR(s_uyt, ey - 1, k, m, ex) : SHY(0, k, m, ex);
+                wR[m] = STR(s_uyb, ey, k, m, ex);
+            }
+            riemann2d<Real, 1, FLUX>(wL, wR, a.gamma, a.gm1, F);
+#pragma unroll
+            for (int m = 0; m < 4; ++m) SFY(ey, k, m, ex) = F[m];
+            if (ey == vy - 1) {
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    wL[m] = STR(s_uyt, ey, k, m, ex);
+                    wR[m] = SHY(1, k, m, ex);
+                }
+                riemann2d<Real, 1, FLUX>(wL, wR, a.gamma, a.gm1, F);
+#pragma unroll
+                for (int m = 0; m < 4; ++m) SFY(ey + 1, k, m, ex) = F[m];
+            }
+            // x correction of row l = ln: rx + (F*_L iJx - f_L) dgl + (F*_R iJx - f_R) dgr
+            const int l = ln;
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                const Real aL = SFX(ey, l, m, ex) * a.iJx - fxl[m];
+                const Real aR = SFX(ey, l, m, ex + 1) * a.iJx - fxr[m];
+#pragma unroll
+                for (int kk = 0; kk < NP; ++kk) SG(ey, l, kk, m, ex) = fmaR<Real>(aR, op.dgr[kk], fmaR<Real>(aL, op.dgl[kk], rx[kk][m]));
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- phase D: y correction, residual, stage update (column k = ln) ------
+    if (valid) {
+        const int k = ln;
+        const Real dt = (Real)(*a.dtp);
+        const size_t base = (size_t)i + (size_t)nx * j + plane * k;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            const Real bB = SFY(ey, k, m, ex) * a.iJy - gyb[m];
+            const Real bT = SFY(ey + 1, k, m, ex) * a.iJy - gyt[m];
+#pragma unroll
+            for (int l = 0; l < NP; ++l) {
+                const Real r = fmaR<Real>(bT, op.dgr[l], fmaR<Real>(bB, op.dgl[l], SG(ey, l, k, m, ex) + ry[l][m]));
+                const Real du = -r;
+                const size_t idx = base + plane * (NP * (l + NP * m));
+                Real res;
+                if (STAGE == 0) {
+                    res = du;
+                    a.out[idx] = res;
+                } else if (MODE == MODE_FP64) {
+                    const Real ui = SU(ey, l, k, m, ex);
+                    if (STAGE == 1) {
+                        res = fmaR<Real>(dt, du, ui);
+                    } else if (STAGE == 2) {
+                        const Real un = a.un[idx];
+                        res = (fmaR<Real>(dt, du, fmaR<Real>(Real(3), un, ui))) * Real(0.25);
+                    } else {
+                        const Real un = a.un[idx];
+                        res = fmaR<Real>(Real(2) * dt, du, fmaR<Real>(Real(2), ui, un)) * Real(1.0 / 3.0);
+                    }
+                    a.out[idx] = res;
+                } else {
+                    // FP32K: stage values are u^n + d; only increments are stored,
+                    // and the step's total increment is added to u^n with a
+                    // compensated (Kahan/Fast2Sum) sum whose low part persists.
+                    if (STAGE == 1) {
+                        res = dt * du;
+                        a.out[idx] = res;
+                    } else if (STAGE == 2) {
+                        const Real d1 = __ldg(din + idx);
+                        res = fmaR<Real>(dt, du, d1) * Real(0.25);
+                        a.out[idx] = res;
+                    } else {
+                        const Real d2 = __ldg(din + idx);
+                        const Real d3 = fmaR<Real>(dt, du, d2) * Real(2.0 / 3.0);
+                        const Real hi = __ldg(uin + idx);
+                        const Real lo = a.ul[idx];
+                        const Real y = d3 + lo;
+                        const Real t = hi + y;
+                        const Real lo_new = y - (t - hi);
+                        a.out[idx] = t;
+                        a.ul[idx] = lo_new;
+                        res = t;
+                    }
+                }
+                if (!isfinite(res)) bad |= ST_NONFINITE;
+            }
+        }
+    }
+    if (bad) atomicOr(a.status, bad);
+#undef SU
+#undef SG
+#undef STR
+#undef SHY
+#undef SHX
+#undef SFX
+#undef SFY
+}
+
+template <class Real, int NP> Ops<Real, NP> make_ops(const frgpu_space &s) {
+    Ops<Real, NP> o;
+    for (int k = 0; k < NP; ++k) {
+        o.ll[k] = (Real)s.ll[k];
+        o.lr[k] = (Real)s.lr[k];
+        o.dgl[k] = (Real)s.dhl[k];
+        o.dgr[k] = (Real)s.dhr[k];
+        for (int q = 0; q < NP; ++q) o.D[k][q] = (Real)s.dl[k + NP * q];
+    }
+    return o;
+}
+
+template <class Real, int NP, int FLUX, int MODE, int STAGE>
+int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
+    using T = Tile<Real, NP>;
+    using S = Smem<Real, NP, T::TX, T::TY>;
+    E2DArgs<Real, NP> a;
+    a.nx = p->sp.nx;
+    a.ny = p->sp.ny;
+    a.uin = (const Real *)in;
+    a.din = (const Real *)din;
+    a.un = (const Real *)p->s0;
+    a.out = (Real *)out;
+    a.ul = (Real *)p->s3;
+    a.dtp = p->d_dt;
+    a.iJx = (Real)(1.0 / (0.5 * p->sp.dx));
+    a.iJy = (Real)(1.0 / (0.5 * p->sp.dy));
+    a.gamma = (Real)p->d.gamma;
+    a.gm1 = (Real)(p->d.gamma - 1.0);
+    for (int s = 0; s < 4; ++s) {
+        a.bc[s] = p->d.bc[s];
+        for (int m = 0; m < 4; ++m) a.fixed[s][m] = (Real)p->d.fixed_state[s][m];
+    }
+    a.ops = make_ops<Real, NP>(p->sp);
+    a.status = p->d_status;
+    static_assert(S::bytes <= 227 * 1024, "shared memory per CTA exceeds 227 KB");
+    auto kern = k_euler2d<Real, NP, FLUX, MODE, STAGE>;
+    // the dynamic shared-memory opt-in is set once per instantiation (and on
+    // every prepare pass, which precedes each graph capture)
+    static bool attr_set = false;
+    if (!attr_set || p->prepare_only) {
+        FR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::bytes));
+        attr_set = true;
+    }
+    if (p->prepare_only) return FRGPU_OK;
+    dim3 grid((a.nx + T::TX - 1) / T::TX, (a.ny + T::TY - 1) / T::TY);
+    kern<<<grid, T::TX * NP * T::TY, S::bytes, p->stream>>>(a);
+    FR_CUDA(cudaGetLastError());
+    p->launches += 1;
+    return FRGPU_OK;
+}
+
+template <class Real, int NP, int MODE>
+int dispatch_stage(frgpu_problem *p, int stage, const void *in, const void *din, void *out) {
+    const int flux = p->d.flux == FRGPU_FLUX_HLL ? FLUX_HLL : FLUX_LF;
+#define FR_ST(S)                                                                                                   \
+    return flux == FLUX_HLL ? launch_t<Real, NP, FLUX_HLL, MODE, S>(p, in, din, out)                               \
+                            : launch_t<Real, NP, FLUX_LF, MODE, S>(p, in, din, out)
+    switch (stage) {
+    case 0: FR_ST(0);
+    case 1: FR_ST(1);
+    case 2: FR_ST(2);
+    case 3: FR_ST(3);
+    }
+#undef FR_ST
+    fr_set_error("euler2d: bad stage");
+    return FRGPU_ERR_ARG;
+}
+
+template <class Real, int MODE>
+int dispatch_np(frgpu_problem *p, int stage, const void *in, const void *din, void *out) {
+    switch (p->sp.np) {
+    case 2: return dispatch_stage<Real, 2, MODE>(p, stage, in, din, out);
+    case 3: return dispatch_stage<Real, 3, MODE>(p, stage, in, din, out);
+    case 4: return dispatch_stage<Real, 4, MODE>(p, stage, in, din, out);
+    case 5: return dispatch_stage<Real, 5, MODE>(p, stage, in, din, out);
+    case 6: return dispatch_stage<Real, 6, MODE>(p, stage, in, din, out);
+    }
+    fr_set_error("euler2d: polynomial degree must be 1..5");
+    return FRGPU_ERR_UNSUPPORTED;
+}
+
+} // namespace

@@ -1,0 +1,105 @@
+// frgpu_internal.h -- host-side structures shared by the libfrgpu translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/frgpu.h"
+
+struct frgpu_space {
+    int dim = 1, nx = 0, ny = 1, deg = 0, np = 0;
+    double x0 = 0, x1 = 1, y0 = 0, y1 = 1, dx = 0, dy = 0;
+    std::vector<double> J;        // 1D: per-element Jacobian dx_i / 2
+    std::vector<double> xpl, w1;  // Gauss-Legendre nodes / weights on [-1, 1]
+    std::vector<double> wp;       // 1D: w1; 2D: w1 (x) w1, wp[k + np*l] = w_k w_l
+    std::vector<double> ll, lr;   // Lagrange basis at r = -1, +1
+    std::vector<double> dl;       // lpdm, column-major dl[m + np*k] = l_k'(r_m)
+    std::vector<double> dhl, dhr; // correction-function derivatives at the nodes
+    std::vector<double> V, iV;    // Vandermonde matrix and inverse (1D np x np, 2D np^2 x np^2)
+    std::vector<double> xc, yc;   // element centres
+};
+
+// Device buffers of a problem.  FP64: s0 = u^n, s1/s2 = stage states.
+// FP32K: s0 = u^n high part, s1/s2 = stage increments d1/d2, s3 = low part.
+struct frgpu_problem {
+    frgpu_space sp;
+    frgpu_problem_desc d{};
+    std::vector<double> velo, weights;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    long ndof = 0;
+    size_t esize = 8; // bytes per state value on the device
+    void *s0 = nullptr, *s1 = nullptr, *s2 = nullptr, *s3 = nullptr;
+    double *d_dt = nullptr;  // device copy of dt (graphs read it from here)
+    int *d_status = nullptr; // accumulated status bits
+    double *d_red = nullptr; // reduction scratch
+    int *d_flags = nullptr;  // troubled flags per element
+    int *d_count = nullptr;  // troubled count
+    void *d_velo = nullptr, *d_w = nullptr; // BGK velocity grid (state precision)
+    void *d_J = nullptr;                    // 1D per-element Jacobian (state precision)
+    void *d_V = nullptr, *d_iV = nullptr;   // Vandermonde matrix / inverse (state precision)
+    void *rhs_in = nullptr, *rhs_out = nullptr; // scratch of frgpu_rhs
+    int parity = 0;                         // FP32K: which buffer holds u^n (0: s0, 1: s1)
+    bool prepare_only = false;              // launchers only set kernel attributes
+    // post-step filter
+    int indicator = FRGPU_IND_NONE;
+    double lam = 0, S0 = 0, kappa = 0;
+    // captured step graph
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    int graph_ind = -1;
+    long graph_launches = 0; // kernels per captured step
+    double host_dt = -1.0;
+    long launches = 0;
+};
+
+constexpr int FR_RED_BLOCKS = 608; // reduction partial blocks (4 x 152 SMs)
+// d_red layout: [FR_RED_BLOCKS*6 partials][8 final][64 quadrature weights]
+constexpr int FR_RED_FINAL = FR_RED_BLOCKS * 6;
+constexpr int FR_RED_WP = FR_RED_BLOCKS * 6 + 8;
+constexpr int FR_RED_SIZE = FR_RED_BLOCKS * 6 + 8 + 64;
+
+// Current u^n buffers of a problem (FP32K ping-pongs the high part).
+inline void *fr_state_hi(frgpu_problem *p) { return p->parity ? p->s1 : p->s0; }
+inline void *fr_state_tmp(frgpu_problem *p) { return p->parity ? p->s0 : p->s1; }
+
+// Thread-local error handling.
+void fr_set_error(const std::string &msg);
+int fr_cuda_fail(cudaError_t e, const char *what);
+#define FR_CUDA(call)                                                                                              \
+    do {                                                                                                           \
+        cudaError_t _e = (call);                                                                                   \
+        if (_e != cudaSuccess) return fr_cuda_fail(_e, #call);                                                     \
+    } while (0)
+
+// Setup math (setup.cpp)
+namespace frsetup {
+void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w);
+double dlegendre(int n, double x);
+void lagrange_point(const double *sp, int nsp, double x, double *l);
+void dlagrange(const double *sp, int nsp, double *lpdm);
+void dcorrection(int kind, int deg, const double *x, int n, double *dgl, double *dgr);
+double jacobi_orthonormal(int n, double x);
+void vandermonde(int deg, const double *r, int n, double *V);
+void vandermonde_quad(int deg, const double *r, const double *s, int n, double *V);
+bool invert(int n, const double *A, double *Ainv);
+void build_1d(frgpu_space &s, int correction);
+void build_2d(frgpu_space &s);
+} // namespace frsetup
+
+// Kernel launchers (return FRGPU_OK or an error; stage 0 = residual only)
+// euler2d.cu
+int fr_launch_euler2d(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
+int fr_launch_euler2d_reduce(frgpu_problem *p, const void *state, const void *lo, double *out_sums,
+                             double *out_speed, double cfl_dx, double cfl_dy);
+// scalar1d.cu
+int fr_launch_scalar1d(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
+int fr_launch_euler1d(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
+int fr_launch_bgk1d(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
+int fr_launch_interp_face(const double *d_f, long n, int np, const double *ll, const double *lr, double *d_out,
+                          cudaStream_t st);
+int fr_launch_poly_derivative(const double *d_f, long n, int np, const double *pdm, double *d_out,
+                              cudaStream_t st);
+// filter.cu
+int fr_launch_filter2d(frgpu_problem *p, int indicator, double lam, double S0, double kappa);
+int fr_launch_filter1d(frgpu_problem *p, int indicator, double lam, double S0, double kappa);

@@ -1,0 +1,802 @@
+// runtime.cu -- the C ABI of libfrgpu.so: spaces, problems, device memory,
+// streams, captured SSPRK3 step graphs, error handling.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <exception>
+#include <string>
+#include <vector>
+
+#include "frgpu_internal.h"
+
+static thread_local std::string g_err;
+
+void fr_set_error(const std::string &msg) { g_err = msg; }
+int fr_cuda_fail(cudaError_t e, const char *what) {
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return FRGPU_ERR_CUDA;
+}
+
+#define FR_TRY try {
+#define FR_CATCH                                                                                                   \
+    }                                                                                                              \
+    catch (const std::exception &ex) {                                                                             \
+        fr_set_error(ex.what());                                                                                   \
+        return FRGPU_ERR_ARG;                                                                                      \
+    }                                                                                                              \
+    catch (...) {                                                                                                  \
+        fr_set_error("unknown C++ exception");                                                                     \
+        return FRGPU_ERR_ARG;                                                                                      \
+    }
+
+#define FR_REQ(cond, msg)                                                                                          \
+    do {                                                                                                           \
+        if (!(cond)) {                                                                                             \
+            fr_set_error(msg);                                                                                     \
+            return FRGPU_ERR_ARG;                                                                                  \
+        }                                                                                                          \
+    } while (0)
+
+extern "C" {
+
+FRGPU_API int frgpu_version(void) { return 100; }
+
+FRGPU_API int frgpu_last_error(char *buf, unsigned long n) {
+    if (!buf || n == 0) return (int)g_err.size();
+    std::snprintf(buf, n, "%s", g_err.c_str());
+    return (int)g_err.size();
+}
+
+// ------------------------------------------------------------------ setup math
+FRGPU_API int frgpu_legendre_point(int deg, double *r, double *w) {
+    FR_REQ(deg >= 0 && deg < 64 && r, "legendre_point: bad arguments");
+    FR_TRY
+    std::vector<double> x, wt;
+    frsetup::gauss_legendre(deg + 1, x, wt);
+    std::memcpy(r, x.data(), sizeof(double) * (deg + 1));
+    if (w) std::memcpy(w, wt.data(), sizeof(double) * (deg + 1));
+    return FRGPU_OK;
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_lagrange_point(const double *sp, int nsp, double x, double *l) {
+    FR_REQ(sp && l && nsp > 0, "lagrange_point: bad arguments");
+    frsetup::lagrange_point(sp, nsp, x, l);
+    return FRGPU_OK;
+}
+
+FRGPU_API int frgpu_dlagrange(const double *sp, int nsp, double *lpdm) {
+    FR_REQ(sp && lpdm && nsp > 0, "dlagrange: bad arguments");
+    frsetup::dlagrange(sp, nsp, lpdm);
+    return FRGPU_OK;
+}
+
+FRGPU_API int frgpu_dcorrection(int correction, int deg, const double *x, int n, double *dgl, double *dgr) {
+    FR_REQ(x && dgl && dgr && n > 0 && deg >= 1, "dcorrection: bad arguments");
+    FR_REQ(correction >= FRGPU_RADAU && correction <= FRGPU_HUYNH, "dcorrection: unknown correction");
+    frsetup::dcorrection(correction, deg, x, n, dgl, dgr);
+    return FRGPU_OK;
+}
+
+FRGPU_API int frgpu_vandermonde(int deg, const double *r, int n, double *V) {
+    FR_REQ(r && V && n > 0 && deg >= 0, "vandermonde: bad arguments");
+    frsetup::vandermonde(deg, r, n, V);
+    return FRGPU_OK;
+}
+
+FRGPU_API int frgpu_vandermonde_quad(int deg, const double *r, const double *s, int n, double *V) {
+    FR_REQ(r && s && V && n > 0 && deg >= 0, "vandermonde_quad: bad arguments");
+    frsetup::vandermonde_quad(deg, r, s, n, V);
+    return FRGPU_OK;
+}
+
+// ------------------------------------------------------------------ spaces
+FRGPU_API int frgpu_space_create_1d(double x0, double x1, int nx, int deg, int correction, frgpu_space **out) {
+    FR_REQ(out, "space_create_1d: null output");
+    *out = nullptr;
+    FR_REQ(nx >= 1 && deg >= 1 && deg <= 5, "space_create_1d: need nx >= 1 and 1 <= deg <= 5");
+    FR_REQ(x1 > x0, "space_create_1d: need x1 > x0");
+    FR_REQ(correction >= FRGPU_RADAU && correction <= FRGPU_HUYNH, "space_create_1d: unknown correction");
+    FR_TRY
+    auto *s = new frgpu_space();
+    s->dim = 1;
+    s->nx = nx;
+    s->ny = 1;
+    s->deg = deg;
+    s->np = deg + 1;
+    s->x0 = x0;
+    s->x1 = x1;
+    frsetup::build_1d(*s, correction);
+    *out = s;
+    return FRGPU_OK;
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_space_create_2d(double x0, double x1, int nx, double y0, double y1, int ny, int deg,
+                                    frgpu_space **out) {
+    FR_REQ(out, "space_create_2d: null output");
+    *out = nullptr;
+    FR_REQ(nx >= 1 && ny >= 1 && deg >= 1 && deg <= 5, "space_create_2d: need nx, ny >= 1 and 1 <= deg <= 5");
+    FR_REQ(x1 > x0 && y1 > y0, "space_create_2d: empty domain");
+    FR_TRY
+    auto *s = new frgpu_space();
+    s->dim = 2;
+    s->nx = nx;
+    s->ny = ny;
+    s->deg = deg;
+    s->np = deg + 1;
+    s->x0 = x0;
+    s->x1 = x1;
+    s->y0 = y0;
+    s->y1 = y1;
+    frsetup::build_2d(*s);
+    *out = s;
+    return FRGPU_OK;
+    FR_CATCH
+}
+
+static void copy_ops(frgpu_space &s, const double *ll, const double *lr, const double *dl, const double *dhl,
+                     const double *dhr, const double *V, const double *iV, int nV) {
+    const int np = s.np;
+    s.ll.assign(ll, ll + np);
+    s.lr.assign(lr, lr + np);
+    s.dl.assign(dl, dl + np * np);
+    s.dhl.assign(dhl, dhl + np);
+    s.dhr.assign(dhr, dhr + np);
+    if (V) s.V.assign(V, V + nV * nV);
+    if (iV) s.iV.assign(iV, iV + nV * nV);
+}
+
+FRGPU_API int frgpu_space_create_1d_ops(int nx, int deg, const double *J, const double *ll, const double *lr,
+                                        const double *dl, const double *dhl, const double *dhr, const double *V,
+                                        const double *iV, frgpu_space **out) {
+    FR_REQ(out, "space_create_1d_ops: null output");
+    *out = nullptr;
+    FR_REQ(nx >= 1 && deg >= 1 && deg <= 5 && J && ll && lr && dl && dhl && dhr, "space_create_1d_ops: bad arguments");
+    FR_TRY
+    auto *s = new frgpu_space();
+    s->dim = 1;
+    s->nx = nx;
+    s->deg = deg;
+    s->np = deg + 1;
+    std::vector<double> w;
+    frsetup::gauss_legendre(s->np, s->xpl, s->w1);
+    s->wp = s->w1;
+    s->J.assign(J, J + nx);
+    copy_ops(*s, ll, lr, dl, dhl, dhr, V, iV, s->np);
+    double len = 0;
+    for (int i = 0; i < nx; ++i) len += 2 * J[i];
+    s->x0 = 0;
+    s->x1 = len;
+    s->dx = len / nx;
+    s->xc.resize(nx);
+    double x = 0;
+    for (int i = 0; i < nx; ++i) {
+        s->xc[i] = x + J[i];
+        x += 2 * J[i];
+    }
+    *out = s;
+    return FRGPU_OK;
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_space_create_2d_ops(int nx, int ny, int deg, double dx, double dy, const double *ll,
+                                        const double *lr, const double *dl, const double *dhl, const double *dhr,
+                                        const double *V, const double *iV, frgpu_space **out) {
+    FR_REQ(out, "space_create_2d_ops: null output");
+    *out = nullptr;
+    FR_REQ(nx >= 1 && ny >= 1 && deg >= 1 && deg <= 5 && dx > 0 && dy > 0 && ll && lr && dl && dhl && dhr,
+           "space_create_2d_ops: bad arguments");
+    FR_TRY
+    auto *s = new frgpu_space();
+    s->dim = 2;
+    s->nx = nx;
+    s->ny = ny;
+    s->deg = deg;
+    s->np = deg + 1;
+    frsetup::gauss_legendre(s->np, s->xpl, s->w1);
+    s->wp.resize(s->np * s->np);
+    for (int l = 0; l < s->np; ++l)
+        for (int k = 0; k < s->np; ++k) s->wp[k + s->np * l] = s->w1[k] * s->w1[l];
+    copy_ops(*s, ll, lr, dl, dhl, dhr, V, iV, s->np * s->np);
+    s->x0 = 0;
+    s->x1 = dx * nx;
+    s->y0 = 0;
+    s->y1 = dy * ny;
+    s->dx = dx;
+    s->dy = dy;
+    s->xc.resize(nx);
+    s->yc.resize(ny);
+    for (int i = 0; i < nx; ++i) s->xc[i] = (i + 0.5) * dx;
+    for (int j = 0; j < ny; ++j) s->yc[j] = (j + 0.5) * dy;
+    *out = s;
+    return FRGPU_OK;
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_space_info(const frgpu_space *s, int *dim, int *nx, int *ny, int *deg) {
+    FR_REQ(s, "space_info: null space");
+    if (dim) *dim = s->dim;
+    if (nx) *nx = s->nx;
+    if (ny) *ny = s->ny;
+    if (deg) *deg = s->deg;
+    return FRGPU_OK;
+}
+
+FRGPU_API int frgpu_space_get(const frgpu_space *s, const char *name, double *out, long n) {
+    FR_REQ(s && name && out, "space_get: null argument");
+    FR_TRY
+    std::vector<double> tmp;
+    const std::vector<double> *v = nullptr;
+    std::string k(name);
+    if (k == "xpl") v = &s->xpl;
+    else if (k == "wp") v = &s->wp;
+    else if (k == "ll") v = &s->ll;
+    else if (k == "lr") v = &s->lr;
+    else if (k == "dl") v = &s->dl;
+    else if (k == "dhl") v = &s->dhl;
+    else if (k == "dhr") v = &s->dhr;
+    else if (k == "V") v = &s->V;
+    else if (k == "iV") v = &s->iV;
+    else if (k == "J") v = &s->J;
+    else if (k == "xpg") {
+        // global solution points, src/Geometry/geo_points.jl:8-15 (1D, xpg[i, k]);
+        // 2D: xpg[i, j, k, l, 1:2] of src/struct.jl:161-175 on rectangles
+        const int np = s->np;
+        if (s->dim == 1) {
+            tmp.resize((size_t)s->nx * np);
+            for (int kk = 0; kk < np; ++kk)
+                for (int i = 0; i < s->nx; ++i) {
+                    // r_x (src/Geometry/geo_transform.jl:7): ((1-r)/2) x_l + ((1+r)/2) x_r
+                    const double J = s->J.empty() ? 0.5 * s->dx : s->J[i];
+                    const double xl = s->xc[i] - J, xr = s->xc[i] + J, r = s->xpl[kk];
+                    tmp[i + (size_t)s->nx * kk] = ((1.0 - r) / 2.0) * xl + ((1.0 + r) / 2.0) * xr;
+                }
+        } else {
+            const size_t nn = (size_t)s->nx * s->ny;
+            tmp.resize(nn * np * np * 2);
+            for (int d = 0; d < 2; ++d)
+                for (int l = 0; l < np; ++l)
+                    for (int kk = 0; kk < np; ++kk)
+                        for (int j = 0; j < s->ny; ++j)
+                            for (int i = 0; i < s->nx; ++i) {
+                                double val = d == 0 ? s->xc[i] + 0.5 * s->dx * s->xpl[kk]
+                                                    : s->yc[j] + 0.5 * s->dy * s->xpl[l];
+                                tmp[i + (size_t)s->nx * j + nn * (kk + np * (l + (size_t)np * d))] = val;
+                            }
+        }
+        v = &tmp;
+    } else {
+        fr_set_error("space_get: unknown field '" + k + "'");
+        return FRGPU_ERR_ARG;
+    }
+    FR_REQ((long)v->size() <= n, "space_get: output too small");
+    std::memcpy(out, v->data(), sizeof(double) * v->size());
+    return (int)v->size();
+    FR_CATCH
+}
+
+FRGPU_API void frgpu_space_destroy(frgpu_space *s) { delete s; }
+
+} // extern "C"
+
+// ------------------------------------------------------------------ problems
+static void free_problem(frgpu_problem *p) {
+    if (!p) return;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(p->device);
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    for (auto &g : p->gexec)
+        if (g) cudaGraphExecDestroy(g);
+    void *bufs[] = {p->s0, p->s1, p->s2, p->s3, p->d_dt, p->d_status, p->d_red, p->d_flags, p->d_count,
+                    p->d_velo, p->d_w, p->d_J, p->d_V, p->d_iV, p->rhs_in, p->rhs_out};
+    for (void *b : bufs)
+        if (b) cudaFree(b);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    cudaSetDevice(cur);
+    delete p;
+}
+
+template <class T> static int upload_as(void **dst, const std::vector<double> &src) {
+    std::vector<T> tmp(src.begin(), src.end());
+    FR_CUDA(cudaMalloc(dst, sizeof(T) * (tmp.empty() ? 1 : tmp.size())));
+    if (!tmp.empty()) FR_CUDA(cudaMemcpy(*dst, tmp.data(), sizeof(T) * tmp.size(), cudaMemcpyHostToDevice));
+    return FRGPU_OK;
+}
+
+static int upload_vec(frgpu_problem *p, void **dst, const std::vector<double> &src) {
+    return p->esize == 8 ? upload_as<double>(dst, src) : upload_as<float>(dst, src);
+}
+
+static int check_status(frgpu_problem *p) {
+    int st = 0;
+    FR_CUDA(cudaMemcpyAsync(&st, p->d_status, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+    FR_CUDA(cudaStreamSynchronize(p->stream));
+    if (st == 0) return FRGPU_OK;
+    FR_CUDA(cudaMemsetAsync(p->d_status, 0, sizeof(int), p->stream));
+    if (st & 1) {
+        fr_set_error("non-finite value in the state");
+        return FRGPU_ERR_NONFINITE;
+    }
+    if (st & 2) {
+        fr_set_error("non-positive density or pressure in the state");
+        return FRGPU_ERR_UNPHYSICAL;
+    }
+    fr_set_error("device-side wait timed out");
+    return FRGPU_ERR_TIMEOUT;
+}
+
+static int launch_stage(frgpu_problem *p, int stage, const void *in, const void *din, void *out) {
+    switch (p->d.equation) {
+    case FRGPU_ADVECTION:
+    case FRGPU_BURGERS: return fr_launch_scalar1d(p, stage, in, din, out);
+    case FRGPU_EULER1D: return fr_launch_euler1d(p, stage, in, din, out);
+    case FRGPU_EULER2D: return fr_launch_euler2d(p, stage, in, din, out);
+    case FRGPU_BGK1D: return fr_launch_bgk1d(p, stage, in, din, out);
+    }
+    fr_set_error("unknown equation");
+    return FRGPU_ERR_ARG;
+}
+
+// One SSPRK3 step (+ filter) on the current buffers.
+static int enqueue_step(frgpu_problem *p) {
+    int rc;
+    if (p->d.precision == FRGPU_FP64) {
+        if ((rc = launch_stage(p, 1, p->s0, nullptr, p->s1))) return rc;
+        if ((rc = launch_stage(p, 2, p->s1, nullptr, p->s2))) return rc;
+        if ((rc = launch_stage(p, 3, p->s2, nullptr, p->s0))) return rc;
+    } else {
+        void *hi = fr_state_hi(p), *tmp = fr_state_tmp(p);
+        if ((rc = launch_stage(p, 1, hi, nullptr, tmp))) return rc;
+        if ((rc = launch_stage(p, 2, hi, tmp, p->s2))) return rc;
+        if ((rc = launch_stage(p, 3, hi, p->s2, tmp))) return rc;
+    }
+    if (p->indicator != FRGPU_IND_NONE) {
+        // the filter runs on the new state: for FP32K that is the buffer the
+        // high part moves to, so evaluate with the parity flipped
+        if (p->d.precision == FRGPU_FP32K) p->parity ^= 1;
+        rc = p->sp.dim == 2 ? fr_launch_filter2d(p, p->indicator, p->lam, p->S0, p->kappa)
+                            : fr_launch_filter1d(p, p->indicator, p->lam, p->S0, p->kappa);
+        if (p->d.precision == FRGPU_FP32K) p->parity ^= 1;
+        if (rc) return rc;
+    }
+    return FRGPU_OK;
+}
+
+static int build_graphs(frgpu_problem *p) {
+    for (auto &g : p->gexec)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    const int ngraphs = p->d.precision == FRGPU_FP32K ? 2 : 1;
+    const int parity0 = p->parity;
+    for (int gi = 0; gi < ngraphs; ++gi) {
+        p->parity = gi;
+        p->prepare_only = true;
+        int rc = enqueue_step(p);
+        p->prepare_only = false;
+        if (rc) {
+            p->parity = parity0;
+            return rc;
+        }
+        const long before = p->launches;
+        cudaGraph_t g = nullptr;
+        FR_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+        rc = enqueue_step(p);
+        cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
+        p->graph_launches = p->launches - before;
+        p->launches = before;
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            p->parity = parity0;
+            return rc;
+        }
+        if (ce != cudaSuccess) {
+            p->parity = parity0;
+            return fr_cuda_fail(ce, "cudaStreamEndCapture");
+        }
+        ce = cudaGraphInstantiate(&p->gexec[gi], g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+            p->parity = parity0;
+            return fr_cuda_fail(ce, "cudaGraphInstantiate");
+        }
+    }
+    p->parity = parity0;
+    p->graph_ind = p->indicator;
+    return FRGPU_OK;
+}
+
+extern "C" {
+
+FRGPU_API int frgpu_problem_create(const frgpu_space *s, const frgpu_problem_desc *d, frgpu_problem **out) {
+    FR_REQ(out, "problem_create: null output");
+    *out = nullptr;
+    FR_REQ(s && d, "problem_create: null space or description");
+    FR_REQ(d->precision == FRGPU_FP64 || d->precision == FRGPU_FP32K, "problem_create: unknown precision");
+    const int eq = d->equation;
+    FR_REQ(eq >= FRGPU_ADVECTION && eq <= FRGPU_BGK1D, "problem_create: unknown equation");
+    FR_REQ((eq == FRGPU_EULER2D) == (s->dim == 2), "problem_create: equation and space dimension disagree");
+    FR_REQ(s->np >= 2 && s->np <= 6, "problem_create: polynomial degree must be 1..5");
+    if (eq == FRGPU_EULER1D || eq == FRGPU_EULER2D) FR_REQ(d->gamma > 1.0, "problem_create: need gamma > 1");
+    if (eq == FRGPU_BGK1D)
+        FR_REQ(d->nvel >= 1 && d->velo && d->weights && d->tau > 0, "problem_create: BGK needs nvel, velo, weights, tau");
+    if (eq == FRGPU_EULER2D) {
+        for (int side = 0; side < 4; ++side)
+            FR_REQ(d->bc[side] == FRGPU_BC_PERIODIC || d->bc[side] == FRGPU_BC_COPY || d->bc[side] == FRGPU_BC_FIXED,
+                   "problem_create: 2D boundaries are periodic, copy or fixed");
+        FR_REQ((d->bc[0] == FRGPU_BC_PERIODIC) == (d->bc[1] == FRGPU_BC_PERIODIC) &&
+                   (d->bc[2] == FRGPU_BC_PERIODIC) == (d->bc[3] == FRGPU_BC_PERIODIC),
+               "problem_create: periodic boundaries come in pairs");
+    } else if (eq == FRGPU_BGK1D) {
+        FR_REQ(d->bc[0] == FRGPU_BC_PERIODIC, "problem_create: BGK supports periodic boundaries");
+    } else {
+        FR_REQ(d->bc[0] == FRGPU_BC_PERIODIC || d->bc[0] == FRGPU_BC_DIRICHLET,
+               "problem_create: 1D boundaries are periodic or dirichlet");
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        fr_set_error("problem_create: no CUDA device");
+        return FRGPU_ERR_CUDA;
+    }
+    FR_TRY
+    auto *p = new frgpu_problem();
+    p->sp = *s;
+    p->d = *d;
+    cudaGetDevice(&p->device);
+    p->esize = d->precision == FRGPU_FP64 ? 8 : 4;
+    const long np = s->np;
+    switch (eq) {
+    case FRGPU_ADVECTION:
+    case FRGPU_BURGERS: p->ndof = (long)s->nx * np; break;
+    case FRGPU_EULER1D: p->ndof = (long)s->nx * np * 3; break;
+    case FRGPU_EULER2D: p->ndof = (long)s->nx * s->ny * np * np * 4; break;
+    case FRGPU_BGK1D: p->ndof = (long)s->nx * d->nvel * np; break;
+    }
+    if (eq == FRGPU_BGK1D) {
+        p->velo.assign(d->velo, d->velo + d->nvel);
+        p->weights.assign(d->weights, d->weights + d->nvel);
+        p->d.velo = nullptr;
+        p->d.weights = nullptr;
+    }
+    int rc = FRGPU_OK;
+    auto fail = [&](int code) {
+        free_problem(p);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        fr_set_error("problem_create: cudaStreamCreate failed");
+        return fail(FRGPU_ERR_CUDA);
+    }
+    const size_t bytes = (size_t)p->ndof * p->esize;
+    if ((rc = [&]() -> int {
+            FR_CUDA(cudaMalloc(&p->s0, bytes));
+            FR_CUDA(cudaMalloc(&p->s1, bytes));
+            FR_CUDA(cudaMalloc(&p->s2, bytes));
+            FR_CUDA(cudaMemset(p->s0, 0, bytes));
+            FR_CUDA(cudaMemset(p->s1, 0, bytes));
+            FR_CUDA(cudaMemset(p->s2, 0, bytes));
+            if (p->d.precision == FRGPU_FP32K) {
+                FR_CUDA(cudaMalloc(&p->s3, bytes));
+                FR_CUDA(cudaMemset(p->s3, 0, bytes));
+            }
+            FR_CUDA(cudaMalloc(&p->d_dt, sizeof(double)));
+            FR_CUDA(cudaMemset(p->d_dt, 0, sizeof(double)));
+            FR_CUDA(cudaMalloc(&p->d_status, sizeof(int)));
+            FR_CUDA(cudaMemset(p->d_status, 0, sizeof(int)));
+            FR_CUDA(cudaMalloc(&p->d_red, sizeof(double) * FR_RED_SIZE));
+            FR_CUDA(cudaMemset(p->d_red, 0, sizeof(double) * FR_RED_SIZE));
+            const size_t ne = (size_t)s->nx * s->ny;
+            FR_CUDA(cudaMalloc(&p->d_flags, sizeof(int) * ne));
+            FR_CUDA(cudaMemset(p->d_flags, 0, sizeof(int) * ne));
+            FR_CUDA(cudaMalloc(&p->d_count, sizeof(int)));
+            FR_CUDA(cudaMemset(p->d_count, 0, sizeof(int)));
+            if (!s->wp.empty())
+                FR_CUDA(cudaMemcpy(p->d_red + FR_RED_WP, s->wp.data(), sizeof(double) * s->wp.size(),
+                                   cudaMemcpyHostToDevice));
+            int r2;
+            if (s->dim == 1) {
+                std::vector<double> J = s->J;
+                if (J.empty()) J.assign(s->nx, 0.5 * s->dx);
+                if ((r2 = upload_vec(p, &p->d_J, J))) return r2;
+            }
+            if (!s->V.empty() && (r2 = upload_vec(p, &p->d_V, s->V))) return r2;
+            if (!s->iV.empty() && (r2 = upload_vec(p, &p->d_iV, s->iV))) return r2;
+            if (eq == FRGPU_BGK1D) {
+                if ((r2 = upload_vec(p, &p->d_velo, p->velo))) return r2;
+                if ((r2 = upload_vec(p, &p->d_w, p->weights))) return r2;
+            }
+            return FRGPU_OK;
+        }()))
+        return fail(rc);
+    *out = p;
+    return FRGPU_OK;
+    FR_CATCH
+}
+
+FRGPU_API void frgpu_problem_destroy(frgpu_problem *p) { free_problem(p); }
+
+FRGPU_API long frgpu_problem_ndof(const frgpu_problem *p) { return p ? p->ndof : -1; }
+
+// Host (Julia layout, FP64) <-> device layout/precision.
+static void to_device_order(const frgpu_problem *p, const double *u, std::vector<double> &dst) {
+    dst.resize(p->ndof);
+    if (p->d.equation != FRGPU_BGK1D) {
+        std::memcpy(dst.data(), u, sizeof(double) * p->ndof);
+        return;
+    }
+    const long ne = p->sp.nx, nv = p->d.nvel, np = p->sp.np;
+    for (long k = 0; k < np; ++k)
+        for (long v = 0; v < nv; ++v)
+            for (long i = 0; i < ne; ++i) dst[(i * np + k) * nv + v] = u[i + ne * (v + nv * k)];
+}
+
+static void to_host_order(const frgpu_problem *p, const std::vector<double> &src, double *u) {
+    if (p->d.equation != FRGPU_BGK1D) {
+        std::memcpy(u, src.data(), sizeof(double) * p->ndof);
+        return;
+    }
+    const long ne = p->sp.nx, nv = p->d.nvel, np = p->sp.np;
+    for (long k = 0; k < np; ++k)
+        for (long v = 0; v < nv; ++v)
+            for (long i = 0; i < ne; ++i) u[i + ne * (v + nv * k)] = src[(i * np + k) * nv + v];
+}
+
+static int put_state(frgpu_problem *p, const double *u, void *hi, void *lo) {
+    std::vector<double> tmp;
+    to_device_order(p, u, tmp);
+    for (long q = 0; q < p->ndof; ++q)
+        if (!std::isfinite(tmp[q])) {
+            fr_set_error("state upload: non-finite value at index " + std::to_string(q));
+            return FRGPU_ERR_NONFINITE;
+        }
+    if (p->esize == 8) {
+        FR_CUDA(cudaMemcpy(hi, tmp.data(), sizeof(double) * p->ndof, cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> h(p->ndof), l(p->ndof);
+        for (long q = 0; q < p->ndof; ++q) {
+            h[q] = (float)tmp[q];
+            l[q] = (float)(tmp[q] - (double)h[q]);
+        }
+        FR_CUDA(cudaMemcpy(hi, h.data(), sizeof(float) * p->ndof, cudaMemcpyHostToDevice));
+        if (lo) FR_CUDA(cudaMemcpy(lo, l.data(), sizeof(float) * p->ndof, cudaMemcpyHostToDevice));
+    }
+    return FRGPU_OK;
+}
+
+static int get_state(frgpu_problem *p, const void *hi, const void *lo, double *u) {
+    std::vector<double> tmp(p->ndof);
+    FR_CUDA(cudaStreamSynchronize(p->stream));
+    if (p->esize == 8) {
+        FR_CUDA(cudaMemcpy(tmp.data(), hi, sizeof(double) * p->ndof, cudaMemcpyDeviceToHost));
+    } else {
+        std::vector<float> h(p->ndof), l(p->ndof, 0.0f);
+        FR_CUDA(cudaMemcpy(h.data(), hi, sizeof(float) * p->ndof, cudaMemcpyDeviceToHost));
+        if (lo) FR_CUDA(cudaMemcpy(l.data(), lo, sizeof(float) * p->ndof, cudaMemcpyDeviceToHost));
+        for (long q = 0; q < p->ndof; ++q) tmp[q] = (double)h[q] + (double)l[q];
+    }
+    to_host_order(p, tmp, u);
+    return FRGPU_OK;
+}
+
+FRGPU_API int frgpu_state_upload(frgpu_problem *p, const double *u) {
+    FR_REQ(p && u, "state_upload: null argument");
+    FR_TRY
+    FR_CUDA(cudaStreamSynchronize(p->stream));
+    p->parity = 0;
+    return put_state(p, u, p->s0, p->s3);
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_state_download(frgpu_problem *p, double *u) {
+    FR_REQ(p && u, "state_download: null argument");
+    FR_TRY
+    return get_state(p, fr_state_hi(p), p->s3, u);
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_rhs(frgpu_problem *p, double *du, const double *u, double t) {
+    (void)t; // the residuals are autonomous
+    FR_REQ(p && du && u, "rhs: null argument");
+    FR_TRY
+    const size_t bytes = (size_t)p->ndof * p->esize;
+    if (!p->rhs_in) {
+        FR_CUDA(cudaMalloc(&p->rhs_in, bytes));
+        FR_CUDA(cudaMalloc(&p->rhs_out, bytes));
+    }
+    int rc = put_state(p, u, p->rhs_in, nullptr);
+    if (rc) return rc;
+    if ((rc = launch_stage(p, 0, p->rhs_in, nullptr, p->rhs_out))) return rc;
+    if ((rc = check_status(p))) return rc;
+    return get_state(p, p->rhs_out, nullptr, du);
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_step_ssprk3(frgpu_problem *p, double dt, int nsteps) {
+    FR_REQ(p, "step_ssprk3: null problem");
+    FR_REQ(nsteps >= 0, "step_ssprk3: negative step count");
+    if (!(dt > 0.0) || !std::isfinite(dt)) {
+        fr_set_error("step_ssprk3: dt must be positive and finite");
+        return FRGPU_ERR_DT;
+    }
+    if (nsteps == 0) return FRGPU_OK;
+    FR_TRY
+    if (dt != p->host_dt) {
+        FR_CUDA(cudaMemcpyAsync(p->d_dt, &dt, sizeof(double), cudaMemcpyHostToDevice, p->stream));
+        FR_CUDA(cudaStreamSynchronize(p->stream));
+        p->host_dt = dt;
+    }
+    if (!p->gexec[0] || p->graph_ind != p->indicator) {
+        int rc = build_graphs(p);
+        if (rc) return rc;
+    }
+    for (int s = 0; s < nsteps; ++s) {
+        const int g = p->d.precision == FRGPU_FP32K ? p->parity : 0;
+        FR_CUDA(cudaGraphLaunch(p->gexec[g], p->stream));
+        if (p->d.precision == FRGPU_FP32K) p->parity ^= 1;
+        p->launches += p->graph_launches;
+    }
+    return check_status(p);
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_reduce(frgpu_problem *p, double *sums, double *maxspeed) {
+    FR_REQ(p, "reduce: null problem");
+    if (p->d.equation != FRGPU_EULER2D) {
+        fr_set_error("reduce: implemented for the 2D Euler problem");
+        return FRGPU_ERR_UNSUPPORTED;
+    }
+    FR_TRY
+    double sp[2];
+    int rc = fr_launch_euler2d_reduce(p, fr_state_hi(p), p->d.precision == FRGPU_FP32K ? p->s3 : nullptr, sums, sp,
+                                      1.0 / p->sp.dx, 1.0 / p->sp.dy);
+    if (rc) return rc;
+    if (maxspeed) *maxspeed = sp[0];
+    return FRGPU_OK;
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_cfl_dt(frgpu_problem *p, double cfl, double *dt) {
+    FR_REQ(p && dt && cfl > 0, "cfl_dt: bad arguments");
+    FR_TRY
+    if (p->d.equation == FRGPU_EULER2D) {
+        double sp[2];
+        int rc = fr_launch_euler2d_reduce(p, fr_state_hi(p), p->d.precision == FRGPU_FP32K ? p->s3 : nullptr,
+                                          nullptr, sp, 1.0 / p->sp.dx, 1.0 / p->sp.dy);
+        if (rc) return rc;
+        if (!(sp[1] > 0) || !std::isfinite(sp[1])) {
+            fr_set_error("cfl_dt: non-positive or non-finite wave speed");
+            return FRGPU_ERR_DT;
+        }
+        *dt = cfl / sp[1];
+        return FRGPU_OK;
+    }
+    if (p->d.equation == FRGPU_ADVECTION) {
+        double dxmin = 1e300;
+        for (int i = 0; i < p->sp.nx; ++i) dxmin = std::min(dxmin, p->sp.J.empty() ? p->sp.dx : 2 * p->sp.J[i]);
+        *dt = cfl * dxmin / std::max(std::fabs(p->d.a), 1e-300);
+        return FRGPU_OK;
+    }
+    if (p->d.equation == FRGPU_BGK1D) {
+        double dxmin = 1e300, vmax = 0;
+        for (int i = 0; i < p->sp.nx; ++i) dxmin = std::min(dxmin, p->sp.J.empty() ? p->sp.dx : 2 * p->sp.J[i]);
+        for (double v : p->velo) vmax = std::max(vmax, std::fabs(v));
+        *dt = cfl * dxmin / vmax;
+        return FRGPU_OK;
+    }
+    fr_set_error("cfl_dt: not available for this equation");
+    return FRGPU_ERR_UNSUPPORTED;
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_set_filter(frgpu_problem *p, int indicator, double lam, double S0, double kappa) {
+    FR_REQ(p, "set_filter: null problem");
+    FR_REQ(indicator >= FRGPU_IND_NONE && indicator <= FRGPU_IND_MLP, "set_filter: unknown indicator");
+    FR_REQ(p->d.equation == FRGPU_EULER2D || p->d.equation == FRGPU_EULER1D || indicator == FRGPU_IND_NONE,
+           "set_filter: the modal filter is available for the Euler problems");
+    p->indicator = indicator;
+    p->lam = lam;
+    p->S0 = S0;
+    p->kappa = kappa;
+    p->graph_ind = -2; // force a re-capture
+    return FRGPU_OK;
+}
+
+FRGPU_API int frgpu_modal_filter(frgpu_problem *p, int indicator, double lam, double S0, double kappa,
+                                 int *ntroubled) {
+    FR_REQ(p, "modal_filter: null problem");
+    FR_REQ(p->d.equation == FRGPU_EULER2D || p->d.equation == FRGPU_EULER1D,
+           "modal_filter: available for the Euler problems");
+    FR_REQ(indicator == FRGPU_IND_PLAIN || indicator == FRGPU_IND_MLP, "modal_filter: unknown indicator");
+    FR_TRY
+    int rc = p->sp.dim == 2 ? fr_launch_filter2d(p, indicator, lam, S0, kappa)
+                            : fr_launch_filter1d(p, indicator, lam, S0, kappa);
+    if (rc) return rc;
+    if (ntroubled) {
+        FR_CUDA(cudaMemcpyAsync(ntroubled, p->d_count, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+    }
+    FR_CUDA(cudaStreamSynchronize(p->stream));
+    return check_status(p);
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_troubled_flags(frgpu_problem *p, int *flags, long n) {
+    FR_REQ(p && flags, "troubled_flags: null argument");
+    const long ne = (long)p->sp.nx * p->sp.ny;
+    FR_REQ(n >= ne, "troubled_flags: output too small");
+    FR_CUDA(cudaStreamSynchronize(p->stream));
+    FR_CUDA(cudaMemcpy(flags, p->d_flags, sizeof(int) * ne, cudaMemcpyDeviceToHost));
+    return FRGPU_OK;
+}
+
+FRGPU_API int frgpu_problem_device_state(frgpu_problem *p, void **dptr, int *elem_bytes) {
+    FR_REQ(p && dptr, "problem_device_state: null argument");
+    *dptr = fr_state_hi(p);
+    if (elem_bytes) *elem_bytes = (int)p->esize;
+    return FRGPU_OK;
+}
+
+FRGPU_API int frgpu_problem_stream(frgpu_problem *p, void **stream) {
+    FR_REQ(p && stream, "problem_stream: null argument");
+    *stream = (void *)p->stream;
+    return FRGPU_OK;
+}
+
+FRGPU_API long frgpu_problem_launches(const frgpu_problem *p) { return p ? p->launches : -1; }
+
+FRGPU_API int frgpu_synchronize(frgpu_problem *p) {
+    FR_REQ(p, "synchronize: null problem");
+    FR_CUDA(cudaStreamSynchronize(p->stream));
+    return FRGPU_OK;
+}
+
+// ------------------------------------------------------------------ stateless operators
+static int stateless_op(const double *f, long n, int np, const double *a, int na, const double *b, int nb,
+                        double *out, int nout, bool derivative) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        fr_set_error("no CUDA device");
+        return FRGPU_ERR_CUDA;
+    }
+    double *d_f = nullptr, *d_a = nullptr, *d_b = nullptr, *d_o = nullptr;
+    cudaStream_t st = nullptr;
+    int rc = [&]() -> int {
+        FR_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        FR_CUDA(cudaMalloc(&d_f, sizeof(double) * n * np));
+        FR_CUDA(cudaMalloc(&d_a, sizeof(double) * na));
+        if (nb) FR_CUDA(cudaMalloc(&d_b, sizeof(double) * nb));
+        FR_CUDA(cudaMalloc(&d_o, sizeof(double) * n * nout));
+        FR_CUDA(cudaMemcpyAsync(d_f, f, sizeof(double) * n * np, cudaMemcpyHostToDevice, st));
+        FR_CUDA(cudaMemcpyAsync(d_a, a, sizeof(double) * na, cudaMemcpyHostToDevice, st));
+        if (nb) FR_CUDA(cudaMemcpyAsync(d_b, b, sizeof(double) * nb, cudaMemcpyHostToDevice, st));
+        int r = derivative ? fr_launch_poly_derivative(d_f, n, np, d_a, d_o, st)
+                           : fr_launch_interp_face(d_f, n, np, d_a, d_b, d_o, st);
+        if (r) return r;
+        FR_CUDA(cudaMemcpyAsync(out, d_o, sizeof(double) * n * nout, cudaMemcpyDeviceToHost, st));
+        FR_CUDA(cudaStreamSynchronize(st));
+        return FRGPU_OK;
+    }();
+    if (d_f) cudaFree(d_f);
+    if (d_a) cudaFree(d_a);
+    if (d_b) cudaFree(d_b);
+    if (d_o) cudaFree(d_o);
+    if (st) cudaStreamDestroy(st);
+    return rc;
+}
+
+FRGPU_API int frgpu_interp_face(const double *f, long n, int np, const double *ll, const double *lr, double *fdelta) {
+    FR_REQ(f && ll && lr && fdelta && n >= 0 && np >= 1, "interp_face: bad arguments");
+    if (n == 0) return FRGPU_OK;
+    return stateless_op(f, n, np, ll, np, lr, np, fdelta, 2, false);
+}
+
+FRGPU_API int frgpu_poly_derivative(const double *f, long n, int np, const double *pdm, double *df) {
+    FR_REQ(f && pdm && df && n >= 0 && np >= 1, "poly_derivative: bad arguments");
+    if (n == 0) return FRGPU_OK;
+    return stateless_op(f, n, np, pdm, np * np, nullptr, 0, df, np, true);
+}
+
+} // extern "C"

@@ -1,0 +1,40 @@
+"""frgpu: GB300-native flux-reconstruction residual and explicit time stepping.
+
+The compute path is libfrgpu.so (hand-written CUDA for sm_103a behind the C ABI
+of include/frgpu.h).  This package is its Python host binding; it mirrors the
+FluxReconstruction.jl interface for the hot path (see ``api``).
+"""
+from ._lib import FRGPUError, lib, last_error  # noqa: F401
+from .api import (  # noqa: F401
+    FRAdvectionProblem,
+    FRBGKProblem,
+    FRBurgersProblem,
+    FREuler2DProblem,
+    FREulerProblem,
+    FRPSpace1D,
+    FRPSpace2D,
+    Integrator,
+    L1_error,
+    L2_error,
+    Linf_error,
+    ODEProblem,
+    SSPRK33,
+    dhuynh,
+    dlagrange,
+    dradau,
+    dsd,
+    gauss_weights,
+    init,
+    interp_face_,
+    lagrange_point,
+    legendre_point,
+    modal_filter_,
+    poly_derivative_,
+    shock_detector,
+    solve,
+    standard_lagrange,
+    step_,
+    vandermonde_matrix,
+)
+
+__all__ = [n for n in dir() if not n.startswith("_")]

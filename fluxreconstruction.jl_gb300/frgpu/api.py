@@ -1,0 +1,466 @@
+"""Python mirror of FluxReconstruction.jl's interface for the residual and
+time-stepping hot path, backed by libfrgpu.so (CUDA, sm_103a).
+
+Names follow the reference (Julia's ``!`` becomes a trailing ``_``):
+
+* ``FRPSpace1D`` / ``FRPSpace2D``           -- src/struct.jl:40-88, :229-245
+* ``interp_face_`` / ``poly_derivative_``    -- src/interpolate.jl:1-10, src/derivative.jl:1-10
+* ``FRAdvectionProblem`` / ``FREulerProblem`` -- src/Equation/eq_advection.jl:1-26, eq_euler.jl:1-27
+* ``FREuler2DProblem`` / ``FRBGKProblem`` / ``FRBurgersProblem`` -- the ``dudt!`` / ``mol!``
+  closures of example/shock-vortex.jl:26-118 and example/bgk_wave.jl:69-129
+* ``init`` / ``step_`` / ``solve`` with ``SSPRK33``  -- OrdinaryDiffEq's integrator API as used
+  by the examples (``init(prob, alg; adaptive=false, dt)``, ``step!(itg)``, ``itg.u``)
+* ``shock_detector`` -- src/dissipation.jl:13-23; ``L1_error``/``L2_error``/``Linf_error`` --
+  src/tools.jl:43-53; ``modal_filter_`` -- the :l2 filter called at example/shock-vortex.jl:316.
+
+Arrays use the reference's index order and Julia's column-major memory order
+(numpy ``order='F'``): ``u[i, k]`` (1D scalar), ``u[i, k, m]`` (1D Euler),
+``u[i, j, k, l, m]`` (2D Euler), ``u[i, v, k]`` (BGK).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import check, dptr
+
+_CORR = {"radau": L.RADAU, "sd": L.SD, "huynh": L.HUYNH}
+_BC = {"period": L.BC_PERIODIC, "periodic": L.BC_PERIODIC, "copy": L.BC_COPY, "extra": L.BC_COPY,
+       "fix": L.BC_FIXED, "fixed": L.BC_FIXED, "dirichlet": L.BC_DIRICHLET}
+_FLUX = {"roe": L.FLUX_ROE, "lf": L.FLUX_LF, "lax": L.FLUX_LF, "hll": L.FLUX_HLL, "upwind": L.FLUX_UPWIND}
+_PREC = {"fp64": L.FP64, "fp32k": L.FP32K, "fp32": L.FP32K}
+_IND = {"none": L.IND_NONE, "plain": L.IND_PLAIN, "mlp": L.IND_MLP}
+
+
+def _f64(a) -> np.ndarray:
+    return np.asfortranarray(np.asarray(a, dtype=np.float64))
+
+
+# ---------------------------------------------------------------- setup math
+def legendre_point(deg: int) -> np.ndarray:
+    """Gauss-Legendre nodes of degree deg (src/Polynomial/poly_legendre.jl:6)."""
+    r = np.zeros(deg + 1)
+    check(L.lib().frgpu_legendre_point(deg, dptr(r), None))
+    return r
+
+
+def gauss_weights(deg: int) -> np.ndarray:
+    r, w = np.zeros(deg + 1), np.zeros(deg + 1)
+    check(L.lib().frgpu_legendre_point(deg, dptr(r), dptr(w)))
+    return w
+
+
+def lagrange_point(sp, x) -> np.ndarray:
+    """lagrange_point (src/Polynomial/poly_lagrange.jl:6-31), scalar or vector x."""
+    sp = _f64(sp).ravel()
+    if np.ndim(x) == 0:
+        out = np.zeros_like(sp)
+        check(L.lib().frgpu_lagrange_point(dptr(sp), len(sp), float(x), dptr(out)))
+        return out
+    return np.stack([lagrange_point(sp, xi) for xi in np.asarray(x, dtype=np.float64)])
+
+
+def dlagrange(sp) -> np.ndarray:
+    """∂lagrange(sp) (src/Polynomial/poly_lagrange.jl:38-59): lpdm[m, k] = l_k'(r_m)."""
+    sp = _f64(sp).ravel()
+    n = len(sp)
+    out = np.zeros((n, n), order="F")
+    check(L.lib().frgpu_dlagrange(dptr(sp), n, dptr(out)))
+    return out
+
+
+def standard_lagrange(x):
+    """standard_lagrange (src/Polynomial/poly_lagrange.jl:99-105) -> (ll, lr, lpdm)."""
+    return lagrange_point(x, -1.0), lagrange_point(x, 1.0), dlagrange(x)
+
+
+def _dcorr(kind: int, deg: int, x):
+    x = _f64(np.atleast_1d(x)).ravel()
+    dgl, dgr = np.zeros_like(x), np.zeros_like(x)
+    check(L.lib().frgpu_dcorrection(kind, deg, dptr(x), len(x), dptr(dgl), dptr(dgr)))
+    return dgl, dgr
+
+
+def dradau(deg: int, x):
+    """∂radau (src/Polynomial/poly_legendre.jl:29-37)."""
+    return _dcorr(L.RADAU, deg, x)
+
+
+def dsd(deg: int, x):
+    """∂sd (src/Polynomial/poly_legendre.jl:44-54)."""
+    return _dcorr(L.SD, deg, x)
+
+
+def dhuynh(deg: int, x):
+    """∂huynh (src/Polynomial/poly_legendre.jl:61-71)."""
+    return _dcorr(L.HUYNH, deg, x)
+
+
+def vandermonde_matrix(deg: int, r, s=None) -> np.ndarray:
+    """vandermonde_matrix(N, r) (transform.jl:18-26) or (Quad, N, r, s) (:55-68)."""
+    r = _f64(r).ravel()
+    if s is None:
+        V = np.zeros((len(r), deg + 1), order="F")
+        check(L.lib().frgpu_vandermonde(deg, dptr(r), len(r), dptr(V)))
+        return V
+    s = _f64(s).ravel()
+    V = np.zeros((len(r), (deg + 1) ** 2), order="F")
+    check(L.lib().frgpu_vandermonde_quad(deg, dptr(r), dptr(s), len(r), dptr(V)))
+    return V
+
+
+# ---------------------------------------------------------------- spaces
+class _Space:
+    _h = None
+
+    def _get(self, name: str, shape) -> np.ndarray:
+        n = int(np.prod(shape))
+        out = np.zeros(n)
+        check(L.lib().frgpu_space_get(self._h, name.encode(), dptr(out), n))
+        return out.reshape(shape, order="F")
+
+    def __del__(self):
+        if self._h is not None and L._lib is not None:
+            L._lib.frgpu_space_destroy(self._h)
+            self._h = None
+
+
+class FRPSpace1D(_Space):
+    """FRPSpace1D(x0, x1, nx, deg, ng=0, correction=:radau) (src/struct.jl:40-85).
+
+    Fields as in the reference: deg, J, np, xpl, xpg, wp, dl, ll, lr, dhl, dhr,
+    V, iV, plus the forwarded mesh fields x0, x1, nx, dx, x.  Ghost layers (ng)
+    are not stored: the problem's boundary kind supplies the neighbours."""
+
+    def __init__(self, x0, x1, nx, deg, ng=0, correction="radau"):
+        h = C.c_void_p()
+        check(L.lib().frgpu_space_create_1d(float(x0), float(x1), int(nx), int(deg), _CORR[correction],
+                                            C.byref(h)))
+        self._h = h
+        self.x0, self.x1, self.nx, self.deg, self.np, self.ng = float(x0), float(x1), int(nx), int(deg), deg + 1, ng
+        n = self.np
+        self.dx = np.full(nx, (x1 - x0) / nx)
+        self.x = x0 + (np.arange(nx) + 0.5) * self.dx
+        self.J = self._get("J", (nx,))
+        self.xpl = self._get("xpl", (n,))
+        self.wp = self._get("wp", (n,))
+        self.xpg = self._get("xpg", (nx, n))
+        self.ll = self._get("ll", (n,))
+        self.lr = self._get("lr", (n,))
+        self.dl = self._get("dl", (n, n))
+        self.dhl = self._get("dhl", (n,))
+        self.dhr = self._get("dhr", (n,))
+        self.V = self._get("V", (n, n))
+        self.iV = self._get("iV", (n, n))
+
+
+class FRPSpace2D(_Space):
+    """FRPSpace2D(x0, x1, nx, y0, y1, ny, deg, ngx=0, ngy=0) (src/struct.jl:229-242)
+    on uniform rectangles.  As in the reference, ``np`` is (deg+1)^2, ``wp`` is
+    the tensor weight matrix, ``dhl``/``dhr`` are the Radau derivatives
+    (src/struct.jl:193) and ``V``/``iV`` the tensor Vandermonde matrices.
+    ``iJ`` is the (constant) inverse Jacobian diag(2/dx, 2/dy)."""
+
+    def __init__(self, x0, x1, nx, y0, y1, ny, deg, ngx=0, ngy=0):
+        h = C.c_void_p()
+        check(L.lib().frgpu_space_create_2d(float(x0), float(x1), int(nx), float(y0), float(y1), int(ny),
+                                            int(deg), C.byref(h)))
+        self._h = h
+        self.x0, self.x1, self.y0, self.y1 = float(x0), float(x1), float(y0), float(y1)
+        self.nx, self.ny, self.deg = int(nx), int(ny), int(deg)
+        n = deg + 1
+        self.np = n * n
+        self.dx = (x1 - x0) / nx
+        self.dy = (y1 - y0) / ny
+        self.iJ = np.array([[1.0 / (0.5 * self.dx), 0.0], [0.0, 1.0 / (0.5 * self.dy)]])
+        self.J = np.array([[0.5 * self.dx, 0.0], [0.0, 0.5 * self.dy]])
+        self.xpl = self._get("xpl", (n,))
+        self.wp = self._get("wp", (n, n))
+        self.xpg = self._get("xpg", (nx, ny, n, n, 2))
+        self.ll = self._get("ll", (n,))
+        self.lr = self._get("lr", (n,))
+        self.dl = self._get("dl", (n, n))
+        self.dhl = self._get("dhl", (n,))
+        self.dhr = self._get("dhr", (n,))
+        self.V = self._get("V", (n * n, n * n))
+        self.iV = self._get("iV", (n * n, n * n))
+        xc = x0 + (np.arange(nx) + 0.5) * self.dx
+        yc = y0 + (np.arange(ny) + 0.5) * self.dy
+        self.x, self.y = np.meshgrid(xc, yc, indexing="ij")
+
+
+# ---------------------------------------------------------------- stateless operators
+def interp_face_(fdelta: np.ndarray, f: np.ndarray, ll, lr) -> None:
+    """interp_face!(fδ, f, ll, lr) (src/interpolate.jl:1-10): fδ[.., 0] = f·ll,
+    fδ[.., 1] = f·lr, row by row for a matrix f, evaluated on the GPU."""
+    f2 = _f64(np.atleast_2d(f))
+    n, npts = f2.shape
+    out = np.zeros((n, 2), order="F")
+    check(L.lib().frgpu_interp_face(dptr(f2), n, npts, dptr(_f64(ll)), dptr(_f64(lr)), dptr(out)))
+    if np.ndim(f) == 1:
+        fdelta[0], fdelta[1] = out[0, 0], out[0, 1]
+    else:
+        fdelta[...] = out
+
+
+def poly_derivative_(df: np.ndarray, f: np.ndarray, pdm) -> None:
+    """poly_derivative!(df, f, pdm) (src/derivative.jl:1-10): df[m] = f·pdm[m, :]
+    (row by row for a matrix f), evaluated on the GPU."""
+    f2 = _f64(np.atleast_2d(f))
+    n, npts = f2.shape
+    if np.shape(pdm) != (npts, npts):
+        raise ValueError("poly_derivative_: pdm must be np x np with np = len(f)")
+    out = np.zeros((n, npts), order="F")
+    check(L.lib().frgpu_poly_derivative(dptr(f2), n, npts, dptr(_f64(pdm)), dptr(out)))
+    if np.ndim(f) == 1:
+        df[...] = out[0]
+    else:
+        df[...] = out
+
+
+def shock_detector(Se: float, deg: int, S0: float | None = None, kappa: float = 4.0) -> bool:
+    """shock_detector(Se, deg, S0 = -3 log10(deg), κ = 4) (src/dissipation.jl:13-23)."""
+    if S0 is None:
+        S0 = -3.0 * math.log10(deg)
+    if Se < S0 - kappa:
+        sigma = 1.0
+    elif S0 - kappa <= Se < S0 + kappa:
+        sigma = 0.5 * (1.0 - math.sin(0.5 * math.pi * (Se - S0) / kappa))
+    else:
+        sigma = 0.0
+    return sigma < 0.99
+
+
+def modal_filter_(uh: np.ndarray, lam: float, filter: str = "l2") -> None:
+    """KitBase modal_filter!(û, λ; filter=:l2) on a flat modal vector, as called at
+    example/shock-vortex.jl:316: û[q] /= 1 + λ q²(q+1)² (q = 0-based mode)."""
+    if filter != "l2":
+        raise NotImplementedError("only the :l2 filter is on the accelerated path")
+    q = np.arange(len(uh), dtype=np.float64)
+    uh /= 1.0 + lam * (q + 1) ** 2 * q ** 2
+
+
+def L1_error(u, ue, dx):
+    """src/tools.jl:43-45"""
+    return float(np.sum(np.abs(np.asarray(u) - np.asarray(ue)) * dx))
+
+
+def L2_error(u, ue, dx):
+    """src/tools.jl:47-49 (Δx inside the square)"""
+    return float(np.sqrt(np.sum((np.abs(np.asarray(u) - np.asarray(ue)) * dx) ** 2)))
+
+
+def Linf_error(u, ue, dx):
+    """src/tools.jl:51-53"""
+    return float(np.max(np.abs(np.asarray(u) - np.asarray(ue)) * dx))
+
+
+# ---------------------------------------------------------------- problems
+class ODEProblem:
+    """The object FRAdvectionProblem / FREulerProblem return (an ODEProblem of
+    rhs!(du, u, p, t) over u0 and tspan); ``p`` is the device-resident problem."""
+
+    def __init__(self, space, desc: L.ProblemDesc, u0, tspan, shape, keep=()):
+        self.space = space
+        self.shape = tuple(shape)
+        self._keep = keep
+        h = C.c_void_p()
+        check(L.lib().frgpu_problem_create(space._h, C.byref(desc), C.byref(h)))
+        self._h = h
+        self.desc = desc
+        self.u0 = _f64(u0)
+        if self.u0.shape != self.shape:
+            raise ValueError(f"u0 has shape {self.u0.shape}, expected {self.shape}")
+        self.tspan = (float(tspan[0]), float(tspan[1]))
+        self.p = self
+
+    @property
+    def ndof(self) -> int:
+        return int(L.lib().frgpu_problem_ndof(self._h))
+
+    def f(self, du: np.ndarray, u: np.ndarray, p=None, t: float = 0.0) -> None:
+        """rhs!(du, u, p, t): residual of host array u into host array du."""
+        uf = _f64(u)
+        if uf.shape != self.shape:
+            raise ValueError(f"u has shape {uf.shape}, expected {self.shape}")
+        out = np.zeros(self.shape, order="F")
+        check(L.lib().frgpu_rhs(self._h, dptr(out), dptr(uf), float(t)))
+        du[...] = out
+
+    def rhs(self, u: np.ndarray, t: float = 0.0) -> np.ndarray:
+        du = np.zeros(self.shape, order="F")
+        self.f(du, u, self, t)
+        return du
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and L._lib is not None:
+            L._lib.frgpu_problem_destroy(self._h)
+            self._h = None
+
+
+def _desc(equation, flux=L.FLUX_ROE, precision="fp64", bcs=(L.BC_PERIODIC,) * 4, a=1.0, gamma=1.4, tau=1.0,
+          fixed_states=None, eps_interior=1e-8, eps_periodic=1e-6):
+    d = L.ProblemDesc()
+    d.equation, d.flux, d.precision = equation, flux, _PREC[precision]
+    for s in range(4):
+        d.bc[s] = bcs[s]
+    if fixed_states is not None:
+        for s in range(4):
+            if fixed_states[s] is not None:
+                for m in range(len(fixed_states[s])):
+                    d.fixed_state[s][m] = float(fixed_states[s][m])
+    d.a, d.gamma, d.tau = float(a), float(gamma), float(tau)
+    d.eps_interior, d.eps_periodic = eps_interior, eps_periodic
+    return d
+
+
+def FRAdvectionProblem(u, tspan, ps: FRPSpace1D, a, bc="period", precision="fp64") -> ODEProblem:
+    """FRAdvectionProblem(u, tspan, ps, a, bc) (src/Equation/eq_advection.jl:1-26)."""
+    d = _desc(L.ADVECTION, precision=precision, bcs=(_BC[str(bc)],) * 4, a=a)
+    return ODEProblem(ps, d, u, tspan, (ps.nx, ps.np))
+
+
+def FRBurgersProblem(u, tspan, ps: FRPSpace1D, bc="period", precision="fp64") -> ODEProblem:
+    """Inviscid Burgers u_t + (u²/2)_x = 0 with the scalar machinery of
+    eq_advection.jl (Roe flux, same epsilons)."""
+    d = _desc(L.BURGERS, precision=precision, bcs=(_BC[str(bc)],) * 4)
+    return ODEProblem(ps, d, u, tspan, (ps.nx, ps.np))
+
+
+def FREulerProblem(u, tspan, ps: FRPSpace1D, gamma, bc="dirichlet", precision="fp64") -> ODEProblem:
+    """FREulerProblem(u, tspan, ps, γ, bc) (src/Equation/eq_euler.jl:1-27), HLL flux."""
+    d = _desc(L.EULER1D, flux=L.FLUX_HLL, precision=precision, bcs=(_BC[str(bc)],) * 4, gamma=gamma)
+    return ODEProblem(ps, d, u, tspan, (ps.nx, ps.np, 3))
+
+
+def FREuler2DProblem(u, tspan, ps: FRPSpace2D, gamma, flux="hll", bc="period", fixed_states=None,
+                     precision="fp64") -> ODEProblem:
+    """The 2D Euler ``dudt!`` closure of example/shock-vortex.jl:26-118 as an
+    ODEProblem.  ``bc`` is one kind for all sides or (left, right, bottom, top);
+    ``fixed_states`` gives the conserved ghost state of each fixed side."""
+    bcs = (bc,) * 4 if isinstance(bc, str) else tuple(bc)
+    d = _desc(L.EULER2D, flux=_FLUX[flux], precision=precision, bcs=tuple(_BC[b] for b in bcs), gamma=gamma,
+              fixed_states=fixed_states)
+    n = ps.deg + 1
+    return ODEProblem(ps, d, u, tspan, (ps.nx, ps.ny, n, n, 4))
+
+
+def FRBGKProblem(u, tspan, ps: FRPSpace1D, velo, weights, tau, precision="fp64") -> ODEProblem:
+    """The 1D1V BGK ``mol!`` closure of example/bgk_wave.jl:69-129 (kinetic
+    upwind flux, Maxwellian relaxation with time tau, periodic)."""
+    velo = np.ascontiguousarray(velo, dtype=np.float64)
+    weights = np.ascontiguousarray(weights, dtype=np.float64)
+    d = _desc(L.BGK1D, flux=L.FLUX_UPWIND, precision=precision, tau=tau)
+    d.nvel = len(velo)
+    d.velo, d.weights = dptr(velo), dptr(weights)
+    return ODEProblem(ps, d, u, tspan, (ps.nx, len(velo), ps.np), keep=(velo, weights))
+
+
+class SSPRK33:
+    """Marker for the three-stage SSP Runge-Kutta method (OrdinaryDiffEq SSPRK33)."""
+
+
+class Integrator:
+    """Device-resident integrator: ``itg.u`` reads the state back, ``step_(itg)``
+    advances one step of ``dt`` on the GPU (OrdinaryDiffEq's init/step! API)."""
+
+    def __init__(self, prob: ODEProblem, dt: float):
+        self.prob = prob
+        self.dt = float(dt)
+        self.t = prob.tspan[0]
+        check(L.lib().frgpu_state_upload(prob._h, dptr(prob.u0)))
+
+    @property
+    def u(self) -> np.ndarray:
+        out = np.zeros(self.prob.shape, order="F")
+        check(L.lib().frgpu_state_download(self.prob._h, dptr(out)))
+        return out
+
+    @u.setter
+    def u(self, value) -> None:
+        v = _f64(value)
+        if v.shape != self.prob.shape:
+            raise ValueError("state shape mismatch")
+        check(L.lib().frgpu_state_upload(self.prob._h, dptr(v)))
+
+    def step(self, n: int = 1, dt: float | None = None) -> None:
+        dt = self.dt if dt is None else float(dt)
+        check(L.lib().frgpu_step_ssprk3(self.prob._h, dt, int(n)))
+        self.t += n * dt
+
+    def set_filter(self, indicator="plain", lam=5e-4, S0=None, kappa=9.0) -> None:
+        """Post-step troubled-cell indicator + :l2 modal filter (shock-vortex.jl:308-321)."""
+        deg = self.prob.space.deg
+        if S0 is None:
+            S0 = -3.0 * math.log10(deg)
+        check(L.lib().frgpu_set_filter(self.prob._h, _IND[indicator], float(lam), float(S0), float(kappa)))
+
+    def modal_filter(self, indicator="plain", lam=5e-4, S0=None, kappa=9.0) -> int:
+        deg = self.prob.space.deg
+        if S0 is None:
+            S0 = -3.0 * math.log10(deg)
+        n = C.c_int(0)
+        check(L.lib().frgpu_modal_filter(self.prob._h, _IND[indicator], float(lam), float(S0), float(kappa),
+                                         C.byref(n)))
+        return n.value
+
+    def troubled(self) -> np.ndarray:
+        sp = self.prob.space
+        ne = sp.nx * getattr(sp, "ny", 1)
+        flags = np.zeros(ne, dtype=np.int32)
+        check(L.lib().frgpu_troubled_flags(self.prob._h, flags.ctypes.data_as(L._I), ne))
+        return flags
+
+    def cfl_dt(self, cfl: float) -> float:
+        dt = C.c_double()
+        check(L.lib().frgpu_cfl_dt(self.prob._h, float(cfl), C.byref(dt)))
+        return dt.value
+
+    def reduce(self):
+        """FP64 conserved sums (per variable) and the maximum wave speed."""
+        sums = np.zeros(4)
+        ms = C.c_double()
+        check(L.lib().frgpu_reduce(self.prob._h, dptr(sums), C.byref(ms)))
+        return sums, ms.value
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        check(L.lib().frgpu_problem_stream(self.prob._h, C.byref(s)))
+        return s.value or 0
+
+    def launches(self) -> int:
+        return int(L.lib().frgpu_problem_launches(self.prob._h))
+
+    def synchronize(self) -> None:
+        check(L.lib().frgpu_synchronize(self.prob._h))
+
+
+def init(prob: ODEProblem, alg=None, *, dt: float, adaptive: bool = False, **kwargs) -> Integrator:
+    """init(prob, SSPRK33(); adaptive=false, dt) (OrdinaryDiffEq)."""
+    if alg is not None and not isinstance(alg, SSPRK33) and alg is not SSPRK33:
+        raise NotImplementedError("the device integrator implements SSPRK33")
+    if adaptive:
+        raise NotImplementedError("fixed time steps only (adaptive=false)")
+    return Integrator(prob, dt)
+
+
+def step_(itg: Integrator, n: int = 1) -> None:
+    """step!(itg)"""
+    itg.step(n)
+
+
+def solve(prob: ODEProblem, alg=None, *, dt: float, adaptive: bool = False, **kwargs) -> np.ndarray:
+    """solve(prob, SSPRK33(); adaptive=false, dt): full steps of dt to tspan[1],
+    the last one shortened to land on it.  Returns the final state."""
+    itg = init(prob, alg, dt=dt, adaptive=adaptive)
+    span = prob.tspan[1] - prob.tspan[0]
+    n = int(math.floor(span / dt + 1e-9))
+    if n:
+        itg.step(n)
+    rest = span - n * dt
+    if rest > 1e-12 * max(1.0, abs(span)):
+        itg.step(1, rest)
+    return itg.u

@@ -1,0 +1,191 @@
+/*
+ * frgpu.h -- C ABI of libfrgpu.so, the GB300 (sm_103a) flux-reconstruction
+ * element-residual and explicit time-stepping library.
+ *
+ * Plain C types only.  Every function returns an int status (FRGPU_OK = 0,
+ * negative on error) and never aborts; frgpu_last_error() returns the message
+ * of the calling thread's last failure.  Host arrays are borrowed for the
+ * duration of a call.  All state arrays use the reference's Julia column-major
+ * layouts, element index fastest:
+ *   1D scalar      u[ne, np]                 (src/Equation/eq_advection.jl)
+ *   1D Euler       u[ne, np, 3]              (src/Equation/eq_euler.jl)
+ *   2D Euler       u[nx, ny, np, np, 4]      (example/shock-vortex.jl:26-118, interior only)
+ *   1D1V BGK       u[ne, nvel, np]           (example/bgk_wave.jl:69-129)
+ * Matrices are column-major.  Each entry point names the reference interface
+ * it replaces (path:line within FluxReconstruction.jl).
+ */
+#ifndef FRGPU_H
+#define FRGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define FRGPU_API __attribute__((visibility("default")))
+#else
+#define FRGPU_API
+#endif
+
+/* ---- status codes ---- */
+#define FRGPU_OK 0
+#define FRGPU_ERR_ARG (-1)         /* bad argument / shape / null handle */
+#define FRGPU_ERR_CUDA (-2)        /* CUDA runtime error or no usable device */
+#define FRGPU_ERR_NONFINITE (-3)   /* NaN/Inf met in the state */
+#define FRGPU_ERR_UNPHYSICAL (-4)  /* non-positive density or pressure */
+#define FRGPU_ERR_DT (-5)          /* non-positive or non-finite time step */
+#define FRGPU_ERR_TIMEOUT (-6)     /* a bounded device-side wait ran out */
+#define FRGPU_ERR_UNSUPPORTED (-7) /* combination not built (e.g. degree) */
+
+/* ---- enumerations ---- */
+enum frgpu_equation {
+    FRGPU_ADVECTION = 0, /* u_t + a u_x = 0         eq_advection.jl          */
+    FRGPU_BURGERS = 1,   /* u_t + (u^2/2)_x = 0     same scalar machinery    */
+    FRGPU_EULER1D = 2,   /* 1D Euler                eq_euler.jl              */
+    FRGPU_EULER2D = 3,   /* 2D Euler                shock-vortex.jl:26-118   */
+    FRGPU_BGK1D = 4      /* 1D1V BGK                bgk_wave.jl:69-129       */
+};
+enum frgpu_flux { FRGPU_FLUX_ROE = 0, FRGPU_FLUX_LF = 1, FRGPU_FLUX_HLL = 2, FRGPU_FLUX_UPWIND = 3 };
+enum frgpu_precision {
+    FRGPU_FP64 = 0, /* plain FP64 residual and stage combination            */
+    FRGPU_FP32K = 1 /* FP32 residual, compensated (Kahan) stage combination  */
+};
+enum frgpu_bc {
+    FRGPU_BC_PERIODIC = 0,  /* period_advection!/period_euler!, periodic ghosts        */
+    FRGPU_BC_COPY = 1,      /* ghost element = copy of the adjacent interior element   */
+    FRGPU_BC_FIXED = 2,     /* ghost element = a fixed conserved state                 */
+    FRGPU_BC_DIRICHLET = 3  /* dirichlet_advection!/dirichlet_euler!: du = 0 at ends   */
+};
+enum frgpu_correction { FRGPU_RADAU = 0, FRGPU_SD = 1, FRGPU_HUYNH = 2 };
+enum frgpu_indicator { FRGPU_IND_NONE = 0, FRGPU_IND_PLAIN = 1, FRGPU_IND_MLP = 2 };
+
+typedef struct frgpu_space frgpu_space;
+typedef struct frgpu_problem frgpu_problem;
+
+/* ======================================================================
+ * Setup math (host).  Used by the space constructors; exported so a caller
+ * can compare against its own FRPSpace fields.
+ * ==================================================================== */
+
+/* legendre_point(p) (src/Polynomial/poly_legendre.jl:6): deg+1 Gauss-Legendre
+ * nodes, ascending, and the matching weights (src/struct.jl:47).  w may be NULL. */
+FRGPU_API int frgpu_legendre_point(int deg, double *r, double *w);
+/* lagrange_point(sp, x) (src/Polynomial/poly_lagrange.jl:6-20) */
+FRGPU_API int frgpu_lagrange_point(const double *sp, int nsp, double x, double *l);
+/* dlagrange(sp) (src/Polynomial/poly_lagrange.jl:38-59): lpdm[m + nsp*k] = l_k'(r_m) */
+FRGPU_API int frgpu_dlagrange(const double *sp, int nsp, double *lpdm);
+/* dradau / dsd / dhuynh (src/Polynomial/poly_legendre.jl:29-71) */
+FRGPU_API int frgpu_dcorrection(int correction, int deg, const double *x, int n, double *dgl, double *dgr);
+/* vandermonde_matrix(N, r) (src/Transform/transform.jl:18-26), V[i + n*j] */
+FRGPU_API int frgpu_vandermonde(int deg, const double *r, int n, double *V);
+/* vandermonde_matrix(Quad, N, r, s) (src/Transform/transform.jl:55-68) */
+FRGPU_API int frgpu_vandermonde_quad(int deg, const double *r, const double *s, int n, double *V);
+
+/* ======================================================================
+ * Spaces (FRPSpace1D / FRPSpace2D)
+ * ==================================================================== */
+
+/* FRPSpace1D(x0, x1, nx, deg, ng=0, correction) (src/struct.jl:40-85) */
+FRGPU_API int frgpu_space_create_1d(double x0, double x1, int nx, int deg, int correction, frgpu_space **out);
+/* FRPSpace2D(x0, x1, nx, y0, y1, ny, deg) (src/struct.jl:229-242), uniform
+ * rectangles, dhl/dhr = dradau as at src/struct.jl:193 */
+FRGPU_API int frgpu_space_create_2d(double x0, double x1, int nx, double y0, double y1, int ny, int deg,
+                                    frgpu_space **out);
+/* Adopt operators built by the caller (e.g. the reference's own FRPSpace1D
+ * fields ps.J, ps.ll, ps.lr, ps.dl, ps.dhl, ps.dhr, ps.V, ps.iV; V/iV may be NULL). */
+FRGPU_API int frgpu_space_create_1d_ops(int nx, int deg, const double *J, const double *ll, const double *lr,
+                                        const double *dl, const double *dhl, const double *dhr, const double *V,
+                                        const double *iV, frgpu_space **out);
+/* Same for FRPSpace2D on uniform rectangles of size dx x dy (iJ = diag(2/dx, 2/dy)). */
+FRGPU_API int frgpu_space_create_2d_ops(int nx, int ny, int deg, double dx, double dy, const double *ll,
+                                        const double *lr, const double *dl, const double *dhl, const double *dhr,
+                                        const double *V, const double *iV, frgpu_space **out);
+/* Query: dim, nx, ny (1 in 1D), deg. */
+FRGPU_API int frgpu_space_info(const frgpu_space *s, int *dim, int *nx, int *ny, int *deg);
+/* Copy a named field out: "xpl","wp","ll","lr","dl","dhl","dhr","V","iV","J","xpg".
+ * n = capacity in doubles; returns the number of doubles written (>0) or an error. */
+FRGPU_API int frgpu_space_get(const frgpu_space *s, const char *name, double *out, long n);
+FRGPU_API void frgpu_space_destroy(frgpu_space *s);
+
+/* ======================================================================
+ * Problems: device-resident state + residual + SSPRK3 stepping
+ * ==================================================================== */
+typedef struct {
+    int equation;           /* frgpu_equation */
+    int flux;               /* frgpu_flux */
+    int precision;          /* frgpu_precision */
+    int bc[4];              /* 1D: bc[0] (both ends); 2D: left, right, bottom, top */
+    double fixed_state[4][4]; /* per side, conserved ghost state for FRGPU_BC_FIXED */
+    double a;               /* advection speed (FRGPU_ADVECTION) */
+    double gamma;           /* ratio of specific heats (Euler) */
+    double tau;             /* BGK relaxation time */
+    int nvel;               /* BGK velocity points */
+    const double *velo;     /* BGK velocity nodes [nvel] */
+    const double *weights;  /* BGK quadrature weights [nvel] */
+    double eps_interior;    /* scalar Roe epsilon, eq_advection.jl:130 (1e-8) */
+    double eps_periodic;    /* scalar Roe epsilon at the periodic face, :163 (1e-6) */
+} frgpu_problem_desc;
+
+/* FRAdvectionProblem (eq_advection.jl:1-26) / FREulerProblem (eq_euler.jl:1-27)
+ * / the ODEProblem(dudt!, ...) closures of the 2D and BGK examples: binds a
+ * space and a physics description, allocates the device state. */
+FRGPU_API int frgpu_problem_create(const frgpu_space *s, const frgpu_problem_desc *d, frgpu_problem **out);
+FRGPU_API void frgpu_problem_destroy(frgpu_problem *p);
+/* number of DOFs (doubles in one state array at the boundary) */
+FRGPU_API long frgpu_problem_ndof(const frgpu_problem *p);
+/* itg.u <- host u (FP64, Julia layout) / host u <- itg.u */
+FRGPU_API int frgpu_state_upload(frgpu_problem *p, const double *u);
+FRGPU_API int frgpu_state_download(frgpu_problem *p, double *u);
+/* rhs!(du, u, p, t): frode_advection! (eq_advection.jl:55-77), frode_euler!
+ * (eq_euler.jl:29-73), dudt! (shock-vortex.jl:26-118), mol! (bgk_wave.jl:69-129).
+ * Host arrays in, host array out (one H2D and one D2H copy per call). */
+FRGPU_API int frgpu_rhs(frgpu_problem *p, double *du, const double *u, double t);
+/* nsteps of step!(itg) with SSPRK33 at fixed dt on the device-resident state
+ * (OrdinaryDiffEq init(prob, SSPRK33(); adaptive=false, dt) + step!).  Steps
+ * are replayed from a captured CUDA graph; the post-step filter configured by
+ * frgpu_set_filter runs after every step. */
+FRGPU_API int frgpu_step_ssprk3(frgpu_problem *p, double dt, int nsteps);
+/* dt = cfl / max over points of sum_d (|u_d| + c)/dx_d (FP64 max-reduction on the GPU) */
+FRGPU_API int frgpu_cfl_dt(frgpu_problem *p, double cfl, double *dt);
+/* FP64 conserved sums (quadrature-weighted, per variable) and max wave speed */
+FRGPU_API int frgpu_reduce(frgpu_problem *p, double *sums, double *maxspeed);
+/* Post-step troubled-cell indicator + :l2 modal filter, example/shock-vortex.jl:308-321
+ * (2D, detection on density, S0/kappa as given) and example/euler_highlevel.jl:37-52 (1D).
+ * indicator = FRGPU_IND_NONE disables it. */
+FRGPU_API int frgpu_set_filter(frgpu_problem *p, int indicator, double lam, double S0, double kappa);
+/* Apply the indicator + filter once now; *ntroubled receives the troubled-element count. */
+FRGPU_API int frgpu_modal_filter(frgpu_problem *p, int indicator, double lam, double S0, double kappa,
+                                 int *ntroubled);
+/* Per-element troubled flags of the last filter application (ne ints). */
+FRGPU_API int frgpu_troubled_flags(frgpu_problem *p, int *flags, long n);
+/* Device pointer to the primary state array and its element type size
+ * (8 for FP64, 4 for FP32K), for zero-copy hand-off; the stream the problem's
+ * kernels run on; the number of this library's kernel launches so far. */
+FRGPU_API int frgpu_problem_device_state(frgpu_problem *p, void **dptr, int *elem_bytes);
+FRGPU_API int frgpu_problem_stream(frgpu_problem *p, void **stream);
+FRGPU_API long frgpu_problem_launches(const frgpu_problem *p);
+FRGPU_API int frgpu_synchronize(frgpu_problem *p);
+
+/* ======================================================================
+ * Stateless operators
+ * ==================================================================== */
+
+/* interp_face!(fdelta, f, ll, lr) for a matrix f[n, np]
+ * (src/interpolate.jl:6-10): fdelta[i, 1] = f[i,:].ll, fdelta[i, 2] = f[i,:].lr.
+ * Host arrays (column-major), computed on the GPU. */
+FRGPU_API int frgpu_interp_face(const double *f, long n, int np, const double *ll, const double *lr,
+                                double *fdelta);
+/* poly_derivative!(df, f, pdm) row-wise for a matrix f[n, np]
+ * (src/derivative.jl:1-10): df[i, m] = sum_k f[i, k] pdm[m, k]. */
+FRGPU_API int frgpu_poly_derivative(const double *f, long n, int np, const double *pdm, double *df);
+
+/* ======================================================================
+ * Diagnostics
+ * ==================================================================== */
+FRGPU_API int frgpu_last_error(char *buf, unsigned long n);
+FRGPU_API int frgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1109 @@
+/*
+ * fr_oracle.c -- CPU FP64 restatement of FluxReconstruction.jl's hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker and the timed CPU baseline).  See
+ * fr_oracle.h for the layout conventions and the parity status.  Every
+ * function cites the reference file:line it restates.  Compiled with
+ * -ffp-contract=off so that each operation rounds like the reference's Julia
+ * code (Julia does not fuse multiply-adds unless asked to).
+ */
+#include "fr_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+static int g_threads = 0;
+void fro_set_threads(int n) { g_threads = n; }
+int fro_get_threads(void) {
+#ifdef _OPENMP
+    return g_threads > 0 ? g_threads : omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+#ifdef _OPENMP
+#define OMP_THREADS num_threads(fro_get_threads())
+#endif
+
+/* ------------------------------------------------------------------------
+ * Setup math
+ * ---------------------------------------------------------------------- */
+
+/* Legendre polynomial P_n(x) by the three-term recurrence. */
+double fro_legendre_p(int n, double x) {
+    if (n == 0) return 1.0;
+    double p0 = 1.0, p1 = x;
+    for (int k = 1; k < n; ++k) {
+        double p2 = ((2.0 * k + 1.0) * x * p1 - k * p0) / (k + 1.0);
+        p0 = p1;
+        p1 = p2;
+    }
+    return p1;
+}
+
+/* P_n'(x): replaces GSL sf_legendre_Pl_deriv_array used by
+ * src/Polynomial/poly_legendre.jl:13 (last element of the derivative array).
+ * Recurrence P'_n = P'_{n-2} + (2n-1) P_{n-1}, exact at x = +-1. */
+double fro_dlegendre(int n, double x) {
+    if (n <= 0) return 0.0;
+    double dm2 = 0.0, dm1 = 1.0; /* P'_0, P'_1 */
+    if (n == 1) return 1.0;
+    for (int k = 2; k <= n; ++k) {
+        double d = dm2 + (2.0 * k - 1.0) * fro_legendre_p(k - 1, x);
+        dm2 = dm1;
+        dm1 = d;
+    }
+    return dm1;
+}
+
+/* Gauss-Legendre nodes (ascending) and weights: the values of
+ * FastGaussQuadrature.gausslegendre used at src/Polynomial/poly_legendre.jl:6
+ * and src/struct.jl:47.  Newton iteration on P_n from the Chebyshev-like
+ * initial guess; weights 2/((1-x^2) P_n'(x)^2). */
+void fro_gauss_legendre(int n, double *x, double *w) {
+    for (int i = 0; i < n; ++i) {
+        double z = cos(M_PI * (i + 0.75) / (n + 0.5));
+        for (int it = 0; it < 100; ++it) {
+            double p = fro_legendre_p(n, z);
+            double dp = fro_dlegendre(n, z);
+            double dz = p / dp;
+            z -= dz;
+            if (fabs(dz) < 1e-16) break;
+        }
+        double dp = fro_dlegendre(n, z);
+        /* ascending order: the guess above is descending */
+        x[n - 1 - i] = z;
+        w[n - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+    }
+    /* symmetrise to remove the last ulp of asymmetry */
+    for (int i = 0; i < n / 2; ++i) {
+        double a = 0.5 * (x[n - 1 - i] - x[i]);
+        x[i] = -a;
+        x[n - 1 - i] = a;
+        double b = 0.5 * (w[i] + w[n - 1 - i]);
+        w[i] = b;
+        w[n - 1 - i] = b;
+    }
+    if (n % 2 == 1) x[n / 2] = 0.0;
+}
+
+/* Correction-function derivatives, src/Polynomial/poly_legendre.jl:29-71:
+ * kind 0 = dradau (:29-37), 1 = dsd (:44-54), 2 = dhuynh (:61-71). */
+void fro_dcorrection(int kind, int p, const double *x, int nx, double *dgl, double *dgr) {
+    double sgn = (p % 2 == 0) ? 1.0 : -1.0; /* (-1.0)^p */
+    for (int i = 0; i < nx; ++i) {
+        double d = fro_dlegendre(p, x[i]);
+        double dp = fro_dlegendre(p + 1, x[i]);
+        double y;
+        if (kind == 0) {
+            y = dp;
+        } else {
+            double dm = fro_dlegendre(p - 1, x[i]);
+            if (kind == 1)
+                y = (p * dm + (p + 1) * dp) / (2 * p + 1);
+            else
+                y = ((p + 1) * dm + p * dp) / (2 * p + 1);
+        }
+        dgl[i] = sgn * 0.5 * (d - y);
+        dgr[i] = 0.5 * (d + y);
+    }
+}
+
+/* lagrange_point, src/Polynomial/poly_lagrange.jl:6-20 */
+void fro_lagrange_point(const double *sp, int nsp, double x, double *l) {
+    for (int k = 0; k < nsp; ++k) {
+        double tmp = 1.0;
+        for (int j = 0; j < nsp; ++j)
+            if (j != k) tmp *= (x - sp[j]) / (sp[k] - sp[j]);
+        l[k] = tmp;
+    }
+}
+
+/* dlagrange (nodal differentiation matrix lpdm[m,k] = l_k'(r_m)),
+ * src/Polynomial/poly_lagrange.jl:38-59; column-major lpdm[m + nsp*k]. */
+void fro_dlagrange(const double *sp, int nsp, double *lpdm) {
+    for (int k = 0; k < nsp; ++k)
+        for (int m = 0; m < nsp; ++m) {
+            double lsum = 0.0;
+            for (int l = 0; l < nsp; ++l) {
+                double tmp = 1.0;
+                for (int j = 0; j < nsp; ++j)
+                    if (j != k && j != l) tmp *= (sp[m] - sp[j]) / (sp[k] - sp[j]);
+                if (l != k) lsum += tmp / (sp[k] - sp[l]);
+            }
+            lpdm[m + nsp * k] = lsum;
+        }
+}
+
+/* Orthonormal Jacobi polynomial, src/Polynomial/poly_jacobi.jl:7-42 */
+double fro_jacobi_p(double x, double alpha, double beta, int N) {
+    double gamma0 = pow(2.0, alpha + beta + 1) / (alpha + beta + 1) * tgamma(alpha + 1) *
+                    tgamma(beta + 1) / tgamma(alpha + beta + 1);
+    double p0 = 1.0 / sqrt(gamma0);
+    if (N == 0) return p0;
+    double gamma1 = (alpha + 1) * (beta + 1) / (alpha + beta + 3) * gamma0;
+    double p1 = ((alpha + beta + 2) * x / 2 + (alpha - beta) / 2) / sqrt(gamma1);
+    if (N == 1) return p1;
+    double aold = 2 / (2 + alpha + beta) * sqrt((alpha + 1) * (beta + 1) / (alpha + beta + 3));
+    for (int i = 1; i <= N - 1; ++i) {
+        double h1 = 2 * i + alpha + beta;
+        double anew = 2 / (h1 + 2) *
+                      sqrt((i + 1) * (i + 1 + alpha + beta) * (i + 1 + alpha) * (i + 1 + beta) /
+                           (h1 + 1) / (h1 + 3));
+        double bnew = -(alpha * alpha - beta * beta) / h1 / (h1 + 2);
+        double p2 = 1 / anew * (-aold * p0 + (x - bnew) * p1);
+        aold = anew;
+        p0 = p1;
+        p1 = p2;
+    }
+    return p1;
+}
+
+/* dJacobiP, src/Polynomial/poly_jacobi.jl:88-95 */
+double fro_djacobi_p(double x, double alpha, double beta, int N) {
+    if (N == 0) return 0.0;
+    return sqrt(N * (N + alpha + beta + 1)) * fro_jacobi_p(x, alpha + 1, beta + 1, N - 1);
+}
+
+/* vandermonde_matrix(N, r), src/Transform/transform.jl:18-26; V[i + nr*j] */
+void fro_vandermonde_1d(int N, const double *r, int nr, double *V) {
+    for (int j = 0; j <= N; ++j)
+        for (int i = 0; i < nr; ++i) V[i + nr * j] = fro_jacobi_p(r[i], 0, 0, j);
+}
+
+/* dvandermonde_matrix(N, r), src/Transform/transform.jl:76-84 */
+void fro_dvandermonde_1d(int N, const double *r, int nr, double *Vr) {
+    for (int j = 0; j <= N; ++j)
+        for (int i = 0; i < nr; ++i) Vr[i + nr * j] = fro_djacobi_p(r[i], 0, 0, j);
+}
+
+/* vandermonde_matrix(Quad, N, r, s), src/Transform/transform.jl:55-68:
+ * mode sk runs over i (outer) and j (inner); V[pt + n*sk]. */
+void fro_vandermonde_quad(int N, const double *r, const double *s, int n, double *V) {
+    int sk = 0;
+    for (int i = 0; i <= N; ++i)
+        for (int j = 0; j <= N; ++j) {
+            for (int q = 0; q < n; ++q)
+                V[q + n * sk] = fro_jacobi_p(r[q], 0, 0, i) * fro_jacobi_p(s[q], 0, 0, j);
+            ++sk;
+        }
+}
+
+/* Gauss-Jordan inverse with partial pivoting (stands in for Julia's inv). */
+int fro_inverse(int n, const double *A, double *Ainv) {
+    double *M = (double *)malloc(sizeof(double) * n * 2 * n);
+    if (!M) return -1;
+    for (int r = 0; r < n; ++r)
+        for (int c = 0; c < 2 * n; ++c)
+            M[r * 2 * n + c] = c < n ? A[r + n * c] : (c - n == r ? 1.0 : 0.0);
+    for (int c = 0; c < n; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < n; ++r)
+            if (fabs(M[r * 2 * n + c]) > fabs(M[piv * 2 * n + c])) piv = r;
+        if (M[piv * 2 * n + c] == 0.0) {
+            free(M);
+            return -2;
+        }
+        if (piv != c)
+            for (int k = 0; k < 2 * n; ++k) {
+                double t = M[c * 2 * n + k];
+                M[c * 2 * n + k] = M[piv * 2 * n + k];
+                M[piv * 2 * n + k] = t;
+            }
+        double d = M[c * 2 * n + c];
+        for (int k = 0; k < 2 * n; ++k) M[c * 2 * n + k] /= d;
+        for (int r = 0; r < n; ++r)
+            if (r != c) {
+                double f = M[r * 2 * n + c];
+                if (f != 0.0)
+                    for (int k = 0; k < 2 * n; ++k) M[r * 2 * n + k] -= f * M[c * 2 * n + k];
+            }
+    }
+    for (int r = 0; r < n; ++r)
+        for (int c = 0; c < n; ++c) Ainv[r + n * c] = M[r * 2 * n + n + c];
+    free(M);
+    return 0;
+}
+
+/* shock_detector, src/dissipation.jl:13-23 */
+int fro_shock_detector(double Se, int deg, double S0, double kappa) {
+    (void)deg;
+    double sigma;
+    if (Se < S0 - kappa)
+        sigma = 1.0;
+    else if (S0 - kappa <= Se && Se < S0 + kappa)
+        sigma = 0.5 * (1.0 - sin(0.5 * M_PI * (Se - S0) / kappa));
+    else
+        sigma = 0.0;
+    return sigma < 0.99 ? 1 : 0;
+}
+
+/* ------------------------------------------------------------------------
+ * Physics helpers (KitBase 0.9 restatements; the package is not vendored)
+ * ---------------------------------------------------------------------- */
+
+/* prim = [rho, U, V, lambda], lambda = rho / (2 p) (KitBase convention) */
+void fro_prim_conserve2d(const double *prim, double gamma, double *w) {
+    w[0] = prim[0];
+    w[1] = prim[0] * prim[1];
+    w[2] = prim[0] * prim[2];
+    w[3] = 0.5 * prim[0] / prim[3] / (gamma - 1.0) + 0.5 * prim[0] * (prim[1] * prim[1] + prim[2] * prim[2]);
+}
+
+void fro_conserve_prim2d(const double *w, double gamma, double *prim) {
+    prim[0] = w[0];
+    prim[1] = w[1] / w[0];
+    prim[2] = w[2] / w[0];
+    prim[3] = 0.5 * w[0] / (gamma - 1.0) / (w[3] - 0.5 * (w[1] * w[1] + w[2] * w[2]) / w[0]);
+}
+
+void fro_prim_conserve1d(const double *prim, double gamma, double *w) {
+    w[0] = prim[0];
+    w[1] = prim[0] * prim[1];
+    w[2] = 0.5 * prim[0] / prim[2] / (gamma - 1.0) + 0.5 * prim[0] * prim[1] * prim[1];
+}
+
+/* Physical Euler flux in direction dir (0 = x, 1 = y) of the conserved state
+ * w, with velocity components and pressure computed once:
+ * U = mx/rho, V = my/rho, p = (gamma-1)(E - 0.5 (mx U + my V)). */
+static inline void euler_flux_dir(const double *w, double gamma, int dir, double *f, double *un_out,
+                                  double *p_out) {
+    double rinv = 1.0 / w[0];
+    double U = w[1] * rinv, V = w[2] * rinv;
+    double p = (gamma - 1.0) * (w[3] - 0.5 * (w[1] * U + w[2] * V));
+    double un = dir == 0 ? U : V;
+    f[0] = w[1 + dir];
+    f[1] = w[1] * un + (dir == 0 ? p : 0.0);
+    f[2] = w[2] * un + (dir == 1 ? p : 0.0);
+    f[3] = (w[3] + p) * un;
+    if (un_out) *un_out = un;
+    if (p_out) *p_out = p;
+}
+
+/* HLL flux with Davis wave-speed estimates (Toro, "Riemann Solvers and
+ * Numerical Methods for Fluid Dynamics", ch. 10), in direction dir.  Stands
+ * in for KitBase.flux_hll!(fw, wL, wR, gamma, 1.0) called at
+ * example/shock-vortex.jl:78 (x faces) and :84-87 (y faces through
+ * local_frame/global_frame, which this directional form equals exactly). */
+void fro_flux_hll2d(const double *wL, const double *wR, double gamma, int dir, double *fw) {
+    double fL[4], fR[4], uL, uR, pL, pR;
+    euler_flux_dir(wL, gamma, dir, fL, &uL, &pL);
+    euler_flux_dir(wR, gamma, dir, fR, &uR, &pR);
+    double cL = sqrt(gamma * pL / wL[0]);
+    double cR = sqrt(gamma * pR / wR[0]);
+    double sl = fmin(uL - cL, uR - cR);
+    double sr = fmax(uL + cL, uR + cR);
+    if (sl >= 0.0) {
+        for (int m = 0; m < 4; ++m) fw[m] = fL[m];
+    } else if (sr <= 0.0) {
+        for (int m = 0; m < 4; ++m) fw[m] = fR[m];
+    } else {
+        double factor = 1.0 / (sr - sl);
+        for (int m = 0; m < 4; ++m)
+            fw[m] = factor * (sr * fL[m] - sl * fR[m] + sl * sr * (wR[m] - wL[m]));
+    }
+}
+
+/* Local Lax-Friedrichs (Rusanov) flux: 0.5 (FL + FR) - 0.5 lambda (wR - wL),
+ * lambda = max(|uL| + cL, |uR| + cR). */
+void fro_flux_lf2d(const double *wL, const double *wR, double gamma, int dir, double *fw) {
+    double fL[4], fR[4], uL, uR, pL, pR;
+    euler_flux_dir(wL, gamma, dir, fL, &uL, &pL);
+    euler_flux_dir(wR, gamma, dir, fR, &uR, &pR);
+    double cL = sqrt(gamma * pL / wL[0]);
+    double cR = sqrt(gamma * pR / wR[0]);
+    double lam = fmax(fabs(uL) + cL, fabs(uR) + cR);
+    for (int m = 0; m < 4; ++m) fw[m] = 0.5 * (fL[m] + fR[m]) - 0.5 * lam * (wR[m] - wL[m]);
+}
+
+/* 1D Euler flux [m, m U + p, (E + p) U] */
+static inline void euler_flux_1d(const double *w, double gamma, double *f, double *u_out, double *p_out) {
+    double U = w[1] / w[0];
+    double p = (gamma - 1.0) * (w[2] - 0.5 * w[1] * U);
+    f[0] = w[1];
+    f[1] = w[1] * U + p;
+    f[2] = (w[2] + p) * U;
+    if (u_out) *u_out = U;
+    if (p_out) *p_out = p;
+}
+
+/* 1D HLL, stands in for KitBase.flux_hll! at src/Equation/eq_euler.jl:53 */
+void fro_flux_hll1d(const double *wL, const double *wR, double gamma, double *fw) {
+    double fL[3], fR[3], uL, uR, pL, pR;
+    euler_flux_1d(wL, gamma, fL, &uL, &pL);
+    euler_flux_1d(wR, gamma, fR, &uR, &pR);
+    double cL = sqrt(gamma * pL / wL[0]);
+    double cR = sqrt(gamma * pR / wR[0]);
+    double sl = fmin(uL - cL, uR - cR);
+    double sr = fmax(uL + cL, uR + cR);
+    if (sl >= 0.0) {
+        for (int m = 0; m < 3; ++m) fw[m] = fL[m];
+    } else if (sr <= 0.0) {
+        for (int m = 0; m < 3; ++m) fw[m] = fR[m];
+    } else {
+        double factor = 1.0 / (sr - sl);
+        for (int m = 0; m < 3; ++m)
+            fw[m] = factor * (sr * fL[m] - sl * fR[m] + sl * sr * (wR[m] - wL[m]));
+    }
+}
+
+/* Normal-shock (Rankine-Hugoniot) states for a shock of upstream Mach Ma
+ * with upstream rho = 1, p = 1 (so c = sqrt(gamma)).  pre/post = [rho, u, p].
+ * Stands in for KitBase.ib_rh used at example/shock-vortex.jl:162. */
+void fro_ib_rh(double Ma, double gamma, double *pre, double *post) {
+    double c1 = sqrt(gamma);
+    pre[0] = 1.0;
+    pre[1] = Ma * c1;
+    pre[2] = 1.0;
+    double M2 = Ma * Ma;
+    double rr = (gamma + 1.0) * M2 / ((gamma - 1.0) * M2 + 2.0);
+    double pr = 1.0 + 2.0 * gamma / (gamma + 1.0) * (M2 - 1.0);
+    post[0] = rr;
+    post[1] = pre[1] / rr;
+    post[2] = pr;
+}
+
+/* ------------------------------------------------------------------------
+ * Residuals
+ * ---------------------------------------------------------------------- */
+
+long fro_ndof(const fro_cfg *c) {
+    switch (c->kind) {
+    case FRO_ADVECTION:
+    case FRO_BURGERS: return (long)c->nx * c->np;
+    case FRO_EULER1D: return (long)c->nx * c->np * 3;
+    case FRO_EULER2D: return (long)c->nx * c->ny * c->np * c->np * 4;
+    case FRO_BGK1D: return (long)c->nx * c->nvel * c->np;
+    }
+    return 0;
+}
+
+/* Scalar 1D residual: frode_advection! (src/Equation/eq_advection.jl:55-77)
+ * with advection_dflux! (:103-111), the face interpolation (:63-64),
+ * advection_iflux! (:128-137, epsilon 1e-8), rhs1 = f*lpdm' (:68),
+ * scalar_rhs! (src/Equation/eq_scalar.jl:1-12) and period_advection!
+ * (eq_advection.jl:158-175, epsilon 1e-6) or dirichlet_advection! (:153-156).
+ * Burgers uses the same machinery with the flux u^2/2. */
+static void rhs_scalar1d(const fro_cfg *c, double *du, const double *u) {
+    int ne = c->nx, np = c->np;
+    double *f = (double *)malloc(sizeof(double) * ne * np);
+    double *uf = (double *)malloc(sizeof(double) * ne * 2);
+    double *ff = (double *)malloc(sizeof(double) * ne * 2);
+    double *fi = (double *)malloc(sizeof(double) * (ne + 1));
+    for (int k = 0; k < np; ++k)
+        for (int i = 0; i < ne; ++i) {
+            double x = u[i + ne * k];
+            double fl = c->kind == FRO_BURGERS ? 0.5 * x * x : c->a * x;
+            f[i + ne * k] = fl / c->J[i];
+        }
+    for (int i = 0; i < ne; ++i) {
+        double a0 = 0, a1 = 0, b0 = 0, b1 = 0;
+        for (int k = 0; k < np; ++k) {
+            a0 += u[i + ne * k] * c->ll[k];
+            a1 += u[i + ne * k] * c->lr[k];
+            b0 += f[i + ne * k] * c->ll[k];
+            b1 += f[i + ne * k] * c->lr[k];
+        }
+        uf[i] = a0;
+        uf[i + ne] = a1;
+        ff[i] = b0;
+        ff[i + ne] = b1;
+    }
+    for (int i = 1; i < ne; ++i) {
+        double au = (ff[i] - ff[i - 1 + ne]) / (uf[i] - uf[i - 1 + ne] + c->eps_interior);
+        fi[i] = 0.5 * (ff[i] + ff[i - 1 + ne]) - 0.5 * fabs(au) * (uf[i] - uf[i - 1 + ne]);
+    }
+    int periodic = c->bc[0] == FRO_BC_PERIODIC;
+    if (periodic) {
+        double au = (ff[0] - ff[ne - 1 + ne]) / (uf[0] - uf[ne - 1 + ne] + c->eps_periodic);
+        fi[0] = 0.5 * (ff[ne - 1 + ne] + ff[0]) - 0.5 * fabs(au) * (uf[0] - uf[ne - 1 + ne]);
+        fi[ne] = fi[0];
+    }
+    for (int m = 0; m < np; ++m)
+        for (int i = 0; i < ne; ++i) {
+            int boundary = (i == 0 || i == ne - 1);
+            if (boundary && !periodic) {
+                du[i + ne * m] = 0.0;
+                continue;
+            }
+            double r = 0.0;
+            for (int k = 0; k < np; ++k) r += f[i + ne * k] * c->lpdm[m + np * k];
+            du[i + ne * m] = -(r + (fi[i] - ff[i]) * c->dgl[m] + (fi[i + 1] - ff[i + ne]) * c->dgr[m]);
+        }
+    free(f);
+    free(uf);
+    free(ff);
+    free(fi);
+}
+
+/* 1D Euler residual: frode_euler! (src/Equation/eq_euler.jl:29-73) with
+ * period_euler! (:80-98) or dirichlet_euler! (:75-78).  The interface flux
+ * is scaled by 1/J[i] in the combination (:63-64). */
+static void rhs_euler1d(const fro_cfg *c, double *du, const double *u) {
+    int ne = c->nx, np = c->np;
+    double g = c->gamma;
+    double *f = (double *)malloc(sizeof(double) * ne * np * 3);
+    double *uf = (double *)malloc(sizeof(double) * ne * 2 * 3);
+    double *ff = (double *)malloc(sizeof(double) * ne * 2 * 3);
+    double *fi = (double *)malloc(sizeof(double) * (ne + 1) * 3);
+#define U1(i, k, m) u[(i) + ne * ((k) + np * (m))]
+#define F1(i, k, m) f[(i) + ne * ((k) + np * (m))]
+    for (int k = 0; k < np; ++k)
+        for (int i = 0; i < ne; ++i) {
+            double w[3] = {U1(i, k, 0), U1(i, k, 1), U1(i, k, 2)}, fl[3];
+            euler_flux_1d(w, g, fl, NULL, NULL);
+            for (int m = 0; m < 3; ++m) F1(i, k, m) = fl[m] / c->J[i];
+        }
+    /* u_face[i, side, m]: side 0 = left (ll), 1 = right (lr) */
+    for (int m = 0; m < 3; ++m)
+        for (int i = 0; i < ne; ++i) {
+            double a0 = 0, a1 = 0, b0 = 0, b1 = 0;
+            for (int k = 0; k < np; ++k) {
+                a0 += U1(i, k, m) * c->ll[k];
+                a1 += U1(i, k, m) * c->lr[k];
+                b0 += F1(i, k, m) * c->ll[k];
+                b1 += F1(i, k, m) * c->lr[k];
+            }
+            uf[i + ne * (0 + 2 * m)] = a0;
+            uf[i + ne * (1 + 2 * m)] = a1;
+            ff[i + ne * (0 + 2 * m)] = b0;
+            ff[i + ne * (1 + 2 * m)] = b1;
+        }
+    for (int i = 1; i < ne; ++i) {
+        double wL[3], wR[3], fw[3];
+        for (int m = 0; m < 3; ++m) {
+            wL[m] = uf[(i - 1) + ne * (1 + 2 * m)];
+            wR[m] = uf[i + ne * (0 + 2 * m)];
+        }
+        fro_flux_hll1d(wL, wR, g, fw);
+        for (int m = 0; m < 3; ++m) fi[i + (ne + 1) * m] = fw[m];
+    }
+    int periodic = c->bc[0] == FRO_BC_PERIODIC;
+    if (periodic) {
+        double wL[3], wR[3], fw[3];
+        for (int m = 0; m < 3; ++m) {
+            wL[m] = uf[(ne - 1) + ne * (1 + 2 * m)];
+            wR[m] = uf[0 + ne * (0 + 2 * m)];
+        }
+        fro_flux_hll1d(wL, wR, g, fw);
+        for (int m = 0; m < 3; ++m) {
+            fi[0 + (ne + 1) * m] = fw[m];
+            fi[ne + (ne + 1) * m] = fw[m];
+        }
+    }
+    for (int m = 0; m < 3; ++m)
+        for (int kk = 0; kk < np; ++kk)
+            for (int i = 0; i < ne; ++i) {
+                int boundary = (i == 0 || i == ne - 1);
+                double *d = &du[i + ne * (kk + np * m)];
+                if (boundary && !periodic) {
+                    *d = 0.0;
+                    continue;
+                }
+                double r = 0.0;
+                for (int k = 0; k < np; ++k) r += F1(i, k, m) * c->lpdm[kk + np * k];
+                *d = -(r + (fi[i + (ne + 1) * m] / c->J[i] - ff[i + ne * (0 + 2 * m)]) * c->dgl[kk] +
+                       (fi[i + 1 + (ne + 1) * m] / c->J[i] - ff[i + ne * (1 + 2 * m)]) * c->dgr[kk]);
+            }
+#undef U1
+#undef F1
+    free(f);
+    free(uf);
+    free(ff);
+    free(fi);
+}
+
+/* 2D Euler residual on rectangular elements: the dudt! closure of
+ * example/shock-vortex.jl:26-118 (same as example/euler2d_wave.jl:35-107)
+ * with a choice of HLL or local Lax-Friedrichs interface flux and with the
+ * ghost layer refreshed every stage from the boundary kinds (periodic:
+ * euler2d_wave.jl:125-135 without the sign flips; copy and fixed inflow:
+ * shock-vortex.jl:323-330).
+ * Face numbering follows the reference: 0 = bottom (s=-1), 1 = right
+ * (r=+1), 2 = top (s=+1), 3 = left (r=-1).  Internally elements are stored
+ * contiguously (64 values for p=3) to keep the CPU loops cache-friendly. */
+typedef struct {
+    int nxg, nyg, np, E;
+    double *ug;  /* ghosted element-contiguous state [jg][ig][m][l][k] */
+    double *uface; /* [jg][ig][face][pt][m] */
+    double *fface; /* normal flux trace [jg][ig][face][pt][m] (interior only) */
+    double *fvol;  /* [j][i][dir][m][l][k] interior only */
+    double *fxi;   /* [j][i(0..nx)][pt][m] */
+    double *fyi;   /* [j(0..ny)][i][pt][m] */
+} e2d_work;
+
+static void e2d_fill_ghosts(const fro_cfg *c, const double *u, e2d_work *w) {
+    int nx = c->nx, ny = c->ny, np = c->np, E = w->E, nxg = w->nxg;
+    long nn = (long)nx * ny;
+#ifdef _OPENMP
+#pragma omp parallel for OMP_THREADS
+#endif
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            double *dst = w->ug + ((long)(j + 1) * nxg + (i + 1)) * E;
+            for (int m = 0; m < 4; ++m)
+                for (int l = 0; l < np; ++l)
+                    for (int k = 0; k < np; ++k)
+                        dst[(m * np + l) * np + k] = u[i + (long)nx * j + nn * (k + np * (l + (long)np * m))];
+        }
+    /* sides: 0 left (ig=0), 1 right (ig=nx+1), 2 bottom (jg=0), 3 top (jg=ny+1) */
+    for (int j = 1; j <= ny; ++j) {
+        for (int side = 0; side < 2; ++side) {
+            int ig = side == 0 ? 0 : nx + 1;
+            double *dst = w->ug + ((long)j * nxg + ig) * E;
+            int bc = c->bc[side];
+            if (bc == FRO_BC_FIXED) {
+                for (int m = 0; m < 4; ++m)
+                    for (int q = 0; q < np * np; ++q) dst[m * np * np + q] = c->fixed_state[side][m];
+            } else {
+                int src_i = bc == FRO_BC_PERIODIC ? (side == 0 ? nx : 1) : (side == 0 ? 1 : nx);
+                memcpy(dst, w->ug + ((long)j * nxg + src_i) * E, sizeof(double) * E);
+            }
+        }
+    }
+    for (int i = 1; i <= nx; ++i) {
+        for (int side = 2; side < 4; ++side) {
+            int jg = side == 2 ? 0 : ny + 1;
+            double *dst = w->ug + ((long)jg * nxg + i) * E;
+            int bc = c->bc[side];
+            if (bc == FRO_BC_FIXED) {
+                for (int m = 0; m < 4; ++m)
+                    for (int q = 0; q < np * np; ++q) dst[m * np * np + q] = c->fixed_state[side][m];
+            } else {
+                int src_j = bc == FRO_BC_PERIODIC ? (side == 2 ? ny : 1) : (side == 2 ? 1 : ny);
+                memcpy(dst, w->ug + ((long)src_j * nxg + i) * E, sizeof(double) * E);
+            }
+        }
+    }
+}
+
+static void rhs_euler2d(const fro_cfg *c, double *du, const double *u) {
+    int nx = c->nx, ny = c->ny, np = c->np;
+    double g = c->gamma;
+    e2d_work w;
+    w.nxg = nx + 2;
+    w.nyg = ny + 2;
+    w.np = np;
+    w.E = 4 * np * np;
+    long ng = (long)w.nxg * w.nyg;
+    int FS = 4 * np * 4; /* per element face block: face, pt, m */
+    w.ug = (double *)malloc(sizeof(double) * ng * w.E);
+    w.uface = (double *)malloc(sizeof(double) * ng * FS);
+    w.fface = (double *)malloc(sizeof(double) * ng * FS);
+    w.fvol = (double *)malloc(sizeof(double) * (long)nx * ny * 2 * w.E);
+    w.fxi = (double *)malloc(sizeof(double) * (long)(nx + 1) * ny * np * 4);
+    w.fyi = (double *)malloc(sizeof(double) * (long)nx * (ny + 1) * np * 4);
+    e2d_fill_ghosts(c, u, &w);
+    const double *ll = c->ll, *lr = c->lr, *lpdm = c->lpdm;
+    int E = w.E, nxg = w.nxg;
+
+    /* volume flux f = iJ * [F, G] (shock-vortex.jl:48-55) and face traces
+     * of u (all elements incl. ghosts) and of the normal flux (interior),
+     * shock-vortex.jl:57-71 */
+#ifdef _OPENMP
+#pragma omp parallel for OMP_THREADS schedule(static)
+#endif
+    for (long e = 0; e < ng; ++e) {
+        int jg = (int)(e / nxg), ig = (int)(e % nxg);
+        int interior = ig >= 1 && ig <= nx && jg >= 1 && jg <= ny;
+        int needed = interior || ((ig >= 1 && ig <= nx) != (jg >= 1 && jg <= ny));
+        if (!needed) continue;
+        const double *ue = w.ug + e * E;
+        double *uf = w.uface + e * FS;
+        /* u traces */
+        for (int m = 0; m < 4; ++m)
+            for (int l = 0; l < np; ++l) {
+                double b = 0, r = 0, t = 0, lf = 0;
+                for (int q = 0; q < np; ++q) {
+                    /* face 0/2 along s at r-index l: u[l, q]; face 1/3 along r at s-index l: u[q, l] */
+                    double us = ue[(m * np + q) * np + l]; /* k = l, l' = q */
+                    double ur = ue[(m * np + l) * np + q]; /* k = q, l' = l */
+                    b += us * ll[q];
+                    t += us * lr[q];
+                    r += ur * lr[q];
+                    lf += ur * ll[q];
+                }
+                uf[(0 * np + l) * 4 + m] = b;
+                uf[(1 * np + l) * 4 + m] = r;
+                uf[(2 * np + l) * 4 + m] = t;
+                uf[(3 * np + l) * 4 + m] = lf;
+            }
+        if (!interior) continue;
+        long ei = (long)(jg - 1) * nx + (ig - 1);
+        double *fv = w.fvol + ei * 2 * E;
+        for (int l = 0; l < np; ++l)
+            for (int k = 0; k < np; ++k) {
+                double ww[4], F[4], G[4];
+                for (int m = 0; m < 4; ++m) ww[m] = ue[(m * np + l) * np + k];
+                euler_flux_dir(ww, g, 0, F, NULL, NULL);
+                euler_flux_dir(ww, g, 1, G, NULL, NULL);
+                for (int m = 0; m < 4; ++m) {
+                    fv[(0 * 4 + m) * np * np + l * np + k] = c->iJx * F[m];
+                    fv[(1 * 4 + m) * np * np + l * np + k] = c->iJy * G[m];
+                }
+            }
+        double *ff = w.fface + e * FS;
+        for (int m = 0; m < 4; ++m)
+            for (int l = 0; l < np; ++l) {
+                double b = 0, r = 0, t = 0, lf = 0;
+                for (int q = 0; q < np; ++q) {
+                    double gs = fv[(1 * 4 + m) * np * np + q * np + l]; /* y flux at (k=l, l'=q) */
+                    double fr = fv[(0 * 4 + m) * np * np + l * np + q]; /* x flux at (k=q, l'=l) */
+                    b += gs * ll[q];
+                    t += gs * lr[q];
+                    r += fr * lr[q];
+                    lf += fr * ll[q];
+                }
+                ff[(0 * np + l) * 4 + m] = b;
+                ff[(1 * np + l) * 4 + m] = r;
+                ff[(2 * np + l) * 4 + m] = t;
+                ff[(3 * np + l) * 4 + m] = lf;
+            }
+    }
+
+    /* interface fluxes: x faces shock-vortex.jl:73-80, y faces :81-89 */
+#ifdef _OPENMP
+#pragma omp parallel for OMP_THREADS schedule(static)
+#endif
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i <= nx; ++i) {
+            const double *L = w.uface + ((long)(j + 1) * nxg + i) * FS;     /* element i-1 (ghost index i) */
+            const double *R = w.uface + ((long)(j + 1) * nxg + i + 1) * FS; /* element i */
+            for (int k = 0; k < np; ++k) {
+                double *fw = w.fxi + (((long)j * (nx + 1) + i) * np + k) * 4;
+                if (c->flux == FRO_FLUX_HLL)
+                    fro_flux_hll2d(L + (1 * np + k) * 4, R + (3 * np + k) * 4, g, 0, fw);
+                else
+                    fro_flux_lf2d(L + (1 * np + k) * 4, R + (3 * np + k) * 4, g, 0, fw);
+            }
+        }
+#ifdef _OPENMP
+#pragma omp parallel for OMP_THREADS schedule(static)
+#endif
+    for (int j = 0; j <= ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const double *B = w.uface + ((long)j * nxg + i + 1) * FS;       /* element j-1 */
+            const double *T = w.uface + ((long)(j + 1) * nxg + i + 1) * FS; /* element j */
+            for (int k = 0; k < np; ++k) {
+                double *fw = w.fyi + (((long)j * nx + i) * np + k) * 4;
+                if (c->flux == FRO_FLUX_HLL)
+                    fro_flux_hll2d(B + (2 * np + k) * 4, T + (0 * np + k) * 4, g, 1, fw);
+                else
+                    fro_flux_lf2d(B + (2 * np + k) * 4, T + (0 * np + k) * 4, g, 1, fw);
+            }
+        }
+
+    /* derivative (shock-vortex.jl:91-100) and combination (:102-115) */
+    long nn = (long)nx * ny;
+#ifdef _OPENMP
+#pragma omp parallel for OMP_THREADS schedule(static)
+#endif
+    for (long ei = 0; ei < nn; ++ei) {
+        int j = (int)(ei / nx), i = (int)(ei % nx);
+        const double *fv = w.fvol + ei * 2 * E;
+        const double *ff = w.fface + ((long)(j + 1) * nxg + i + 1) * FS;
+        for (int m = 0; m < 4; ++m)
+            for (int l = 0; l < np; ++l)
+                for (int k = 0; k < np; ++k) {
+                    double r1 = 0, r2 = 0;
+                    for (int q = 0; q < np; ++q) {
+                        r1 += fv[(0 * 4 + m) * np * np + l * np + q] * lpdm[k + np * q];
+                        r2 += fv[(1 * 4 + m) * np * np + q * np + k] * lpdm[l + np * q];
+                    }
+                    double fxl = w.fxi[(((long)j * (nx + 1) + i) * np + l) * 4 + m];
+                    double fxr = w.fxi[(((long)j * (nx + 1) + i + 1) * np + l) * 4 + m];
+                    double fyb = w.fyi[(((long)j * nx + i) * np + k) * 4 + m];
+                    double fyt = w.fyi[(((long)(j + 1) * nx + i) * np + k) * 4 + m];
+                    double v = -(r1 + r2 + (fxl * c->iJx - ff[(3 * np + l) * 4 + m]) * c->dgl[k] +
+                                 (fxr * c->iJx - ff[(1 * np + l) * 4 + m]) * c->dgr[k] +
+                                 (fyb * c->iJy - ff[(0 * np + k) * 4 + m]) * c->dgl[l] +
+                                 (fyt * c->iJy - ff[(2 * np + k) * 4 + m]) * c->dgr[l]);
+                    du[i + (long)nx * j + nn * (k + np * (l + (long)np * m))] = v;
+                }
+    }
+    free(w.ug);
+    free(w.uface);
+    free(w.fface);
+    free(w.fvol);
+    free(w.fxi);
+    free(w.fyi);
+}
+
+/* 1D1V BGK residual: mol! of example/bgk_wave.jl:69-129 (moments ->
+ * conserve_prim(w, 3.0) -> maxwellian :76-81; f = v u / J :84-88;
+ * interp_face! :99-101; kinetic upwind through f2e/e2f :103-107;
+ * poly_derivative! :114-116; combination + relaxation (M - u)/tau
+ * :122-128).  Periodic faces.  tau comes from the configuration (the
+ * example hard-codes 1e-2 at :82). */
+static void rhs_bgk1d(const fro_cfg *c, double *du, const double *u) {
+    int ne = c->nx, nv = c->nvel, np = c->np;
+    double *ffL = (double *)malloc(sizeof(double) * ne * nv); /* left-face trace of f */
+    double *ffR = (double *)malloc(sizeof(double) * ne * nv); /* right-face trace */
+#define UB(i, v, k) u[(i) + (long)ne * ((v) + (long)nv * (k))]
+#ifdef _OPENMP
+#pragma omp parallel for OMP_THREADS schedule(static)
+#endif
+    for (int i = 0; i < ne; ++i) {
+        double J = c->J[i];
+        for (int v = 0; v < nv; ++v) {
+            double a = 0, b = 0;
+            for (int k = 0; k < np; ++k) {
+                double f = c->velo[v] * UB(i, v, k) / J;
+                a += f * c->ll[k];
+                b += f * c->lr[k];
+            }
+            ffL[i + ne * v] = a;
+            ffR[i + ne * v] = b;
+        }
+    }
+#ifdef _OPENMP
+#pragma omp parallel for OMP_THREADS schedule(static)
+#endif
+    for (int i = 0; i < ne; ++i) {
+        double J = c->J[i];
+        int il = (i + ne - 1) % ne, ir = (i + 1) % ne;
+        double *M = (double *)malloc(sizeof(double) * nv * np);
+        for (int k = 0; k < np; ++k) {
+            double w0 = 0, w1 = 0, w2 = 0;
+            for (int v = 0; v < nv; ++v) {
+                double x = UB(i, v, k);
+                w0 += c->weights[v] * x;
+                w1 += c->weights[v] * c->velo[v] * x;
+                w2 += c->weights[v] * (c->velo[v] * c->velo[v]) * x;
+            }
+            w2 *= 0.5;
+            /* conserve_prim(w, gamma = 3): lambda = 0.5 rho / (gamma-1) / (E - 0.5 m^2/rho) */
+            double rho = w0, U = w1 / w0;
+            double lam = 0.5 * w0 / (3.0 - 1.0) / (w2 - 0.5 * w1 * w1 / w0);
+            for (int v = 0; v < nv; ++v) {
+                double dv = c->velo[v] - U;
+                M[v + nv * k] = rho * sqrt(lam / M_PI) * exp(-lam * dv * dv);
+            }
+        }
+        for (int v = 0; v < nv; ++v) {
+            double vel = c->velo[v];
+            double delta = vel > 0.0 ? 1.0 : 0.0; /* heaviside */
+            /* face left of i: upwind between right trace of il and left trace of i */
+            double fl = ffL[i + ne * v] * (1.0 - delta) + ffR[il + ne * v] * delta;
+            double fr = ffL[ir + ne * v] * (1.0 - delta) + ffR[i + ne * v] * delta;
+            for (int m = 0; m < np; ++m) {
+                double r = 0.0;
+                for (int k = 0; k < np; ++k) r += (vel * UB(i, v, k) / J) * c->lpdm[m + np * k];
+                du[i + (long)ne * (v + (long)nv * m)] =
+                    -(r + (fl - ffL[i + ne * v]) * c->dgl[m] + (fr - ffR[i + ne * v]) * c->dgr[m]) +
+                    (M[v + nv * m] - UB(i, v, m)) / c->tau;
+            }
+        }
+        free(M);
+    }
+#undef UB
+    free(ffL);
+    free(ffR);
+}
+
+void fro_rhs(const fro_cfg *c, double *du, const double *u) {
+    switch (c->kind) {
+    case FRO_ADVECTION:
+    case FRO_BURGERS: rhs_scalar1d(c, du, u); break;
+    case FRO_EULER1D: rhs_euler1d(c, du, u); break;
+    case FRO_EULER2D: rhs_euler2d(c, du, u); break;
+    case FRO_BGK1D: rhs_bgk1d(c, du, u); break;
+    }
+}
+
+/* SSPRK3 in Shu-Osher form (OrdinaryDiffEq SSPRK33; the stepping the
+ * reference's examples hand to OrdinaryDiffEq's init/step!):
+ *   u1 = u + dt L(u);  u2 = (3u + u1 + dt L(u1))/4;  u' = (u + 2 u2 + 2 dt L(u2))/3 */
+void fro_ssprk3(const fro_cfg *c, double *u, double dt, int nsteps, double *work) {
+    long n = fro_ndof(c);
+    double *s = work, *k = work + n;
+    for (int it = 0; it < nsteps; ++it) {
+        fro_rhs(c, k, u);
+        for (long q = 0; q < n; ++q) s[q] = u[q] + dt * k[q];
+        fro_rhs(c, k, s);
+        for (long q = 0; q < n; ++q) s[q] = (3.0 * u[q] + s[q] + dt * k[q]) / 4.0;
+        fro_rhs(c, k, s);
+        for (long q = 0; q < n; ++q) u[q] = (u[q] + 2.0 * s[q] + 2.0 * dt * k[q]) / 3.0;
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * Troubled-cell indicator and modal filter
+ * ---------------------------------------------------------------------- */
+
+/* KitBase :l2 modal filter on a flat modal vector (as called on the
+ * flattened 2D modes at example/shock-vortex.jl:316):
+ * u[q] /= 1 + lam * (q+1)^2 q^2, q = 0-based mode index. */
+static void filter_l2_flat(double *uh, int n, double lam) {
+    for (int q = 0; q < n; ++q) uh[q] /= (1.0 + lam * (double)(q + 1) * (q + 1) * (double)q * q);
+}
+
+/* Post-step indicator + filter, example/shock-vortex.jl:308-321 (over the
+ * full np x np block; the example hard-codes 1:3, i.e. p = 2). */
+int fro_filter2d(const fro_cfg *c, double *u, const double *V, const double *iV, double lam, double S0,
+                 double kappa, int *flags) {
+    int nx = c->nx, ny = c->ny, np = c->np, N = np * np;
+    long nn = (long)nx * ny;
+    int count = 0;
+#ifdef _OPENMP
+#pragma omp parallel for OMP_THREADS reduction(+ : count) schedule(static)
+#endif
+    for (long e = 0; e < nn; ++e) {
+        double ue[36], uh[36];
+        for (int q = 0; q < N; ++q) ue[q] = u[e + nn * q];
+        for (int a = 0; a < N; ++a) {
+            double s = 0;
+            for (int b = 0; b < N; ++b) s += iV[a + N * b] * ue[b];
+            uh[a] = s;
+        }
+        double tot = 0;
+        for (int a = 0; a < N; ++a) tot += uh[a] * uh[a];
+        double su = uh[N - 1] * uh[N - 1] / tot;
+        int troubled = fro_shock_detector(log10(su), np - 1, S0, kappa);
+        if (flags) flags[e] = troubled;
+        if (!troubled) continue;
+        ++count;
+        for (int m = 0; m < 4; ++m) {
+            for (int q = 0; q < N; ++q) ue[q] = u[e + nn * (q + (long)N * m)];
+            for (int a = 0; a < N; ++a) {
+                double s = 0;
+                for (int b = 0; b < N; ++b) s += iV[a + N * b] * ue[b];
+                uh[a] = s;
+            }
+            filter_l2_flat(uh, N, lam);
+            for (int a = 0; a < N; ++a) {
+                double s = 0;
+                for (int b = 0; b < N; ++b) s += V[a + N * b] * uh[b];
+                u[e + nn * (a + (long)N * m)] = s;
+            }
+        }
+    }
+    return count;
+}
+
+/* 1D indicator + filter, example/euler_highlevel.jl:37-52:
+ * su = u_N^2 / (sum u^2 + 1e-6), shock_detector(log10(su), deg) with the
+ * default S0 = -3 log10(deg), kappa = 4. */
+int fro_filter1d(const fro_cfg *c, double *u, int nvar, const double *V, const double *iV, double lam,
+                 int *flags) {
+    int ne = c->nx, np = c->np, deg = np - 1;
+    int count = 0;
+    for (int i = 0; i < ne; ++i) {
+        double ue[8], uh[8];
+        for (int q = 0; q < np; ++q) ue[q] = u[i + (long)ne * q];
+        for (int a = 0; a < np; ++a) {
+            double s = 0;
+            for (int b = 0; b < np; ++b) s += iV[a + np * b] * ue[b];
+            uh[a] = s;
+        }
+        double tot = 0;
+        for (int a = 0; a < np; ++a) tot += uh[a] * uh[a];
+        double su = uh[np - 1] * uh[np - 1] / (tot + 1e-6);
+        int troubled = fro_shock_detector(log10(su), deg, -3.0 * log10((double)deg), 4.0);
+        if (flags) flags[i] = troubled;
+        if (!troubled) continue;
+        ++count;
+        for (int m = 0; m < nvar; ++m) {
+            for (int q = 0; q < np; ++q) ue[q] = u[i + (long)ne * (q + (long)np * m)];
+            for (int a = 0; a < np; ++a) {
+                double s = 0;
+                for (int b = 0; b < np; ++b) s += iV[a + np * b] * ue[b];
+                uh[a] = s;
+            }
+            filter_l2_flat(uh, np, lam);
+            for (int a = 0; a < np; ++a) {
+                double s = 0;
+                for (int b = 0; b < np; ++b) s += V[a + np * b] * uh[b];
+                u[i + (long)ne * (a + (long)np * m)] = s;
+            }
+        }
+    }
+    return count;
+}
+
+/* Learned-indicator inputs: per element the normalised modal energies of
+ * density and pressure, x_q = clamp(log10(uh_q^2 / sum uh^2 + 1e-16), -16, 0)/8 + 1. */
+void fro_modal_features2d(const fro_cfg *c, const double *u, const double *iV, double *feat) {
+    int nx = c->nx, ny = c->ny, np = c->np, N = np * np;
+    long nn = (long)nx * ny;
+    double g = c->gamma;
+    for (long e = 0; e < nn; ++e) {
+        double ue[2][36], uh[36];
+        for (int q = 0; q < N; ++q) {
+            double w[4];
+            for (int m = 0; m < 4; ++m) w[m] = u[e + nn * (q + (long)N * m)];
+            double rinv = 1.0 / w[0];
+            double U = w[1] * rinv, Vv = w[2] * rinv;
+            ue[0][q] = w[0];
+            ue[1][q] = (g - 1.0) * (w[3] - 0.5 * (w[1] * U + w[2] * Vv));
+        }
+        for (int v = 0; v < 2; ++v) {
+            double tot = 0;
+            for (int a = 0; a < N; ++a) {
+                double s = 0;
+                for (int b = 0; b < N; ++b) s += iV[a + N * b] * ue[v][b];
+                uh[a] = s * s;
+                tot += uh[a];
+            }
+            for (int a = 0; a < N; ++a) {
+                double x = log10(uh[a] / tot + 1e-16);
+                if (x < -16.0) x = -16.0;
+                if (x > 0.0) x = 0.0;
+                feat[e * 2 * N + v * N + a] = x / 8.0 + 1.0;
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * Reductions and norms
+ * ---------------------------------------------------------------------- */
+
+void fro_conserved_sums2d(const fro_cfg *c, const double *u, const double *wp, double *sums) {
+    int np = c->np, N = np * np;
+    long nn = (long)c->nx * c->ny;
+    double area = 1.0 / (c->iJx * c->iJy); /* dx dy / 4 per unit reference weight */
+    for (int m = 0; m < 4; ++m) {
+        double s = 0.0;
+        for (int q = 0; q < N; ++q) {
+            double t = 0.0;
+            for (long e = 0; e < nn; ++e) t += u[e + nn * (q + (long)N * m)];
+            s += wp[q] * t;
+        }
+        sums[m] = s * area;
+    }
+}
+
+double fro_max_speed2d(const fro_cfg *c, const double *u) {
+    long n = (long)c->nx * c->ny * c->np * c->np;
+    double g = c->gamma, mx = 0.0;
+    for (long q = 0; q < n; ++q) {
+        double w[4] = {u[q], u[q + n], u[q + 2 * n], u[q + 3 * n]};
+        double U = w[1] / w[0], V = w[2] / w[0];
+        double p = (g - 1.0) * (w[3] - 0.5 * (w[1] * U + w[2] * V));
+        double cs = sqrt(g * p / w[0]);
+        double s = fmax(fabs(U) + cs, fabs(V) + cs);
+        if (s > mx) mx = s;
+    }
+    return mx;
+}
+
+/* L1_error / L2_error / Linf_error, src/tools.jl:43-53 (note dx inside the
+ * square for L2) */
+double fro_L1_error(const double *u, const double *ue, long n, double dx) {
+    double s = 0;
+    for (long i = 0; i < n; ++i) s += fabs(u[i] - ue[i]) * dx;
+    return s;
+}
+double fro_L2_error(const double *u, const double *ue, long n, double dx) {
+    double s = 0;
+    for (long i = 0; i < n; ++i) {
+        double t = fabs(u[i] - ue[i]) * dx;
+        s += t * t;
+    }
+    return sqrt(s);
+}
+double fro_Linf_error(const double *u, const double *ue, long n, double dx) {
+    double s = 0;
+    for (long i = 0; i < n; ++i) {
+        double t = fabs(u[i] - ue[i]) * dx;
+        if (t > s) s = t;
+    }
+    return s;
+}
+
+/* ------------------------------------------------------------------------
+ * Learned indicator, FP64 reference for the GPU kernels' gradients
+ * ---------------------------------------------------------------------- */
+
+static double gelu(double x) { return 0.5 * x * (1.0 + erf(x / sqrt(2.0))); }
+static double dgelu(double x) {
+    return 0.5 * (1.0 + erf(x / sqrt(2.0))) + x * exp(-0.5 * x * x) / sqrt(2.0 * M_PI);
+}
+
+void fro_mlp_forward(const double *P, const double *x, int n, int nin, int nh, double *y) {
+    const double *W1 = P, *b1 = W1 + nh * nin, *W2 = b1 + nh, *b2 = W2 + nh * nh, *W3 = b2 + nh,
+                 *b3 = W3 + nh;
+    double *h1 = (double *)malloc(sizeof(double) * nh * 2), *h2 = h1 + nh;
+    for (int s = 0; s < n; ++s) {
+        const double *xs = x + (long)s * nin;
+        for (int o = 0; o < nh; ++o) {
+            double a = b1[o];
+            for (int i = 0; i < nin; ++i) a += W1[o * nin + i] * xs[i];
+            h1[o] = gelu(a);
+        }
+        for (int o = 0; o < nh; ++o) {
+            double a = b2[o];
+            for (int i = 0; i < nh; ++i) a += W2[o * nh + i] * h1[i];
+            h2[o] = gelu(a);
+        }
+        double a = b3[0];
+        for (int i = 0; i < nh; ++i) a += W3[i] * h2[i];
+        y[s] = 1.0 / (1.0 + exp(-a));
+    }
+    free(h1);
+}
+
+double fro_mlp_loss_grad(const double *P, const double *x, const double *label, int n, int nin, int nh,
+                         double *grad) {
+    const double *W1 = P, *b1 = W1 + nh * nin, *W2 = b1 + nh, *b2 = W2 + nh * nh, *W3 = b2 + nh,
+                 *b3 = W3 + nh;
+    long np_ = (long)nh * nin + nh + (long)nh * nh + nh + nh + 1;
+    memset(grad, 0, sizeof(double) * np_);
+    double *gW1 = grad, *gb1 = gW1 + nh * nin, *gW2 = gb1 + nh, *gb2 = gW2 + nh * nh, *gW3 = gb2 + nh,
+           *gb3 = gW3 + nh;
+    double *buf = (double *)malloc(sizeof(double) * nh * 6);
+    double *a1 = buf, *h1 = buf + nh, *a2 = buf + 2 * nh, *h2 = buf + 3 * nh, *d2 = buf + 4 * nh,
+           *d1 = buf + 5 * nh;
+    double loss = 0.0;
+    for (int s = 0; s < n; ++s) {
+        const double *xs = x + (long)s * nin;
+        for (int o = 0; o < nh; ++o) {
+            double a = b1[o];
+            for (int i = 0; i < nin; ++i) a += W1[o * nin + i] * xs[i];
+            a1[o] = a;
+            h1[o] = gelu(a);
+        }
+        for (int o = 0; o < nh; ++o) {
+            double a = b2[o];
+            for (int i = 0; i < nh; ++i) a += W2[o * nh + i] * h1[i];
+            a2[o] = a;
+            h2[o] = gelu(a);
+        }
+        double a3 = b3[0];
+        for (int i = 0; i < nh; ++i) a3 += W3[i] * h2[i];
+        double y = 1.0 / (1.0 + exp(-a3));
+        double t = label[s];
+        double ye = fmin(fmax(y, 1e-12), 1.0 - 1e-12);
+        loss += -(t * log(ye) + (1.0 - t) * log(1.0 - ye));
+        double g3 = (y - t) / n; /* d loss / d a3 for sigmoid + BCE, mean */
+        gb3[0] += g3;
+        for (int i = 0; i < nh; ++i) {
+            gW3[i] += g3 * h2[i];
+            d2[i] = g3 * W3[i] * dgelu(a2[i]);
+        }
+        for (int o = 0; o < nh; ++o) {
+            gb2[o] += d2[o];
+            for (int i = 0; i < nh; ++i) gW2[o * nh + i] += d2[o] * h1[i];
+        }
+        for (int i = 0; i < nh; ++i) {
+            double s2 = 0.0;
+            for (int o = 0; o < nh; ++o) s2 += d2[o] * W2[o * nh + i];
+            d1[i] = s2 * dgelu(a1[i]);
+        }
+        for (int o = 0; o < nh; ++o) {
+            gb1[o] += d1[o];
+            for (int i = 0; i < nin; ++i) gW1[o * nin + i] += d1[o] * xs[i];
+        }
+    }
+    free(buf);
+    return loss / n;
+}

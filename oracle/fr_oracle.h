@@ -1,0 +1,115 @@
+/*
+ * fr_oracle.h -- CPU FP64 oracle for the flux-reconstruction hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library restates, in plain C, the
+ * reference's (FluxReconstruction.jl) algorithms for the element residual and
+ * explicit time stepping.  It is linked only by tests/, by the smoke check in
+ * __graft_entry__.py and by the cpu_baseline / --impl reference legs of
+ * bench.py.  The product library (libfrgpu.so) never calls it.
+ *
+ * Parity status: the setup math (Gauss-Legendre points, Lagrange operators,
+ * correction-function derivatives, orthonormal Jacobi / Vandermonde matrices)
+ * is pinned against the reference's own identities
+ * (example/vandermonde_lagrange.jl:14,15,25) and against numpy's
+ * leggauss.  The residual structure follows the cited reference code line by
+ * line.  The KitBase 0.9 physics kernels (flux_hll!, euler_flux, the :l2
+ * modal filter, conserve_prim, maxwellian) are not vendored in the reference,
+ * so they are restated from their published methods; at that boundary parity
+ * is unpinned (the reference cannot run here: no Julia).
+ *
+ * Array layouts are the reference's Julia column-major layouts:
+ *   1D scalar      u[i, k]            -> u[i + ne*k]
+ *   1D Euler       u[i, k, m]         -> u[i + ne*(k + np*m)]
+ *   2D Euler       u[i, j, k, l, m]   -> u[i + nx*(j + ny*(k + np*(l + np*m)))]
+ *   1D1V BGK       u[i, v, k]         -> u[i + ne*(v + nvel*k)]
+ * Matrices (lpdm, V, iV) are column-major: A[r + n*c].
+ */
+#ifndef FR_ORACLE_H
+#define FR_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- setup math ---- */
+void fro_gauss_legendre(int n, double *x, double *w);
+double fro_legendre_p(int n, double x);
+double fro_dlegendre(int n, double x);
+/* kind: 0 radau, 1 sd, 2 huynh */
+void fro_dcorrection(int kind, int deg, const double *x, int nx, double *dgl, double *dgr);
+void fro_lagrange_point(const double *sp, int nsp, double x, double *l);
+void fro_dlagrange(const double *sp, int nsp, double *lpdm);
+double fro_jacobi_p(double x, double alpha, double beta, int N);
+double fro_djacobi_p(double x, double alpha, double beta, int N);
+void fro_vandermonde_1d(int N, const double *r, int nr, double *V);
+void fro_dvandermonde_1d(int N, const double *r, int nr, double *Vr);
+void fro_vandermonde_quad(int N, const double *r, const double *s, int n, double *V);
+int fro_inverse(int n, const double *A, double *Ainv);
+int fro_shock_detector(double Se, int deg, double S0, double kappa);
+
+/* ---- residual configuration ---- */
+enum { FRO_ADVECTION = 0, FRO_BURGERS = 1, FRO_EULER1D = 2, FRO_EULER2D = 3, FRO_BGK1D = 4 };
+enum { FRO_FLUX_ROE = 0, FRO_FLUX_LF = 1, FRO_FLUX_HLL = 2, FRO_FLUX_UPWIND = 3 };
+enum { FRO_BC_PERIODIC = 0, FRO_BC_COPY = 1, FRO_BC_FIXED = 2, FRO_BC_DIRICHLET = 3 };
+
+typedef struct {
+    int kind, flux;
+    int nx, ny, np, nvel;
+    double a, gamma, tau;
+    int bc[4];                 /* 1D: bc[0] for both ends; 2D: left, right, bottom, top */
+    double fixed_state[4][4];  /* conserved ghost state per side for FRO_BC_FIXED */
+    double eps_interior, eps_periodic;
+    const double *J;           /* 1D: per-element Jacobian dx_i/2 */
+    double iJx, iJy;           /* 2D rectangular elements: 2/dx, 2/dy */
+    const double *ll, *lr, *lpdm, *dgl, *dgr;
+    const double *velo, *weights; /* BGK velocity grid */
+} fro_cfg;
+
+long fro_ndof(const fro_cfg *c);
+void fro_rhs(const fro_cfg *c, double *du, const double *u);
+/* Shu-Osher SSPRK3, nsteps fixed steps of size dt; work must hold 2*ndof doubles */
+void fro_ssprk3(const fro_cfg *c, double *u, double dt, int nsteps, double *work);
+
+/* ---- troubled-cell indicator and modal filter ---- */
+/* 2D, per step: detect on rho with iV (np^2 x np^2), filter all 4 variables
+ * with the flattened L2 filter of strength lam.  Returns number of troubled
+ * elements; flags (may be NULL) receives 0/1 per element (i fastest). */
+int fro_filter2d(const fro_cfg *c, double *u, const double *V, const double *iV,
+                 double lam, double S0, double kappa, int *flags);
+/* 1D Euler form (euler_highlevel.jl): su = u_N^2/(sum u^2 + 1e-6), kappa = 4 */
+int fro_filter1d(const fro_cfg *c, double *u, int nvar, const double *V, const double *iV,
+                 double lam, int *flags);
+/* modal energies for the learned indicator: per element 2*np^2 features */
+void fro_modal_features2d(const fro_cfg *c, const double *u, const double *iV, double *feat);
+
+/* ---- reductions and norms ---- */
+void fro_conserved_sums2d(const fro_cfg *c, const double *u, const double *wp, double *sums);
+double fro_max_speed2d(const fro_cfg *c, const double *u);
+double fro_L1_error(const double *u, const double *ue, long n, double dx);
+double fro_L2_error(const double *u, const double *ue, long n, double dx);
+double fro_Linf_error(const double *u, const double *ue, long n, double dx);
+
+/* ---- physics helpers (KitBase restatements) ---- */
+void fro_prim_conserve2d(const double *prim, double gamma, double *w);
+void fro_conserve_prim2d(const double *w, double gamma, double *prim);
+void fro_prim_conserve1d(const double *prim, double gamma, double *w);
+void fro_flux_hll2d(const double *wL, const double *wR, double gamma, int dir, double *fw);
+void fro_flux_lf2d(const double *wL, const double *wR, double gamma, int dir, double *fw);
+void fro_flux_hll1d(const double *wL, const double *wR, double gamma, double *fw);
+void fro_ib_rh(double Ma, double gamma, double *pre, double *post);
+
+/* ---- learned indicator (MLP 32->64->64->1, GELU, sigmoid), FP64 ---- */
+/* params layout: W1[64x32] b1[64] W2[64x64] b2[64] W3[1x64] b3[1], row-major W[out][in] */
+void fro_mlp_forward(const double *params, const double *x, int n, int nin, int nh, double *y);
+/* mean binary cross-entropy loss and its gradient w.r.t. params */
+double fro_mlp_loss_grad(const double *params, const double *x, const double *label, int n,
+                         int nin, int nh, double *grad);
+
+/* threads used by the OpenMP loops (0 = library default) */
+void fro_set_threads(int n);
+int fro_get_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,208 @@
+"""Pin the CPU oracle: golden setup-math vectors, the reference's own identity
+checks, analytic known answers for the residuals, convergence order and
+conservation.  CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "setup_math.npz")
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(GOLD)
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3, 4, 5])
+def test_setup_math_matches_golden(oracle, gold, deg):
+    x, w = oracle.gauss_legendre(deg + 1)
+    np.testing.assert_allclose(x, gold[f"x{deg}"], rtol=0, atol=2e-16)
+    np.testing.assert_allclose(w, gold[f"w{deg}"], rtol=0, atol=5e-16)
+    xn, wn = np.polynomial.legendre.leggauss(deg + 1)
+    np.testing.assert_allclose(x, xn, atol=1e-15)
+    np.testing.assert_allclose(oracle.lagrange_point(x, -1.0), gold[f"ll{deg}"], atol=5e-15)
+    np.testing.assert_allclose(oracle.lagrange_point(x, 1.0), gold[f"lr{deg}"], atol=5e-15)
+    np.testing.assert_allclose(oracle.dlagrange(x), gold[f"dl{deg}"], atol=5e-14)
+    for name in ("radau", "sd", "huynh"):
+        gl, gr = oracle.dcorrection(name, deg, x)
+        np.testing.assert_allclose(gl, gold[f"{name}_l{deg}"], atol=5e-14)
+        np.testing.assert_allclose(gr, gold[f"{name}_r{deg}"], atol=5e-14)
+    np.testing.assert_allclose(oracle.vandermonde_1d(deg, x), gold[f"V{deg}"], atol=5e-15)
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3, 4, 5])
+def test_vandermonde_lagrange_identities(oracle, deg):
+    """example/vandermonde_lagrange.jl:14,15,25: ll, lr and dl equal the
+    Vandermonde-based construction V' \\ psi_f and V' \\ Vr."""
+    ps = oracle.Space1D(0, 1, 100, deg)
+    V = oracle.vandermonde_1d(deg, ps.xpl)
+    psi = oracle.vandermonde_1d(deg, [-1.0, 1.0])
+    lf = np.linalg.solve(V.T, psi.T).T
+    np.testing.assert_allclose(lf[0], ps.ll, atol=1e-13)
+    np.testing.assert_allclose(lf[1], ps.lr, atol=1e-13)
+    Vr = oracle.dvandermonde_1d(deg, ps.xpl)
+    dl = np.linalg.solve(V.T, Vr.T).T
+    np.testing.assert_allclose(dl, ps.dl, atol=1e-12)
+    # row sums of the differentiation matrix vanish, it differentiates x exactly,
+    # Lagrange weights sum to one
+    np.testing.assert_allclose(ps.dl.sum(axis=1), 0.0, atol=1e-12)
+    np.testing.assert_allclose(ps.dl @ ps.xpl, 1.0, atol=1e-12)
+    assert abs(ps.ll.sum() - 1) < 1e-14 and abs(ps.lr.sum() - 1) < 1e-14
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3, 4])
+def test_correction_endpoint_values(oracle, deg):
+    """g_L(-1) = 1, g_L(1) = 0 (and mirrored for g_R): integrate the nodal
+    derivative polynomial (degree deg+... exact via quadrature on deg+2 points)."""
+    xs, ws = np.polynomial.legendre.leggauss(deg + 3)
+    gl, gr = oracle.dcorrection("radau", deg, xs)
+    # int_{-1}^{1} g_L' = g_L(1) - g_L(-1) = -1
+    assert abs(np.dot(ws, gl) + 1.0) < 1e-13
+    assert abs(np.dot(ws, gr) - 1.0) < 1e-13
+
+
+def test_shock_detector_cases(oracle):
+    """src/dissipation.jl:13-23 on the inputs of test/runtests.jl:12-14."""
+    assert oracle.shock_detector(-np.inf, 3) is False
+    assert oracle.shock_detector(np.log10(0.1), 3) is True
+    assert oracle.shock_detector(np.log10(1e5), 3) is True
+    S0 = -3 * np.log10(3)
+    assert oracle.shock_detector(S0 - 4.0 - 1e-9, 3) is False
+    # sigma = 0.5(1 - sin(pi/2 (Se-S0)/k)) < 0.99 unless Se is close to S0 - k
+    assert oracle.shock_detector(S0 - 3.9, 3) is False
+    assert oracle.shock_detector(S0, 3) is True
+
+
+def test_error_norms(oracle):
+    """src/tools.jl:43-53 (dx inside the square for L2)."""
+    rng = np.random.default_rng(0)
+    u, ue = rng.random(7), rng.random(7)
+    dx = 0.1
+    assert abs(oracle.l1_error(u, ue, dx) - np.sum(np.abs(u - ue) * dx)) < 1e-15
+    assert abs(oracle.l2_error(u, ue, dx) - np.sqrt(np.sum((np.abs(u - ue) * dx) ** 2))) < 1e-15
+    assert abs(oracle.linf_error(u, ue, dx) - np.max(np.abs(u - ue) * dx)) < 1e-15
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3, 4])
+def test_advection_residual_exact_for_polynomials(oracle, deg):
+    """For a global polynomial of degree <= deg the face traces agree, the
+    Roe flux is the physical flux, the corrections vanish and the residual is
+    exactly -a u'(x) on interior elements."""
+    ps = oracle.Space1D(-1, 1, 12, deg)
+    c = np.random.default_rng(deg).standard_normal(deg + 1)
+    u = np.polynomial.polynomial.polyval(ps.xpg, c)
+    du_exact = -0.7 * np.polynomial.polynomial.polyval(ps.xpg, np.polynomial.polynomial.polyder(c))
+    P = oracle.Problem(oracle.ADVECTION, ps, a=0.7, bc=oracle.BC_DIRICHLET)
+    du = P.rhs(u)
+    np.testing.assert_allclose(du[1:-1], du_exact[1:-1], atol=1e-11)
+    assert np.all(du[0] == 0) and np.all(du[-1] == 0)
+
+
+def test_euler2d_residual_exact_for_linear_density(oracle):
+    """Uniform velocity and pressure make the Euler flux linear in density:
+    for a density linear in x and y the residual is exact,
+    d(rho)/dt = -(u rho_x + v rho_y)."""
+    ps = oracle.Space2D(0, 1, 6, 0, 1, 5, 3)
+    g, U, V, p = 1.4, 0.8, -0.3, 1.0
+    X, Y = ps.xpg[..., 0], ps.xpg[..., 1]
+    rho = 2.0 + 0.3 * X - 0.2 * Y
+    u = np.zeros((6, 5, 4, 4, 4), order="F")
+    u[..., 0] = rho
+    u[..., 1] = rho * U
+    u[..., 2] = rho * V
+    u[..., 3] = p / (g - 1) + 0.5 * rho * (U * U + V * V)
+    P = oracle.Problem(oracle.EULER2D, ps, flux=oracle.FLUX_HLL, gamma=g,
+                       bcs=[oracle.BC_COPY] * 4)
+    du = P.rhs(u)
+    drho = -(U * 0.3 + V * -0.2)
+    inner = (slice(1, -1), slice(1, -1))
+    np.testing.assert_allclose(du[inner][..., 0], drho, atol=1e-11)
+    np.testing.assert_allclose(du[inner][..., 1], drho * U, atol=1e-11)
+    np.testing.assert_allclose(du[inner][..., 3], drho * 0.5 * (U * U + V * V), atol=1e-11)
+
+
+def test_advection_sine_one_period(oracle):
+    """Config 1 (periodic [0,1], 100 elements, p=2, Radau, SSPRK3 at CFL 0.1 to
+    t=1): the wave returns to its initial condition up to the scheme error."""
+    ps = oracle.Space1D(0, 1, 100, 2)
+    u0 = np.sin(2 * np.pi * ps.xpg)
+    P = oracle.Problem(oracle.ADVECTION, ps, a=1.0)
+    dt = 0.1 * 0.01
+    u1 = P.ssprk3(u0, dt, 1000)
+    assert np.max(np.abs(u1 - u0)) < 5e-6
+    # mass is conserved to round-off
+    assert abs(np.sum(u1 @ ps.wp) - np.sum(u0 @ ps.wp)) < 1e-12
+
+
+def test_euler1d_density_wave_convergence(oracle):
+    """example/euler1d_convergence.jl:58-150 setup (p=3, gamma=5/3, density
+    wave with u = p = 1): the error falls at about order p+1."""
+    errs = []
+    for ne in (8, 16, 32):
+        ps = oracle.Space1D(0, 1, ne, 3)
+        g = 5 / 3
+        rho = 1 + 0.2 * np.sin(2 * np.pi * ps.xpg)
+        u = np.zeros((ne, 4, 3), order="F")
+        u[..., 0] = rho
+        u[..., 1] = rho
+        u[..., 2] = 1 / (g - 1) + 0.5 * rho
+        P = oracle.Problem(oracle.EULER1D, ps, gamma=g, flux=oracle.FLUX_HLL)
+        dt = 0.08 * (1 / ne) / 2.5
+        n = int(round(0.2 / dt))
+        dt = 0.2 / n
+        u1 = P.ssprk3(u, dt, n)
+        exact = 1 + 0.2 * np.sin(2 * np.pi * (ps.xpg - 0.2))
+        errs.append(np.max(np.abs(u1[..., 0] - exact)))
+    rates = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
+    assert np.all(rates > 3.3), (errs, rates)
+
+
+def test_euler2d_conservation_periodic(oracle):
+    ps = oracle.Space2D(0, 1, 8, 0, 1, 8, 2)
+    g = 1.4
+    X, Y = ps.xpg[..., 0], ps.xpg[..., 1]
+    rho = 1 + 0.2 * np.sin(2 * np.pi * (X + Y))
+    u = np.zeros((8, 8, 3, 3, 4), order="F")
+    u[..., 0] = rho
+    u[..., 1] = rho
+    u[..., 2] = rho
+    u[..., 3] = 1 / (g - 1) + rho
+    P = oracle.Problem(oracle.EULER2D, ps, flux=oracle.FLUX_LF, gamma=g)
+    s0 = P.conserved_sums2d(u)
+    u1 = P.ssprk3(u, 2e-3, 20)
+    np.testing.assert_allclose(P.conserved_sums2d(u1), s0, rtol=0, atol=1e-13)
+
+
+def test_bgk_moments_conserved(oracle):
+    """The BGK relaxation conserves mass; the transport is conservative."""
+    ps = oracle.Space1D(0, 1, 16, 3)
+    nv = 64
+    dv = 16 / nv
+    v = -8 + (np.arange(nv) + 0.5) * dv
+    w = np.full(nv, dv)
+    rho = 1 + 0.1 * np.sin(2 * np.pi * ps.xpg)
+    f = np.zeros((16, nv, 4), order="F")
+    for k in range(4):
+        f[:, :, k] = rho[:, k, None] * np.sqrt(1 / np.pi) * np.exp(-(v[None, :] - 1) ** 2)
+    P = oracle.Problem(oracle.BGK1D, ps, tau=1e-2, velo=v, weights=w)
+    mass0 = np.einsum("ivk,v,k->", f, w, ps.wp)
+    f1 = P.ssprk3(f, 1e-4, 20)
+    mass1 = np.einsum("ivk,v,k->", f1, w, ps.wp)
+    assert abs(mass1 - mass0) < 1e-12
+
+
+def test_mlp_gradient_matches_finite_difference(oracle):
+    rng = np.random.default_rng(1)
+    nin, nh = 32, 64
+    n_params = nh * nin + nh + nh * nh + nh + nh + 1
+    P = rng.standard_normal(n_params) * 0.2
+    x = rng.standard_normal((5, nin))
+    t = (rng.random(5) > 0.5).astype(np.float64)
+    loss, g = oracle.mlp_loss_grad(P, x, t)
+    for idx in rng.choice(n_params, 12, replace=False):
+        e = np.zeros(n_params)
+        e[idx] = 1e-6
+        lp, _ = oracle.mlp_loss_grad(P + e, x, t)
+        lm, _ = oracle.mlp_loss_grad(P - e, x, t)
+        assert abs((lp - lm) / 2e-6 - g[idx]) < 1e-7 * max(1, abs(g[idx]))

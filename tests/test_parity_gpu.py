@@ -1,0 +1,344 @@
+"""Parity of libfrgpu.so (CUDA, through the C ABI) with the CPU FP64 oracle.
+
+Tolerances: the plain FP64 path must match the oracle to 1e-12 relative
+(max |gpu - oracle| / max |oracle|), residual and time stepping alike; the
+FP32 compensated path (FP32K) is held to the per-test tolerances stated below.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL64 = 1e-12
+
+
+def rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(b)), 1e-300))
+
+
+def wave2d(xpg, g=1.4, amp=0.2):
+    X, Y = xpg[..., 0], xpg[..., 1]
+    rho = 1 + amp * np.sin(2 * np.pi * (X + Y))
+    u = np.zeros(X.shape + (4,), order="F")
+    u[..., 0] = rho
+    u[..., 1] = rho
+    u[..., 2] = rho
+    u[..., 3] = 1 / (g - 1) + rho
+    return u
+
+
+def vortex2d(xpg, g=1.4, eps=0.3, shock=True):
+    """Stationary normal shock at x = 0.5 and an isentropic vortex at (0.25, 0.5)."""
+    X, Y = xpg[..., 0], xpg[..., 1]
+    Ma = 1.1
+    c1 = math.sqrt(g)
+    u1 = Ma * c1
+    M2 = Ma * Ma
+    rr = (g + 1) * M2 / ((g - 1) * M2 + 2)
+    pr = 1 + 2 * g / (g + 1) * (M2 - 1)
+    r = np.hypot(X - 0.25, Y - 0.5)
+    tau = r / 0.075
+    a = 0.204
+    du = eps * tau * np.exp(a * (1 - tau ** 2)) * (Y - 0.5) / np.maximum(r, 1e-30)
+    dv = -eps * tau * np.exp(a * (1 - tau ** 2)) * (X - 0.25) / np.maximum(r, 1e-30)
+    dT = -(g - 1) * eps ** 2 / (4 * a * g) * np.exp(2 * a * (1 - tau ** 2))
+    T = 1 + dT
+    rho = T ** (1 / (g - 1))
+    p = rho * T
+    U, V = u1 + du, dv
+    if shock:
+        post = X > 0.5
+        rho = np.where(post, rr, rho)
+        p = np.where(post, pr, p)
+        U = np.where(post, u1 / rr, U)
+        V = np.where(post, 0.0, V)
+    w = np.zeros(X.shape + (4,), order="F")
+    w[..., 0] = rho
+    w[..., 1] = rho * U
+    w[..., 2] = rho * V
+    w[..., 3] = p / (g - 1) + 0.5 * rho * (U * U + V * V)
+    return w, (1.0, u1, 0.0, 1.0)
+
+
+# ---------------------------------------------------------------- stateless operators
+def test_interp_face_and_poly_derivative(frgpu):
+    rng = np.random.default_rng(0)
+    ps = frgpu.FRPSpace1D(0, 1, 20, 5)
+    f = rng.standard_normal((5, 6))
+    fd = np.zeros((5, 2))
+    frgpu.interp_face_(fd, f, ps.ll, ps.lr)
+    np.testing.assert_allclose(fd[:, 0], f @ ps.ll, rtol=0, atol=1e-14)
+    np.testing.assert_allclose(fd[:, 1], f @ ps.lr, rtol=0, atol=1e-14)
+    v = rng.standard_normal(6)
+    fv = np.zeros(2)
+    frgpu.interp_face_(fv, v, ps.ll, ps.lr)
+    assert abs(fv[0] - v @ ps.ll) < 1e-14 and abs(fv[1] - v @ ps.lr) < 1e-14
+    df = np.zeros_like(f)
+    frgpu.poly_derivative_(df, f, ps.dl)
+    np.testing.assert_allclose(df, f @ ps.dl.T, atol=1e-13)
+    # empty input is a no-op
+    frgpu.interp_face_(np.zeros((0, 2)), np.zeros((0, 6)), ps.ll, ps.lr)
+
+
+# ---------------------------------------------------------------- 1D scalar
+def test_config1_advection_matches_oracle(frgpu, oracle):
+    """Config 1: periodic [0,1], 100 elements, p=2, Radau, Roe/upwind flux,
+    u0 = sin(2 pi x), SSPRK3 at CFL 0.1 to t = 1, FP64."""
+    ps = frgpu.FRPSpace1D(0, 1, 100, 2)
+    po = oracle.Space1D(0, 1, 100, 2)
+    u0 = np.sin(2 * np.pi * ps.xpg)
+    prob = frgpu.FRAdvectionProblem(u0, (0.0, 1.0), ps, 1.0, "period")
+    P = oracle.Problem(oracle.ADVECTION, po, a=1.0)
+    assert rel(prob.rhs(u0), P.rhs(u0)) < RTOL64
+    dt = 0.1 * 0.01
+    itg = frgpu.init(prob, frgpu.SSPRK33(), dt=dt)
+    frgpu.step_(itg, 1000)
+    ref = P.ssprk3(u0, dt, 1000)
+    assert rel(itg.u, ref) < RTOL64
+    assert np.max(np.abs(itg.u - u0)) < 5e-6
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("bc", ["period", "dirichlet"])
+def test_scalar_residual_and_steps(frgpu, oracle, deg, bc):
+    rng = np.random.default_rng(deg)
+    ne = 300 + 17 * deg  # several CTAs, ragged last one
+    ps = frgpu.FRPSpace1D(0, 2 * math.pi, ne, deg)
+    po = oracle.Space1D(0, 2 * math.pi, ne, deg)
+    k = np.arange(1, 9)
+    a = rng.normal(0, 0.3, 8)
+    ph = rng.uniform(0, 2 * math.pi, 8)
+    u0 = np.sum(a[:, None, None] * np.sin(k[:, None, None] * ps.xpg[None] + ph[:, None, None]), axis=0)
+    bcode = oracle.BC_PERIODIC if bc == "period" else oracle.BC_DIRICHLET
+    for eq, ofn in (("adv", oracle.ADVECTION), ("burgers", oracle.BURGERS)):
+        if eq == "adv":
+            prob = frgpu.FRAdvectionProblem(u0, (0, 1), ps, 1.3, bc)
+        else:
+            prob = frgpu.FRBurgersProblem(u0, (0, 1), ps, bc)
+        P = oracle.Problem(ofn, po, a=1.3, bc=bcode)
+        assert rel(prob.rhs(u0), P.rhs(u0)) < RTOL64, eq
+        dt = 0.05 * (2 * math.pi / ne) / 2.0
+        itg = frgpu.init(prob, dt=dt)
+        itg.step(40)
+        assert rel(itg.u, P.ssprk3(u0, dt, 40)) < RTOL64, eq
+
+
+# ---------------------------------------------------------------- 1D Euler
+@pytest.mark.parametrize("bc", ["period", "dirichlet"])
+@pytest.mark.parametrize("deg", [2, 3, 5])
+def test_euler1d_matches_oracle(frgpu, oracle, bc, deg):
+    ne = 260
+    g = 5 / 3
+    ps = frgpu.FRPSpace1D(0, 1, ne, deg)
+    po = oracle.Space1D(0, 1, ne, deg)
+    rho = 1 + 0.2 * np.sin(2 * np.pi * ps.xpg)
+    if bc == "dirichlet":  # Sod-like jump smoothed over a few elements
+        rho = 1 - 0.875 * 0.5 * (1 + np.tanh((ps.xpg - 0.5) / 0.02))
+    u = np.zeros((ne, deg + 1, 3), order="F")
+    u[..., 0] = rho
+    u[..., 1] = 0.3 * rho
+    u[..., 2] = 1 / (g - 1) + 0.5 * 0.09 * rho
+    prob = frgpu.FREulerProblem(u, (0, 1), ps, g, bc)
+    P = oracle.Problem(oracle.EULER1D, po, gamma=g, flux=oracle.FLUX_HLL,
+                       bc=oracle.BC_PERIODIC if bc == "period" else oracle.BC_DIRICHLET)
+    assert rel(prob.rhs(u), P.rhs(u)) < RTOL64
+    dt = 0.05 * (1 / ne) / 2.0
+    itg = frgpu.init(prob, dt=dt)
+    itg.step(30)
+    assert rel(itg.u, P.ssprk3(u, dt, 30)) < RTOL64
+
+
+# ---------------------------------------------------------------- 2D Euler
+@pytest.mark.parametrize("deg", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("flux", ["lf", "hll"])
+def test_euler2d_periodic_matches_oracle(frgpu, oracle, deg, flux):
+    nx, ny = 37, 11  # ragged tiles in both directions
+    ps = frgpu.FRPSpace2D(0, 1, nx, 0, 1, ny, deg)
+    po = oracle.Space2D(0, 1, nx, 0, 1, ny, deg)
+    u = wave2d(ps.xpg)
+    prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux=flux, bc="period")
+    P = oracle.Problem(oracle.EULER2D, po, gamma=1.4,
+                       flux=oracle.FLUX_LF if flux == "lf" else oracle.FLUX_HLL)
+    assert rel(prob.rhs(u), P.rhs(u)) < RTOL64
+    dt = 0.05 / ((2.33) / ps.dx + 2.33 / ps.dy)
+    itg = frgpu.init(prob, dt=dt)
+    itg.step(15)
+    assert rel(itg.u, P.ssprk3(u, dt, 15)) < RTOL64
+
+
+@pytest.mark.parametrize("deg", [2, 3])
+def test_euler2d_shock_vortex_bcs_match_oracle(frgpu, oracle, deg):
+    """Copy (zero-gradient) and fixed inflow ghosts as in shock-vortex.jl:323-330, HLL."""
+    nx, ny = 70, 35
+    ps = frgpu.FRPSpace2D(0, 2, nx, 0, 1, ny, deg)
+    po = oracle.Space2D(0, 2, nx, 0, 1, ny, deg)
+    u, inflow_prim = vortex2d(ps.xpg)
+    rho, U, V, p = inflow_prim
+    inflow = [rho, rho * U, rho * V, p / 0.4 + 0.5 * rho * U * U]
+    fixed = [inflow, None, None, None]
+    prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="hll", bc=("fix", "copy", "copy", "copy"),
+                                  fixed_states=fixed)
+    P = oracle.Problem(oracle.EULER2D, po, gamma=1.4, flux=oracle.FLUX_HLL,
+                       bcs=[oracle.BC_FIXED, oracle.BC_COPY, oracle.BC_COPY, oracle.BC_COPY],
+                       fixed_states=[inflow, [0] * 4, [0] * 4, [0] * 4])
+    assert rel(prob.rhs(u), P.rhs(u)) < RTOL64
+    dt = 0.05 / (3.0 / ps.dx + 1.5 / ps.dy)
+    itg = frgpu.init(prob, dt=dt)
+    itg.step(10)
+    assert rel(itg.u, P.ssprk3(u, dt, 10)) < RTOL64
+
+
+def test_euler2d_conservation_and_determinism(frgpu):
+    ps = frgpu.FRPSpace2D(0, 1, 64, 0, 1, 48, 3)
+    u = wave2d(ps.xpg)
+    prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf")
+    itg = frgpu.init(prob, dt=1e-3)
+    s0, _ = itg.reduce()
+    itg.step(50)
+    s1, _ = itg.reduce()
+    np.testing.assert_allclose(s1, s0, rtol=0, atol=1e-13 * np.abs(s0).max())
+    a = itg.u
+    itg2 = frgpu.init(prob, dt=1e-3)
+    itg2.step(50)
+    assert np.array_equal(a, itg2.u)
+
+
+def test_euler2d_reductions_match_oracle(frgpu, oracle):
+    ps = frgpu.FRPSpace2D(0, 1, 24, 0, 1, 20, 3)
+    po = oracle.Space2D(0, 1, 24, 0, 1, 20, 3)
+    u = wave2d(ps.xpg)
+    prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf")
+    P = oracle.Problem(oracle.EULER2D, po, gamma=1.4, flux=oracle.FLUX_LF)
+    itg = frgpu.init(prob, dt=1e-3)
+    sums, smax = itg.reduce()
+    np.testing.assert_allclose(sums, P.conserved_sums2d(u), rtol=1e-13)
+    assert abs(smax - P.max_speed2d(u)) < 1e-13
+    # CFL time step: cfl / max((|u|+c)/dx + (|v|+c)/dy)
+    X = u
+    U = X[..., 1] / X[..., 0]
+    V = X[..., 2] / X[..., 0]
+    pr = 0.4 * (X[..., 3] - 0.5 * (X[..., 1] * U + X[..., 2] * V))
+    c = np.sqrt(1.4 * pr / X[..., 0])
+    rate = np.max((np.abs(U) + c) / ps.dx + (np.abs(V) + c) / ps.dy)
+    assert abs(itg.cfl_dt(0.1) - 0.1 / rate) < 1e-15
+
+
+# ---------------------------------------------------------------- FP32 compensated form
+def test_euler2d_fp32k_close_to_fp64(frgpu, oracle):
+    """FP32 residual + compensated stage combination: within 2e-6 relative of
+    the FP64 oracle after 60 steps of the density wave (64 x 64, p = 3)."""
+    ps = frgpu.FRPSpace2D(0, 1, 64, 0, 1, 64, 3)
+    po = oracle.Space2D(0, 1, 64, 0, 1, 64, 3)
+    u = wave2d(ps.xpg)
+    dt = 0.1 / (2 * 2.33 / ps.dx)
+    prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf", precision="fp32k")
+    itg = frgpu.init(prob, dt=dt)
+    itg.step(60)
+    P = oracle.Problem(oracle.EULER2D, po, gamma=1.4, flux=oracle.FLUX_LF)
+    ref = P.ssprk3(u, dt, 60)
+    assert rel(itg.u, ref) < 2e-6
+    # residual alone in FP32
+    assert rel(prob.rhs(u), P.rhs(u)) < 5e-4
+
+
+@pytest.mark.parametrize("deg", [1, 3, 5])
+def test_burgers_fp32k_close_to_fp64(frgpu, oracle, deg):
+    ne = 512
+    ps = frgpu.FRPSpace1D(0, 2 * math.pi, ne, deg)
+    po = oracle.Space1D(0, 2 * math.pi, ne, deg)
+    u0 = 0.5 * np.sin(ps.xpg) + 0.2 * np.cos(3 * ps.xpg)
+    dt = 0.05 * (2 * math.pi / ne) / 0.7
+    prob = frgpu.FRBurgersProblem(u0, (0, 1), ps, "period", precision="fp32k")
+    itg = frgpu.init(prob, dt=dt)
+    itg.step(100)
+    P = oracle.Problem(oracle.BURGERS, po)
+    assert rel(itg.u, P.ssprk3(u0, dt, 100)) < 2e-6
+
+
+# ---------------------------------------------------------------- BGK
+@pytest.mark.parametrize("precision,tol", [("fp64", RTOL64), ("fp32k", 2e-5)])
+def test_bgk_matches_oracle(frgpu, oracle, precision, tol):
+    ne, nv, deg = 64, 96, 3
+    ps = frgpu.FRPSpace1D(0, 1, ne, deg)
+    po = oracle.Space1D(0, 1, ne, deg)
+    dv = 16 / nv
+    v = -8 + (np.arange(nv) + 0.5) * dv
+    w = np.full(nv, dv)
+    rho = 1 + 0.1 * np.sin(2 * np.pi * ps.xpg)
+    f = np.zeros((ne, nv, deg + 1), order="F")
+    for k in range(deg + 1):
+        f[:, :, k] = rho[:, k, None] * np.sqrt(1 / np.pi) * np.exp(-(v[None, :] - 1) ** 2)
+    prob = frgpu.FRBGKProblem(f, (0, 1), ps, v, w, 1e-2, precision=precision)
+    P = oracle.Problem(oracle.BGK1D, po, tau=1e-2, velo=v, weights=w)
+    if precision == "fp64":
+        assert rel(prob.rhs(f), P.rhs(f)) < RTOL64
+    dt = 0.1 * (1 / ne) / 8
+    itg = frgpu.init(prob, dt=dt)
+    itg.step(25)
+    assert rel(itg.u, P.ssprk3(f, dt, 25)) < tol
+
+
+# ---------------------------------------------------------------- indicator + filter
+def test_filter2d_matches_oracle(frgpu, oracle):
+    ps = frgpu.FRPSpace2D(0, 2, 80, 0, 1, 40, 3)
+    po = oracle.Space2D(0, 2, 80, 0, 1, 40, 3)
+    u, _ = vortex2d(ps.xpg)
+    prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="hll", bc="copy")
+    itg = frgpu.init(prob, dt=1e-4)
+    S0 = -3 * math.log10(3)
+    n = itg.modal_filter("plain", 5e-4, S0, 9.0)
+    P = oracle.Problem(oracle.EULER2D, po, gamma=1.4, flux=oracle.FLUX_HLL, bc=oracle.BC_COPY)
+    ref, flags, nref = P.filter2d(u, 5e-4, S0, 9.0)
+    assert n == nref and n > 0
+    assert np.array_equal(itg.troubled().reshape(80, 40, order="F"), flags)
+    assert rel(itg.u, ref) < RTOL64
+
+
+def test_filter_inside_step_graph(frgpu, oracle):
+    ps = frgpu.FRPSpace2D(0, 2, 40, 0, 1, 20, 3)
+    po = oracle.Space2D(0, 2, 40, 0, 1, 20, 3)
+    u, inflow_prim = vortex2d(ps.xpg)
+    rho, U, V, p = inflow_prim
+    inflow = [rho, rho * U, rho * V, p / 0.4 + 0.5 * rho * U * U]
+    prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="hll", bc=("fix", "copy", "copy", "copy"),
+                                  fixed_states=[inflow, None, None, None])
+    P = oracle.Problem(oracle.EULER2D, po, gamma=1.4, flux=oracle.FLUX_HLL,
+                       bcs=[oracle.BC_FIXED, oracle.BC_COPY, oracle.BC_COPY, oracle.BC_COPY],
+                       fixed_states=[inflow, [0] * 4, [0] * 4, [0] * 4])
+    dt = 2e-4
+    S0 = -3 * math.log10(3)
+    itg = frgpu.init(prob, dt=dt)
+    itg.set_filter("plain", 5e-4, S0, 9.0)
+    ref = u.copy(order="F")
+    for _ in range(5):
+        itg.step(1)
+        ref = P.ssprk3(ref, dt, 1)
+        ref, _, _ = P.filter2d(ref, 5e-4, S0, 9.0)
+    assert rel(itg.u, ref) < RTOL64
+
+
+# ---------------------------------------------------------------- failure detection
+def test_nonfinite_and_unphysical_states_are_reported(frgpu):
+    ps = frgpu.FRPSpace2D(0, 1, 16, 0, 1, 16, 2)
+    u = wave2d(ps.xpg)
+    prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf")
+    bad = u.copy(order="F")
+    bad[3, 4, 1, 1, 0] = np.nan
+    with pytest.raises(frgpu.FRGPUError) as e:
+        prob.rhs(bad)
+    assert e.value.code == -3
+    neg = u.copy(order="F")
+    neg[5, 5, :, :, 0] = -1.0
+    itg = frgpu.init(prob, dt=1e-3)
+    itg.u = neg
+    with pytest.raises(frgpu.FRGPUError) as e:
+        itg.step(1)
+    assert e.value.code in (-3, -4)
+    # the problem stays usable afterwards
+    itg.u = u
+    itg.step(1)
+    with pytest.raises(frgpu.FRGPUError) as e:
+        itg.step(1, dt=-1.0)
+    assert e.value.code == -5
