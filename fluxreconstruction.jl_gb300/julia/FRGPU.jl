@@ -1,0 +1,186 @@
+"""
+    FRGPU
+
+Julia binding of libfrgpu.so (include/frgpu.h) for FluxReconstruction.jl users.
+It keeps the reference's signatures for the residual / time-stepping hot path:
+
+* `FRGPU.FRAdvectionProblem(u, tspan, ps, a, bc)` and
+  `FRGPU.FREulerProblem(u, tspan, ps, γ, bc)` take the reference's own
+  `FRPSpace1D` (src/struct.jl:13-88) and return an `ODEProblem` whose
+  `rhs!(du, u, p, t)` runs on the GPU (src/Equation/eq_advection.jl:1-26,
+  src/Equation/eq_euler.jl:1-27);
+* `FRGPU.FREuler2DProblem(u, tspan, ps, γ; flux, bc, fixed)` takes the
+  reference's `FRPSpace2D` (src/struct.jl:99-245) and stands in for the `dudt!`
+  closure of example/shock-vortex.jl:26-118;
+* `FRGPU.interp_face!(fδ, f, ll, lr)` (src/interpolate.jl:1-10);
+* `FRGPU.init(prob, FRGPU.SSPRK33(); dt)` + `FRGPU.step!(itg)` + `itg.u` keep the
+  state on the device between steps (OrdinaryDiffEq's init/step! API).
+
+The library path comes from `ENV["FRGPU_LIB"]` (default: next to this file's
+package, `../libfrgpu.so`).
+"""
+module FRGPU
+
+using OrdinaryDiffEq: ODEProblem
+
+const libfrgpu = get(ENV, "FRGPU_LIB", joinpath(@__DIR__, "..", "libfrgpu.so"))
+
+const ADVECTION, BURGERS, EULER1D, EULER2D, BGK1D = Cint(0), Cint(1), Cint(2), Cint(3), Cint(4)
+const FLUX = Dict(:roe => Cint(0), :lf => Cint(1), :hll => Cint(2), :upwind => Cint(3))
+const BC = Dict(:period => Cint(0), :copy => Cint(1), :fix => Cint(2), :dirichlet => Cint(3))
+const PRECISION = Dict(:fp64 => Cint(0), :fp32k => Cint(1))
+
+# mirror of frgpu_problem_desc (include/frgpu.h)
+struct ProblemDesc
+    equation::Cint
+    flux::Cint
+    precision::Cint
+    bc::NTuple{4,Cint}
+    fixed_state::NTuple{16,Cdouble}
+    a::Cdouble
+    gamma::Cdouble
+    tau::Cdouble
+    nvel::Cint
+    velo::Ptr{Cdouble}
+    weights::Ptr{Cdouble}
+    eps_interior::Cdouble
+    eps_periodic::Cdouble
+end
+
+function check(rc::Cint)
+    if rc < 0
+        buf = Vector{UInt8}(undef, 1024)
+        ccall((:frgpu_last_error, libfrgpu), Cint, (Ptr{UInt8}, Culong), buf, length(buf))
+        error("frgpu error $rc: " * unsafe_string(pointer(buf)))
+    end
+    return rc
+end
+
+mutable struct Space
+    h::Ptr{Cvoid}
+end
+
+"""Device copy of the operators of a reference FRPSpace1D (src/struct.jl:40-85)."""
+function Space(ps1d)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:frgpu_space_create_1d_ops, libfrgpu), Cint,
+                (Cint, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble},
+                 Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ref{Ptr{Cvoid}}),
+                length(ps1d.J), ps1d.deg, collect(Float64, ps1d.J), collect(Float64, ps1d.ll),
+                collect(Float64, ps1d.lr), Matrix{Float64}(ps1d.dl), collect(Float64, ps1d.dhl),
+                collect(Float64, ps1d.dhr), Matrix{Float64}(ps1d.V), Matrix{Float64}(ps1d.iV), r))
+    s = Space(r[])
+    finalizer(x -> ccall((:frgpu_space_destroy, libfrgpu), Cvoid, (Ptr{Cvoid},), x.h), s)
+    return s
+end
+
+"""Device copy of the operators of a reference FRPSpace2D on uniform rectangles."""
+function Space2D(ps2d)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    dx = ps2d.dx[1, 1]
+    dy = ps2d.dy[1, 1]
+    check(ccall((:frgpu_space_create_2d_ops, libfrgpu), Cint,
+                (Cint, Cint, Cint, Cdouble, Cdouble, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble},
+                 Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ref{Ptr{Cvoid}}),
+                ps2d.nx, ps2d.ny, ps2d.deg, dx, dy, collect(Float64, ps2d.ll), collect(Float64, ps2d.lr),
+                Matrix{Float64}(ps2d.dl), collect(Float64, ps2d.dhl), collect(Float64, ps2d.dhr),
+                Matrix{Float64}(ps2d.V), Matrix{Float64}(ps2d.iV), r))
+    s = Space(r[])
+    finalizer(x -> ccall((:frgpu_space_destroy, libfrgpu), Cvoid, (Ptr{Cvoid},), x.h), s)
+    return s
+end
+
+mutable struct Problem
+    h::Ptr{Cvoid}
+    space::Space
+    dims::Tuple
+end
+
+function Problem(space::Space, d::ProblemDesc, dims)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:frgpu_problem_create, libfrgpu), Cint, (Ptr{Cvoid}, Ref{ProblemDesc}, Ref{Ptr{Cvoid}}),
+                space.h, d, r))
+    p = Problem(r[], space, dims)
+    finalizer(x -> ccall((:frgpu_problem_destroy, libfrgpu), Cvoid, (Ptr{Cvoid},), x.h), p)
+    return p
+end
+
+desc(eq, flux, prec, bcs; a=1.0, γ=1.4, τ=1.0, fixed=zeros(16)) = ProblemDesc(eq, flux, prec, bcs,
+    NTuple{16,Cdouble}(fixed), a, γ, τ, 0, C_NULL, C_NULL, 1e-8, 1e-6)
+
+"""rhs!(du, u, p, t) on the GPU: frgpu_rhs (one host->device and one device->host copy)."""
+function rhs!(du, u, p::Problem, t)
+    uh = Array{Float64}(u)
+    dh = similar(uh)
+    check(ccall((:frgpu_rhs, libfrgpu), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Cdouble),
+                p.h, dh, uh, t))
+    du .= dh
+    return nothing
+end
+
+"""FRAdvectionProblem(u, tspan, ps, a, bc) of src/Equation/eq_advection.jl:1-26."""
+function FRAdvectionProblem(u::AbstractMatrix, tspan, ps, a, bc::Symbol; precision=:fp64)
+    p = Problem(Space(ps), desc(ADVECTION, FLUX[:roe], PRECISION[precision], ntuple(_ -> BC[bc], 4); a=a), size(u))
+    return ODEProblem(rhs!, Array{Float64}(u), tspan, p)
+end
+
+"""FREulerProblem(u, tspan, ps, γ, bc) of src/Equation/eq_euler.jl:1-27 (HLL flux)."""
+function FREulerProblem(u::AbstractArray{<:Real,3}, tspan, ps, γ, bc::Symbol; precision=:fp64)
+    p = Problem(Space(ps), desc(EULER1D, FLUX[:hll], PRECISION[precision], ntuple(_ -> BC[bc], 4); γ=γ), size(u))
+    return ODEProblem(rhs!, Array{Float64}(u), tspan, p)
+end
+
+"""The `dudt!` of example/shock-vortex.jl:26-118 on the interior u[1:nx, 1:ny, :, :, :];
+`bc` = (left, right, bottom, top) kinds, `fixed` the 4x4 conserved ghost states."""
+function FREuler2DProblem(u::AbstractArray{<:Real,5}, tspan, ps, γ; flux=:hll, bc=(:period, :period, :period, :period),
+                          fixed=zeros(16), precision=:fp64)
+    bcs = ntuple(i -> BC[bc[i]], 4)
+    p = Problem(Space2D(ps), desc(EULER2D, FLUX[flux], PRECISION[precision], bcs; γ=γ, fixed=fixed), size(u))
+    return ODEProblem(rhs!, Array{Float64}(u), tspan, p)
+end
+
+"""interp_face!(fδ, f, ll, lr) of src/interpolate.jl:1-10, evaluated on the GPU."""
+function interp_face!(fδ, f::AbstractMatrix, ll, lr)
+    fh = Matrix{Float64}(f)
+    out = zeros(size(f, 1), 2)
+    check(ccall((:frgpu_interp_face, libfrgpu), Cint,
+                (Ptr{Cdouble}, Clong, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}),
+                fh, size(f, 1), size(f, 2), collect(Float64, ll), collect(Float64, lr), out))
+    fδ .= out
+    return nothing
+end
+
+struct SSPRK33 end
+
+mutable struct Integrator
+    p::Problem
+    t::Float64
+    dt::Float64
+end
+
+"""init(prob, SSPRK33(); dt): upload u0 once; the state stays on the device."""
+function init(prob::ODEProblem, ::SSPRK33; dt, adaptive=false, kwargs...)
+    adaptive && error("FRGPU integrates with fixed dt")
+    p = prob.p::Problem
+    check(ccall((:frgpu_state_upload, libfrgpu), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), p.h, Array{Float64}(prob.u0)))
+    return Integrator(p, prob.tspan[1], dt)
+end
+
+"""step!(itg): one SSPRK3 step on the device (a captured CUDA graph)."""
+function step!(itg::Integrator, n::Integer=1)
+    check(ccall((:frgpu_step_ssprk3, libfrgpu), Cint, (Ptr{Cvoid}, Cdouble, Cint), itg.p.h, itg.dt, n))
+    itg.t += n * itg.dt
+    return nothing
+end
+
+function Base.getproperty(itg::Integrator, s::Symbol)
+    if s === :u
+        p = getfield(itg, :p)
+        out = zeros(p.dims)
+        check(ccall((:frgpu_state_download, libfrgpu), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), p.h, out))
+        return out
+    end
+    return getfield(itg, s)
+end
+
+end # module
