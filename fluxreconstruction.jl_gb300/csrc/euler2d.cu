@@ -1,4 +1,7 @@
 // euler2d.cu -- 2D Euler dispatch and the FP64 reductions (conserved sums, CFL).
+#include <mutex>
+#include <string>
+
 #include "fr_common.cuh"
 #include "frgpu_internal.h"
 
@@ -104,5 +107,101 @@ int fr_launch_euler2d_reduce(frgpu_problem *p, const void *state, const void *lo
         out_speed[0] = h[4];
         out_speed[1] = h[5];
     }
+    return FRGPU_OK;
+}
+
+// ---- allocation-free variant of the 2D reduction -----------------------------
+// Some callers cannot let this library call cudaMalloc: hosts that own every
+// device byte through their own pool (a Julia CUDA.jl or PyTorch caching
+// allocator that must see all device memory), and processes that fix their
+// device footprint at start-up.  frgpu_reduce2d_noalloc serves them: it runs
+// the same partial/final reduction kernels as frgpu_reduce, but its partial
+// sums live in the file-scope device array below instead of memory allocated
+// per problem.  The array is 4096 x 6 doubles (192 KiB); one partial block
+// covers up to NOALLOC_POINTS_PER_BLOCK solution points, so a call accepts at
+// most 4096 * 16384 = 67,108,864 solution points (nx * ny * (deg+1)^2) and
+// rejects larger meshes.  Every GPU that loads the library keeps the array
+// until the process exits.
+namespace {
+constexpr int NOALLOC_MAX_BLOCKS = 4096;
+constexpr long NOALLOC_POINTS_PER_BLOCK = (long)RED_THREADS * 64;
+constexpr int FR_MAX_DEVICES = 64;
+__device__ __align__(256) double g_noalloc_partials[NOALLOC_MAX_BLOCKS * 6];
+
+// Device address of g_noalloc_partials, looked up once per device (host code
+// cannot use the symbol itself: on the host it names a stand-in, not device memory).
+void *g_noalloc_addr[FR_MAX_DEVICES] = {};
+std::mutex g_noalloc_mu;
+
+int noalloc_scratch(double **out) {
+    int dev = 0;
+    FR_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= FR_MAX_DEVICES) {
+        fr_set_error("reduce2d_noalloc: device index out of range");
+        return FRGPU_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_partials);
+        if (e != cudaSuccess || ptr == nullptr) return fr_cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_partials)");
+        g_noalloc_addr[dev] = ptr;
+    }
+    *out = (double *)g_noalloc_addr[dev];
+    return FRGPU_OK;
+}
+
+// final pass of the allocation-free reduction: sums scaled by the element area
+__global__ void k_reduce_final_scaled(const double *__restrict__ part, int nblocks, double scale,
+                                      double *__restrict__ out) {
+    if (threadIdx.x < 6) {
+        const int v = threadIdx.x;
+        double x = part[v];
+        for (int b = 1; b < nblocks; ++b) x = v < 4 ? x + part[b * 6 + v] : fmax(x, part[b * 6 + v]);
+        out[v] = v < 4 ? x * scale : x;
+    }
+}
+} // namespace
+
+extern "C" FRGPU_API int frgpu_reduce2d_noalloc(const void *d_state, const void *d_lo, int precision, int nx, int ny,
+                                                int deg, double dx, double dy, double gamma, const double *d_wp,
+                                                double *d_out, void *stream) {
+    if (!d_state || !d_wp || !d_out) {
+        fr_set_error("reduce2d_noalloc: null device pointer");
+        return FRGPU_ERR_ARG;
+    }
+    if (precision != FRGPU_FP64 && precision != FRGPU_FP32K) {
+        fr_set_error("reduce2d_noalloc: unknown precision");
+        return FRGPU_ERR_ARG;
+    }
+    if (nx < 1 || ny < 1 || deg < 1 || deg > 5 || !(dx > 0) || !(dy > 0) || !(gamma > 1)) {
+        fr_set_error("reduce2d_noalloc: need nx, ny >= 1, 1 <= deg <= 5, dx, dy > 0 and gamma > 1");
+        return FRGPU_ERR_ARG;
+    }
+    const int np = deg + 1;
+    const size_t plane = (size_t)nx * ny;
+    const size_t npts = plane * np * np;
+    const long nblocks = (long)((npts + NOALLOC_POINTS_PER_BLOCK - 1) / NOALLOC_POINTS_PER_BLOCK);
+    if (nblocks > NOALLOC_MAX_BLOCKS) {
+        fr_set_error("reduce2d_noalloc: " + std::to_string(npts) + " solution points exceed the maximum of " +
+                     std::to_string((long)NOALLOC_MAX_BLOCKS * NOALLOC_POINTS_PER_BLOCK) +
+                     " that the static scratch array holds");
+        return FRGPU_ERR_ARG;
+    }
+    double *part = nullptr;
+    int rc = noalloc_scratch(&part);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    // each partial block overwrites its own six slots, so the previous call's
+    // contents never need clearing
+    if (precision == FRGPU_FP64)
+        k_reduce2d_partial<double><<<(int)nblocks, RED_THREADS, 0, st>>>(
+            (const double *)d_state, (const double *)d_lo, plane, np, d_wp, gamma, 1.0 / dx, 1.0 / dy, part);
+    else
+        k_reduce2d_partial<float><<<(int)nblocks, RED_THREADS, 0, st>>>(
+            (const float *)d_state, (const float *)d_lo, plane, np, d_wp, gamma, 1.0 / dx, 1.0 / dy, part);
+    FR_CUDA(cudaGetLastError());
+    k_reduce_final_scaled<<<1, 32, 0, st>>>(part, (int)nblocks, dx * dy * 0.25, d_out);
+    FR_CUDA(cudaGetLastError());
     return FRGPU_OK;
 }

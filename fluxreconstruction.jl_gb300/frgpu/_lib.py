@@ -69,6 +69,8 @@ SIGNATURES = {
     "frgpu_problem_stream": (C.c_int, [_VP, C.POINTER(_VP)]),
     "frgpu_problem_launches": (C.c_long, [_VP]),
     "frgpu_synchronize": (C.c_int, [_VP]),
+    "frgpu_reduce2d_noalloc": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                         C.c_double, _VP, _VP, _VP]),
     "frgpu_interp_face": (C.c_int, [_D, C.c_long, C.c_int, _D, _D, _D]),
     "frgpu_poly_derivative": (C.c_int, [_D, C.c_long, C.c_int, _D, _D]),
     "frgpu_last_error": (C.c_int, [C.c_char_p, C.c_ulong]),

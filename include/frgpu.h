@@ -166,6 +166,29 @@ FRGPU_API int frgpu_problem_stream(frgpu_problem *p, void **stream);
 FRGPU_API long frgpu_problem_launches(const frgpu_problem *p);
 FRGPU_API int frgpu_synchronize(frgpu_problem *p);
 
+/* Allocation-free 2D Euler reduction.  No counterpart in the reference: it
+ * exists for callers that cannot let this library call cudaMalloc -- hosts
+ * whose own pool (a Julia CUDA.jl or PyTorch caching allocator) must own every
+ * device byte, and processes that fix their device footprint at start-up.
+ * Inputs and outputs are the caller's device memory: the state d_state
+ * (u[nx, ny, deg+1, deg+1, 4] in the Julia layout; double for FRGPU_FP64,
+ * float for FRGPU_FP32K, with d_lo the optional float low part), the
+ * quadrature weights d_wp[(deg+1)^2] (wp[k + (deg+1) l] = w_k w_l), and d_out[6]
+ * receiving the FP64 conserved sums (4), the maximum wave speed and the
+ * maximum CFL rate max((|u|+c)/dx + (|v|+c)/dy) -- the values frgpu_reduce and
+ * frgpu_cfl_dt compute.  The work is queued on `stream` (NULL = legacy
+ * default stream) and nothing is synchronised.  Scratch is a fixed 192 KiB
+ * device array inside the library, held by every GPU that loads it until the
+ * process exits; meshes above 67,108,864 solution points (nx*ny*(deg+1)^2)
+ * are rejected with FRGPU_ERR_ARG.  No cudaMalloc/cudaFree is called.  The
+ * first call on each device looks up the array's device address, so make
+ * that first call before any stream capture.  All calls share the one array:
+ * calls that overlap on the GPU (different streams, or different host
+ * threads) race and must be serialised by the caller. */
+FRGPU_API int frgpu_reduce2d_noalloc(const void *d_state, const void *d_lo, int precision, int nx, int ny, int deg,
+                                     double dx, double dy, double gamma, const double *d_wp, double *d_out,
+                                     void *stream);
+
 /* ======================================================================
  * Stateless operators
  * ==================================================================== */

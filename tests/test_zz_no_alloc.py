@@ -1,0 +1,72 @@
+"""The allocation-free reduction entry point (frgpu_reduce2d_noalloc).
+
+It serves callers that cannot let the library call cudaMalloc (hosts whose
+own memory pool must own every device byte, or processes with a fixed device
+footprint): scratch comes from a static device array inside libfrgpu.so, and
+the caller passes device inputs and a device output.  Checked through the C
+ABI against the allocating entry points frgpu_reduce / frgpu_cfl_dt on the
+same state, two calls in a row on meshes of different sizes (so the second
+call runs on scratch the first one left behind), within the 1e-13 relative
+tolerance the other reduction tests use.  Kept in a file of its own, collected
+last.
+"""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-13
+
+
+def _problem(frgpu, nx, ny, deg, amp):
+    ps = frgpu.FRPSpace2D(0, 1, nx, 0, 1, ny, deg)
+    X, Y = ps.xpg[..., 0], ps.xpg[..., 1]
+    rho = 1 + amp * np.sin(2 * math.pi * (X + 2 * Y))
+    u = np.zeros(X.shape + (4,), order="F")
+    u[..., 0] = rho
+    u[..., 1] = 0.7 * rho
+    u[..., 2] = -0.4 * rho
+    u[..., 3] = 1 / 0.4 + 0.5 * rho * (0.49 + 0.16) + 0.1 * np.cos(2 * math.pi * X)
+    prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf", bc="period")
+    itg = frgpu.init(prob, dt=1e-4)
+    sums, speed = itg.reduce()
+    rate = 0.1 / itg.cfl_dt(0.1)
+    return ps, prob, itg, sums, speed, rate
+
+
+def test_reduce2d_noalloc_matches_allocating_reduce(frgpu):
+    import torch
+
+    from frgpu import _lib as L
+
+    lib = L.lib()
+    torch.cuda.set_device(0)
+    cases = [_problem(frgpu, 96, 80, 3, 0.2), _problem(frgpu, 20, 12, 2, 0.3)]
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for ps, prob, itg, sums, speed, rate in cases:
+        itg.synchronize()
+        ptr, eb = C.c_void_p(), C.c_int()
+        L.check(lib.frgpu_problem_device_state(prob._h, C.byref(ptr), C.byref(eb)))
+        assert eb.value == 8
+        wp = torch.tensor(np.asarray(ps.wp).ravel(order="F"), dtype=torch.float64, device="cuda")
+        out = torch.full((6,), float("nan"), dtype=torch.float64, device="cuda")
+        L.check(lib.frgpu_reduce2d_noalloc(ptr, None, L.FP64, ps.nx, ps.ny, ps.deg, ps.dx, ps.dy, 1.4,
+                                           C.c_void_p(wp.data_ptr()), C.c_void_p(out.data_ptr()), stream))
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        np.testing.assert_allclose(got[:4], sums, rtol=RTOL, atol=RTOL * np.abs(sums).max())
+        assert abs(got[4] - speed) <= RTOL * speed
+        assert abs(got[5] - rate) <= RTOL * rate
+
+
+def test_reduce2d_noalloc_rejects_meshes_beyond_its_scratch(frgpu):
+    from frgpu import _lib as L
+
+    lib = L.lib()
+    dummy = C.c_void_p(16)  # never dereferenced: the size check comes first
+    rc = lib.frgpu_reduce2d_noalloc(dummy, None, L.FP64, 8192, 8192, 3, 1e-4, 1e-4, 1.4, dummy, dummy, None)
+    assert rc == L.ERR_ARG
+    assert "exceed the maximum" in L.last_error()
