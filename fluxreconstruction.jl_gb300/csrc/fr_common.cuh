@@ -18,6 +18,19 @@ template <class Real> __device__ __forceinline__ Real sqrtR(Real a);
 template <> __device__ __forceinline__ double sqrtR<double>(double a) { return sqrt(a); }
 template <> __device__ __forceinline__ float sqrtR<float>(float a) { return sqrtf(a); }
 
+// Reciprocal and square root of the physics kernels: IEEE in FP64 (the
+// bit-exact path), hardware approximations in FP32 (MUFU.RCP / MUFU.RSQ,
+// about 2 ulp), whose error is part of the FP32 form's stated tolerance.
+template <class Real> __device__ __forceinline__ Real recipR(Real a);
+template <> __device__ __forceinline__ double recipR<double>(double a) { return 1.0 / a; }
+template <> __device__ __forceinline__ float recipR<float>(float a) { return __fdividef(1.0f, a); }
+template <class Real> __device__ __forceinline__ Real divR(Real a, Real b);
+template <> __device__ __forceinline__ double divR<double>(double a, double b) { return a / b; }
+template <> __device__ __forceinline__ float divR<float>(float a, float b) { return __fdividef(a, b); }
+template <class Real> __device__ __forceinline__ Real sqrtP(Real a); // a >= 0
+template <> __device__ __forceinline__ double sqrtP<double>(double a) { return sqrt(a); }
+template <> __device__ __forceinline__ float sqrtP<float>(float a) { return a > 0.0f ? a * rsqrtf(a) : 0.0f; }
+
 template <class Real> __device__ __forceinline__ Real absR(Real a) { return a < Real(0) ? -a : a; }
 template <class Real> __device__ __forceinline__ Real maxR(Real a, Real b) { return a > b ? a : b; }
 template <class Real> __device__ __forceinline__ Real minR(Real a, Real b) { return a < b ? a : b; }
@@ -46,7 +59,7 @@ template <class Real, int NP> struct Ops {
 template <class Real>
 __device__ __forceinline__ void euler2d_flux(const Real (&w)[4], Real gm1, Real iJx, Real iJy, Real (&f)[4],
                                              Real (&g)[4], int &bad) {
-    Real rinv = Real(1) / w[0];
+    Real rinv = recipR<Real>(w[0]);
     Real U = w[1] * rinv, V = w[2] * rinv;
     Real p = gm1 * (w[3] - Real(0.5) * fmaR<Real>(w[1], U, w[2] * V));
     Real Ep = w[3] + p;
@@ -65,7 +78,7 @@ __device__ __forceinline__ void euler2d_flux(const Real (&w)[4], Real gm1, Real 
 template <class Real, int DIR>
 __device__ __forceinline__ void euler2d_dirflux(const Real (&w)[4], Real gamma, Real gm1, Real (&f)[4], Real &un,
                                                 Real &c) {
-    Real rinv = Real(1) / w[0];
+    Real rinv = recipR<Real>(w[0]);
     Real U = w[1] * rinv, V = w[2] * rinv;
     Real p = gm1 * (w[3] - Real(0.5) * fmaR<Real>(w[1], U, w[2] * V));
     un = DIR == 0 ? U : V;
@@ -73,7 +86,7 @@ __device__ __forceinline__ void euler2d_dirflux(const Real (&w)[4], Real gamma, 
     f[1] = DIR == 0 ? fmaR<Real>(w[1], U, p) : w[1] * V;
     f[2] = DIR == 1 ? fmaR<Real>(w[2], V, p) : w[2] * U;
     f[3] = (w[3] + p) * un;
-    c = sqrtR<Real>(gamma * p * rinv);
+    c = sqrtP<Real>(gamma * p * rinv);
 }
 
 enum { FLUX_ROE = 0, FLUX_LF = 1, FLUX_HLL = 2, FLUX_UPWIND = 3 };
@@ -101,7 +114,7 @@ __device__ __forceinline__ void riemann2d(const Real (&wL)[4], const Real (&wR)[
 #pragma unroll
             for (int m = 0; m < 4; ++m) F[m] = fR[m];
         } else {
-            Real factor = Real(1) / (sr - sl);
+            Real factor = recipR<Real>(sr - sl);
 #pragma unroll
             for (int m = 0; m < 4; ++m) F[m] = factor * (sr * fL[m] - sl * fR[m] + sl * sr * (wR[m] - wL[m]));
         }

@@ -28,6 +28,17 @@ def _nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libfrgpu.so")
 
 
+def _extra_flags(src: str) -> list[str]:
+    """FP64 translation units (and the filter) contract no multiply-adds on
+    their own: their only fused operations are the explicit fma() calls,
+    which the oracle performs in the same order, so the FP64 path reproduces
+    the oracle bit for bit.  The FP32 units keep the default contraction."""
+    name = os.path.basename(src)
+    if name.endswith("_f64.cu") or name == "filter.cu":
+        return ["-fmad=false"]
+    return []
+
+
 def sources() -> list[str]:
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
@@ -51,7 +62,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for src in sources():
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         objs.append(obj)
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
+        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *_extra_flags(src), "-c", src, "-o", obj]
         if src.endswith(".cpp"):
             cmd[1:1] = ["-x", "cu"]
         if verbose:

@@ -3,9 +3,15 @@
  *
  * TEST INFRASTRUCTURE ONLY (the checker and the timed CPU baseline).  See
  * fr_oracle.h for the layout conventions and the parity status.  Every
- * function cites the reference file:line it restates.  Compiled with
- * -ffp-contract=off so that each operation rounds like the reference's Julia
- * code (Julia does not fuse multiply-adds unless asked to).
+ * function cites the reference file:line it restates.
+ *
+ * Rounding: the reference's dot products (`dot`, `u * ll`, `f * lpdm'`) go
+ * through BLAS, whose summation order and use of fused multiply-adds depend on
+ * the BLAS build and cannot be pinned.  The oracle fixes one order: every dot
+ * product is s = v0 w0, then s = fma(v_q, w_q, s) in ascending q (dotw below),
+ * and the few other fused multiply-adds are written out with fma().  It is
+ * compiled with -ffp-contract=off so that no other operation is fused; every
+ * other expression keeps the reference's operation order.
  */
 #include "fr_oracle.h"
 
@@ -32,6 +38,14 @@ int fro_get_threads(void) {
 #ifdef _OPENMP
 #define OMP_THREADS num_threads(fro_get_threads())
 #endif
+
+/* dot product of n values v[q*sv] with weights w[q*sw] in the fixed order
+ * s = v0 w0; s = fma(v_q, w_q, s) */
+static inline double dotw(const double *v, long sv, const double *w, long sw, int n) {
+    double s = v[0] * w[0];
+    for (int q = 1; q < n; ++q) s = fma(v[q * sv], w[q * sw], s);
+    return s;
+}
 
 /* ------------------------------------------------------------------------
  * Setup math
@@ -275,17 +289,17 @@ void fro_prim_conserve1d(const double *prim, double gamma, double *w) {
  * w, with velocity components and pressure computed once:
  * U = mx/rho, V = my/rho, p = (gamma-1)(E - 0.5 (mx U + my V)). */
 static inline void euler_flux_dir(const double *w, double gamma, int dir, double *f, double *un_out,
-                                  double *p_out) {
+                                  double *c_out) {
     double rinv = 1.0 / w[0];
     double U = w[1] * rinv, V = w[2] * rinv;
-    double p = (gamma - 1.0) * (w[3] - 0.5 * (w[1] * U + w[2] * V));
+    double p = (gamma - 1.0) * (w[3] - 0.5 * fma(w[1], U, w[2] * V));
     double un = dir == 0 ? U : V;
     f[0] = w[1 + dir];
-    f[1] = w[1] * un + (dir == 0 ? p : 0.0);
-    f[2] = w[2] * un + (dir == 1 ? p : 0.0);
+    f[1] = dir == 0 ? fma(w[1], U, p) : w[1] * V;
+    f[2] = dir == 1 ? fma(w[2], V, p) : w[2] * U;
     f[3] = (w[3] + p) * un;
     if (un_out) *un_out = un;
-    if (p_out) *p_out = p;
+    if (c_out) *c_out = sqrt(gamma * p * rinv);
 }
 
 /* HLL flux with Davis wave-speed estimates (Toro, "Riemann Solvers and
@@ -294,11 +308,9 @@ static inline void euler_flux_dir(const double *w, double gamma, int dir, double
  * example/shock-vortex.jl:78 (x faces) and :84-87 (y faces through
  * local_frame/global_frame, which this directional form equals exactly). */
 void fro_flux_hll2d(const double *wL, const double *wR, double gamma, int dir, double *fw) {
-    double fL[4], fR[4], uL, uR, pL, pR;
-    euler_flux_dir(wL, gamma, dir, fL, &uL, &pL);
-    euler_flux_dir(wR, gamma, dir, fR, &uR, &pR);
-    double cL = sqrt(gamma * pL / wL[0]);
-    double cR = sqrt(gamma * pR / wR[0]);
+    double fL[4], fR[4], uL, uR, cL, cR;
+    euler_flux_dir(wL, gamma, dir, fL, &uL, &cL);
+    euler_flux_dir(wR, gamma, dir, fR, &uR, &cR);
     double sl = fmin(uL - cL, uR - cR);
     double sr = fmax(uL + cL, uR + cR);
     if (sl >= 0.0) {
@@ -315,11 +327,9 @@ void fro_flux_hll2d(const double *wL, const double *wR, double gamma, int dir, d
 /* Local Lax-Friedrichs (Rusanov) flux: 0.5 (FL + FR) - 0.5 lambda (wR - wL),
  * lambda = max(|uL| + cL, |uR| + cR). */
 void fro_flux_lf2d(const double *wL, const double *wR, double gamma, int dir, double *fw) {
-    double fL[4], fR[4], uL, uR, pL, pR;
-    euler_flux_dir(wL, gamma, dir, fL, &uL, &pL);
-    euler_flux_dir(wR, gamma, dir, fR, &uR, &pR);
-    double cL = sqrt(gamma * pL / wL[0]);
-    double cR = sqrt(gamma * pR / wR[0]);
+    double fL[4], fR[4], uL, uR, cL, cR;
+    euler_flux_dir(wL, gamma, dir, fL, &uL, &cL);
+    euler_flux_dir(wR, gamma, dir, fR, &uR, &cR);
     double lam = fmax(fabs(uL) + cL, fabs(uR) + cR);
     for (int m = 0; m < 4; ++m) fw[m] = 0.5 * (fL[m] + fR[m]) - 0.5 * lam * (wR[m] - wL[m]);
 }
@@ -329,7 +339,7 @@ static inline void euler_flux_1d(const double *w, double gamma, double *f, doubl
     double U = w[1] / w[0];
     double p = (gamma - 1.0) * (w[2] - 0.5 * w[1] * U);
     f[0] = w[1];
-    f[1] = w[1] * U + p;
+    f[1] = fma(w[1], U, p);
     f[2] = (w[2] + p) * U;
     if (u_out) *u_out = U;
     if (p_out) *p_out = p;
@@ -405,17 +415,10 @@ static void rhs_scalar1d(const fro_cfg *c, double *du, const double *u) {
             f[i + ne * k] = fl / c->J[i];
         }
     for (int i = 0; i < ne; ++i) {
-        double a0 = 0, a1 = 0, b0 = 0, b1 = 0;
-        for (int k = 0; k < np; ++k) {
-            a0 += u[i + ne * k] * c->ll[k];
-            a1 += u[i + ne * k] * c->lr[k];
-            b0 += f[i + ne * k] * c->ll[k];
-            b1 += f[i + ne * k] * c->lr[k];
-        }
-        uf[i] = a0;
-        uf[i + ne] = a1;
-        ff[i] = b0;
-        ff[i + ne] = b1;
+        uf[i] = dotw(u + i, ne, c->ll, 1, np);
+        uf[i + ne] = dotw(u + i, ne, c->lr, 1, np);
+        ff[i] = dotw(f + i, ne, c->ll, 1, np);
+        ff[i + ne] = dotw(f + i, ne, c->lr, 1, np);
     }
     for (int i = 1; i < ne; ++i) {
         double au = (ff[i] - ff[i - 1 + ne]) / (uf[i] - uf[i - 1 + ne] + c->eps_interior);
@@ -434,9 +437,8 @@ static void rhs_scalar1d(const fro_cfg *c, double *du, const double *u) {
                 du[i + ne * m] = 0.0;
                 continue;
             }
-            double r = 0.0;
-            for (int k = 0; k < np; ++k) r += f[i + ne * k] * c->lpdm[m + np * k];
-            du[i + ne * m] = -(r + (fi[i] - ff[i]) * c->dgl[m] + (fi[i + 1] - ff[i + ne]) * c->dgr[m]);
+            double r = dotw(f + i, ne, c->lpdm + m, np, np);
+            du[i + ne * m] = -fma(fi[i + 1] - ff[i + ne], c->dgr[m], fma(fi[i] - ff[i], c->dgl[m], r));
         }
     free(f);
     free(uf);
@@ -465,17 +467,10 @@ static void rhs_euler1d(const fro_cfg *c, double *du, const double *u) {
     /* u_face[i, side, m]: side 0 = left (ll), 1 = right (lr) */
     for (int m = 0; m < 3; ++m)
         for (int i = 0; i < ne; ++i) {
-            double a0 = 0, a1 = 0, b0 = 0, b1 = 0;
-            for (int k = 0; k < np; ++k) {
-                a0 += U1(i, k, m) * c->ll[k];
-                a1 += U1(i, k, m) * c->lr[k];
-                b0 += F1(i, k, m) * c->ll[k];
-                b1 += F1(i, k, m) * c->lr[k];
-            }
-            uf[i + ne * (0 + 2 * m)] = a0;
-            uf[i + ne * (1 + 2 * m)] = a1;
-            ff[i + ne * (0 + 2 * m)] = b0;
-            ff[i + ne * (1 + 2 * m)] = b1;
+            uf[i + ne * (0 + 2 * m)] = dotw(&U1(i, 0, m), ne, c->ll, 1, np);
+            uf[i + ne * (1 + 2 * m)] = dotw(&U1(i, 0, m), ne, c->lr, 1, np);
+            ff[i + ne * (0 + 2 * m)] = dotw(&F1(i, 0, m), ne, c->ll, 1, np);
+            ff[i + ne * (1 + 2 * m)] = dotw(&F1(i, 0, m), ne, c->lr, 1, np);
         }
     for (int i = 1; i < ne; ++i) {
         double wL[3], wR[3], fw[3];
@@ -508,10 +503,10 @@ static void rhs_euler1d(const fro_cfg *c, double *du, const double *u) {
                     *d = 0.0;
                     continue;
                 }
-                double r = 0.0;
-                for (int k = 0; k < np; ++k) r += F1(i, k, m) * c->lpdm[kk + np * k];
-                *d = -(r + (fi[i + (ne + 1) * m] / c->J[i] - ff[i + ne * (0 + 2 * m)]) * c->dgl[kk] +
-                       (fi[i + 1 + (ne + 1) * m] / c->J[i] - ff[i + ne * (1 + 2 * m)]) * c->dgr[kk]);
+                double r = dotw(&F1(i, 0, m), ne, c->lpdm + kk, np, np);
+                double aL = fi[i + (ne + 1) * m] / c->J[i] - ff[i + ne * (0 + 2 * m)];
+                double aR = fi[i + 1 + (ne + 1) * m] / c->J[i] - ff[i + ne * (1 + 2 * m)];
+                *d = -fma(aR, c->dgr[kk], fma(aL, c->dgl[kk], r));
             }
 #undef U1
 #undef F1
@@ -618,23 +613,16 @@ static void rhs_euler2d(const fro_cfg *c, double *du, const double *u) {
         if (!needed) continue;
         const double *ue = w.ug + e * E;
         double *uf = w.uface + e * FS;
-        /* u traces */
+        /* u traces: faces 0/2 along s at r-index l (points u[l, q]),
+         * faces 1/3 along r at s-index l (points u[q, l]) */
         for (int m = 0; m < 4; ++m)
             for (int l = 0; l < np; ++l) {
-                double b = 0, r = 0, t = 0, lf = 0;
-                for (int q = 0; q < np; ++q) {
-                    /* face 0/2 along s at r-index l: u[l, q]; face 1/3 along r at s-index l: u[q, l] */
-                    double us = ue[(m * np + q) * np + l]; /* k = l, l' = q */
-                    double ur = ue[(m * np + l) * np + q]; /* k = q, l' = l */
-                    b += us * ll[q];
-                    t += us * lr[q];
-                    r += ur * lr[q];
-                    lf += ur * ll[q];
-                }
-                uf[(0 * np + l) * 4 + m] = b;
-                uf[(1 * np + l) * 4 + m] = r;
-                uf[(2 * np + l) * 4 + m] = t;
-                uf[(3 * np + l) * 4 + m] = lf;
+                const double *us = ue + (m * np + 0) * np + l; /* stride np over q */
+                const double *ur = ue + (m * np + l) * np;     /* stride 1 over q */
+                uf[(0 * np + l) * 4 + m] = dotw(us, np, ll, 1, np);
+                uf[(1 * np + l) * 4 + m] = dotw(ur, 1, lr, 1, np);
+                uf[(2 * np + l) * 4 + m] = dotw(us, np, lr, 1, np);
+                uf[(3 * np + l) * 4 + m] = dotw(ur, 1, ll, 1, np);
             }
         if (!interior) continue;
         long ei = (long)(jg - 1) * nx + (ig - 1);
@@ -653,19 +641,12 @@ static void rhs_euler2d(const fro_cfg *c, double *du, const double *u) {
         double *ff = w.fface + e * FS;
         for (int m = 0; m < 4; ++m)
             for (int l = 0; l < np; ++l) {
-                double b = 0, r = 0, t = 0, lf = 0;
-                for (int q = 0; q < np; ++q) {
-                    double gs = fv[(1 * 4 + m) * np * np + q * np + l]; /* y flux at (k=l, l'=q) */
-                    double fr = fv[(0 * 4 + m) * np * np + l * np + q]; /* x flux at (k=q, l'=l) */
-                    b += gs * ll[q];
-                    t += gs * lr[q];
-                    r += fr * lr[q];
-                    lf += fr * ll[q];
-                }
-                ff[(0 * np + l) * 4 + m] = b;
-                ff[(1 * np + l) * 4 + m] = r;
-                ff[(2 * np + l) * 4 + m] = t;
-                ff[(3 * np + l) * 4 + m] = lf;
+                const double *gs = fv + (1 * 4 + m) * np * np + l;      /* y flux at (k=l, l'=q), stride np */
+                const double *fr = fv + (0 * 4 + m) * np * np + l * np; /* x flux at (k=q, l'=l), stride 1 */
+                ff[(0 * np + l) * 4 + m] = dotw(gs, np, ll, 1, np);
+                ff[(1 * np + l) * 4 + m] = dotw(fr, 1, lr, 1, np);
+                ff[(2 * np + l) * 4 + m] = dotw(gs, np, lr, 1, np);
+                ff[(3 * np + l) * 4 + m] = dotw(fr, 1, ll, 1, np);
             }
     }
 
@@ -713,19 +694,19 @@ static void rhs_euler2d(const fro_cfg *c, double *du, const double *u) {
         for (int m = 0; m < 4; ++m)
             for (int l = 0; l < np; ++l)
                 for (int k = 0; k < np; ++k) {
-                    double r1 = 0, r2 = 0;
-                    for (int q = 0; q < np; ++q) {
-                        r1 += fv[(0 * 4 + m) * np * np + l * np + q] * lpdm[k + np * q];
-                        r2 += fv[(1 * 4 + m) * np * np + q * np + k] * lpdm[l + np * q];
-                    }
+                    double r1 = dotw(fv + (0 * 4 + m) * np * np + l * np, 1, lpdm + k, np, np);
+                    double r2 = dotw(fv + (1 * 4 + m) * np * np + k, np, lpdm + l, np, np);
                     double fxl = w.fxi[(((long)j * (nx + 1) + i) * np + l) * 4 + m];
                     double fxr = w.fxi[(((long)j * (nx + 1) + i + 1) * np + l) * 4 + m];
                     double fyb = w.fyi[(((long)j * nx + i) * np + k) * 4 + m];
                     double fyt = w.fyi[(((long)(j + 1) * nx + i) * np + k) * 4 + m];
-                    double v = -(r1 + r2 + (fxl * c->iJx - ff[(3 * np + l) * 4 + m]) * c->dgl[k] +
-                                 (fxr * c->iJx - ff[(1 * np + l) * 4 + m]) * c->dgr[k] +
-                                 (fyb * c->iJy - ff[(0 * np + k) * 4 + m]) * c->dgl[l] +
-                                 (fyt * c->iJy - ff[(2 * np + k) * 4 + m]) * c->dgr[l]);
+                    /* the x and y correction terms added to the two derivatives */
+                    double aL = fxl * c->iJx - ff[(3 * np + l) * 4 + m];
+                    double aR = fxr * c->iJx - ff[(1 * np + l) * 4 + m];
+                    double bB = fyb * c->iJy - ff[(0 * np + k) * 4 + m];
+                    double bT = fyt * c->iJy - ff[(2 * np + k) * 4 + m];
+                    double cx = fma(aR, c->dgr[k], fma(aL, c->dgl[k], r1));
+                    double v = -fma(bT, c->dgr[l], fma(bB, c->dgl[l], cx + r2));
                     du[i + (long)nx * j + nn * (k + np * (l + (long)np * m))] = v;
                 }
     }
@@ -825,13 +806,14 @@ void fro_rhs(const fro_cfg *c, double *du, const double *u) {
 void fro_ssprk3(const fro_cfg *c, double *u, double dt, int nsteps, double *work) {
     long n = fro_ndof(c);
     double *s = work, *k = work + n;
+    const double third = 1.0 / 3.0;
     for (int it = 0; it < nsteps; ++it) {
         fro_rhs(c, k, u);
-        for (long q = 0; q < n; ++q) s[q] = u[q] + dt * k[q];
+        for (long q = 0; q < n; ++q) s[q] = fma(dt, k[q], u[q]);
         fro_rhs(c, k, s);
-        for (long q = 0; q < n; ++q) s[q] = (3.0 * u[q] + s[q] + dt * k[q]) / 4.0;
+        for (long q = 0; q < n; ++q) s[q] = fma(dt, k[q], fma(3.0, u[q], s[q])) * 0.25;
         fro_rhs(c, k, s);
-        for (long q = 0; q < n; ++q) u[q] = (u[q] + 2.0 * s[q] + 2.0 * dt * k[q]) / 3.0;
+        for (long q = 0; q < n; ++q) u[q] = fma(2.0 * dt, k[q], fma(2.0, s[q], u[q])) * third;
     }
 }
 
@@ -841,9 +823,34 @@ void fro_ssprk3(const fro_cfg *c, double *u, double dt, int nsteps, double *work
 
 /* KitBase :l2 modal filter on a flat modal vector (as called on the
  * flattened 2D modes at example/shock-vortex.jl:316):
- * u[q] /= 1 + lam * (q+1)^2 q^2, q = 0-based mode index. */
+ * u[q] /= 1 + lam (q+1)^2 q^2, q = 0-based mode index. */
 static void filter_l2_flat(double *uh, int n, double lam) {
-    for (int q = 0; q < n; ++q) uh[q] /= (1.0 + lam * (double)(q + 1) * (q + 1) * (double)q * q);
+    for (int q = 0; q < n; ++q) uh[q] = uh[q] / (1.0 + lam * (double)((q + 1) * (q + 1) * q * q));
+}
+
+/* y = A x for a column-major n x n matrix, fixed dot order */
+static void matvec(const double *A, const double *x, int n, double *y) {
+    for (int a = 0; a < n; ++a) y[a] = dotw(A + a, n, x, 1, n);
+}
+
+/* the modal-decay detector input su = uh_N^2 / (sum uh^2 + add) */
+static double decay_ratio(const double *uh, int n, double add) {
+    double tot = 0.0;
+    for (int a = 0; a < n; ++a) tot = fma(uh[a], uh[a], tot);
+    return uh[n - 1] * uh[n - 1] / (tot + add);
+}
+
+/* filter one element's nvar variables (point stride ps, variable stride vs) */
+static void filter_element(double *u, long ps, long vs, int nvar, int n, const double *V, const double *iV,
+                           double lam) {
+    double ue[36], uh[36];
+    for (int m = 0; m < nvar; ++m) {
+        for (int q = 0; q < n; ++q) ue[q] = u[ps * q + vs * m];
+        matvec(iV, ue, n, uh);
+        filter_l2_flat(uh, n, lam);
+        matvec(V, uh, n, ue);
+        for (int q = 0; q < n; ++q) u[ps * q + vs * m] = ue[q];
+    }
 }
 
 /* Post-step indicator + filter, example/shock-vortex.jl:308-321 (over the
@@ -859,32 +866,13 @@ int fro_filter2d(const fro_cfg *c, double *u, const double *V, const double *iV,
     for (long e = 0; e < nn; ++e) {
         double ue[36], uh[36];
         for (int q = 0; q < N; ++q) ue[q] = u[e + nn * q];
-        for (int a = 0; a < N; ++a) {
-            double s = 0;
-            for (int b = 0; b < N; ++b) s += iV[a + N * b] * ue[b];
-            uh[a] = s;
-        }
-        double tot = 0;
-        for (int a = 0; a < N; ++a) tot += uh[a] * uh[a];
-        double su = uh[N - 1] * uh[N - 1] / tot;
+        matvec(iV, ue, N, uh);
+        double su = decay_ratio(uh, N, 0.0);
         int troubled = fro_shock_detector(log10(su), np - 1, S0, kappa);
         if (flags) flags[e] = troubled;
         if (!troubled) continue;
         ++count;
-        for (int m = 0; m < 4; ++m) {
-            for (int q = 0; q < N; ++q) ue[q] = u[e + nn * (q + (long)N * m)];
-            for (int a = 0; a < N; ++a) {
-                double s = 0;
-                for (int b = 0; b < N; ++b) s += iV[a + N * b] * ue[b];
-                uh[a] = s;
-            }
-            filter_l2_flat(uh, N, lam);
-            for (int a = 0; a < N; ++a) {
-                double s = 0;
-                for (int b = 0; b < N; ++b) s += V[a + N * b] * uh[b];
-                u[e + nn * (a + (long)N * m)] = s;
-            }
-        }
+        filter_element(u + e, nn, nn * N, 4, N, V, iV, lam);
     }
     return count;
 }
@@ -899,32 +887,13 @@ int fro_filter1d(const fro_cfg *c, double *u, int nvar, const double *V, const d
     for (int i = 0; i < ne; ++i) {
         double ue[8], uh[8];
         for (int q = 0; q < np; ++q) ue[q] = u[i + (long)ne * q];
-        for (int a = 0; a < np; ++a) {
-            double s = 0;
-            for (int b = 0; b < np; ++b) s += iV[a + np * b] * ue[b];
-            uh[a] = s;
-        }
-        double tot = 0;
-        for (int a = 0; a < np; ++a) tot += uh[a] * uh[a];
-        double su = uh[np - 1] * uh[np - 1] / (tot + 1e-6);
+        matvec(iV, ue, np, uh);
+        double su = decay_ratio(uh, np, 1e-6);
         int troubled = fro_shock_detector(log10(su), deg, -3.0 * log10((double)deg), 4.0);
         if (flags) flags[i] = troubled;
         if (!troubled) continue;
         ++count;
-        for (int m = 0; m < nvar; ++m) {
-            for (int q = 0; q < np; ++q) ue[q] = u[i + (long)ne * (q + (long)np * m)];
-            for (int a = 0; a < np; ++a) {
-                double s = 0;
-                for (int b = 0; b < np; ++b) s += iV[a + np * b] * ue[b];
-                uh[a] = s;
-            }
-            filter_l2_flat(uh, np, lam);
-            for (int a = 0; a < np; ++a) {
-                double s = 0;
-                for (int b = 0; b < np; ++b) s += V[a + np * b] * uh[b];
-                u[i + (long)ne * (a + (long)np * m)] = s;
-            }
-        }
+        filter_element(u + i, ne, (long)ne * np, nvar, np, V, iV, lam);
     }
     return count;
 }
