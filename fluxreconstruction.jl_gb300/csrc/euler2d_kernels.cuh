@@ -54,14 +54,22 @@ template <int NP> struct Tile<float, NP> {
     static constexpr int TY = NP <= 2 ? 8 : (NP <= 4 ? 2 : 1);
 };
 
-template <class Real, int NP, int TX, int TY> struct Smem {
+// NST: state-sized stash arrays holding the stage update's extra inputs
+// (u^n in FP64 stages 2-3; the increment, and in stage 3 also the high and
+// low parts, in FP32K), loaded together with the state so that their latency
+// is not exposed after the residual.
+template <int MODE, int STAGE> struct Stash {
+    static constexpr int n = MODE == MODE_FP32K ? (STAGE == 2 ? 1 : (STAGE == 3 ? 3 : 0)) : (STAGE >= 2 ? 1 : 0);
+};
+
+template <class Real, int NP, int TX, int TY, int NST = 0> struct Smem {
     static constexpr int U = TY * NP * NP * 4 * TX;
     static constexpr int TR = TY * NP * 4 * TX;
     static constexpr int HY = 2 * NP * 4 * TX;
     static constexpr int HX = 2 * TY * NP * 4;
     static constexpr int FX = TY * NP * 4 * (TX + 1);
     static constexpr int FY = (TY + 1) * NP * 4 * TX;
-    static constexpr int total = 2 * U + 4 * TR + HY + HX + FX + FY;
+    static constexpr int total = 2 * U + 4 * TR + HY + HX + FX + FY + NST * U;
     static constexpr size_t bytes = sizeof(Real) * total;
 };
 
@@ -94,7 +102,8 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
     k_euler2d(const E2DArgs<Real, NP> a) {
     constexpr int TX = Tile<Real, NP>::TX, TY = Tile<Real, NP>::TY;
     constexpr int NT = TX * NP * TY;
-    using S = Smem<Real, NP, TX, TY>;
+    constexpr int NST = Stash<MODE, STAGE>::n;
+    using S = Smem<Real, NP, TX, TY, NST>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Real *s_u = reinterpret_cast<Real *>(smem_raw);
     Real *s_g = s_u + S::U;
@@ -106,6 +115,8 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
     Real *s_hx = s_hy + S::HY;
     Real *s_Fx = s_hx + S::HX;
     Real *s_Fy = s_Fx + S::FX;
+    Real *s_st = s_Fy + S::FY;
+#define SST(q, ey, l, k, m, ex) s_st[(q) * S::U + ((((ey) * NP + (l)) * NP + (k)) * 4 + (m)) * TX + (ex)]
 #define SU(ey, l, k, m, ex) s_u[((((ey) * NP + (l)) * NP + (k)) * 4 + (m)) * TX + (ex)]
 #define SG(ey, l, k, m, ex) s_g[((((ey) * NP + (l)) * NP + (k)) * 4 + (m)) * TX + (ex)]
 #define STR(arr, ey, q, m, ex) arr[(((ey) * NP + (q)) * 4 + (m)) * TX + (ex)]
@@ -196,7 +207,21 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
 #pragma unroll
             for (int m = 0; m < 4; ++m)
 #pragma unroll
-                for (int k = 0; k < NP; ++k) u[k][m] = ld_state(uin, din, base + plane * (k + NP * NP * m));
+                for (int k = 0; k < NP; ++k) {
+                    const size_t idx = base + plane * (k + NP * NP * m);
+                    if (MODE == MODE_FP32K && STAGE >= 2) {
+                        const Real h = __ldg(uin + idx), d = __ldg(din + idx);
+                        u[k][m] = h + d;
+                        SST(0, ey, l, k, m, ex) = d;
+                        if (STAGE == 3) {
+                            SST(1, ey, l, k, m, ex) = h;
+                            SST(2, ey, l, k, m, ex) = a.ul[idx];
+                        }
+                    } else {
+                        u[k][m] = ld_state(uin, din, idx);
+                        if (MODE == MODE_FP64 && STAGE >= 2) SST(0, ey, l, k, m, ex) = a.un[idx];
+                    }
+                }
         } else {
 #pragma unroll
             for (int k = 0; k < NP; ++k) {
@@ -309,6 +334,7 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
         const int k = ln;
         const Real dt = (Real)(*a.dtp);
         const size_t base = (size_t)i + (size_t)nx * j + plane * k;
+        Real chk = Real(0);
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
             const Real bB = SFY(ey, k, m, ex) * a.iJy - gyb[m];
@@ -327,10 +353,10 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
                     if (STAGE == 1) {
                         res = fmaR<Real>(dt, du, ui);
                     } else if (STAGE == 2) {
-                        const Real un = a.un[idx];
+                        const Real un = SST(0, ey, l, k, m, ex);
                         res = (fmaR<Real>(dt, du, fmaR<Real>(Real(3), un, ui))) * Real(0.25);
                     } else {
-                        const Real un = a.un[idx];
+                        const Real un = SST(0, ey, l, k, m, ex);
                         res = fmaR<Real>(Real(2) * dt, du, fmaR<Real>(Real(2), ui, un)) * Real(1.0 / 3.0);
                     }
                     a.out[idx] = res;
@@ -342,14 +368,14 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
                         res = dt * du;
                         a.out[idx] = res;
                     } else if (STAGE == 2) {
-                        const Real d1 = __ldg(din + idx);
+                        const Real d1 = SST(0, ey, l, k, m, ex);
                         res = fmaR<Real>(dt, du, d1) * Real(0.25);
                         a.out[idx] = res;
                     } else {
-                        const Real d2 = __ldg(din + idx);
+                        const Real d2 = SST(0, ey, l, k, m, ex);
                         const Real d3 = fmaR<Real>(dt, du, d2) * Real(2.0 / 3.0);
-                        const Real hi = __ldg(uin + idx);
-                        const Real lo = a.ul[idx];
+                        const Real hi = SST(1, ey, l, k, m, ex);
+                        const Real lo = SST(2, ey, l, k, m, ex);
                         const Real y = d3 + lo;
                         const Real t = hi + y;
                         const Real lo_new = y - (t - hi);
@@ -358,9 +384,10 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
                         res = t;
                     }
                 }
-                if (!isfinite(res)) bad |= ST_NONFINITE;
+                chk += res; // NaN and Inf propagate into the check sum
             }
         }
+        if (!isfinite(chk)) bad |= ST_NONFINITE;
     }
     if (bad) atomicOr(a.status, bad);
 #undef SU
@@ -370,6 +397,7 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
 #undef SHX
 #undef SFX
 #undef SFY
+#undef SST
 }
 
 template <class Real, int NP> Ops<Real, NP> make_ops(const frgpu_space &s) {
@@ -384,10 +412,34 @@ template <class Real, int NP> Ops<Real, NP> make_ops(const frgpu_space &s) {
     return o;
 }
 
+template <class Real, int NP>
+E2DArgs<Real, NP> make_e2d_args(frgpu_problem *p, const void *in, const void *din, void *out) {
+    E2DArgs<Real, NP> a;
+    a.nx = p->sp.nx;
+    a.ny = p->sp.ny;
+    a.uin = (const Real *)in;
+    a.din = (const Real *)din;
+    a.un = (const Real *)p->s0;
+    a.out = (Real *)out;
+    a.ul = (Real *)p->s3;
+    a.dtp = p->d_dt;
+    a.iJx = (Real)(1.0 / (0.5 * p->sp.dx));
+    a.iJy = (Real)(1.0 / (0.5 * p->sp.dy));
+    a.gamma = (Real)p->d.gamma;
+    a.gm1 = (Real)(p->d.gamma - 1.0);
+    for (int s = 0; s < 4; ++s) {
+        a.bc[s] = p->d.bc[s];
+        for (int m = 0; m < 4; ++m) a.fixed[s][m] = (Real)p->d.fixed_state[s][m];
+    }
+    a.ops = make_ops<Real, NP>(p->sp);
+    a.status = p->d_status;
+    return a;
+}
+
 template <class Real, int NP, int FLUX, int MODE, int STAGE>
 int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     using T = Tile<Real, NP>;
-    using S = Smem<Real, NP, T::TX, T::TY>;
+    using S = Smem<Real, NP, T::TX, T::TY, Stash<MODE, STAGE>::n>;
     E2DArgs<Real, NP> a;
     a.nx = p->sp.nx;
     a.ny = p->sp.ny;

@@ -113,10 +113,11 @@ template <class Real> int filter1d_np(frgpu_problem *p, double lam, double S0, d
 } // namespace
 
 int fr_launch_filter2d(frgpu_problem *p, int indicator, double lam, double S0, double kappa) {
-    if (indicator == FRGPU_IND_MLP) {
-        fr_set_error("filter2d: the learned indicator is not loaded");
-        return FRGPU_ERR_UNSUPPORTED;
+    if (!p->d_V || !p->d_iV) {
+        fr_set_error("filter2d: the space has no Vandermonde matrices");
+        return FRGPU_ERR_ARG;
     }
+    if (indicator == FRGPU_IND_MLP) return fr_launch_mlp_indicator(p, lam, S0, kappa);
     if (!p->d_V || !p->d_iV) {
         fr_set_error("filter2d: the space has no Vandermonde matrices");
         return FRGPU_ERR_ARG;

@@ -31,6 +31,22 @@ template <class Real> __device__ __forceinline__ Real sqrtP(Real a); // a >= 0
 template <> __device__ __forceinline__ double sqrtP<double>(double a) { return sqrt(a); }
 template <> __device__ __forceinline__ float sqrtP<float>(float a) { return a > 0.0f ? a * rsqrtf(a) : 0.0f; }
 
+// Global load that stays where it is written.  The stage updates read their
+// extra inputs (u^n, increments, low parts) only after the residual; plain
+// read-only loads there may be hoisted by the compiler across the block's
+// barriers to the kernel start, where they would hold registers through the
+// whole residual.
+__device__ __forceinline__ float ld_here(const float *p) {
+    float v;
+    asm volatile("ld.global.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ double ld_here(const double *p) {
+    double v;
+    asm volatile("ld.global.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    return v;
+}
+
 template <class Real> __device__ __forceinline__ Real absR(Real a) { return a < Real(0) ? -a : a; }
 template <class Real> __device__ __forceinline__ Real maxR(Real a, Real b) { return a > b ? a : b; }
 template <class Real> __device__ __forceinline__ Real minR(Real a, Real b) { return a < b ? a : b; }

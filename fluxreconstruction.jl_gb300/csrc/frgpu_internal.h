@@ -45,6 +45,8 @@ struct frgpu_problem {
     // post-step filter
     int indicator = FRGPU_IND_NONE;
     double lam = 0, S0 = 0, kappa = 0;
+    const frgpu_mlp *mlp = nullptr; // learned indicator (borrowed)
+    float mlp_thr = 0.5f, mlp_band = 0.0f;
     // captured step graph
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int graph_ind = -1;
@@ -103,3 +105,6 @@ int fr_launch_poly_derivative(const double *d_f, long n, int np, const double *p
 // filter.cu
 int fr_launch_filter2d(frgpu_problem *p, int indicator, double lam, double S0, double kappa);
 int fr_launch_filter1d(frgpu_problem *p, int indicator, double lam, double S0, double kappa);
+// mlp.cu
+int fr_launch_features(frgpu_problem *p, float *d_feat);
+int fr_launch_mlp_indicator(frgpu_problem *p, double lam, double S0, double kappa);

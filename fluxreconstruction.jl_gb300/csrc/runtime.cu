@@ -492,8 +492,8 @@ FRGPU_API int frgpu_problem_create(const frgpu_space *s, const frgpu_problem_des
             const size_t ne = (size_t)s->nx * s->ny;
             FR_CUDA(cudaMalloc(&p->d_flags, sizeof(int) * ne));
             FR_CUDA(cudaMemset(p->d_flags, 0, sizeof(int) * ne));
-            FR_CUDA(cudaMalloc(&p->d_count, sizeof(int)));
-            FR_CUDA(cudaMemset(p->d_count, 0, sizeof(int)));
+            FR_CUDA(cudaMalloc(&p->d_count, sizeof(int) * 4));
+            FR_CUDA(cudaMemset(p->d_count, 0, sizeof(int) * 4));
             if (!s->wp.empty())
                 FR_CUDA(cudaMemcpy(p->d_red + FR_RED_WP, s->wp.data(), sizeof(double) * s->wp.size(),
                                    cudaMemcpyHostToDevice));
@@ -721,6 +721,44 @@ FRGPU_API int frgpu_modal_filter(frgpu_problem *p, int indicator, double lam, do
     FR_CUDA(cudaStreamSynchronize(p->stream));
     return check_status(p);
     FR_CATCH
+}
+
+FRGPU_API int frgpu_problem_set_mlp(frgpu_problem *p, const frgpu_mlp *m, double threshold, double band) {
+    FR_REQ(p, "problem_set_mlp: null problem");
+    FR_REQ(p->d.equation == FRGPU_EULER2D && p->sp.np == 4, "problem_set_mlp: 2D Euler with deg = 3");
+    FR_REQ(threshold > 0 && threshold < 1 && band >= 0 && band < 0.5, "problem_set_mlp: need 0 < threshold < 1, 0 <= band < 0.5");
+    p->mlp = m;
+    p->mlp_thr = (float)threshold;
+    p->mlp_band = (float)band;
+    p->graph_ind = -2; // the captured step refers to the network: re-capture
+    return FRGPU_OK;
+}
+
+FRGPU_API int frgpu_modal_features(frgpu_problem *p, float *feat, long n) {
+    FR_REQ(p && feat, "modal_features: null argument");
+    const long ne = (long)p->sp.nx * p->sp.ny;
+    FR_REQ(n >= ne * 32, "modal_features: output needs nx*ny*32 floats");
+    FR_TRY
+    float *d = nullptr;
+    FR_CUDA(cudaMalloc(&d, sizeof(float) * ne * 32));
+    int rc = fr_launch_features(p, d);
+    cudaError_t e = cudaSuccess;
+    if (!rc) {
+        e = cudaMemcpyAsync(feat, d, sizeof(float) * ne * 32, cudaMemcpyDeviceToHost, p->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+    }
+    cudaFree(d);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fr_cuda_fail(e, "modal_features copy");
+    return FRGPU_OK;
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_indicator_stats(frgpu_problem *p, int *stats) {
+    FR_REQ(p && stats, "indicator_stats: null argument");
+    FR_CUDA(cudaStreamSynchronize(p->stream));
+    FR_CUDA(cudaMemcpy(stats, p->d_count, sizeof(int) * 3, cudaMemcpyDeviceToHost));
+    return FRGPU_OK;
 }
 
 FRGPU_API int frgpu_troubled_flags(frgpu_problem *p, int *flags, long n) {

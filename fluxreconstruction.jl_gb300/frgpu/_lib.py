@@ -21,6 +21,7 @@ RADAU, SD, HUYNH = 0, 1, 2
 IND_NONE, IND_PLAIN, IND_MLP = 0, 1, 2
 
 _D = C.POINTER(C.c_double)
+_F = C.POINTER(C.c_float)
 _I = C.POINTER(C.c_int)
 _VP = C.c_void_p
 
@@ -71,6 +72,17 @@ SIGNATURES = {
     "frgpu_synchronize": (C.c_int, [_VP]),
     "frgpu_reduce2d_noalloc": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                          C.c_double, _VP, _VP, _VP]),
+    "frgpu_mlp_nparams": (C.c_int, []),
+    "frgpu_mlp_create": (C.c_int, [C.c_int, C.POINTER(_VP)]),
+    "frgpu_mlp_destroy": (None, [_VP]),
+    "frgpu_mlp_get_params": (C.c_int, [_VP, _F]),
+    "frgpu_mlp_set_params": (C.c_int, [_VP, _F]),
+    "frgpu_mlp_forward": (C.c_int, [_VP, _F, C.c_long, _F]),
+    "frgpu_mlp_loss_grad": (C.c_int, [_VP, _F, _F, C.c_long, _F, _F]),
+    "frgpu_mlp_train": (C.c_int, [_VP, _F, _F, C.c_long, C.c_int, C.c_int, C.c_float, C.c_int, _F]),
+    "frgpu_problem_set_mlp": (C.c_int, [_VP, _VP, C.c_double, C.c_double]),
+    "frgpu_modal_features": (C.c_int, [_VP, _F, C.c_long]),
+    "frgpu_indicator_stats": (C.c_int, [_VP, _I]),
     "frgpu_interp_face": (C.c_int, [_D, C.c_long, C.c_int, _D, _D, _D]),
     "frgpu_poly_derivative": (C.c_int, [_D, C.c_long, C.c_int, _D, _D]),
     "frgpu_last_error": (C.c_int, [C.c_char_p, C.c_ulong]),
@@ -120,3 +132,7 @@ def check(rc: int) -> int:
 
 def dptr(a):
     return a.ctypes.data_as(_D)
+
+
+def fptr(a):
+    return a.ctypes.data_as(_F)

@@ -61,6 +61,7 @@ enum frgpu_indicator { FRGPU_IND_NONE = 0, FRGPU_IND_PLAIN = 1, FRGPU_IND_MLP = 
 
 typedef struct frgpu_space frgpu_space;
 typedef struct frgpu_problem frgpu_problem;
+typedef struct frgpu_mlp frgpu_mlp;
 
 /* ======================================================================
  * Setup math (host).  Used by the space constructors; exported so a caller
@@ -165,6 +166,39 @@ FRGPU_API int frgpu_problem_device_state(frgpu_problem *p, void **dptr, int *ele
 FRGPU_API int frgpu_problem_stream(frgpu_problem *p, void **stream);
 FRGPU_API long frgpu_problem_launches(const frgpu_problem *p);
 FRGPU_API int frgpu_synchronize(frgpu_problem *p);
+
+/* ======================================================================
+ * Learned troubled-cell indicator.  Stands in for the modal-decay test
+ * shock_detector(log10(su), ...) (src/dissipation.jl:13-23) in the post-step
+ * filter loop of example/shock-vortex.jl:308-321: a 32 -> 64 -> 64 -> 1
+ * perceptron (GELU, GELU, sigmoid) on per-element normalised modal energies
+ * of density and pressure (deg = 3), BF16 inputs/weights, FP32 accumulation
+ * on the tensor cores.  Parameters (FP32): W1[64][32] b1[64] W2[64][64]
+ * b2[64] W3[64] b3[1], row-major [out][in].
+ * ==================================================================== */
+FRGPU_API int frgpu_mlp_nparams(void);
+FRGPU_API int frgpu_mlp_create(int seed, frgpu_mlp **out);
+FRGPU_API void frgpu_mlp_destroy(frgpu_mlp *m);
+FRGPU_API int frgpu_mlp_get_params(const frgpu_mlp *m, float *params);
+FRGPU_API int frgpu_mlp_set_params(frgpu_mlp *m, const float *params);
+/* y[i] = network(x[i, 0:32]) for host arrays x[n][32], y[n] */
+FRGPU_API int frgpu_mlp_forward(frgpu_mlp *m, const float *x, long n, float *y);
+/* mean binary cross-entropy of (x, t) and its gradient (nparams floats) */
+FRGPU_API int frgpu_mlp_loss_grad(frgpu_mlp *m, const float *x, const float *t, long n, float *loss, float *grad);
+/* mini-batch Adam training; loss_out[epochs] (optional) receives the mean loss per epoch */
+FRGPU_API int frgpu_mlp_train(frgpu_mlp *m, const float *x, const float *t, long n, int epochs, int batch, float lr,
+                              int seed, float *loss_out);
+/* Bind a network to a 2D Euler problem (deg = 3) for FRGPU_IND_MLP: an element
+ * is troubled when the network's probability exceeds `threshold`; within
+ * `band` of the threshold the plain modal-decay test decides (fallback).  The
+ * network is borrowed and must outlive its use. */
+FRGPU_API int frgpu_problem_set_mlp(frgpu_problem *p, const frgpu_mlp *m, double threshold, double band);
+/* The 32 indicator inputs of every element of the current state, feat[ne][32]. */
+FRGPU_API int frgpu_modal_features(frgpu_problem *p, float *feat, long n);
+/* After an FRGPU_IND_MLP filter: stats[0] troubled elements, stats[1]
+ * network-vs-plain disagreements (misfires judged by the plain test),
+ * stats[2] elements decided by the plain fallback. */
+FRGPU_API int frgpu_indicator_stats(frgpu_problem *p, int *stats);
 
 /* Allocation-free 2D Euler reduction.  No counterpart in the reference: it
  * exists for callers that cannot let this library call cudaMalloc -- hosts
