@@ -168,11 +168,14 @@ def label_run(ps, mach_v, nsteps, every, cfl=0.1, keep_neg=0.02, seed=0):
     done = 0
     while done < nsteps:
         n = min(every, nsteps - done)
-        itg.set_filter("plain", FILTER_LAMBDA, S0, FILTER_KAPPA)
-        if n > 1:
-            itg.step(n - 1)
-        itg.set_filter("none")
-        itg.step(1)
+        try:
+            itg.set_filter("plain", FILTER_LAMBDA, S0, FILTER_KAPPA)
+            if n > 1:
+                itg.step(n - 1)
+            itg.set_filter("none")
+            itg.step(1)
+        except L.FRGPUError:
+            break  # the filtered scheme lost positivity: keep the snapshots taken so far
         done += n
         feat = np.zeros(ne * NIN, dtype=np.float32)
         check(L.lib().frgpu_modal_features(prob._h, fptr(feat), feat.size))
@@ -208,3 +211,111 @@ def balance(x, t, seed=0, ratio=3.0):
     sel = np.concatenate([pos, rng.choice(neg, k, replace=False)])
     rng.shuffle(sel)
     return x[sel], t[sel]
+
+
+# ---------------------------------------------------------------- full-scale training
+import os as _os
+
+WEIGHTS = _os.path.join(_os.path.dirname(_os.path.abspath(__file__)), "data", "shock_vortex_mlp.npy")
+RECORD = _os.path.join(_os.path.dirname(_os.path.abspath(__file__)), "data", "shock_vortex_mlp.json")
+CONFIG3 = dict(x0=0.0, x1=2.0, nx=400, y0=0.0, y1=1.0, ny=200, deg=3)
+
+
+def config3_space():
+    c = CONFIG3
+    return api.FRPSpace2D(c["x0"], c["x1"], c["nx"], c["y0"], c["y1"], c["ny"], c["deg"])
+
+
+def load_trained() -> "MLPIndicator":
+    """The network trained by `train_config3` (shipped with the package)."""
+    return MLPIndicator.load(WEIGHTS)
+
+
+def evaluate(m, ps, mach_v, nsteps, indicator, cfl=0.1, threshold=0.5, band=0.0):
+    """Run the shock-vortex problem with one indicator ('none', 'plain', 'mlp')
+    and report the final state, the network's misfires (judged by the plain
+    test) and the troubled-element count of the last step."""
+    prob = shock_vortex_problem(ps, mach_v)
+    itg = api.init(prob, dt=1.0)
+    itg.dt = itg.cfl_dt(cfl)
+    if indicator == "mlp":
+        check(L.lib().frgpu_problem_set_mlp(prob._h, m._h, float(threshold), float(band)))
+    stats = np.zeros(3, dtype=np.int32)
+    mis = 0
+    seen = 0
+    ok = True
+    if indicator != "none":
+        itg.set_filter(indicator, FILTER_LAMBDA, filter_S0(ps.deg), FILTER_KAPPA)
+    try:
+        if indicator == "mlp":
+            for _ in range(nsteps):
+                itg.step(1)
+                check(L.lib().frgpu_indicator_stats(prob._h, stats.ctypes.data_as(L._I)))
+                mis += int(stats[1])
+                seen += ps.nx * ps.ny
+        else:
+            itg.step(nsteps)
+        u = itg.u
+    except L.FRGPUError:
+        ok = False
+        u = None
+    return {"ok": ok, "u": u, "misfires": mis, "elements_seen": seen, "dt": itg.dt}
+
+
+def train_config3(nseeds=64, nsteps=2400, every=240, epochs=20, batch=4096, lr=2e-3, seed=0, log=print):
+    """Labels from plain-indicator runs of config 3 (400 x 200, deg 3) over
+    `nseeds` seeded vortex strengths (seeds 0..nseeds-1, Mach uniform on
+    [0.1, 0.4]); seeds >= nseeds - 8 are held out for validation."""
+    import json
+    import time
+
+    ps = config3_space()
+    t0 = time.time()
+    train_seeds = range(0, nseeds - 8)
+    val_seeds = range(nseeds - 8, nseeds)
+    x, t = build_dataset(ps, train_seeds, nsteps=nsteps, every=every, keep_neg=0.01)
+    xv, tv = build_dataset(ps, val_seeds, nsteps=nsteps, every=every, keep_neg=0.01)
+    t_data = time.time() - t0
+    log(f"dataset: {len(t)} samples ({int(t.sum())} troubled), validation {len(tv)} ({int(tv.sum())}); {t_data:.1f} s")
+    xb, tb = balance(x, t, seed=seed)
+    m = MLPIndicator(seed=seed)
+    t1 = time.time()
+    losses = m.train(xb, tb, epochs=epochs, batch=batch, lr=lr, seed=seed)
+    t_train = time.time() - t1
+    yv = m.forward(xv)
+    pred = yv > 0.5
+    lab = tv > 0.5
+    rec = {
+        "config": dict(CONFIG3, nseeds=nseeds, nsteps=nsteps, every=every, epochs=epochs, batch=batch, lr=lr,
+                       seed=seed, mach_range=[0.1, 0.4], filter_lambda=FILTER_LAMBDA, kappa=FILTER_KAPPA),
+        "samples": int(len(t)), "troubled": int(t.sum()), "balanced_samples": int(len(tb)),
+        "loss_per_epoch": [float(v) for v in losses],
+        "validation": {"samples": int(len(tv)), "troubled": int(lab.sum()),
+                       "accuracy": float(np.mean(pred == lab)),
+                       "false_positive": int(np.sum(pred & ~lab)), "false_negative": int(np.sum(~pred & lab))},
+        "seconds": {"labels": t_data, "training": t_train},
+    }
+    log(json.dumps(rec["validation"]))
+    return m, rec
+
+
+def main(argv=None):
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description="train the learned troubled-cell indicator on config 3")
+    ap.add_argument("--out", default=WEIGHTS)
+    ap.add_argument("--record", default=RECORD)
+    ap.add_argument("--nseeds", type=int, default=64)
+    ap.add_argument("--nsteps", type=int, default=2400)
+    ap.add_argument("--epochs", type=int, default=20)
+    a = ap.parse_args(argv)
+    m, rec = train_config3(nseeds=a.nseeds, nsteps=a.nsteps, epochs=a.epochs)
+    _os.makedirs(_os.path.dirname(a.out), exist_ok=True)
+    m.save(a.out)
+    with open(a.record, "w") as f:
+        json.dump(rec, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()
