@@ -234,6 +234,8 @@ def gpu_arm(args, dist, rank, ws):
     # of example/shock-vortex.jl:308-321); "fp32k" is the bare stage kernel
     # the roofline is quoted on
     forms = (("fp32k_learned", "fp32k", "mlp"), ("fp32k", "fp32k", "none"), ("fp64_plain", "fp64", "plain"))
+    if args.forms:
+        forms = tuple(f for f in forms if f[0] in args.forms.split(","))
     for form, precision, indicator in forms:
         prob = frgpu.FREuler2DProblem(u0, (0, 1), ps, GAMMA, flux="lf", bc="period", precision=precision)
         itg = frgpu.init(prob, dt=1.0)
@@ -264,7 +266,7 @@ def gpu_arm(args, dist, rank, ws):
                      "dt": dt, "t_end": t_end, "rms_err_rho_vs_exact": err, "indicator": indicator,
                      "troubled_last_step": int(np.sum(itg.troubled())) if indicator != "none" else 0,
                      "launches_timed": launches}
-        if form == "fp32k_learned":
+        if form == "fp32k_learned" and not args.no_e2e:
             # end to end through the C ABI with host buffers
             host_u = np.asfortranarray(u0)
             sums_steps = []
@@ -323,6 +325,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    # profiling aids: run a subset of the forms (comma list of fp32k_learned,
+    # fp32k, fp64_plain) and/or skip the end-to-end leg; the line then only
+    # carries the forms that ran
+    ap.add_argument("--forms", default="")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     ws, rank, _ = dist_env()
     dist = init_dist(ws)
@@ -343,6 +350,10 @@ def main():
 
     res, clocks = gpu_arm(args, dist, rank, ws)
     if rank != 0:
+        return
+    if args.forms or args.no_e2e:
+        print(json.dumps({"metric": METRIC, "unit": UNIT, "partial_run": True, "forms": res, "clocks": clocks}),
+              flush=True)
         return
     peak, peak_kind = measured_peaks()
     lrn = res["fp32k_learned"]

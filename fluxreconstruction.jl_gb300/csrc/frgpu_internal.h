@@ -47,6 +47,7 @@ struct frgpu_problem {
     double lam = 0, S0 = 0, kappa = 0;
     const frgpu_mlp *mlp = nullptr; // learned indicator (borrowed)
     float mlp_thr = 0.5f, mlp_band = 0.0f;
+    int bgk_tensor = 1;             // FP32 BGK transport on the tensor cores
     // captured step graph
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int graph_ind = -1;
@@ -98,6 +99,7 @@ int fr_launch_euler2d_reduce(frgpu_problem *p, const void *state, const void *lo
 int fr_launch_scalar1d(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
 int fr_launch_euler1d(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
 int fr_launch_bgk1d(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
+int fr_launch_bgk1d_tc(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
 int fr_launch_interp_face(const double *d_f, long n, int np, const double *ll, const double *lr, double *d_out,
                           cudaStream_t st);
 int fr_launch_poly_derivative(const double *d_f, long n, int np, const double *pdm, double *d_out,
@@ -107,4 +109,10 @@ int fr_launch_filter2d(frgpu_problem *p, int indicator, double lam, double S0, d
 int fr_launch_filter1d(frgpu_problem *p, int indicator, double lam, double S0, double kappa);
 // mlp.cu
 int fr_launch_features(frgpu_problem *p, float *d_feat);
+// Device pointers of a network (FP32 parameters, BF16 W1 [64][32], W2 and W2^T [64][64]).
+struct fr_mlp_ptrs {
+    const float *P;
+    const void *W1, *W2, *W2T;
+};
+fr_mlp_ptrs fr_mlp_device(const frgpu_mlp *m);
 int fr_launch_mlp_indicator(frgpu_problem *p, double lam, double S0, double kappa);

@@ -19,112 +19,11 @@
 #include "fr_common.cuh"
 #include "frgpu_internal.h"
 
+#include "mlp_device.cuh"
+
 namespace {
 
-constexpr int NIN = 32, NH = 64;
-constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + NH * NIN, OFF_W2 = OFF_B1 + NH, OFF_B2 = OFF_W2 + NH * NH,
-              OFF_W3 = OFF_B2 + NH, OFF_B3 = OFF_W3 + NH, NPARAM = OFF_B3 + 1;
-constexpr int WARPS = 4;  // warps per CTA of the forward and indicator kernels
-constexpr int GWARPS = 2; // warps per CTA of the gradient kernel (static shared memory < 48 KB)
-
-struct MLPDev {
-    const float *P;             // FP32 parameters
-    const __nv_bfloat16 *W1;    // [64][32]
-    const __nv_bfloat16 *W2;    // [64][64]  row = output unit
-    const __nv_bfloat16 *W2T;   // [64][64]  row = input unit
-};
-
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
-    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-    return *reinterpret_cast<uint32_t *>(&v);
-}
-__device__ __forceinline__ uint32_t pack_bf16_raw(__nv_bfloat16 lo, __nv_bfloat16 hi) {
-    __nv_bfloat162 v;
-    v.x = lo;
-    v.y = hi;
-    return *reinterpret_cast<uint32_t *>(&v);
-}
-__device__ __forceinline__ uint32_t ld_pair(const __nv_bfloat16 *p) { return *reinterpret_cast<const uint32_t *>(p); }
-
-// D = A (16x16 bf16, row) * B (16x8 bf16, col) + C (f32)
-__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
-    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                 "{%0,%1,%2,%3};\n"
-                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
-__device__ __forceinline__ float dgelu(float x) {
-    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * expf(-0.5f * x * x) * 0.39894228040143268f;
-}
-
-// Forward pass of one warp tile (16 samples).  xs: the tile's features in
-// shared memory, bf16 [16][32].  Outputs per lane: pre-activations a1, a2 and
-// activations h2 in the m16n8 accumulator layout (rows g and g+8, columns
-// 8j + 2t and +1, g = lane/4, t = lane%4), layer-2 input fragments ah1, and
-// the logits of rows g and g+8.
-struct Fwd {
-    float a1[8][4], a2[8][4];
-    uint32_t ah1[4][4];
-    float logit_g, logit_g8;
-};
-
-__device__ __forceinline__ void mlp_forward_tile(const MLPDev &w, const __nv_bfloat16 *xs, Fwd &f) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    uint32_t ax[2][4];
-#pragma unroll
-    for (int kk = 0; kk < 2; ++kk) {
-        ax[kk][0] = ld_pair(xs + g * NIN + 16 * kk + 2 * t);
-        ax[kk][1] = ld_pair(xs + (g + 8) * NIN + 16 * kk + 2 * t);
-        ax[kk][2] = ld_pair(xs + g * NIN + 16 * kk + 8 + 2 * t);
-        ax[kk][3] = ld_pair(xs + (g + 8) * NIN + 16 * kk + 8 + 2 * t);
-    }
-    const float *b1 = w.P + OFF_B1, *b2 = w.P + OFF_B2, *w3 = w.P + OFF_W3;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        const float c0 = __ldg(b1 + 8 * j + 2 * t), c1 = __ldg(b1 + 8 * j + 2 * t + 1);
-        f.a1[j][0] = c0;
-        f.a1[j][1] = c1;
-        f.a1[j][2] = c0;
-        f.a1[j][3] = c1;
-        const __nv_bfloat16 *row = w.W1 + (8 * j + g) * NIN;
-#pragma unroll
-        for (int kk = 0; kk < 2; ++kk) mma16816(f.a1[j], ax[kk], ld_pair(row + 16 * kk + 2 * t), ld_pair(row + 16 * kk + 8 + 2 * t));
-    }
-#pragma unroll
-    for (int kk = 0; kk < 4; ++kk) {
-        f.ah1[kk][0] = pack_bf16(gelu(f.a1[2 * kk][0]), gelu(f.a1[2 * kk][1]));
-        f.ah1[kk][1] = pack_bf16(gelu(f.a1[2 * kk][2]), gelu(f.a1[2 * kk][3]));
-        f.ah1[kk][2] = pack_bf16(gelu(f.a1[2 * kk + 1][0]), gelu(f.a1[2 * kk + 1][1]));
-        f.ah1[kk][3] = pack_bf16(gelu(f.a1[2 * kk + 1][2]), gelu(f.a1[2 * kk + 1][3]));
-    }
-    float sg = 0.f, sg8 = 0.f;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        const float c0 = __ldg(b2 + 8 * j + 2 * t), c1 = __ldg(b2 + 8 * j + 2 * t + 1);
-        f.a2[j][0] = c0;
-        f.a2[j][1] = c1;
-        f.a2[j][2] = c0;
-        f.a2[j][3] = c1;
-        const __nv_bfloat16 *row = w.W2 + (8 * j + g) * NH;
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk)
-            mma16816(f.a2[j], f.ah1[kk], ld_pair(row + 16 * kk + 2 * t), ld_pair(row + 16 * kk + 8 + 2 * t));
-        const float w0 = __ldg(w3 + 8 * j + 2 * t), w1 = __ldg(w3 + 8 * j + 2 * t + 1);
-        sg = fmaf(gelu(f.a2[j][0]), w0, fmaf(gelu(f.a2[j][1]), w1, sg));
-        sg8 = fmaf(gelu(f.a2[j][2]), w0, fmaf(gelu(f.a2[j][3]), w1, sg8));
-    }
-    sg += __shfl_xor_sync(0xffffffffu, sg, 1);
-    sg += __shfl_xor_sync(0xffffffffu, sg, 2);
-    sg8 += __shfl_xor_sync(0xffffffffu, sg8, 1);
-    sg8 += __shfl_xor_sync(0xffffffffu, sg8, 2);
-    const float b3 = __ldg(w.P + OFF_B3);
-    f.logit_g = sg + b3;
-    f.logit_g8 = sg8 + b3;
-}
-
-__device__ __forceinline__ float sigmoidf_(float z) { return 1.0f / (1.0f + expf(-z)); }
+using namespace frmlp;
 
 // ---------------------------------------------------------------- forward (tests, evaluation)
 __global__ void __launch_bounds__(32 * WARPS) k_mlp_forward(MLPDev w, const float *__restrict__ X, long n,
@@ -140,7 +39,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_mlp_forward(MLPDev w, const floa
         }
         __syncwarp();
         Fwd f;
-        mlp_forward_tile(w, xs, f);
+        mlp_forward_tile(global_view(w), xs, f);
         const int g = lane >> 2, t = lane & 3;
         if (t == 0) {
             const long s0 = tile * 16 + g, s1 = tile * 16 + g + 8;
@@ -182,7 +81,7 @@ __global__ void __launch_bounds__(32 * GWARPS) k_mlp_grad(MLPDev w, const float 
         }
         __syncwarp();
         Fwd f;
-        mlp_forward_tile(w, xs, f);
+        mlp_forward_tile(global_view(w), xs, f);
         // output layer: delta3 = (y - t) / N for the mean BCE with a sigmoid
         const long s0 = tile * 16 + g, s1 = tile * 16 + g + 8;
         float d3g = 0.f, d3g8 = 0.f, lpart = 0.f;
@@ -365,54 +264,88 @@ __global__ void k_mlp_refresh(const float *__restrict__ P, __nv_bfloat16 *W1, __
 }
 
 // ---------------------------------------------------------------- features + indicator
-// Modal energies of density and pressure of element e (np = 4).  Lanes 0-15
-// of a warp produce the density half of 16 elements, lanes 16-31 the pressure
-// half; the density lane also returns the plain modal-decay ratio su.
+// 1D inverse Vandermonde matrix of deg 3 (iV1[i][k]); the tensor inverse of
+// FRPSpace2D (src/struct.jl:196-205) factors as iV[(i,j)][(k,l)] = iV1[i][k] iV1[j][l].
+struct IV1 {
+    float m[4][4];
+};
+
+// Modal energies of density and pressure of 16 elements per warp (np = 4).
+// Lane L and L + 16 share element e = base + (L & 15): each loads the four
+// variables at 8 of the 16 points (lower lane points 0-7, upper 8-15), then
+// they swap halves so that the lower lane holds the density values and the
+// upper lane the pressure values.  The lower lane's su is the plain
+// modal-decay ratio of the density.  Lanes of elements past the end (valid
+// false) must still take part in the exchange; they return zero features.
 template <class Real>
-__device__ __forceinline__ void element_features(const Real *__restrict__ u, size_t ne, size_t e, bool pressure,
-                                                 const Real *__restrict__ iV, float gm1, float (&feat)[16],
+__device__ __forceinline__ void element_features(const Real *__restrict__ u, size_t ne, size_t e, bool valid,
+                                                 bool pressure, const IV1 &iv, float gm1, float (&feat)[16],
                                                  float &su) {
     float v[16];
+    const int q0 = pressure ? 8 : 0;
 #pragma unroll
-    for (int q = 0; q < 16; ++q) {
-        if (!pressure) {
-            v[q] = (float)u[e + ne * q];
-        } else {
-            const float w0 = (float)u[e + ne * q], w1 = (float)u[e + ne * (q + 16)];
-            const float w2 = (float)u[e + ne * (q + 32)], w3 = (float)u[e + ne * (q + 48)];
-            const float ri = 1.0f / w0;
-            v[q] = gm1 * (w3 - 0.5f * (w1 * (w1 * ri) + w2 * (w2 * ri)));
+    for (int k = 0; k < 8; ++k) {
+        float w0 = 1.f, w1 = 0.f, w2 = 0.f, w3 = 0.f;
+        if (valid) {
+            const size_t at = e + ne * (size_t)(q0 + k);
+            w0 = (float)u[at];
+            w1 = (float)u[at + ne * 16];
+            w2 = (float)u[at + ne * 32];
+            w3 = (float)u[at + ne * 48];
         }
+        const float ri = __fdividef(1.0f, w0);
+        const float pk = gm1 * (w3 - 0.5f * (w1 * (w1 * ri) + w2 * (w2 * ri)));
+        const float recv = __shfl_xor_sync(0xffffffffu, pressure ? w0 : pk, 16);
+        v[k] = pressure ? recv : w0;     // density (lower) / pressure (upper) at point k
+        v[8 + k] = pressure ? pk : recv; // ... at point 8 + k
     }
+    // modal coefficients by sum factorisation: t[i][l] = sum_k iV1[i][k] v[k + 4 l],
+    // u_hat[4 i + j] = sum_l iV1[j][l] t[i][l]
+    float t[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            float s = iv.m[i][0] * v[4 * l];
+#pragma unroll
+            for (int k = 1; k < 4; ++k) s = fmaf(iv.m[i][k], v[k + 4 * l], s);
+            t[i][l] = s;
+        }
     float tot = 0.f;
     float en[16];
 #pragma unroll
-    for (int a = 0; a < 16; ++a) {
-        float s = (float)iV[a] * v[0];
+    for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int b = 1; b < 16; ++b) s = fmaf((float)iV[a + 16 * b], v[b], s);
-        en[a] = s * s;
-        tot += en[a];
-    }
+        for (int j = 0; j < 4; ++j) {
+            float s = iv.m[j][0] * t[i][0];
+#pragma unroll
+            for (int l = 1; l < 4; ++l) s = fmaf(iv.m[j][l], t[i][l], s);
+            en[4 * i + j] = s * s;
+            tot += s * s;
+        }
     su = en[15] / tot;
     const float itot = 1.0f / tot;
 #pragma unroll
     for (int a = 0; a < 16; ++a) {
-        float x = log10f(en[a] * itot + 1e-16f);
+        float x = __log2f(en[a] * itot + 1e-16f) * 0.30102999566398120f; // log10 through the hardware log2
         x = fminf(fmaxf(x, -16.f), 0.f);
-        feat[a] = x * 0.125f + 1.0f;
+        feat[a] = valid ? x * 0.125f + 1.0f : 0.f;
     }
 }
 
+// One warp per 16 elements (the indicator kernel's tiling, so that training
+// features and inference features are the same numbers).
 template <class Real>
-__global__ void __launch_bounds__(128) k_features(const Real *__restrict__ u, size_t ne, const Real *__restrict__ iV,
-                                                  float gm1, float *__restrict__ feat) {
+__global__ void __launch_bounds__(128) k_features(const Real *__restrict__ u, size_t ne, IV1 iv, float gm1,
+                                                  float *__restrict__ feat) {
     const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (t >= 2 * ne) return;
-    const size_t e = t >> 1;
-    const bool pr = t & 1;
+    const int lane = threadIdx.x & 31;
+    const size_t e = (t >> 5) * 16 + (lane & 15);
+    if ((t >> 5) * 16 >= ne) return; // whole warp past the end
+    const bool pr = lane >= 16, valid = e < ne;
     float f[16], su;
-    element_features<Real>(u, ne, e, pr, iV, gm1, f, su);
+    element_features<Real>(u, ne, e, valid, pr, iv, gm1, f, su);
+    if (!valid) return;
 #pragma unroll
     for (int a = 0; a < 16; ++a) feat[e * NIN + (pr ? 16 : 0) + a] = f[a];
 }
@@ -435,13 +368,20 @@ __device__ __forceinline__ bool plain_troubled(float su, float S0, float kappa) 
 // network does.  stats: [0] troubled, [1] network vs plain disagreements
 // (misfires, judged by the plain test), [2] fallbacks.
 template <class Real>
-__global__ void __launch_bounds__(32 * WARPS) k_mlp_indicator(MLPDev w, Real *__restrict__ u, Real *__restrict__ lo,
+__global__ void __launch_bounds__(32 * WARPS, 5) k_mlp_indicator(MLPDev w, Real *__restrict__ u, Real *__restrict__ lo,
                                                             size_t ne, const Real *__restrict__ V,
-                                                            const Real *__restrict__ iV, float gm1, float thr,
-                                                            float band, float S0, float kappa, double lam,
+                                                            const Real *__restrict__ iV, IV1 iv, float gm1,
+                                                            float thr, float band, float S0, float kappa, double lam,
                                                             int *__restrict__ flags, int *__restrict__ stats) {
     __shared__ __align__(16) __nv_bfloat16 xs_all[WARPS][16 * NIN];
     __shared__ float prob_all[WARPS][16];
+    // the CTA's copy of the weights: W1, W2 (bf16) and b1, b2, w3, b3
+    __shared__ __align__(16) __nv_bfloat16 sW1[NH * NIN];
+    __shared__ __align__(16) __nv_bfloat16 sW2[NH * NH];
+    __shared__ float sb[3 * NH + 1];
+    stage_weights(w, sW1, sW2, sb);
+    __syncthreads();
+    const MLPView view = smem_view(sW1, sW2, sb);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     __nv_bfloat16 *xs = xs_all[warp];
     float *prob = prob_all[warp];
@@ -451,56 +391,53 @@ __global__ void __launch_bounds__(32 * WARPS) k_mlp_indicator(MLPDev w, Real *__
         const size_t e = tile * 16 + (lane & 15);
         const bool pr = lane >= 16;
         float feat[16], su = 0.f;
-        if (e < ne) {
-            element_features<Real>(u, ne, e, pr, iV, gm1, feat, su);
-        } else {
-#pragma unroll
-            for (int a = 0; a < 16; ++a) feat[a] = 0.f;
-        }
+        element_features<Real>(u, ne, e, e < ne, pr, iv, gm1, feat, su);
 #pragma unroll
         for (int a = 0; a < 16; ++a) xs[(lane & 15) * NIN + (pr ? 16 : 0) + a] = __float2bfloat16_rn(feat[a]);
         __syncwarp();
         Fwd f;
-        mlp_forward_tile(w, xs, f);
+        mlp_forward_tile(view, xs, f);
         const int g = lane >> 2, t = lane & 3;
         if (t == 0) {
             prob[g] = sigmoidf_(f.logit_g);
             prob[g + 8] = sigmoidf_(f.logit_g8);
         }
         __syncwarp();
+        bool bad = false;
         if (!pr && e < ne) {
             const bool plain = plain_troubled(su, S0, kappa);
             const float pm = prob[lane];
             const bool fallback = fabsf(pm - thr) < band;
             const bool net = pm > thr;
-            const bool bad = fallback ? plain : net;
+            bad = fallback ? plain : net;
             n_fb += fallback;
             n_mis += (net != plain);
             n_trouble += bad;
             flags[e] = bad ? 1 : 0;
-            if (bad) {
-                // :l2 modal filter of all four variables (as in filter.cu)
-                for (int m = 0; m < 4; ++m) {
-                    Real *um = u + ne * 16 * (size_t)m;
-                    Real x[16], h[16];
+        }
+        // :l2 modal filter of the troubled elements, one element at a time by
+        // the whole warp: lane = 16 (variable pair) + mode a.  Every output is
+        // the same ascending FMA chain as the plain filter kernel's.
+        unsigned todo = __ballot_sync(0xffffffffu, bad);
+        const int a = lane & 15, half = lane & 16;
+        const Real den = Real(1) + mul_rn(Real(lam), Real((double)((a + 1) * (a + 1) * a * a)));
+        while (todo) {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const size_t et = tile * 16 + src;
+            for (int mp = 0; mp < 4; mp += 2) {
+                const int m = mp + (half >> 4);
+                Real *um = u + ne * 16 * (size_t)m;
+                const Real xa = um[et + ne * a];
+                Real s = iV[a] * __shfl_sync(0xffffffffu, xa, half);
 #pragma unroll
-                    for (int q = 0; q < 16; ++q) x[q] = um[e + ne * q];
+                for (int b = 1; b < 16; ++b) s = frk::fmaR<Real>(iV[a + 16 * b], __shfl_sync(0xffffffffu, xa, half + b), s);
+                const Real ha = s / den;
+                Real r = V[a] * __shfl_sync(0xffffffffu, ha, half);
 #pragma unroll
-                    for (int a = 0; a < 16; ++a) {
-                        Real s = iV[a] * x[0];
-#pragma unroll
-                        for (int b = 1; b < 16; ++b) s = frk::fmaR<Real>(iV[a + 16 * b], x[b], s);
-                        h[a] = s / (Real(1) + Real(lam) * Real((double)((a + 1) * (a + 1) * a * a)));
-                    }
-#pragma unroll
-                    for (int a = 0; a < 16; ++a) {
-                        Real s = V[a] * h[0];
-#pragma unroll
-                        for (int b = 1; b < 16; ++b) s = frk::fmaR<Real>(V[a + 16 * b], h[b], s);
-                        um[e + ne * a] = s;
-                        if (lo) lo[e + ne * (a + 16 * (size_t)m)] = Real(0);
-                    }
-                }
+                for (int b = 1; b < 16; ++b) r = frk::fmaR<Real>(V[a + 16 * b], __shfl_sync(0xffffffffu, ha, half + b), r);
+                um[et + ne * a] = r;
+                if (lo) lo[et + ne * (a + 16 * (size_t)m)] = Real(0);
             }
         }
         __syncwarp();
@@ -739,19 +676,32 @@ FRGPU_API int frgpu_mlp_train(frgpu_mlp *m, const float *x, const float *t, long
 } // extern "C"
 
 // ---- used by runtime.cu -------------------------------------------------------
+fr_mlp_ptrs fr_mlp_device(const frgpu_mlp *m) { return fr_mlp_ptrs{m->P, m->W1, m->W2, m->W2T}; }
+
+// The 1D factor of the space's tensor inverse Vandermonde matrix:
+// iV[(i,0),(k,0)] = iV1[i][k] iV1[0][0], and iV1[0][0] = w_0 / sqrt(2) > 0.
+static IV1 iv1_from_tensor(const frgpu_problem *p) {
+    const double *iV = p->sp.iV.data();
+    const double c = std::sqrt(iV[0]);
+    IV1 r;
+    for (int i = 0; i < 4; ++i)
+        for (int k = 0; k < 4; ++k) r.m[i][k] = (float)(iV[4 * i + 16 * k] / c);
+    return r;
+}
+
 int fr_launch_features(frgpu_problem *p, float *d_feat) {
     if (p->d.equation != FRGPU_EULER2D || p->sp.np != 4) {
         fr_set_error("modal features: 2D Euler with deg = 3 (32 inputs)");
         return FRGPU_ERR_UNSUPPORTED;
     }
     const size_t ne = (size_t)p->sp.nx * p->sp.ny;
-    const int grid = (int)((2 * ne + 127) / 128);
+    const int grid = (int)(((ne + 15) / 16 * 32 + 127) / 128);
     const float gm1 = (float)(p->d.gamma - 1.0);
     if (p->d.precision == FRGPU_FP64)
-        k_features<double><<<grid, 128, 0, p->stream>>>((const double *)fr_state_hi(p), ne, (const double *)p->d_iV,
-                                                        gm1, d_feat);
+        k_features<double><<<grid, 128, 0, p->stream>>>((const double *)fr_state_hi(p), ne, iv1_from_tensor(p), gm1,
+                                                        d_feat);
     else
-        k_features<float><<<grid, 128, 0, p->stream>>>((const float *)fr_state_hi(p), ne, (const float *)p->d_iV, gm1,
+        k_features<float><<<grid, 128, 0, p->stream>>>((const float *)fr_state_hi(p), ne, iv1_from_tensor(p), gm1,
                                                        d_feat);
     FR_CUDA(cudaGetLastError());
     p->launches += 1;
@@ -770,18 +720,22 @@ int fr_launch_mlp_indicator(frgpu_problem *p, double lam, double S0, double kapp
     }
     const size_t ne = (size_t)p->sp.nx * p->sp.ny;
     const size_t ntiles = (ne + 15) / 16;
-    const int grid = (int)std::min<size_t>((ntiles + WARPS - 1) / WARPS, 152 * 8);
+    // persistent: as many CTAs as fit at once (5 per SM at 96 registers per thread)
+    int nsm = 152;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device);
+    const int grid = (int)std::min<size_t>((ntiles + WARPS - 1) / WARPS, (size_t)nsm * 5);
     const float gm1 = (float)(p->d.gamma - 1.0);
     FR_CUDA(cudaMemsetAsync(p->d_count, 0, sizeof(int) * 4, p->stream));
     const MLPDev w = p->mlp->dev();
+    const IV1 iv1 = iv1_from_tensor(p);
     if (p->d.precision == FRGPU_FP64)
         k_mlp_indicator<double><<<grid, 32 * WARPS, 0, p->stream>>>(
-            w, (double *)fr_state_hi(p), nullptr, ne, (const double *)p->d_V, (const double *)p->d_iV, gm1,
-            p->mlp_thr, p->mlp_band, (float)S0, (float)kappa, lam, p->d_flags, p->d_count);
+            w, (double *)fr_state_hi(p), nullptr, ne, (const double *)p->d_V, (const double *)p->d_iV, iv1,
+            gm1, p->mlp_thr, p->mlp_band, (float)S0, (float)kappa, lam, p->d_flags, p->d_count);
     else
         k_mlp_indicator<float><<<grid, 32 * WARPS, 0, p->stream>>>(
-            w, (float *)fr_state_hi(p), (float *)p->s3, ne, (const float *)p->d_V, (const float *)p->d_iV, gm1,
-            p->mlp_thr, p->mlp_band, (float)S0, (float)kappa, lam, p->d_flags, p->d_count);
+            w, (float *)fr_state_hi(p), (float *)p->s3, ne, (const float *)p->d_V, (const float *)p->d_iV, iv1,
+            gm1, p->mlp_thr, p->mlp_band, (float)S0, (float)kappa, lam, p->d_flags, p->d_count);
     FR_CUDA(cudaGetLastError());
     p->launches += 1;
     return FRGPU_OK;

@@ -705,6 +705,14 @@ FRGPU_API int frgpu_set_filter(frgpu_problem *p, int indicator, double lam, doub
     return FRGPU_OK;
 }
 
+FRGPU_API int frgpu_problem_set_option(frgpu_problem *p, int option, int value) {
+    FR_REQ(p, "set_option: null problem");
+    FR_REQ(option == FRGPU_OPT_BGK_TENSOR, "set_option: unknown option");
+    p->bgk_tensor = value != 0;
+    p->graph_ind = -2; // force a re-capture
+    return FRGPU_OK;
+}
+
 FRGPU_API int frgpu_modal_filter(frgpu_problem *p, int indicator, double lam, double S0, double kappa,
                                  int *ntroubled) {
     FR_REQ(p, "modal_filter: null problem");

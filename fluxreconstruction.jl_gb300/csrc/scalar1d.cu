@@ -50,7 +50,10 @@ int fr_launch_scalar1d(frgpu_problem *p, int stage, const void *in, const void *
 int fr_launch_euler1d(frgpu_problem *p, int stage, const void *in, const void *din, void *out) {
     return dispatch1(KIND_EULER, p, stage, in, din, out);
 }
+// FP32: transport on the tensor cores (bgk_tc.cu) unless the problem's
+// FRGPU_OPT_BGK_TENSOR option is 0; FP64: the CUDA-core kernel
 int fr_launch_bgk1d(frgpu_problem *p, int stage, const void *in, const void *din, void *out) {
+    if (p->d.precision != FRGPU_FP64 && p->bgk_tensor) return fr_launch_bgk1d_tc(p, stage, in, din, out);
     return dispatch1(KIND_BGK, p, stage, in, din, out);
 }
 

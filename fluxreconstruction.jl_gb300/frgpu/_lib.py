@@ -19,6 +19,7 @@ FP64, FP32K = 0, 1
 BC_PERIODIC, BC_COPY, BC_FIXED, BC_DIRICHLET = 0, 1, 2, 3
 RADAU, SD, HUYNH = 0, 1, 2
 IND_NONE, IND_PLAIN, IND_MLP = 0, 1, 2
+OPT_BGK_TENSOR = 1
 
 _D = C.POINTER(C.c_double)
 _F = C.POINTER(C.c_float)
@@ -64,6 +65,7 @@ SIGNATURES = {
     "frgpu_cfl_dt": (C.c_int, [_VP, C.c_double, _D]),
     "frgpu_reduce": (C.c_int, [_VP, _D, _D]),
     "frgpu_set_filter": (C.c_int, [_VP, C.c_int, C.c_double, C.c_double, C.c_double]),
+    "frgpu_problem_set_option": (C.c_int, [_VP, C.c_int, C.c_int]),
     "frgpu_modal_filter": (C.c_int, [_VP, C.c_int, C.c_double, C.c_double, C.c_double, _I]),
     "frgpu_troubled_flags": (C.c_int, [_VP, _I, C.c_long]),
     "frgpu_problem_device_state": (C.c_int, [_VP, C.POINTER(_VP), _I]),
@@ -83,6 +85,23 @@ SIGNATURES = {
     "frgpu_problem_set_mlp": (C.c_int, [_VP, _VP, C.c_double, C.c_double]),
     "frgpu_modal_features": (C.c_int, [_VP, _F, C.c_long]),
     "frgpu_indicator_stats": (C.c_int, [_VP, _I]),
+    "frgpu_ensemble_config4_sizes": (C.c_int, [C.c_int, C.c_uint, _I, _I]),
+    "frgpu_ensemble_create": (C.c_int, [C.c_int, _I, _I, C.c_double, C.c_double, C.c_int, C.POINTER(_VP)]),
+    "frgpu_ensemble_destroy": (None, [_VP]),
+    "frgpu_ensemble_ndof": (C.c_long, [_VP]),
+    "frgpu_ensemble_set_state": (C.c_int, [_VP, C.c_int, _D]),
+    "frgpu_ensemble_get_state": (C.c_int, [_VP, C.c_int, _D]),
+    "frgpu_ensemble_init_fourier": (C.c_int, [_VP, C.c_double, C.c_uint]),
+    "frgpu_ensemble_set_tiles": (C.c_int, [_VP, _I]),
+    "frgpu_ensemble_get_tiles": (C.c_int, [_VP, _I]),
+    "frgpu_ensemble_run": (C.c_int, [_VP, C.c_double, C.c_double, C.c_int]),
+    "frgpu_ensemble_stats": (C.c_int, [_VP, _D, _I, _F, _D, _I]),
+    "frgpu_ensemble_tune": (C.c_int, [_VP, C.c_double, C.c_double, C.c_int, _I]),
+    "frgpu_ensemble_launches": (C.c_long, [_VP]),
+    "frgpu_ensemble_set_mlp": (C.c_int, [_VP, _VP, C.c_double, C.c_double]),
+    "frgpu_ensemble_indicator_stats": (C.c_int, [_VP, C.POINTER(C.c_longlong)]),
+    "frgpu_ensemble_nelem": (C.c_long, [_VP]),
+    "frgpu_ensemble_features": (C.c_int, [_VP, _F, _I, C.c_long]),
     "frgpu_interp_face": (C.c_int, [_D, C.c_long, C.c_int, _D, _D, _D]),
     "frgpu_poly_derivative": (C.c_int, [_D, C.c_long, C.c_int, _D, _D]),
     "frgpu_last_error": (C.c_int, [C.c_char_p, C.c_ulong]),

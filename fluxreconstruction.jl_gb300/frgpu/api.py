@@ -295,6 +295,11 @@ class ODEProblem:
         self.f(du, u, self, t)
         return du
 
+    def set_option(self, option: int, value: int) -> None:
+        """Kernel choice for measurements (frgpu_problem_set_option), e.g.
+        ``set_option(L.OPT_BGK_TENSOR, 0)`` for the CUDA-core BGK transport."""
+        check(L.lib().frgpu_problem_set_option(self._h, int(option), int(value)))
+
     def __del__(self):
         if getattr(self, "_h", None) is not None and L._lib is not None:
             L._lib.frgpu_problem_destroy(self._h)

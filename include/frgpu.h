@@ -58,6 +58,7 @@ enum frgpu_bc {
 };
 enum frgpu_correction { FRGPU_RADAU = 0, FRGPU_SD = 1, FRGPU_HUYNH = 2 };
 enum frgpu_indicator { FRGPU_IND_NONE = 0, FRGPU_IND_PLAIN = 1, FRGPU_IND_MLP = 2 };
+enum frgpu_option { FRGPU_OPT_BGK_TENSOR = 1 };
 
 typedef struct frgpu_space frgpu_space;
 typedef struct frgpu_problem frgpu_problem;
@@ -159,6 +160,10 @@ FRGPU_API int frgpu_modal_filter(frgpu_problem *p, int indicator, double lam, do
                                  int *ntroubled);
 /* Per-element troubled flags of the last filter application (ne ints). */
 FRGPU_API int frgpu_troubled_flags(frgpu_problem *p, int *flags, long n);
+/* Kernel choice for measurements; no counterpart in the reference.
+ * FRGPU_OPT_BGK_TENSOR: 1 (default) runs the FP32 BGK transport as a TF32-split
+ * tensor-core product, 0 on the CUDA cores.  The next step re-captures its graph. */
+FRGPU_API int frgpu_problem_set_option(frgpu_problem *p, int option, int value);
 /* Device pointer to the primary state array and its element type size
  * (8 for FP64, 4 for FP32K), for zero-copy hand-off; the stream the problem's
  * kernels run on; the number of this library's kernel launches so far. */
@@ -199,6 +204,46 @@ FRGPU_API int frgpu_modal_features(frgpu_problem *p, float *feat, long n);
  * network-vs-plain disagreements (misfires judged by the plain test),
  * stats[2] elements decided by the plain fallback. */
 FRGPU_API int frgpu_indicator_stats(frgpu_problem *p, int *stats);
+
+/* ======================================================================
+ * Batched ensembles of 1D Burgers instances of uneven size and degree.  Each
+ * instance is the scalar residual of frode_advection!
+ * (src/Equation/eq_advection.jl:55-77) with the flux u^2/2 on periodic
+ * [x0, x1]; frgpu_ensemble_run advances all of them to t_end in one
+ * persistent kernel launch.  No single call in the reference does this: it
+ * replaces a host loop over FRAdvectionProblem-style problems.
+ * ==================================================================== */
+typedef struct frgpu_ensemble frgpu_ensemble;
+FRGPU_API int frgpu_ensemble_config4_sizes(int n, unsigned seed, int *ne, int *deg);
+FRGPU_API int frgpu_ensemble_create(int n, const int *ne, const int *deg, double x0, double x1, int precision,
+                                    frgpu_ensemble **out);
+FRGPU_API void frgpu_ensemble_destroy(frgpu_ensemble *e);
+FRGPU_API long frgpu_ensemble_ndof(const frgpu_ensemble *e);
+FRGPU_API int frgpu_ensemble_set_state(frgpu_ensemble *e, int i, const double *u);
+FRGPU_API int frgpu_ensemble_get_state(frgpu_ensemble *e, int i, double *u);
+FRGPU_API int frgpu_ensemble_init_fourier(frgpu_ensemble *e, double sigma, unsigned seed);
+FRGPU_API int frgpu_ensemble_set_tiles(frgpu_ensemble *e, const int *thr);
+FRGPU_API int frgpu_ensemble_get_tiles(const frgpu_ensemble *e, int *thr);
+FRGPU_API int frgpu_ensemble_run(frgpu_ensemble *e, double t_end, double cfl, int filter);
+FRGPU_API int frgpu_ensemble_stats(const frgpu_ensemble *e, double *dof_stage_updates, int *max_steps, float *ms,
+                                   double *dt, int *steps);
+FRGPU_API int frgpu_ensemble_tune(frgpu_ensemble *e, double t_probe, double cfl, int filter, int *thr);
+FRGPU_API long frgpu_ensemble_launches(const frgpu_ensemble *e);
+/* Learned indicator in the ensemble's post-step filter (config-4 form; no
+ * counterpart in the reference): network m (NULL = plain modal-decay test of
+ * example/euler_highlevel.jl:37-52), probability threshold, fallback band
+ * within which the plain test decides.  The network is borrowed. */
+FRGPU_API int frgpu_ensemble_set_mlp(frgpu_ensemble *e, const frgpu_mlp *m, double threshold, double band);
+/* Last run's learned-indicator counts over all steps and instances:
+ * stats[0] troubled, [1] misfires (network != plain test), [2] fallbacks, [3] judged. */
+FRGPU_API int frgpu_ensemble_indicator_stats(frgpu_ensemble *e, long long *stats);
+/* Total element count over all instances. */
+FRGPU_API long frgpu_ensemble_nelem(const frgpu_ensemble *e);
+/* Training rows of the 1D learned indicator: 32 features per element (modal
+ * energies, degree one-hot, energy level) and the plain test's label (1 =
+ * troubled) for every element of the current state, instance by instance;
+ * n = frgpu_ensemble_nelem(e). */
+FRGPU_API int frgpu_ensemble_features(frgpu_ensemble *e, float *feat, int *labels, long n);
 
 /* Allocation-free 2D Euler reduction.  No counterpart in the reference: it
  * exists for callers that cannot let this library call cudaMalloc -- hosts

@@ -993,9 +993,15 @@ double fro_Linf_error(const double *u, const double *ue, long n, double dx) {
  * Learned indicator, FP64 reference for the GPU kernels' gradients
  * ---------------------------------------------------------------------- */
 
-static double gelu(double x) { return 0.5 * x * (1.0 + erf(x / sqrt(2.0))); }
+/* GELU in its tanh form (Hendrycks and Gimpel, arXiv:1606.08415) */
+static double gelu(double x) {
+    const double c = sqrt(2.0 / M_PI), a = 0.044715;
+    return 0.5 * x * (1.0 + tanh(c * (x + a * x * x * x)));
+}
 static double dgelu(double x) {
-    return 0.5 * (1.0 + erf(x / sqrt(2.0))) + x * exp(-0.5 * x * x) / sqrt(2.0 * M_PI);
+    const double c = sqrt(2.0 / M_PI), a = 0.044715;
+    const double t = tanh(c * (x + a * x * x * x));
+    return 0.5 * (1.0 + t) + 0.5 * x * (1.0 - t * t) * c * (1.0 + 3.0 * a * x * x);
 }
 
 void fro_mlp_forward(const double *P, const double *x, int n, int nin, int nh, double *y) {

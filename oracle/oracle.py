@@ -317,6 +317,16 @@ class Problem:
                                kappa, flags.ctypes.data_as(_I))
         return uf, flags.reshape((self.cfg.nx, self.cfg.ny), order="F"), n
 
+    def filter1d(self, u: np.ndarray, nvar: int, lam: float):
+        """example/euler_highlevel.jl:37-52 indicator + :l2 filter (1D)."""
+        uf = np.array(u, dtype=np.float64, order="F", copy=True)
+        flags = np.zeros(self.cfg.nx, dtype=np.int32)
+        V = _f64(self.space.V)
+        iV = _f64(self.space.iV)
+        n = lib().fro_filter1d(C.byref(self.cfg), uf.ctypes.data_as(_D), int(nvar), _p(V), _p(iV), float(lam),
+                               flags.ctypes.data_as(_I))
+        return uf, flags, n
+
     def features2d(self, u: np.ndarray) -> np.ndarray:
         uf = np.asfortranarray(u, dtype=np.float64)
         nn = self.cfg.nx * self.cfg.ny
