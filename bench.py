@@ -52,9 +52,10 @@ WORKLOAD = "2D Euler density wave, periodic [0,1]^2, 512x512 quads, p=3, LF flux
 # arrays per stage on average (stage 1 reads u^n and writes u1; stages 2 and 3
 # read u^n and the stage input and write the result).
 BYTES_PER_DOF_STAGE = {"fp32k": 4 * 8 / 3, "fp64": 8 * 8 / 3}
-# DRAM bytes (read + write) per stage launch measured by ncu on this workload;
-# summarised in profiles/euler2d_stage_512x512_p3.md.  None until captured.
-NCU_TRAFFIC_PER_LAUNCH = {"fp32k": None, "fp64": None}
+# DRAM bytes (read + write) per stage launch measured by ncu on this workload
+# (mean over the three SSPRK3 stages of the FP32K form); summarised in
+# profiles/euler2d_stage_512x512_p3.md.
+NCU_TRAFFIC_PER_LAUNCH = {"fp32k": 191.1e6, "fp64": None}
 
 
 def log(*a):
@@ -294,6 +295,169 @@ def gpu_arm(args, dist, rank, ws):
     return out, clocks
 
 
+def _event_timer(stream):
+    import torch
+
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def timer(fn):
+        ev[0].record(stream)
+        fn()
+        ev[1].record(stream)
+        ev[1].synchronize()
+        return ev[0].elapsed_time(ev[1]) / 1e3
+
+    return timer
+
+
+def shock_vortex_entry(steps=100, warmup=5):
+    """Config 3: shock-vortex on [0,2]x[0,1], 400x200, p=3, HLL, indicator +
+    :l2 filter after every step.  Learned + FP32K against plain FP64 (DOF
+    updates/s), the network's misfire rate (judged by the plain test on every
+    element of every step), and the L2 distance of each form's final density
+    from the plain FP64 run (the FP64 GPU path is bit-identical to the oracle
+    in the parity tests)."""
+    import torch
+
+    import frgpu
+    from frgpu import learned
+
+    ps = learned.config3_space()
+    net = learned.load_trained()
+    S0 = learned.filter_S0(3)
+    ndof = ps.nx * ps.ny * 16 * 4
+    out = {"workload": "shock-vortex 400x200 p=3 HLL, Mach 1.1 shock + Mach 0.25 vortex, filter every step",
+           "ndof": ndof, "steps": steps}
+    finals = {}
+    dt = None
+    for form, precision, ind in (("learned_fp32k", "fp32k", "mlp"), ("plain_fp32k", "fp32k", "plain"),
+                                 ("plain_fp64", "fp64", "plain")):
+        prob = learned.shock_vortex_problem(ps, 0.25, precision=precision)
+        itg = frgpu.init(prob, dt=1.0)
+        if dt is None:
+            dt = itg.cfl_dt(0.1)
+        itg.dt = dt
+        if ind == "mlp":
+            frgpu._lib.check(frgpu.lib().frgpu_problem_set_mlp(prob._h, net._h, 0.5, 0.0))
+        itg.set_filter(ind, learned.FILTER_LAMBDA, S0, learned.FILTER_KAPPA)
+        timer = _event_timer(torch.cuda.ExternalStream(itg.stream()))
+        itg.step(warmup)
+        itg.synchronize()
+        secs = timer(lambda: itg.step(steps))
+        rec = {"value": ndof * 3 * steps / secs, "ms_per_step": secs / steps * 1e3}
+        if ind == "mlp":
+            # misfires over a further stretch of steps, read after each step
+            st = np.zeros(3, dtype=np.int32)
+            mis = trb = fb = 0
+            for _ in range(50):
+                itg.step(1)
+                frgpu._lib.check(frgpu.lib().frgpu_indicator_stats(prob._h, st.ctypes.data_as(frgpu._lib._I)))
+                trb, mis, fb = trb + int(st[0]), mis + int(st[1]), fb + int(st[2])
+            rec["misfire_rate"] = mis / (50 * ps.nx * ps.ny)
+            rec["troubled_per_step"] = trb / 50
+        else:
+            itg.step(50)
+        finals[form] = itg.u[..., 0]
+        out[form] = rec
+    ref = finals["plain_fp64"]
+    for form in ("learned_fp32k", "plain_fp32k"):
+        out[form]["rms_rho_diff_vs_plain_fp64"] = float(np.sqrt(np.mean((finals[form] - ref) ** 2)))
+    out["speedup_learned_fp32k_vs_plain_fp64"] = out["learned_fp32k"]["value"] / out["plain_fp64"]["value"]
+    out["dt"] = dt
+    return out
+
+
+def ensemble_entry(n=4096, t_end=0.5):
+    """Config 4: 4096 Burgers instances (ne log-uniform [32,2048], p in 1..5,
+    8 random Fourier modes, seed 0) to t = 0.5 in one persistent launch, tiles
+    from the autotuner, FP32; the learned 1D indicator when its weights ship,
+    else the plain one.  DOF updates/s = sum_i 3 ndof_i steps_i / kernel time."""
+    import os as _os
+
+    from frgpu import learned
+    from frgpu.ensemble import Ensemble
+
+    e = Ensemble.config4(n, seed=0, precision="fp32")
+    have_net = _os.path.exists(learned.BURGERS_WEIGHTS)
+    if have_net:
+        e.set_mlp(learned.load_trained_burgers1d(), 0.5, 0.0)
+    tiles = e.tune(t_probe=0.01)
+    out = {"workload": f"{n} Burgers instances, ne log-uniform [32,2048], p 1..5, to t={t_end}, FP32",
+           "ndof": e.ndof, "tiles": [int(t) for t in tiles],
+           "indicator": "learned" if have_net else "plain"}
+    e.run(t_end)
+    st = e.stats()
+    out["value"] = st["dof_stage_updates"] / (st["ms"] * 1e-3)
+    out["ms"] = st["ms"]
+    out["max_steps"] = st["max_steps"]
+    out["launches_per_run"] = 1
+    if have_net:
+        out["indicator_stats"] = e.indicator_stats()
+        s = out["indicator_stats"]
+        out["misfire_rate"] = s["misfires"] / max(s["judged"], 1)
+        # the same ensemble with the plain indicator, for comparison
+        e2 = Ensemble.config4(n, seed=0, precision="fp32")
+        e2.tiles = tiles
+        e2.run(t_end)
+        st2 = e2.stats()
+        out["plain_indicator"] = {"value": st2["dof_stage_updates"] / (st2["ms"] * 1e-3), "ms": st2["ms"]}
+    return out
+
+
+def bgk_entry(steps=400, warmup=5):
+    """Config 5: BGK 1D1V, 256 elements on periodic [0,1], p=3, 512 velocity
+    midpoints on [-8,8], FP32, tau = Kn in {1e-4, 1e-2}, Maxwellian IC
+    rho = 1 + 0.1 sin(2 pi x), U = 1, T = 1, SSPRK3 at dt = 0.1 dx / 8.
+    Timed: `steps` steps; moments at t = 0.2 (4096 steps) against the FP64
+    path (bit-identical to the oracle in the parity tests)."""
+    import torch
+
+    import frgpu
+    from frgpu import _lib as L
+
+    ne, nv, deg = 256, 512, 3
+    dv = 16 / nv
+    v = -8 + (np.arange(nv) + 0.5) * dv
+    w = np.full(nv, dv)
+    ps = frgpu.FRPSpace1D(0, 1, ne, deg)
+    rho = 1 + 0.1 * np.sin(2 * np.pi * ps.xpg)
+    f = np.zeros((ne, nv, deg + 1), order="F")
+    for k in range(deg + 1):
+        f[:, :, k] = rho[:, k, None] * np.sqrt(1 / np.pi) * np.exp(-(v[None, :] - 1) ** 2)
+    dt = 0.1 * (1 / ne) / 8
+    nfull = int(round(0.2 / dt))
+    ndof = ne * nv * (deg + 1)
+    out = {"workload": "BGK 1D1V 256 el x 512 vel, p=3, FP32, SSPRK3 to t=0.2", "ndof": ndof, "dt": dt,
+           "steps_to_t02": nfull}
+
+    def moments(u):
+        return np.stack([np.einsum("ivk,v->ik", u, w * c) for c in (np.ones(nv), v, 0.5 * v * v)])
+
+    for kn in (1e-2, 1e-4):
+        rec = {}
+        for form, precision, tensor in (("fp32_tensor", "fp32k", 1), ("fp32_cuda_cores", "fp32k", 0),
+                                        ("fp64", "fp64", 0)):
+            prob = frgpu.FRBGKProblem(f, (0, 1), ps, v, w, kn, precision=precision)
+            if precision == "fp32k":
+                prob.set_option(L.OPT_BGK_TENSOR, tensor)
+            itg = frgpu.init(prob, dt=dt)
+            timer = _event_timer(torch.cuda.ExternalStream(itg.stream()))
+            itg.step(warmup)
+            itg.synchronize()
+            secs = timer(lambda: itg.step(steps))
+            rec[form] = {"value": ndof * 3 * steps / secs, "stage_us": secs / (3 * steps) * 1e6}
+            itg.u = f
+            itg.step(nfull)
+            rec[form]["moments"] = moments(itg.u)
+        ref = rec["fp64"].pop("moments")
+        for form in ("fp32_tensor", "fp32_cuda_cores"):
+            m = rec[form].pop("moments")
+            rec[form]["moment_rel_err_vs_fp64"] = [float(np.max(np.abs(m[q] - ref[q])) / np.max(np.abs(ref[q])))
+                                                   for q in range(3)]
+        out[f"Kn={kn:g}"] = rec
+    return out
+
+
 def cpu_baseline(target_s=12.0, nthreads=None):
     """The oracle (FP64, OpenMP) on the full 512x512 p=3 mesh, timed over as many
     SSPRK3 steps as fit in about target_s seconds (at least one)."""
@@ -330,6 +494,7 @@ def main():
     # carries the forms that ran
     ap.add_argument("--forms", default="")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the shock-vortex, ensemble and BGK entries")
     args = ap.parse_args()
     ws, rank, _ = dist_env()
     dist = init_dist(ws)
@@ -390,6 +555,15 @@ def main():
         "gpu_launches": lrn["launches_timed"],
         "clocks": clocks,
     }
+    if not args.no_configs:
+        # the other workloads of the spec, each on its own clock (not part of `value`)
+        line["configs"] = {}
+        for name, fn in (("shock_vortex_400x200_p3", shock_vortex_entry), ("burgers_ensemble_4096", ensemble_entry),
+                         ("bgk_256x512_p3", bgk_entry)):
+            try:
+                line["configs"][name] = fn()
+            except Exception as e:  # report, do not lose the headline line
+                line["configs"][name] = {"error": f"{type(e).__name__}: {e}"}
     if not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline()

@@ -63,6 +63,7 @@ struct frgpu_ensemble {
     void *u = nullptr, *s1 = nullptr, *s2 = nullptr, *backup = nullptr, *ops = nullptr;
     EnsInstance *d_inst = nullptr;
     int *d_qc = nullptr, *d_qw = nullptr, *d_counters = nullptr, *d_steps = nullptr, *d_status = nullptr;
+    int *d_failed = nullptr; // per instance: 0 or the step at which it turned non-finite
     double *d_dt = nullptr;
     cudaStream_t stream = nullptr;
     int thr[5] = {128, 128, 128, 128, 128}; // warp queue if ne <= thr[deg-1]
@@ -82,7 +83,8 @@ static void ens_free(frgpu_ensemble *e) {
     if (!e) return;
     if (e->stream) cudaStreamSynchronize(e->stream);
     void *b[] = {e->u,         e->s1,     e->s2,     e->backup,   e->ops,      e->d_inst,  e->d_qc,
-                 e->d_qw,      e->d_counters, e->d_steps, e->d_status, e->d_dt, e->d_istats, e->d_eoff};
+                 e->d_qw,      e->d_counters, e->d_steps, e->d_status, e->d_dt, e->d_istats, e->d_eoff,
+                 e->d_failed};
     for (void *p : b)
         if (p) cudaFree(p);
     if (e->stream) cudaStreamDestroy(e->stream);
@@ -134,6 +136,7 @@ static EnsArgs<Real> ens_args(frgpu_ensemble *e, int n_cta, int n_warp, double t
     a.filter = filter;
     a.dt_out = e->d_dt;
     a.steps_out = e->d_steps;
+    a.failed = e->d_failed;
     a.status = e->d_status;
     a.mlp = frmlp::MLPDev{nullptr, nullptr, nullptr, nullptr};
     if (e->mlp) {
@@ -276,6 +279,8 @@ FRGPU_API int frgpu_ensemble_create(int n, const int *ne, const int *deg, double
         FR_CUDA(cudaMalloc(&e->d_dt, sizeof(double) * n));
         FR_CUDA(cudaMalloc(&e->d_status, sizeof(int)));
         FR_CUDA(cudaMemset(e->d_status, 0, sizeof(int)));
+        FR_CUDA(cudaMalloc(&e->d_failed, sizeof(int) * n));
+        FR_CUDA(cudaMemset(e->d_failed, 0, sizeof(int) * n));
         FR_CUDA(cudaMalloc(&e->d_istats, sizeof(unsigned long long) * 4));
         FR_CUDA(cudaMemset(e->d_istats, 0, sizeof(unsigned long long) * 4));
         std::vector<long> eoff(n);
@@ -317,6 +322,7 @@ FRGPU_API int frgpu_ensemble_set_state(frgpu_ensemble *e, int i, const double *u
         return FRGPU_ERR_ARG;
     }
     const long n = (long)e->inst[i].ne * e->inst[i].np;
+    FR_CUDA(cudaMemset(e->d_failed + i, 0, sizeof(int)));
     if (e->esize == 8) {
         FR_CUDA(cudaMemcpy((double *)e->u + e->inst[i].off, u, sizeof(double) * n, cudaMemcpyHostToDevice));
     } else {
@@ -379,6 +385,7 @@ FRGPU_API int frgpu_ensemble_init_fourier(frgpu_ensemble *e, double sigma, unsig
                 all[in.off + el + (long)in.ne * k] = v;
             }
     }
+    FR_CUDA(cudaMemset(e->d_failed, 0, sizeof(int) * e->n));
     if (e->esize == 8) {
         FR_CUDA(cudaMemcpy(e->u, all.data(), sizeof(double) * e->ndof, cudaMemcpyHostToDevice));
     } else {
@@ -525,6 +532,27 @@ FRGPU_API int frgpu_ensemble_indicator_stats(frgpu_ensemble *e, long long *stats
     FR_CUDA(cudaStreamSynchronize(e->stream));
     for (int c = 0; c < 4; ++c) stats[c] = (long long)h[c];
     return FRGPU_OK;
+}
+
+/* Instances stopped because their state turned non-finite (flags[i] = the
+ * step, 1-based, after which instance i stopped; 0 = running normally).
+ * Returns the number of stopped instances, or a negative error.  A stopped
+ * instance stays stopped in later runs until its state is set again
+ * (frgpu_ensemble_set_state / frgpu_ensemble_init_fourier). */
+FRGPU_API int frgpu_ensemble_failed(frgpu_ensemble *e, int *flags) {
+    if (!e) {
+        fr_set_error("ensemble_failed: null ensemble");
+        return FRGPU_ERR_ARG;
+    }
+    std::vector<int> f(e->n);
+    FR_CUDA(cudaMemcpyAsync(f.data(), e->d_failed, sizeof(int) * e->n, cudaMemcpyDeviceToHost, e->stream));
+    FR_CUDA(cudaStreamSynchronize(e->stream));
+    int cnt = 0;
+    for (int i = 0; i < e->n; ++i) {
+        cnt += f[i] != 0;
+        if (flags) flags[i] = f[i];
+    }
+    return cnt;
 }
 
 /* Number of elements over all instances (the rows of frgpu_ensemble_features). */

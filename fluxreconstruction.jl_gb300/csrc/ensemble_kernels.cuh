@@ -58,6 +58,7 @@ template <class Real> struct EnsArgs {
     int filter;
     double *dt_out;                    // per instance dt used (diagnostics)
     int *steps_out;                    // per instance number of steps
+    int *failed;                       // per instance: 0, or the step (1-based) whose state was non-finite
     int *status;
     frmlp::MLPDev mlp;                 // P == nullptr: plain indicator
     float thr, band;                   // learned decision threshold, fallback band
@@ -78,6 +79,12 @@ struct EnsLearn {
     float thr, band;
     bool on;
 };
+
+// Does any thread of the worker group (CTA or warp) hold p?  Also a barrier.
+template <int G> __device__ __forceinline__ bool group_any(bool p) {
+    if (G == 32) return __any_sync(0xffffffffu, p);
+    return __syncthreads_or(p) != 0;
+}
 
 // Synchronisation of a worker group: the CTA (256 threads) or one warp.
 template <int G> __device__ __forceinline__ void group_sync() {
@@ -290,6 +297,10 @@ __device__ void ens_run(const EnsArgs<Real> &a, int id, Real *s_t, double *s_red
     Real *u = a.u + in.off, *s1 = a.s1 + in.off, *s2 = a.s2 + in.off;
     const int ne = in.ne;
     const EnsOps<Real> &op = *a.ops;
+    if (a.failed[id] != 0) { // stopped by an earlier run: its state is not finite
+        if (r == 0) a.steps_out[id] = 0;
+        return;
+    }
     // max |u| over the instance (FP64), then the CFL time step
     double mx = 0.0;
     for (size_t q = r; q < (size_t)ne * NP; q += G) mx = fmax(mx, fabs((double)u[q]));
@@ -314,9 +325,19 @@ __device__ void ens_run(const EnsArgs<Real> &a, int id, Real *s_t, double *s_red
     for (long s = 0; s < nsteps; ++s) {
         const double h = s < nfull ? dt : last;
         const Real hr = (Real)h;
-        ens_stage<Real, NP, G, 1>(u, u, s1, ne, J, hr, op, s_t, r, bad);
-        ens_stage<Real, NP, G, 2>(s1, u, s2, ne, J, hr, op, s_t, r, bad);
-        ens_stage<Real, NP, G, 3>(s2, u, u, ne, J, hr, op, s_t, r, bad);
+        int sbad = 0;
+        ens_stage<Real, NP, G, 1>(u, u, s1, ne, J, hr, op, s_t, r, sbad);
+        ens_stage<Real, NP, G, 2>(s1, u, s2, ne, J, hr, op, s_t, r, sbad);
+        ens_stage<Real, NP, G, 3>(s2, u, u, ne, J, hr, op, s_t, r, sbad);
+        // an instance whose state turned non-finite stops here (the others go on);
+        // the whole group takes the same decision
+        if (group_any<G>(sbad != 0)) {
+            if (r == 0) {
+                a.failed[id] = (int)(s + 1);
+                a.steps_out[id] = (int)(s + 1);
+            }
+            break;
+        }
         if (a.filter) {
             const double lam = h * op.expfac[NP - 2] * 0.15;
             if (LEARNED)

@@ -15,34 +15,67 @@ namespace {
 constexpr int RED_BLOCKS = FR_RED_BLOCKS;
 constexpr int RED_THREADS = 256;
 
+// Accumulator of a thread's partial sums.  FP64 form: plain double.  FP32K
+// form (state hi + lo in FP32): a double-float pair (s, e) updated by Knuth's
+// TwoSum, so the FP32 pipe carries an FP64-accurate sum over the thread's
+// values; the cross-thread tree is FP64.
+template <class Real> struct SumAcc;
+template <> struct SumAcc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double hi, double lo) { s += hi + lo; }
+    __device__ __forceinline__ double value() const { return s; }
+};
+template <> struct SumAcc<float> {
+    float s = 0.f, e = 0.f;
+    __device__ __forceinline__ void add(float hi, float lo) {
+        const float t = __fadd_rn(s, hi);
+        const float bp = __fsub_rn(t, s);
+        const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(hi, bp));
+        s = t;
+        e = __fadd_rn(e, __fadd_rn(err, lo));
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)e; }
+};
+
+// Block (b, q) of a grid (eblocks, nq) reduces solution point q of the
+// elements [b chunk, (b + 1) chunk): the unweighted sums of the four
+// conserved variables (scaled by the quadrature weight wp[q] in FP64 at the
+// end), the largest directional wave speed max(|u| + c, |v| + c) and the
+// largest CFL rate (|u| + c)/dx + (|v| + c)/dy.  The wave speeds are
+// evaluated in the state's precision.
 template <class Real>
 __global__ void __launch_bounds__(RED_THREADS) k_reduce2d_partial(const Real *__restrict__ u, const Real *__restrict__ lo,
-                                                             size_t plane, int np, const double *__restrict__ wp,
+                                                             size_t plane, int nq, const double *__restrict__ wp,
                                                              double gamma, double idx_, double idy_,
                                                              double *__restrict__ part) {
-    // part layout: [block][6]: 4 sums, max directional speed, max CFL rate
-    double s[4] = {0, 0, 0, 0}, smax = 0, rmax = 0;
-    const int nq = np * np;
+    // part layout: [q * gridDim.x + b][6]: 4 sums, max directional speed, max CFL rate
+    const int q = blockIdx.y;
     const size_t npts = plane * nq;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < npts; t += (size_t)gridDim.x * blockDim.x) {
-        const int q = (int)(t / plane);
-        double w[4];
+    const size_t chunk = (plane + gridDim.x - 1) / gridDim.x;
+    const size_t e0 = (size_t)blockIdx.x * chunk, e1 = e0 + chunk < plane ? e0 + chunk : plane;
+    const Real g = (Real)gamma, gm1 = (Real)(gamma - 1.0), ix = (Real)idx_, iy = (Real)idy_;
+    SumAcc<Real> acc[4];
+    Real smax = Real(0), rmax = Real(0);
+    for (size_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const size_t t = e + plane * q;
+        Real w[4];
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
-            double v = (double)u[t + npts * m];
-            if (lo != nullptr) v += (double)lo[t + npts * m];
-            w[m] = v;
-            s[m] += wp[q] * v;
+            const Real h = u[t + npts * m];
+            const Real l = lo != nullptr ? lo[t + npts * m] : Real(0);
+            acc[m].add(h, l);
+            w[m] = h + l;
         }
-        double U = w[1] / w[0], V = w[2] / w[0];
-        double p = (gamma - 1.0) * (w[3] - 0.5 * (w[1] * U + w[2] * V));
-        double c = sqrt(gamma * p / w[0]);
-        double a = fabs(U) + c, b = fabs(V) + c;
-        smax = fmax(smax, fmax(a, b));
-        rmax = fmax(rmax, a * idx_ + b * idy_);
+        const Real rinv = frk::recipR<Real>(w[0]);
+        const Real U = w[1] * rinv, V = w[2] * rinv;
+        const Real p = gm1 * (w[3] - Real(0.5) * (w[1] * U + w[2] * V));
+        const Real c = frk::sqrtP<Real>(g * p * rinv);
+        const Real a = fabs(U) + c, bb = fabs(V) + c;
+        smax = fmax(smax, fmax(a, bb));
+        rmax = fmax(rmax, a * ix + bb * iy);
     }
     __shared__ double red[6][RED_THREADS / 32];
-    double vals[6] = {s[0], s[1], s[2], s[3], smax, rmax};
+    double vals[6] = {acc[0].value(), acc[1].value(), acc[2].value(), acc[3].value(), (double)smax, (double)rmax};
 #pragma unroll
     for (int v = 0; v < 6; ++v) {
         double x = vals[v];
@@ -57,7 +90,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce2d_partial(const Real *__
         const int v = threadIdx.x;
         double x = red[v][0];
         for (int w = 1; w < RED_THREADS / 32; ++w) x = v < 4 ? x + red[v][w] : fmax(x, red[v][w]);
-        part[blockIdx.x * 6 + v] = x;
+        part[((size_t)q * gridDim.x + blockIdx.x) * 6 + v] = v < 4 ? x * wp[q] : x;
     }
 }
 
@@ -85,16 +118,16 @@ int fr_launch_euler2d_reduce(frgpu_problem *p, const void *state, const void *lo
     double *wp = p->d_red + FR_RED_WP;
     double *part = p->d_red;
     double *fin = p->d_red + FR_RED_FINAL;
+    const int nq = np * np;
+    const dim3 grid(RED_BLOCKS / nq, nq);
     if (p->d.precision == FRGPU_FP64)
-        k_reduce2d_partial<double><<<RED_BLOCKS, RED_THREADS, 0, p->stream>>>((const double *)state, (const double *)lo,
-                                                                           plane, np, wp, p->d.gamma, cfl_dx,
-                                                                           cfl_dy, part);
+        k_reduce2d_partial<double><<<grid, RED_THREADS, 0, p->stream>>>((const double *)state, (const double *)lo,
+                                                                     plane, nq, wp, p->d.gamma, cfl_dx, cfl_dy, part);
     else
-        k_reduce2d_partial<float><<<RED_BLOCKS, RED_THREADS, 0, p->stream>>>((const float *)state, (const float *)lo,
-                                                                          plane, np, wp, p->d.gamma, cfl_dx, cfl_dy,
-                                                                          part);
+        k_reduce2d_partial<float><<<grid, RED_THREADS, 0, p->stream>>>((const float *)state, (const float *)lo,
+                                                                    plane, nq, wp, p->d.gamma, cfl_dx, cfl_dy, part);
     FR_CUDA(cudaGetLastError());
-    k_reduce_final<<<1, 32, 0, p->stream>>>(part, RED_BLOCKS, fin);
+    k_reduce_final<<<1, 32, 0, p->stream>>>(part, (int)(grid.x * grid.y), fin);
     FR_CUDA(cudaGetLastError());
     p->launches += 2;
     double h[6];
@@ -118,9 +151,10 @@ int fr_launch_euler2d_reduce(frgpu_problem *p, const void *state, const void *lo
 // the same partial/final reduction kernels as frgpu_reduce, but its partial
 // sums live in the file-scope device array below instead of memory allocated
 // per problem.  The array is 4096 x 6 doubles (192 KiB); one partial block
-// covers up to NOALLOC_POINTS_PER_BLOCK solution points, so a call accepts at
-// most 4096 * 16384 = 67,108,864 solution points (nx * ny * (deg+1)^2) and
-// rejects larger meshes.  Every GPU that loads the library keeps the array
+// covers one solution point q of up to NOALLOC_POINTS_PER_BLOCK elements, so a
+// call needs ceil(nx * ny / 16384) * (deg+1)^2 <= 4096 blocks: at most
+// 67,108,864 solution points (nx * ny * (deg+1)^2), and larger meshes are
+// rejected.  Every GPU that loads the library keeps the array
 // until the process exits.
 namespace {
 constexpr int NOALLOC_MAX_BLOCKS = 4096;
@@ -181,7 +215,8 @@ extern "C" FRGPU_API int frgpu_reduce2d_noalloc(const void *d_state, const void 
     const int np = deg + 1;
     const size_t plane = (size_t)nx * ny;
     const size_t npts = plane * np * np;
-    const long nblocks = (long)((npts + NOALLOC_POINTS_PER_BLOCK - 1) / NOALLOC_POINTS_PER_BLOCK);
+    const long eblocks = (long)((plane + NOALLOC_POINTS_PER_BLOCK - 1) / NOALLOC_POINTS_PER_BLOCK);
+    const long nblocks = eblocks * np * np;
     if (nblocks > NOALLOC_MAX_BLOCKS) {
         fr_set_error("reduce2d_noalloc: " + std::to_string(npts) + " solution points exceed the maximum of " +
                      std::to_string((long)NOALLOC_MAX_BLOCKS * NOALLOC_POINTS_PER_BLOCK) +
@@ -194,12 +229,13 @@ extern "C" FRGPU_API int frgpu_reduce2d_noalloc(const void *d_state, const void 
     cudaStream_t st = (cudaStream_t)stream;
     // each partial block overwrites its own six slots, so the previous call's
     // contents never need clearing
+    const dim3 grid((unsigned)eblocks, (unsigned)(np * np));
     if (precision == FRGPU_FP64)
-        k_reduce2d_partial<double><<<(int)nblocks, RED_THREADS, 0, st>>>(
-            (const double *)d_state, (const double *)d_lo, plane, np, d_wp, gamma, 1.0 / dx, 1.0 / dy, part);
+        k_reduce2d_partial<double><<<grid, RED_THREADS, 0, st>>>(
+            (const double *)d_state, (const double *)d_lo, plane, np * np, d_wp, gamma, 1.0 / dx, 1.0 / dy, part);
     else
-        k_reduce2d_partial<float><<<(int)nblocks, RED_THREADS, 0, st>>>(
-            (const float *)d_state, (const float *)d_lo, plane, np, d_wp, gamma, 1.0 / dx, 1.0 / dy, part);
+        k_reduce2d_partial<float><<<grid, RED_THREADS, 0, st>>>(
+            (const float *)d_state, (const float *)d_lo, plane, np * np, d_wp, gamma, 1.0 / dx, 1.0 / dy, part);
     FR_CUDA(cudaGetLastError());
     k_reduce_final_scaled<<<1, 32, 0, st>>>(part, (int)nblocks, dx * dy * 0.25, d_out);
     FR_CUDA(cudaGetLastError());

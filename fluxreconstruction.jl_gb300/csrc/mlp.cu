@@ -277,22 +277,30 @@ struct IV1 {
 // upper lane the pressure values.  The lower lane's su is the plain
 // modal-decay ratio of the density.  Lanes of elements past the end (valid
 // false) must still take part in the exchange; they return zero features.
+// The raw values a lane needs: the four variables at its 8 points.
 template <class Real>
-__device__ __forceinline__ void element_features(const Real *__restrict__ u, size_t ne, size_t e, bool valid,
-                                                 bool pressure, const IV1 &iv, float gm1, float (&feat)[16],
-                                                 float &su) {
-    float v[16];
+__device__ __forceinline__ void load_raw(const Real *__restrict__ u, size_t ne, size_t e, bool valid, bool pressure,
+                                         float (&w)[8][4]) {
     const int q0 = pressure ? 8 : 0;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-        float w0 = 1.f, w1 = 0.f, w2 = 0.f, w3 = 0.f;
         if (valid) {
             const size_t at = e + ne * (size_t)(q0 + k);
-            w0 = (float)u[at];
-            w1 = (float)u[at + ne * 16];
-            w2 = (float)u[at + ne * 32];
-            w3 = (float)u[at + ne * 48];
+#pragma unroll
+            for (int m = 0; m < 4; ++m) w[k][m] = (float)u[at + ne * 16 * (size_t)m];
+        } else {
+            w[k][0] = 1.f;
+            w[k][1] = w[k][2] = w[k][3] = 0.f;
         }
+    }
+}
+
+__device__ __forceinline__ void features_from_raw(const float (&w)[8][4], bool valid, bool pressure, const IV1 &iv,
+                                                  float gm1, float (&feat)[16], float &su) {
+    float v[16];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const float w0 = w[k][0], w1 = w[k][1], w2 = w[k][2], w3 = w[k][3];
         const float ri = __fdividef(1.0f, w0);
         const float pk = gm1 * (w3 - 0.5f * (w1 * (w1 * ri) + w2 * (w2 * ri)));
         const float recv = __shfl_xor_sync(0xffffffffu, pressure ? w0 : pk, 16);
@@ -333,6 +341,15 @@ __device__ __forceinline__ void element_features(const Real *__restrict__ u, siz
     }
 }
 
+template <class Real>
+__device__ __forceinline__ void element_features(const Real *__restrict__ u, size_t ne, size_t e, bool valid,
+                                                 bool pressure, const IV1 &iv, float gm1, float (&feat)[16],
+                                                 float &su) {
+    float w[8][4];
+    load_raw<Real>(u, ne, e, valid, pressure, w);
+    features_from_raw(w, valid, pressure, iv, gm1, feat, su);
+}
+
 // One warp per 16 elements (the indicator kernel's tiling, so that training
 // features and inference features are the same numbers).
 template <class Real>
@@ -368,7 +385,7 @@ __device__ __forceinline__ bool plain_troubled(float su, float S0, float kappa) 
 // network does.  stats: [0] troubled, [1] network vs plain disagreements
 // (misfires, judged by the plain test), [2] fallbacks.
 template <class Real>
-__global__ void __launch_bounds__(32 * WARPS, 5) k_mlp_indicator(MLPDev w, Real *__restrict__ u, Real *__restrict__ lo,
+__global__ void __launch_bounds__(32 * WARPS, 4) k_mlp_indicator(MLPDev w, Real *__restrict__ u, Real *__restrict__ lo,
                                                             size_t ne, const Real *__restrict__ V,
                                                             const Real *__restrict__ iV, IV1 iv, float gm1,
                                                             float thr, float band, float S0, float kappa, double lam,
@@ -387,11 +404,20 @@ __global__ void __launch_bounds__(32 * WARPS, 5) k_mlp_indicator(MLPDev w, Real 
     float *prob = prob_all[warp];
     const size_t ntiles = (ne + 15) / 16;
     int n_trouble = 0, n_mis = 0, n_fb = 0;
-    for (size_t tile = (size_t)blockIdx.x * WARPS + warp; tile < ntiles; tile += (size_t)gridDim.x * WARPS) {
+    const bool pr = lane >= 16;
+    const size_t step = (size_t)gridDim.x * WARPS;
+    float raw[8][4]; // this lane's values of the tile being processed, loaded one tile ahead
+    size_t tile = (size_t)blockIdx.x * WARPS + warp;
+    if (tile < ntiles) load_raw<Real>(u, ne, tile * 16 + (lane & 15), tile * 16 + (lane & 15) < ne, pr, raw);
+    for (; tile < ntiles; tile += step) {
         const size_t e = tile * 16 + (lane & 15);
-        const bool pr = lane >= 16;
         float feat[16], su = 0.f;
-        element_features<Real>(u, ne, e, e < ne, pr, iv, gm1, feat, su);
+        features_from_raw(raw, e < ne, pr, iv, gm1, feat, su);
+        // issue the next tile's loads now; they land while the network runs
+        if (tile + step < ntiles) {
+            const size_t en = (tile + step) * 16 + (lane & 15);
+            load_raw<Real>(u, ne, en, en < ne, pr, raw);
+        }
 #pragma unroll
         for (int a = 0; a < 16; ++a) xs[(lane & 15) * NIN + (pr ? 16 : 0) + a] = __float2bfloat16_rn(feat[a]);
         __syncwarp();
@@ -720,10 +746,10 @@ int fr_launch_mlp_indicator(frgpu_problem *p, double lam, double S0, double kapp
     }
     const size_t ne = (size_t)p->sp.nx * p->sp.ny;
     const size_t ntiles = (ne + 15) / 16;
-    // persistent: as many CTAs as fit at once (5 per SM at 96 registers per thread)
+    // persistent: as many CTAs as fit at once (4 per SM at <= 128 registers per thread)
     int nsm = 152;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device);
-    const int grid = (int)std::min<size_t>((ntiles + WARPS - 1) / WARPS, (size_t)nsm * 5);
+    const int grid = (int)std::min<size_t>((ntiles + WARPS - 1) / WARPS, (size_t)nsm * 4);
     const float gm1 = (float)(p->d.gamma - 1.0);
     FR_CUDA(cudaMemsetAsync(p->d_count, 0, sizeof(int) * 4, p->stream));
     const MLPDev w = p->mlp->dev();

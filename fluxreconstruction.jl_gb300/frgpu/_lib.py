@@ -101,6 +101,7 @@ SIGNATURES = {
     "frgpu_ensemble_set_mlp": (C.c_int, [_VP, _VP, C.c_double, C.c_double]),
     "frgpu_ensemble_indicator_stats": (C.c_int, [_VP, C.POINTER(C.c_longlong)]),
     "frgpu_ensemble_nelem": (C.c_long, [_VP]),
+    "frgpu_ensemble_failed": (C.c_int, [_VP, _I]),
     "frgpu_ensemble_features": (C.c_int, [_VP, _F, _I, C.c_long]),
     "frgpu_interp_face": (C.c_int, [_D, C.c_long, C.c_int, _D, _D, _D]),
     "frgpu_poly_derivative": (C.c_int, [_D, C.c_long, C.c_int, _D, _D]),

@@ -8,7 +8,7 @@ import math
 import numpy as np
 
 from . import _lib as L
-from ._lib import check, dptr
+from ._lib import check, dptr, fptr
 
 _PREC = {"fp64": L.FP64, "fp32": L.FP32K}
 
@@ -73,8 +73,19 @@ class Ensemble:
         t = np.ascontiguousarray(thr, dtype=np.int32)
         check(L.lib().frgpu_ensemble_set_tiles(self._h, t.ctypes.data_as(L._I)))
 
-    def run(self, t_end, cfl=0.4, filter=True):
+    def run(self, t_end, cfl=0.4, filter=True) -> int:
+        """Advance every running instance by t_end; returns the number of
+        instances stopped so far because their state turned non-finite."""
         check(L.lib().frgpu_ensemble_run(self._h, float(t_end), float(cfl), int(bool(filter))))
+        return self.failed().astype(bool).sum()
+
+    def failed(self) -> np.ndarray:
+        """Per instance: 0, or the step after which it stopped (non-finite state)."""
+        f = np.zeros(self.n, dtype=np.int32)
+        rc = L.lib().frgpu_ensemble_failed(self._h, f.ctypes.data_as(L._I))
+        if rc < 0:
+            check(rc)
+        return f
 
     def tune(self, t_probe=0.01, cfl=0.4, filter=True):
         t = np.zeros(5, dtype=np.int32)
@@ -94,3 +105,27 @@ class Ensemble:
 
     def launches(self) -> int:
         return int(L.lib().frgpu_ensemble_launches(self._h))
+
+    def set_mlp(self, net, threshold=0.5, band=0.0):
+        """Learned indicator in the post-step filter (None: plain modal-decay test)."""
+        check(L.lib().frgpu_ensemble_set_mlp(self._h, net._h if net is not None else None, float(threshold),
+                                             float(band)))
+        self._net = net  # the library borrows the network
+
+    def indicator_stats(self):
+        """Last run's learned-indicator counts over all steps and instances."""
+        s = (C.c_longlong * 4)()
+        check(L.lib().frgpu_ensemble_indicator_stats(self._h, s))
+        return {"troubled": s[0], "misfires": s[1], "fallbacks": s[2], "judged": s[3]}
+
+    @property
+    def nelem(self) -> int:
+        return int(L.lib().frgpu_ensemble_nelem(self._h))
+
+    def features(self):
+        """(features [nelem, 32] float32, plain labels [nelem] int32) of the current state."""
+        n = self.nelem
+        feat = np.zeros((n, 32), dtype=np.float32)
+        lab = np.zeros(n, dtype=np.int32)
+        check(L.lib().frgpu_ensemble_features(self._h, fptr(feat), lab.ctypes.data_as(L._I), n))
+        return feat, lab

@@ -299,18 +299,102 @@ def train_config3(nseeds=64, nsteps=2400, every=240, epochs=20, batch=4096, lr=2
     return m, rec
 
 
+# ---------------------------------------------------------------- 1D Burgers ensembles
+# The ensemble's indicator is the 1D modal-decay test of
+# example/euler_highlevel.jl:37-52 (su = u_N^2 / (sum u^2 + 1e-6), S0 =
+# -3 log10(deg), kappa = 4).  Its learned replacement sees 32 features per
+# element: the normalised modal energies (slots 0..deg), a degree one-hot
+# (slots 8..12) and the energy level against the 1e-6 floor (slot 16).
+BURGERS_WEIGHTS = _os.path.join(_os.path.dirname(_os.path.abspath(__file__)), "data", "burgers1d_mlp.npy")
+BURGERS_RECORD = _os.path.join(_os.path.dirname(_os.path.abspath(__file__)), "data", "burgers1d_mlp.json")
+
+
+def burgers_label_run(n_inst, seed, t_samples, cfl=0.4, keep_neg=0.03):
+    """Features and plain labels of a config-4-like ensemble (sizes and ICs
+    from Philox with `seed`) run with the plain indicator, sampled at the
+    times `t_samples`; all troubled elements and `keep_neg` of the others."""
+    from .ensemble import Ensemble, config4_sizes
+
+    ne, deg = config4_sizes(n_inst, seed)
+    e = Ensemble(ne, deg, precision="fp32")
+    e.init_fourier(0.3, seed)
+    rng = np.random.default_rng(seed)
+    xs, ts = [], []
+    t = 0.0
+    for ts_ in t_samples:
+        e.run(ts_ - t, cfl=cfl, filter=True)
+        t = ts_
+        x, lab = e.features()
+        # rows of instances stopped by a blow-up are not finite: leave them out
+        keep = ((lab > 0) | (rng.random(len(lab)) < keep_neg)) & np.all(np.isfinite(x), axis=1)
+        xs.append(x[keep])
+        ts.append(lab[keep].astype(np.float32))
+    return np.concatenate(xs), np.concatenate(ts)
+
+
+def load_trained_burgers1d() -> "MLPIndicator":
+    """The network trained by `train_burgers1d` (shipped with the package)."""
+    return MLPIndicator.load(BURGERS_WEIGHTS)
+
+
+def train_burgers1d(n_inst=512, nseeds=16, t_samples=(0.05, 0.1, 0.15, 0.2, 0.25, 0.3, 0.35, 0.4, 0.45, 0.5),
+                    epochs=20, batch=4096, lr=2e-3, seed=0, log=print):
+    """Labels from plain-indicator ensembles with Philox seeds 1000..1000+nseeds-1
+    (the config-4 bench uses seed 0); the last two seeds are held out."""
+    import json
+    import time
+
+    t0 = time.time()
+    seeds = [1000 + s for s in range(nseeds)]
+    parts = [burgers_label_run(n_inst, s, t_samples) for s in seeds]
+    x = np.concatenate([p[0] for p in parts[:-2]])
+    t = np.concatenate([p[1] for p in parts[:-2]])
+    xv = np.concatenate([p[0] for p in parts[-2:]])
+    tv = np.concatenate([p[1] for p in parts[-2:]])
+    t_data = time.time() - t0
+    log(f"dataset: {len(t)} samples ({int(t.sum())} troubled), validation {len(tv)} ({int(tv.sum())}); {t_data:.1f} s")
+    xb, tb = balance(x, t, seed=seed)
+    m = MLPIndicator(seed=seed)
+    t1 = time.time()
+    losses = m.train(xb, tb, epochs=epochs, batch=batch, lr=lr, seed=seed)
+    t_train = time.time() - t1
+    yv = m.forward(xv)
+    pred = yv > 0.5
+    lab = tv > 0.5
+    rec = {
+        "config": dict(n_inst=n_inst, seeds=seeds, t_samples=list(t_samples), epochs=epochs, batch=batch, lr=lr,
+                       seed=seed, sigma=0.3, cfl=0.4),
+        "samples": int(len(t)), "troubled": int(t.sum()), "balanced_samples": int(len(tb)),
+        "loss_per_epoch": [float(v) for v in losses],
+        "validation": {"samples": int(len(tv)), "troubled": int(lab.sum()),
+                       "accuracy": float(np.mean(pred == lab)),
+                       "false_positive": int(np.sum(pred & ~lab)), "false_negative": int(np.sum(~pred & lab))},
+        "seconds": {"labels": t_data, "training": t_train},
+    }
+    log(json.dumps(rec["validation"]))
+    return m, rec
+
+
 def main(argv=None):
     import argparse
     import json
 
-    ap = argparse.ArgumentParser(description="train the learned troubled-cell indicator on config 3")
-    ap.add_argument("--out", default=WEIGHTS)
-    ap.add_argument("--record", default=RECORD)
-    ap.add_argument("--nseeds", type=int, default=64)
+    ap = argparse.ArgumentParser(description="train a learned troubled-cell indicator")
+    ap.add_argument("--workload", choices=["shock-vortex", "burgers1d"], default="shock-vortex")
+    ap.add_argument("--out", default=None)
+    ap.add_argument("--record", default=None)
+    ap.add_argument("--nseeds", type=int, default=None)
     ap.add_argument("--nsteps", type=int, default=2400)
     ap.add_argument("--epochs", type=int, default=20)
     a = ap.parse_args(argv)
-    m, rec = train_config3(nseeds=a.nseeds, nsteps=a.nsteps, epochs=a.epochs)
+    if a.workload == "burgers1d":
+        m, rec = train_burgers1d(nseeds=a.nseeds or 16, epochs=a.epochs)
+        a.out = a.out or BURGERS_WEIGHTS
+        a.record = a.record or BURGERS_RECORD
+    else:
+        m, rec = train_config3(nseeds=a.nseeds or 64, nsteps=a.nsteps, epochs=a.epochs)
+        a.out = a.out or WEIGHTS
+        a.record = a.record or RECORD
     _os.makedirs(_os.path.dirname(a.out), exist_ok=True)
     m.save(a.out)
     with open(a.record, "w") as f:

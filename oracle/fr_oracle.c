@@ -932,6 +932,37 @@ void fro_modal_features2d(const fro_cfg *c, const double *u, const double *iV, d
     }
 }
 
+/* Features of the 1D learned indicator of a scalar state u[ne, np] (32 per
+ * element): slots 0..np-1 the normalised modal energies as in the 2D form,
+ * slot 8 + deg - 1 a degree one-hot, slot 16 the energy level
+ * clamp(log10(sum u_hat^2 + 1e-30) + 6, -8, 8) / 8, other slots 0.  The modes
+ * are u_hat = iV u of the indicator of example/euler_highlevel.jl:37-40. */
+void fro_modal_features1d(const fro_cfg *c, const double *u, const double *iV, double *feat) {
+    int ne = c->nx, np = c->np;
+    for (long e = 0; e < ne; ++e) {
+        double uh[8], tot = 0.0;
+        for (int a = 0; a < np; ++a) {
+            double s = 0.0;
+            for (int b = 0; b < np; ++b) s += iV[a + np * b] * u[e + (long)ne * b];
+            uh[a] = s;
+            tot += s * s;
+        }
+        double *row = feat + e * 32;
+        for (int q = 0; q < 32; ++q) row[q] = 0.0;
+        for (int a = 0; a < np; ++a) {
+            double x = log10(uh[a] * uh[a] / tot + 1e-16);
+            if (x < -16.0) x = -16.0;
+            if (x > 0.0) x = 0.0;
+            row[a] = x / 8.0 + 1.0;
+        }
+        row[8 + np - 2] = 1.0;
+        double lv = log10(tot + 1e-30) + 6.0;
+        if (lv < -8.0) lv = -8.0;
+        if (lv > 8.0) lv = 8.0;
+        row[16] = lv / 8.0;
+    }
+}
+
 /* ------------------------------------------------------------------------
  * Reductions and norms
  * ---------------------------------------------------------------------- */

@@ -81,6 +81,7 @@ int fro_filter1d(const fro_cfg *c, double *u, int nvar, const double *V, const d
                  double lam, int *flags);
 /* modal energies for the learned indicator: per element 2*np^2 features */
 void fro_modal_features2d(const fro_cfg *c, const double *u, const double *iV, double *feat);
+void fro_modal_features1d(const fro_cfg *c, const double *u, const double *iV, double *feat);
 
 /* ---- reductions and norms ---- */
 void fro_conserved_sums2d(const fro_cfg *c, const double *u, const double *wp, double *sums);

@@ -82,6 +82,7 @@ def lib():
                                        C.c_double, _I]),
             "fro_filter1d": (C.c_int, [C.POINTER(Cfg), _D, C.c_int, _D, _D, C.c_double, _I]),
             "fro_modal_features2d": (None, [C.POINTER(Cfg), _D, _D, _D]),
+            "fro_modal_features1d": (None, [C.POINTER(Cfg), _D, _D, _D]),
             "fro_conserved_sums2d": (None, [C.POINTER(Cfg), _D, _D, _D]),
             "fro_max_speed2d": (C.c_double, [C.POINTER(Cfg), _D]),
             "fro_L1_error": (C.c_double, [_D, _D, C.c_long, C.c_double]),
@@ -335,6 +336,14 @@ class Problem:
         iV = _f64(self.space.iV)
         lib().fro_modal_features2d(C.byref(self.cfg), uf.ctypes.data_as(_D), _p(iV), _p(feat))
         return feat.reshape(nn, 2 * N)
+
+    def features1d(self, u: np.ndarray) -> np.ndarray:
+        """Features of the 1D learned indicator (32 per element) of a scalar state u[ne, np]."""
+        uf = np.asfortranarray(u, dtype=np.float64)
+        feat = np.zeros(self.cfg.nx * 32)
+        iV = _f64(self.space.iV)
+        lib().fro_modal_features1d(C.byref(self.cfg), uf.ctypes.data_as(_D), _p(iV), _p(feat))
+        return feat.reshape(self.cfg.nx, 32)
 
     def conserved_sums2d(self, u: np.ndarray) -> np.ndarray:
         uf = np.asfortranarray(u, dtype=np.float64)

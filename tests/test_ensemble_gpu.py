@@ -101,3 +101,88 @@ def test_config4_sizes_and_autotuner(frgpu):
         assert np.array_equal(a, b)
     e.run(0.01)
     assert np.all(np.isfinite(e.get_state(0)))
+
+
+# ---------------------------------------------------------------- learned 1D indicator
+def test_ensemble_features_and_labels_match_oracle(frgpu, oracle):
+    """Features (BF16-rounded, as the network sees them) and plain labels of
+    every element against the oracle's features1d and filter1d flags."""
+    e = small_ensemble(frgpu, "fp64")
+    e.run(0.1, filter=True)  # steepening fronts: some elements are troubled
+    feat, lab = e.features()
+    assert feat.shape == (e.nelem, 32) and lab.sum() > 0
+    row = 0
+    for i in range(e.n):
+        ne, deg = int(e.ne[i]), int(e.deg[i])
+        u = e.get_state(i)
+        ps = frgpu.FRPSpace1D(0, 2 * math.pi, ne, deg)
+        po = oracle.Space1D(0, 2 * math.pi, ne, deg)
+        for f in ("ll", "lr", "dl", "dhl", "dhr", "V", "iV", "wp", "J"):
+            setattr(po, f, np.array(getattr(ps, f)))
+        P = oracle.Problem(oracle.BURGERS, po)
+        ref = P.features1d(u)
+        _, flags, _ = P.filter1d(u, 1, 0.0)
+        got = feat[row:row + ne]
+        assert np.array_equal(lab[row:row + ne], flags), i
+        # BF16 keeps 8 significant bits; compare modes carrying energy above 1e-8 of the total
+        sel = np.zeros_like(ref, dtype=bool)
+        sel[:, :deg + 1] = ref[:, :deg + 1] > 0
+        sel[:, 8:17] = True
+        assert np.max(np.abs(got[sel] - ref[sel])) < 1e-2, i
+        row += ne
+    assert row == e.nelem
+
+
+def test_learned_full_fallback_equals_plain(frgpu):
+    """band = 0.5 sends every element to the plain test: the learned path must
+    then reproduce the plain indicator + filter bit for bit (FP64)."""
+    from frgpu import learned
+
+    outs = []
+    for mode in ("plain", "mlp"):
+        e = small_ensemble(frgpu, "fp64")
+        if mode == "mlp":
+            e.set_mlp(learned.MLPIndicator(seed=3), 0.5, 0.5)
+        e.run(0.2, filter=True)
+        outs.append([e.get_state(i) for i in range(e.n)])
+        if mode == "mlp":
+            st = e.indicator_stats()
+            assert st["fallbacks"] == st["judged"] > 0 and st["troubled"] > 0
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+
+
+def test_trained_burgers1d_indicator_agrees_with_plain(frgpu):
+    """The shipped 1D network on held-out config-4 instances (seed 0, which
+    training never saw): misfires below 5% of the elements judged, finite run."""
+    import os
+
+    from frgpu import learned
+    from frgpu.ensemble import Ensemble
+
+    if not os.path.exists(learned.BURGERS_WEIGHTS):
+        pytest.skip("no trained 1D network shipped yet")
+    e = Ensemble.config4(512, seed=0, precision="fp32")
+    e.set_mlp(learned.load_trained_burgers1d(), 0.5, 0.0)
+    e.run(0.5)
+    st = e.indicator_stats()
+    assert st["judged"] > 0 and st["troubled"] > 0
+    assert st["misfires"] < 0.05 * st["judged"]
+    assert all(np.all(np.isfinite(e.get_state(i))) for i in range(0, 512, 51))
+
+
+def test_non_finite_instance_stops_alone(frgpu, oracle):
+    """With the reference's filter strength (lambda = dt e^(0.875 deg) 0.15) the
+    2048-element p = 2 instance blows up before t = 0.3, on the GPU and in the
+    oracle alike.  It stops there, the other 15 instances finish and still
+    match the oracle bit for bit, and setting its state again revives it."""
+    e = small_ensemble(frgpu, "fp64")
+    u0 = [e.get_state(i) for i in range(e.n)]
+    e.run(0.3, filter=True)
+    f = e.failed()
+    assert np.flatnonzero(f).tolist() == [11]
+    for i in (0, 4, 12, 15):
+        ref, _, _ = oracle_run(oracle, frgpu, int(e.ne[i]), int(e.deg[i]), u0[i], 0.3, 0.4, True)
+        assert np.array_equal(e.get_state(i), ref), i
+    e.set_state(11, u0[11])
+    assert e.failed()[11] == 0
