@@ -53,8 +53,8 @@ WORKLOAD = "2D Euler density wave, periodic [0,1]^2, 512x512 quads, p=3, LF flux
 # read u^n and the stage input and write the result).
 BYTES_PER_DOF_STAGE = {"fp32k": 4 * 8 / 3, "fp64": 8 * 8 / 3}
 # DRAM bytes (read + write) per stage launch measured by ncu on this workload
-# (mean over the three SSPRK3 stages of the FP32K form); summarised in
-# profiles/euler2d_stage_512x512_p3.md.
+# (mean over the three SSPRK3 stages of the FP32K form; the capture of the
+# 512x512 p=3 stage kernels kept under profiles/).
 NCU_TRAFFIC_PER_LAUNCH = {"fp32k": 191.1e6, "fp64": None}
 
 
@@ -362,8 +362,30 @@ def shock_vortex_entry(steps=100, warmup=5):
     ref = finals["plain_fp64"]
     for form in ("learned_fp32k", "plain_fp32k"):
         out[form]["rms_rho_diff_vs_plain_fp64"] = float(np.sqrt(np.mean((finals[form] - ref) ** 2)))
+    # matched error: element-mean density of each form against a run on the
+    # 2x refined mesh (800 x 400, plain indicator, half the step, same end time),
+    # aggregated to the coarse elements
+    nsteps_total = warmup + steps + 50
+    psf = frgpu.FRPSpace2D(ps.x0, ps.x1, 2 * ps.nx, ps.y0, ps.y1, 2 * ps.ny, 3)
+    probf = learned.shock_vortex_problem(psf, 0.25, precision="fp32k")
+    itgf = frgpu.init(probf, dt=dt / 2)
+    itgf.set_filter("plain", learned.FILTER_LAMBDA, S0, learned.FILTER_KAPPA)
+    itgf.step(2 * nsteps_total)
+    w1 = np.polynomial.legendre.leggauss(4)[1]
+    W = np.outer(w1, w1) / 4
+
+    def means(rho):
+        return np.einsum("ijkl,kl->ij", rho, W)
+
+    mf = means(itgf.u[..., 0])
+    mf = 0.25 * (mf[0::2, 0::2] + mf[1::2, 0::2] + mf[0::2, 1::2] + mf[1::2, 1::2])
+    errs = {form: float(np.sqrt(np.mean((means(finals[form]) - mf) ** 2))) for form in finals}
+    out["rms_element_mean_rho_err_vs_refined"] = errs
+    out["matched"] = {"ratio_learned_fp32k_to_plain_fp64": errs["learned_fp32k"] / errs["plain_fp64"],
+                      "within_1.5x": bool(errs["learned_fp32k"] <= 1.5 * errs["plain_fp64"])}
     out["speedup_learned_fp32k_vs_plain_fp64"] = out["learned_fp32k"]["value"] / out["plain_fp64"]["value"]
     out["dt"] = dt
+    out["t_end"] = nsteps_total * dt
     return out
 
 
@@ -495,9 +517,25 @@ def main():
     ap.add_argument("--forms", default="")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-configs", action="store_true", help="skip the shock-vortex, ensemble and BGK entries")
+    # profiling aid: run one of the other workloads alone (small sizes through --steps / --instances)
+    ap.add_argument("--workload", choices=["shock_vortex", "ensemble", "bgk"], default=None)
+    ap.add_argument("--instances", type=int, default=4096)
     args = ap.parse_args()
     ws, rank, _ = dist_env()
     dist = init_dist(ws)
+
+    if args.workload is not None:
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        if args.workload == "shock_vortex":
+            r = shock_vortex_entry(steps=args.steps, warmup=args.warmup)
+        elif args.workload == "ensemble":
+            r = ensemble_entry(n=args.instances, t_end=0.5)
+        else:
+            r = bgk_entry(steps=args.steps, warmup=args.warmup)
+        print(json.dumps({"partial_run": True, "workload": args.workload, "result": r}), flush=True)
+        return
 
     if args.impl == "reference":
         if rank != 0:

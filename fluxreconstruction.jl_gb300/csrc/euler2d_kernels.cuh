@@ -54,12 +54,14 @@ template <int NP> struct Tile<float, NP> {
     static constexpr int TY = NP <= 2 ? 8 : (NP <= 4 ? 2 : 1);
 };
 
-// NST: state-sized stash arrays holding the stage update's extra inputs
-// (u^n in FP64 stages 2-3; the increment, and in stage 3 also the high and
-// low parts, in FP32K), loaded together with the state so that their latency
-// is not exposed after the residual.
+// NST: state-sized stash arrays holding the stage update's extra inputs,
+// loaded together with the state so that their latency is not exposed after
+// the residual: u^n in FP64 stages 2-3.  The FP32K stages instead read their
+// extra inputs (increment; in stage 3 also the high and low parts) directly
+// in the update, after an L2 prefetch issued before the y sweep: that keeps
+// shared memory at one residual's worth, so three CTAs fit on an SM.
 template <int MODE, int STAGE> struct Stash {
-    static constexpr int n = MODE == MODE_FP32K ? (STAGE == 2 ? 1 : (STAGE == 3 ? 3 : 0)) : (STAGE >= 2 ? 1 : 0);
+    static constexpr int n = MODE == MODE_FP32K ? 0 : (STAGE >= 2 ? 1 : 0);
 };
 
 template <class Real, int NP, int TX, int TY, int NST = 0> struct Smem {
@@ -97,8 +99,10 @@ __device__ __forceinline__ Real ld_state(const Real *__restrict__ uin, const Rea
     return v;
 }
 
+// FP32 CTAs of up to 256 threads: registers capped so that three CTAs share an SM
 template <class Real, int NP, int FLUX, int MODE, int STAGE>
-__global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
+__global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
+                                  sizeof(Real) == 4 && Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY <= 256 ? 3 : 1)
     k_euler2d(const E2DArgs<Real, NP> a) {
     constexpr int TX = Tile<Real, NP>::TX, TY = Tile<Real, NP>::TY;
     constexpr int NT = TX * NP * TY;
@@ -131,7 +135,10 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
     const int nx = a.nx, ny = a.ny;
     const int vx = min(TX, nx - i0), vy = min(TY, ny - j0);
     const bool valid = ex < vx && ey < vy;
-    const size_t plane = (size_t)nx * ny;
+    // 32-bit offsets into the state arrays (problem_create keeps every array
+    // below 2^32 values); 64-bit products of the plane stride cost the kernel
+    // about 50 registers per thread
+    const unsigned plane = (unsigned)nx * (unsigned)ny;
     const Real *__restrict__ uin = a.uin;
     const Real *__restrict__ din = a.din;
     const Ops<Real, NP> &op = a.ops;
@@ -148,7 +155,7 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
             const Real *w = side == 0 ? op.lr : op.ll;
             int jo;
             if (resolve(jn, ny, a.bc[2], a.bc[3], jo)) {
-                const size_t base = (size_t)(i0 + hx) + (size_t)nx * jo + plane * hk;
+                const unsigned base = (unsigned)(i0 + hx) + (unsigned)nx * jo + plane * hk;
 #pragma unroll
                 for (int m = 0; m < 4; ++m) {
                     Real v[NP];
@@ -176,7 +183,7 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
             const Real *w = side == 0 ? op.lr : op.ll;
             int io;
             if (resolve(in_, nx, a.bc[0], a.bc[1], io)) {
-                const size_t base = (size_t)io + (size_t)nx * (j0 + hy) + plane * (NP * hl);
+                const unsigned base = (unsigned)io + (unsigned)nx * (j0 + hy) + plane * (NP * hl);
 #pragma unroll
                 for (int m = 0; m < 4; ++m) {
                     Real v[NP];
@@ -203,20 +210,15 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
         const int l = ln;
         Real u[NP][4];
         if (valid) {
-            const size_t base = (size_t)i + (size_t)nx * j + plane * (NP * l);
+            const unsigned base = (unsigned)i + (unsigned)nx * j + plane * (NP * l);
 #pragma unroll
             for (int m = 0; m < 4; ++m)
 #pragma unroll
                 for (int k = 0; k < NP; ++k) {
-                    const size_t idx = base + plane * (k + NP * NP * m);
+                    const unsigned idx = base + plane * (k + NP * NP * m);
                     if (MODE == MODE_FP32K && STAGE >= 2) {
                         const Real h = __ldg(uin + idx), d = __ldg(din + idx);
                         u[k][m] = h + d;
-                        SST(0, ey, l, k, m, ex) = d;
-                        if (STAGE == 3) {
-                            SST(1, ey, l, k, m, ex) = h;
-                            SST(2, ey, l, k, m, ex) = a.ul[idx];
-                        }
                     } else {
                         u[k][m] = ld_state(uin, din, idx);
                         if (MODE == MODE_FP64 && STAGE >= 2) SST(0, ey, l, k, m, ex) = a.un[idx];
@@ -294,6 +296,22 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
     __syncthreads();
 
     // ---- phase C: y interface flux; x correction into s_g -------------------
+    // FP32K: bring the stage update's extra inputs of this thread's column
+    // into L2 now; phase D reads them after the Riemann solves and corrections
+    if (MODE == MODE_FP32K && STAGE >= 2 && valid) {
+        const unsigned pb = (unsigned)i + (unsigned)nx * j + plane * ln;
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+#pragma unroll
+            for (int l = 0; l < NP; ++l) {
+                const unsigned idx = pb + plane * (NP * (l + NP * m));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(din + idx));
+                if (STAGE == 3) {
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(uin + idx));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.ul + idx));
+                }
+            }
+    }
     {
         const int k = ln;
         if (valid) {
@@ -333,7 +351,7 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
     if (valid) {
         const int k = ln;
         const Real dt = (Real)(*a.dtp);
-        const size_t base = (size_t)i + (size_t)nx * j + plane * k;
+        const unsigned base = (unsigned)i + (unsigned)nx * j + plane * k;
         Real chk = Real(0);
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
@@ -343,7 +361,7 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
             for (int l = 0; l < NP; ++l) {
                 const Real r = fmaR<Real>(bT, op.dgr[l], fmaR<Real>(bB, op.dgl[l], SG(ey, l, k, m, ex) + ry[l][m]));
                 const Real du = -r;
-                const size_t idx = base + plane * (NP * (l + NP * m));
+                const unsigned idx = base + plane * (NP * (l + NP * m));
                 Real res;
                 if (STAGE == 0) {
                     res = du;
@@ -368,14 +386,14 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY)
                         res = dt * du;
                         a.out[idx] = res;
                     } else if (STAGE == 2) {
-                        const Real d1 = SST(0, ey, l, k, m, ex);
+                        const Real d1 = __ldg(din + idx);
                         res = fmaR<Real>(dt, du, d1) * Real(0.25);
                         a.out[idx] = res;
                     } else {
-                        const Real d2 = SST(0, ey, l, k, m, ex);
+                        const Real d2 = __ldg(din + idx);
                         const Real d3 = fmaR<Real>(dt, du, d2) * Real(2.0 / 3.0);
-                        const Real hi = SST(1, ey, l, k, m, ex);
-                        const Real lo = SST(2, ey, l, k, m, ex);
+                        const Real hi = __ldg(uin + idx);
+                        const Real lo = a.ul[idx];
                         const Real y = d3 + lo;
                         const Real t = hi + y;
                         const Real lo_new = y - (t - hi);

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <string>
 #include <vector>
 
@@ -48,6 +49,8 @@ struct frgpu_problem {
     const frgpu_mlp *mlp = nullptr; // learned indicator (borrowed)
     float mlp_thr = 0.5f, mlp_band = 0.0f;
     int bgk_tensor = 1;             // FP32 BGK transport on the tensor cores
+    float *d_bgk_prim = nullptr;    // FP32 BGK: (rho, U, lambda) per (element, point), from the moments
+    uint32_t *d_bgk_frag = nullptr; // FP32 BGK: TF32 A fragments of the transport operator (both signs, split)
     // captured step graph
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int graph_ind = -1;
@@ -100,6 +103,7 @@ int fr_launch_scalar1d(frgpu_problem *p, int stage, const void *in, const void *
 int fr_launch_euler1d(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
 int fr_launch_bgk1d(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
 int fr_launch_bgk1d_tc(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
+int fr_bgk_tc_setup(frgpu_problem *p); // device buffers of the tensor-core BGK path
 int fr_launch_interp_face(const double *d_f, long n, int np, const double *ll, const double *lr, double *d_out,
                           cudaStream_t st);
 int fr_launch_poly_derivative(const double *d_f, long n, int np, const double *pdm, double *d_out,

@@ -291,7 +291,8 @@ static void free_problem(frgpu_problem *p) {
     for (auto &g : p->gexec)
         if (g) cudaGraphExecDestroy(g);
     void *bufs[] = {p->s0, p->s1, p->s2, p->s3, p->d_dt, p->d_status, p->d_red, p->d_flags, p->d_count,
-                    p->d_velo, p->d_w, p->d_J, p->d_V, p->d_iV, p->rhs_in, p->rhs_out};
+                    p->d_velo, p->d_w, p->d_J, p->d_V, p->d_iV, p->rhs_in, p->rhs_out, p->d_bgk_prim,
+                    p->d_bgk_frag};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -431,6 +432,9 @@ FRGPU_API int frgpu_problem_create(const frgpu_space *s, const frgpu_problem_des
         FR_REQ((d->bc[0] == FRGPU_BC_PERIODIC) == (d->bc[1] == FRGPU_BC_PERIODIC) &&
                    (d->bc[2] == FRGPU_BC_PERIODIC) == (d->bc[3] == FRGPU_BC_PERIODIC),
                "problem_create: periodic boundaries come in pairs");
+        // the 2D kernels address a state array with 32-bit offsets
+        FR_REQ((unsigned long long)s->nx * s->ny * s->np * s->np * 4ull < (1ull << 32),
+               "problem_create: 2D state exceeds 2^32 values (nx * ny * (deg+1)^2 * 4)");
     } else if (eq == FRGPU_BGK1D) {
         FR_REQ(d->bc[0] == FRGPU_BC_PERIODIC, "problem_create: BGK supports periodic boundaries");
     } else {
@@ -508,6 +512,7 @@ FRGPU_API int frgpu_problem_create(const frgpu_space *s, const frgpu_problem_des
             if (eq == FRGPU_BGK1D) {
                 if ((r2 = upload_vec(p, &p->d_velo, p->velo))) return r2;
                 if ((r2 = upload_vec(p, &p->d_w, p->weights))) return r2;
+                if (p->d.precision == FRGPU_FP32K && (r2 = fr_bgk_tc_setup(p))) return r2;
             }
             return FRGPU_OK;
         }()))

@@ -139,6 +139,39 @@ function FREuler2DProblem(u::AbstractArray{<:Real,5}, tspan, ps, γ; flux=:hll, 
     return ODEProblem(rhs!, Array{Float64}(u), tspan, p)
 end
 
+"""The `mol!` closure of example/bgk_wave.jl:69-129 (1D1V BGK, kinetic upwind flux,
+relaxation time τ) on the reference's FRPSpace1D and velocity grid `velo`/`weights`;
+`f[i, v, k]` is the reference's layout.  `precision=:fp32k` runs the transport on the
+tensor cores."""
+function FRBGKProblem(f::AbstractArray{<:Real,3}, tspan, ps, velo, weights, τ; precision=:fp64)
+    v = collect(Float64, velo)
+    w = collect(Float64, weights)
+    d = ProblemDesc(BGK1D, FLUX[:upwind], PRECISION[precision], ntuple(_ -> BC[:period], 4),
+                    NTuple{16,Cdouble}(zeros(16)), 1.0, 3.0, τ, length(v), pointer(v), pointer(w), 1e-8, 1e-6)
+    p = GC.@preserve v w Problem(Space(ps), d, size(f))
+    return ODEProblem(rhs!, Array{Float64}(f), tspan, p)
+end
+
+const INDICATOR = Dict(:none => Cint(0), :plain => Cint(1), :mlp => Cint(2))
+
+"""The post-step troubled-cell indicator + `modal_filter!(û, λ; filter=:l2)` loop of
+example/shock-vortex.jl:308-321 (2D) / example/euler_highlevel.jl:37-52 (1D), run inside
+every `step!` from now on (`indicator = :none` switches it off)."""
+function set_filter!(itg, indicator::Symbol, λ, S0, κ)
+    check(ccall((:frgpu_set_filter, libfrgpu), Cint, (Ptr{Cvoid}, Cint, Cdouble, Cdouble, Cdouble),
+                itg.p.h, INDICATOR[indicator], λ, S0, κ))
+    return nothing
+end
+
+"""Apply the indicator + :l2 modal filter once to the integrator's state; returns the
+number of troubled elements."""
+function modal_filter!(itg, indicator::Symbol, λ, S0, κ)
+    n = Ref{Cint}(0)
+    check(ccall((:frgpu_modal_filter, libfrgpu), Cint, (Ptr{Cvoid}, Cint, Cdouble, Cdouble, Cdouble, Ref{Cint}),
+                itg.p.h, INDICATOR[indicator], λ, S0, κ, n))
+    return Int(n[])
+end
+
 """interp_face!(fδ, f, ll, lr) of src/interpolate.jl:1-10, evaluated on the GPU."""
 function interp_face!(fδ, f::AbstractMatrix, ll, lr)
     fh = Matrix{Float64}(f)

@@ -77,7 +77,8 @@ def test_bgk_tensor_and_cuda_core_forms_agree(frgpu, oracle):
         itg = frgpu.init(prob, dt=0.1 / ne / 8)
         l0 = itg.launches()
         itg.step(20)
-        assert itg.launches() - l0 == 60
+        # tensor-core form: a moments kernel and a transport kernel per stage
+        assert itg.launches() - l0 == (120 if on else 60)
         outs.append(itg.u)
     assert rel(outs[0], outs[1]) < 1e-5
 
