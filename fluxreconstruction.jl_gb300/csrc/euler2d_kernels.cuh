@@ -144,6 +144,34 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
     const Ops<Real, NP> &op = a.ops;
     int bad = 0;
 
+    // ---- phase A loads, issued before the halo so that both are in flight ----
+    const int i = i0 + ex, j = j0 + ey;
+    Real u[NP][4];
+    {
+        const int l = ln;
+        if (valid) {
+            const unsigned base = (unsigned)i + (unsigned)nx * j + plane * (NP * l);
+#pragma unroll
+            for (int m = 0; m < 4; ++m)
+#pragma unroll
+                for (int k = 0; k < NP; ++k) {
+                    const unsigned idx = base + plane * (k + NP * NP * m);
+                    if (MODE == MODE_FP32K && STAGE >= 2) {
+                        const Real h = __ldg(uin + idx), d = __ldg(din + idx);
+                        u[k][m] = h + d;
+                    } else {
+                        u[k][m] = ld_state(uin, din, idx);
+                        if (MODE == MODE_FP64 && STAGE >= 2) SST(0, ey, l, k, m, ex) = a.un[idx];
+                    }
+                }
+        } else {
+#pragma unroll
+            for (int k = 0; k < NP; ++k) {
+                u[k][0] = Real(1); u[k][1] = Real(0); u[k][2] = Real(0); u[k][3] = Real(1);
+            }
+        }
+    }
+
     // ---- halo: traces of the neighbours across the tile edges --------------
     for (int t = tid; t < 2 * NP * (TX + TY); t += NT) {
         if (t < 2 * NP * TX) {
@@ -204,32 +232,9 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
     }
 
     // ---- phase A: x-line (element ex, row l = ln) --------------------------
-    const int i = i0 + ex, j = j0 + ey;
     Real rx[NP][4], fxl[4], fxr[4];
     {
         const int l = ln;
-        Real u[NP][4];
-        if (valid) {
-            const unsigned base = (unsigned)i + (unsigned)nx * j + plane * (NP * l);
-#pragma unroll
-            for (int m = 0; m < 4; ++m)
-#pragma unroll
-                for (int k = 0; k < NP; ++k) {
-                    const unsigned idx = base + plane * (k + NP * NP * m);
-                    if (MODE == MODE_FP32K && STAGE >= 2) {
-                        const Real h = __ldg(uin + idx), d = __ldg(din + idx);
-                        u[k][m] = h + d;
-                    } else {
-                        u[k][m] = ld_state(uin, din, idx);
-                        if (MODE == MODE_FP64 && STAGE >= 2) SST(0, ey, l, k, m, ex) = a.un[idx];
-                    }
-                }
-        } else {
-#pragma unroll
-            for (int k = 0; k < NP; ++k) {
-                u[k][0] = Real(1); u[k][1] = Real(0); u[k][2] = Real(0); u[k][3] = Real(1);
-            }
-        }
         Real fx[NP][4], gy[NP][4];
 #pragma unroll
         for (int k = 0; k < NP; ++k) euler2d_flux<Real>(u[k], a.gm1, a.iJx, a.iJy, fx[k], gy[k], bad);
@@ -281,15 +286,22 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             riemann2d<Real, 0, FLUX>(wL, wR, a.gamma, a.gm1, F);
 #pragma unroll
             for (int m = 0; m < 4; ++m) SFX(ey, l, m, ex) = F[m];
-            if (ex == vx - 1) {
+        }
+        // the TY * NP faces on the tile's right edge, by the first threads of
+        // warp 0 only (an extra solve on every warp's last lane would make all
+        // warps wait for it)
+        if (tid < TY * NP) {
+            const int ye = tid / NP, le = tid % NP;
+            if (ye < vy) {
+                Real wL[4], wR[4], F[4];
 #pragma unroll
                 for (int m = 0; m < 4; ++m) {
-                    wL[m] = STR(s_uxr, ey, l, m, ex);
-                    wR[m] = SHX(1, ey, l, m);
+                    wL[m] = STR(s_uxr, ye, le, m, vx - 1);
+                    wR[m] = SHX(1, ye, le, m);
                 }
                 riemann2d<Real, 0, FLUX>(wL, wR, a.gamma, a.gm1, F);
 #pragma unroll
-                for (int m = 0; m < 4; ++m) SFX(ey, l, m, ex + 1) = F[m];
+                for (int m = 0; m < 4; ++m) SFX(ye, le, m, vx) = F[m];
             }
         }
     }
