@@ -16,8 +16,11 @@
 // recomputed from global memory (L2-resident) with the same arithmetic as the
 // owner, so both sides of every face see bit-identical fluxes.
 #pragma once
+#include <type_traits>
+
 #include "fr_common.cuh"
 #include "frgpu_internal.h"
+#include "mlp_device.cuh"
 
 using namespace frk;
 
@@ -38,6 +41,16 @@ template <class Real, int NP> struct E2DArgs {
     Real fixed[4][4];
     Ops<Real, NP> ops;
     int *status;
+    // learned indicator fused into stage 3 (FP32K, np = 4): network, 1D inverse
+    // Vandermonde factor, decision threshold / fallback band, plain-test S0 and
+    // kappa, filter strength, V / iV of the filter, per-element flags and the
+    // [troubled, misfires, fallbacks] counters
+    frmlp::MLPDev mlp;
+    frmlp::IV1 iv1;
+    float ind_thr, ind_band, ind_S0, ind_kappa;
+    double ind_lam;
+    const Real *V, *iV;
+    int *flags, *stats;
 };
 
 template <class Real, int NP> struct Tile;
@@ -100,7 +113,10 @@ __device__ __forceinline__ Real ld_state(const Real *__restrict__ uin, const Rea
 }
 
 // FP32 CTAs of up to 256 threads: registers capped so that three CTAs share an SM
-template <class Real, int NP, int FLUX, int MODE, int STAGE>
+// FUSE: stage 3 of the FP32K form with np = 4 also runs the learned troubled-cell
+// indicator + :l2 filter on the elements it has just updated (the post-step
+// filter of example/shock-vortex.jl:308-321 with the network of mlp.cu).
+template <class Real, int NP, int FLUX, int MODE, int STAGE, bool FUSE = false>
 __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                                   sizeof(Real) == 4 && Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY <= 256 ? 3 : 1)
     k_euler2d(const E2DArgs<Real, NP> a) {
@@ -412,6 +428,7 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                         a.out[idx] = t;
                         a.ul[idx] = lo_new;
                         res = t;
+                        if (FUSE) SU(ey, l, k, m, ex) = t; // u is dead in FP32K phase D: it now holds u^{n+1}
                     }
                 }
                 chk += res; // NaN and Inf propagate into the check sum
@@ -420,6 +437,72 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
         if (!isfinite(chk)) bad |= ST_NONFINITE;
     }
     if (bad) atomicOr(a.status, bad);
+
+    // ---- fused learned indicator (FP32K stage 3, np = 4) --------------------
+    // Warps 0-3 each take 16 elements of the tile (one half-row): features from
+    // the new state in shared memory, the network (weights through L1; staging
+    // them in shared memory per CTA measured slower), the
+    // decision with the plain test as fallback and judge, and the :l2 filter
+    // of the troubled elements in global memory.
+    if constexpr (FUSE) {
+        static_assert(NP == 4 && TX == 32 && TY == 2, "the fused indicator works on 32 x 2 tiles of np = 4");
+        __syncthreads();
+        const int warp = tid >> 5, lane = tid & 31;
+        if (warp < 4) {
+            using namespace frmlp;
+            __nv_bfloat16 *xs = reinterpret_cast<__nv_bfloat16 *>(s_g) + warp * 16 * NIN;
+            float *prob = reinterpret_cast<float *>(s_g) + 2 * 16 * NIN + warp * 16;
+            const int h = warp & 1, eyt = warp >> 1;
+            const int exl = 16 * h + (lane & 15);
+            const bool pr = lane >= 16;
+            const bool ev = exl < vx && eyt < vy;
+            float w[8][4];
+#pragma unroll
+            for (int kq = 0; kq < 8; ++kq) {
+                const int q = (pr ? 8 : 0) + kq, kk = q & 3, ll = q >> 2;
+#pragma unroll
+                for (int m = 0; m < 4; ++m) w[kq][m] = ev ? (float)SU(eyt, ll, kk, m, exl) : (m == 0 ? 1.f : 0.f);
+            }
+            float feat[16], su = 0.f;
+            features_from_raw(w, ev, pr, a.iv1, (float)a.gm1, feat, su);
+#pragma unroll
+            for (int q = 0; q < 16; ++q) xs[(lane & 15) * NIN + (pr ? 16 : 0) + q] = __float2bfloat16_rn(feat[q]);
+            __syncwarp();
+            Fwd f;
+            mlp_forward_tile(global_view(a.mlp), xs, f); // 12 KB of weights, L1-resident
+            if ((lane & 3) == 0) {
+                prob[lane >> 2] = sigmoidf_(f.logit_g);
+                prob[(lane >> 2) + 8] = sigmoidf_(f.logit_g8);
+            }
+            __syncwarp();
+            bool tr = false;
+            int n_tr = 0, n_mis = 0, n_fb = 0;
+            if (!pr && ev) {
+                const bool plain = plain_troubled(su, a.ind_S0, a.ind_kappa);
+                const float pm = prob[lane];
+                const bool fb = fabsf(pm - a.ind_thr) < a.ind_band, net = pm > a.ind_thr;
+                tr = fb ? plain : net;
+                n_tr = tr;
+                n_mis = net != plain;
+                n_fb = fb;
+                a.flags[(i0 + exl) + nx * (j0 + eyt)] = tr ? 1 : 0;
+            }
+            const size_t ebase = (size_t)(i0 + 16 * h) + (size_t)nx * (j0 + eyt);
+            warp_filter_elements<Real>(__ballot_sync(0xffffffffu, tr), ebase, a.out, a.ul, plane, a.V, a.iV,
+                                       a.ind_lam);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                n_tr += __shfl_xor_sync(0xffffffffu, n_tr, off);
+                n_mis += __shfl_xor_sync(0xffffffffu, n_mis, off);
+                n_fb += __shfl_xor_sync(0xffffffffu, n_fb, off);
+            }
+            if (lane == 0) {
+                if (n_tr) atomicAdd(&a.stats[0], n_tr);
+                if (n_mis) atomicAdd(&a.stats[1], n_mis);
+                if (n_fb) atomicAdd(&a.stats[2], n_fb);
+            }
+        }
+    }
 #undef SU
 #undef SG
 #undef STR
@@ -466,7 +549,7 @@ E2DArgs<Real, NP> make_e2d_args(frgpu_problem *p, const void *in, const void *di
     return a;
 }
 
-template <class Real, int NP, int FLUX, int MODE, int STAGE>
+template <class Real, int NP, int FLUX, int MODE, int STAGE, bool FUSE = false>
 int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     using T = Tile<Real, NP>;
     using S = Smem<Real, NP, T::TX, T::TY, Stash<MODE, STAGE>::n>;
@@ -489,8 +572,26 @@ int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     }
     a.ops = make_ops<Real, NP>(p->sp);
     a.status = p->d_status;
+    a.mlp = frmlp::MLPDev{nullptr, nullptr, nullptr, nullptr};
+    a.V = a.iV = nullptr;
+    a.flags = a.stats = nullptr;
+    if (FUSE) {
+        const fr_mlp_ptrs m = fr_mlp_device(p->mlp);
+        a.mlp = frmlp::MLPDev{m.P, (const __nv_bfloat16 *)m.W1, (const __nv_bfloat16 *)m.W2,
+                              (const __nv_bfloat16 *)m.W2T};
+        fr_iv1_from_tensor(p->sp, &a.iv1.m[0][0]);
+        a.ind_thr = p->mlp_thr;
+        a.ind_band = p->mlp_band;
+        a.ind_S0 = (float)p->S0;
+        a.ind_kappa = (float)p->kappa;
+        a.ind_lam = p->lam;
+        a.V = (const Real *)p->d_V;
+        a.iV = (const Real *)p->d_iV;
+        a.flags = p->d_flags;
+        a.stats = p->d_count;
+    }
     static_assert(S::bytes <= 227 * 1024, "shared memory per CTA exceeds 227 KB");
-    auto kern = k_euler2d<Real, NP, FLUX, MODE, STAGE>;
+    auto kern = k_euler2d<Real, NP, FLUX, MODE, STAGE, FUSE>;
     // the dynamic shared-memory opt-in is set once per instantiation (and on
     // every prepare pass, which precedes each graph capture)
     static bool attr_set = false;
@@ -499,6 +600,7 @@ int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
         attr_set = true;
     }
     if (p->prepare_only) return FRGPU_OK;
+    if (FUSE) FR_CUDA(cudaMemsetAsync(p->d_count, 0, sizeof(int) * 4, p->stream));
     dim3 grid((a.nx + T::TX - 1) / T::TX, (a.ny + T::TY - 1) / T::TY);
     kern<<<grid, T::TX * NP * T::TY, S::bytes, p->stream>>>(a);
     FR_CUDA(cudaGetLastError());
@@ -512,6 +614,11 @@ int dispatch_stage(frgpu_problem *p, int stage, const void *in, const void *din,
 #define FR_ST(S)                                                                                                   \
     return flux == FLUX_HLL ? launch_t<Real, NP, FLUX_HLL, MODE, S>(p, in, din, out)                               \
                             : launch_t<Real, NP, FLUX_LF, MODE, S>(p, in, din, out)
+    if constexpr (std::is_same<Real, float>::value && NP == 4 && MODE == MODE_FP32K) {
+        if (stage == 3 && fr_fused_indicator(p))
+            return flux == FLUX_HLL ? launch_t<Real, NP, FLUX_HLL, MODE, 3, true>(p, in, din, out)
+                                    : launch_t<Real, NP, FLUX_LF, MODE, 3, true>(p, in, din, out);
+    }
     switch (stage) {
     case 0: FR_ST(0);
     case 1: FR_ST(1);

@@ -49,6 +49,7 @@ struct frgpu_problem {
     const frgpu_mlp *mlp = nullptr; // learned indicator (borrowed)
     float mlp_thr = 0.5f, mlp_band = 0.0f;
     int bgk_tensor = 1;             // FP32 BGK transport on the tensor cores
+    int fuse_indicator = 1;         // FP32K 2D: learned indicator inside stage 3
     float *d_bgk_prim = nullptr;    // FP32 BGK: (rho, U, lambda) per (element, point), from the moments
     uint32_t *d_bgk_frag = nullptr; // FP32 BGK: TF32 A fragments of the transport operator (both signs, split)
     // captured step graph
@@ -119,4 +120,9 @@ struct fr_mlp_ptrs {
     const void *W1, *W2, *W2T;
 };
 fr_mlp_ptrs fr_mlp_device(const frgpu_mlp *m);
+// 1D factor iV1[i][k] (row-major 4 x 4, float) of a deg-3 2D space's tensor inverse Vandermonde matrix
+void fr_iv1_from_tensor(const frgpu_space &s, float *iv1);
+// Does stage 3 of this problem run the learned indicator itself (FP32K 2D Euler,
+// deg 3, learned indicator bound and selected, fusion not switched off)?
+bool fr_fused_indicator(const frgpu_problem *p);
 int fr_launch_mlp_indicator(frgpu_problem *p, double lam, double S0, double kappa);

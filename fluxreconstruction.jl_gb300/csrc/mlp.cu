@@ -243,10 +243,10 @@ __global__ void k_mlp_adam(float *__restrict__ P, float *__restrict__ m, float *
     const float p = P[q] - lr * (mq * c1) / (sqrtf(vq * c2) + eps);
     P[q] = p;
     const __nv_bfloat16 pb = __float2bfloat16_rn(p);
-    if (q < OFF_B1) W1[q - OFF_W1] = pb;
+    if (q < OFF_B1) W1[frag_w1((q - OFF_W1) / NIN, (q - OFF_W1) % NIN)] = pb;
     else if (q >= OFF_W2 && q < OFF_B2) {
         const int r = q - OFF_W2, o = r / NH, i = r % NH;
-        W2[r] = pb;
+        W2[frag_w2(o, i)] = pb;
         W2T[i * NH + o] = pb;
     }
 }
@@ -255,20 +255,15 @@ __global__ void k_mlp_refresh(const float *__restrict__ P, __nv_bfloat16 *W1, __
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= NPARAM) return;
     const __nv_bfloat16 pb = __float2bfloat16_rn(P[q]);
-    if (q < OFF_B1) W1[q - OFF_W1] = pb;
+    if (q < OFF_B1) W1[frag_w1((q - OFF_W1) / NIN, (q - OFF_W1) % NIN)] = pb;
     else if (q >= OFF_W2 && q < OFF_B2) {
         const int r = q - OFF_W2, o = r / NH, i = r % NH;
-        W2[r] = pb;
+        W2[frag_w2(o, i)] = pb;
         W2T[i * NH + o] = pb;
     }
 }
 
 // ---------------------------------------------------------------- features + indicator
-// 1D inverse Vandermonde matrix of deg 3 (iV1[i][k]); the tensor inverse of
-// FRPSpace2D (src/struct.jl:196-205) factors as iV[(i,j)][(k,l)] = iV1[i][k] iV1[j][l].
-struct IV1 {
-    float m[4][4];
-};
 
 // Modal energies of density and pressure of 16 elements per warp (np = 4).
 // Lane L and L + 16 share element e = base + (L & 15): each loads the four
@@ -295,51 +290,6 @@ __device__ __forceinline__ void load_raw(const Real *__restrict__ u, size_t ne, 
     }
 }
 
-__device__ __forceinline__ void features_from_raw(const float (&w)[8][4], bool valid, bool pressure, const IV1 &iv,
-                                                  float gm1, float (&feat)[16], float &su) {
-    float v[16];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const float w0 = w[k][0], w1 = w[k][1], w2 = w[k][2], w3 = w[k][3];
-        const float ri = __fdividef(1.0f, w0);
-        const float pk = gm1 * (w3 - 0.5f * (w1 * (w1 * ri) + w2 * (w2 * ri)));
-        const float recv = __shfl_xor_sync(0xffffffffu, pressure ? w0 : pk, 16);
-        v[k] = pressure ? recv : w0;     // density (lower) / pressure (upper) at point k
-        v[8 + k] = pressure ? pk : recv; // ... at point 8 + k
-    }
-    // modal coefficients by sum factorisation: t[i][l] = sum_k iV1[i][k] v[k + 4 l],
-    // u_hat[4 i + j] = sum_l iV1[j][l] t[i][l]
-    float t[4][4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int l = 0; l < 4; ++l) {
-            float s = iv.m[i][0] * v[4 * l];
-#pragma unroll
-            for (int k = 1; k < 4; ++k) s = fmaf(iv.m[i][k], v[k + 4 * l], s);
-            t[i][l] = s;
-        }
-    float tot = 0.f;
-    float en[16];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            float s = iv.m[j][0] * t[i][0];
-#pragma unroll
-            for (int l = 1; l < 4; ++l) s = fmaf(iv.m[j][l], t[i][l], s);
-            en[4 * i + j] = s * s;
-            tot += s * s;
-        }
-    su = en[15] / tot;
-    const float itot = 1.0f / tot;
-#pragma unroll
-    for (int a = 0; a < 16; ++a) {
-        float x = __log2f(en[a] * itot + 1e-16f) * 0.30102999566398120f; // log10 through the hardware log2
-        x = fminf(fmaxf(x, -16.f), 0.f);
-        feat[a] = valid ? x * 0.125f + 1.0f : 0.f;
-    }
-}
 
 template <class Real>
 __device__ __forceinline__ void element_features(const Real *__restrict__ u, size_t ne, size_t e, bool valid,
@@ -367,17 +317,6 @@ __global__ void __launch_bounds__(128) k_features(const Real *__restrict__ u, si
     for (int a = 0; a < 16; ++a) feat[e * NIN + (pr ? 16 : 0) + a] = f[a];
 }
 
-__device__ __forceinline__ bool plain_troubled(float su, float S0, float kappa) {
-    const float Se = log10f(su);
-    float sigma;
-    if (Se < S0 - kappa)
-        sigma = 1.f;
-    else if (S0 - kappa <= Se && Se < S0 + kappa)
-        sigma = 0.5f * (1.f - sinf(1.5707963267948966f * (Se - S0) / kappa));
-    else
-        sigma = 0.f;
-    return sigma < 0.99f;
-}
 
 // Learned indicator + :l2 modal filter on a 2D Euler state (np = 4).  Per
 // element: features -> MLP -> probability.  Where the probability is within
@@ -441,31 +380,8 @@ __global__ void __launch_bounds__(32 * WARPS, 4) k_mlp_indicator(MLPDev w, Real 
             n_trouble += bad;
             flags[e] = bad ? 1 : 0;
         }
-        // :l2 modal filter of the troubled elements, one element at a time by
-        // the whole warp: lane = 16 (variable pair) + mode a.  Every output is
-        // the same ascending FMA chain as the plain filter kernel's.
-        unsigned todo = __ballot_sync(0xffffffffu, bad);
-        const int a = lane & 15, half = lane & 16;
-        const Real den = Real(1) + mul_rn(Real(lam), Real((double)((a + 1) * (a + 1) * a * a)));
-        while (todo) {
-            const int src = __ffs(todo) - 1;
-            todo &= todo - 1;
-            const size_t et = tile * 16 + src;
-            for (int mp = 0; mp < 4; mp += 2) {
-                const int m = mp + (half >> 4);
-                Real *um = u + ne * 16 * (size_t)m;
-                const Real xa = um[et + ne * a];
-                Real s = iV[a] * __shfl_sync(0xffffffffu, xa, half);
-#pragma unroll
-                for (int b = 1; b < 16; ++b) s = frk::fmaR<Real>(iV[a + 16 * b], __shfl_sync(0xffffffffu, xa, half + b), s);
-                const Real ha = s / den;
-                Real r = V[a] * __shfl_sync(0xffffffffu, ha, half);
-#pragma unroll
-                for (int b = 1; b < 16; ++b) r = frk::fmaR<Real>(V[a + 16 * b], __shfl_sync(0xffffffffu, ha, half + b), r);
-                um[et + ne * a] = r;
-                if (lo) lo[et + ne * (a + 16 * (size_t)m)] = Real(0);
-            }
-        }
+        // :l2 modal filter of the troubled elements
+        warp_filter_elements<Real>(__ballot_sync(0xffffffffu, bad), tile * 16, u, lo, ne, V, iV, lam);
         __syncwarp();
     }
     // warp-reduce the statistics, one atomic per warp
@@ -706,13 +622,22 @@ fr_mlp_ptrs fr_mlp_device(const frgpu_mlp *m) { return fr_mlp_ptrs{m->P, m->W1, 
 
 // The 1D factor of the space's tensor inverse Vandermonde matrix:
 // iV[(i,0),(k,0)] = iV1[i][k] iV1[0][0], and iV1[0][0] = w_0 / sqrt(2) > 0.
-static IV1 iv1_from_tensor(const frgpu_problem *p) {
-    const double *iV = p->sp.iV.data();
+void fr_iv1_from_tensor(const frgpu_space &s, float *iv1) {
+    const double *iV = s.iV.data();
     const double c = std::sqrt(iV[0]);
-    IV1 r;
     for (int i = 0; i < 4; ++i)
-        for (int k = 0; k < 4; ++k) r.m[i][k] = (float)(iV[4 * i + 16 * k] / c);
+        for (int k = 0; k < 4; ++k) iv1[4 * i + k] = (float)(iV[4 * i + 16 * k] / c);
+}
+
+static IV1 iv1_from_tensor(const frgpu_problem *p) {
+    IV1 r;
+    fr_iv1_from_tensor(p->sp, &r.m[0][0]);
     return r;
+}
+
+bool fr_fused_indicator(const frgpu_problem *p) {
+    return p->fuse_indicator && p->indicator == FRGPU_IND_MLP && p->mlp && p->d.equation == FRGPU_EULER2D &&
+           p->d.precision == FRGPU_FP32K && p->sp.np == 4 && p->d_V && p->d_iV;
 }
 
 int fr_launch_features(frgpu_problem *p, float *d_feat) {

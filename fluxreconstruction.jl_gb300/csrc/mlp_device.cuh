@@ -9,6 +9,8 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 
+#include "fr_common.cuh"
+
 namespace frmlp {
 
 constexpr int NIN = 32, NH = 64;
@@ -19,10 +21,22 @@ constexpr int GWARPS = 2; // warps per CTA of the gradient kernel (static shared
 
 struct MLPDev {
     const float *P;             // FP32 parameters
-    const __nv_bfloat16 *W1;    // [64][32]
-    const __nv_bfloat16 *W2;    // [64][64]  row = output unit
-    const __nv_bfloat16 *W2T;   // [64][64]  row = input unit
+    const __nv_bfloat16 *W1;    // W1 [64][32] in fragment order (frag_w1)
+    const __nv_bfloat16 *W2;    // W2 [64][64] in fragment order (frag_w2)
+    const __nv_bfloat16 *W2T;   // [64][64]  row = input unit (backward pass)
 };
+
+// Fragment order of the BF16 weight copies: the m16n8k16 B fragments that lane
+// (g = lane / 4, t = lane % 4) needs for output tile j (units 8j..8j+7) are
+// contiguous, so one 128-bit load fetches two k-steps: word kk * 2 + h holds
+// W[8j + g][16 kk + 8 h + 2 t], W[8j + g][16 kk + 8 h + 2 t + 1].
+// Position of W1[o][i] (i < 32: 4 words per lane) and W2[o][i] (i < 64: 8 words).
+__host__ __device__ __forceinline__ int frag_pos(int o, int i, int words) {
+    const int j = o >> 3, g = o & 7, kk = i >> 4, r = i & 15, h = r >> 3, t = (r & 7) >> 1, e = r & 1;
+    return ((j * 32 + 4 * g + t) * words + kk * 2 + h) * 2 + e;
+}
+__host__ __device__ __forceinline__ int frag_w1(int o, int i) { return frag_pos(o, i, 4); }
+__host__ __device__ __forceinline__ int frag_w2(int o, int i) { return frag_pos(o, i, 8); }
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
@@ -105,9 +119,9 @@ __device__ __forceinline__ void mlp_forward_tile(const MLPView &w, const __nv_bf
         f.a1[j][1] = c1;
         f.a1[j][2] = c0;
         f.a1[j][3] = c1;
-        const __nv_bfloat16 *row = w.W1 + (8 * j + g) * NIN;
-#pragma unroll
-        for (int kk = 0; kk < 2; ++kk) mma16816(f.a1[j], ax[kk], ld_pair(row + 16 * kk + 2 * t), ld_pair(row + 16 * kk + 8 + 2 * t));
+        const uint4 b = reinterpret_cast<const uint4 *>(w.W1)[j * 32 + lane];
+        mma16816(f.a1[j], ax[0], b.x, b.y);
+        mma16816(f.a1[j], ax[1], b.z, b.w);
     }
 #pragma unroll
     for (int kk = 0; kk < 4; ++kk) {
@@ -124,10 +138,12 @@ __device__ __forceinline__ void mlp_forward_tile(const MLPView &w, const __nv_bf
         f.a2[j][1] = c1;
         f.a2[j][2] = c0;
         f.a2[j][3] = c1;
-        const __nv_bfloat16 *row = w.W2 + (8 * j + g) * NH;
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk)
-            mma16816(f.a2[j], f.ah1[kk], ld_pair(row + 16 * kk + 2 * t), ld_pair(row + 16 * kk + 8 + 2 * t));
+        const uint4 *bp = reinterpret_cast<const uint4 *>(w.W2) + (j * 32 + lane) * 2;
+        const uint4 b01 = bp[0], b23 = bp[1];
+        mma16816(f.a2[j], f.ah1[0], b01.x, b01.y);
+        mma16816(f.a2[j], f.ah1[1], b01.z, b01.w);
+        mma16816(f.a2[j], f.ah1[2], b23.x, b23.y);
+        mma16816(f.a2[j], f.ah1[3], b23.z, b23.w);
         const float w0 = w3[8 * j + 2 * t], w1 = w3[8 * j + 2 * t + 1];
         sg = fmaf(gelu(f.a2[j][0]), w0, fmaf(gelu(f.a2[j][1]), w1, sg));
         sg8 = fmaf(gelu(f.a2[j][2]), w0, fmaf(gelu(f.a2[j][3]), w1, sg8));
@@ -160,6 +176,123 @@ __device__ __forceinline__ void stage_weights(const MLPDev &w, __nv_bfloat16 *sW
 }
 __device__ __forceinline__ MLPView smem_view(const __nv_bfloat16 *sW1, const __nv_bfloat16 *sW2, const float *sb) {
     return MLPView{sb, sb + NH, sb + 2 * NH, sb + 3 * NH, sW1, sW2};
+}
+
+// ---- features and decisions of the 2D indicator (np = 4) ------------------
+// 1D inverse Vandermonde matrix of deg 3 (iV1[i][k]); the tensor inverse of
+// FRPSpace2D (src/struct.jl:196-205) factors as iV[(i,j)][(k,l)] = iV1[i][k] iV1[j][l].
+struct IV1 {
+    float m[4][4];
+};
+
+// Normalised modal energies of one field from its 16 point values v[k + 4 l]:
+// feat[a] = clamp(log10(u_hat_a^2 / sum u_hat^2 + 1e-16), -16, 0) / 8 + 1 (0 when
+// !valid), and su = u_hat_15^2 / sum u_hat^2 (the plain test's ratio).
+__device__ __forceinline__ void modal_features16(const float (&v)[16], bool valid, const IV1 &iv, float (&feat)[16],
+                                                 float &su) {
+    // modal coefficients by sum factorisation: t[i][l] = sum_k iV1[i][k] v[k + 4 l],
+    // u_hat[4 i + j] = sum_l iV1[j][l] t[i][l]
+    float t[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            float s = iv.m[i][0] * v[4 * l];
+#pragma unroll
+            for (int k = 1; k < 4; ++k) s = fmaf(iv.m[i][k], v[k + 4 * l], s);
+            t[i][l] = s;
+        }
+    float tot = 0.f;
+    float en[16];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float s = iv.m[j][0] * t[i][0];
+#pragma unroll
+            for (int l = 1; l < 4; ++l) s = fmaf(iv.m[j][l], t[i][l], s);
+            en[4 * i + j] = s * s;
+            tot += s * s;
+        }
+    su = en[15] / tot;
+    const float itot = 1.0f / tot;
+#pragma unroll
+    for (int a = 0; a < 16; ++a) {
+        float x = __log2f(en[a] * itot + 1e-16f) * 0.30102999566398120f; // log10 through the hardware log2
+        x = fminf(fmaxf(x, -16.f), 0.f);
+        feat[a] = valid ? x * 0.125f + 1.0f : 0.f;
+    }
+}
+
+// Pressure of a conserved 2D Euler state, as the indicator's features see it.
+__device__ __forceinline__ float feature_pressure(float w0, float w1, float w2, float w3, float gm1) {
+    const float ri = __fdividef(1.0f, w0);
+    return gm1 * (w3 - 0.5f * (w1 * (w1 * ri) + w2 * (w2 * ri)));
+}
+
+// Features of the element shared by lanes L and L + 16 of a warp: each holds the
+// four variables w[k][m] at 8 of its 16 points (the lower lane points 0-7, the
+// upper 8-15, in the order q = k + 4 l); they swap halves so that the lower lane
+// gets the density features, the upper lane the pressure features.  Lanes of
+// elements past the end (valid false) take part in the exchange.
+__device__ __forceinline__ void features_from_raw(const float (&w)[8][4], bool valid, bool pressure, const IV1 &iv,
+                                                  float gm1, float (&feat)[16], float &su) {
+    float v[16];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const float w0 = w[k][0], w1 = w[k][1], w2 = w[k][2], w3 = w[k][3];
+        const float pk = feature_pressure(w0, w1, w2, w3, gm1);
+        const float recv = __shfl_xor_sync(0xffffffffu, pressure ? w0 : pk, 16);
+        v[k] = pressure ? recv : w0;     // density (lower) / pressure (upper) at point k
+        v[8 + k] = pressure ? pk : recv; // ... at point 8 + k
+    }
+    modal_features16(v, valid, iv, feat, su);
+}
+
+// The plain modal-decay test (shock_detector, src/dissipation.jl:13-23) in FP32.
+__device__ __forceinline__ bool plain_troubled(float su, float S0, float kappa) {
+    const float Se = log10f(su);
+    float sigma;
+    if (Se < S0 - kappa)
+        sigma = 1.f;
+    else if (S0 - kappa <= Se && Se < S0 + kappa)
+        sigma = 0.5f * (1.f - sinf(1.5707963267948966f * (Se - S0) / kappa));
+    else
+        sigma = 0.f;
+    return sigma < 0.99f;
+}
+
+// :l2 modal filter of the elements ebase + b for the bits b set in todo (b < 16;
+// the same mask on every lane), one element at a time by the whole warp: lane =
+// 16 (variable pair) + mode a.  State u[e + ne q + 16 ne m] (np = 4, 4
+// variables); lo (FP32K low part, may be null) is cleared where u is filtered.
+// Every output is the same ascending FMA chain as the plain filter kernel's.
+template <class Real>
+__device__ __forceinline__ void warp_filter_elements(unsigned todo, size_t ebase, Real *u, Real *lo, size_t ne,
+                                                     const Real *V, const Real *iV, double lam) {
+    const int lane = threadIdx.x & 31, a = lane & 15, half = lane & 16;
+    const Real den = Real(1) + mul_rn(Real(lam), Real((double)((a + 1) * (a + 1) * a * a)));
+    while (todo) {
+        const int src = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const size_t et = ebase + src;
+        for (int mp = 0; mp < 4; mp += 2) {
+            const int m = mp + (half >> 4);
+            Real *um = u + ne * 16 * (size_t)m;
+            const Real xa = um[et + ne * a];
+            Real s = iV[a] * __shfl_sync(0xffffffffu, xa, half);
+#pragma unroll
+            for (int b = 1; b < 16; ++b)
+                s = frk::fmaR<Real>(iV[a + 16 * b], __shfl_sync(0xffffffffu, xa, half + b), s);
+            const Real ha = s / den;
+            Real r = V[a] * __shfl_sync(0xffffffffu, ha, half);
+#pragma unroll
+            for (int b = 1; b < 16; ++b)
+                r = frk::fmaR<Real>(V[a + 16 * b], __shfl_sync(0xffffffffu, ha, half + b), r);
+            um[et + ne * a] = r;
+            if (lo) lo[et + ne * (a + 16 * (size_t)m)] = Real(0);
+        }
+    }
 }
 
 } // namespace frmlp

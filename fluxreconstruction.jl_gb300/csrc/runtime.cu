@@ -354,7 +354,7 @@ static int enqueue_step(frgpu_problem *p) {
         if ((rc = launch_stage(p, 2, hi, tmp, p->s2))) return rc;
         if ((rc = launch_stage(p, 3, hi, p->s2, tmp))) return rc;
     }
-    if (p->indicator != FRGPU_IND_NONE) {
+    if (p->indicator != FRGPU_IND_NONE && !fr_fused_indicator(p)) {
         // the filter runs on the new state: for FP32K that is the buffer the
         // high part moves to, so evaluate with the parity flipped
         if (p->d.precision == FRGPU_FP32K) p->parity ^= 1;
@@ -712,8 +712,9 @@ FRGPU_API int frgpu_set_filter(frgpu_problem *p, int indicator, double lam, doub
 
 FRGPU_API int frgpu_problem_set_option(frgpu_problem *p, int option, int value) {
     FR_REQ(p, "set_option: null problem");
-    FR_REQ(option == FRGPU_OPT_BGK_TENSOR, "set_option: unknown option");
-    p->bgk_tensor = value != 0;
+    FR_REQ(option == FRGPU_OPT_BGK_TENSOR || option == FRGPU_OPT_FUSED_INDICATOR, "set_option: unknown option");
+    if (option == FRGPU_OPT_BGK_TENSOR) p->bgk_tensor = value != 0;
+    if (option == FRGPU_OPT_FUSED_INDICATOR) p->fuse_indicator = value != 0;
     p->graph_ind = -2; // force a re-capture
     return FRGPU_OK;
 }

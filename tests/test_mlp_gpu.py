@@ -149,3 +149,33 @@ def test_learned_indicator_trains_and_judges_misfires(frgpu):
     ne = 100 * 50
     assert stats[1] <= 0.05 * ne, stats
     assert np.all(np.isfinite(itg.u))
+
+
+def test_fused_indicator_equals_separate_kernel(frgpu):
+    """The learned indicator inside the third SSPRK3 stage (FP32K, deg 3) and the
+    stand-alone indicator kernel after the step give the same state, flags and
+    counts, bit for bit: same features, same network arithmetic, same filter."""
+    from frgpu import _lib as L
+    from frgpu import learned
+
+    ps = frgpu.FRPSpace2D(0, 2, 100, 0, 1, 50, 3)
+    net = learned.load_trained()
+    out = []
+    for fuse in (1, 0):
+        prob = learned.shock_vortex_problem(ps, 0.3)
+        prob.set_option(L.OPT_FUSED_INDICATOR, fuse)
+        itg = frgpu.init(prob, dt=1.0)
+        itg.dt = itg.cfl_dt(0.1)
+        L.check(frgpu.lib().frgpu_problem_set_mlp(prob._h, net._h, 0.5, 0.02))
+        itg.set_filter("mlp", learned.FILTER_LAMBDA, learned.filter_S0(3), learned.FILTER_KAPPA)
+        l0 = itg.launches()
+        itg.step(400)
+        launches = itg.launches() - l0
+        st = np.zeros(3, dtype=np.int32)
+        L.check(frgpu.lib().frgpu_indicator_stats(prob._h, st.ctypes.data_as(L._I)))
+        out.append((itg.u, itg.troubled(), st, launches))
+    (u1, f1, s1, n1), (u0, f0, s0, n0) = out
+    assert np.array_equal(u1, u0)
+    assert np.array_equal(f1, f0) and np.array_equal(s1, s0)
+    assert f1.sum() > 0  # the vortex has met the shock: something was filtered
+    assert n1 < n0       # one launch fewer per step
