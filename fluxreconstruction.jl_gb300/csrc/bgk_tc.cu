@@ -80,6 +80,7 @@ __global__ void __launch_bounds__(32 * MW) k_bgk_moments(const float *__restrict
     if (row >= ne * NP) return; // whole warp
     const size_t base = (size_t)row * nv;
     float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f, s2 = 0.f, e2 = 0.f;
+#pragma unroll 4
     for (int v = lane; v < nv; v += 32) {
         const float x = ld_state(uin, din, base + v);
         const float vel = __ldg(velo + v), wx = __ldg(w + v) * x;

@@ -94,13 +94,26 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce2d_partial(const Real *__
     }
 }
 
-__global__ void k_reduce_final(const double *__restrict__ part, int nblocks, double *__restrict__ out) {
-    if (threadIdx.x < 6) {
-        const int v = threadIdx.x;
-        double x = part[v];
-        for (int b = 1; b < nblocks; ++b) x = v < 4 ? x + part[b * 6 + v] : fmax(x, part[b * 6 + v]);
-        out[v] = x;
+// Final pass over the per-block partials: warp v (of 6) combines value v, each
+// lane over a fixed strided subset of the blocks, then a fixed butterfly: the
+// same order every call, so the result is deterministic.
+__device__ __forceinline__ double final_value(const double *__restrict__ part, int nblocks, int v) {
+    const int lane = threadIdx.x & 31;
+    double x = 0.0; // sums start at 0; the maxima are of non-negative speeds
+    for (int b = lane; b < nblocks; b += 32) x = v < 4 ? x + part[b * 6 + v] : fmax(x, part[b * 6 + v]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const double y = __shfl_xor_sync(0xffffffffu, x, off);
+        x = v < 4 ? x + y : fmax(x, y);
     }
+    return x;
+}
+
+__global__ void __launch_bounds__(192) k_reduce_final(const double *__restrict__ part, int nblocks,
+                                                      double *__restrict__ out) {
+    const int v = threadIdx.x >> 5;
+    const double x = final_value(part, nblocks, v);
+    if ((threadIdx.x & 31) == 0) out[v] = x;
 }
 
 } // namespace
@@ -127,7 +140,7 @@ int fr_launch_euler2d_reduce(frgpu_problem *p, const void *state, const void *lo
         k_reduce2d_partial<float><<<grid, RED_THREADS, 0, p->stream>>>((const float *)state, (const float *)lo,
                                                                     plane, nq, wp, p->d.gamma, cfl_dx, cfl_dy, part);
     FR_CUDA(cudaGetLastError());
-    k_reduce_final<<<1, 32, 0, p->stream>>>(part, (int)(grid.x * grid.y), fin);
+    k_reduce_final<<<1, 192, 0, p->stream>>>(part, (int)(grid.x * grid.y), fin);
     FR_CUDA(cudaGetLastError());
     p->launches += 2;
     double h[6];
@@ -186,14 +199,11 @@ int noalloc_scratch(double **out) {
 }
 
 // final pass of the allocation-free reduction: sums scaled by the element area
-__global__ void k_reduce_final_scaled(const double *__restrict__ part, int nblocks, double scale,
-                                      double *__restrict__ out) {
-    if (threadIdx.x < 6) {
-        const int v = threadIdx.x;
-        double x = part[v];
-        for (int b = 1; b < nblocks; ++b) x = v < 4 ? x + part[b * 6 + v] : fmax(x, part[b * 6 + v]);
-        out[v] = v < 4 ? x * scale : x;
-    }
+__global__ void __launch_bounds__(192) k_reduce_final_scaled(const double *__restrict__ part, int nblocks,
+                                                             double scale, double *__restrict__ out) {
+    const int v = threadIdx.x >> 5;
+    const double x = final_value(part, nblocks, v);
+    if ((threadIdx.x & 31) == 0) out[v] = v < 4 ? x * scale : x;
 }
 } // namespace
 
@@ -237,7 +247,7 @@ extern "C" FRGPU_API int frgpu_reduce2d_noalloc(const void *d_state, const void 
         k_reduce2d_partial<float><<<grid, RED_THREADS, 0, st>>>(
             (const float *)d_state, (const float *)d_lo, plane, np * np, d_wp, gamma, 1.0 / dx, 1.0 / dy, part);
     FR_CUDA(cudaGetLastError());
-    k_reduce_final_scaled<<<1, 32, 0, st>>>(part, (int)nblocks, dx * dy * 0.25, d_out);
+    k_reduce_final_scaled<<<1, 192, 0, st>>>(part, (int)nblocks, dx * dy * 0.25, d_out);
     FR_CUDA(cudaGetLastError());
     return FRGPU_OK;
 }
