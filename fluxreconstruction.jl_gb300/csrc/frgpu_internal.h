@@ -41,6 +41,7 @@ struct frgpu_problem {
     void *d_J = nullptr;                    // 1D per-element Jacobian (state precision)
     void *d_V = nullptr, *d_iV = nullptr;   // Vandermonde matrix / inverse (state precision)
     void *rhs_in = nullptr, *rhs_out = nullptr; // scratch of frgpu_rhs
+    void *d_stage = nullptr;                // FP64 staging of state uploads / downloads (+ 8 bytes)
     int parity = 0;                         // FP32K: which buffer holds u^n (0: s0, 1: s1)
     bool prepare_only = false;              // launchers only set kernel attributes
     // post-step filter
@@ -105,6 +106,9 @@ int fr_launch_euler1d(frgpu_problem *p, int stage, const void *in, const void *d
 int fr_launch_bgk1d(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
 int fr_launch_bgk1d_tc(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
 int fr_bgk_tc_setup(frgpu_problem *p); // device buffers of the tensor-core BGK path
+// Host FP64 state (reference layout) <-> device state (transfer.cu)
+int fr_put_state(frgpu_problem *p, const double *u, void *hi, void *lo);
+int fr_get_state(frgpu_problem *p, const void *hi, const void *lo, double *u);
 int fr_launch_interp_face(const double *d_f, long n, int np, const double *ll, const double *lr, double *d_out,
                           cudaStream_t st);
 int fr_launch_poly_derivative(const double *d_f, long n, int np, const double *pdm, double *d_out,

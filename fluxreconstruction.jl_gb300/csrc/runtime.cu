@@ -292,7 +292,7 @@ static void free_problem(frgpu_problem *p) {
         if (g) cudaGraphExecDestroy(g);
     void *bufs[] = {p->s0, p->s1, p->s2, p->s3, p->d_dt, p->d_status, p->d_red, p->d_flags, p->d_count,
                     p->d_velo, p->d_w, p->d_J, p->d_V, p->d_iV, p->rhs_in, p->rhs_out, p->d_bgk_prim,
-                    p->d_bgk_frag};
+                    p->d_bgk_frag, p->d_stage};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -527,64 +527,17 @@ FRGPU_API void frgpu_problem_destroy(frgpu_problem *p) { free_problem(p); }
 FRGPU_API long frgpu_problem_ndof(const frgpu_problem *p) { return p ? p->ndof : -1; }
 
 // Host (Julia layout, FP64) <-> device layout/precision.
-static void to_device_order(const frgpu_problem *p, const double *u, std::vector<double> &dst) {
-    dst.resize(p->ndof);
-    if (p->d.equation != FRGPU_BGK1D) {
-        std::memcpy(dst.data(), u, sizeof(double) * p->ndof);
-        return;
-    }
-    const long ne = p->sp.nx, nv = p->d.nvel, np = p->sp.np;
-    for (long k = 0; k < np; ++k)
-        for (long v = 0; v < nv; ++v)
-            for (long i = 0; i < ne; ++i) dst[(i * np + k) * nv + v] = u[i + ne * (v + nv * k)];
-}
-
-static void to_host_order(const frgpu_problem *p, const std::vector<double> &src, double *u) {
-    if (p->d.equation != FRGPU_BGK1D) {
-        std::memcpy(u, src.data(), sizeof(double) * p->ndof);
-        return;
-    }
-    const long ne = p->sp.nx, nv = p->d.nvel, np = p->sp.np;
-    for (long k = 0; k < np; ++k)
-        for (long v = 0; v < nv; ++v)
-            for (long i = 0; i < ne; ++i) u[i + ne * (v + nv * k)] = src[(i * np + k) * nv + v];
-}
-
+// Host <-> device state conversions run on the GPU (transfer.cu).
 static int put_state(frgpu_problem *p, const double *u, void *hi, void *lo) {
-    std::vector<double> tmp;
-    to_device_order(p, u, tmp);
-    for (long q = 0; q < p->ndof; ++q)
-        if (!std::isfinite(tmp[q])) {
-            fr_set_error("state upload: non-finite value at index " + std::to_string(q));
-            return FRGPU_ERR_NONFINITE;
-        }
-    if (p->esize == 8) {
-        FR_CUDA(cudaMemcpy(hi, tmp.data(), sizeof(double) * p->ndof, cudaMemcpyHostToDevice));
-    } else {
-        std::vector<float> h(p->ndof), l(p->ndof);
-        for (long q = 0; q < p->ndof; ++q) {
-            h[q] = (float)tmp[q];
-            l[q] = (float)(tmp[q] - (double)h[q]);
-        }
-        FR_CUDA(cudaMemcpy(hi, h.data(), sizeof(float) * p->ndof, cudaMemcpyHostToDevice));
-        if (lo) FR_CUDA(cudaMemcpy(lo, l.data(), sizeof(float) * p->ndof, cudaMemcpyHostToDevice));
-    }
-    return FRGPU_OK;
+    const int rc = fr_put_state(p, u, hi, lo);
+    p->launches += 1;
+    return rc;
 }
 
 static int get_state(frgpu_problem *p, const void *hi, const void *lo, double *u) {
-    std::vector<double> tmp(p->ndof);
-    FR_CUDA(cudaStreamSynchronize(p->stream));
-    if (p->esize == 8) {
-        FR_CUDA(cudaMemcpy(tmp.data(), hi, sizeof(double) * p->ndof, cudaMemcpyDeviceToHost));
-    } else {
-        std::vector<float> h(p->ndof), l(p->ndof, 0.0f);
-        FR_CUDA(cudaMemcpy(h.data(), hi, sizeof(float) * p->ndof, cudaMemcpyDeviceToHost));
-        if (lo) FR_CUDA(cudaMemcpy(l.data(), lo, sizeof(float) * p->ndof, cudaMemcpyDeviceToHost));
-        for (long q = 0; q < p->ndof; ++q) tmp[q] = (double)h[q] + (double)l[q];
-    }
-    to_host_order(p, tmp, u);
-    return FRGPU_OK;
+    const int rc = fr_get_state(p, hi, lo, u);
+    p->launches += 1;
+    return rc;
 }
 
 FRGPU_API int frgpu_state_upload(frgpu_problem *p, const double *u) {

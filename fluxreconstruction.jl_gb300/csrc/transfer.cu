@@ -1,0 +1,117 @@
+// transfer.cu -- host state arrays (FP64, the reference's Julia layout) to and
+// from the device state (internal layout, FP64 or the FP32 high/low pair).
+//
+// One cudaMemcpy moves the FP64 array into a device staging buffer; a kernel
+// then checks it for non-finite values, splits it into the FP32 high part and
+// the FP32 low part x - (double)hi (FP32K), and transposes the BGK layout
+// f[i, v, k] -> u[(i * np + k) * nvel + v].  Downloads run the reverse kernel
+// (hi + lo in FP64) and one cudaMemcpy back.  No per-element host loop.
+#include <string>
+
+#include "frgpu_internal.h"
+
+namespace {
+
+struct Layout {
+    int bgk;
+    long ne, nv, np;
+};
+
+// internal index of host index q (q = i + ne (v + nv k) for BGK, else the same)
+__device__ __forceinline__ long dev_index(const Layout &L, long q) {
+    if (!L.bgk) return q;
+    const long i = q % L.ne, r = q / L.ne, v = r % L.nv, k = r / L.nv;
+    return (i * L.np + k) * L.nv + v;
+}
+
+template <class Real>
+__global__ void k_upload(const double *__restrict__ src, Real *__restrict__ hi, Real *__restrict__ lo, long n,
+                         Layout L, unsigned long long *__restrict__ first_bad) {
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const double x = src[q];
+        if (!isfinite(x)) atomicMin(first_bad, (unsigned long long)q);
+        const long d = dev_index(L, q);
+        if (sizeof(Real) == 8) {
+            hi[d] = (Real)x;
+        } else {
+            const float h = (float)x;
+            hi[d] = h;
+            if (lo) lo[d] = (float)(x - (double)h);
+        }
+    }
+}
+
+template <class Real>
+__global__ void k_download(const Real *__restrict__ hi, const Real *__restrict__ lo, double *__restrict__ dst,
+                           long n, Layout L) {
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const long d = dev_index(L, q);
+        double x = (double)hi[d];
+        if (lo) x += (double)lo[d];
+        dst[q] = x;
+    }
+}
+
+Layout layout_of(const frgpu_problem *p) {
+    Layout L{p->d.equation == FRGPU_BGK1D ? 1 : 0, p->sp.nx, p->d.nvel, p->sp.np};
+    return L;
+}
+
+int stage_buffer(frgpu_problem *p) {
+    if (!p->d_stage) {
+        FR_CUDA(cudaMalloc(&p->d_stage, sizeof(double) * (size_t)p->ndof + sizeof(unsigned long long)));
+    }
+    return FRGPU_OK;
+}
+
+int grid_for(long n) {
+    const long g = (n + 255) / 256;
+    return (int)(g < 4 * 152 * 8 ? (g > 0 ? g : 1) : 4 * 152 * 8);
+}
+
+} // namespace
+
+// Host u (FP64, reference layout) -> device hi (and lo for FP32K); rejects
+// non-finite values with FRGPU_ERR_NONFINITE naming the first bad index.
+int fr_put_state(frgpu_problem *p, const double *u, void *hi, void *lo) {
+    int rc = stage_buffer(p);
+    if (rc) return rc;
+    double *stage = (double *)p->d_stage;
+    unsigned long long *first_bad = reinterpret_cast<unsigned long long *>(stage + p->ndof);
+    const unsigned long long none = ~0ull;
+    FR_CUDA(cudaMemcpyAsync(stage, u, sizeof(double) * (size_t)p->ndof, cudaMemcpyHostToDevice, p->stream));
+    FR_CUDA(cudaMemcpyAsync(first_bad, &none, sizeof(none), cudaMemcpyHostToDevice, p->stream));
+    const Layout L = layout_of(p);
+    if (p->esize == 8)
+        k_upload<double><<<grid_for(p->ndof), 256, 0, p->stream>>>(stage, (double *)hi, nullptr, p->ndof, L,
+                                                                     first_bad);
+    else
+        k_upload<float><<<grid_for(p->ndof), 256, 0, p->stream>>>(stage, (float *)hi, (float *)lo, p->ndof, L,
+                                                                    first_bad);
+    FR_CUDA(cudaGetLastError());
+    unsigned long long bad = none;
+    FR_CUDA(cudaMemcpyAsync(&bad, first_bad, sizeof(bad), cudaMemcpyDeviceToHost, p->stream));
+    FR_CUDA(cudaStreamSynchronize(p->stream));
+    if (bad != none) {
+        fr_set_error("state upload: non-finite value at index " + std::to_string(bad));
+        return FRGPU_ERR_NONFINITE;
+    }
+    return FRGPU_OK;
+}
+
+// Device hi (+ lo) -> host u (FP64, reference layout).
+int fr_get_state(frgpu_problem *p, const void *hi, const void *lo, double *u) {
+    int rc = stage_buffer(p);
+    if (rc) return rc;
+    double *stage = (double *)p->d_stage;
+    const Layout L = layout_of(p);
+    if (p->esize == 8)
+        k_download<double><<<grid_for(p->ndof), 256, 0, p->stream>>>((const double *)hi, nullptr, stage, p->ndof, L);
+    else
+        k_download<float><<<grid_for(p->ndof), 256, 0, p->stream>>>((const float *)hi, (const float *)lo, stage,
+                                                                      p->ndof, L);
+    FR_CUDA(cudaGetLastError());
+    FR_CUDA(cudaMemcpyAsync(u, stage, sizeof(double) * (size_t)p->ndof, cudaMemcpyDeviceToHost, p->stream));
+    FR_CUDA(cudaStreamSynchronize(p->stream));
+    return FRGPU_OK;
+}
