@@ -71,8 +71,9 @@ template <int NP> struct Tile<float, NP> {
 // loaded together with the state so that their latency is not exposed after
 // the residual: u^n in FP64 stages 2-3.  The FP32K stages instead read their
 // extra inputs (increment; in stage 3 also the high and low parts) directly
-// in the update, after an L2 prefetch issued before the y sweep: that keeps
-// shared memory at one residual's worth, so three CTAs fit on an SM.
+// in the update (stage 3's low part after an L2 prefetch issued before the y
+// sweep): that keeps shared memory at one residual's worth, so three CTAs fit
+// on an SM.
 template <int MODE, int STAGE> struct Stash {
     static constexpr int n = MODE == MODE_FP32K ? 0 : (STAGE >= 2 ? 1 : 0);
 };
@@ -324,20 +325,18 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
     __syncthreads();
 
     // ---- phase C: y interface flux; x correction into s_g -------------------
-    // FP32K: bring the stage update's extra inputs of this thread's column
-    // into L2 now; phase D reads them after the Riemann solves and corrections
-    if (MODE == MODE_FP32K && STAGE >= 2 && valid) {
+    // FP32K stage 3: bring the low part of this thread's column into L2 now;
+    // phase D reads it after the Riemann solves and corrections.  (The high
+    // part and the increments were just read by the CTA's row threads and are
+    // L2-resident already; prefetching them as well measured slower.)
+    if (MODE == MODE_FP32K && STAGE == 3 && valid) {
         const unsigned pb = (unsigned)i + (unsigned)nx * j + plane * ln;
 #pragma unroll
         for (int m = 0; m < 4; ++m)
 #pragma unroll
             for (int l = 0; l < NP; ++l) {
                 const unsigned idx = pb + plane * (NP * (l + NP * m));
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(din + idx));
-                if (STAGE == 3) {
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(uin + idx));
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(a.ul + idx));
-                }
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(a.ul + idx));
             }
     }
     {
