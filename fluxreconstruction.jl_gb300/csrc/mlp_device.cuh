@@ -159,111 +159,6 @@ __device__ __forceinline__ void mlp_forward_tile(const MLPView &w, const __nv_bf
 
 __device__ __forceinline__ float sigmoidf_(float z) { return 1.0f / (1.0f + expf(-z)); }
 
-__device__ __forceinline__ void pair_sync(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
-
-// The forward pass of one 16-sample tile shared by two warps (role 0 and 1),
-// bit-identical to mlp_forward_tile: each role computes half of the output
-// tiles of both layers; the layer-1 activations are exchanged through shared
-// memory (xch: [2 roles][32 lanes][8] words), and the output sum, which
-// mlp_forward_tile accumulates over the tiles in order, is handed from role 0
-// to role 1 (part: [32 lanes][2]).  Role 1 writes the 16 probabilities to prob.
-// bar: the named barrier of the pair (64 threads).  Both warps call it.
-__device__ __forceinline__ void mlp_forward_pair(const MLPView &w, const __nv_bfloat16 *xs, int role, int bar,
-                                                 uint32_t *xch, float *part, float *prob) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    uint32_t ax[2][4];
-#pragma unroll
-    for (int kk = 0; kk < 2; ++kk) {
-        ax[kk][0] = ld_pair(xs + g * NIN + 16 * kk + 2 * t);
-        ax[kk][1] = ld_pair(xs + (g + 8) * NIN + 16 * kk + 2 * t);
-        ax[kk][2] = ld_pair(xs + g * NIN + 16 * kk + 8 + 2 * t);
-        ax[kk][3] = ld_pair(xs + (g + 8) * NIN + 16 * kk + 8 + 2 * t);
-    }
-    // layer 1: output tiles 4 role .. 4 role + 3 -> activations of k-steps 2 role, 2 role + 1
-    float a1[4][4];
-#pragma unroll
-    for (int jj = 0; jj < 4; ++jj) {
-        const int j = 4 * role + jj;
-        const float c0 = w.b1[8 * j + 2 * t], c1 = w.b1[8 * j + 2 * t + 1];
-        a1[jj][0] = c0;
-        a1[jj][1] = c1;
-        a1[jj][2] = c0;
-        a1[jj][3] = c1;
-        const uint4 b = reinterpret_cast<const uint4 *>(w.W1)[j * 32 + lane];
-        mma16816(a1[jj], ax[0], b.x, b.y);
-        mma16816(a1[jj], ax[1], b.z, b.w);
-    }
-    uint32_t ah1[4][4];
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        const int kk = 2 * role + q;
-        ah1[kk][0] = pack_bf16(gelu(a1[2 * q][0]), gelu(a1[2 * q][1]));
-        ah1[kk][1] = pack_bf16(gelu(a1[2 * q][2]), gelu(a1[2 * q][3]));
-        ah1[kk][2] = pack_bf16(gelu(a1[2 * q + 1][0]), gelu(a1[2 * q + 1][1]));
-        ah1[kk][3] = pack_bf16(gelu(a1[2 * q + 1][2]), gelu(a1[2 * q + 1][3]));
-#pragma unroll
-        for (int r = 0; r < 4; ++r) xch[(role * 32 + lane) * 8 + 4 * q + r] = ah1[kk][r];
-    }
-    pair_sync(bar);
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        const int kk = 2 * (1 - role) + q;
-#pragma unroll
-        for (int r = 0; r < 4; ++r) ah1[kk][r] = xch[((1 - role) * 32 + lane) * 8 + 4 * q + r];
-    }
-    // layer 2: output tiles 4 role .. 4 role + 3, GELU
-    float h2[4][4];
-#pragma unroll
-    for (int jj = 0; jj < 4; ++jj) {
-        const int j = 4 * role + jj;
-        float a2[4];
-        const float c0 = w.b2[8 * j + 2 * t], c1 = w.b2[8 * j + 2 * t + 1];
-        a2[0] = c0;
-        a2[1] = c1;
-        a2[2] = c0;
-        a2[3] = c1;
-        const uint4 *bp = reinterpret_cast<const uint4 *>(w.W2) + (j * 32 + lane) * 2;
-        const uint4 b01 = bp[0], b23 = bp[1];
-        mma16816(a2, ah1[0], b01.x, b01.y);
-        mma16816(a2, ah1[1], b01.z, b01.w);
-        mma16816(a2, ah1[2], b23.x, b23.y);
-        mma16816(a2, ah1[3], b23.z, b23.w);
-#pragma unroll
-        for (int r = 0; r < 4; ++r) h2[jj][r] = gelu(a2[r]);
-    }
-    // the output sum in the order of mlp_forward_tile: tiles 0..3 (role 0), then 4..7 (role 1)
-    float sg = 0.f, sg8 = 0.f;
-    if (role == 1) {
-        pair_sync(bar);
-        sg = part[2 * lane];
-        sg8 = part[2 * lane + 1];
-    }
-#pragma unroll
-    for (int jj = 0; jj < 4; ++jj) {
-        const int j = 4 * role + jj;
-        const float w0 = w.w3[8 * j + 2 * t], w1 = w.w3[8 * j + 2 * t + 1];
-        sg = fmaf(h2[jj][0], w0, fmaf(h2[jj][1], w1, sg));
-        sg8 = fmaf(h2[jj][2], w0, fmaf(h2[jj][3], w1, sg8));
-    }
-    if (role == 0) {
-        part[2 * lane] = sg;
-        part[2 * lane + 1] = sg8;
-        pair_sync(bar); // hand the partial sums to role 1
-        pair_sync(bar); // wait for the probabilities
-        return;
-    }
-    sg += __shfl_xor_sync(0xffffffffu, sg, 1);
-    sg += __shfl_xor_sync(0xffffffffu, sg, 2);
-    sg8 += __shfl_xor_sync(0xffffffffu, sg8, 1);
-    sg8 += __shfl_xor_sync(0xffffffffu, sg8, 2);
-    const float b3 = *w.b3;
-    if (t == 0) {
-        prob[g] = sigmoidf_(sg + b3);
-        prob[g + 8] = sigmoidf_(sg8 + b3);
-    }
-    pair_sync(bar);
-}
-
 // Copy the BF16 weights and the FP32 biases / output weights to shared memory
 // (W1: NH*NIN, W2: NH*NH bf16; b: 3*NH+1 floats) with the threads of a CTA;
 // the caller synchronises.  W1 and W2 must be 16-byte aligned.
