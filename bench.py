@@ -108,9 +108,10 @@ class ClockSampler:
 
     def start(self):
         try:
-            os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-            self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
-            self.f = open(self.path, "w")
+            import tempfile
+
+            fd, self.path = tempfile.mkstemp(prefix="frgpu_clocks_", suffix=".csv")
+            self.f = os.fdopen(fd, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
@@ -132,6 +133,7 @@ class ClockSampler:
                 parts = [p.strip() for p in ln.split(",")]
                 if len(parts) >= 9:
                     rows.append(parts)
+        os.unlink(self.path)
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
 
