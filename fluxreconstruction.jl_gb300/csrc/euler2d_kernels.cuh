@@ -113,6 +113,38 @@ __device__ __forceinline__ Real ld_state(const Real *__restrict__ uin, const Rea
     return v;
 }
 
+// Shared-memory arrays keep the 4 conserved variables of a slot in 16-byte
+// chunks (4 floats or 2 doubles): variable m of slot s at lane x of a row of W
+// lanes sits at ((s * NC + m / VW) * W + x) * VW + m % VW.  A thread moves all
+// 4 variables with NC 16-byte accesses, and a warp's lanes touch consecutive
+// chunks (conflict-free).  cs is the distance between a slot's chunks.
+template <class Real> struct Vec {
+    static constexpr int VW = 16 / (int)sizeof(Real);
+    static constexpr int NC = 4 / VW;
+};
+__device__ __forceinline__ void st16(float *p, const float *v) {
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void st16(double *p, const double *v) {
+    *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
+}
+__device__ __forceinline__ void ld16(const float *p, float *v) {
+    const float4 t = *reinterpret_cast<const float4 *>(p);
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+__device__ __forceinline__ void ld16(const double *p, double *v) {
+    const double2 t = *reinterpret_cast<const double2 *>(p);
+    v[0] = t.x; v[1] = t.y;
+}
+template <class Real> __device__ __forceinline__ void put4(Real *p, int cs, const Real (&v)[4]) {
+#pragma unroll
+    for (int c = 0; c < Vec<Real>::NC; ++c) st16(p + c * cs, v + c * Vec<Real>::VW);
+}
+template <class Real> __device__ __forceinline__ void get4(const Real *p, int cs, Real (&v)[4]) {
+#pragma unroll
+    for (int c = 0; c < Vec<Real>::NC; ++c) ld16(p + c * cs, v + c * Vec<Real>::VW);
+}
+
 // FP32 CTAs of up to 256 threads: registers capped so that three CTAs share an SM
 // FUSE: stage 3 of the FP32K form with np = 4 also runs the learned troubled-cell
 // indicator + :l2 filter on the elements it has just updated (the post-step
@@ -137,14 +169,18 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
     Real *s_Fx = s_hx + S::HX;
     Real *s_Fy = s_Fx + S::FX;
     Real *s_st = s_Fy + S::FY;
-#define SST(q, ey, l, k, m, ex) s_st[(q) * S::U + ((((ey) * NP + (l)) * NP + (k)) * 4 + (m)) * TX + (ex)]
-#define SU(ey, l, k, m, ex) s_u[((((ey) * NP + (l)) * NP + (k)) * 4 + (m)) * TX + (ex)]
-#define SG(ey, l, k, m, ex) s_g[((((ey) * NP + (l)) * NP + (k)) * 4 + (m)) * TX + (ex)]
-#define STR(arr, ey, q, m, ex) arr[(((ey) * NP + (q)) * 4 + (m)) * TX + (ex)]
-#define SHY(side, k, m, ex) s_hy[(((side) * NP + (k)) * 4 + (m)) * TX + (ex)]
+    constexpr int VW = Vec<Real>::VW, NC = Vec<Real>::NC;
+#define VIX(sl, m, x, W) ((((sl) * NC + (m) / VW) * (W) + (x)) * VW + (m) % VW)
+#define SST(q, ey, l, k, m, ex) s_st[(q) * S::U + VIX(((ey) * NP + (l)) * NP + (k), m, ex, TX)]
+#define SU(ey, l, k, m, ex) s_u[VIX(((ey) * NP + (l)) * NP + (k), m, ex, TX)]
+#define SG(ey, l, k, m, ex) s_g[VIX(((ey) * NP + (l)) * NP + (k), m, ex, TX)]
+#define STR(arr, ey, q, m, ex) arr[VIX((ey) * NP + (q), m, ex, TX)]
+#define SHY(side, k, m, ex) s_hy[VIX((side) * NP + (k), m, ex, TX)]
 #define SHX(side, ey, l, m) s_hx[(((side) * TY + (ey)) * NP + (l)) * 4 + (m)]
-#define SFX(ey, l, m, f) s_Fx[(((ey) * NP + (l)) * 4 + (m)) * (TX + 1) + (f)]
-#define SFY(fy, k, m, ex) s_Fy[(((fy) * NP + (k)) * 4 + (m)) * TX + (ex)]
+#define SFX(ey, l, m, f) s_Fx[VIX((ey) * NP + (l), m, f, TX + 1)]
+#define SFY(fy, k, m, ex) s_Fy[VIX((fy) * NP + (k), m, ex, TX)]
+    // chunk strides: rows of TX lanes, the TX + 1 x-faces, and the contiguous SHX
+    constexpr int CS = TX * VW, CSF = (TX + 1) * VW, CSX = VW;
 
     const int tid = threadIdx.x;
     const int ex = tid % TX, ln = (tid / TX) % NP, ey = tid / (TX * NP);
@@ -169,18 +205,21 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
         if (valid) {
             const unsigned base = (unsigned)i + (unsigned)nx * j + plane * (NP * l);
 #pragma unroll
-            for (int m = 0; m < 4; ++m)
+            for (int k = 0; k < NP; ++k) {
+                Real un[4];
 #pragma unroll
-                for (int k = 0; k < NP; ++k) {
+                for (int m = 0; m < 4; ++m) {
                     const unsigned idx = base + plane * (k + NP * NP * m);
                     if (MODE == MODE_FP32K && STAGE >= 2) {
                         const Real h = __ldg(uin + idx), d = __ldg(din + idx);
                         u[k][m] = h + d;
                     } else {
                         u[k][m] = ld_state(uin, din, idx);
-                        if (MODE == MODE_FP64 && STAGE >= 2) SST(0, ey, l, k, m, ex) = a.un[idx];
+                        if (MODE == MODE_FP64 && STAGE >= 2) un[m] = a.un[idx];
                     }
                 }
+                if (MODE == MODE_FP64 && STAGE >= 2) put4(&SST(0, ey, l, k, 0, ex), CS, un);
+            }
         } else {
 #pragma unroll
             for (int k = 0; k < NP; ++k) {
@@ -201,22 +240,26 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             int jo;
             if (resolve(jn, ny, a.bc[2], a.bc[3], jo)) {
                 const unsigned base = (unsigned)(i0 + hx) + (unsigned)nx * jo + plane * hk;
+                Real h[4];
 #pragma unroll
                 for (int m = 0; m < 4; ++m) {
                     Real v[NP];
 #pragma unroll
                     for (int l = 0; l < NP; ++l) v[l] = ld_state(uin, din, base + plane * (NP * (l + NP * m)));
-                    SHY(side, hk, m, hx) = dotw<Real, NP>(v, w);
+                    h[m] = dotw<Real, NP>(v, w);
                 }
+                put4(&SHY(side, hk, 0, hx), CS, h);
             } else {
                 const int s = side == 0 ? 2 : 3;
+                Real h[4];
 #pragma unroll
                 for (int m = 0; m < 4; ++m) {
                     Real v[NP];
 #pragma unroll
                     for (int l = 0; l < NP; ++l) v[l] = a.fixed[s][m];
-                    SHY(side, hk, m, hx) = dotw<Real, NP>(v, w);
+                    h[m] = dotw<Real, NP>(v, w);
                 }
+                put4(&SHY(side, hk, 0, hx), CS, h);
             }
         } else {
             const int u = t - 2 * NP * TX;
@@ -229,21 +272,25 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             int io;
             if (resolve(in_, nx, a.bc[0], a.bc[1], io)) {
                 const unsigned base = (unsigned)io + (unsigned)nx * (j0 + hy) + plane * (NP * hl);
+                Real h[4];
 #pragma unroll
                 for (int m = 0; m < 4; ++m) {
                     Real v[NP];
 #pragma unroll
                     for (int k = 0; k < NP; ++k) v[k] = ld_state(uin, din, base + plane * (k + NP * NP * m));
-                    SHX(side, hy, hl, m) = dotw<Real, NP>(v, w);
+                    h[m] = dotw<Real, NP>(v, w);
                 }
+                put4(&SHX(side, hy, hl, 0), CSX, h);
             } else {
+                Real h[4];
 #pragma unroll
                 for (int m = 0; m < 4; ++m) {
                     Real v[NP];
 #pragma unroll
                     for (int k = 0; k < NP; ++k) v[k] = a.fixed[side][m];
-                    SHX(side, hy, hl, m) = dotw<Real, NP>(v, w);
+                    h[m] = dotw<Real, NP>(v, w);
                 }
+                put4(&SHX(side, hy, hl, 0), CSX, h);
             }
         }
     }
@@ -255,6 +302,7 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
         Real fx[NP][4], gy[NP][4];
 #pragma unroll
         for (int k = 0; k < NP; ++k) euler2d_flux<Real>(u[k], a.gm1, a.iJx, a.iJy, fx[k], gy[k], bad);
+        Real tl[4], tr[4];
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
             Real uc[NP], fc[NP];
@@ -262,15 +310,17 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             for (int k = 0; k < NP; ++k) { uc[k] = u[k][m]; fc[k] = fx[k][m]; }
 #pragma unroll
             for (int k = 0; k < NP; ++k) rx[k][m] = dotw<Real, NP>(fc, op.D[k]);
-            STR(s_uxl, ey, l, m, ex) = dotw<Real, NP>(uc, op.ll);
-            STR(s_uxr, ey, l, m, ex) = dotw<Real, NP>(uc, op.lr);
+            tl[m] = dotw<Real, NP>(uc, op.ll);
+            tr[m] = dotw<Real, NP>(uc, op.lr);
             fxl[m] = dotw<Real, NP>(fc, op.ll);
             fxr[m] = dotw<Real, NP>(fc, op.lr);
+        }
+        put4(&STR(s_uxl, ey, l, 0, ex), CS, tl);
+        put4(&STR(s_uxr, ey, l, 0, ex), CS, tr);
 #pragma unroll
-            for (int k = 0; k < NP; ++k) {
-                SU(ey, l, k, m, ex) = u[k][m];
-                SG(ey, l, k, m, ex) = gy[k][m];
-            }
+        for (int k = 0; k < NP; ++k) {
+            put4(&SU(ey, l, k, 0, ex), CS, u[k]);
+            put4(&SG(ey, l, k, 0, ex), CS, gy[k]);
         }
     }
     __syncthreads();
@@ -279,30 +329,45 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
     Real ry[NP][4], gyb[4], gyt[4];
     {
         const int k = ln;
+        {
+            Real col[NP][4], tb[4], tt[4];
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            Real uc[NP], gc[NP];
+            for (int l = 0; l < NP; ++l) get4(&SU(ey, l, k, 0, ex), CS, col[l]);
 #pragma unroll
-            for (int l = 0; l < NP; ++l) { uc[l] = SU(ey, l, k, m, ex); gc[l] = SG(ey, l, k, m, ex); }
+            for (int m = 0; m < 4; ++m) {
+                Real uc[NP];
 #pragma unroll
-            for (int l = 0; l < NP; ++l) ry[l][m] = dotw<Real, NP>(gc, op.D[l]);
-            STR(s_uyb, ey, k, m, ex) = dotw<Real, NP>(uc, op.ll);
-            STR(s_uyt, ey, k, m, ex) = dotw<Real, NP>(uc, op.lr);
-            gyb[m] = dotw<Real, NP>(gc, op.ll);
-            gyt[m] = dotw<Real, NP>(gc, op.lr);
+                for (int l = 0; l < NP; ++l) uc[l] = col[l][m];
+                tb[m] = dotw<Real, NP>(uc, op.ll);
+                tt[m] = dotw<Real, NP>(uc, op.lr);
+            }
+            put4(&STR(s_uyb, ey, k, 0, ex), CS, tb);
+            put4(&STR(s_uyt, ey, k, 0, ex), CS, tt);
+        }
+        {
+            Real col[NP][4];
+#pragma unroll
+            for (int l = 0; l < NP; ++l) get4(&SG(ey, l, k, 0, ex), CS, col[l]);
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                Real gc[NP];
+#pragma unroll
+                for (int l = 0; l < NP; ++l) gc[l] = col[l][m];
+#pragma unroll
+                for (int l = 0; l < NP; ++l) ry[l][m] = dotw<Real, NP>(gc, op.D[l]);
+                gyb[m] = dotw<Real, NP>(gc, op.ll);
+                gyt[m] = dotw<Real, NP>(gc, op.lr);
+            }
         }
         // x interface flux at the left face of element ex (row l = ln)
         if (valid) {
             const int l = ln;
             Real wL[4], wR[4], F[4];
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                wL[m] = ex > 0 ? STR(s_uxr, ey, l, m, ex - 1) : SHX(0, ey, l, m);
-                wR[m] = STR(s_uxl, ey, l, m, ex);
-            }
+            if (ex > 0) get4(&STR(s_uxr, ey, l, 0, ex - 1), CS, wL);
+            else get4(&SHX(0, ey, l, 0), CSX, wL);
+            get4(&STR(s_uxl, ey, l, 0, ex), CS, wR);
             riemann2d<Real, 0, FLUX>(wL, wR, a.gamma, a.gm1, F);
-#pragma unroll
-            for (int m = 0; m < 4; ++m) SFX(ey, l, m, ex) = F[m];
+            put4(&SFX(ey, l, 0, ex), CSF, F);
         }
         // the TY * NP faces on the tile's right edge, by the first threads of
         // warp 0 only (an extra solve on every warp's last lane would make all
@@ -311,14 +376,10 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             const int ye = tid / NP, le = tid % NP;
             if (ye < vy) {
                 Real wL[4], wR[4], F[4];
-#pragma unroll
-                for (int m = 0; m < 4; ++m) {
-                    wL[m] = STR(s_uxr, ye, le, m, vx - 1);
-                    wR[m] = SHX(1, ye, le, m);
-                }
+                get4(&STR(s_uxr, ye, le, 0, vx - 1), CS, wL);
+                get4(&SHX(1, ye, le, 0), CSX, wR);
                 riemann2d<Real, 0, FLUX>(wL, wR, a.gamma, a.gm1, F);
-#pragma unroll
-                for (int m = 0; m < 4; ++m) SFX(ye, le, m, vx) = F[m];
+                put4(&SFX(ye, le, 0, vx), CSF, F);
             }
         }
     }
@@ -343,32 +404,32 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
         const int k = ln;
         if (valid) {
             Real wL[4], wR[4], F[4];
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                wL[m] = ey > 0 ? STR(s_uyt, ey - 1, k, m, ex) : SHY(0, k, m, ex);
-                wR[m] = STR(s_uyb, ey, k, m, ex);
-            }
+            get4(ey > 0 ? &STR(s_uyt, ey - 1, k, 0, ex) : &SHY(0, k, 0, ex), CS, wL);
+            get4(&STR(s_uyb, ey, k, 0, ex), CS, wR);
             riemann2d<Real, 1, FLUX>(wL, wR, a.gamma, a.gm1, F);
-#pragma unroll
-            for (int m = 0; m < 4; ++m) SFY(ey, k, m, ex) = F[m];
+            put4(&SFY(ey, k, 0, ex), CS, F);
             if (ey == vy - 1) {
-#pragma unroll
-                for (int m = 0; m < 4; ++m) {
-                    wL[m] = STR(s_uyt, ey, k, m, ex);
-                    wR[m] = SHY(1, k, m, ex);
-                }
+                get4(&STR(s_uyt, ey, k, 0, ex), CS, wL);
+                get4(&SHY(1, k, 0, ex), CS, wR);
                 riemann2d<Real, 1, FLUX>(wL, wR, a.gamma, a.gm1, F);
-#pragma unroll
-                for (int m = 0; m < 4; ++m) SFY(ey + 1, k, m, ex) = F[m];
+                put4(&SFY(ey + 1, k, 0, ex), CS, F);
             }
             // x correction of row l = ln: rx + (F*_L iJx - f_L) dgl + (F*_R iJx - f_R) dgr
             const int l = ln;
+            Real aL[4], aR[4];
+            get4(&SFX(ey, l, 0, ex), CSF, aL);
+            get4(&SFX(ey, l, 0, ex + 1), CSF, aR);
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
-                const Real aL = SFX(ey, l, m, ex) * a.iJx - fxl[m];
-                const Real aR = SFX(ey, l, m, ex + 1) * a.iJx - fxr[m];
+                aL[m] = aL[m] * a.iJx - fxl[m];
+                aR[m] = aR[m] * a.iJx - fxr[m];
+            }
 #pragma unroll
-                for (int kk = 0; kk < NP; ++kk) SG(ey, l, kk, m, ex) = fmaR<Real>(aR, op.dgr[kk], fmaR<Real>(aL, op.dgl[kk], rx[kk][m]));
+            for (int kk = 0; kk < NP; ++kk) {
+                Real g[4];
+#pragma unroll
+                for (int m = 0; m < 4; ++m) g[m] = fmaR<Real>(aR[m], op.dgr[kk], fmaR<Real>(aL[m], op.dgl[kk], rx[kk][m]));
+                put4(&SG(ey, l, kk, 0, ex), CS, g);
             }
         }
     }
@@ -380,13 +441,23 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
         const Real dt = (Real)(*a.dtp);
         const unsigned base = (unsigned)i + (unsigned)nx * j + plane * k;
         Real chk = Real(0);
+        Real bB[4], bT[4];
+        get4(&SFY(ey, k, 0, ex), CS, bB);
+        get4(&SFY(ey + 1, k, 0, ex), CS, bT);
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
-            const Real bB = SFY(ey, k, m, ex) * a.iJy - gyb[m];
-            const Real bT = SFY(ey + 1, k, m, ex) * a.iJy - gyt[m];
+            bB[m] = bB[m] * a.iJy - gyb[m];
+            bT[m] = bT[m] * a.iJy - gyt[m];
+        }
 #pragma unroll
-            for (int l = 0; l < NP; ++l) {
-                const Real r = fmaR<Real>(bT, op.dgr[l], fmaR<Real>(bB, op.dgl[l], SG(ey, l, k, m, ex) + ry[l][m]));
+        for (int l = 0; l < NP; ++l) {
+            Real g[4], ui4[4], un4[4], tn[4];
+            get4(&SG(ey, l, k, 0, ex), CS, g);
+            if (MODE == MODE_FP64 && STAGE >= 1) get4(&SU(ey, l, k, 0, ex), CS, ui4);
+            if (MODE == MODE_FP64 && STAGE >= 2) get4(&SST(0, ey, l, k, 0, ex), CS, un4);
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                const Real r = fmaR<Real>(bT[m], op.dgr[l], fmaR<Real>(bB[m], op.dgl[l], g[m] + ry[l][m]));
                 const Real du = -r;
                 const unsigned idx = base + plane * (NP * (l + NP * m));
                 Real res;
@@ -394,14 +465,14 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                     res = du;
                     a.out[idx] = res;
                 } else if (MODE == MODE_FP64) {
-                    const Real ui = SU(ey, l, k, m, ex);
+                    const Real ui = ui4[m];
                     if (STAGE == 1) {
                         res = fmaR<Real>(dt, du, ui);
                     } else if (STAGE == 2) {
-                        const Real un = SST(0, ey, l, k, m, ex);
+                        const Real un = un4[m];
                         res = (fmaR<Real>(dt, du, fmaR<Real>(Real(3), un, ui))) * Real(0.25);
                     } else {
-                        const Real un = SST(0, ey, l, k, m, ex);
+                        const Real un = un4[m];
                         res = fmaR<Real>(Real(2) * dt, du, fmaR<Real>(Real(2), ui, un)) * Real(1.0 / 3.0);
                     }
                     a.out[idx] = res;
@@ -427,11 +498,13 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                         a.out[idx] = t;
                         a.ul[idx] = lo_new;
                         res = t;
-                        if (FUSE) SU(ey, l, k, m, ex) = t; // u is dead in FP32K phase D: it now holds u^{n+1}
+                        tn[m] = t;
                     }
                 }
                 chk += res; // NaN and Inf propagate into the check sum
             }
+            // u is dead in FP32K phase D: with the fused indicator it now holds u^{n+1}
+            if (FUSE) put4(&SU(ey, l, k, 0, ex), CS, tn);
         }
         if (!isfinite(chk)) bad |= ST_NONFINITE;
     }
@@ -459,8 +532,10 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
 #pragma unroll
             for (int kq = 0; kq < 8; ++kq) {
                 const int q = (pr ? 8 : 0) + kq, kk = q & 3, ll = q >> 2;
+                Real t4[4];
+                get4(&SU(eyt, ll, kk, 0, exl), CS, t4);
 #pragma unroll
-                for (int m = 0; m < 4; ++m) w[kq][m] = ev ? (float)SU(eyt, ll, kk, m, exl) : (m == 0 ? 1.f : 0.f);
+                for (int m = 0; m < 4; ++m) w[kq][m] = ev ? (float)t4[m] : (m == 0 ? 1.f : 0.f);
             }
             float feat[16], su = 0.f;
             features_from_raw(w, ev, pr, a.iv1, (float)a.gm1, feat, su);
@@ -510,6 +585,7 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
 #undef SFX
 #undef SFY
 #undef SST
+#undef VIX
 }
 
 template <class Real, int NP> Ops<Real, NP> make_ops(const frgpu_space &s) {
@@ -522,30 +598,6 @@ template <class Real, int NP> Ops<Real, NP> make_ops(const frgpu_space &s) {
         for (int q = 0; q < NP; ++q) o.D[k][q] = (Real)s.dl[k + NP * q];
     }
     return o;
-}
-
-template <class Real, int NP>
-E2DArgs<Real, NP> make_e2d_args(frgpu_problem *p, const void *in, const void *din, void *out) {
-    E2DArgs<Real, NP> a;
-    a.nx = p->sp.nx;
-    a.ny = p->sp.ny;
-    a.uin = (const Real *)in;
-    a.din = (const Real *)din;
-    a.un = (const Real *)p->s0;
-    a.out = (Real *)out;
-    a.ul = (Real *)p->s3;
-    a.dtp = p->d_dt;
-    a.iJx = (Real)(1.0 / (0.5 * p->sp.dx));
-    a.iJy = (Real)(1.0 / (0.5 * p->sp.dy));
-    a.gamma = (Real)p->d.gamma;
-    a.gm1 = (Real)(p->d.gamma - 1.0);
-    for (int s = 0; s < 4; ++s) {
-        a.bc[s] = p->d.bc[s];
-        for (int m = 0; m < 4; ++m) a.fixed[s][m] = (Real)p->d.fixed_state[s][m];
-    }
-    a.ops = make_ops<Real, NP>(p->sp);
-    a.status = p->d_status;
-    return a;
 }
 
 template <class Real, int NP, int FLUX, int MODE, int STAGE, bool FUSE = false>
