@@ -304,17 +304,11 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
         for (int k = 0; k < NP; ++k) euler2d_flux<Real>(u[k], a.gm1, a.iJx, a.iJy, fx[k], gy[k], bad);
         Real tl[4], tr[4];
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            Real uc[NP], fc[NP];
-#pragma unroll
-            for (int k = 0; k < NP; ++k) { uc[k] = u[k][m]; fc[k] = fx[k][m]; }
-#pragma unroll
-            for (int k = 0; k < NP; ++k) rx[k][m] = dotw<Real, NP>(fc, op.D[k]);
-            tl[m] = dotw<Real, NP>(uc, op.ll);
-            tr[m] = dotw<Real, NP>(uc, op.lr);
-            fxl[m] = dotw<Real, NP>(fc, op.ll);
-            fxr[m] = dotw<Real, NP>(fc, op.lr);
-        }
+        for (int k = 0; k < NP; ++k) v4_dotw<Real, NP>(fx, op.D[k], rx[k]);
+        v4_dotw<Real, NP>(u, op.ll, tl);
+        v4_dotw<Real, NP>(u, op.lr, tr);
+        v4_dotw<Real, NP>(fx, op.ll, fxl);
+        v4_dotw<Real, NP>(fx, op.lr, fxr);
         put4(&STR(s_uxl, ey, l, 0, ex), CS, tl);
         put4(&STR(s_uxr, ey, l, 0, ex), CS, tr);
 #pragma unroll
@@ -333,14 +327,8 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             Real col[NP][4], tb[4], tt[4];
 #pragma unroll
             for (int l = 0; l < NP; ++l) get4(&SU(ey, l, k, 0, ex), CS, col[l]);
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                Real uc[NP];
-#pragma unroll
-                for (int l = 0; l < NP; ++l) uc[l] = col[l][m];
-                tb[m] = dotw<Real, NP>(uc, op.ll);
-                tt[m] = dotw<Real, NP>(uc, op.lr);
-            }
+            v4_dotw<Real, NP>(col, op.ll, tb);
+            v4_dotw<Real, NP>(col, op.lr, tt);
             put4(&STR(s_uyb, ey, k, 0, ex), CS, tb);
             put4(&STR(s_uyt, ey, k, 0, ex), CS, tt);
         }
@@ -349,15 +337,9 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
 #pragma unroll
             for (int l = 0; l < NP; ++l) get4(&SG(ey, l, k, 0, ex), CS, col[l]);
 #pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                Real gc[NP];
-#pragma unroll
-                for (int l = 0; l < NP; ++l) gc[l] = col[l][m];
-#pragma unroll
-                for (int l = 0; l < NP; ++l) ry[l][m] = dotw<Real, NP>(gc, op.D[l]);
-                gyb[m] = dotw<Real, NP>(gc, op.ll);
-                gyt[m] = dotw<Real, NP>(gc, op.lr);
-            }
+            for (int l = 0; l < NP; ++l) v4_dotw<Real, NP>(col, op.D[l], ry[l]);
+            v4_dotw<Real, NP>(col, op.ll, gyb);
+            v4_dotw<Real, NP>(col, op.lr, gyt);
         }
         // x interface flux at the left face of element ex (row l = ln)
         if (valid) {
@@ -416,19 +398,16 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             }
             // x correction of row l = ln: rx + (F*_L iJx - f_L) dgl + (F*_R iJx - f_R) dgr
             const int l = ln;
-            Real aL[4], aR[4];
-            get4(&SFX(ey, l, 0, ex), CSF, aL);
-            get4(&SFX(ey, l, 0, ex + 1), CSF, aR);
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                aL[m] = aL[m] * a.iJx - fxl[m];
-                aR[m] = aR[m] * a.iJx - fxr[m];
-            }
+            Real FL[4], FR[4], aL[4], aR[4];
+            get4(&SFX(ey, l, 0, ex), CSF, FL);
+            get4(&SFX(ey, l, 0, ex + 1), CSF, FR);
+            v4_fms<Real>(FL, a.iJx, fxl, aL);
+            v4_fms<Real>(FR, a.iJx, fxr, aR);
 #pragma unroll
             for (int kk = 0; kk < NP; ++kk) {
                 Real g[4];
-#pragma unroll
-                for (int m = 0; m < 4; ++m) g[m] = fmaR<Real>(aR[m], op.dgr[kk], fmaR<Real>(aL[m], op.dgl[kk], rx[kk][m]));
+                v4_fma<Real>(aL, op.dgl[kk], rx[kk], g);
+                v4_fma<Real>(aR, op.dgr[kk], g, g);
                 put4(&SG(ey, l, kk, 0, ex), CS, g);
             }
         }
@@ -440,73 +419,83 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
         const int k = ln;
         const Real dt = (Real)(*a.dtp);
         const unsigned base = (unsigned)i + (unsigned)nx * j + plane * k;
-        Real chk = Real(0);
-        Real bB[4], bT[4];
-        get4(&SFY(ey, k, 0, ex), CS, bB);
-        get4(&SFY(ey + 1, k, 0, ex), CS, bT);
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            bB[m] = bB[m] * a.iJy - gyb[m];
-            bT[m] = bT[m] * a.iJy - gyt[m];
-        }
+        Real chk[4] = {Real(0), Real(0), Real(0), Real(0)};
+        Real FB[4], FT[4], bB[4], bT[4];
+        get4(&SFY(ey, k, 0, ex), CS, FB);
+        get4(&SFY(ey + 1, k, 0, ex), CS, FT);
+        v4_fms<Real>(FB, a.iJy, gyb, bB);
+        v4_fms<Real>(FT, a.iJy, gyt, bT);
 #pragma unroll
         for (int l = 0; l < NP; ++l) {
-            Real g[4], ui4[4], un4[4], tn[4];
-            get4(&SG(ey, l, k, 0, ex), CS, g);
-            if (MODE == MODE_FP64 && STAGE >= 1) get4(&SU(ey, l, k, 0, ex), CS, ui4);
-            if (MODE == MODE_FP64 && STAGE >= 2) get4(&SST(0, ey, l, k, 0, ex), CS, un4);
+            // r = -du/dt at the NP points of row l, column k, all 4 variables
+            Real r[4], res[4];
+            get4(&SG(ey, l, k, 0, ex), CS, r);
+            v4_add<Real>(r, ry[l], r);
+            v4_fma<Real>(bB, op.dgl[l], r, r);
+            v4_fma<Real>(bT, op.dgr[l], r, r);
+            unsigned idx[4];
 #pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                const Real r = fmaR<Real>(bT[m], op.dgr[l], fmaR<Real>(bB[m], op.dgl[l], g[m] + ry[l][m]));
-                const Real du = -r;
-                const unsigned idx = base + plane * (NP * (l + NP * m));
-                Real res;
-                if (STAGE == 0) {
-                    res = du;
-                    a.out[idx] = res;
-                } else if (MODE == MODE_FP64) {
-                    const Real ui = ui4[m];
-                    if (STAGE == 1) {
-                        res = fmaR<Real>(dt, du, ui);
-                    } else if (STAGE == 2) {
-                        const Real un = un4[m];
-                        res = (fmaR<Real>(dt, du, fmaR<Real>(Real(3), un, ui))) * Real(0.25);
-                    } else {
-                        const Real un = un4[m];
-                        res = fmaR<Real>(Real(2) * dt, du, fmaR<Real>(Real(2), ui, un)) * Real(1.0 / 3.0);
-                    }
-                    a.out[idx] = res;
-                } else {
-                    // FP32K: stage values are u^n + d; only increments are stored,
-                    // and the step's total increment is added to u^n with a
-                    // compensated (Kahan/Fast2Sum) sum whose low part persists.
-                    if (STAGE == 1) {
-                        res = dt * du;
-                        a.out[idx] = res;
-                    } else if (STAGE == 2) {
-                        const Real d1 = __ldg(din + idx);
-                        res = fmaR<Real>(dt, du, d1) * Real(0.25);
-                        a.out[idx] = res;
-                    } else {
-                        const Real d2 = __ldg(din + idx);
-                        const Real d3 = fmaR<Real>(dt, du, d2) * Real(2.0 / 3.0);
-                        const Real hi = __ldg(uin + idx);
-                        const Real lo = a.ul[idx];
-                        const Real y = d3 + lo;
-                        const Real t = hi + y;
-                        const Real lo_new = y - (t - hi);
-                        a.out[idx] = t;
-                        a.ul[idx] = lo_new;
-                        res = t;
-                        tn[m] = t;
-                    }
+            for (int m = 0; m < 4; ++m) idx[m] = base + plane * (NP * (l + NP * m));
+            if (STAGE == 0) {
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    res[m] = -r[m];
+                    a.out[idx[m]] = res[m];
                 }
-                chk += res; // NaN and Inf propagate into the check sum
+            } else if (MODE == MODE_FP64) {
+                Real ui4[4], un4[4];
+                get4(&SU(ey, l, k, 0, ex), CS, ui4);
+                if (STAGE >= 2) get4(&SST(0, ey, l, k, 0, ex), CS, un4);
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    const Real du = -r[m], ui = ui4[m];
+                    if (STAGE == 1) {
+                        res[m] = fmaR<Real>(dt, du, ui);
+                    } else if (STAGE == 2) {
+                        res[m] = (fmaR<Real>(dt, du, fmaR<Real>(Real(3), un4[m], ui))) * Real(0.25);
+                    } else {
+                        res[m] = fmaR<Real>(Real(2) * dt, du, fmaR<Real>(Real(2), ui, un4[m])) * Real(1.0 / 3.0);
+                    }
+                    a.out[idx[m]] = res[m];
+                }
+            } else {
+                // FP32K: stage values are u^n + d; only increments are stored,
+                // and the step's total increment is added to u^n with a
+                // compensated (Kahan/Fast2Sum) sum whose low part persists.
+                // dt du = (-dt) r exactly.
+                if (STAGE == 1) {
+                    v4_mul<Real>(r, -dt, res);
+                } else if (STAGE == 2) {
+                    Real d1[4];
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) d1[m] = __ldg(din + idx[m]);
+                    v4_fma<Real>(r, -dt, d1, res);
+                    v4_mul<Real>(res, Real(0.25), res);
+                } else {
+                    Real d2[4], hi[4], lo[4], y[4], e[4];
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) {
+                        d2[m] = __ldg(din + idx[m]);
+                        hi[m] = __ldg(uin + idx[m]);
+                        lo[m] = a.ul[idx[m]];
+                    }
+                    v4_fma<Real>(r, -dt, d2, y);
+                    v4_mul<Real>(y, Real(2.0 / 3.0), y); // d3
+                    v4_add<Real>(y, lo, y);               // y = d3 + lo
+                    v4_add<Real>(hi, y, res);             // t = hi + y
+                    v4_sub<Real>(res, hi, e);
+                    v4_sub<Real>(y, e, lo);               // lo_new = y - (t - hi)
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) a.ul[idx[m]] = lo[m];
+                    // u is dead in FP32K phase D: with the fused indicator it now holds u^{n+1}
+                    if (FUSE) put4(&SU(ey, l, k, 0, ex), CS, res);
+                }
+#pragma unroll
+                for (int m = 0; m < 4; ++m) a.out[idx[m]] = res[m];
             }
-            // u is dead in FP32K phase D: with the fused indicator it now holds u^{n+1}
-            if (FUSE) put4(&SU(ey, l, k, 0, ex), CS, tn);
+            v4_add<Real>(chk, res, chk); // NaN and Inf propagate into the check sums
         }
-        if (!isfinite(chk)) bad |= ST_NONFINITE;
+        if (!isfinite(chk[0] + chk[1] + chk[2] + chk[3])) bad |= ST_NONFINITE;
     }
     if (bad) atomicOr(a.status, bad);
 

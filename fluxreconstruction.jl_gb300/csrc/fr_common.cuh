@@ -63,6 +63,71 @@ __device__ __forceinline__ Real dotw(const Real (&v)[NP], const Real *w) {
     return s;
 }
 
+// Arithmetic on the 4 conserved variables of one point.  FP32 runs it as two
+// packed pairs (variables 0-1 and 2-3) with the f32x2 instructions of sm_100+
+// (__ffma2_rn, __fmul2_rn, __fadd2_rn): each lane rounds exactly as the scalar
+// operation does, at half the instruction count.  FP64 runs the four scalar
+// operations, in the same order as the oracle.
+template <class Real> __device__ __forceinline__ void v4_mul(const Real (&a)[4], Real w, Real (&d)[4]) {
+#pragma unroll
+    for (int m = 0; m < 4; ++m) d[m] = a[m] * w;
+}
+template <class Real>
+__device__ __forceinline__ void v4_fma(const Real (&a)[4], Real w, const Real (&c)[4], Real (&d)[4]) {
+#pragma unroll
+    for (int m = 0; m < 4; ++m) d[m] = fmaR<Real>(a[m], w, c[m]);
+}
+template <class Real> __device__ __forceinline__ void v4_add(const Real (&a)[4], const Real (&b)[4], Real (&d)[4]) {
+#pragma unroll
+    for (int m = 0; m < 4; ++m) d[m] = a[m] + b[m];
+}
+template <class Real> __device__ __forceinline__ void v4_sub(const Real (&a)[4], const Real (&b)[4], Real (&d)[4]) {
+#pragma unroll
+    for (int m = 0; m < 4; ++m) d[m] = a[m] - b[m];
+}
+__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+template <> __device__ __forceinline__ void v4_mul<float>(const float (&a)[4], float w, float (&d)[4]) {
+    const float2 ww = f2(w, w), lo = __fmul2_rn(f2(a[0], a[1]), ww), hi = __fmul2_rn(f2(a[2], a[3]), ww);
+    d[0] = lo.x; d[1] = lo.y; d[2] = hi.x; d[3] = hi.y;
+}
+template <>
+__device__ __forceinline__ void v4_fma<float>(const float (&a)[4], float w, const float (&c)[4], float (&d)[4]) {
+    const float2 ww = f2(w, w);
+    const float2 lo = __ffma2_rn(f2(a[0], a[1]), ww, f2(c[0], c[1]));
+    const float2 hi = __ffma2_rn(f2(a[2], a[3]), ww, f2(c[2], c[3]));
+    d[0] = lo.x; d[1] = lo.y; d[2] = hi.x; d[3] = hi.y;
+}
+template <> __device__ __forceinline__ void v4_add<float>(const float (&a)[4], const float (&b)[4], float (&d)[4]) {
+    const float2 lo = __fadd2_rn(f2(a[0], a[1]), f2(b[0], b[1])), hi = __fadd2_rn(f2(a[2], a[3]), f2(b[2], b[3]));
+    d[0] = lo.x; d[1] = lo.y; d[2] = hi.x; d[3] = hi.y;
+}
+template <> __device__ __forceinline__ void v4_sub<float>(const float (&a)[4], const float (&b)[4], float (&d)[4]) {
+    const float2 lo = __fadd2_rn(f2(a[0], a[1]), f2(-b[0], -b[1])), hi = __fadd2_rn(f2(a[2], a[3]), f2(-b[2], -b[3]));
+    d[0] = lo.x; d[1] = lo.y; d[2] = hi.x; d[3] = hi.y;
+}
+// d = a w - c: FP64 rounds the product and the difference (the oracle's
+// order); FP32 fuses them into one fma (what the FP32 build contracts it to)
+template <class Real>
+__device__ __forceinline__ void v4_fms(const Real (&a)[4], Real w, const Real (&c)[4], Real (&d)[4]) {
+    if constexpr (sizeof(Real) == 4) {
+        const Real nc[4] = {-c[0], -c[1], -c[2], -c[3]};
+        v4_fma<Real>(a, w, nc, d);
+    } else {
+#pragma unroll
+        for (int m = 0; m < 4; ++m) d[m] = a[m] * w - c[m];
+    }
+}
+// d[m] = sum_q v[q][m] w[q] as the ascending chain of dotw, for 4 variables
+template <class Real, int NP>
+__device__ __forceinline__ void v4_dotw(const Real (&v)[NP][4], const Real *w, Real (&d)[4]) {
+    Real s[4];
+    v4_mul<Real>(v[0], w[0], s);
+#pragma unroll
+    for (int q = 1; q < NP; ++q) v4_fma<Real>(v[q], w[q], s, s);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) d[m] = s[m];
+}
+
 // Operators of one space, passed by value (kernel parameter / constant bank).
 template <class Real, int NP> struct Ops {
     Real ll[NP], lr[NP], dgl[NP], dgr[NP];
@@ -118,8 +183,17 @@ __device__ __forceinline__ void riemann2d(const Real (&wL)[4], const Real (&wR)[
     euler2d_dirflux<Real, DIR>(wR, gamma, gm1, fR, uR, cR);
     if (FLUX == FLUX_LF) {
         Real lam = maxR<Real>(absR<Real>(uL) + cL, absR<Real>(uR) + cR);
+        if constexpr (sizeof(Real) == 4) {
+            // 0.5 (fL + fR) + (-0.5 lam)(wR - wL), one fma per variable
+            Real s[4], d[4], h[4];
+            v4_add<Real>(fL, fR, s);
+            v4_sub<Real>(wR, wL, d);
+            v4_mul<Real>(s, Real(0.5), h);
+            v4_fma<Real>(d, Real(-0.5) * lam, h, F);
+        } else {
 #pragma unroll
-        for (int m = 0; m < 4; ++m) F[m] = Real(0.5) * (fL[m] + fR[m]) - Real(0.5) * lam * (wR[m] - wL[m]);
+            for (int m = 0; m < 4; ++m) F[m] = Real(0.5) * (fL[m] + fR[m]) - Real(0.5) * lam * (wR[m] - wL[m]);
+        }
     } else {
         Real sl = minR<Real>(uL - cL, uR - cR);
         Real sr = maxR<Real>(uL + cL, uR + cR);
