@@ -106,11 +106,19 @@ __device__ __forceinline__ bool resolve(int i, int n, int bc_lo, int bc_hi, int 
     return true;
 }
 
-template <class Real>
-__device__ __forceinline__ Real ld_state(const Real *__restrict__ uin, const Real *__restrict__ din, size_t idx) {
-    Real v = __ldg(uin + idx);
-    if (din != nullptr) v += __ldg(din + idx);
-    return v;
+// The 4 variables of one point (variable m at idx + m NP^2 plane) of a stage
+// input: uin, plus the increment din when there is one.
+template <class Real, int NP>
+__device__ __forceinline__ void ld_state4(const Real *__restrict__ uin, const Real *__restrict__ din, unsigned idx,
+                                          unsigned plane, Real (&v)[4]) {
+#pragma unroll
+    for (int m = 0; m < 4; ++m) v[m] = __ldg(uin + idx + plane * (NP * NP * m));
+    if (din != nullptr) {
+        Real d[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) d[m] = __ldg(din + idx + plane * (NP * NP * m));
+        v4_add<Real>(v, d, v);
+    }
 }
 
 // Shared-memory arrays keep the 4 conserved variables of a slot in 16-byte
@@ -211,13 +219,14 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                 for (int m = 0; m < 4; ++m) {
                     const unsigned idx = base + plane * (k + NP * NP * m);
                     if (MODE == MODE_FP32K && STAGE >= 2) {
-                        const Real h = __ldg(uin + idx), d = __ldg(din + idx);
-                        u[k][m] = h + d;
-                    } else {
-                        u[k][m] = ld_state(uin, din, idx);
+                        u[k][m] = __ldg(uin + idx);
+                        un[m] = __ldg(din + idx);
+                    } else { // FP64, and FP32K stages 0-1: no increment
+                        u[k][m] = __ldg(uin + idx);
                         if (MODE == MODE_FP64 && STAGE >= 2) un[m] = a.un[idx];
                     }
                 }
+                if (MODE == MODE_FP32K && STAGE >= 2) v4_add<Real>(u[k], un, u[k]); // u^n high part + increment
                 if (MODE == MODE_FP64 && STAGE >= 2) put4(&SST(0, ey, l, k, 0, ex), CS, un);
             }
         } else {
@@ -240,14 +249,10 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             int jo;
             if (resolve(jn, ny, a.bc[2], a.bc[3], jo)) {
                 const unsigned base = (unsigned)(i0 + hx) + (unsigned)nx * jo + plane * hk;
-                Real h[4];
+                Real v[NP][4], h[4];
 #pragma unroll
-                for (int m = 0; m < 4; ++m) {
-                    Real v[NP];
-#pragma unroll
-                    for (int l = 0; l < NP; ++l) v[l] = ld_state(uin, din, base + plane * (NP * (l + NP * m)));
-                    h[m] = dotw<Real, NP>(v, w);
-                }
+                for (int l = 0; l < NP; ++l) ld_state4<Real, NP>(uin, din, base + plane * (NP * l), plane, v[l]);
+                v4_dotw<Real, NP>(v, w, h);
                 put4(&SHY(side, hk, 0, hx), CS, h);
             } else {
                 const int s = side == 0 ? 2 : 3;
@@ -272,14 +277,10 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             int io;
             if (resolve(in_, nx, a.bc[0], a.bc[1], io)) {
                 const unsigned base = (unsigned)io + (unsigned)nx * (j0 + hy) + plane * (NP * hl);
-                Real h[4];
+                Real v[NP][4], h[4];
 #pragma unroll
-                for (int m = 0; m < 4; ++m) {
-                    Real v[NP];
-#pragma unroll
-                    for (int k = 0; k < NP; ++k) v[k] = ld_state(uin, din, base + plane * (k + NP * NP * m));
-                    h[m] = dotw<Real, NP>(v, w);
-                }
+                for (int k = 0; k < NP; ++k) ld_state4<Real, NP>(uin, din, base + plane * k, plane, v[k]);
+                v4_dotw<Real, NP>(v, w, h);
                 put4(&SHX(side, hy, hl, 0), CSX, h);
             } else {
                 Real h[4];

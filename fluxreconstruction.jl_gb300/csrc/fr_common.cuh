@@ -205,8 +205,18 @@ __device__ __forceinline__ void riemann2d(const Real (&wL)[4], const Real (&wR)[
             for (int m = 0; m < 4; ++m) F[m] = fR[m];
         } else {
             Real factor = recipR<Real>(sr - sl);
+            if constexpr (sizeof(Real) == 4) {
+                // factor (sr fL - sl fR + sl sr (wR - wL)), as fused pair operations
+                Real d[4], t[4];
+                v4_sub<Real>(wR, wL, d);
+                v4_mul<Real>(fL, sr, t);
+                v4_fma<Real>(fR, -sl, t, t);
+                v4_fma<Real>(d, sl * sr, t, t);
+                v4_mul<Real>(t, factor, F);
+            } else {
 #pragma unroll
-            for (int m = 0; m < 4; ++m) F[m] = factor * (sr * fL[m] - sl * fR[m] + sl * sr * (wR[m] - wL[m]));
+                for (int m = 0; m < 4; ++m) F[m] = factor * (sr * fL[m] - sl * fR[m] + sl * sr * (wR[m] - wL[m]));
+            }
         }
     }
 }
