@@ -38,12 +38,14 @@ template <> struct SumAcc<float> {
 };
 
 // Block (b, q) of a grid (eblocks, nq) reduces solution point q of the
-// elements [b chunk, (b + 1) chunk): the unweighted sums of the four
+// elements [b chunk, (b + 1) chunk) of a state in the 2D device layout (DEV)
+// or in the reference's u[i, j, k, l, m] (arrays a caller passes to the
+// allocation-free entry point): the unweighted sums of the four
 // conserved variables (scaled by the quadrature weight wp[q] in FP64 at the
 // end), the largest directional wave speed max(|u| + c, |v| + c) and the
 // largest CFL rate (|u| + c)/dx + (|v| + c)/dy.  The wave speeds are
 // evaluated in the state's precision.
-template <class Real>
+template <class Real, bool DEV>
 __global__ void __launch_bounds__(RED_THREADS) k_reduce2d_partial(const Real *__restrict__ u, const Real *__restrict__ lo,
                                                              size_t plane, int nq, const double *__restrict__ wp,
                                                              double gamma, double idx_, double idy_,
@@ -57,14 +59,23 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce2d_partial(const Real *__
     SumAcc<Real> acc[4];
     Real smax = Real(0), rmax = Real(0);
     for (size_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        const size_t t = e + plane * q;
-        Real w[4];
+        Real w[4], wl[4] = {Real(0), Real(0), Real(0), Real(0)};
+        if (DEV) {
+            const size_t at = frk::e2d_index(e, q, 0, plane);
+            frk::ldg4(u + at, w);
+            if (lo != nullptr) frk::ldg4(lo + at, wl);
+        } else {
+            const size_t t = e + plane * q;
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                w[m] = u[t + npts * m];
+                if (lo != nullptr) wl[m] = lo[t + npts * m];
+            }
+        }
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
-            const Real h = u[t + npts * m];
-            const Real l = lo != nullptr ? lo[t + npts * m] : Real(0);
-            acc[m].add(h, l);
-            w[m] = h + l;
+            acc[m].add(w[m], wl[m]);
+            w[m] += wl[m];
         }
         const Real rinv = frk::recipR<Real>(w[0]);
         const Real U = w[1] * rinv, V = w[2] * rinv;
@@ -134,10 +145,10 @@ int fr_launch_euler2d_reduce(frgpu_problem *p, const void *state, const void *lo
     const int nq = np * np;
     const dim3 grid(RED_BLOCKS / nq, nq);
     if (p->d.precision == FRGPU_FP64)
-        k_reduce2d_partial<double><<<grid, RED_THREADS, 0, p->stream>>>((const double *)state, (const double *)lo,
+        k_reduce2d_partial<double, true><<<grid, RED_THREADS, 0, p->stream>>>((const double *)state, (const double *)lo,
                                                                      plane, nq, wp, p->d.gamma, cfl_dx, cfl_dy, part);
     else
-        k_reduce2d_partial<float><<<grid, RED_THREADS, 0, p->stream>>>((const float *)state, (const float *)lo,
+        k_reduce2d_partial<float, true><<<grid, RED_THREADS, 0, p->stream>>>((const float *)state, (const float *)lo,
                                                                     plane, nq, wp, p->d.gamma, cfl_dx, cfl_dy, part);
     FR_CUDA(cudaGetLastError());
     k_reduce_final<<<1, 192, 0, p->stream>>>(part, (int)(grid.x * grid.y), fin);
@@ -241,10 +252,10 @@ extern "C" FRGPU_API int frgpu_reduce2d_noalloc(const void *d_state, const void 
     // contents never need clearing
     const dim3 grid((unsigned)eblocks, (unsigned)(np * np));
     if (precision == FRGPU_FP64)
-        k_reduce2d_partial<double><<<grid, RED_THREADS, 0, st>>>(
+        k_reduce2d_partial<double, false><<<grid, RED_THREADS, 0, st>>>(
             (const double *)d_state, (const double *)d_lo, plane, np * np, d_wp, gamma, 1.0 / dx, 1.0 / dy, part);
     else
-        k_reduce2d_partial<float><<<grid, RED_THREADS, 0, st>>>(
+        k_reduce2d_partial<float, false><<<grid, RED_THREADS, 0, st>>>(
             (const float *)d_state, (const float *)d_lo, plane, np * np, d_wp, gamma, 1.0 / dx, 1.0 / dy, part);
     FR_CUDA(cudaGetLastError());
     k_reduce_final_scaled<<<1, 192, 0, st>>>(part, (int)nblocks, dx * dy * 0.25, d_out);

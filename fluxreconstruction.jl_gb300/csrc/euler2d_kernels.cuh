@@ -106,17 +106,15 @@ __device__ __forceinline__ bool resolve(int i, int n, int bc_lo, int bc_hi, int 
     return true;
 }
 
-// The 4 variables of one point (variable m at idx + m NP^2 plane) of a stage
-// input: uin, plus the increment din when there is one.
-template <class Real, int NP>
-__device__ __forceinline__ void ld_state4(const Real *__restrict__ uin, const Real *__restrict__ din, unsigned idx,
-                                          unsigned plane, Real (&v)[4]) {
-#pragma unroll
-    for (int m = 0; m < 4; ++m) v[m] = __ldg(uin + idx + plane * (NP * NP * m));
+// The 4 variables of one point of a stage input (at offset `at` of the device
+// layout): uin, plus the increment din when there is one.
+template <class Real>
+__device__ __forceinline__ void ld_state4(const Real *__restrict__ uin, const Real *__restrict__ din, unsigned at,
+                                          Real (&v)[4]) {
+    ldg4(uin + at, v);
     if (din != nullptr) {
         Real d[4];
-#pragma unroll
-        for (int m = 0; m < 4; ++m) d[m] = __ldg(din + idx + plane * (NP * NP * m));
+        ldg4(din + at, d);
         v4_add<Real>(v, d, v);
     }
 }
@@ -207,27 +205,25 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
 
     // ---- phase A loads, issued before the halo so that both are in flight ----
     const int i = i0 + ex, j = j0 + ey;
+    const unsigned e = (unsigned)i + (unsigned)nx * j;
     Real u[NP][4];
     {
         const int l = ln;
         if (valid) {
-            const unsigned base = (unsigned)i + (unsigned)nx * j + plane * (NP * l);
 #pragma unroll
             for (int k = 0; k < NP; ++k) {
-                Real un[4];
-#pragma unroll
-                for (int m = 0; m < 4; ++m) {
-                    const unsigned idx = base + plane * (k + NP * NP * m);
-                    if (MODE == MODE_FP32K && STAGE >= 2) {
-                        u[k][m] = __ldg(uin + idx);
-                        un[m] = __ldg(din + idx);
-                    } else { // FP64, and FP32K stages 0-1: no increment
-                        u[k][m] = __ldg(uin + idx);
-                        if (MODE == MODE_FP64 && STAGE >= 2) un[m] = a.un[idx];
-                    }
+                const unsigned at = ((unsigned)(k + NP * l) * plane + e) * 4;
+                ldg4(uin + at, u[k]);
+                if (MODE == MODE_FP32K && STAGE >= 2) {
+                    Real d[4];
+                    ldg4(din + at, d);
+                    v4_add<Real>(u[k], d, u[k]); // u^n high part + increment
                 }
-                if (MODE == MODE_FP32K && STAGE >= 2) v4_add<Real>(u[k], un, u[k]); // u^n high part + increment
-                if (MODE == MODE_FP64 && STAGE >= 2) put4(&SST(0, ey, l, k, 0, ex), CS, un);
+                if (MODE == MODE_FP64 && STAGE >= 2) {
+                    Real un[4];
+                    ldg4(a.un + at, un);
+                    put4(&SST(0, ey, l, k, 0, ex), CS, un);
+                }
             }
         } else {
 #pragma unroll
@@ -248,10 +244,10 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             const Real *w = side == 0 ? op.lr : op.ll;
             int jo;
             if (resolve(jn, ny, a.bc[2], a.bc[3], jo)) {
-                const unsigned base = (unsigned)(i0 + hx) + (unsigned)nx * jo + plane * hk;
+                const unsigned en = (unsigned)(i0 + hx) + (unsigned)nx * jo;
                 Real v[NP][4], h[4];
 #pragma unroll
-                for (int l = 0; l < NP; ++l) ld_state4<Real, NP>(uin, din, base + plane * (NP * l), plane, v[l]);
+                for (int l = 0; l < NP; ++l) ld_state4(uin, din, ((unsigned)(hk + NP * l) * plane + en) * 4, v[l]);
                 v4_dotw<Real, NP>(v, w, h);
                 put4(&SHY(side, hk, 0, hx), CS, h);
             } else {
@@ -276,10 +272,10 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             const Real *w = side == 0 ? op.lr : op.ll;
             int io;
             if (resolve(in_, nx, a.bc[0], a.bc[1], io)) {
-                const unsigned base = (unsigned)io + (unsigned)nx * (j0 + hy) + plane * (NP * hl);
+                const unsigned en = (unsigned)io + (unsigned)nx * (j0 + hy);
                 Real v[NP][4], h[4];
 #pragma unroll
-                for (int k = 0; k < NP; ++k) ld_state4<Real, NP>(uin, din, base + plane * k, plane, v[k]);
+                for (int k = 0; k < NP; ++k) ld_state4(uin, din, ((unsigned)(k + NP * hl) * plane + en) * 4, v[k]);
                 v4_dotw<Real, NP>(v, w, h);
                 put4(&SHX(side, hy, hl, 0), CSX, h);
             } else {
@@ -374,14 +370,11 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
     // part and the increments were just read by the CTA's row threads and are
     // L2-resident already; prefetching them as well measured slower.)
     if (MODE == MODE_FP32K && STAGE == 3 && valid) {
-        const unsigned pb = (unsigned)i + (unsigned)nx * j + plane * ln;
 #pragma unroll
-        for (int m = 0; m < 4; ++m)
-#pragma unroll
-            for (int l = 0; l < NP; ++l) {
-                const unsigned idx = pb + plane * (NP * (l + NP * m));
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(a.ul + idx));
-            }
+        for (int l = 0; l < NP; ++l) {
+            const unsigned at = ((unsigned)(ln + NP * l) * plane + e) * 4;
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(a.ul + at));
+        }
     }
     {
         const int k = ln;
@@ -419,7 +412,6 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
     if (valid) {
         const int k = ln;
         const Real dt = (Real)(*a.dtp);
-        const unsigned base = (unsigned)i + (unsigned)nx * j + plane * k;
         Real chk[4] = {Real(0), Real(0), Real(0), Real(0)};
         Real FB[4], FT[4], bB[4], bT[4];
         get4(&SFY(ey, k, 0, ex), CS, FB);
@@ -434,15 +426,11 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             v4_add<Real>(r, ry[l], r);
             v4_fma<Real>(bB, op.dgl[l], r, r);
             v4_fma<Real>(bT, op.dgr[l], r, r);
-            unsigned idx[4];
-#pragma unroll
-            for (int m = 0; m < 4; ++m) idx[m] = base + plane * (NP * (l + NP * m));
+            const unsigned at = ((unsigned)(k + NP * l) * plane + e) * 4;
             if (STAGE == 0) {
 #pragma unroll
-                for (int m = 0; m < 4; ++m) {
-                    res[m] = -r[m];
-                    a.out[idx[m]] = res[m];
-                }
+                for (int m = 0; m < 4; ++m) res[m] = -r[m];
+                st4(a.out + at, res);
             } else if (MODE == MODE_FP64) {
                 Real ui4[4], un4[4];
                 get4(&SU(ey, l, k, 0, ex), CS, ui4);
@@ -457,8 +445,8 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                     } else {
                         res[m] = fmaR<Real>(Real(2) * dt, du, fmaR<Real>(Real(2), ui, un4[m])) * Real(1.0 / 3.0);
                     }
-                    a.out[idx[m]] = res[m];
                 }
+                st4(a.out + at, res);
             } else {
                 // FP32K: stage values are u^n + d; only increments are stored,
                 // and the step's total increment is added to u^n with a
@@ -468,31 +456,25 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                     v4_mul<Real>(r, -dt, res);
                 } else if (STAGE == 2) {
                     Real d1[4];
-#pragma unroll
-                    for (int m = 0; m < 4; ++m) d1[m] = __ldg(din + idx[m]);
+                    ldg4(din + at, d1);
                     v4_fma<Real>(r, -dt, d1, res);
                     v4_mul<Real>(res, Real(0.25), res);
                 } else {
-                    Real d2[4], hi[4], lo[4], y[4], e[4];
-#pragma unroll
-                    for (int m = 0; m < 4; ++m) {
-                        d2[m] = __ldg(din + idx[m]);
-                        hi[m] = __ldg(uin + idx[m]);
-                        lo[m] = a.ul[idx[m]];
-                    }
+                    Real d2[4], hi[4], lo[4], y[4], c[4];
+                    ldg4(din + at, d2);
+                    ldg4(uin + at, hi);
+                    ld4(a.ul + at, lo);
                     v4_fma<Real>(r, -dt, d2, y);
                     v4_mul<Real>(y, Real(2.0 / 3.0), y); // d3
                     v4_add<Real>(y, lo, y);               // y = d3 + lo
                     v4_add<Real>(hi, y, res);             // t = hi + y
-                    v4_sub<Real>(res, hi, e);
-                    v4_sub<Real>(y, e, lo);               // lo_new = y - (t - hi)
-#pragma unroll
-                    for (int m = 0; m < 4; ++m) a.ul[idx[m]] = lo[m];
+                    v4_sub<Real>(res, hi, c);
+                    v4_sub<Real>(y, c, lo);               // lo_new = y - (t - hi)
+                    st4(a.ul + at, lo);
                     // u is dead in FP32K phase D: with the fused indicator it now holds u^{n+1}
                     if (FUSE) put4(&SU(ey, l, k, 0, ex), CS, res);
                 }
-#pragma unroll
-                for (int m = 0; m < 4; ++m) a.out[idx[m]] = res[m];
+                st4(a.out + at, res);
             }
             v4_add<Real>(chk, res, chk); // NaN and Inf propagate into the check sums
         }

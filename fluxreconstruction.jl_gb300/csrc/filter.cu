@@ -26,6 +26,12 @@ __device__ __forceinline__ bool troubled_sigma(double Se, double S0, double kapp
     return sigma < 0.99;
 }
 
+// Offset of variable m at point q of element e: the 1D Euler layout
+// u[e, q, m] of the reference, or the 2D device layout.
+template <int N, bool ONE_D> __device__ __forceinline__ size_t sidx(size_t e, int q, int m, size_t ne) {
+    return ONE_D ? e + ne * ((size_t)q + (size_t)N * m) : e2d_index(e, q, m, ne);
+}
+
 template <class Real, int N, int NVAR, bool ONE_D>
 __global__ void __launch_bounds__(128) k_filter(Real *u, Real *lo, size_t ne, const Real *__restrict__ V,
                                                 const Real *__restrict__ iV, double lam, double S0, double kappa,
@@ -34,7 +40,7 @@ __global__ void __launch_bounds__(128) k_filter(Real *u, Real *lo, size_t ne, co
     if (e >= ne) return;
     Real x[N], h[N];
 #pragma unroll
-    for (int q = 0; q < N; ++q) x[q] = u[e + ne * q];
+    for (int q = 0; q < N; ++q) x[q] = u[sidx<N, ONE_D>(e, q, 0, ne)];
     Real tot = 0;
 #pragma unroll
     for (int a = 0; a < N; ++a) {
@@ -52,9 +58,8 @@ __global__ void __launch_bounds__(128) k_filter(Real *u, Real *lo, size_t ne, co
     atomicAdd(count, 1);
 #pragma unroll 1
     for (int m = 0; m < NVAR; ++m) {
-        Real *um = u + ne * (size_t)N * m;
 #pragma unroll
-        for (int q = 0; q < N; ++q) x[q] = um[e + ne * q];
+        for (int q = 0; q < N; ++q) x[q] = u[sidx<N, ONE_D>(e, q, m, ne)];
 #pragma unroll
         for (int a = 0; a < N; ++a) {
             Real s = iV[a] * x[0];
@@ -67,8 +72,8 @@ __global__ void __launch_bounds__(128) k_filter(Real *u, Real *lo, size_t ne, co
             Real s = V[a] * h[0];
 #pragma unroll
             for (int b = 1; b < N; ++b) s = fmaR<Real>(V[a + N * b], h[b], s);
-            um[e + ne * a] = s;
-            if (lo) lo[e + ne * (a + (size_t)N * m)] = Real(0);
+            u[sidx<N, ONE_D>(e, a, m, ne)] = s;
+            if (lo) lo[sidx<N, ONE_D>(e, a, m, ne)] = Real(0);
         }
     }
 }
@@ -118,10 +123,6 @@ int fr_launch_filter2d(frgpu_problem *p, int indicator, double lam, double S0, d
         return FRGPU_ERR_ARG;
     }
     if (indicator == FRGPU_IND_MLP) return fr_launch_mlp_indicator(p, lam, S0, kappa);
-    if (!p->d_V || !p->d_iV) {
-        fr_set_error("filter2d: the space has no Vandermonde matrices");
-        return FRGPU_ERR_ARG;
-    }
     return p->d.precision == FRGPU_FP64 ? filter2d_np<double>(p, lam, S0, kappa) : filter2d_np<float>(p, lam, S0, kappa);
 }
 

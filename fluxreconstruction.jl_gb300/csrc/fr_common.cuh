@@ -31,20 +31,42 @@ template <class Real> __device__ __forceinline__ Real sqrtP(Real a); // a >= 0
 template <> __device__ __forceinline__ double sqrtP<double>(double a) { return sqrt(a); }
 template <> __device__ __forceinline__ float sqrtP<float>(float a) { return a > 0.0f ? a * rsqrtf(a) : 0.0f; }
 
-// Global load that stays where it is written.  The stage updates read their
-// extra inputs (u^n, increments, low parts) only after the residual; plain
-// read-only loads there may be hoisted by the compiler across the block's
-// barriers to the kernel start, where they would hold registers through the
-// whole residual.
-__device__ __forceinline__ float ld_here(const float *p) {
-    float v;
-    asm volatile("ld.global.f32 %0, [%1];" : "=f"(v) : "l"(p));
-    return v;
+// Device layout of the 2D Euler state (both precisions): the 4 conserved
+// variables of one solution point are adjacent, and each point's plane keeps
+// the element index fastest:
+//     u[(q ne + e) 4 + m],  element e = i + nx j,  point q = k + np l,  variable m.
+// A thread reads or writes a whole point with one 16-byte access (FP32; two
+// in FP64), and 32 consecutive elements make one contiguous 512-byte (1 KB)
+// warp access.  The host arrays keep the reference's u[i, j, k, l, m];
+// transfer.cu converts.
+__host__ __device__ __forceinline__ size_t e2d_index(size_t e, int q, int m, size_t ne) {
+    return ((size_t)q * ne + e) * 4 + (size_t)m;
 }
-__device__ __forceinline__ double ld_here(const double *p) {
-    double v;
-    asm volatile("ld.global.f64 %0, [%1];" : "=d"(v) : "l"(p));
-    return v;
+
+// The 4 variables of one point: 16-byte vector loads (read-only path or
+// plain) and stores.
+__device__ __forceinline__ void ldg4(const float *p, float (&v)[4]) {
+    const float4 t = __ldg(reinterpret_cast<const float4 *>(p));
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+__device__ __forceinline__ void ldg4(const double *p, double (&v)[4]) {
+    const double2 a = __ldg(reinterpret_cast<const double2 *>(p)), b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+__device__ __forceinline__ void ld4(const float *p, float (&v)[4]) {
+    const float4 t = *reinterpret_cast<const float4 *>(p);
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+__device__ __forceinline__ void ld4(const double *p, double (&v)[4]) {
+    const double2 a = reinterpret_cast<const double2 *>(p)[0], b = reinterpret_cast<const double2 *>(p)[1];
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+__device__ __forceinline__ void st4(float *p, const float (&v)[4]) {
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void st4(double *p, const double (&v)[4]) {
+    reinterpret_cast<double2 *>(p)[0] = make_double2(v[0], v[1]);
+    reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
 }
 
 template <class Real> __device__ __forceinline__ Real absR(Real a) { return a < Real(0) ? -a : a; }

@@ -280,9 +280,10 @@ __device__ __forceinline__ void load_raw(const Real *__restrict__ u, size_t ne, 
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         if (valid) {
-            const size_t at = e + ne * (size_t)(q0 + k);
+            Real v[4];
+            frk::ld4(u + frk::e2d_index(e, q0 + k, 0, ne), v);
 #pragma unroll
-            for (int m = 0; m < 4; ++m) w[k][m] = (float)u[at + ne * 16 * (size_t)m];
+            for (int m = 0; m < 4; ++m) w[k][m] = (float)v[m];
         } else {
             w[k][0] = 1.f;
             w[k][1] = w[k][2] = w[k][3] = 0.f;

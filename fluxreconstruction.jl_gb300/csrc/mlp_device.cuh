@@ -264,8 +264,9 @@ __device__ __forceinline__ bool plain_troubled(float su, float S0, float kappa) 
 
 // :l2 modal filter of the elements ebase + b for the bits b set in todo (b < 16;
 // the same mask on every lane), one element at a time by the whole warp: lane =
-// 16 (variable pair) + mode a.  State u[e + ne q + 16 ne m] (np = 4, 4
-// variables); lo (FP32K low part, may be null) is cleared where u is filtered.
+// 16 (variable pair) + mode a.  State in the 2D device layout (np = 4, 16
+// points, 4 variables); lo (FP32K low part, may be null) is cleared where u is
+// filtered.
 // Every output is the same ascending FMA chain as the plain filter kernel's.
 template <class Real>
 __device__ __forceinline__ void warp_filter_elements(unsigned todo, size_t ebase, Real *u, Real *lo, size_t ne,
@@ -278,8 +279,8 @@ __device__ __forceinline__ void warp_filter_elements(unsigned todo, size_t ebase
         const size_t et = ebase + src;
         for (int mp = 0; mp < 4; mp += 2) {
             const int m = mp + (half >> 4);
-            Real *um = u + ne * 16 * (size_t)m;
-            const Real xa = um[et + ne * a];
+            const size_t at = frk::e2d_index(et, a, m, ne);
+            const Real xa = u[at];
             Real s = iV[a] * __shfl_sync(0xffffffffu, xa, half);
 #pragma unroll
             for (int b = 1; b < 16; ++b)
@@ -289,8 +290,8 @@ __device__ __forceinline__ void warp_filter_elements(unsigned todo, size_t ebase
 #pragma unroll
             for (int b = 1; b < 16; ++b)
                 r = frk::fmaR<Real>(V[a + 16 * b], __shfl_sync(0xffffffffu, ha, half + b), r);
-            um[et + ne * a] = r;
-            if (lo) lo[et + ne * (a + 16 * (size_t)m)] = Real(0);
+            u[at] = r;
+            if (lo) lo[at] = Real(0);
         }
     }
 }

@@ -3,25 +3,37 @@
 //
 // One cudaMemcpy moves the FP64 array into a device staging buffer; a kernel
 // then checks it for non-finite values, splits it into the FP32 high part and
-// the FP32 low part x - (double)hi (FP32K), and transposes the BGK layout
-// f[i, v, k] -> u[(i * np + k) * nvel + v].  Downloads run the reverse kernel
-// (hi + lo in FP64) and one cudaMemcpy back.  No per-element host loop.
+// the FP32 low part x - (double)hi (FP32K), and reorders the layouts that
+// differ on the device: BGK f[i, v, k] -> u[(i * np + k) * nvel + v], and the
+// 2D Euler u[i, j, k, l, m] -> the point-vector layout of e2d_index.
+// Downloads run the reverse kernel (hi + lo in FP64) and one cudaMemcpy back.
+// No per-element host loop.
 #include <string>
 
+#include "fr_common.cuh"
 #include "frgpu_internal.h"
 
 namespace {
 
+enum { LAYOUT_SAME = 0, LAYOUT_BGK = 1, LAYOUT_E2D = 2 };
+
 struct Layout {
-    int bgk;
+    int kind;
     long ne, nv, np;
 };
 
-// internal index of host index q (q = i + ne (v + nv k) for BGK, else the same)
+// device index of host index q: BGK q = i + ne (v + nv k); 2D Euler
+// q = e + ne (point + np^2 m); the other equations keep the host layout
 __device__ __forceinline__ long dev_index(const Layout &L, long q) {
-    if (!L.bgk) return q;
-    const long i = q % L.ne, r = q / L.ne, v = r % L.nv, k = r / L.nv;
-    return (i * L.np + k) * L.nv + v;
+    if (L.kind == LAYOUT_BGK) {
+        const long i = q % L.ne, r = q / L.ne, v = r % L.nv, k = r / L.nv;
+        return (i * L.np + k) * L.nv + v;
+    }
+    if (L.kind == LAYOUT_E2D) {
+        const long e = q % L.ne, r = q / L.ne, pt = r % (L.np * L.np), m = r / (L.np * L.np);
+        return (long)frk::e2d_index((size_t)e, (int)pt, (int)m, (size_t)L.ne);
+    }
+    return q;
 }
 
 template <class Real>
@@ -53,7 +65,9 @@ __global__ void k_download(const Real *__restrict__ hi, const Real *__restrict__
 }
 
 Layout layout_of(const frgpu_problem *p) {
-    Layout L{p->d.equation == FRGPU_BGK1D ? 1 : 0, p->sp.nx, p->d.nvel, p->sp.np};
+    const int kind = p->d.equation == FRGPU_BGK1D ? LAYOUT_BGK : (p->d.equation == FRGPU_EULER2D ? LAYOUT_E2D : LAYOUT_SAME);
+    const long ne = p->d.equation == FRGPU_EULER2D ? (long)p->sp.nx * p->sp.ny : (long)p->sp.nx;
+    Layout L{kind, ne, p->d.nvel, p->sp.np};
     return L;
 }
 

@@ -5,8 +5,8 @@
  * Plain C types only.  Every function returns an int status (FRGPU_OK = 0,
  * negative on error) and never aborts; frgpu_last_error() returns the message
  * of the calling thread's last failure.  Host arrays are borrowed for the
- * duration of a call.  All state arrays use the reference's Julia column-major
- * layouts, element index fastest:
+ * duration of a call.  All host state arrays use the reference's Julia
+ * column-major layouts, element index fastest:
  *   1D scalar      u[ne, np]                 (src/Equation/eq_advection.jl)
  *   1D Euler       u[ne, np, 3]              (src/Equation/eq_euler.jl)
  *   2D Euler       u[nx, ny, np, np, 4]      (example/shock-vortex.jl:26-118, interior only)
@@ -169,7 +169,11 @@ FRGPU_API int frgpu_troubled_flags(frgpu_problem *p, int *flags, long n);
 FRGPU_API int frgpu_problem_set_option(frgpu_problem *p, int option, int value);
 /* Device pointer to the primary state array and its element type size
  * (8 for FP64, 4 for FP32K), for zero-copy hand-off; the stream the problem's
- * kernels run on; the number of this library's kernel launches so far. */
+ * kernels run on; the number of this library's kernel launches so far.
+ * The device state keeps the host layout except for 2D Euler, whose device
+ * array holds the 4 conserved variables of each solution point together:
+ * value (i, j, k, l, m) of the host u[nx, ny, deg+1, deg+1, 4] sits at
+ * ((q * nx * ny) + i + nx * j) * 4 + m with q = k + (deg + 1) * l. */
 FRGPU_API int frgpu_problem_device_state(frgpu_problem *p, void **dptr, int *elem_bytes);
 FRGPU_API int frgpu_problem_stream(frgpu_problem *p, void **stream);
 FRGPU_API long frgpu_problem_launches(const frgpu_problem *p);

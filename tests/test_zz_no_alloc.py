@@ -34,7 +34,7 @@ def _problem(frgpu, nx, ny, deg, amp):
     itg = frgpu.init(prob, dt=1e-4)
     sums, speed = itg.reduce()
     rate = 0.1 / itg.cfl_dt(0.1)
-    return ps, prob, itg, sums, speed, rate
+    return ps, u, itg, sums, speed, rate
 
 
 def test_reduce2d_noalloc_matches_allocating_reduce(frgpu):
@@ -46,11 +46,11 @@ def test_reduce2d_noalloc_matches_allocating_reduce(frgpu):
     torch.cuda.set_device(0)
     cases = [_problem(frgpu, 96, 80, 3, 0.2), _problem(frgpu, 20, 12, 2, 0.3)]
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-    for ps, prob, itg, sums, speed, rate in cases:
+    for ps, u, itg, sums, speed, rate in cases:
         itg.synchronize()
-        ptr, eb = C.c_void_p(), C.c_int()
-        L.check(lib.frgpu_problem_device_state(prob._h, C.byref(ptr), C.byref(eb)))
-        assert eb.value == 8
+        # the caller's own device array in the reference layout u[i, j, k, l, m]
+        state = torch.tensor(np.asarray(u).ravel(order="F"), dtype=torch.float64, device="cuda")
+        ptr = C.c_void_p(state.data_ptr())
         wp = torch.tensor(np.asarray(ps.wp).ravel(order="F"), dtype=torch.float64, device="cuda")
         out = torch.full((6,), float("nan"), dtype=torch.float64, device="cuda")
         L.check(lib.frgpu_reduce2d_noalloc(ptr, None, L.FP64, ps.nx, ps.ny, ps.deg, ps.dx, ps.dy, 1.4,
@@ -70,3 +70,27 @@ def test_reduce2d_noalloc_rejects_meshes_beyond_its_scratch(frgpu):
     rc = lib.frgpu_reduce2d_noalloc(dummy, None, L.FP64, 8192, 8192, 3, 1e-4, 1e-4, 1.4, dummy, dummy, None)
     assert rc == L.ERR_ARG
     assert "exceed the maximum" in L.last_error()
+
+
+def test_device_state_has_the_documented_2d_layout(frgpu):
+    """frgpu_problem_device_state hands out the 2D Euler state in the device
+    layout include/frgpu.h documents: value (i, j, k, l, m) at
+    ((k + np l) nx ny + i + nx j) 4 + m."""
+    import torch
+
+    from frgpu import _lib as L
+
+    ps, u, itg, *_ = _problem(frgpu, 24, 10, 3, 0.2)
+    itg.synchronize()
+    ptr, eb = C.c_void_p(), C.c_int()
+    L.check(L.lib().frgpu_problem_device_state(itg.prob._h, C.byref(ptr), C.byref(eb)))
+    assert eb.value == 8
+    n = u.size
+
+    class _Dev:
+        __cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr.value, False), "version": 3}
+
+    dev = torch.as_tensor(_Dev(), device="cuda").cpu().numpy()
+    npp = ps.deg + 1
+    want = np.transpose(np.asarray(u).reshape(ps.nx, ps.ny, npp * npp, 4, order="F"), (2, 1, 0, 3)).ravel()
+    np.testing.assert_array_equal(dev, want)
