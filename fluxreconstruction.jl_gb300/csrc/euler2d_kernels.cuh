@@ -511,8 +511,7 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             }
             float feat[16], su = 0.f;
             features_from_raw(w, ev, pr, a.iv1, (float)a.gm1, feat, su);
-#pragma unroll
-            for (int q = 0; q < 16; ++q) xs[(lane & 15) * NIN + (pr ? 16 : 0) + q] = __float2bfloat16_rn(feat[q]);
+            store_features_bf16(xs + (lane & 15) * NIN + (pr ? 16 : 0), feat);
             __syncwarp();
             Fwd f;
             mlp_forward_tile(global_view(a.mlp), xs, f); // 12 KB of weights, L1-resident

@@ -358,8 +358,7 @@ __global__ void __launch_bounds__(32 * WARPS, 4) k_mlp_indicator(MLPDev w, Real 
             const size_t en = (tile + step) * 16 + (lane & 15);
             load_raw<Real>(u, ne, en, en < ne, pr, raw);
         }
-#pragma unroll
-        for (int a = 0; a < 16; ++a) xs[(lane & 15) * NIN + (pr ? 16 : 0) + a] = __float2bfloat16_rn(feat[a]);
+        store_features_bf16(xs + (lane & 15) * NIN + (pr ? 16 : 0), feat);
         __syncwarp();
         Fwd f;
         mlp_forward_tile(view, xs, f);

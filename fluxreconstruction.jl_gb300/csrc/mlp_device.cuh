@@ -75,6 +75,16 @@ __device__ __forceinline__ float gelu(float x) {
     const float t = tanh_fast(GELU_C * fmaf(GELU_A * x, x * x, x));
     return 0.5f * x * (1.0f + t);
 }
+// gelu of two values as packed FP32 pairs: per lane the same operations (and
+// roundings) as gelu(), half the arithmetic instructions
+__device__ __forceinline__ float2 gelu2(float x0, float x1) {
+    const float2 x = make_float2(x0, x1);
+    const float2 xx = __fmul2_rn(x, x);
+    const float2 ax = __fmul2_rn(make_float2(GELU_A, GELU_A), x);
+    const float2 z = __fmul2_rn(make_float2(GELU_C, GELU_C), __ffma2_rn(ax, xx, x));
+    const float2 t = make_float2(tanh_fast(z.x), tanh_fast(z.y));
+    return __fmul2_rn(__fmul2_rn(make_float2(0.5f, 0.5f), x), __fadd2_rn(make_float2(1.0f, 1.0f), t));
+}
 __device__ __forceinline__ float dgelu(float x) {
     const float t = tanh_fast(GELU_C * fmaf(GELU_A * x, x * x, x));
     return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * GELU_C * fmaf(3.0f * GELU_A, x * x, 1.0f);
@@ -125,10 +135,12 @@ __device__ __forceinline__ void mlp_forward_tile(const MLPView &w, const __nv_bf
     }
 #pragma unroll
     for (int kk = 0; kk < 4; ++kk) {
-        f.ah1[kk][0] = pack_bf16(gelu(f.a1[2 * kk][0]), gelu(f.a1[2 * kk][1]));
-        f.ah1[kk][1] = pack_bf16(gelu(f.a1[2 * kk][2]), gelu(f.a1[2 * kk][3]));
-        f.ah1[kk][2] = pack_bf16(gelu(f.a1[2 * kk + 1][0]), gelu(f.a1[2 * kk + 1][1]));
-        f.ah1[kk][3] = pack_bf16(gelu(f.a1[2 * kk + 1][2]), gelu(f.a1[2 * kk + 1][3]));
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float *a = f.a1[2 * kk + (q >> 1)] + 2 * (q & 1);
+            const float2 h = gelu2(a[0], a[1]);
+            f.ah1[kk][q] = pack_bf16(h.x, h.y);
+        }
     }
     float sg = 0.f, sg8 = 0.f;
 #pragma unroll
@@ -145,8 +157,9 @@ __device__ __forceinline__ void mlp_forward_tile(const MLPView &w, const __nv_bf
         mma16816(f.a2[j], f.ah1[2], b23.x, b23.y);
         mma16816(f.a2[j], f.ah1[3], b23.z, b23.w);
         const float w0 = w3[8 * j + 2 * t], w1 = w3[8 * j + 2 * t + 1];
-        sg = fmaf(gelu(f.a2[j][0]), w0, fmaf(gelu(f.a2[j][1]), w1, sg));
-        sg8 = fmaf(gelu(f.a2[j][2]), w0, fmaf(gelu(f.a2[j][3]), w1, sg8));
+        const float2 h01 = gelu2(f.a2[j][0], f.a2[j][1]), h23 = gelu2(f.a2[j][2], f.a2[j][3]);
+        sg = fmaf(h01.x, w0, fmaf(h01.y, w1, sg));
+        sg8 = fmaf(h23.x, w0, fmaf(h23.y, w1, sg8));
     }
     sg += __shfl_xor_sync(0xffffffffu, sg, 1);
     sg += __shfl_xor_sync(0xffffffffu, sg, 2);
@@ -155,6 +168,17 @@ __device__ __forceinline__ void mlp_forward_tile(const MLPView &w, const __nv_bf
     const float b3 = *w.b3;
     f.logit_g = sg + b3;
     f.logit_g8 = sg8 + b3;
+}
+
+// The 16 features of one lane as BF16 into row (16 values, 16-byte aligned)
+// of a tile's feature matrix: two 128-bit shared-memory stores.
+__device__ __forceinline__ void store_features_bf16(__nv_bfloat16 *row, const float (&feat)[16]) {
+    uint4 *d = reinterpret_cast<uint4 *>(row);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const float *f = feat + 8 * h;
+        d[h] = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
+    }
 }
 
 __device__ __forceinline__ float sigmoidf_(float z) { return 1.0f / (1.0f + expf(-z)); }
