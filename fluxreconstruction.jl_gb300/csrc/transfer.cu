@@ -22,16 +22,12 @@ struct Layout {
     long ne, nv, np;
 };
 
-// device index of host index q: BGK q = i + ne (v + nv k); 2D Euler
-// q = e + ne (point + np^2 m); the other equations keep the host layout
+// device index of host index q (BGK q = i + ne (v + nv k)); the 1D equations
+// keep the host layout, and 2D Euler has kernels of its own below
 __device__ __forceinline__ long dev_index(const Layout &L, long q) {
     if (L.kind == LAYOUT_BGK) {
         const long i = q % L.ne, r = q / L.ne, v = r % L.nv, k = r / L.nv;
         return (i * L.np + k) * L.nv + v;
-    }
-    if (L.kind == LAYOUT_E2D) {
-        const long e = q % L.ne, r = q / L.ne, pt = r % (L.np * L.np), m = r / (L.np * L.np);
-        return (long)frk::e2d_index((size_t)e, (int)pt, (int)m, (size_t)L.ne);
     }
     return q;
 }
@@ -51,6 +47,41 @@ __global__ void k_upload(const double *__restrict__ src, Real *__restrict__ hi, 
             if (lo) lo[d] = (float)(x - (double)h);
         }
     }
+}
+
+// 2D Euler: one thread per (element, point) moves the point's 4 variables: 4
+// coalesced FP64 reads of the host-order planes, one vector store per output.
+// Grid (element blocks, points).
+template <class Real>
+__global__ void k_upload_e2d(const double *__restrict__ src, Real *__restrict__ hi, Real *__restrict__ lo, long ne,
+                             long nq, unsigned long long *__restrict__ first_bad) {
+    const long e = blockIdx.x * (long)blockDim.x + threadIdx.x, pt = blockIdx.y;
+    if (e >= ne) return;
+    Real h[4], l[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        const long s = e + ne * (pt + nq * m);
+        const double x = src[s];
+        if (!isfinite(x)) atomicMin(first_bad, (unsigned long long)s);
+        h[m] = (Real)x;
+        l[m] = (Real)(x - (double)h[m]);
+    }
+    const size_t at = frk::e2d_index((size_t)e, (int)pt, 0, (size_t)ne);
+    frk::st4(hi + at, h);
+    if (sizeof(Real) == 4 && lo) frk::st4(lo + at, l);
+}
+
+template <class Real>
+__global__ void k_download_e2d(const Real *__restrict__ hi, const Real *__restrict__ lo, double *__restrict__ dst,
+                               long ne, long nq) {
+    const long e = blockIdx.x * (long)blockDim.x + threadIdx.x, pt = blockIdx.y;
+    if (e >= ne) return;
+    const size_t at = frk::e2d_index((size_t)e, (int)pt, 0, (size_t)ne);
+    Real h[4], l[4] = {Real(0), Real(0), Real(0), Real(0)};
+    frk::ldg4(hi + at, h);
+    if (lo) frk::ldg4(lo + at, l);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) dst[e + ne * (pt + nq * m)] = (double)h[m] + (double)l[m];
 }
 
 template <class Real>
@@ -96,7 +127,14 @@ int fr_put_state(frgpu_problem *p, const double *u, void *hi, void *lo) {
     FR_CUDA(cudaMemcpyAsync(stage, u, sizeof(double) * (size_t)p->ndof, cudaMemcpyHostToDevice, p->stream));
     FR_CUDA(cudaMemcpyAsync(first_bad, &none, sizeof(none), cudaMemcpyHostToDevice, p->stream));
     const Layout L = layout_of(p);
-    if (p->esize == 8)
+    if (L.kind == LAYOUT_E2D) {
+        const long nq = L.np * L.np;
+        const dim3 grid((unsigned)((L.ne + 255) / 256), (unsigned)nq);
+        if (p->esize == 8)
+            k_upload_e2d<double><<<grid, 256, 0, p->stream>>>(stage, (double *)hi, nullptr, L.ne, nq, first_bad);
+        else
+            k_upload_e2d<float><<<grid, 256, 0, p->stream>>>(stage, (float *)hi, (float *)lo, L.ne, nq, first_bad);
+    } else if (p->esize == 8)
         k_upload<double><<<grid_for(p->ndof), 256, 0, p->stream>>>(stage, (double *)hi, nullptr, p->ndof, L,
                                                                      first_bad);
     else
@@ -119,7 +157,14 @@ int fr_get_state(frgpu_problem *p, const void *hi, const void *lo, double *u) {
     if (rc) return rc;
     double *stage = (double *)p->d_stage;
     const Layout L = layout_of(p);
-    if (p->esize == 8)
+    if (L.kind == LAYOUT_E2D) {
+        const long nq = L.np * L.np;
+        const dim3 grid((unsigned)((L.ne + 255) / 256), (unsigned)nq);
+        if (p->esize == 8)
+            k_download_e2d<double><<<grid, 256, 0, p->stream>>>((const double *)hi, nullptr, stage, L.ne, nq);
+        else
+            k_download_e2d<float><<<grid, 256, 0, p->stream>>>((const float *)hi, (const float *)lo, stage, L.ne, nq);
+    } else if (p->esize == 8)
         k_download<double><<<grid_for(p->ndof), 256, 0, p->stream>>>((const double *)hi, nullptr, stage, p->ndof, L);
     else
         k_download<float><<<grid_for(p->ndof), 256, 0, p->stream>>>((const float *)hi, (const float *)lo, stage,

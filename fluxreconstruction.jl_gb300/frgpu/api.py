@@ -384,6 +384,15 @@ class Integrator:
         check(L.lib().frgpu_state_download(self.prob._h, dptr(out)))
         return out
 
+    def read_u(self, out: np.ndarray) -> np.ndarray:
+        """Download the state into a caller-owned FP64 array of the host layout
+        (for example page-locked memory, which the copy engine reads and
+        writes directly)."""
+        if out.shape != self.prob.shape or out.dtype != np.float64 or not out.flags.f_contiguous:
+            raise ValueError("read_u needs an F-contiguous float64 array of the state's shape")
+        check(L.lib().frgpu_state_download(self.prob._h, dptr(out)))
+        return out
+
     @u.setter
     def u(self, value) -> None:
         v = _f64(value)
