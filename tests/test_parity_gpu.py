@@ -398,3 +398,30 @@ def test_nonfinite_and_unphysical_states_are_reported(frgpu):
     with pytest.raises(frgpu.FRGPUError) as e:
         itg.step(1, dt=-1.0)
     assert e.value.code == -5
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32k"])
+@pytest.mark.parametrize("nx,ny,deg", [(37, 5, 2), (33, 3, 3), (1, 1, 3)])
+def test_euler2d_state_transfer_round_trip(frgpu, precision, nx, ny, deg):
+    """Host u[i, j, k, l, m] -> the point-vector device layout -> host: exact in
+    FP64; in FP32K the high + low pair returns every value to within 2^-46 of
+    itself.  A non-finite value is reported by its host index."""
+    ps = frgpu.FRPSpace2D(0, 1, nx, 0, 1, ny, deg)
+    rng = np.random.default_rng(7)
+    u = np.asfortranarray(rng.uniform(0.5, 2.0, size=(nx, ny, deg + 1, deg + 1, 4)))
+    prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf", precision=precision)
+    itg = frgpu.init(prob, dt=1e-4)
+    back = itg.u
+    if precision == "fp64":
+        assert np.array_equal(back, u)
+    else:
+        assert np.max(np.abs(back - u) / np.abs(u)) <= 2.0 ** -46
+    out = np.asfortranarray(np.zeros_like(u))
+    assert np.array_equal(itg.read_u(out), back)
+    bad = u.copy(order="F")
+    bad[nx - 1, ny - 1, deg, 0, 2] = np.inf
+    with pytest.raises(frgpu.FRGPUError) as e:
+        itg.u = bad
+    assert e.value.code == -3
+    flat = np.ravel_multi_index((nx - 1, ny - 1, deg, 0, 2), u.shape, order="F")
+    assert f"index {flat}" in str(e.value)
