@@ -368,6 +368,20 @@ def shock_vortex_entry(steps=100, warmup=5):
             itg.step(50)
         finals[form] = itg.u[..., 0]
         out[form] = rec
+    # the learned form with the positivity-preserving limiter before every step,
+    # the full loop of example/shock-vortex.jl:297-321 (limiter, step, filter)
+    prob = learned.shock_vortex_problem(ps, 0.25, precision="fp32k")
+    itg = frgpu.init(prob, dt=dt)
+    frgpu._lib.check(frgpu.lib().frgpu_problem_set_mlp(prob._h, net._h, 0.5, 0.0))
+    itg.set_filter("mlp", learned.FILTER_LAMBDA, S0, learned.FILTER_KAPPA)
+    nlim = itg.positive_limiter()
+    itg.set_limiter(True)
+    timer = _event_timer(torch.cuda.ExternalStream(itg.stream()))
+    itg.step(warmup)
+    itg.synchronize()
+    secs = timer(lambda: itg.step(steps))
+    out["learned_fp32k_with_limiter"] = {"value": ndof * 3 * steps / secs, "ms_per_step": secs / steps * 1e3,
+                                         "limited_elements_at_start": nlim}
     ref = finals["plain_fp64"]
     for form in ("learned_fp32k", "plain_fp32k"):
         out[form]["rms_rho_diff_vs_plain_fp64"] = float(np.sqrt(np.mean((finals[form] - ref) ** 2)))

@@ -36,7 +36,7 @@ struct frgpu_problem {
     int *d_status = nullptr; // accumulated status bits
     double *d_red = nullptr; // reduction scratch
     int *d_flags = nullptr;  // troubled flags per element
-    int *d_count = nullptr;  // troubled count
+    int *d_count = nullptr;  // counters: [0..2] indicator (troubled, misfires, fallbacks), [FR_COUNT_LIMITER]
     void *d_velo = nullptr, *d_w = nullptr; // BGK velocity grid (state precision)
     void *d_J = nullptr;                    // 1D per-element Jacobian (state precision)
     void *d_V = nullptr, *d_iV = nullptr;   // Vandermonde matrix / inverse (state precision)
@@ -51,6 +51,9 @@ struct frgpu_problem {
     float mlp_thr = 0.5f, mlp_band = 0.0f;
     int bgk_tensor = 1;             // FP32 BGK transport on the tensor cores
     int fuse_indicator = 1;         // FP32K 2D: learned indicator inside stage 3
+    int limiter = 0;                // positivity-preserving limiter before every step
+    double lim_t0 = 1.0;            // its t0 (cap of the energy scaling)
+    std::vector<double> lim_w;      // its element weights
     float *d_bgk_prim = nullptr;    // FP32 BGK: (rho, U, lambda) per (element, point), from the moments
     uint32_t *d_bgk_frag = nullptr; // FP32 BGK: TF32 A fragments of the transport operator (both signs, split)
     // captured step graph
@@ -61,6 +64,7 @@ struct frgpu_problem {
     long launches = 0;
 };
 
+constexpr int FR_NCOUNT = 8, FR_COUNT_LIMITER = 4; // d_count entries
 constexpr int FR_RED_BLOCKS = 608; // reduction partial blocks (4 x 152 SMs)
 // d_red layout: [FR_RED_BLOCKS*6 partials][8 final][64 quadrature weights]
 constexpr int FR_RED_FINAL = FR_RED_BLOCKS * 6;
@@ -130,3 +134,6 @@ void fr_iv1_from_tensor(const frgpu_space &s, float *iv1);
 // deg 3, learned indicator bound and selected, fusion not switched off)?
 bool fr_fused_indicator(const frgpu_problem *p);
 int fr_launch_mlp_indicator(frgpu_problem *p, double lam, double S0, double kappa);
+// positivity-preserving limiter (limiter.cu)
+int fr_launch_limiter(frgpu_problem *p, const std::vector<double> &w, double t0);
+int fr_limiter_weights(const frgpu_problem *p, const double *weights, std::vector<double> &w);

@@ -341,9 +341,11 @@ static int launch_stage(frgpu_problem *p, int stage, const void *in, const void 
     return FRGPU_ERR_ARG;
 }
 
-// One SSPRK3 step (+ filter) on the current buffers.
+// One SSPRK3 step (limiter before it, filter after it, the order of the loop
+// of example/shock-vortex.jl:297-321) on the current buffers.
 static int enqueue_step(frgpu_problem *p) {
     int rc;
+    if (p->limiter && (rc = fr_launch_limiter(p, p->lim_w, p->lim_t0))) return rc;
     if (p->d.precision == FRGPU_FP64) {
         if ((rc = launch_stage(p, 1, p->s0, nullptr, p->s1))) return rc;
         if ((rc = launch_stage(p, 2, p->s1, nullptr, p->s2))) return rc;
@@ -496,8 +498,8 @@ FRGPU_API int frgpu_problem_create(const frgpu_space *s, const frgpu_problem_des
             const size_t ne = (size_t)s->nx * s->ny;
             FR_CUDA(cudaMalloc(&p->d_flags, sizeof(int) * ne));
             FR_CUDA(cudaMemset(p->d_flags, 0, sizeof(int) * ne));
-            FR_CUDA(cudaMalloc(&p->d_count, sizeof(int) * 4));
-            FR_CUDA(cudaMemset(p->d_count, 0, sizeof(int) * 4));
+            FR_CUDA(cudaMalloc(&p->d_count, sizeof(int) * FR_NCOUNT));
+            FR_CUDA(cudaMemset(p->d_count, 0, sizeof(int) * FR_NCOUNT));
             if (!s->wp.empty())
                 FR_CUDA(cudaMemcpy(p->d_red + FR_RED_WP, s->wp.data(), sizeof(double) * s->wp.size(),
                                    cudaMemcpyHostToDevice));
@@ -688,6 +690,38 @@ FRGPU_API int frgpu_modal_filter(frgpu_problem *p, int indicator, double lam, do
     FR_CUDA(cudaStreamSynchronize(p->stream));
     return check_status(p);
     FR_CATCH
+}
+
+FRGPU_API int frgpu_positive_limiter(frgpu_problem *p, const double *weights, double t0, int *nlimited) {
+    FR_REQ(p, "positive_limiter: null problem");
+    FR_REQ(t0 > 0.0 && t0 <= 1.0, "positive_limiter: need 0 < t0 <= 1");
+    FR_TRY
+    std::vector<double> w;
+    int rc = fr_limiter_weights(p, weights, w);
+    if (rc) return rc;
+    if ((rc = fr_launch_limiter(p, w, t0))) return rc;
+    int n = 0;
+    FR_CUDA(cudaMemcpyAsync(&n, p->d_count + FR_COUNT_LIMITER, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+    FR_CUDA(cudaStreamSynchronize(p->stream));
+    if (nlimited) *nlimited = n;
+    return check_status(p);
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_set_limiter(frgpu_problem *p, int on, const double *weights, double t0) {
+    FR_REQ(p, "set_limiter: null problem");
+    FR_REQ(p->d.equation != FRGPU_BGK1D, "set_limiter: not defined for the kinetic equation");
+    FR_REQ(!on || (t0 > 0.0 && t0 <= 1.0), "set_limiter: need 0 < t0 <= 1");
+    if (on) {
+        std::vector<double> w;
+        const int rc = fr_limiter_weights(p, weights, w);
+        if (rc) return rc;
+        p->lim_w = w;
+        p->lim_t0 = t0;
+    }
+    p->limiter = on != 0;
+    p->graph_ind = -2; // force a re-capture
+    return FRGPU_OK;
 }
 
 FRGPU_API int frgpu_problem_set_mlp(frgpu_problem *p, const frgpu_mlp *m, double threshold, double band) {

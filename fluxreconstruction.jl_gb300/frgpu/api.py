@@ -421,6 +421,21 @@ class Integrator:
                                          C.byref(n)))
         return n.value
 
+    def positive_limiter(self, weights=None, t0: float = 1.0) -> int:
+        """positive_limiter (src/dissipation.jl:38-216) on every element, once
+        now; returns the number of elements it scaled.  weights: element
+        quadrature weights (Euler forms: summing to 1), default the space's
+        Gauss weights so normalised."""
+        n = C.c_int(0)
+        w = None if weights is None else _f64(np.asarray(weights).ravel(order="F"))
+        check(L.lib().frgpu_positive_limiter(self.prob._h, None if w is None else dptr(w), float(t0), C.byref(n)))
+        return n.value
+
+    def set_limiter(self, on: bool = True, weights=None, t0: float = 1.0) -> None:
+        """Run the limiter before every step (example/shock-vortex.jl:297-303)."""
+        w = None if weights is None else _f64(np.asarray(weights).ravel(order="F"))
+        check(L.lib().frgpu_set_limiter(self.prob._h, int(bool(on)), None if w is None else dptr(w), float(t0)))
+
     def troubled(self) -> np.ndarray:
         sp = self.prob.space
         ne = sp.nx * getattr(sp, "ny", 1)

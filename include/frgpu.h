@@ -158,6 +158,21 @@ FRGPU_API int frgpu_set_filter(frgpu_problem *p, int indicator, double lam, doub
 /* Apply the indicator + filter once now; *ntroubled receives the troubled-element count. */
 FRGPU_API int frgpu_modal_filter(frgpu_problem *p, int indicator, double lam, double S0, double kappa,
                                  int *ntroubled);
+/* positive_limiter(u, γ, weights, ll, lr, t0) (src/dissipation.jl:38-216) on
+ * every element of the device state, once now: the scalar form for advection
+ * and Burgers, the 1D and 2D Euler forms with the density and energy
+ * correctors.  weights: the element quadrature weights (np values in 1D, np^2
+ * in 2D, q = k + np l; the Euler forms expect them to sum to 1, as
+ * example/shock-vortex.jl:301 passes ps.wp ./ 4), or NULL for the space's
+ * Gauss weights so normalised.  t0 in (0, 1] caps the energy scaling.
+ * *nlimited receives the number of elements scaled with a parameter below 1.
+ * FRGPU_ERR_UNPHYSICAL when an element's density parameter leaves (0, 1] (the
+ * reference's assertion).  Closed-form energy parameter and min(t_j, t0):
+ * see csrc/limiter.cu. */
+FRGPU_API int frgpu_positive_limiter(frgpu_problem *p, const double *weights, double t0, int *nlimited);
+/* Run the limiter before every step of frgpu_step_ssprk3 (the loop of
+ * example/shock-vortex.jl:297-303); on = 0 turns it off. */
+FRGPU_API int frgpu_set_limiter(frgpu_problem *p, int on, const double *weights, double t0);
 /* Per-element troubled flags of the last filter application (ne ints). */
 FRGPU_API int frgpu_troubled_flags(frgpu_problem *p, int *flags, long n);
 /* Kernel choices for measurements; no counterpart in the reference.

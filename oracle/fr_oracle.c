@@ -898,6 +898,185 @@ int fro_filter1d(const fro_cfg *c, double *u, int nvar, const double *V, const d
     return count;
 }
 
+/* ------------------------------------------------------------------------
+ * Positivity-preserving limiter, src/dissipation.jl:38-216 (Vandenhoeck & Lani
+ * 2019).  Per element: the weighted mean u_mean (weights summing to 1), the
+ * face traces, eps = min(1e-13, rho_mean, p_mean), the density scaling
+ * t1 = min((rho_mean - eps) / (rho_mean - rho_min + 1e-8), 1) over the solution
+ * and face points, applied to the density; then for every face point (from
+ * the state before the density scaling, as the reference does) and every
+ * solution point whose lambda = rho / (2 p) falls below eps, the t at which
+ * p(t (u - u_mean) + u_mean) = eps, and all variables scaled by
+ * t2 = min(t_j, t0).  The reference takes min(tj, t0) with a call that throws
+ * whenever any t_j exists; this restatement defines it as the minimum, and
+ * solves p(t) = eps in closed form (p rho is quadratic in t) instead of the
+ * reference's Newton iteration from t = 1: the root in [0, 1] nearest to 1.
+ * Every dot product is the fma chain of dotw.  Return value: 1 when the
+ * element was scaled with t1 < 1 or t2 < 1, 0 otherwise, -1 when t1 left
+ * (0, 1] (the reference's assertion).
+ * ---------------------------------------------------------------------- */
+
+/* root in [0, 1] nearest to 1 of a t^2 + b t + c (c >= 0 at t = 0); 1 if none */
+static double limiter_root(double a, double b, double c) {
+    double r = 1.0;
+    if (fabs(a) <= 1e-300) {
+        if (b != 0.0) r = -c / b;
+    } else {
+        const double disc = b * b - 4.0 * a * c;
+        if (disc >= 0.0) {
+            const double q = -0.5 * (b + copysign(sqrt(disc), b));
+            const double r1 = q / a, r2 = q != 0.0 ? c / q : r1;
+            const int ok1 = r1 >= 0.0 && r1 <= 1.0, ok2 = r2 >= 0.0 && r2 <= 1.0;
+            if (ok1 && ok2) r = r1 > r2 ? r1 : r2;
+            else if (ok1) r = r1;
+            else if (ok2) r = r2;
+        }
+    }
+    return r < 0.0 ? 0.0 : (r > 1.0 ? 1.0 : r);
+}
+
+/* t with p(t) = eps on the segment from the mean um to the state w (nv = 3:
+ * 1D, nv = 4: 2D): (g - 1)(2 E rho - |m|^2) - 2 eps rho = a t^2 + b t + c */
+static double limiter_t(const double *w, const double *um, int nv, double g, double eps) {
+    const double gm1 = g - 1.0;
+    const int ie = nv - 1;
+    const double dr = w[0] - um[0], de = w[ie] - um[ie];
+    double dm2 = 0.0, mdm = 0.0, mm = 0.0;
+    for (int v = 1; v < ie; ++v) {
+        const double dm = w[v] - um[v];
+        dm2 = fma(dm, dm, dm2);
+        mdm = fma(um[v], dm, mdm);
+        mm = fma(um[v], um[v], mm);
+    }
+    const double a = gm1 * (2.0 * de * dr - dm2);
+    const double b = gm1 * (2.0 * (um[ie] * dr + de * um[0]) - 2.0 * mdm) - 2.0 * eps * dr;
+    const double c = gm1 * (2.0 * um[ie] * um[0] - mm) - 2.0 * eps * um[0];
+    return limiter_root(a, b, c);
+}
+
+/* lambda = rho / (2 p) of a conserved state (nv = 3 or 4), conserve_prim's last entry */
+static double limiter_lambda(const double *w, int nv, double g) {
+    double kin = 0.0;
+    for (int v = 1; v < nv - 1; ++v) kin = fma(w[v], w[v], kin);
+    return 0.5 * w[0] / (g - 1.0) / (w[nv - 1] - 0.5 * kin / w[0]);
+}
+
+/* One Euler element: value (q, v) at u[q * sq + v * sv], nq points with weights
+ * wq; nface face points whose traces are the dot products of the state along
+ * the face lines: face point f takes the np values u[fb[f] + r * fs[f]] with
+ * weights fw[f][r]. */
+static int limit_euler_element(double *u, long sq, long sv, int nq, int nv, const double *wq, int nface,
+                               const long *fb, const long *fs, const double *const *fw, int np, double g, double t0) {
+    double um[4], wb[24][4];
+    for (int v = 0; v < nv; ++v) um[v] = dotw(u + v * sv, sq, wq, 1, nq);
+    double lm = limiter_lambda(um, nv, g);
+    const double pm = 0.5 * um[0] * (1.0 / lm);
+    double eps = 1e-13;
+    if (um[0] < eps) eps = um[0];
+    if (pm < eps) eps = pm;
+    double rmin = INFINITY;
+    for (int f = 0; f < nface; ++f) {
+        for (int v = 0; v < nv; ++v) wb[f][v] = dotw(u + fb[f] + v * sv, fs[f], fw[f], 1, np);
+        if (wb[f][0] < rmin) rmin = wb[f][0];
+    }
+    for (int q = 0; q < nq; ++q)
+        if (u[q * sq] < rmin) rmin = u[q * sq];
+    double t1 = (um[0] - eps) / (um[0] - rmin + 1e-8);
+    if (t1 > 1.0) t1 = 1.0;
+    if (!(t1 > 0.0)) return -1;
+    for (int q = 0; q < nq; ++q) u[q * sq] = t1 * (u[q * sq] - um[0]) + um[0];
+    double t2 = t0;
+    int found = 0;
+    for (int f = 0; f < nface; ++f)
+        if (limiter_lambda(wb[f], nv, g) < eps) {
+            const double t = limiter_t(wb[f], um, nv, g, eps);
+            if (t < t2) t2 = t;
+            found = 1;
+        }
+    for (int q = 0; q < nq; ++q) {
+        double w[4];
+        for (int v = 0; v < nv; ++v) w[v] = u[q * sq + v * sv];
+        if (limiter_lambda(w, nv, g) < eps) {
+            const double t = limiter_t(w, um, nv, g, eps);
+            if (t < t2) t2 = t;
+            found = 1;
+        }
+    }
+    if (found)
+        for (int v = 0; v < nv; ++v)
+            for (int q = 0; q < nq; ++q) u[q * sq + v * sv] = t2 * (u[q * sq + v * sv] - um[v]) + um[v];
+    return (t1 < 1.0 || (found && t2 < 1.0)) ? 1 : 0;
+}
+
+int fro_positive_limiter2d(const fro_cfg *c, double *u, const double *w, double t0) {
+    const int np = c->np, nq = np * np;
+    const long nn = (long)c->nx * c->ny;
+    int count = 0, bad = 0;
+#ifdef _OPENMP
+#pragma omp parallel for OMP_THREADS reduction(+ : count, bad) schedule(static)
+#endif
+    for (long e = 0; e < nn; ++e) {
+        /* face points, in the reference's order (dissipation.jl:143-161):
+         * bottom (column j along s, ll), right (row j along r, lr), top
+         * (column j, lr), left (row j, ll) for j = 0..np-1 */
+        long fb[24], fs[24];
+        const double *fw[24];
+        int f = 0;
+        for (int j = 0; j < np; ++j) {
+            fb[f] = nn * j; fs[f] = nn * np; fw[f++] = c->ll;
+            fb[f] = nn * (np * j); fs[f] = nn; fw[f++] = c->lr;
+            fb[f] = nn * j; fs[f] = nn * np; fw[f++] = c->lr;
+            fb[f] = nn * (np * j); fs[f] = nn; fw[f++] = c->ll;
+        }
+        const int r = limit_euler_element(u + e, nn, nn * nq, nq, 4, w, f, fb, fs, fw, np, c->gamma, t0);
+        if (r < 0) ++bad;
+        else count += r;
+    }
+    return bad ? -bad : count;
+}
+
+int fro_positive_limiter1d(const fro_cfg *c, double *u, const double *w, double t0) {
+    const int np = c->np, ne = c->nx;
+    int count = 0, bad = 0;
+    for (int i = 0; i < ne; ++i) {
+        long fb[2] = {0, 0}, fs[2] = {ne, ne};
+        const double *fw[2] = {c->ll, c->lr};
+        const int r = limit_euler_element(u + i, ne, (long)ne * np, np, 3, w, 2, fb, fs, fw, np, c->gamma, t0);
+        if (r < 0) ++bad;
+        else count += r;
+    }
+    return bad ? -bad : count;
+}
+
+/* scalar form, dissipation.jl:38-58: mean = sum(u w) / sum(w), theta over the
+ * two face traces and the solution points */
+int fro_positive_limiter_scalar(const fro_cfg *c, double *u, const double *w, double t0) {
+    (void)t0; /* the reference's scalar form accepts t0 and does not use it */
+    const int np = c->np, ne = c->nx;
+    int count = 0, bad = 0;
+    double sw = w[0];
+    for (int q = 1; q < np; ++q) sw += w[q];
+    for (int i = 0; i < ne; ++i) {
+        double *ue = u + i;
+        const double um = dotw(ue, ne, w, 1, np) / sw;
+        const double ub0 = dotw(ue, ne, c->ll, 1, np), ub1 = dotw(ue, ne, c->lr, 1, np);
+        double eps = 1e-13;
+        if (um < eps) eps = um;
+        double th = ub0 < ub1 ? ub0 : ub1;
+        for (int q = 0; q < np; ++q)
+            if (ue[(long)ne * q] < th) th = ue[(long)ne * q];
+        double t = (um - eps) / (um - th + 1e-8);
+        if (t > 1.0) t = 1.0;
+        if (!(t > 0.0)) {
+            ++bad;
+            continue;
+        }
+        for (int q = 0; q < np; ++q) ue[(long)ne * q] = t * (ue[(long)ne * q] - um) + um;
+        count += t < 1.0;
+    }
+    return bad ? -bad : count;
+}
+
 /* Learned-indicator inputs: per element the normalised modal energies of
  * density and pressure, x_q = clamp(log10(uh_q^2 / sum uh^2 + 1e-16), -16, 0)/8 + 1. */
 void fro_modal_features2d(const fro_cfg *c, const double *u, const double *iV, double *feat) {

@@ -83,6 +83,15 @@ int fro_filter1d(const fro_cfg *c, double *u, int nvar, const double *V, const d
 void fro_modal_features2d(const fro_cfg *c, const double *u, const double *iV, double *feat);
 void fro_modal_features1d(const fro_cfg *c, const double *u, const double *iV, double *feat);
 
+/* ---- positivity-preserving limiter (src/dissipation.jl:38-216) ---- */
+/* w: the element quadrature weights normalised to sum 1 (2D: np^2 values, the
+ * reference passes ps.wp / 4; 1D: np values); t0 caps the energy scaling.
+ * Return: the number of elements scaled with a parameter below 1, or minus the
+ * number of elements whose density parameter left (0, 1]. */
+int fro_positive_limiter2d(const fro_cfg *c, double *u, const double *w, double t0);
+int fro_positive_limiter1d(const fro_cfg *c, double *u, const double *w, double t0);
+int fro_positive_limiter_scalar(const fro_cfg *c, double *u, const double *w, double t0);
+
 /* ---- reductions and norms ---- */
 void fro_conserved_sums2d(const fro_cfg *c, const double *u, const double *wp, double *sums);
 double fro_max_speed2d(const fro_cfg *c, const double *u);

@@ -83,6 +83,9 @@ def lib():
             "fro_filter1d": (C.c_int, [C.POINTER(Cfg), _D, C.c_int, _D, _D, C.c_double, _I]),
             "fro_modal_features2d": (None, [C.POINTER(Cfg), _D, _D, _D]),
             "fro_modal_features1d": (None, [C.POINTER(Cfg), _D, _D, _D]),
+            "fro_positive_limiter2d": (C.c_int, [C.POINTER(Cfg), _D, _D, C.c_double]),
+            "fro_positive_limiter1d": (C.c_int, [C.POINTER(Cfg), _D, _D, C.c_double]),
+            "fro_positive_limiter_scalar": (C.c_int, [C.POINTER(Cfg), _D, _D, C.c_double]),
             "fro_conserved_sums2d": (None, [C.POINTER(Cfg), _D, _D, _D]),
             "fro_max_speed2d": (C.c_double, [C.POINTER(Cfg), _D]),
             "fro_L1_error": (C.c_double, [_D, _D, C.c_long, C.c_double]),
@@ -344,6 +347,23 @@ class Problem:
         iV = _f64(self.space.iV)
         lib().fro_modal_features1d(C.byref(self.cfg), uf.ctypes.data_as(_D), _p(iV), _p(feat))
         return feat.reshape(self.cfg.nx, 32)
+
+    def positive_limiter(self, u: np.ndarray, w=None, t0: float = 1.0):
+        """positive_limiter (src/dissipation.jl:38-216) on every element.  w:
+        element quadrature weights summing to 1 (default: the Gauss weights,
+        2D: wp / 4 as example/shock-vortex.jl:301 passes them).  Returns the
+        limited state and the count (negative: elements whose density
+        parameter left (0, 1])."""
+        uf = np.array(u, dtype=np.float64, order="F", copy=True)
+        kind = self.cfg.kind
+        if w is None:
+            w = np.asarray(self.space.wp).ravel(order="F")
+            w = w / 4.0 if kind == EULER2D else w / 2.0
+        w = _f64(np.asarray(w).ravel(order="F"))
+        fn = {EULER2D: "fro_positive_limiter2d", EULER1D: "fro_positive_limiter1d"}.get(kind,
+                                                                                        "fro_positive_limiter_scalar")
+        n = getattr(lib(), fn)(C.byref(self.cfg), uf.ctypes.data_as(_D), _p(w), float(t0))
+        return uf, n
 
     def conserved_sums2d(self, u: np.ndarray) -> np.ndarray:
         uf = np.asfortranarray(u, dtype=np.float64)

@@ -206,3 +206,80 @@ def test_mlp_gradient_matches_finite_difference(oracle):
         lp, _ = oracle.mlp_loss_grad(P + e, x, t)
         lm, _ = oracle.mlp_loss_grad(P - e, x, t)
         assert abs((lp - lm) / 2e-6 - g[idx]) < 1e-7 * max(1, abs(g[idx]))
+
+
+# ---- positivity-preserving limiter (src/dissipation.jl:38-216) -------------
+def _euler2d_state(O, sp, seed, gamma=1.4):
+    rng = np.random.default_rng(seed)
+    shape = (sp.nx, sp.ny, sp.np, sp.np)
+    rho = 1 + 0.1 * rng.standard_normal(shape)
+    U, V = 0.3 * rng.standard_normal(shape), 0.2 * rng.standard_normal(shape)
+    p = 1 + 0.1 * rng.standard_normal(shape)
+    u = np.zeros(shape + (4,), order="F")
+    u[..., 0], u[..., 1], u[..., 2] = rho, rho * U, rho * V
+    u[..., 3] = p / (gamma - 1) + 0.5 * rho * (U ** 2 + V ** 2)
+    return u
+
+
+def _prim_p(w, gamma=1.4):
+    return (gamma - 1) * (w[..., -1] - 0.5 * np.sum(w[..., 1:-1] ** 2, axis=-1) / w[..., 0])
+
+
+def test_positive_limiter_reference_test_inputs(oracle):
+    """The reference's own calls (test/runtests.jl:25-26) on constant states
+    leave them unchanged."""
+    O = oracle
+    sp = O.Space1D(0, 1, 20, 5)
+    u = np.ones((1, 6), order="F")
+    out, n = O.Problem(O.ADVECTION, O.Space1D(0, 1, 1, 5)).positive_limiter(u, w=np.full(6, 1 / 6))
+    assert n == 0 and np.array_equal(out, u)
+    u3 = np.ones((1, 6, 3), order="F")
+    out3, n3 = O.Problem(O.EULER1D, O.Space1D(0, 1, 1, 5), gamma=5 / 3).positive_limiter(u3, w=np.full(6, 1 / 6))
+    assert n3 == 0 and np.array_equal(out3, u3)
+    assert sp.np == 6
+
+
+@pytest.mark.parametrize("deg", [2, 3])
+def test_positive_limiter_2d_restores_positivity_and_keeps_means(oracle, deg):
+    O = oracle
+    sp = O.Space2D(0, 1, 5, 0, 1, 4, deg)
+    pr = O.Problem(O.EULER2D, sp, gamma=1.4)
+    u = _euler2d_state(O, sp, deg)
+    u[1, 0, 1, 1, 0] = -0.3          # negative density at a solution point
+    u[2, 1, 0, deg, 3] = 0.01        # energy too low: negative pressure
+    u[4, 3, 2, 2, 3] = -0.5          # negative energy inside an element
+    out, n = pr.positive_limiter(u)
+    assert n == 3
+    wq = np.asarray(sp.wp).ravel(order="F") / 4
+    for i in range(sp.nx):
+        for j in range(sp.ny):
+            for m in range(4):
+                before = u[i, j, :, :, m].ravel(order="F") @ wq
+                after = out[i, j, :, :, m].ravel(order="F") @ wq
+                assert abs(after - before) <= 1e-13 * max(1.0, abs(before))
+    # positive density and pressure (pressure down to eps = 1e-13, up to the
+    # round-off of E - |m|^2 / (2 rho) at O(1) energies)
+    assert np.all(out[..., 0] > 0)
+    assert np.all(_prim_p(out) >= -1e-13)
+    # elements the limiter leaves alone move by round-off only ((u - mean) + mean)
+    assert np.max(np.abs(out[0, 0] - u[0, 0])) < 1e-14
+
+
+def test_positive_limiter_1d_forms(oracle):
+    O = oracle
+    sp = O.Space1D(0, 1, 6, 3)
+    rng = np.random.default_rng(3)
+    u = np.zeros((6, 4, 3), order="F")
+    rho = 1 + 0.1 * rng.standard_normal((6, 4))
+    u[..., 0], u[..., 1] = rho, 0.2 * rho
+    u[..., 2] = 1 / 0.4 + 0.5 * rho * 0.04
+    u[2, 1, 0] = -0.2
+    u[4, 3, 2] = 0.0
+    out, n = O.Problem(O.EULER1D, sp, gamma=1.4).positive_limiter(u)
+    assert n == 2 and np.all(out[..., 0] > 0) and np.all(_prim_p(out) >= -1e-13)
+    w = np.asarray(sp.wp) / 2
+    assert np.allclose(np.einsum("iqm,q->im", out, w), np.einsum("iqm,q->im", u, w), rtol=0, atol=1e-13)
+    s = 1 + 0.5 * np.sin(2 * np.pi * np.asarray(sp.xpg))
+    s[3, 2] = -0.4
+    outs, ns = O.Problem(O.ADVECTION, sp).positive_limiter(s)
+    assert ns == 1 and outs[3].min() > 0 and np.allclose((outs[3] - s[3]) @ np.asarray(sp.wp), 0, atol=1e-14)

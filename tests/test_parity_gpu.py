@@ -425,3 +425,89 @@ def test_euler2d_state_transfer_round_trip(frgpu, precision, nx, ny, deg):
     assert e.value.code == -3
     flat = np.ravel_multi_index((nx - 1, ny - 1, deg, 0, 2), u.shape, order="F")
     assert f"index {flat}" in str(e.value)
+
+
+# ---------------------------------------------------------------- positivity-preserving limiter
+def _limiter_state2d(xpg, deg):
+    u = wave2d(xpg, amp=0.1)
+    u[1, 0, 1, 1, 0] = -0.3      # negative density at a solution point
+    u[2, 1, 0, deg, 3] = 0.01    # energy too low: negative pressure
+    u[4, 3, 1, 0, 3] = -0.5      # negative energy
+    return u
+
+
+@pytest.mark.parametrize("deg", [2, 3, 4])
+def test_positive_limiter_2d_matches_oracle(frgpu, oracle, deg):
+    """positive_limiter (src/dissipation.jl:125-206) on every element: FP64
+    bit-identical to the oracle (including the round-off of (u - mean) + mean on
+    the elements it leaves alone), FP32K within FP32 rounding and the same
+    elements limited."""
+    ps = frgpu.FRPSpace2D(0, 1, 7, 0, 1, 5, deg)
+    po = oracle_space2d(ps, 0, 1, 7, 0, 1, 5, deg)
+    u = _limiter_state2d(ps.xpg, deg)
+    w = np.asarray(ps.wp).ravel(order="F") / 4
+    P = oracle.Problem(oracle.EULER2D, po, gamma=1.4)
+    ref, nref = P.positive_limiter(u, w=w)
+    assert nref == 3
+    itg = frgpu.init(frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf"), dt=1e-4)
+    assert itg.positive_limiter(w) == nref
+    assert np.array_equal(itg.u, ref)
+    itg32 = frgpu.init(frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf", precision="fp32k"), dt=1e-4)
+    assert itg32.positive_limiter(w) == nref
+    got = itg32.u
+    assert np.max(np.abs(got - ref)) < 1e-5 * np.max(np.abs(ref))
+    # FP32K rewrites only the limited elements
+    assert np.max(np.abs(got[0, 0] - u[0, 0])) < 1e-6
+    # uniform elements: the FP32 mean may exceed the point values by an ulp
+    flat = wave2d(ps.xpg, amp=0.0)
+    itgf = frgpu.init(frgpu.FREuler2DProblem(flat, (0, 1), ps, 1.4, flux="lf", precision="fp32k"), dt=1e-4)
+    assert itgf.positive_limiter(w) == 0
+    assert np.array_equal(itgf.u, flat)
+
+
+@pytest.mark.parametrize("deg", [2, 3])
+def test_positive_limiter_1d_matches_oracle(frgpu, oracle, deg):
+    ps = frgpu.FRPSpace1D(0, 1, 9, deg)
+    po = oracle_space1d(ps, 0, 1, 9, deg)
+    x = np.asarray(ps.xpg)
+    rho = 1 + 0.1 * np.sin(2 * np.pi * x)
+    u = np.zeros(x.shape + (3,), order="F")
+    u[..., 0], u[..., 1], u[..., 2] = rho, 0.2 * rho, 1 / 0.4 + 0.02 * rho
+    u[2, 1, 0] = -0.2
+    u[5, deg, 2] = 0.0
+    prob = frgpu.FREulerProblem(u, (0, 1), ps, 1.4)
+    itg = frgpu.init(prob, dt=1e-4)
+    ref, nref = oracle.Problem(oracle.EULER1D, po, gamma=1.4).positive_limiter(u)
+    assert nref == 2
+    assert itg.positive_limiter() == nref
+    assert np.array_equal(itg.u, ref)
+    s = 1 + 0.5 * np.sin(2 * np.pi * x)
+    s[3, 1] = -0.4
+    itg_s = frgpu.init(frgpu.FRAdvectionProblem(s, (0, 1), ps, 1.0, "period"), dt=1e-3)
+    refs, ns = oracle.Problem(oracle.ADVECTION, po).positive_limiter(s)
+    assert ns == 1 and itg_s.positive_limiter() == 1
+    assert np.array_equal(itg_s.u, refs)
+
+
+def test_limiter_inside_step_graph(frgpu, oracle):
+    """set_limiter runs the limiter before every step (the loop of
+    example/shock-vortex.jl:297-303): bit-identical to the oracle's limiter +
+    SSPRK3 sequence in FP64."""
+    ps = frgpu.FRPSpace2D(0, 1, 24, 0, 1, 16, 3)
+    po = oracle_space2d(ps, 0, 1, 24, 0, 1, 16, 3)
+    u = wave2d(ps.xpg)
+    prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf", bc="period")
+    P = oracle.Problem(oracle.EULER2D, po, gamma=1.4, flux=oracle.FLUX_LF)
+    dt = 1e-4
+    w = np.asarray(ps.wp).ravel(order="F") / 4
+    itg = frgpu.init(prob, dt=dt)
+    itg.set_limiter(True, w)
+    itg.step(3)
+    ref = u.copy(order="F")
+    for _ in range(3):
+        ref, _ = P.positive_limiter(ref, w=w)
+        ref = P.ssprk3(ref, dt, 1)
+    assert np.array_equal(itg.u, ref)
+    itg.set_limiter(False)
+    itg.step(1)
+    assert np.array_equal(itg.u, P.ssprk3(ref, dt, 1))
