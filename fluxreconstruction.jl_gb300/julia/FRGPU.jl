@@ -172,6 +172,26 @@ function modal_filter!(itg, indicator::Symbol, λ, S0, κ)
     return Int(n[])
 end
 
+"""`positive_limiter(ũ, γ, weights, ll, lr, t0)` of src/dissipation.jl:38-216 on every
+element of the integrator's state at once (the loop of example/shock-vortex.jl:298-303);
+`weights` as the reference takes them (`ps.wp ./ 4` in 2D), or `nothing` for the space's
+Gauss weights so normalised.  Returns the number of elements scaled."""
+function positive_limiter!(itg, weights=nothing, t0=1.0)
+    n = Ref{Cint}(0)
+    w = weights === nothing ? C_NULL : Vector{Float64}(vec(weights))
+    check(ccall((:frgpu_positive_limiter, libfrgpu), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Cdouble, Ref{Cint}),
+                itg.p.h, w, t0, n))
+    return Int(n[])
+end
+
+"""Run `positive_limiter!` before every `step!` from now on (`on = false` switches it off)."""
+function set_limiter!(itg, on::Bool, weights=nothing, t0=1.0)
+    w = weights === nothing ? C_NULL : Vector{Float64}(vec(weights))
+    check(ccall((:frgpu_set_limiter, libfrgpu), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cdouble),
+                itg.p.h, on ? 1 : 0, w, t0))
+    return nothing
+end
+
 """interp_face!(fδ, f, ll, lr) of src/interpolate.jl:1-10, evaluated on the GPU."""
 function interp_face!(fδ, f::AbstractMatrix, ll, lr)
     fh = Matrix{Float64}(f)
