@@ -54,6 +54,14 @@ struct frgpu_problem {
     int limiter = 0;                // positivity-preserving limiter before every step
     double lim_t0 = 1.0;            // its t0 (cap of the energy scaling)
     std::vector<double> lim_w;      // its element weights
+    // explicit Runge-Kutta stepping (erk.cu): tableau, k buffers + stage buffer, step graph
+    int erk_s = 0;
+    std::vector<double> erk_A, erk_b;
+    void *d_erk = nullptr;
+    size_t erk_cap = 0; // stages d_erk holds
+    cudaGraphExec_t erk_gexec = nullptr;
+    long erk_launches = 0; // kernels per captured ERK step
+    bool erk_dirty = true;
     float *d_bgk_prim = nullptr;    // FP32 BGK: (rho, U, lambda) per (element, point), from the moments
     uint32_t *d_bgk_frag = nullptr; // FP32 BGK: TF32 A fragments of the transport operator (both signs, split)
     // captured step graph
@@ -65,6 +73,7 @@ struct frgpu_problem {
 };
 
 constexpr int FR_NCOUNT = 8, FR_COUNT_LIMITER = 4; // d_count entries
+constexpr int FR_ERK_MAXS = 16;                     // stages of an explicit Runge-Kutta tableau
 constexpr int FR_RED_BLOCKS = 608; // reduction partial blocks (4 x 152 SMs)
 // d_red layout: [FR_RED_BLOCKS*6 partials][8 final][64 quadrature weights]
 constexpr int FR_RED_FINAL = FR_RED_BLOCKS * 6;
@@ -137,3 +146,5 @@ int fr_launch_mlp_indicator(frgpu_problem *p, double lam, double S0, double kapp
 // positivity-preserving limiter (limiter.cu)
 int fr_launch_limiter(frgpu_problem *p, const std::vector<double> &w, double t0);
 int fr_limiter_weights(const frgpu_problem *p, const double *weights, std::vector<double> &w);
+// explicit Runge-Kutta step (erk.cu); launch_residual evaluates k = L(in)
+int fr_enqueue_erk_step(frgpu_problem *p, int (*launch_residual)(frgpu_problem *, const void *, void *));

@@ -290,9 +290,10 @@ static void free_problem(frgpu_problem *p) {
     if (p->stream) cudaStreamSynchronize(p->stream);
     for (auto &g : p->gexec)
         if (g) cudaGraphExecDestroy(g);
+    if (p->erk_gexec) cudaGraphExecDestroy(p->erk_gexec);
     void *bufs[] = {p->s0, p->s1, p->s2, p->s3, p->d_dt, p->d_status, p->d_red, p->d_flags, p->d_count,
                     p->d_velo, p->d_w, p->d_J, p->d_V, p->d_iV, p->rhs_in, p->rhs_out, p->d_bgk_prim,
-                    p->d_bgk_frag, p->d_stage};
+                    p->d_bgk_frag, p->d_stage, p->d_erk};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -365,6 +366,51 @@ static int enqueue_step(frgpu_problem *p) {
         if (p->d.precision == FRGPU_FP32K) p->parity ^= 1;
         if (rc) return rc;
     }
+    return FRGPU_OK;
+}
+
+// One explicit Runge-Kutta step (limiter before it, filter after it).
+static int residual_into(frgpu_problem *p, const void *in, void *out) { return launch_stage(p, 0, in, nullptr, out); }
+
+static int enqueue_erk(frgpu_problem *p) {
+    int rc;
+    if (p->limiter && (rc = fr_launch_limiter(p, p->lim_w, p->lim_t0))) return rc;
+    if ((rc = fr_enqueue_erk_step(p, residual_into))) return rc;
+    if (p->indicator != FRGPU_IND_NONE) {
+        // the high part stays in place (no parity flip); the learned indicator
+        // runs as its own kernel (its fused form lives in SSPRK3's stage 3)
+        rc = p->sp.dim == 2 ? fr_launch_filter2d(p, p->indicator, p->lam, p->S0, p->kappa)
+                            : fr_launch_filter1d(p, p->indicator, p->lam, p->S0, p->kappa);
+        if (rc) return rc;
+    }
+    return FRGPU_OK;
+}
+
+static int build_erk_graph(frgpu_problem *p) {
+    if (p->erk_gexec) {
+        cudaGraphExecDestroy(p->erk_gexec);
+        p->erk_gexec = nullptr;
+    }
+    p->prepare_only = true;
+    int rc = enqueue_erk(p);
+    p->prepare_only = false;
+    if (rc) return rc;
+    const long before = p->launches;
+    cudaGraph_t g = nullptr;
+    FR_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+    rc = enqueue_erk(p);
+    cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
+    p->erk_launches = p->launches - before;
+    p->launches = before;
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (ce != cudaSuccess) return fr_cuda_fail(ce, "cudaStreamEndCapture");
+    ce = cudaGraphInstantiate(&p->erk_gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return fr_cuda_fail(ce, "cudaGraphInstantiate");
+    p->erk_dirty = false;
     return FRGPU_OK;
 }
 
@@ -603,6 +649,52 @@ FRGPU_API int frgpu_step_ssprk3(frgpu_problem *p, double dt, int nsteps) {
     FR_CATCH
 }
 
+FRGPU_API int frgpu_step_erk(frgpu_problem *p, int s, const double *A, const double *b, double dt, int nsteps) {
+    FR_REQ(p && A && b, "step_erk: null argument");
+    FR_REQ(s >= 1 && s <= FR_ERK_MAXS, "step_erk: need 1 <= stages <= 16");
+    FR_REQ(nsteps >= 0, "step_erk: negative step count");
+    for (int i = 0; i < s; ++i)
+        for (int j = i; j < s; ++j)
+            FR_REQ(A[i * s + j] == 0.0, "step_erk: the tableau must be explicit (A strictly lower triangular)");
+    if (!(dt > 0.0) || !std::isfinite(dt)) {
+        fr_set_error("step_erk: dt must be positive and finite");
+        return FRGPU_ERR_DT;
+    }
+    if (nsteps == 0) return FRGPU_OK;
+    FR_TRY
+    if (dt != p->host_dt) {
+        FR_CUDA(cudaMemcpyAsync(p->d_dt, &dt, sizeof(double), cudaMemcpyHostToDevice, p->stream));
+        FR_CUDA(cudaStreamSynchronize(p->stream));
+        p->host_dt = dt;
+    }
+    std::vector<double> Av(A, A + (size_t)s * s), bv(b, b + s);
+    if (s != p->erk_s || Av != p->erk_A || bv != p->erk_b) {
+        p->erk_s = s;
+        p->erk_A = Av;
+        p->erk_b = bv;
+        p->erk_dirty = true;
+    }
+    if ((size_t)s > p->erk_cap) {
+        FR_CUDA(cudaStreamSynchronize(p->stream));
+        if (p->d_erk) cudaFree(p->d_erk);
+        p->d_erk = nullptr;
+        p->erk_cap = 0;
+        FR_CUDA(cudaMalloc(&p->d_erk, (size_t)(s + 1) * p->ndof * p->esize));
+        p->erk_cap = s;
+        p->erk_dirty = true;
+    }
+    if (p->erk_dirty || !p->erk_gexec) {
+        int rc = build_erk_graph(p);
+        if (rc) return rc;
+    }
+    for (int it = 0; it < nsteps; ++it) {
+        FR_CUDA(cudaGraphLaunch(p->erk_gexec, p->stream));
+        p->launches += p->erk_launches;
+    }
+    return check_status(p);
+    FR_CATCH
+}
+
 FRGPU_API int frgpu_reduce(frgpu_problem *p, double *sums, double *maxspeed) {
     FR_REQ(p, "reduce: null problem");
     if (p->d.equation != FRGPU_EULER2D) {
@@ -662,6 +754,7 @@ FRGPU_API int frgpu_set_filter(frgpu_problem *p, int indicator, double lam, doub
     p->S0 = S0;
     p->kappa = kappa;
     p->graph_ind = -2; // force a re-capture
+    p->erk_dirty = true;
     return FRGPU_OK;
 }
 
@@ -671,6 +764,7 @@ FRGPU_API int frgpu_problem_set_option(frgpu_problem *p, int option, int value) 
     if (option == FRGPU_OPT_BGK_TENSOR) p->bgk_tensor = value != 0;
     if (option == FRGPU_OPT_FUSED_INDICATOR) p->fuse_indicator = value != 0;
     p->graph_ind = -2; // force a re-capture
+    p->erk_dirty = true;
     return FRGPU_OK;
 }
 
@@ -721,6 +815,7 @@ FRGPU_API int frgpu_set_limiter(frgpu_problem *p, int on, const double *weights,
     }
     p->limiter = on != 0;
     p->graph_ind = -2; // force a re-capture
+    p->erk_dirty = true;
     return FRGPU_OK;
 }
 
@@ -732,6 +827,7 @@ FRGPU_API int frgpu_problem_set_mlp(frgpu_problem *p, const frgpu_mlp *m, double
     p->mlp_thr = (float)threshold;
     p->mlp_band = (float)band;
     p->graph_ind = -2; // the captured step refers to the network: re-capture
+    p->erk_dirty = true;
     return FRGPU_OK;
 }
 

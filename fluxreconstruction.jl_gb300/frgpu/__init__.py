@@ -18,7 +18,14 @@ from .api import (  # noqa: F401
     L2_error,
     Linf_error,
     ODEProblem,
+    RK4,
+    SSPRK22,
     SSPRK33,
+    ExplicitRK,
+    Heun,
+    Midpoint,
+    Ralston,
+    Tsit5,
     dhuynh,
     dlagrange,
     dradau,

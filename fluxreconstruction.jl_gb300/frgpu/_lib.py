@@ -69,6 +69,7 @@ SIGNATURES = {
     "frgpu_modal_filter": (C.c_int, [_VP, C.c_int, C.c_double, C.c_double, C.c_double, _I]),
     "frgpu_troubled_flags": (C.c_int, [_VP, _I, C.c_long]),
     "frgpu_positive_limiter": (C.c_int, [_VP, _D, C.c_double, _I]),
+    "frgpu_step_erk": (C.c_int, [_VP, C.c_int, _D, _D, C.c_double, C.c_int]),
     "frgpu_set_limiter": (C.c_int, [_VP, C.c_int, _D, C.c_double]),
     "frgpu_problem_device_state": (C.c_int, [_VP, C.POINTER(_VP), _I]),
     "frgpu_problem_stream": (C.c_int, [_VP, C.POINTER(_VP)]),

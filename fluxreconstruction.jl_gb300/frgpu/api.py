@@ -365,17 +365,71 @@ def FRBGKProblem(u, tspan, ps: FRPSpace1D, velo, weights, tau, precision="fp64")
 
 
 class SSPRK33:
-    """Marker for the three-stage SSP Runge-Kutta method (OrdinaryDiffEq SSPRK33)."""
+    """Marker for the three-stage SSP Runge-Kutta method (OrdinaryDiffEq SSPRK33);
+    it runs fused into the residual kernels."""
+
+
+class ExplicitRK:
+    """A fixed-step explicit Runge-Kutta method given by its Butcher tableau
+    (A strictly lower triangular, weights b); stepped by frgpu_step_erk."""
+
+    def __init__(self, A, b, name: str = "ExplicitRK"):
+        self.A = np.ascontiguousarray(np.asarray(A, dtype=np.float64))
+        self.b = np.ascontiguousarray(np.asarray(b, dtype=np.float64))
+        self.name = name
+        s = len(self.b)
+        if self.A.shape != (s, s) or np.any(np.triu(self.A) != 0.0):
+            raise ValueError("need an explicit s x s tableau (A strictly lower triangular)")
+
+    def __repr__(self):
+        return f"{self.name}()"
+
+
+def Midpoint() -> ExplicitRK:
+    """OrdinaryDiffEq Midpoint (explicit midpoint rule), as example/shock-vortex.jl:294 uses it."""
+    return ExplicitRK([[0, 0], [0.5, 0]], [0, 1], "Midpoint")
+
+
+def Heun() -> ExplicitRK:
+    return ExplicitRK([[0, 0], [1, 0]], [0.5, 0.5], "Heun")
+
+
+def Ralston() -> ExplicitRK:
+    return ExplicitRK([[0, 0], [2 / 3, 0]], [0.25, 0.75], "Ralston")
+
+
+def SSPRK22() -> ExplicitRK:
+    return ExplicitRK([[0, 0], [1, 0]], [0.5, 0.5], "SSPRK22")
+
+
+def RK4() -> ExplicitRK:
+    return ExplicitRK([[0, 0, 0, 0], [0.5, 0, 0, 0], [0, 0.5, 0, 0], [0, 0, 1, 0]],
+                      [1 / 6, 1 / 3, 1 / 3, 1 / 6], "RK4")
+
+
+def Tsit5() -> ExplicitRK:
+    """Tsitouras 5(4) pair (Ch. Tsitouras, Comput. Math. Appl. 62 (2011) 770-775),
+    fifth-order weights, fixed dt (adaptive=false): the last row of A is b (FSAL)."""
+    a = np.zeros((7, 7))
+    a[1, 0] = 0.161
+    a[2, :2] = [-0.008480655492356989, 0.335480655492357]
+    a[3, :3] = [2.897153057105493, -6.359448489975075, 4.3622954328695815]
+    a[4, :4] = [5.325864828439257, -11.748883564062828, 7.4955393428898365, -0.09249506636175525]
+    a[5, :5] = [5.86145544294642, -12.92096931784711, 8.159367898576159, -0.071584973281401, -0.028269050394068383]
+    a[6, :6] = [0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081,
+                2.324710524099774]
+    return ExplicitRK(a, np.append(a[6, :6], 0.0), "Tsit5")
 
 
 class Integrator:
     """Device-resident integrator: ``itg.u`` reads the state back, ``step_(itg)``
     advances one step of ``dt`` on the GPU (OrdinaryDiffEq's init/step! API)."""
 
-    def __init__(self, prob: ODEProblem, dt: float):
+    def __init__(self, prob: ODEProblem, dt: float, alg=None):
         self.prob = prob
         self.dt = float(dt)
         self.t = prob.tspan[0]
+        self.alg = alg if isinstance(alg, ExplicitRK) else None
         check(L.lib().frgpu_state_upload(prob._h, dptr(prob.u0)))
 
     @property
@@ -402,7 +456,11 @@ class Integrator:
 
     def step(self, n: int = 1, dt: float | None = None) -> None:
         dt = self.dt if dt is None else float(dt)
-        check(L.lib().frgpu_step_ssprk3(self.prob._h, dt, int(n)))
+        if self.alg is None:
+            check(L.lib().frgpu_step_ssprk3(self.prob._h, dt, int(n)))
+        else:
+            a = self.alg
+            check(L.lib().frgpu_step_erk(self.prob._h, len(a.b), dptr(a.A), dptr(a.b), dt, int(n)))
         self.t += n * dt
 
     def set_filter(self, indicator="plain", lam=5e-4, S0=None, kappa=9.0) -> None:
@@ -468,12 +526,14 @@ class Integrator:
 
 
 def init(prob: ODEProblem, alg=None, *, dt: float, adaptive: bool = False, **kwargs) -> Integrator:
-    """init(prob, SSPRK33(); adaptive=false, dt) (OrdinaryDiffEq)."""
-    if alg is not None and not isinstance(alg, SSPRK33) and alg is not SSPRK33:
-        raise NotImplementedError("the device integrator implements SSPRK33")
+    """init(prob, alg; adaptive=false, dt) (OrdinaryDiffEq): SSPRK33 (default,
+    fused into the residual kernels) or an explicit tableau (Midpoint(), RK4(),
+    Tsit5(), ... or ExplicitRK(A, b))."""
+    if alg is not None and not isinstance(alg, (SSPRK33, ExplicitRK)) and alg is not SSPRK33:
+        raise NotImplementedError("the device integrator implements SSPRK33 and explicit Runge-Kutta tableaux")
     if adaptive:
         raise NotImplementedError("fixed time steps only (adaptive=false)")
-    return Integrator(prob, dt)
+    return Integrator(prob, dt, alg)
 
 
 def step_(itg: Integrator, n: int = 1) -> None:

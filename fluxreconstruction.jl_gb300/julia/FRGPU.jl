@@ -205,23 +205,42 @@ end
 
 struct SSPRK33 end
 
+"""A fixed-step explicit Runge-Kutta method by its Butcher tableau (A strictly lower
+triangular, weights b), stepped on the device by `frgpu_step_erk`."""
+struct ExplicitRK
+    A::Matrix{Float64}
+    b::Vector{Float64}
+end
+Midpoint() = ExplicitRK([0.0 0.0; 0.5 0.0], [0.0, 1.0])     # as example/shock-vortex.jl:294 uses it
+Heun() = ExplicitRK([0.0 0.0; 1.0 0.0], [0.5, 0.5])
+RK4() = ExplicitRK([0 0 0 0; 0.5 0 0 0; 0 0.5 0 0; 0 0 1 0], [1 / 6, 1 / 3, 1 / 3, 1 / 6])
+
 mutable struct Integrator
     p::Problem
     t::Float64
     dt::Float64
+    alg::Union{Nothing,ExplicitRK}
 end
 
-"""init(prob, SSPRK33(); dt): upload u0 once; the state stays on the device."""
-function init(prob::ODEProblem, ::SSPRK33; dt, adaptive=false, kwargs...)
+"""init(prob, SSPRK33(); dt) or init(prob, Midpoint(); dt): upload u0 once; the state
+stays on the device."""
+function init(prob::ODEProblem, alg::Union{SSPRK33,ExplicitRK}; dt, adaptive=false, kwargs...)
     adaptive && error("FRGPU integrates with fixed dt")
     p = prob.p::Problem
     check(ccall((:frgpu_state_upload, libfrgpu), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), p.h, Array{Float64}(prob.u0)))
-    return Integrator(p, prob.tspan[1], dt)
+    return Integrator(p, prob.tspan[1], dt, alg isa ExplicitRK ? alg : nothing)
 end
 
 """step!(itg): one SSPRK3 step on the device (a captured CUDA graph)."""
 function step!(itg::Integrator, n::Integer=1)
-    check(ccall((:frgpu_step_ssprk3, libfrgpu), Cint, (Ptr{Cvoid}, Cdouble, Cint), itg.p.h, itg.dt, n))
+    a = getfield(itg, :alg)
+    if a === nothing
+        check(ccall((:frgpu_step_ssprk3, libfrgpu), Cint, (Ptr{Cvoid}, Cdouble, Cint), itg.p.h, itg.dt, n))
+    else
+        A = Matrix{Float64}(permutedims(a.A))   # row-major for the C ABI
+        check(ccall((:frgpu_step_erk, libfrgpu), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Cdouble, Cint),
+                    itg.p.h, length(a.b), A, a.b, itg.dt, n))
+    end
     itg.t += n * itg.dt
     return nothing
 end

@@ -147,6 +147,14 @@ FRGPU_API int frgpu_rhs(frgpu_problem *p, double *du, const double *u, double t)
  * are replayed from a captured CUDA graph; the post-step filter configured by
  * frgpu_set_filter runs after every step. */
 FRGPU_API int frgpu_step_ssprk3(frgpu_problem *p, double dt, int nsteps);
+/* nsteps of a fixed-step explicit Runge-Kutta method given by its Butcher
+ * tableau: A (s x s, row-major, strictly lower triangular) and b (s), s <= 16
+ * (OrdinaryDiffEq's Midpoint, Heun, RK4, Tsit5, ... with adaptive=false, as
+ * example/shock-vortex.jl:294 uses Midpoint).  Stage i evaluates the residual at
+ * u + dt sum_j a_ij k_j; the step adds dt sum_j b_j k_j.  The limiter and the
+ * filter configured for the problem run before and after every step, as with
+ * frgpu_step_ssprk3.  Steps are replayed from a captured CUDA graph. */
+FRGPU_API int frgpu_step_erk(frgpu_problem *p, int s, const double *A, const double *b, double dt, int nsteps);
 /* dt = cfl / max over points of sum_d (|u_d| + c)/dx_d (FP64 max-reduction on the GPU) */
 FRGPU_API int frgpu_cfl_dt(frgpu_problem *p, double cfl, double *dt);
 /* FP64 conserved sums (quadrature-weighted, per variable) and max wave speed */

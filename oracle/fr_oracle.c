@@ -817,6 +817,43 @@ void fro_ssprk3(const fro_cfg *c, double *u, double dt, int nsteps, double *work
     }
 }
 
+/* Explicit Runge-Kutta with a Butcher tableau (OrdinaryDiffEq's fixed-step
+ * explicit methods: Midpoint, Heun, RK4, Tsit5, ...): per step and stage i,
+ * acc = sum over j < i with a_ij != 0, in ascending j, as the fma chain
+ * acc = a_ij0 k_j0; acc = fma(a_ij, k_j, acc); stage = fma(dt, acc, u) (u when
+ * no a_ij is nonzero); k_i = rhs(stage); then u = fma(dt, acc_b, u) with the b
+ * weights.  A is s x s row-major; work holds (s + 1) * ndof doubles. */
+void fro_erk(const fro_cfg *c, double *u, double dt, int nsteps, int s, const double *A, const double *b,
+             double *work) {
+    long n = fro_ndof(c);
+    double *st = work, *k = work + n;
+    for (int it = 0; it < nsteps; ++it) {
+        for (int i = 0; i < s; ++i) {
+            int first = 1;
+            for (int j = 0; j < i; ++j) {
+                const double a = A[i * s + j];
+                if (a == 0.0) continue;
+                for (long q = 0; q < n; ++q) st[q] = first ? a * k[j * n + q] : fma(a, k[j * n + q], st[q]);
+                first = 0;
+            }
+            if (first)
+                fro_rhs(c, k + i * n, u);
+            else {
+                for (long q = 0; q < n; ++q) st[q] = fma(dt, st[q], u[q]);
+                fro_rhs(c, k + i * n, st);
+            }
+        }
+        int first = 1;
+        for (int j = 0; j < s; ++j) {
+            if (b[j] == 0.0) continue;
+            for (long q = 0; q < n; ++q) st[q] = first ? b[j] * k[j * n + q] : fma(b[j], k[j * n + q], st[q]);
+            first = 0;
+        }
+        if (!first)
+            for (long q = 0; q < n; ++q) u[q] = fma(dt, st[q], u[q]);
+    }
+}
+
 /* ------------------------------------------------------------------------
  * Troubled-cell indicator and modal filter
  * ---------------------------------------------------------------------- */

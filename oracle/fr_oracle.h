@@ -69,6 +69,10 @@ long fro_ndof(const fro_cfg *c);
 void fro_rhs(const fro_cfg *c, double *du, const double *u);
 /* Shu-Osher SSPRK3, nsteps fixed steps of size dt; work must hold 2*ndof doubles */
 void fro_ssprk3(const fro_cfg *c, double *u, double dt, int nsteps, double *work);
+/* explicit Runge-Kutta of s stages (A: s x s row-major, b: s), fixed dt;
+ * work must hold (s + 1) * ndof doubles */
+void fro_erk(const fro_cfg *c, double *u, double dt, int nsteps, int s, const double *A, const double *b,
+             double *work);
 
 /* ---- troubled-cell indicator and modal filter ---- */
 /* 2D, per step: detect on rho with iV (np^2 x np^2), filter all 4 variables

@@ -78,6 +78,7 @@ def lib():
             "fro_ndof": (C.c_long, [C.POINTER(Cfg)]),
             "fro_rhs": (None, [C.POINTER(Cfg), _D, _D]),
             "fro_ssprk3": (None, [C.POINTER(Cfg), _D, C.c_double, C.c_int, _D]),
+            "fro_erk": (None, [C.POINTER(Cfg), _D, C.c_double, C.c_int, C.c_int, _D, _D, _D]),
             "fro_filter2d": (C.c_int, [C.POINTER(Cfg), _D, _D, _D, C.c_double, C.c_double,
                                        C.c_double, _I]),
             "fro_filter1d": (C.c_int, [C.POINTER(Cfg), _D, C.c_int, _D, _D, C.c_double, _I]),
@@ -310,6 +311,16 @@ class Problem:
         uf = np.array(u, dtype=np.float64, order="F", copy=True)
         work = np.zeros(2 * uf.size)
         lib().fro_ssprk3(C.byref(self.cfg), uf.ctypes.data_as(_D), float(dt), int(nsteps), _p(work))
+        return uf
+
+    def erk(self, u: np.ndarray, dt: float, nsteps: int, A, b) -> np.ndarray:
+        """Fixed-step explicit Runge-Kutta with the Butcher tableau (A, b)."""
+        uf = np.array(u, dtype=np.float64, order="F", copy=True)
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        s = len(b)
+        work = np.zeros((s + 1) * uf.size)
+        lib().fro_erk(C.byref(self.cfg), uf.ctypes.data_as(_D), float(dt), int(nsteps), s, _p(A), _p(b), _p(work))
         return uf
 
     def filter2d(self, u: np.ndarray, lam: float, S0: float, kappa: float):

@@ -283,3 +283,53 @@ def test_positive_limiter_1d_forms(oracle):
     s[3, 2] = -0.4
     outs, ns = O.Problem(O.ADVECTION, sp).positive_limiter(s)
     assert ns == 1 and outs[3].min() > 0 and np.allclose((outs[3] - s[3]) @ np.asarray(sp.wp), 0, atol=1e-14)
+
+
+# ---- explicit Runge-Kutta tableaux (OrdinaryDiffEq's fixed-step methods) ----
+def test_erk_tableaux_order_conditions():
+    """The tableaux frgpu ships satisfy their order conditions (Tsit5: fifth
+    order, all 17 conditions up to order 5; RK4: fourth; the two-stage methods:
+    second), so a transcription error in a coefficient cannot pass."""
+    import frgpu
+
+    def conds(A, b, order):
+        c = A.sum(1)
+        out = [(b.sum(), 1.0), (b @ c, 1 / 2)]
+        if order >= 3:
+            out += [(b @ c ** 2, 1 / 3), (b @ A @ c, 1 / 6)]
+        if order >= 4:
+            out += [(b @ c ** 3, 1 / 4), (b @ (c * (A @ c)), 1 / 8), (b @ A @ c ** 2, 1 / 12), (b @ A @ A @ c, 1 / 24)]
+        if order >= 5:
+            out += [(b @ c ** 4, 1 / 5), (b @ (c ** 2 * (A @ c)), 1 / 10), (b @ (c * (A @ c ** 2)), 1 / 15),
+                    (b @ (c * (A @ A @ c)), 1 / 30), (b @ (A @ c) ** 2, 1 / 20), (b @ A @ c ** 3, 1 / 20),
+                    (b @ A @ (c * (A @ c)), 1 / 40), (b @ A @ A @ c ** 2, 1 / 60), (b @ A @ A @ A @ c, 1 / 120)]
+        return out
+
+    for alg, order in ((frgpu.Midpoint(), 2), (frgpu.Heun(), 2), (frgpu.Ralston(), 2), (frgpu.SSPRK22(), 2),
+                       (frgpu.RK4(), 4), (frgpu.Tsit5(), 5)):
+        for got, want in conds(alg.A, alg.b, order):
+            assert abs(got - want) < 1e-13, (alg, got, want)
+    with pytest.raises(ValueError):
+        frgpu.ExplicitRK([[0, 1], [0, 0]], [0.5, 0.5])
+
+
+def test_oracle_erk_reproduces_ssprk3_and_rk4(oracle):
+    """fro_erk with the SSPRK33 tableau matches fro_ssprk3 to round-off, and one
+    RK4 step matches the classical formula written out over the oracle's rhs."""
+    O = oracle
+    sp = O.Space1D(0, 1, 20, 3)
+    pr = O.Problem(O.ADVECTION, sp, a=1.0)
+    u0 = np.sin(2 * np.pi * np.asarray(sp.xpg))
+    A = np.array([[0, 0, 0], [1, 0, 0], [0.25, 0.25, 0]])
+    b = np.array([1 / 6, 1 / 6, 2 / 3])
+    ua, ub = pr.ssprk3(u0, 1e-3, 10), pr.erk(u0, 1e-3, 10, A, b)
+    assert np.max(np.abs(ua - ub)) < 1e-14
+    A4 = np.array([[0, 0, 0, 0], [0.5, 0, 0, 0], [0, 0.5, 0, 0], [0, 0, 1, 0]])
+    b4 = np.array([1, 2, 2, 1]) / 6
+    dt = 2e-3
+    k1 = pr.rhs(u0)
+    k2 = pr.rhs(u0 + 0.5 * dt * k1)
+    k3 = pr.rhs(u0 + 0.5 * dt * k2)
+    k4 = pr.rhs(u0 + dt * k3)
+    want = u0 + dt * (k1 + 2 * k2 + 2 * k3 + k4) / 6
+    assert np.max(np.abs(pr.erk(u0, dt, 1, A4, b4) - want)) < 1e-13

@@ -511,3 +511,73 @@ def test_limiter_inside_step_graph(frgpu, oracle):
     itg.set_limiter(False)
     itg.step(1)
     assert np.array_equal(itg.u, P.ssprk3(ref, dt, 1))
+
+
+# ---------------------------------------------------------------- explicit Runge-Kutta tableaux
+@pytest.mark.parametrize("name", ["Midpoint", "RK4", "Tsit5"])
+def test_erk_2d_matches_oracle(frgpu, oracle, name):
+    """frgpu_step_erk (OrdinaryDiffEq's fixed-step explicit methods, as
+    example/shock-vortex.jl:294 runs Midpoint) against the oracle's fro_erk on
+    the periodic 2D Euler wave, FP64."""
+    alg = getattr(frgpu, name)()
+    ps = frgpu.FRPSpace2D(0, 1, 24, 0, 1, 16, 3)
+    po = oracle_space2d(ps, 0, 1, 24, 0, 1, 16, 3)
+    u = wave2d(ps.xpg)
+    prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf", bc="period")
+    P = oracle.Problem(oracle.EULER2D, po, gamma=1.4, flux=oracle.FLUX_LF)
+    dt = 1e-4
+    itg = frgpu.init(prob, alg, dt=dt)
+    itg.step(2)
+    itg.step(1)
+    ref = P.erk(u, dt, 3, alg.A, alg.b)
+    assert rel(itg.u, ref) < RTOL64
+
+
+def test_erk_1d_and_graph_options_match_oracle(frgpu, oracle):
+    """RK4 on the 1D advection and on the 1D Euler problem, and Midpoint with
+    the limiter before and the filter after every step (2D, the full loop of
+    example/shock-vortex.jl:297-321), against the oracle, FP64."""
+    ps = frgpu.FRPSpace1D(0, 1, 30, 3)
+    po = oracle_space1d(ps, 0, 1, 30, 3)
+    x = np.asarray(ps.xpg)
+    s = np.sin(2 * np.pi * x)
+    itg = frgpu.init(frgpu.FRAdvectionProblem(s, (0, 1), ps, 1.0, "period"), frgpu.RK4(), dt=2e-3)
+    itg.step(4)
+    alg = frgpu.RK4()
+    ref = oracle.Problem(oracle.ADVECTION, po).erk(s, 2e-3, 4, alg.A, alg.b)
+    assert rel(itg.u, ref) < RTOL64
+
+    ps2 = frgpu.FRPSpace2D(0, 2, 40, 0, 1, 20, 3)
+    po2 = oracle_space2d(ps2, 0, 2, 40, 0, 1, 20, 3)
+    u, _ = vortex2d(ps2.xpg)
+    prob = frgpu.FREuler2DProblem(u, (0, 1), ps2, 1.4, flux="hll", bc="copy")
+    P = oracle.Problem(oracle.EULER2D, po2, gamma=1.4, flux=oracle.FLUX_HLL, bc=oracle.BC_COPY)
+    mid = frgpu.Midpoint()
+    dt, S0 = 2e-4, -3 * math.log10(3)
+    w = np.asarray(ps2.wp).ravel(order="F") / 4
+    itg2 = frgpu.init(prob, mid, dt=dt)
+    itg2.set_limiter(True, w)
+    itg2.set_filter("plain", 5e-4, S0, 9.0)
+    itg2.step(3)
+    ref2 = u.copy(order="F")
+    for _ in range(3):
+        ref2, _ = P.positive_limiter(ref2, w=w)
+        ref2 = P.erk(ref2, dt, 1, mid.A, mid.b)
+        ref2, _, _ = P.filter2d(ref2, 5e-4, S0, 9.0)
+    assert rel(itg2.u, ref2) < RTOL64
+
+
+def test_erk_fp32k_close_to_fp64(frgpu):
+    """FP32K Tsit5 (FP32 residual, compensated step update) within FP32 rounding
+    of the FP64 run, and mixing SSPRK3 and ERK steps on one problem."""
+    ps = frgpu.FRPSpace2D(0, 1, 32, 0, 1, 32, 3)
+    u = wave2d(ps.xpg)
+    runs = {}
+    for precision in ("fp64", "fp32k"):
+        prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf", bc="period", precision=precision)
+        itg = frgpu.init(prob, frgpu.Tsit5(), dt=2e-4)
+        itg.step(10)
+        itg.alg = None
+        itg.step(5)                      # SSPRK3 steps on the same state
+        runs[precision] = itg.u
+    assert rel(runs["fp32k"], runs["fp64"]) < 2e-6
