@@ -7,6 +7,8 @@
 
 int fr_euler2d_fp64(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
 int fr_euler2d_fp32k(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
+int fr_euler2d_met_fp64(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
+int fr_euler2d_met_fp32k(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
 
 namespace {
 // ---- FP64 reductions: conserved sums and CFL ---------------------------------
@@ -130,6 +132,10 @@ __global__ void __launch_bounds__(192) k_reduce_final(const double *__restrict__
 } // namespace
 
 int fr_launch_euler2d(frgpu_problem *p, int stage, const void *in, const void *din, void *out) {
+    if (p->d_met) {
+        if (p->d.precision == FRGPU_FP64) return fr_euler2d_met_fp64(p, stage, in, din, out);
+        return fr_euler2d_met_fp32k(p, stage, in, din, out);
+    }
     if (p->d.precision == FRGPU_FP64) return fr_euler2d_fp64(p, stage, in, din, out);
     return fr_euler2d_fp32k(p, stage, in, din, out);
 }

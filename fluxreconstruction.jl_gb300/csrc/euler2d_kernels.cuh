@@ -3,10 +3,11 @@
 // One launch evaluates the residual of example/shock-vortex.jl:26-118 (the
 // dudt! closure: volume flux :48-55, face interpolation :57-71, interface
 // Riemann flux :73-89, derivative :91-100, correction :102-115) on every
-// element and applies one Shu-Osher SSPRK3 stage update to it.  The state
-// never leaves the Julia layout u[i, j, k, l, m] (element index fastest), so a
-// warp of 32 consecutive elements reads every (k, l, m) plane with one
-// 128-byte (FP32) or 256-byte (FP64) coalesced transaction.
+// element and applies one Shu-Osher SSPRK3 stage update to it.  The state is
+// in the point-vector device layout (e2d_index: the 4 variables of a solution
+// point together, element index fastest within a point's plane), so a thread
+// moves a point with one 16-byte access and a warp of 32 consecutive elements
+// reads a point plane with one contiguous 512-byte (FP32) or 1 KB (FP64) access.
 //
 // CTA = TX x TY elements.  Thread (ex, ln, ey) is first an "x-line" thread
 // (element ex, row s = ln: it owns the NP points along r) and later a
@@ -41,6 +42,10 @@ template <class Real, int NP> struct E2DArgs {
     Real fixed[4][4];
     Ops<Real, NP> ops;
     int *status;
+    // per-point inverse Jacobian (a11, a12, a21, a22) in the device layout of
+    // the state (general quadrilaterals), or null for the uniform rectangles'
+    // diagonal iJx, iJy
+    const Real *met;
     // learned indicator fused into stage 3 (FP32K, np = 4): network, 1D inverse
     // Vandermonde factor, decision threshold / fallback band, plain-test S0 and
     // kappa, filter strength, V / iV of the filter, per-element flags and the
@@ -155,7 +160,10 @@ template <class Real> __device__ __forceinline__ void get4(const Real *p, int cs
 // FUSE: stage 3 of the FP32K form with np = 4 also runs the learned troubled-cell
 // indicator + :l2 filter on the elements it has just updated (the post-step
 // filter of example/shock-vortex.jl:308-321 with the network of mlp.cu).
-template <class Real, int NP, int FLUX, int MODE, int STAGE, bool FUSE = false>
+// MET: per-point metric a.met (f = a11 F + a12 G, g = a21 F + a22 G; the
+// corrections scale the interface fluxes by a11 and a22 at each point, as the
+// dudt! closure of example/shock-vortex.jl:48-55, :102-115 does with iJ[i, j][k, l]).
+template <class Real, int NP, int FLUX, int MODE, int STAGE, bool FUSE = false, bool MET = false>
 __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                                   sizeof(Real) == 4 && Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY <= 256 ? 3 : 1)
     k_euler2d(const E2DArgs<Real, NP> a) {
@@ -294,11 +302,26 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
 
     // ---- phase A: x-line (element ex, row l = ln) --------------------------
     Real rx[NP][4], fxl[4], fxr[4];
+    Real j11[MET ? NP : 1]; // MET: a11 at the row's points, for the x correction
     {
         const int l = ln;
         Real fx[NP][4], gy[NP][4];
+        if constexpr (MET) {
 #pragma unroll
-        for (int k = 0; k < NP; ++k) euler2d_flux<Real>(u[k], a.gm1, a.iJx, a.iJy, fx[k], gy[k], bad);
+            for (int k = 0; k < NP; ++k) {
+                Real F[4], G[4], mt[4] = {Real(0), Real(0), Real(0), Real(0)};
+                euler2d_flux<Real>(u[k], a.gm1, Real(1), Real(1), F, G, bad);
+                if (valid) ldg4(a.met + ((unsigned)(k + NP * l) * plane + e) * 4, mt);
+                v4_mul<Real>(F, mt[0], fx[k]);
+                v4_fma<Real>(G, mt[1], fx[k], fx[k]);
+                v4_mul<Real>(F, mt[2], gy[k]);
+                v4_fma<Real>(G, mt[3], gy[k], gy[k]);
+                j11[k] = mt[0];
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < NP; ++k) euler2d_flux<Real>(u[k], a.gm1, a.iJx, a.iJy, fx[k], gy[k], bad);
+        }
         Real tl[4], tr[4];
 #pragma unroll
         for (int k = 0; k < NP; ++k) v4_dotw<Real, NP>(fx, op.D[k], rx[k]);
@@ -395,10 +418,16 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             Real FL[4], FR[4], aL[4], aR[4];
             get4(&SFX(ey, l, 0, ex), CSF, FL);
             get4(&SFX(ey, l, 0, ex + 1), CSF, FR);
-            v4_fms<Real>(FL, a.iJx, fxl, aL);
-            v4_fms<Real>(FR, a.iJx, fxr, aR);
+            if constexpr (!MET) {
+                v4_fms<Real>(FL, a.iJx, fxl, aL);
+                v4_fms<Real>(FR, a.iJx, fxr, aR);
+            }
 #pragma unroll
             for (int kk = 0; kk < NP; ++kk) {
+                if constexpr (MET) {
+                    v4_fms<Real>(FL, j11[kk], fxl, aL);
+                    v4_fms<Real>(FR, j11[kk], fxr, aR);
+                }
                 Real g[4];
                 v4_fma<Real>(aL, op.dgl[kk], rx[kk], g);
                 v4_fma<Real>(aR, op.dgr[kk], g, g);
@@ -416,10 +445,18 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
         Real FB[4], FT[4], bB[4], bT[4];
         get4(&SFY(ey, k, 0, ex), CS, FB);
         get4(&SFY(ey + 1, k, 0, ex), CS, FT);
-        v4_fms<Real>(FB, a.iJy, gyb, bB);
-        v4_fms<Real>(FT, a.iJy, gyt, bT);
+        if constexpr (!MET) {
+            v4_fms<Real>(FB, a.iJy, gyb, bB);
+            v4_fms<Real>(FT, a.iJy, gyt, bT);
+        }
 #pragma unroll
         for (int l = 0; l < NP; ++l) {
+            if constexpr (MET) {
+                // a22 at point (k, l)
+                const Real j22 = __ldg(a.met + ((unsigned)(k + NP * l) * plane + e) * 4 + 3);
+                v4_fms<Real>(FB, j22, gyb, bB);
+                v4_fms<Real>(FT, j22, gyt, bT);
+            }
             // r = -du/dt at the NP points of row l, column k, all 4 variables
             Real r[4], res[4];
             get4(&SG(ey, l, k, 0, ex), CS, r);
@@ -571,7 +608,7 @@ template <class Real, int NP> Ops<Real, NP> make_ops(const frgpu_space &s) {
     return o;
 }
 
-template <class Real, int NP, int FLUX, int MODE, int STAGE, bool FUSE = false>
+template <class Real, int NP, int FLUX, int MODE, int STAGE, bool FUSE = false, bool MET = false>
 int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     using T = Tile<Real, NP>;
     using S = Smem<Real, NP, T::TX, T::TY, Stash<MODE, STAGE>::n>;
@@ -613,7 +650,8 @@ int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
         a.stats = p->d_count;
     }
     static_assert(S::bytes <= 227 * 1024, "shared memory per CTA exceeds 227 KB");
-    auto kern = k_euler2d<Real, NP, FLUX, MODE, STAGE, FUSE>;
+    a.met = MET ? (const Real *)p->d_met : nullptr;
+    auto kern = k_euler2d<Real, NP, FLUX, MODE, STAGE, FUSE, MET>;
     // the dynamic shared-memory opt-in is set once per instantiation (and on
     // every prepare pass, which precedes each graph capture)
     static bool attr_set = false;
@@ -630,13 +668,13 @@ int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     return FRGPU_OK;
 }
 
-template <class Real, int NP, int MODE>
+template <class Real, int NP, int MODE, bool MET>
 int dispatch_stage(frgpu_problem *p, int stage, const void *in, const void *din, void *out) {
     const int flux = p->d.flux == FRGPU_FLUX_HLL ? FLUX_HLL : FLUX_LF;
 #define FR_ST(S)                                                                                                   \
-    return flux == FLUX_HLL ? launch_t<Real, NP, FLUX_HLL, MODE, S>(p, in, din, out)                               \
-                            : launch_t<Real, NP, FLUX_LF, MODE, S>(p, in, din, out)
-    if constexpr (std::is_same<Real, float>::value && NP == 4 && MODE == MODE_FP32K) {
+    return flux == FLUX_HLL ? launch_t<Real, NP, FLUX_HLL, MODE, S, false, MET>(p, in, din, out)                   \
+                            : launch_t<Real, NP, FLUX_LF, MODE, S, false, MET>(p, in, din, out)
+    if constexpr (!MET && std::is_same<Real, float>::value && NP == 4 && MODE == MODE_FP32K) {
         if (stage == 3 && fr_fused_indicator(p))
             return flux == FLUX_HLL ? launch_t<Real, NP, FLUX_HLL, MODE, 3, true>(p, in, din, out)
                                     : launch_t<Real, NP, FLUX_LF, MODE, 3, true>(p, in, din, out);
@@ -652,14 +690,14 @@ int dispatch_stage(frgpu_problem *p, int stage, const void *in, const void *din,
     return FRGPU_ERR_ARG;
 }
 
-template <class Real, int MODE>
+template <class Real, int MODE, bool MET = false>
 int dispatch_np(frgpu_problem *p, int stage, const void *in, const void *din, void *out) {
     switch (p->sp.np) {
-    case 2: return dispatch_stage<Real, 2, MODE>(p, stage, in, din, out);
-    case 3: return dispatch_stage<Real, 3, MODE>(p, stage, in, din, out);
-    case 4: return dispatch_stage<Real, 4, MODE>(p, stage, in, din, out);
-    case 5: return dispatch_stage<Real, 5, MODE>(p, stage, in, din, out);
-    case 6: return dispatch_stage<Real, 6, MODE>(p, stage, in, din, out);
+    case 2: return dispatch_stage<Real, 2, MODE, MET>(p, stage, in, din, out);
+    case 3: return dispatch_stage<Real, 3, MODE, MET>(p, stage, in, din, out);
+    case 4: return dispatch_stage<Real, 4, MODE, MET>(p, stage, in, din, out);
+    case 5: return dispatch_stage<Real, 5, MODE, MET>(p, stage, in, din, out);
+    case 6: return dispatch_stage<Real, 6, MODE, MET>(p, stage, in, din, out);
     }
     fr_set_error("euler2d: polynomial degree must be 1..5");
     return FRGPU_ERR_UNSUPPORTED;

@@ -293,7 +293,7 @@ static void free_problem(frgpu_problem *p) {
     if (p->erk_gexec) cudaGraphExecDestroy(p->erk_gexec);
     void *bufs[] = {p->s0, p->s1, p->s2, p->s3, p->d_dt, p->d_status, p->d_red, p->d_flags, p->d_count,
                     p->d_velo, p->d_w, p->d_J, p->d_V, p->d_iV, p->rhs_in, p->rhs_out, p->d_bgk_prim,
-                    p->d_bgk_frag, p->d_stage, p->d_erk};
+                    p->d_bgk_frag, p->d_stage, p->d_erk, p->d_met};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -799,6 +799,44 @@ FRGPU_API int frgpu_positive_limiter(frgpu_problem *p, const double *weights, do
     FR_CUDA(cudaStreamSynchronize(p->stream));
     if (nlimited) *nlimited = n;
     return check_status(p);
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_problem_set_metric(frgpu_problem *p, const double *iJ) {
+    FR_REQ(p, "problem_set_metric: null problem");
+    FR_REQ(p->d.equation == FRGPU_EULER2D, "problem_set_metric: 2D Euler problems only");
+    FR_TRY
+    FR_CUDA(cudaStreamSynchronize(p->stream));
+    if (!iJ) {
+        if (p->d_met) cudaFree(p->d_met);
+        p->d_met = nullptr;
+    } else {
+        // host iJ[nx, ny, np, np, 2, 2] (column-major: blocks a11, a21, a12, a22)
+        // -> device (a11, a12, a21, a22) per point in the state's point-vector layout
+        const size_t ne = (size_t)p->sp.nx * p->sp.ny, nq = (size_t)p->sp.np * p->sp.np, blk = ne * nq;
+        const int from[4] = {0, 2, 1, 3};
+        std::vector<double> dev(4 * blk);
+        for (size_t q = 0; q < nq; ++q)
+            for (size_t e = 0; e < ne; ++e)
+                for (int m = 0; m < 4; ++m) {
+                    const double v = iJ[e + ne * q + blk * from[m]];
+                    if (!std::isfinite(v)) {
+                        fr_set_error("problem_set_metric: non-finite metric value");
+                        return FRGPU_ERR_ARG;
+                    }
+                    dev[(q * ne + e) * 4 + m] = v;
+                }
+        if (!p->d_met) FR_CUDA(cudaMalloc(&p->d_met, 4 * blk * p->esize));
+        if (p->esize == 8) {
+            FR_CUDA(cudaMemcpy(p->d_met, dev.data(), sizeof(double) * dev.size(), cudaMemcpyHostToDevice));
+        } else {
+            std::vector<float> f(dev.begin(), dev.end());
+            FR_CUDA(cudaMemcpy(p->d_met, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice));
+        }
+    }
+    p->graph_ind = -2; // force a re-capture
+    p->erk_dirty = true;
+    return FRGPU_OK;
     FR_CATCH
 }
 

@@ -295,6 +295,18 @@ class ODEProblem:
         self.f(du, u, self, t)
         return du
 
+    def set_metric(self, iJ) -> None:
+        """Per-point inverse Jacobian of general quadrilaterals (FRPSpace2D's
+        iJ[i, j][k, l], src/struct.jl:135-158) as an array [nx, ny, np, np, 2, 2];
+        None returns to the uniform rectangles."""
+        if iJ is None:
+            check(L.lib().frgpu_problem_set_metric(self._h, None))
+            return
+        a = np.asfortranarray(np.asarray(iJ, dtype=np.float64))
+        if a.shape != tuple(self.shape[:4]) + (2, 2):
+            raise ValueError("iJ must have shape (nx, ny, np, np, 2, 2)")
+        check(L.lib().frgpu_problem_set_metric(self._h, dptr(a)))
+
     def set_option(self, option: int, value: int) -> None:
         """Kernel choice for measurements (frgpu_problem_set_option), e.g.
         ``set_option(L.OPT_BGK_TENSOR, 0)`` for the CUDA-core BGK transport."""

@@ -633,9 +633,20 @@ static void rhs_euler2d(const fro_cfg *c, double *du, const double *u) {
                 for (int m = 0; m < 4; ++m) ww[m] = ue[(m * np + l) * np + k];
                 euler_flux_dir(ww, g, 0, F, NULL, NULL);
                 euler_flux_dir(ww, g, 1, G, NULL, NULL);
-                for (int m = 0; m < 4; ++m) {
-                    fv[(0 * 4 + m) * np * np + l * np + k] = c->iJx * F[m];
-                    fv[(1 * 4 + m) * np * np + l * np + k] = c->iJy * G[m];
+                if (c->iJ) {
+                    /* f = a11 F + a12 G, g = a21 F + a22 G (shock-vortex.jl:52) */
+                    const long nn = (long)nx * ny, blk = nn * np * np, at = ei + nn * (k + (long)np * l);
+                    const double a11 = c->iJ[at], a21 = c->iJ[at + blk], a12 = c->iJ[at + 2 * blk],
+                                 a22 = c->iJ[at + 3 * blk];
+                    for (int m = 0; m < 4; ++m) {
+                        fv[(0 * 4 + m) * np * np + l * np + k] = fma(G[m], a12, F[m] * a11);
+                        fv[(1 * 4 + m) * np * np + l * np + k] = fma(G[m], a22, F[m] * a21);
+                    }
+                } else {
+                    for (int m = 0; m < 4; ++m) {
+                        fv[(0 * 4 + m) * np * np + l * np + k] = c->iJx * F[m];
+                        fv[(1 * 4 + m) * np * np + l * np + k] = c->iJy * G[m];
+                    }
                 }
             }
         double *ff = w.fface + e * FS;
@@ -701,10 +712,16 @@ static void rhs_euler2d(const fro_cfg *c, double *du, const double *u) {
                     double fyb = w.fyi[(((long)j * nx + i) * np + k) * 4 + m];
                     double fyt = w.fyi[(((long)(j + 1) * nx + i) * np + k) * 4 + m];
                     /* the x and y correction terms added to the two derivatives */
-                    double aL = fxl * c->iJx - ff[(3 * np + l) * 4 + m];
-                    double aR = fxr * c->iJx - ff[(1 * np + l) * 4 + m];
-                    double bB = fyb * c->iJy - ff[(0 * np + k) * 4 + m];
-                    double bT = fyt * c->iJy - ff[(2 * np + k) * 4 + m];
+                    double ix = c->iJx, iy = c->iJy;
+                    if (c->iJ) { /* a11, a22 at point (k, l) */
+                        const long at = ei + nn * (k + (long)np * l), blk = nn * np * np;
+                        ix = c->iJ[at];
+                        iy = c->iJ[at + 3 * blk];
+                    }
+                    double aL = fxl * ix - ff[(3 * np + l) * 4 + m];
+                    double aR = fxr * ix - ff[(1 * np + l) * 4 + m];
+                    double bB = fyb * iy - ff[(0 * np + k) * 4 + m];
+                    double bT = fyt * iy - ff[(2 * np + k) * 4 + m];
                     double cx = fma(aR, c->dgr[k], fma(aL, c->dgl[k], r1));
                     double v = -fma(bT, c->dgr[l], fma(bB, c->dgl[l], cx + r2));
                     du[i + (long)nx * j + nn * (k + np * (l + (long)np * m))] = v;

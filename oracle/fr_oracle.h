@@ -63,6 +63,8 @@ typedef struct {
     double iJx, iJy;           /* 2D rectangular elements: 2/dx, 2/dy */
     const double *ll, *lr, *lpdm, *dgl, *dgr;
     const double *velo, *weights; /* BGK velocity grid */
+    const double *iJ;          /* 2D: per-point inverse Jacobian [nx, ny, np, np, 2, 2]
+                                  (column-major) or NULL for diag(iJx, iJy) */
 } fro_cfg;
 
 long fro_ndof(const fro_cfg *c);

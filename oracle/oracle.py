@@ -50,6 +50,7 @@ class Cfg(C.Structure):
         ("iJx", C.c_double), ("iJy", C.c_double),
         ("ll", _D), ("lr", _D), ("lpdm", _D), ("dgl", _D), ("dgr", _D),
         ("velo", _D), ("weights", _D),
+        ("iJ", _D),
     ]
 
 
@@ -290,6 +291,15 @@ class Problem:
         self.cfg = c
         self.space = space
         self.kind = kind
+
+    def set_metric(self, iJ) -> None:
+        """2D: per-point inverse Jacobian iJ[nx, ny, np, np, 2, 2] (None: diag(iJx, iJy))."""
+        if iJ is None:
+            self.cfg.iJ = None
+            return
+        a = np.asfortranarray(np.asarray(iJ, dtype=np.float64))
+        self._keep.append(a)
+        self.cfg.iJ = a.ctypes.data_as(_D)
 
     def shape(self):
         c = self.cfg
