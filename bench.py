@@ -382,6 +382,20 @@ def shock_vortex_entry(steps=100, warmup=5):
     secs = timer(lambda: itg.step(steps))
     out["learned_fp32k_with_limiter"] = {"value": ndof * 3 * steps / secs, "ms_per_step": secs / steps * 1e3,
                                          "limited_elements_at_start": nlim}
+    # the reference's own loop: Midpoint (shock-vortex.jl:294), limiter before
+    # and learned filter after every step; DOF updates counted per RK stage (2)
+    prob = learned.shock_vortex_problem(ps, 0.25, precision="fp32k")
+    itg = frgpu.init(prob, frgpu.Midpoint(), dt=dt)
+    frgpu._lib.check(frgpu.lib().frgpu_problem_set_mlp(prob._h, net._h, 0.5, 0.0))
+    itg.set_filter("mlp", learned.FILTER_LAMBDA, S0, learned.FILTER_KAPPA)
+    itg.set_limiter(True)
+    timer = _event_timer(torch.cuda.ExternalStream(itg.stream()))
+    itg.step(warmup)
+    itg.synchronize()
+    secs = timer(lambda: itg.step(steps))
+    out["learned_fp32k_midpoint_loop"] = {"value": ndof * 2 * steps / secs, "ms_per_step": secs / steps * 1e3,
+                                          "note": "Midpoint + positive_limiter + learned indicator, the loop of "
+                                                  "example/shock-vortex.jl:294-321; 2 RK stages per step"}
     ref = finals["plain_fp64"]
     for form in ("learned_fp32k", "plain_fp32k"):
         out[form]["rms_rho_diff_vs_plain_fp64"] = float(np.sqrt(np.mean((finals[form] - ref) ** 2)))
