@@ -207,6 +207,133 @@ __global__ void __launch_bounds__(128) k_limiter2d(Real *__restrict__ u, Real *_
     if (r > 0) atomicAdd(count, 1);
 }
 
+// FP32K 2D form with np <= 4, four lanes per element: lane l holds row l
+// (points k + np l).  Means, column-face traces and the minima are reduced
+// across the lane quad with shuffles; lane l tests the faces of row l and of
+// column l.  Same decisions as lim_element (sums in another order, FP32).
+template <int NP>
+__global__ void __launch_bounds__(128) k_limiter2d_rows(float *__restrict__ u, float *__restrict__ lo, size_t ne,
+                                                        const LimArgs<float> a, int *status, int *count) {
+    static_assert(NP <= 4, "four lanes per element");
+    const unsigned FULL = 0xffffffffu;
+    const int l = threadIdx.x & 3;
+    const size_t e = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 2;
+    const bool act = e < ne && l < NP;
+    const float g = a.gamma;
+    float v[NP][4];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        v[k][0] = v[k][1] = v[k][2] = v[k][3] = 0.f;
+        if (act) ld4(u + e2d_index(e, k + NP * l, 0, ne), v[k]);
+    }
+    auto qsum = [&](float x) {
+        x += __shfl_xor_sync(FULL, x, 1);
+        return x + __shfl_xor_sync(FULL, x, 2);
+    };
+    auto qmin = [&](float x) {
+        x = fminf(x, __shfl_xor_sync(FULL, x, 1));
+        return fminf(x, __shfl_xor_sync(FULL, x, 2));
+    };
+    // means
+    float um[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        float s = 0.f;
+#pragma unroll
+        for (int k = 0; k < NP; ++k) s = fmaf(v[k][m], act ? a.w[k + NP * l] : 0.f, s);
+        um[m] = qsum(s);
+    }
+    const float lm = lim_lambda<float, 4>(um, g);
+    const float pm = 0.5f * um[0] * (1.f / lm);
+    float eps = 1e-13f;
+    if (um[0] < eps) eps = um[0];
+    if (pm < eps) eps = pm;
+    // face points before the density scaling: left / right of row l (own),
+    // bottom / top of every column (quad sums), of which lane l keeps column l
+    float fL[4], fR[4], fB[4], fT[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        float sl = 0.f, sr = 0.f;
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+            sl = fmaf(v[k][m], a.ll[k], sl);
+            sr = fmaf(v[k][m], a.lr[k], sr);
+        }
+        fL[m] = sl;
+        fR[m] = sr;
+        fB[m] = fT[m] = 0.f;
+    }
+    const float wl = act ? a.ll[l] : 0.f, wr = act ? a.lr[l] : 0.f;
+    float rmin = INFINITY;
+#pragma unroll
+    for (int j = 0; j < NP; ++j)
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            const float b = qsum(v[j][m] * wl), t = qsum(v[j][m] * wr);
+            if (j == l) {
+                fB[m] = b;
+                fT[m] = t;
+            }
+            if (m == 0) rmin = fminf(rmin, fminf(b, t));
+        }
+    if (act) {
+        rmin = fminf(rmin, fminf(fL[0], fR[0]));
+#pragma unroll
+        for (int k = 0; k < NP; ++k) rmin = fminf(rmin, v[k][0]);
+    }
+    rmin = qmin(rmin);
+    float t1 = 1.f;
+    if (!(rmin >= eps + 1e-8f)) { // see lim_element
+        t1 = (um[0] - eps) / (um[0] - rmin + 1e-8f);
+        if (t1 > 1.f) t1 = 1.f;
+    }
+    // every lane of the warp takes part in the shuffles below: a failed
+    // element is flagged and left unchanged, not left early
+    const bool failed = !(t1 > 0.f);
+    if (failed) {
+        if (act && l == 0) atomicOr(status, ST_UNPHYSICAL);
+        t1 = 1.f;
+    }
+#pragma unroll
+    for (int k = 0; k < NP; ++k) v[k][0] = t1 * (v[k][0] - um[0]) + um[0];
+    float t2 = a.t0;
+    float found = 0.f;
+    if (act) {
+        const float *faces[4] = {fL, fR, fB, fT};
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+            float wf[4] = {faces[f][0], faces[f][1], faces[f][2], faces[f][3]};
+            if (lim_lambda<float, 4>(wf, g) < eps) {
+                t2 = fminf(t2, lim_t<float, 4>(wf, um, g, eps));
+                found = 1.f;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NP; ++k)
+            if (lim_lambda<float, 4>(v[k], g) < eps) {
+                t2 = fminf(t2, lim_t<float, 4>(v[k], um, g, eps));
+                found = 1.f;
+            }
+    }
+    t2 = qmin(t2);
+    found = -qmin(-found);
+    const bool fnd = found > 0.f;
+    if (failed || !(t1 < 1.f || (fnd && t2 < 1.f))) return; // after the last shuffle
+    if (fnd)
+#pragma unroll
+        for (int k = 0; k < NP; ++k)
+#pragma unroll
+            for (int m = 0; m < 4; ++m) v[k][m] = t2 * (v[k][m] - um[m]) + um[m];
+    if (!act) return;
+    const float z[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        st4(u + e2d_index(e, k + NP * l, 0, ne), v[k]);
+        if (lo) st4(lo + e2d_index(e, k + NP * l, 0, ne), z);
+    }
+    if (l == 0) atomicAdd(count, 1);
+}
+
 // 1D Euler, u[e + ne (q + np m)]
 template <class Real, int NP, bool FP32K>
 __global__ void __launch_bounds__(128) k_limiter1d(Real *__restrict__ u, Real *__restrict__ lo, size_t ne,
@@ -309,6 +436,19 @@ template <class Real, bool FP32K> int launch_np(frgpu_problem *p, const std::vec
     default: fr_set_error("positive_limiter: polynomial degree must be 1..5"); return FRGPU_ERR_UNSUPPORTED;      \
     }
     if (eq == FRGPU_EULER2D) {
+        if constexpr (FP32K) {
+            if (p->sp.np <= 4) {
+                const int g4 = (int)((4 * ne + 127) / 128);
+                switch (p->sp.np) {
+                case 2: k_limiter2d_rows<2><<<g4, 128, 0, p->stream>>>(u, lo, ne, a, p->d_status, cnt); break;
+                case 3: k_limiter2d_rows<3><<<g4, 128, 0, p->stream>>>(u, lo, ne, a, p->d_status, cnt); break;
+                default: k_limiter2d_rows<4><<<g4, 128, 0, p->stream>>>(u, lo, ne, a, p->d_status, cnt); break;
+                }
+                FR_CUDA(cudaGetLastError());
+                p->launches += 1;
+                return FRGPU_OK;
+            }
+        }
         FR_LIM_NP(k_limiter2d)
     } else if (eq == FRGPU_EULER1D) {
         FR_LIM_NP(k_limiter1d)
