@@ -46,6 +46,11 @@ template <class Real, int NP> struct E2DArgs {
     // the state (general quadrilaterals), or null for the uniform rectangles'
     // diagonal iJx, iJy
     const Real *met;
+    // stage coefficients of the method (SSPRK3: c1 = 1, fa = 1, fs = 2/3,
+    // g = 2, al = 2, be = 1, s3 = 1/3; two-stage methods use stages 1 and 3):
+    // stage 1: FP64 u1 = u + c1 dt L(u), FP32K d1 = c1 dt L(u); stage 3 (last):
+    // FP64 (g dt L + al u_s + be u^n) s3, FP32K d = (fa d_prev + dt L) fs
+    Real c1, fa, fs, g3, al3, be3, s3;
     // learned indicator fused into stage 3 (FP32K, np = 4): network, 1D inverse
     // Vandermonde factor, decision threshold / fallback band, plain-test S0 and
     // kappa, filter strength, V / iV of the filter, per-element flags and the
@@ -476,11 +481,11 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                 for (int m = 0; m < 4; ++m) {
                     const Real du = -r[m], ui = ui4[m];
                     if (STAGE == 1) {
-                        res[m] = fmaR<Real>(dt, du, ui);
+                        res[m] = fmaR<Real>(a.c1 * dt, du, ui);
                     } else if (STAGE == 2) {
                         res[m] = (fmaR<Real>(dt, du, fmaR<Real>(Real(3), un4[m], ui))) * Real(0.25);
                     } else {
-                        res[m] = fmaR<Real>(Real(2) * dt, du, fmaR<Real>(Real(2), ui, un4[m])) * Real(1.0 / 3.0);
+                        res[m] = fmaR<Real>(a.g3 * dt, du, fmaR<Real>(a.al3, ui, a.be3 * un4[m])) * a.s3;
                     }
                 }
                 st4(a.out + at, res);
@@ -490,7 +495,7 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                 // compensated (Kahan/Fast2Sum) sum whose low part persists.
                 // dt du = (-dt) r exactly.
                 if (STAGE == 1) {
-                    v4_mul<Real>(r, -dt, res);
+                    v4_mul<Real>(r, -(a.c1 * dt), res);
                 } else if (STAGE == 2) {
                     Real d1[4];
                     ldg4(din + at, d1);
@@ -501,8 +506,9 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                     ldg4(din + at, d2);
                     ldg4(uin + at, hi);
                     ld4(a.ul + at, lo);
+                    if (a.fa != Real(1)) v4_mul<Real>(d2, a.fa, d2);
                     v4_fma<Real>(r, -dt, d2, y);
-                    v4_mul<Real>(y, Real(2.0 / 3.0), y); // d3
+                    v4_mul<Real>(y, a.fs, y); // d3
                     v4_add<Real>(y, lo, y);               // y = d3 + lo
                     v4_add<Real>(hi, y, res);             // t = hi + y
                     v4_sub<Real>(res, hi, c);
@@ -651,6 +657,13 @@ int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     }
     static_assert(S::bytes <= 227 * 1024, "shared memory per CTA exceeds 227 KB");
     a.met = MET ? (const Real *)p->d_met : nullptr;
+    a.c1 = (Real)p->meth.c1;
+    a.fa = (Real)p->meth.fa;
+    a.fs = (Real)p->meth.fs;
+    a.g3 = (Real)p->meth.g3;
+    a.al3 = (Real)p->meth.al3;
+    a.be3 = (Real)p->meth.be3;
+    a.s3 = (Real)p->meth.s3;
     auto kern = k_euler2d<Real, NP, FLUX, MODE, STAGE, FUSE, MET>;
     // the dynamic shared-memory opt-in is set once per instantiation (and on
     // every prepare pass, which precedes each graph capture)

@@ -23,6 +23,19 @@ struct frgpu_space {
 
 // Device buffers of a problem.  FP64: s0 = u^n, s1/s2 = stage states.
 // FP32K: s0 = u^n high part, s1/s2 = stage increments d1/d2, s3 = low part.
+// Stage coefficients of the fused step (stages 1..3 of the 2D Euler kernel):
+// SSPRK3, or a two-stage explicit method run as stages 1 and 3.
+struct fr_method {
+    int stages = 3;
+    double c1 = 1.0;                                  // stage 1 scale of dt L
+    double fa = 1.0, fs = 2.0 / 3.0;                  // FP32K last stage: (fa d + dt L) fs
+    double g3 = 2.0, al3 = 2.0, be3 = 1.0, s3 = 1.0 / 3.0; // FP64 last stage: (g3 dt L + al3 u_s + be3 u^n) s3
+    bool operator==(const fr_method &o) const {
+        return stages == o.stages && c1 == o.c1 && fa == o.fa && fs == o.fs && g3 == o.g3 && al3 == o.al3 &&
+               be3 == o.be3 && s3 == o.s3;
+    }
+};
+
 struct frgpu_problem {
     frgpu_space sp;
     frgpu_problem_desc d{};
@@ -52,6 +65,8 @@ struct frgpu_problem {
     float mlp_thr = 0.5f, mlp_band = 0.0f;
     int bgk_tensor = 1;             // FP32 BGK transport on the tensor cores
     int fuse_indicator = 1;         // FP32K 2D: learned indicator inside stage 3
+    int fuse_erk = 1;               // 2D Euler: two-stage tableaux fused into the stage kernel
+    fr_method meth;                 // coefficients of the fused step
     int limiter = 0;                // positivity-preserving limiter before every step
     double lim_t0 = 1.0;            // its t0 (cap of the energy scaling)
     std::vector<double> lim_w;      // its element weights

@@ -347,14 +347,17 @@ static int launch_stage(frgpu_problem *p, int stage, const void *in, const void 
 static int enqueue_step(frgpu_problem *p) {
     int rc;
     if (p->limiter && (rc = fr_launch_limiter(p, p->lim_w, p->lim_t0))) return rc;
+    const bool two = p->meth.stages == 2; // stages 1 and 3 only (2D Euler)
     if (p->d.precision == FRGPU_FP64) {
         if ((rc = launch_stage(p, 1, p->s0, nullptr, p->s1))) return rc;
-        if ((rc = launch_stage(p, 2, p->s1, nullptr, p->s2))) return rc;
-        if ((rc = launch_stage(p, 3, p->s2, nullptr, p->s0))) return rc;
+        if (!two && (rc = launch_stage(p, 2, p->s1, nullptr, p->s2))) return rc;
+        if ((rc = launch_stage(p, 3, two ? p->s1 : p->s2, nullptr, p->s0))) return rc;
     } else {
+        // the last stage reads its increment from s2 and writes the new high
+        // part into the other buffer
         void *hi = fr_state_hi(p), *tmp = fr_state_tmp(p);
-        if ((rc = launch_stage(p, 1, hi, nullptr, tmp))) return rc;
-        if ((rc = launch_stage(p, 2, hi, tmp, p->s2))) return rc;
+        if ((rc = launch_stage(p, 1, hi, nullptr, two ? p->s2 : tmp))) return rc;
+        if (!two && (rc = launch_stage(p, 2, hi, tmp, p->s2))) return rc;
         if ((rc = launch_stage(p, 3, hi, p->s2, tmp))) return rc;
     }
     if (p->indicator != FRGPU_IND_NONE && !fr_fused_indicator(p)) {
@@ -621,15 +624,8 @@ FRGPU_API int frgpu_rhs(frgpu_problem *p, double *du, const double *u, double t)
     FR_CATCH
 }
 
-FRGPU_API int frgpu_step_ssprk3(frgpu_problem *p, double dt, int nsteps) {
-    FR_REQ(p, "step_ssprk3: null problem");
-    FR_REQ(nsteps >= 0, "step_ssprk3: negative step count");
-    if (!(dt > 0.0) || !std::isfinite(dt)) {
-        fr_set_error("step_ssprk3: dt must be positive and finite");
-        return FRGPU_ERR_DT;
-    }
-    if (nsteps == 0) return FRGPU_OK;
-    FR_TRY
+// Replay nsteps fused steps of the problem's method (p->meth) from the step graphs.
+static int run_fused_steps(frgpu_problem *p, double dt, int nsteps) {
     if (dt != p->host_dt) {
         FR_CUDA(cudaMemcpyAsync(p->d_dt, &dt, sizeof(double), cudaMemcpyHostToDevice, p->stream));
         FR_CUDA(cudaStreamSynchronize(p->stream));
@@ -646,6 +642,26 @@ FRGPU_API int frgpu_step_ssprk3(frgpu_problem *p, double dt, int nsteps) {
         p->launches += p->graph_launches;
     }
     return check_status(p);
+}
+
+static void use_method(frgpu_problem *p, const fr_method &m) {
+    if (!(m == p->meth)) {
+        p->meth = m;
+        p->graph_ind = -2; // re-capture the step graphs
+    }
+}
+
+FRGPU_API int frgpu_step_ssprk3(frgpu_problem *p, double dt, int nsteps) {
+    FR_REQ(p, "step_ssprk3: null problem");
+    FR_REQ(nsteps >= 0, "step_ssprk3: negative step count");
+    if (!(dt > 0.0) || !std::isfinite(dt)) {
+        fr_set_error("step_ssprk3: dt must be positive and finite");
+        return FRGPU_ERR_DT;
+    }
+    if (nsteps == 0) return FRGPU_OK;
+    FR_TRY
+    use_method(p, fr_method());
+    return run_fused_steps(p, dt, nsteps);
     FR_CATCH
 }
 
@@ -662,6 +678,22 @@ FRGPU_API int frgpu_step_erk(frgpu_problem *p, int s, const double *A, const dou
     }
     if (nsteps == 0) return FRGPU_OK;
     FR_TRY
+    // two-stage methods on the 2D Euler problem run fused into the stage kernel
+    // (stages 1 and 3 with the method's coefficients, see fr_method)
+    if (p->d.equation == FRGPU_EULER2D && s == 2 && A[2] != 0.0 && b[1] != 0.0 && p->fuse_erk) {
+        const double a21 = A[2], b1 = b[0], b2 = b[1];
+        fr_method m;
+        m.stages = 2;
+        m.c1 = a21;
+        m.fa = b1 / (a21 * b2);
+        m.fs = b2;
+        m.g3 = b2;
+        m.al3 = b1 / a21;
+        m.be3 = 1.0 - b1 / a21;
+        m.s3 = 1.0;
+        use_method(p, m);
+        return run_fused_steps(p, dt, nsteps);
+    }
     if (dt != p->host_dt) {
         FR_CUDA(cudaMemcpyAsync(p->d_dt, &dt, sizeof(double), cudaMemcpyHostToDevice, p->stream));
         FR_CUDA(cudaStreamSynchronize(p->stream));
@@ -760,9 +792,12 @@ FRGPU_API int frgpu_set_filter(frgpu_problem *p, int indicator, double lam, doub
 
 FRGPU_API int frgpu_problem_set_option(frgpu_problem *p, int option, int value) {
     FR_REQ(p, "set_option: null problem");
-    FR_REQ(option == FRGPU_OPT_BGK_TENSOR || option == FRGPU_OPT_FUSED_INDICATOR, "set_option: unknown option");
+    FR_REQ(option == FRGPU_OPT_BGK_TENSOR || option == FRGPU_OPT_FUSED_INDICATOR ||
+               option == FRGPU_OPT_FUSED_TWO_STAGE,
+           "set_option: unknown option");
     if (option == FRGPU_OPT_BGK_TENSOR) p->bgk_tensor = value != 0;
     if (option == FRGPU_OPT_FUSED_INDICATOR) p->fuse_indicator = value != 0;
+    if (option == FRGPU_OPT_FUSED_TWO_STAGE) p->fuse_erk = value != 0;
     p->graph_ind = -2; // force a re-capture
     p->erk_dirty = true;
     return FRGPU_OK;

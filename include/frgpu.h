@@ -58,7 +58,7 @@ enum frgpu_bc {
 };
 enum frgpu_correction { FRGPU_RADAU = 0, FRGPU_SD = 1, FRGPU_HUYNH = 2 };
 enum frgpu_indicator { FRGPU_IND_NONE = 0, FRGPU_IND_PLAIN = 1, FRGPU_IND_MLP = 2 };
-enum frgpu_option { FRGPU_OPT_BGK_TENSOR = 1, FRGPU_OPT_FUSED_INDICATOR = 2 };
+enum frgpu_option { FRGPU_OPT_BGK_TENSOR = 1, FRGPU_OPT_FUSED_INDICATOR = 2, FRGPU_OPT_FUSED_TWO_STAGE = 3 };
 
 typedef struct frgpu_space frgpu_space;
 typedef struct frgpu_problem frgpu_problem;
@@ -197,7 +197,11 @@ FRGPU_API int frgpu_troubled_flags(frgpu_problem *p, int *flags, long n);
  * tensor-core product, 0 on the CUDA cores.
  * FRGPU_OPT_FUSED_INDICATOR: 1 (default) runs the learned indicator + filter of
  * an FP32K deg-3 2D Euler problem inside its third SSPRK3 stage, 0 as a kernel
- * of its own after the step.  The next step re-captures its graph. */
+ * of its own after the step.
+ * FRGPU_OPT_FUSED_TWO_STAGE: 1 (default) runs two-stage tableaux of
+ * frgpu_step_erk (Midpoint, Heun, ...) on a 2D Euler problem fused into the
+ * stage kernel, 0 through the generic residual + combination kernels.
+ * The next step re-captures its graph. */
 FRGPU_API int frgpu_problem_set_option(frgpu_problem *p, int option, int value);
 /* Device pointer to the primary state array and its element type size
  * (8 for FP64, 4 for FP32K), for zero-copy hand-off; the stream the problem's

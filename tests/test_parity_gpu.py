@@ -649,3 +649,37 @@ def test_metric_general_matches_oracle(frgpu, oracle, flux):
     prob.set_metric(None)
     P.set_metric(None)
     assert rel(prob.rhs(u), P.rhs(u)) < RTOL64
+
+
+@pytest.mark.parametrize("name", ["Midpoint", "Heun", "Ralston"])
+def test_two_stage_tableaux_fused_into_the_stage_kernel(frgpu, oracle, name):
+    """Two-stage tableaux on the 2D Euler problem run as stages 1 and 3 of the
+    fused kernel: FP64 against the generic residual + combination path (the
+    Midpoint rule bit for bit) and the oracle; FP32K within FP32 rounding."""
+    from frgpu import _lib as L
+
+    alg = getattr(frgpu, name)()
+    ps = frgpu.FRPSpace2D(0, 1, 24, 0, 1, 16, 3)
+    po = oracle_space2d(ps, 0, 1, 24, 0, 1, 16, 3)
+    u = wave2d(ps.xpg)
+    dt = 1e-4
+    runs = {}
+    for fused in (1, 0):
+        prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf", bc="period")
+        prob.set_option(L.OPT_FUSED_TWO_STAGE, fused)
+        itg = frgpu.init(prob, alg, dt=dt)
+        itg.step(4)
+        runs[fused] = itg.u
+    if name == "Midpoint":
+        assert np.array_equal(runs[1], runs[0])
+    assert rel(runs[1], runs[0]) < RTOL64
+    P = oracle.Problem(oracle.EULER2D, po, gamma=1.4, flux=oracle.FLUX_LF)
+    assert rel(runs[1], P.erk(u, dt, 4, alg.A, alg.b)) < RTOL64
+    prob32 = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf", bc="period", precision="fp32k")
+    itg32 = frgpu.init(prob32, alg, dt=dt)
+    itg32.step(4)
+    itg32.alg = None
+    itg32.step(2)                      # back to SSPRK3 on the same problem
+    itg64 = frgpu.init(frgpu.FREuler2DProblem(runs[1], (0, 1), ps, 1.4, flux="lf", bc="period"), dt=dt)
+    itg64.step(2)
+    assert rel(itg32.u, itg64.u) < 2e-6
