@@ -213,7 +213,21 @@ struct ExplicitRK
 end
 Midpoint() = ExplicitRK([0.0 0.0; 0.5 0.0], [0.0, 1.0])     # as example/shock-vortex.jl:294 uses it
 Heun() = ExplicitRK([0.0 0.0; 1.0 0.0], [0.5, 0.5])
+Ralston() = ExplicitRK([0.0 0.0; 2 / 3 0.0], [0.25, 0.75])
+SSPRK22() = ExplicitRK([0.0 0.0; 1.0 0.0], [0.5, 0.5])
 RK4() = ExplicitRK([0 0 0 0; 0.5 0 0 0; 0 0.5 0 0; 0 0 1 0], [1 / 6, 1 / 3, 1 / 3, 1 / 6])
+"""Tsitouras 5(4) pair (Comput. Math. Appl. 62 (2011) 770-775), fifth-order weights, fixed dt."""
+function Tsit5()
+    A = zeros(7, 7)
+    A[2, 1] = 0.161
+    A[3, 1:2] = [-0.008480655492356989, 0.335480655492357]
+    A[4, 1:3] = [2.897153057105493, -6.359448489975075, 4.3622954328695815]
+    A[5, 1:4] = [5.325864828439257, -11.748883564062828, 7.4955393428898365, -0.09249506636175525]
+    A[6, 1:5] = [5.86145544294642, -12.92096931784711, 8.159367898576159, -0.071584973281401, -0.028269050394068383]
+    A[7, 1:6] = [0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081,
+                 2.324710524099774]
+    return ExplicitRK(A, [A[7, 1:6]; 0.0])
+end
 
 mutable struct Integrator
     p::Problem
