@@ -116,3 +116,22 @@ def test_compute_fails_loudly_without_gpu(frgpu, has_gpu):
     with pytest.raises(frgpu.FRGPUError):
         fd = np.zeros((4, 2))
         frgpu.interp_face_(fd, np.ones((4, 3)), ps.ll, ps.lr)
+
+
+def test_new_entry_points_reject_bad_arguments(frgpu):
+    """Argument checks of the limiter, tableau and metric entry points run
+    before any device work."""
+    from frgpu import _lib
+
+    L = _lib.lib()
+    n = C.c_int(0)
+    A = np.array([[0.0, 0.0], [0.5, 0.0]])
+    b = np.array([0.0, 1.0])
+    assert L.frgpu_positive_limiter(None, None, 1.0, C.byref(n)) == _lib.ERR_ARG
+    assert L.frgpu_set_limiter(None, 1, None, 1.0) == _lib.ERR_ARG
+    assert L.frgpu_step_erk(None, 2, _lib.dptr(A), _lib.dptr(b), 0.1, 1) == _lib.ERR_ARG
+    assert L.frgpu_problem_set_metric(None, None) == _lib.ERR_ARG
+    assert "null" in _lib.last_error()
+    with pytest.raises(ValueError):
+        frgpu.ExplicitRK([[0.0, 0.5], [0.0, 0.0]], [0.5, 0.5])   # implicit entry above the diagonal
+    assert frgpu.Midpoint().A[1, 0] == 0.5 and frgpu.Tsit5().b[-1] == 0.0
