@@ -683,3 +683,33 @@ def test_two_stage_tableaux_fused_into_the_stage_kernel(frgpu, oracle, name):
     itg64 = frgpu.init(frgpu.FREuler2DProblem(runs[1], (0, 1), ps, 1.4, flux="lf", bc="period"), dt=dt)
     itg64.step(2)
     assert rel(itg32.u, itg64.u) < 2e-6
+
+
+def test_erk_bgk_and_euler1d_match_oracle(frgpu, oracle):
+    """The generic Runge-Kutta path on the kinetic (BGK) and 1D Euler problems:
+    Heun and RK4 against the oracle, FP64."""
+    ne, nv, deg = 32, 48, 3
+    ps = frgpu.FRPSpace1D(0, 1, ne, deg)
+    po = oracle_space1d(ps, 0, 1, ne, deg)
+    dv = 16 / nv
+    v = -8 + (np.arange(nv) + 0.5) * dv
+    w = np.full(nv, dv)
+    rho = 1 + 0.1 * np.sin(2 * np.pi * ps.xpg)
+    f = np.zeros((ne, nv, deg + 1), order="F")
+    for k in range(deg + 1):
+        f[:, :, k] = rho[:, k, None] * np.sqrt(1 / np.pi) * np.exp(-(v[None, :] - 1) ** 2)
+    heun = frgpu.Heun()
+    dt = 0.1 * (1 / ne) / 8
+    itg = frgpu.init(frgpu.FRBGKProblem(f, (0, 1), ps, v, w, 1e-2), heun, dt=dt)
+    itg.step(6)
+    P = oracle.Problem(oracle.BGK1D, po, tau=1e-2, velo=v, weights=w)
+    assert rel(itg.u, P.erk(f, dt, 6, heun.A, heun.b)) < RTOL64
+    x = np.asarray(ps.xpg)
+    u = np.zeros(x.shape + (3,), order="F")
+    r = 1 + 0.2 * np.sin(2 * np.pi * x)
+    u[..., 0], u[..., 1], u[..., 2] = r, r, 1 / 0.4 + 0.5 * r
+    rk4 = frgpu.RK4()
+    itg1 = frgpu.init(frgpu.FREulerProblem(u, (0, 1), ps, 1.4, bc="period"), rk4, dt=1e-4)
+    itg1.step(5)
+    P1 = oracle.Problem(oracle.EULER1D, po, gamma=1.4, flux=oracle.FLUX_HLL, bc=oracle.BC_PERIODIC)
+    assert rel(itg1.u, P1.erk(u, 1e-4, 5, rk4.A, rk4.b)) < RTOL64
