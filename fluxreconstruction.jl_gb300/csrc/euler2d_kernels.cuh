@@ -477,6 +477,10 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                 Real ui4[4], un4[4];
                 get4(&SU(ey, l, k, 0, ex), CS, ui4);
                 if (STAGE >= 2) get4(&SST(0, ey, l, k, 0, ex), CS, un4);
+                if (STAGE == 3 && a.be3 != Real(1)) { // two-stage methods other than Midpoint
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) un4[m] *= a.be3;
+                }
 #pragma unroll
                 for (int m = 0; m < 4; ++m) {
                     const Real du = -r[m], ui = ui4[m];
@@ -485,7 +489,7 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                     } else if (STAGE == 2) {
                         res[m] = (fmaR<Real>(dt, du, fmaR<Real>(Real(3), un4[m], ui))) * Real(0.25);
                     } else {
-                        res[m] = fmaR<Real>(a.g3 * dt, du, fmaR<Real>(a.al3, ui, a.be3 * un4[m])) * a.s3;
+                        res[m] = fmaR<Real>(a.g3 * dt, du, fmaR<Real>(a.al3, ui, un4[m])) * a.s3;
                     }
                 }
                 st4(a.out + at, res);

@@ -178,14 +178,18 @@ FRGPU_API int frgpu_modal_filter(frgpu_problem *p, int indicator, double lam, do
  * reference's assertion).  Closed-form energy parameter and min(t_j, t0):
  * see csrc/limiter.cu. */
 FRGPU_API int frgpu_positive_limiter(frgpu_problem *p, const double *weights, double t0, int *nlimited);
-/* General quadrilaterals (FRPSpace2D's per-point inverse Jacobian iJ[i, j][k, l],
+/* Per-point metric (FRPSpace2D's inverse Jacobian iJ[i, j][k, l],
  * src/struct.jl:135-158): iJ as a host array [nx, ny, np, np, 2, 2] (column-major,
  * the 2 x 2 matrices last).  The residual then takes f = a11 F + a12 G and
  * g = a21 F + a22 G at every solution point and scales the interface fluxes of
  * the corrections by a11 (x faces) and a22 (y faces) at each point, as the dudt!
- * closure of example/shock-vortex.jl:48-55, :102-115 does.  NULL returns to the
- * uniform rectangles of the space (iJ = diag(2/dx, 2/dy)); 2D Euler only.  The
- * learned indicator then runs as its own kernel after the step. */
+ * closure of example/shock-vortex.jl:48-55, :102-115 does.  That formula is
+ * exact for rectangles of different sizes (a diagonal metric constant within
+ * each element, e.g. stretched meshes); with off-diagonal terms or a metric
+ * varying inside an element it is the reference's formula as it stands, which
+ * does not keep a uniform state.  NULL returns to the uniform rectangles of the
+ * space (iJ = diag(2/dx, 2/dy)); 2D Euler only.  The learned indicator then runs
+ * as its own kernel after the step. */
 FRGPU_API int frgpu_problem_set_metric(frgpu_problem *p, const double *iJ);
 /* Run the limiter before every step of frgpu_step_ssprk3 (the loop of
  * example/shock-vortex.jl:297-303); on = 0 turns it off. */

@@ -333,3 +333,36 @@ def test_oracle_erk_reproduces_ssprk3_and_rk4(oracle):
     k4 = pr.rhs(u0 + dt * k3)
     want = u0 + dt * (k1 + 2 * k2 + 2 * k3 + k4) / 6
     assert np.max(np.abs(pr.erk(u0, dt, 1, A4, b4) - want)) < 1e-13
+
+
+def test_euler2d_metric_free_stream_and_diagonal(oracle):
+    """The 2D residual with a per-point metric (dudt! of example/shock-vortex.jl
+    with iJ[i, j][k, l]): a uniform state stays put on rectangles of different
+    sizes (a diagonal metric constant within each element, varying between
+    elements), and the rectangles' own diag(2/dx, 2/dy) gives the same bits as
+    the uniform path.  (dudt! scales the interface fluxes by iJ11 and iJ22
+    only, so with off-diagonal terms or a metric varying inside an element the
+    formula it defines does not keep a uniform state; that is the reference's
+    formula, reproduced as it is.)"""
+    O = oracle
+    sp = O.Space2D(0, 1, 5, 0, 1, 4, 3)
+    pr = O.Problem(O.EULER2D, sp, gamma=1.4, flux=O.FLUX_HLL)
+    shape = (5, 4, 4, 4)
+    u = np.zeros(shape + (4,), order="F")
+    u[..., 0], u[..., 1], u[..., 2], u[..., 3] = 1.2, 0.3, -0.2, 2.9
+    iJ = np.zeros(shape + (2, 2), order="F")
+    ix = 10.0 * (1 + 0.3 * np.arange(5))[:, None, None, None]
+    iy = 8.0 * (1 + 0.2 * np.arange(4))[None, :, None, None]
+    iJ[..., 0, 0], iJ[..., 1, 1] = ix + 0 * iJ[..., 0, 0], iy + 0 * iJ[..., 1, 1]
+    pr.set_metric(iJ)
+    assert np.max(np.abs(pr.rhs(u))) < 1e-12
+    iJ[..., 0, 1] = 1.5          # off-diagonal: dudt!'s formula moves a uniform state
+    pr.set_metric(iJ)
+    assert np.max(np.abs(pr.rhs(u))) > 1e-3
+    rng = np.random.default_rng(5)
+    w = u + 0.05 * rng.standard_normal(u.shape)
+    iJ[..., 0, 0], iJ[..., 1, 1], iJ[..., 0, 1], iJ[..., 1, 0] = sp.iJx, sp.iJy, 0.0, 0.0
+    pr.set_metric(iJ)
+    r_met = pr.rhs(w)
+    pr.set_metric(None)
+    assert np.array_equal(r_met, pr.rhs(w))
