@@ -46,6 +46,11 @@ template <class Real, int NP> struct E2DArgs {
     // the state (general quadrilaterals), or null for the uniform rectangles'
     // diagonal iJx, iJy
     const Real *met;
+    // MET with face normals (straight-sided quadrilaterals, the formulation of
+    // dev/parallelogram.jl): unit normal (nx, ny) of x face (i, j) at
+    // nfx[2 (i + (nx + 1) j)], of y face (i, j) at nfy[2 (i + nx j)]; null: the
+    // Cartesian axes with the dudt! scaling by a11 / a22
+    const Real *nfx, *nfy;
     // stage coefficients of the method (SSPRK3: c1 = 1, fa = 1, fs = 2/3,
     // g = 2, al = 2, be = 1, s3 = 1/3; two-stage methods use stages 1 and 3):
     // stage 1: FP64 u1 = u + c1 dt L(u), FP32K d1 = c1 dt L(u); stage 3 (last):
@@ -216,6 +221,29 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
     const Ops<Real, NP> &op = a.ops;
     int bad = 0;
 
+    // interface flux across x face (fi, fj) / y face (fi, fj): rotated into the
+    // face frame when the problem has face normals, else along the axis
+    const auto xflux = [&](const Real (&wL)[4], const Real (&wR)[4], int fi, int fj, Real (&F)[4]) {
+        if constexpr (MET) {
+            if (a.nfx != nullptr) {
+                const Real *n = a.nfx + 2 * ((unsigned)fi + (unsigned)(nx + 1) * fj);
+                riemann_n<Real, FLUX>(wL, wR, n[0], n[1], a.gamma, a.gm1, F);
+                return;
+            }
+        }
+        riemann2d<Real, 0, FLUX>(wL, wR, a.gamma, a.gm1, F);
+    };
+    const auto yflux = [&](const Real (&wL)[4], const Real (&wR)[4], int fi, int fj, Real (&F)[4]) {
+        if constexpr (MET) {
+            if (a.nfy != nullptr) {
+                const Real *n = a.nfy + 2 * ((unsigned)fi + (unsigned)nx * fj);
+                riemann_n<Real, FLUX>(wL, wR, n[0], n[1], a.gamma, a.gm1, F);
+                return;
+            }
+        }
+        riemann2d<Real, 1, FLUX>(wL, wR, a.gamma, a.gm1, F);
+    };
+
     // ---- phase A loads, issued before the halo so that both are in flight ----
     const int i = i0 + ex, j = j0 + ey;
     const unsigned e = (unsigned)i + (unsigned)nx * j;
@@ -307,7 +335,6 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
 
     // ---- phase A: x-line (element ex, row l = ln) --------------------------
     Real rx[NP][4], fxl[4], fxr[4];
-    Real j11[MET ? NP : 1]; // MET: a11 at the row's points, for the x correction
     {
         const int l = ln;
         Real fx[NP][4], gy[NP][4];
@@ -321,7 +348,6 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                 v4_fma<Real>(G, mt[1], fx[k], fx[k]);
                 v4_mul<Real>(F, mt[2], gy[k]);
                 v4_fma<Real>(G, mt[3], gy[k], gy[k]);
-                j11[k] = mt[0];
             }
         } else {
 #pragma unroll
@@ -373,7 +399,7 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             if (ex > 0) get4(&STR(s_uxr, ey, l, 0, ex - 1), CS, wL);
             else get4(&SHX(0, ey, l, 0), CSX, wL);
             get4(&STR(s_uxl, ey, l, 0, ex), CS, wR);
-            riemann2d<Real, 0, FLUX>(wL, wR, a.gamma, a.gm1, F);
+            xflux(wL, wR, i, j, F);
             put4(&SFX(ey, l, 0, ex), CSF, F);
         }
         // the TY * NP faces on the tile's right edge, by the first threads of
@@ -385,7 +411,7 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                 Real wL[4], wR[4], F[4];
                 get4(&STR(s_uxr, ye, le, 0, vx - 1), CS, wL);
                 get4(&SHX(1, ye, le, 0), CSX, wR);
-                riemann2d<Real, 0, FLUX>(wL, wR, a.gamma, a.gm1, F);
+                xflux(wL, wR, i0 + vx, j0 + ye, F);
                 put4(&SFX(ye, le, 0, vx), CSF, F);
             }
         }
@@ -410,12 +436,12 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             Real wL[4], wR[4], F[4];
             get4(ey > 0 ? &STR(s_uyt, ey - 1, k, 0, ex) : &SHY(0, k, 0, ex), CS, wL);
             get4(&STR(s_uyb, ey, k, 0, ex), CS, wR);
-            riemann2d<Real, 1, FLUX>(wL, wR, a.gamma, a.gm1, F);
+            yflux(wL, wR, i, j, F);
             put4(&SFY(ey, k, 0, ex), CS, F);
             if (ey == vy - 1) {
                 get4(&STR(s_uyt, ey, k, 0, ex), CS, wL);
                 get4(&SHY(1, k, 0, ex), CS, wR);
-                riemann2d<Real, 1, FLUX>(wL, wR, a.gamma, a.gm1, F);
+                yflux(wL, wR, i, j + 1, F);
                 put4(&SFY(ey + 1, k, 0, ex), CS, F);
             }
             // x correction of row l = ln: rx + (F*_L iJx - f_L) dgl + (F*_R iJx - f_R) dgr
@@ -430,8 +456,17 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
 #pragma unroll
             for (int kk = 0; kk < NP; ++kk) {
                 if constexpr (MET) {
-                    v4_fms<Real>(FL, j11[kk], fxl, aL);
-                    v4_fms<Real>(FR, j11[kk], fxr, aR);
+                    // a11 at point (kk, l); with normals (iJ n)_1 of the left and right faces
+                    const unsigned at = ((unsigned)(kk + NP * l) * plane + e) * 4;
+                    Real sL = __ldg(a.met + at), sR = sL;
+                    if (a.nfx != nullptr) {
+                        const Real a12 = __ldg(a.met + at + 1);
+                        const Real *nL = a.nfx + 2 * ((unsigned)i + (unsigned)(nx + 1) * j);
+                        sL = fmaR<Real>(a12, nL[1], sR * nL[0]);
+                        sR = fmaR<Real>(a12, nL[3], sR * nL[2]);
+                    }
+                    v4_fms<Real>(FL, sL, fxl, aL);
+                    v4_fms<Real>(FR, sR, fxr, aR);
                 }
                 Real g[4];
                 v4_fma<Real>(aL, op.dgl[kk], rx[kk], g);
@@ -457,10 +492,17 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
 #pragma unroll
         for (int l = 0; l < NP; ++l) {
             if constexpr (MET) {
-                // a22 at point (k, l)
-                const Real j22 = __ldg(a.met + ((unsigned)(k + NP * l) * plane + e) * 4 + 3);
-                v4_fms<Real>(FB, j22, gyb, bB);
-                v4_fms<Real>(FT, j22, gyt, bT);
+                // a22 at point (k, l); with normals (iJ n)_2 of the bottom and top faces
+                const unsigned at = ((unsigned)(k + NP * l) * plane + e) * 4;
+                Real sB = __ldg(a.met + at + 3), sT = sB;
+                if (a.nfy != nullptr) {
+                    const Real a21 = __ldg(a.met + at + 2);
+                    const Real *nB = a.nfy + 2 * ((unsigned)i + (unsigned)nx * j), *nT = nB + 2 * nx;
+                    sB = fmaR<Real>(sT, nB[1], a21 * nB[0]);
+                    sT = fmaR<Real>(sT, nT[1], a21 * nT[0]);
+                }
+                v4_fms<Real>(FB, sB, gyb, bB);
+                v4_fms<Real>(FT, sT, gyt, bT);
             }
             // r = -du/dt at the NP points of row l, column k, all 4 variables
             Real r[4], res[4];
@@ -661,6 +703,8 @@ int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     }
     static_assert(S::bytes <= 227 * 1024, "shared memory per CTA exceeds 227 KB");
     a.met = MET ? (const Real *)p->d_met : nullptr;
+    a.nfx = MET ? (const Real *)p->d_nfx : nullptr;
+    a.nfy = MET ? (const Real *)p->d_nfy : nullptr;
     a.c1 = (Real)p->meth.c1;
     a.fa = (Real)p->meth.fa;
     a.fs = (Real)p->meth.fs;

@@ -243,6 +243,23 @@ __device__ __forceinline__ void riemann2d(const Real (&wL)[4], const Real (&wR)[
     }
 }
 
+// Interface flux across a face with unit normal (nx, ny): both states to the
+// face frame (momentum along n and along t = (-ny, nx)), the x-direction flux,
+// back to the global frame (dev/parallelogram.jl:60-73 with local_frame /
+// global_frame).
+template <class Real, int FLUX>
+__device__ __forceinline__ void riemann_n(const Real (&wL)[4], const Real (&wR)[4], Real nx, Real ny, Real gamma,
+                                          Real gm1, Real (&F)[4]) {
+    const Real l[4] = {wL[0], fmaR<Real>(wL[2], ny, wL[1] * nx), fmaR<Real>(-wL[1], ny, wL[2] * nx), wL[3]};
+    const Real r[4] = {wR[0], fmaR<Real>(wR[2], ny, wR[1] * nx), fmaR<Real>(-wR[1], ny, wR[2] * nx), wR[3]};
+    Real f[4];
+    riemann2d<Real, 0, FLUX>(l, r, gamma, gm1, f);
+    F[0] = f[0];
+    F[1] = fmaR<Real>(-f[2], ny, f[1] * nx);
+    F[2] = fmaR<Real>(f[1], ny, f[2] * nx);
+    F[3] = f[3];
+}
+
 template <class Real> __device__ __forceinline__ bool finiteR(Real x) { return isfinite(x); }
 
 } // namespace frk

@@ -56,6 +56,7 @@ struct frgpu_problem {
     void *rhs_in = nullptr, *rhs_out = nullptr; // scratch of frgpu_rhs
     void *d_stage = nullptr;                // FP64 staging of state uploads / downloads (+ 8 bytes)
     void *d_met = nullptr;                  // 2D Euler: per-point inverse Jacobian (a11, a12, a21, a22), or null
+    void *d_nfx = nullptr, *d_nfy = nullptr; // with d_met: unit normals of the x and y faces, or null
     int parity = 0;                         // FP32K: which buffer holds u^n (0: s0, 1: s1)
     bool prepare_only = false;              // launchers only set kernel attributes
     // post-step filter

@@ -293,7 +293,7 @@ static void free_problem(frgpu_problem *p) {
     if (p->erk_gexec) cudaGraphExecDestroy(p->erk_gexec);
     void *bufs[] = {p->s0, p->s1, p->s2, p->s3, p->d_dt, p->d_status, p->d_red, p->d_flags, p->d_count,
                     p->d_velo, p->d_w, p->d_J, p->d_V, p->d_iV, p->rhs_in, p->rhs_out, p->d_bgk_prim,
-                    p->d_bgk_frag, p->d_stage, p->d_erk, p->d_met};
+                    p->d_bgk_frag, p->d_stage, p->d_erk, p->d_met, p->d_nfx, p->d_nfy};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -837,11 +837,40 @@ FRGPU_API int frgpu_positive_limiter(frgpu_problem *p, const double *weights, do
     FR_CATCH
 }
 
-FRGPU_API int frgpu_problem_set_metric(frgpu_problem *p, const double *iJ) {
+// host array (column-major, the 2 components last) -> device pairs (c fastest)
+static int upload_pairs(frgpu_problem *p, void **dst, const double *h, size_t nfaces) {
+    std::vector<double> dev(2 * nfaces);
+    for (size_t f = 0; f < nfaces; ++f)
+        for (int c = 0; c < 2; ++c) {
+            const double v = h[f + nfaces * c];
+            if (!std::isfinite(v)) {
+                fr_set_error("problem_set_metric: non-finite face normal");
+                return FRGPU_ERR_ARG;
+            }
+            dev[2 * f + c] = v;
+        }
+    if (!*dst) FR_CUDA(cudaMalloc(dst, 2 * nfaces * p->esize));
+    if (p->esize == 8) {
+        FR_CUDA(cudaMemcpy(*dst, dev.data(), sizeof(double) * dev.size(), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> f(dev.begin(), dev.end());
+        FR_CUDA(cudaMemcpy(*dst, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice));
+    }
+    return FRGPU_OK;
+}
+
+FRGPU_API int frgpu_problem_set_metric(frgpu_problem *p, const double *iJ, const double *n1, const double *n2) {
     FR_REQ(p, "problem_set_metric: null problem");
     FR_REQ(p->d.equation == FRGPU_EULER2D, "problem_set_metric: 2D Euler problems only");
+    FR_REQ((n1 == nullptr) == (n2 == nullptr), "problem_set_metric: pass both face-normal arrays or neither");
+    FR_REQ(iJ || !n1, "problem_set_metric: face normals need the metric");
     FR_TRY
     FR_CUDA(cudaStreamSynchronize(p->stream));
+    for (void **b : {&p->d_nfx, &p->d_nfy})
+        if (*b) {
+            cudaFree(*b);
+            *b = nullptr;
+        }
     if (!iJ) {
         if (p->d_met) cudaFree(p->d_met);
         p->d_met = nullptr;
@@ -867,6 +896,12 @@ FRGPU_API int frgpu_problem_set_metric(frgpu_problem *p, const double *iJ) {
         } else {
             std::vector<float> f(dev.begin(), dev.end());
             FR_CUDA(cudaMemcpy(p->d_met, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice));
+        }
+        if (n1) {
+            const size_t nx = p->sp.nx, ny = p->sp.ny;
+            int rc = upload_pairs(p, &p->d_nfx, n1, (nx + 1) * ny);
+            if (!rc) rc = upload_pairs(p, &p->d_nfy, n2, nx * (ny + 1));
+            if (rc) return rc;
         }
     }
     p->graph_ind = -2; // force a re-capture

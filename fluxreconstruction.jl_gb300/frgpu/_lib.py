@@ -70,7 +70,7 @@ SIGNATURES = {
     "frgpu_troubled_flags": (C.c_int, [_VP, _I, C.c_long]),
     "frgpu_positive_limiter": (C.c_int, [_VP, _D, C.c_double, _I]),
     "frgpu_step_erk": (C.c_int, [_VP, C.c_int, _D, _D, C.c_double, C.c_int]),
-    "frgpu_problem_set_metric": (C.c_int, [_VP, _D]),
+    "frgpu_problem_set_metric": (C.c_int, [_VP, _D, _D, _D]),
     "frgpu_set_limiter": (C.c_int, [_VP, C.c_int, _D, C.c_double]),
     "frgpu_problem_device_state": (C.c_int, [_VP, C.POINTER(_VP), _I]),
     "frgpu_problem_stream": (C.c_int, [_VP, C.POINTER(_VP)]),

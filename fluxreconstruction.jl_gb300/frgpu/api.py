@@ -295,17 +295,27 @@ class ODEProblem:
         self.f(du, u, self, t)
         return du
 
-    def set_metric(self, iJ) -> None:
-        """Per-point inverse Jacobian of general quadrilaterals (FRPSpace2D's
-        iJ[i, j][k, l], src/struct.jl:135-158) as an array [nx, ny, np, np, 2, 2];
+    def set_metric(self, iJ, n1=None, n2=None) -> None:
+        """Per-point inverse Jacobian (FRPSpace2D's iJ[i, j][k, l],
+        src/struct.jl:135-158) as an array [nx, ny, np, np, 2, 2], and optionally
+        the unit normals of the x faces n1[nx+1, ny, 2] and the y faces
+        n2[nx, ny+1, 2] (straight-sided quadrilaterals, dev/parallelogram.jl:115-160);
         None returns to the uniform rectangles."""
         if iJ is None:
-            check(L.lib().frgpu_problem_set_metric(self._h, None))
+            check(L.lib().frgpu_problem_set_metric(self._h, None, None, None))
             return
         a = np.asfortranarray(np.asarray(iJ, dtype=np.float64))
         if a.shape != tuple(self.shape[:4]) + (2, 2):
             raise ValueError("iJ must have shape (nx, ny, np, np, 2, 2)")
-        check(L.lib().frgpu_problem_set_metric(self._h, dptr(a)))
+        if n1 is None:
+            check(L.lib().frgpu_problem_set_metric(self._h, dptr(a), None, None))
+            return
+        nx, ny = self.shape[0], self.shape[1]
+        b1 = np.asfortranarray(np.asarray(n1, dtype=np.float64))
+        b2 = np.asfortranarray(np.asarray(n2, dtype=np.float64))
+        if b1.shape != (nx + 1, ny, 2) or b2.shape != (nx, ny + 1, 2):
+            raise ValueError("face normals must have shapes (nx+1, ny, 2) and (nx, ny+1, 2)")
+        check(L.lib().frgpu_problem_set_metric(self._h, dptr(a), dptr(b1), dptr(b2)))
 
     def set_option(self, option: int, value: int) -> None:
         """Kernel choice for measurements (frgpu_problem_set_option), e.g.

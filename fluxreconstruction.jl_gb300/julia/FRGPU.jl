@@ -192,6 +192,27 @@ function set_limiter!(itg, on::Bool, weights=nothing, t0=1.0)
     return nothing
 end
 
+"""General quadrilaterals: the per-point inverse Jacobian `iJ[i, j][k, l]` of FRPSpace2D
+(src/struct.jl:135-158) and, for straight-sided quadrilaterals, the unit face normals
+`n1[i, j]` (x faces, (nx+1) x ny) and `n2[i, j]` (y faces, nx x (ny+1)) of
+dev/parallelogram.jl:115-160; `iJ = nothing` returns to the rectangles of the space."""
+function set_metric!(prob, iJ; n1=nothing, n2=nothing)
+    h = prob.p.h
+    if iJ === nothing
+        check(ccall((:frgpu_problem_set_metric, libfrgpu), Cint,
+                    (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}), h, C_NULL, C_NULL, C_NULL))
+        return nothing
+    end
+    nx, ny = size(iJ)
+    np = size(iJ[1, 1], 1)
+    a = Float64[iJ[i, j][k, l][r, c] for i in 1:nx, j in 1:ny, k in 1:np, l in 1:np, r in 1:2, c in 1:2]
+    b1 = n1 === nothing ? C_NULL : Float64[n1[i, j][c] for i in 1:nx+1, j in 1:ny, c in 1:2]
+    b2 = n2 === nothing ? C_NULL : Float64[n2[i, j][c] for i in 1:nx, j in 1:ny+1, c in 1:2]
+    check(ccall((:frgpu_problem_set_metric, libfrgpu), Cint,
+                (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}), h, a, b1, b2))
+    return nothing
+end
+
 """interp_face!(fδ, f, ll, lr) of src/interpolate.jl:1-10, evaluated on the GPU."""
 function interp_face!(fδ, f::AbstractMatrix, ll, lr)
     fh = Matrix{Float64}(f)

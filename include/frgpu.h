@@ -181,16 +181,19 @@ FRGPU_API int frgpu_positive_limiter(frgpu_problem *p, const double *weights, do
 /* Per-point metric (FRPSpace2D's inverse Jacobian iJ[i, j][k, l],
  * src/struct.jl:135-158): iJ as a host array [nx, ny, np, np, 2, 2] (column-major,
  * the 2 x 2 matrices last).  The residual then takes f = a11 F + a12 G and
- * g = a21 F + a22 G at every solution point and scales the interface fluxes of
- * the corrections by a11 (x faces) and a22 (y faces) at each point, as the dudt!
- * closure of example/shock-vortex.jl:48-55, :102-115 does.  That formula is
- * exact for rectangles of different sizes (a diagonal metric constant within
- * each element, e.g. stretched meshes); with off-diagonal terms or a metric
- * varying inside an element it is the reference's formula as it stands, which
- * does not keep a uniform state.  NULL returns to the uniform rectangles of the
- * space (iJ = diag(2/dx, 2/dy)); 2D Euler only.  The learned indicator then runs
- * as its own kernel after the step. */
-FRGPU_API int frgpu_problem_set_metric(frgpu_problem *p, const double *iJ);
+ * g = a21 F + a22 G at every solution point.
+ * Without face normals (n1 = n2 = NULL) the interface fluxes are Cartesian and
+ * the corrections scale them by a11 (x faces) and a22 (y faces), the dudt!
+ * closure of example/shock-vortex.jl:48-55, :102-115: exact for rectangles of
+ * different sizes (stretched meshes).
+ * With the unit normals of the x faces n1[nx+1, ny, 2] and the y faces
+ * n2[nx, ny+1, 2], the interface fluxes are solved in each face's frame and
+ * scaled by (iJ n)_1, (iJ n)_2, the formulation of dev/parallelogram.jl:115-160
+ * for straight-sided quadrilaterals (a uniform flow stays uniform on affine
+ * elements).
+ * iJ = NULL returns to the uniform rectangles of the space (iJ = diag(2/dx,
+ * 2/dy)); 2D Euler only.  The learned indicator then runs as its own kernel. */
+FRGPU_API int frgpu_problem_set_metric(frgpu_problem *p, const double *iJ, const double *n1, const double *n2);
 /* Run the limiter before every step of frgpu_step_ssprk3 (the loop of
  * example/shock-vortex.jl:297-303); on = 0 turns it off. */
 FRGPU_API int frgpu_set_limiter(frgpu_problem *p, int on, const double *weights, double t0);

@@ -580,6 +580,23 @@ static void e2d_fill_ghosts(const fro_cfg *c, const double *u, e2d_work *w) {
     }
 }
 
+/* Interface flux across a face with unit normal n (example
+ * dev/parallelogram.jl:115-133): both states to the face frame (momentum along n
+ * and along t = (-ny, nx)), the x-direction flux, back to the global frame. */
+static void face_flux_n(const fro_cfg *c, const double *wL, const double *wR, double nx_, double ny_, double *fw) {
+    double l[4], r[4], f[4];
+    l[0] = wL[0]; l[1] = fma(wL[2], ny_, wL[1] * nx_); l[2] = fma(-wL[1], ny_, wL[2] * nx_); l[3] = wL[3];
+    r[0] = wR[0]; r[1] = fma(wR[2], ny_, wR[1] * nx_); r[2] = fma(-wR[1], ny_, wR[2] * nx_); r[3] = wR[3];
+    if (c->flux == FRO_FLUX_HLL)
+        fro_flux_hll2d(l, r, c->gamma, 0, f);
+    else
+        fro_flux_lf2d(l, r, c->gamma, 0, f);
+    fw[0] = f[0];
+    fw[1] = fma(-f[2], ny_, f[1] * nx_);
+    fw[2] = fma(f[1], ny_, f[2] * nx_);
+    fw[3] = f[3];
+}
+
 static void rhs_euler2d(const fro_cfg *c, double *du, const double *u) {
     int nx = c->nx, ny = c->ny, np = c->np;
     double g = c->gamma;
@@ -671,7 +688,10 @@ static void rhs_euler2d(const fro_cfg *c, double *du, const double *u) {
             const double *R = w.uface + ((long)(j + 1) * nxg + i + 1) * FS; /* element i */
             for (int k = 0; k < np; ++k) {
                 double *fw = w.fxi + (((long)j * (nx + 1) + i) * np + k) * 4;
-                if (c->flux == FRO_FLUX_HLL)
+                if (c->iJ && c->n1) {
+                    const long f = i + (long)(nx + 1) * j, nf = (long)(nx + 1) * ny;
+                    face_flux_n(c, L + (1 * np + k) * 4, R + (3 * np + k) * 4, c->n1[f], c->n1[f + nf], fw);
+                } else if (c->flux == FRO_FLUX_HLL)
                     fro_flux_hll2d(L + (1 * np + k) * 4, R + (3 * np + k) * 4, g, 0, fw);
                 else
                     fro_flux_lf2d(L + (1 * np + k) * 4, R + (3 * np + k) * 4, g, 0, fw);
@@ -686,7 +706,10 @@ static void rhs_euler2d(const fro_cfg *c, double *du, const double *u) {
             const double *T = w.uface + ((long)(j + 1) * nxg + i + 1) * FS; /* element j */
             for (int k = 0; k < np; ++k) {
                 double *fw = w.fyi + (((long)j * nx + i) * np + k) * 4;
-                if (c->flux == FRO_FLUX_HLL)
+                if (c->iJ && c->n2) {
+                    const long f = i + (long)nx * j, nf = (long)nx * (ny + 1);
+                    face_flux_n(c, B + (2 * np + k) * 4, T + (0 * np + k) * 4, c->n2[f], c->n2[f + nf], fw);
+                } else if (c->flux == FRO_FLUX_HLL)
                     fro_flux_hll2d(B + (2 * np + k) * 4, T + (0 * np + k) * 4, g, 1, fw);
                 else
                     fro_flux_lf2d(B + (2 * np + k) * 4, T + (0 * np + k) * 4, g, 1, fw);
@@ -712,16 +735,30 @@ static void rhs_euler2d(const fro_cfg *c, double *du, const double *u) {
                     double fyb = w.fyi[(((long)j * nx + i) * np + k) * 4 + m];
                     double fyt = w.fyi[(((long)(j + 1) * nx + i) * np + k) * 4 + m];
                     /* the x and y correction terms added to the two derivatives */
-                    double ix = c->iJx, iy = c->iJy;
-                    if (c->iJ) { /* a11, a22 at point (k, l) */
+                    /* interface-flux scales: iJx, iJy; per point a11, a22 (shock-vortex.jl:104-111);
+                     * with face normals (iJ n)_1 and (iJ n)_2 of each face (dev/parallelogram.jl:149-160) */
+                    double sL = c->iJx, sR = c->iJx, sB = c->iJy, sT = c->iJy;
+                    if (c->iJ) {
                         const long at = ei + nn * (k + (long)np * l), blk = nn * np * np;
-                        ix = c->iJ[at];
-                        iy = c->iJ[at + 3 * blk];
+                        const double a11 = c->iJ[at], a21 = c->iJ[at + blk], a12 = c->iJ[at + 2 * blk],
+                                     a22 = c->iJ[at + 3 * blk];
+                        sL = sR = a11;
+                        sB = sT = a22;
+                        if (c->n1) {
+                            const long fl = i + (long)(nx + 1) * j, nf = (long)(nx + 1) * ny;
+                            sL = fma(a12, c->n1[fl + nf], a11 * c->n1[fl]);
+                            sR = fma(a12, c->n1[fl + 1 + nf], a11 * c->n1[fl + 1]);
+                        }
+                        if (c->n2) {
+                            const long fb = i + (long)nx * j, nf = (long)nx * (ny + 1);
+                            sB = fma(a22, c->n2[fb + nf], a21 * c->n2[fb]);
+                            sT = fma(a22, c->n2[fb + nx + nf], a21 * c->n2[fb + nx]);
+                        }
                     }
-                    double aL = fxl * ix - ff[(3 * np + l) * 4 + m];
-                    double aR = fxr * ix - ff[(1 * np + l) * 4 + m];
-                    double bB = fyb * iy - ff[(0 * np + k) * 4 + m];
-                    double bT = fyt * iy - ff[(2 * np + k) * 4 + m];
+                    double aL = fxl * sL - ff[(3 * np + l) * 4 + m];
+                    double aR = fxr * sR - ff[(1 * np + l) * 4 + m];
+                    double bB = fyb * sB - ff[(0 * np + k) * 4 + m];
+                    double bT = fyt * sT - ff[(2 * np + k) * 4 + m];
                     double cx = fma(aR, c->dgr[k], fma(aL, c->dgl[k], r1));
                     double v = -fma(bT, c->dgr[l], fma(bB, c->dgl[l], cx + r2));
                     du[i + (long)nx * j + nn * (k + np * (l + (long)np * m))] = v;

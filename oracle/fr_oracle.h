@@ -65,6 +65,8 @@ typedef struct {
     const double *velo, *weights; /* BGK velocity grid */
     const double *iJ;          /* 2D: per-point inverse Jacobian [nx, ny, np, np, 2, 2]
                                   (column-major) or NULL for diag(iJx, iJy) */
+    const double *n1, *n2;     /* 2D with iJ: unit normals of the x faces [nx+1, ny, 2] and
+                                  the y faces [nx, ny+1, 2], or NULL for the Cartesian axes */
 } fro_cfg;
 
 long fro_ndof(const fro_cfg *c);

@@ -50,7 +50,7 @@ class Cfg(C.Structure):
         ("iJx", C.c_double), ("iJy", C.c_double),
         ("ll", _D), ("lr", _D), ("lpdm", _D), ("dgl", _D), ("dgr", _D),
         ("velo", _D), ("weights", _D),
-        ("iJ", _D),
+        ("iJ", _D), ("n1", _D), ("n2", _D),
     ]
 
 
@@ -292,14 +292,22 @@ class Problem:
         self.space = space
         self.kind = kind
 
-    def set_metric(self, iJ) -> None:
-        """2D: per-point inverse Jacobian iJ[nx, ny, np, np, 2, 2] (None: diag(iJx, iJy))."""
+    def set_metric(self, iJ, n1=None, n2=None) -> None:
+        """2D: per-point inverse Jacobian iJ[nx, ny, np, np, 2, 2] (None: diag(iJx,
+        iJy)), and optionally the unit normals of the x faces n1[nx+1, ny, 2] and
+        the y faces n2[nx, ny+1, 2] (None: the Cartesian axes)."""
+        self.cfg.iJ = self.cfg.n1 = self.cfg.n2 = None
         if iJ is None:
-            self.cfg.iJ = None
             return
-        a = np.asfortranarray(np.asarray(iJ, dtype=np.float64))
-        self._keep.append(a)
-        self.cfg.iJ = a.ctypes.data_as(_D)
+
+        def keep(x):
+            a = np.asfortranarray(np.asarray(x, dtype=np.float64))
+            self._keep.append(a)
+            return a.ctypes.data_as(_D)
+
+        self.cfg.iJ = keep(iJ)
+        if n1 is not None:
+            self.cfg.n1, self.cfg.n2 = keep(n1), keep(n2)
 
     def shape(self):
         c = self.cfg

@@ -130,7 +130,7 @@ def test_new_entry_points_reject_bad_arguments(frgpu):
     assert L.frgpu_positive_limiter(None, None, 1.0, C.byref(n)) == _lib.ERR_ARG
     assert L.frgpu_set_limiter(None, 1, None, 1.0) == _lib.ERR_ARG
     assert L.frgpu_step_erk(None, 2, _lib.dptr(A), _lib.dptr(b), 0.1, 1) == _lib.ERR_ARG
-    assert L.frgpu_problem_set_metric(None, None) == _lib.ERR_ARG
+    assert L.frgpu_problem_set_metric(None, None, None, None) == _lib.ERR_ARG
     assert "null" in _lib.last_error()
     with pytest.raises(ValueError):
         frgpu.ExplicitRK([[0.0, 0.5], [0.0, 0.0]], [0.5, 0.5])   # implicit entry above the diagonal

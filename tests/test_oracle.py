@@ -366,3 +366,48 @@ def test_euler2d_metric_free_stream_and_diagonal(oracle):
     r_met = pr.rhs(w)
     pr.set_metric(None)
     assert np.array_equal(r_met, pr.rhs(w))
+
+
+def parallelogram_metric(nx, ny, np_, dx, dy, s=0.3, t=-0.2):
+    """Metric and unit face normals of the affine mesh x = X + s Y, y = Y + t X
+    of nx x ny cells dx x dy (every element the same parallelogram):
+    iJ = J^-1 with J = [[dx/2, s dy/2], [t dx/2, dy/2]], normals of the x faces
+    along grad(xi) ~ (1, -s) and of the y faces along grad(eta) ~ (-t, 1)."""
+    J = np.array([[dx / 2, s * dy / 2], [t * dx / 2, dy / 2]])
+    iJ = np.zeros((nx, ny, np_, np_, 2, 2), order="F")
+    iJ[...] = np.linalg.inv(J)
+    n1 = np.zeros((nx + 1, ny, 2), order="F")
+    n2 = np.zeros((nx, ny + 1, 2), order="F")
+    n1[...] = np.array([1.0, -s]) / np.hypot(1.0, s)
+    n2[...] = np.array([-t, 1.0]) / np.hypot(1.0, t)
+    return iJ, n1, n2
+
+
+@pytest.mark.parametrize("flux", ["lf", "hll"])
+def test_euler2d_parallelogram_free_stream(oracle, flux):
+    """Straight-sided quadrilaterals with face normals (dev/parallelogram.jl:
+    interface fluxes solved along each face's unit normal and scaled by
+    (iJ n)_1 on x faces, (iJ n)_2 on y faces): a uniform flow stays uniform on
+    sheared parallelograms, which the normal-free formula does not manage."""
+    O = oracle
+    sp = O.Space2D(0, 1, 5, 0, 1, 4, 3)
+    pr = O.Problem(O.EULER2D, sp, gamma=1.4, flux=O.FLUX_HLL if flux == "hll" else O.FLUX_LF)
+    u = np.zeros((5, 4, 4, 4, 4), order="F")
+    u[..., 0], u[..., 1], u[..., 2], u[..., 3] = 1.2, 0.3, -0.2, 2.9
+    iJ, n1, n2 = parallelogram_metric(5, 4, 4, 0.2, 0.25)
+    pr.set_metric(iJ, n1, n2)
+    assert np.max(np.abs(pr.rhs(u))) < 1e-12
+    pr.set_metric(iJ)
+    assert np.max(np.abs(pr.rhs(u))) > 1e-3
+    # the rotated solve with the axes as normals is the Cartesian x-face flux
+    iJ[..., 0, 1] = iJ[..., 1, 0] = 0.0
+    rng = np.random.default_rng(11)
+    w = u + 0.05 * rng.standard_normal(u.shape)
+    ax1 = np.zeros_like(n1)
+    ax1[..., 0] = 1.0
+    ax2 = np.zeros_like(n2)
+    ax2[..., 1] = 1.0
+    pr.set_metric(iJ, ax1, ax2)
+    r_n = pr.rhs(w)
+    pr.set_metric(iJ)
+    assert np.max(np.abs(r_n - pr.rhs(w))) < 1e-12 * np.max(np.abs(r_n))

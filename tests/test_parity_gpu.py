@@ -651,6 +651,61 @@ def test_metric_general_matches_oracle(frgpu, oracle, flux):
     assert rel(prob.rhs(u), P.rhs(u)) < RTOL64
 
 
+def _parallelogram(ps, s=0.3, t=-0.2):
+    """Metric and unit face normals of the affine mesh x = X + s Y, y = Y + t X:
+    iJ = J^-1 with J = [[dx/2, s dy/2], [t dx/2, dy/2]] at every point, x faces
+    along grad(xi) ~ (1, -s), y faces along grad(eta) ~ (-t, 1)."""
+    nx, ny, npt = ps.xpg.shape[:3]
+    J = np.array([[ps.dx / 2, s * ps.dy / 2], [t * ps.dx / 2, ps.dy / 2]])
+    iJ = np.zeros((nx, ny, npt, npt, 2, 2), order="F")
+    iJ[...] = np.linalg.inv(J)
+    n1 = np.zeros((nx + 1, ny, 2), order="F")
+    n2 = np.zeros((nx, ny + 1, 2), order="F")
+    n1[...] = np.array([1.0, -s]) / np.hypot(1.0, s)
+    n2[...] = np.array([-t, 1.0]) / np.hypot(1.0, t)
+    return iJ, n1, n2
+
+
+@pytest.mark.parametrize("flux", ["lf", "hll"])
+def test_metric_face_normals_match_oracle(frgpu, oracle, flux):
+    """Straight-sided quadrilaterals with face normals (dev/parallelogram.jl:
+    rotated interface solves scaled by (iJ n)_1 and (iJ n)_2): a uniform flow
+    stays uniform on sheared parallelograms in FP64 and FP32K; with a general
+    metric and normals turning from face to face the residual and three SSPRK3
+    steps match the oracle in FP64."""
+    nx, ny, deg = 20, 12, 3
+    ps = frgpu.FRPSpace2D(0, 1, nx, 0, 1, ny, deg)
+    po = oracle_space2d(ps, 0, 1, nx, 0, 1, ny, deg)
+    iJ, n1, n2 = _parallelogram(ps)
+    uni = np.zeros(ps.xpg.shape[:4] + (4,), order="F")
+    uni[..., 0], uni[..., 1], uni[..., 2], uni[..., 3] = 1.2, 0.3, -0.2, 2.9
+    for precision, tol in (("fp64", 1e-12), ("fp32k", 1e-5)):
+        prob = frgpu.FREuler2DProblem(uni, (0, 1), ps, 1.4, flux=flux, bc="period", precision=precision)
+        prob.set_metric(iJ, n1, n2)
+        itg = frgpu.init(prob, dt=1e-4)
+        itg.step(5)
+        assert np.max(np.abs(itg.u - uni)) < tol
+    rng = np.random.default_rng(23)
+    th1 = 0.3 * rng.standard_normal((nx + 1, ny))
+    th2 = 0.3 * rng.standard_normal((nx, ny + 1))
+    g1 = np.asfortranarray(np.stack([np.cos(th1), np.sin(th1)], axis=-1))
+    g2 = np.asfortranarray(np.stack([-np.sin(th2), np.cos(th2)], axis=-1))
+    iJg = _metric(ps)
+    u = wave2d(ps.xpg)
+    P = oracle.Problem(oracle.EULER2D, po, gamma=1.4, flux=oracle.FLUX_HLL if flux == "hll" else oracle.FLUX_LF)
+    P.set_metric(iJg, g1, g2)
+    prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux=flux, bc="period")
+    prob.set_metric(iJg, g1, g2)
+    assert rel(prob.rhs(u), P.rhs(u)) < RTOL64
+    dt = 1e-4
+    itg = frgpu.init(prob, dt=dt)
+    itg.step(3)
+    assert rel(itg.u, P.ssprk3(u, dt, 3)) < RTOL64
+    with pytest.raises(frgpu.FRGPUError):
+        frgpu._lib.check(frgpu._lib.lib().frgpu_problem_set_metric(prob._h, frgpu._lib.dptr(iJg),
+                                                                    frgpu._lib.dptr(g1), None))
+
+
 @pytest.mark.parametrize("name", ["Midpoint", "Heun", "Ralston"])
 def test_two_stage_tableaux_fused_into_the_stage_kernel(frgpu, oracle, name):
     """Two-stage tableaux on the 2D Euler problem run as stages 1 and 3 of the
