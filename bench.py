@@ -517,6 +517,72 @@ def bgk_entry(steps=400, warmup=5):
     return out
 
 
+TRI_FLOP_PER_CELL_P3 = 2800      # operations of k_tri_rhs<., 3> per cell, counted from the kernel
+TRI_BYTES_PER_CELL_P3 = {"fp64": 249, "fp32k": 137}  # own state + residual + geometry + neighbour tables
+
+
+def tri_entry(nx=1024, steps=20, warmup=3, reps=20, forms=("fp64", "fp32k"), cpu=True):
+    """Unstructured triangles: the linear-advection dudt! of
+    dev/wave_triangle.jl:44-125 (a = -1) on a periodic triangulated unit square
+    of 2 nx^2 right triangles, p = 3 (10 Williams-Shunn-Jameson points per
+    cell, the golden tri_quadrature(3) points), SSPRK3 at dt = 0.05 h.  Timed:
+    `reps` residuals of the device state and `steps` SSPRK3 steps, per form;
+    the oracle's residual on all host cores over a 128 x 128 sample beside it."""
+    import torch
+
+    import frgpu
+    import oracle as O
+
+    q = np.load(os.path.join(ROOT, "tests", "golden", "tri_quadrature.npz"))
+    deg = 3
+    xpl, wp = np.stack([q["r3"], q["s3"]], axis=1), q["w3"]
+
+    def space(n):
+        pts, cid, key, ct = frgpu.tri_square_mesh(n, n, periodic=True)
+        return frgpu.TriFRPSpace(pts, cid, deg, xpl, wp, key, ct)
+
+    sp = space(nx)
+    X, Y = sp.xpg[..., 0], sp.xpg[..., 1]
+    u = np.asfortranarray(1.0 + 0.5 * np.sin(2 * np.pi * X) * np.cos(2 * np.pi * Y))
+    del X, Y
+    ndof = sp.ncell * sp.np
+    dt = 0.05 / nx
+    out = {"workload": f"triangles: linear advection (a = -1), periodic unit square, {sp.ncell} cells "
+                       f"({nx}x{nx} squares x 2), p=3, SSPRK3", "ndof": ndof, "cells": sp.ncell}
+    for form in forms:
+        prob = frgpu.TriAdvectionProblem(u, sp, -1.0, precision=form)
+        timer = _event_timer(torch.cuda.ExternalStream(prob.stream()))
+        for _ in range(warmup):
+            prob.rhs_device()
+        secs = timer(lambda: [prob.rhs_device() for _ in range(reps)]) / reps
+        prob.step(warmup, dt)
+        l0 = prob.launches()
+        secs_step = timer(lambda: prob.step(steps, dt)) / steps
+        rec = {"value": ndof * steps / (secs_step * steps), "unit": "DOF-updates/s", "step_ms": secs_step * 1e3,
+               "rhs_us": secs * 1e6, "rhs_dof_per_s": ndof / secs,
+               "achieved_gflops": TRI_FLOP_PER_CELL_P3 * sp.ncell / secs / 1e9,
+               "achieved_gbs_compulsory": TRI_BYTES_PER_CELL_P3[form] * sp.ncell / secs / 1e9,
+               "launches_per_step": (prob.launches() - l0) / steps}
+        out[form] = rec
+        del prob
+    if not cpu:
+        return out
+    # the oracle's residual on the host cores, on a smaller mesh
+    ss = space(128)
+    P = O.TriProblem(deg, -1.0, ss.dl, ss.lf, ss.phi, ss.J, ss.iJ, ss.nb_cell, ss.nb_face, ss.nb_point,
+                     ss.cell_type)
+    us = np.asfortranarray(1.0 + 0.5 * np.sin(2 * np.pi * ss.xpg[..., 0]))
+    P.rhs(us)
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < 3.0:
+        P.rhs(us)
+        n += 1
+    cpu = ss.ncell * ss.np * n / (time.perf_counter() - t0)
+    out["cpu_oracle_rhs_dof_per_s"] = {"value": cpu, "cores": O.get_threads(),
+                                       "sample": f"{n} residuals of a {ss.ncell}-cell mesh, FP64 oracle"}
+    return out
+
+
 def cpu_baseline(target_s=12.0, nthreads=None):
     """The oracle (FP64, OpenMP) on the full 512x512 p=3 mesh, timed over as many
     SSPRK3 steps as fit in about target_s seconds (at least one)."""
@@ -555,8 +621,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-configs", action="store_true", help="skip the shock-vortex, ensemble and BGK entries")
     # profiling aid: run one of the other workloads alone (small sizes through --steps / --instances)
-    ap.add_argument("--workload", choices=["shock_vortex", "ensemble", "bgk"], default=None)
+    ap.add_argument("--workload", choices=["shock_vortex", "ensemble", "bgk", "triangles"], default=None)
     ap.add_argument("--instances", type=int, default=4096)
+    ap.add_argument("--tri-nx", type=int, default=1024, help="triangles: squares per side (2 nx^2 cells)")
     args = ap.parse_args()
     ws, rank, _ = dist_env()
     dist = init_dist(ws)
@@ -569,6 +636,10 @@ def main():
             r = shock_vortex_entry(steps=args.steps, warmup=args.warmup)
         elif args.workload == "ensemble":
             r = ensemble_entry(n=args.instances, t_end=0.5)
+        elif args.workload == "triangles":
+            # FP32K first, so that a profiler's first residual launch is the FP32K one
+            r = tri_entry(nx=args.tri_nx, steps=args.steps, warmup=args.warmup, reps=args.steps,
+                          forms=("fp32k", "fp64"), cpu=False)
         else:
             r = bgk_entry(steps=args.steps, warmup=args.warmup)
         print(json.dumps({"partial_run": True, "workload": args.workload, "result": r}), flush=True)
@@ -634,7 +705,7 @@ def main():
         # the other workloads of the spec, each on its own clock (not part of `value`)
         line["configs"] = {}
         for name, fn in (("shock_vortex_400x200_p3", shock_vortex_entry), ("burgers_ensemble_4096", ensemble_entry),
-                         ("bgk_256x512_p3", bgk_entry)):
+                         ("bgk_256x512_p3", bgk_entry), ("triangles_advection_2M_cells_p3", tri_entry)):
             try:
                 line["configs"][name] = fn()
             except Exception as e:  # report, do not lose the headline line

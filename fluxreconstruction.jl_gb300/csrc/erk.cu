@@ -82,47 +82,78 @@ template <class Real> Comb<Real> comb_of(const double *coef, int nterms) {
 
 } // namespace
 
-// Enqueue one ERK step on the problem's stream (capturable).  launch_residual
-// evaluates k = L(in) with the equation's stage-0 kernel.
-int fr_enqueue_erk_step(frgpu_problem *p, int (*launch_residual)(frgpu_problem *, const void *, void *)) {
-    const int s = p->erk_s;
-    const size_t n = (size_t)p->ndof, kstride = n;
-    const bool f32 = p->d.precision == FRGPU_FP32K;
-    void *u = f32 ? fr_state_hi(p) : p->s0;
-    char *kb = (char *)p->d_erk;
-    char *stage = kb + (size_t)s * n * p->esize;
+// Enqueue one ERK step on a stream (capturable) over raw buffers: r.kbuf holds
+// the s stage derivatives and one stage input, n values each; residual(ctx,
+// in, out) evaluates k = L(in).
+int fr_erk_enqueue_raw(const fr_erk_raw &r, int (*residual)(void *, const void *, void *), void *ctx) {
+    const int s = r.s;
+    const size_t n = r.n, kstride = n;
+    char *kb = r.kbuf;
+    char *stage = kb + (size_t)s * n * r.esize;
     int rc;
     for (int i = 0; i < s; ++i) {
-        const double *Ai = &p->erk_A[(size_t)i * s];
+        const double *Ai = &r.A[(size_t)i * s];
         const int nt = comb_of<double>(Ai, i).nt;
-        void *ki = kb + (size_t)i * n * p->esize;
-        const void *in = u;
+        void *ki = kb + (size_t)i * n * r.esize;
+        const void *in = r.u;
         if (nt > 0) {
-            if (!p->prepare_only) {
-                if (f32)
-                    k_erk_stage<float><<<grid_for(n), 256, 0, p->stream>>>(
-                        (const float *)u, (const float *)kb, kstride, n, comb_of<float>(Ai, i), p->d_dt, (float *)stage);
+            if (!r.prepare_only) {
+                if (r.f32)
+                    k_erk_stage<float><<<grid_for(n), 256, 0, r.stream>>>(
+                        (const float *)r.u, (const float *)kb, kstride, n, comb_of<float>(Ai, i), r.d_dt, (float *)stage);
                 else
-                    k_erk_stage<double><<<grid_for(n), 256, 0, p->stream>>>((const double *)u, (const double *)kb,
-                                                                            kstride, n, comb_of<double>(Ai, i),
-                                                                            p->d_dt, (double *)stage);
+                    k_erk_stage<double><<<grid_for(n), 256, 0, r.stream>>>((const double *)r.u, (const double *)kb,
+                                                                           kstride, n, comb_of<double>(Ai, i),
+                                                                           r.d_dt, (double *)stage);
                 FR_CUDA(cudaGetLastError());
-                p->launches += 1;
+                *r.launches += 1;
             }
             in = stage;
         }
-        if ((rc = launch_residual(p, in, ki))) return rc;
+        if ((rc = residual(ctx, in, ki))) return rc;
     }
-    if (comb_of<double>(p->erk_b.data(), s).nt == 0 || p->prepare_only) return FRGPU_OK;
-    if (f32)
-        k_erk_update<float><<<grid_for(n), 256, 0, p->stream>>>((float *)u, (float *)p->s3, (const float *)kb, kstride,
-                                                                n, comb_of<float>(p->erk_b.data(), s), p->d_dt,
-                                                                p->d_status);
+    if (comb_of<double>(r.b, s).nt == 0 || r.prepare_only) return FRGPU_OK;
+    if (r.f32)
+        k_erk_update<float><<<grid_for(n), 256, 0, r.stream>>>((float *)r.u, (float *)r.lo, (const float *)kb, kstride,
+                                                               n, comb_of<float>(r.b, s), r.d_dt, r.d_status);
     else
-        k_erk_update<double><<<grid_for(n), 256, 0, p->stream>>>((double *)u, nullptr, (const double *)kb, kstride,
-                                                                 n, comb_of<double>(p->erk_b.data(), s), p->d_dt,
-                                                                 p->d_status);
+        k_erk_update<double><<<grid_for(n), 256, 0, r.stream>>>((double *)r.u, nullptr, (const double *)kb, kstride,
+                                                                n, comb_of<double>(r.b, s), r.d_dt, r.d_status);
     FR_CUDA(cudaGetLastError());
-    p->launches += 1;
+    *r.launches += 1;
     return FRGPU_OK;
+}
+
+namespace {
+struct ProblemResidual {
+    frgpu_problem *p;
+    int (*launch)(frgpu_problem *, const void *, void *);
+};
+int problem_residual(void *ctx, const void *in, void *out) {
+    const ProblemResidual *c = (const ProblemResidual *)ctx;
+    return c->launch(c->p, in, out);
+}
+} // namespace
+
+// Enqueue one ERK step on the problem's stream (capturable).  launch_residual
+// evaluates k = L(in) with the equation's stage-0 kernel.
+int fr_enqueue_erk_step(frgpu_problem *p, int (*launch_residual)(frgpu_problem *, const void *, void *)) {
+    const bool f32 = p->d.precision == FRGPU_FP32K;
+    fr_erk_raw r;
+    r.stream = p->stream;
+    r.s = p->erk_s;
+    r.A = p->erk_A.data();
+    r.b = p->erk_b.data();
+    r.n = (size_t)p->ndof;
+    r.f32 = f32;
+    r.u = f32 ? fr_state_hi(p) : p->s0;
+    r.lo = f32 ? p->s3 : nullptr;
+    r.kbuf = (char *)p->d_erk;
+    r.esize = p->esize;
+    r.d_dt = p->d_dt;
+    r.d_status = p->d_status;
+    r.prepare_only = p->prepare_only;
+    r.launches = &p->launches;
+    ProblemResidual ctx{p, launch_residual};
+    return fr_erk_enqueue_raw(r, problem_residual, &ctx);
 }

@@ -121,6 +121,9 @@ double jacobi_orthonormal(int n, double x);
 void vandermonde(int deg, const double *r, int n, double *V);
 void vandermonde_quad(int deg, const double *r, const double *s, int n, double *V);
 bool invert(int n, const double *A, double *Ainv);
+void vandermonde_tri(int deg, const double *r, const double *s, int n, double *V, double *Vr, double *Vs);
+void triface_points(int deg, double *pr, double *ps, double *wf);
+void tri_operators(int deg, const double *r, const double *s, double *V, double *dl, double *lf, double *phi);
 void build_1d(frgpu_space &s, int correction);
 void build_2d(frgpu_space &s);
 } // namespace frsetup
@@ -165,3 +168,19 @@ int fr_launch_limiter(frgpu_problem *p, const std::vector<double> &w, double t0)
 int fr_limiter_weights(const frgpu_problem *p, const double *weights, std::vector<double> &w);
 // explicit Runge-Kutta step (erk.cu); launch_residual evaluates k = L(in)
 int fr_enqueue_erk_step(frgpu_problem *p, int (*launch_residual)(frgpu_problem *, const void *, void *));
+// One explicit Runge-Kutta step over raw device buffers (erk.cu).
+struct fr_erk_raw {
+    cudaStream_t stream;
+    int s;                      // stages
+    const double *A, *b;        // host tableau, A row-major s x s
+    size_t n;                   // values in the state
+    bool f32;                   // FP32 state with compensated update into lo
+    void *u, *lo;               // state (high part) and FP32 low part (null for FP64)
+    char *kbuf;                 // (s + 1) n values: k_0 .. k_{s-1}, stage input
+    size_t esize;               // bytes per value
+    const double *d_dt;         // device dt
+    int *d_status;              // device status flags
+    bool prepare_only;          // launch nothing but the residual's preparation
+    long *launches;             // incremented per kernel enqueued
+};
+int fr_erk_enqueue_raw(const fr_erk_raw &r, int (*residual)(void *, const void *, void *), void *ctx);

@@ -222,4 +222,120 @@ void build_2d(frgpu_space &s) {
     if (!invert(n2, s.V.data(), s.iV.data())) throw std::runtime_error("singular Vandermonde matrix");
 }
 
+// ---------------------------------------------------------------- triangles
+// Orthonormal Jacobi polynomial P~_n^(alpha, 0)(x) (weight (1 - x)^alpha) from
+// the classical three-term recurrence of P_n^(alpha, beta) and its norm
+// h_n = 2^(alpha+beta+1) / (2n+alpha+beta+1) G(n+alpha+1) G(n+beta+1) / (G(n+alpha+beta+1) n!);
+// the same functions JacobiP / dJacobiP of src/Polynomial/poly_jacobi.jl evaluate.
+static ld jacobi_raw(int n, ld al, ld be, ld x) {
+    if (n == 0) return 1;
+    ld p0 = 1, p1 = (al + 1) + (al + be + 2) * (x - 1) / 2;
+    for (int k = 2; k <= n; ++k) {
+        const ld c = 2 * k + al + be;
+        const ld p2 = ((c - 1) * (c * (c - 2) * x + al * al - be * be) * p1 - 2 * (k + al - 1) * (k + be - 1) * c * p0) /
+                      (2 * k * (k + al + be) * (c - 2));
+        p0 = p1;
+        p1 = p2;
+    }
+    return p1;
+}
+static ld jacobi_norm(int n, ld al, ld be) {
+    return std::pow((ld)2, al + be + 1) / (2 * n + al + be + 1) * std::tgamma(n + al + 1) * std::tgamma(n + be + 1) /
+           (std::tgamma(n + al + be + 1) * std::tgamma((ld)n + 1));
+}
+static ld jacobi_on(int n, ld al, ld x) { return jacobi_raw(n, al, 0, x) / std::sqrt(jacobi_norm(n, al, 0)); }
+// d/dx P_n^(al, 0) = (n + al + 1) / 2 P_{n-1}^(al+1, 1)
+static ld djacobi_on(int n, ld al, ld x) {
+    if (n == 0) return 0;
+    return (n + al + 1) / 2 * jacobi_raw(n - 1, al + 1, 1, x) / std::sqrt(jacobi_norm(n, al, 0));
+}
+
+// The orthonormal simplex mode (i, j) of vandermonde_matrix(Tri, ...)
+// (src/Transform/transform.jl:36-50, transform_triangle.jl:8-56) and its r and s
+// derivatives at (r, s): psi = sqrt(2) P~_i(a) P~_j^(2i+1,0)(b) (1 - b)^i with
+// a = 2 (1 + r) / (1 - s) - 1 (a = -1 at s = 1), b = s, by the chain rule
+// da/dr = 2 / (1 - b), da/ds = (1 + a) / (1 - b).
+static void simplex_mode(int i, int j, double r, double s, ld &v, ld &vr, ld &vs) {
+    const ld a = s != 1.0 ? 2 * (1 + (ld)r) / (1 - (ld)s) - 1 : -1, b = s;
+    const ld F = jacobi_on(i, 0, a), dF = djacobi_on(i, 0, a);
+    const ld G = jacobi_on(j, 2 * i + 1, b), dG = djacobi_on(j, 2 * i + 1, b);
+    const ld sq2 = std::sqrt((ld)2), om = 1 - b;
+    const ld omi = std::pow(om, (ld)i), omi1 = i > 0 ? std::pow(om, (ld)(i - 1)) : 0;
+    v = sq2 * F * G * omi;
+    vr = i > 0 ? 2 * sq2 * dF * G * omi1 : 0;
+    vs = sq2 * (F * dG * omi + (i > 0 ? (dF * (1 + a) - i * F) * G * omi1 : 0));
+}
+
+void vandermonde_tri(int deg, const double *r, const double *s, int n, double *V, double *Vr, double *Vs) {
+    int sk = 0;
+    for (int i = 0; i <= deg; ++i)
+        for (int j = 0; j <= deg - i; ++j, ++sk)
+            for (int q = 0; q < n; ++q) {
+                ld v, vr, vs;
+                simplex_mode(i, j, r[q], s[q], v, vr, vs);
+                if (V) V[q + (size_t)n * sk] = (double)v;
+                if (Vr) Vr[q + (size_t)n * sk] = (double)vr;
+                if (Vs) Vs[q + (size_t)n * sk] = (double)vs;
+            }
+}
+
+// Face flux points of the reference right triangle (triface_quadrature,
+// src/Quadrature/quadrature.jl:86-106): Gauss-Legendre nodes x_k along face 1
+// (r = x_k, s = -1), face 2 (r = x_{N-k}, s = x_k) and face 3 (r = -1, s = x_{N-k});
+// weights w_k times the face lengths 1, sqrt(2), 1.
+void triface_points(int deg, double *pr, double *ps, double *wf) {
+    std::vector<double> x, w;
+    gauss_legendre(deg + 1, x, w);
+    const int m = deg + 1;
+    for (int k = 0; k < m; ++k) {
+        pr[0 + 3 * k] = x[k];
+        ps[0 + 3 * k] = -1.0;
+        pr[1 + 3 * k] = x[m - 1 - k];
+        ps[1 + 3 * k] = x[k];
+        pr[2 + 3 * k] = -1.0;
+        ps[2 + 3 * k] = x[m - 1 - k];
+        wf[0 + 3 * k] = w[k];
+        wf[1 + 3 * k] = w[k] * std::sqrt(2.0);
+        wf[2 + 3 * k] = w[k];
+    }
+}
+
+// TriFRPSpace operators (src/struct.jl:305-352) at the np solution points (r, s):
+// V; dl[i, q, d] = d l_q / d r_d at point i (dlagrange(V, Vr, Vs):
+// V' \ Vr[i, :]); lf[f, k, q] = l_q at flux point (f, k) (V' \ psi_f);
+// phi[f, k, i] = sum_m wf[f, k] psi_f[f, k, m] V[i, m] (correction_field,
+// src/Polynomial/poly_triangle.jl:1-28).  Column-major outputs; any may be null.
+void tri_operators(int deg, const double *r, const double *s, double *Vout, double *dl, double *lf, double *phi) {
+    const int np = (deg + 1) * (deg + 2) / 2, m = deg + 1, nf = 3 * m;
+    std::vector<double> V((size_t)np * np), Vr(V.size()), Vs(V.size()), iV(V.size());
+    vandermonde_tri(deg, r, s, np, V.data(), Vr.data(), Vs.data());
+    if (!invert(np, V.data(), iV.data())) throw std::runtime_error("singular triangle Vandermonde matrix");
+    std::vector<double> pr(nf), ps(nf), wf(nf), Pf((size_t)nf * np);
+    triface_points(deg, pr.data(), ps.data(), wf.data());
+    vandermonde_tri(deg, pr.data(), ps.data(), nf, Pf.data(), nullptr, nullptr);
+    if (Vout) std::copy(V.begin(), V.end(), Vout);
+    for (int i = 0; i < np; ++i)
+        for (int q = 0; q < np; ++q) {
+            ld a = 0, b = 0;
+            for (int t = 0; t < np; ++t) {
+                a += (ld)Vr[i + (size_t)np * t] * iV[t + (size_t)np * q];
+                b += (ld)Vs[i + (size_t)np * t] * iV[t + (size_t)np * q];
+            }
+            if (dl) {
+                dl[i + (size_t)np * q] = (double)a;
+                dl[i + (size_t)np * q + (size_t)np * np] = (double)b;
+            }
+        }
+    for (int f = 0; f < nf; ++f) // f = face + 3 k, the flux point's flat index
+        for (int q = 0; q < np; ++q) {
+            ld a = 0, c = 0;
+            for (int t = 0; t < np; ++t) {
+                a += (ld)Pf[f + (size_t)nf * t] * iV[t + (size_t)np * q];
+                c += (ld)wf[f] * Pf[f + (size_t)nf * t] * V[q + (size_t)np * t];
+            }
+            if (lf) lf[f + (size_t)nf * q] = (double)a;
+            if (phi) phi[f + (size_t)nf * q] = (double)c;
+        }
+}
+
 } // namespace frsetup

@@ -5,6 +5,16 @@ of include/frgpu.h).  This package is its Python host binding; it mirrors the
 FluxReconstruction.jl interface for the hot path (see ``api``).
 """
 from ._lib import FRGPUError, lib, last_error  # noqa: F401
+from .tri import (  # noqa: F401
+    Euler,
+    TriAdvectionProblem,
+    TriFRPSpace,
+    rs_jacobi,
+    tri_operators,
+    tri_square_mesh,
+    triface_quadrature,
+    vandermonde_tri,
+)
 from .api import (  # noqa: F401
     FRAdvectionProblem,
     FRBGKProblem,

@@ -71,6 +71,18 @@ SIGNATURES = {
     "frgpu_positive_limiter": (C.c_int, [_VP, _D, C.c_double, _I]),
     "frgpu_step_erk": (C.c_int, [_VP, C.c_int, _D, _D, C.c_double, C.c_int]),
     "frgpu_problem_set_metric": (C.c_int, [_VP, _D, _D, _D]),
+    "frgpu_vandermonde_tri": (C.c_int, [C.c_int, _D, _D, C.c_int, _D, _D, _D]),
+    "frgpu_tri_operators": (C.c_int, [C.c_int, _D, _D, _D, _D, _D, _D]),
+    "frgpu_tri_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, _D, _D, _D, _D, _D, _I, _I, _I, _I,
+                                   C.POINTER(_VP)]),
+    "frgpu_tri_destroy": (C.c_int, [_VP]),
+    "frgpu_tri_set_state": (C.c_int, [_VP, _D]),
+    "frgpu_tri_get_state": (C.c_int, [_VP, _D]),
+    "frgpu_tri_rhs": (C.c_int, [_VP, _D, _D]),
+    "frgpu_tri_rhs_device": (C.c_int, [_VP]),
+    "frgpu_tri_step_erk": (C.c_int, [_VP, C.c_int, _D, _D, C.c_double, C.c_int]),
+    "frgpu_tri_stream": (C.c_int, [_VP, C.POINTER(_VP)]),
+    "frgpu_tri_launches": (C.c_int, [_VP, C.POINTER(C.c_longlong)]),
     "frgpu_set_limiter": (C.c_int, [_VP, C.c_int, _D, C.c_double]),
     "frgpu_problem_device_state": (C.c_int, [_VP, C.POINTER(_VP), _I]),
     "frgpu_problem_stream": (C.c_int, [_VP, C.POINTER(_VP)]),

@@ -63,6 +63,7 @@ enum frgpu_option { FRGPU_OPT_BGK_TENSOR = 1, FRGPU_OPT_FUSED_INDICATOR = 2, FRG
 typedef struct frgpu_space frgpu_space;
 typedef struct frgpu_problem frgpu_problem;
 typedef struct frgpu_mlp frgpu_mlp;
+typedef struct frgpu_tri frgpu_tri;
 
 /* ======================================================================
  * Setup math (host).  Used by the space constructors; exported so a caller
@@ -335,6 +336,49 @@ FRGPU_API int frgpu_interp_face(const double *f, long n, int np, const double *l
 /* poly_derivative!(df, f, pdm) row-wise for a matrix f[n, np]
  * (src/derivative.jl:1-10): df[i, m] = sum_k f[i, k] pdm[m, k]. */
 FRGPU_API int frgpu_poly_derivative(const double *f, long n, int np, const double *pdm, double *df);
+
+/* ======================================================================
+ * Unstructured triangles: TriFRPSpace (src/struct.jl:305-352) and the
+ * linear-advection dudt! of dev/wave_triangle.jl:44-125.  Column-major
+ * arrays, cell index fastest: u[ncell, np] with np = (deg+1)(deg+2)/2.
+ * ==================================================================== */
+
+/* vandermonde_matrix(Tri, N, r, s) and dvandermonde_matrix(Tri, N, r, s)
+ * (src/Transform/transform.jl:36-50, :106-127): V, Vr, Vs [n, np], mode (i, j)
+ * with j fastest; any output may be NULL. */
+FRGPU_API int frgpu_vandermonde_tri(int deg, const double *r, const double *s, int n, double *V, double *Vr,
+                                    double *Vs);
+/* The operators TriFRPSpace builds from its solution points (r, s) (the np
+ * points of tri_quadrature(deg), src/Quadrature/quadrature.jl:14-71): V[np, np];
+ * dl[np, np, 2] (dlagrange(V, Vr, Vs): dl[j, q, d] = d l_q / d r_d at point j);
+ * lf[3, deg+1, np] (l_q at the flux points of triface_quadrature,
+ * quadrature.jl:86-106); phi[3, deg+1, np] (correction_field,
+ * src/Polynomial/poly_triangle.jl:1-28).  Any output may be NULL. */
+FRGPU_API int frgpu_tri_operators(int deg, const double *r, const double *s, double *V, double *dl, double *lf,
+                                  double *phi);
+/* A triangle problem: ncell cells of degree 1..3, precision FRGPU_FP64 or
+ * FRGPU_FP32K, speed a (u_t + a u_x + a u_y = 0); the space's dl, lf, phi as
+ * above; J and iJ [ncell, 2, 2] (rs_jacobi, src/Geometry/geo_jacobi.jl:32-43,
+ * and its inverse); nb_cell, nb_face, nb_point [ncell, 3, deg+1]: the 0-based
+ * neighbour_fpidx of every flux point (src/Geometry/geo_neighbor.jl:8-60;
+ * nb_cell < 0 on a boundary face); cell_type[ncell] (only cells of type 0 are
+ * updated, as in dev/wave_triangle.jl:117-121).  The state starts at zero. */
+FRGPU_API int frgpu_tri_create(int ncell, int deg, int precision, double a, const double *dl, const double *lf,
+                               const double *phi, const double *J, const double *iJ, const int *nb_cell,
+                               const int *nb_face, const int *nb_point, const int *cell_type, frgpu_tri **out);
+FRGPU_API int frgpu_tri_destroy(frgpu_tri *t);
+FRGPU_API int frgpu_tri_set_state(frgpu_tri *t, const double *u);
+FRGPU_API int frgpu_tri_get_state(frgpu_tri *t, double *u);
+/* du = L(u) for host arrays: dudt!(du, u, p, t) of dev/wave_triangle.jl:44 */
+FRGPU_API int frgpu_tri_rhs(frgpu_tri *t, double *du, const double *u);
+/* L(device state) into device scratch on the object's stream (no host copy) */
+FRGPU_API int frgpu_tri_rhs_device(frgpu_tri *t);
+/* nsteps fixed steps of the explicit tableau (A row-major s x s, b) on the
+ * device state: init(prob, alg; dt, adaptive=false) + step!
+ * (dev/wave_triangle.jl:131-135 with Euler()); replayed from a CUDA graph. */
+FRGPU_API int frgpu_tri_step_erk(frgpu_tri *t, int s, const double *A, const double *b, double dt, int nsteps);
+FRGPU_API int frgpu_tri_stream(frgpu_tri *t, void **stream);
+FRGPU_API int frgpu_tri_launches(frgpu_tri *t, long long *n);
 
 /* ======================================================================
  * Diagnostics

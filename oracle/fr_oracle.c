@@ -1383,3 +1383,182 @@ double fro_mlp_loss_grad(const double *P, const double *x, const double *label, 
     free(buf);
     return loss / n;
 }
+
+/* ------------------------------------------------------------------------
+ * Unstructured triangles: the modal basis of TriFRPSpace (src/struct.jl:305-352)
+ * and the linear-advection residual of dev/wave_triangle.jl:44-125
+ * ---------------------------------------------------------------------- */
+
+/* rs_ab, src/Geometry/geo_transform.jl:102-108 */
+static void tri_rs_ab(double r, double s, double *a, double *b) {
+    *a = s != 1.0 ? 2.0 * (1.0 + r) / (1.0 - s) - 1.0 : -1.0;
+    *b = s;
+}
+
+/* simplex_basis, src/Transform/transform_triangle.jl:8-14 */
+static double tri_simplex(double a, double b, int i, int j) {
+    double h1 = fro_jacobi_p(a, 0, 0, i), h2 = fro_jacobi_p(b, 2 * i + 1, 0, j);
+    return sqrt(2.0) * h1 * h2 * pow(1 - b, i);
+}
+
+/* dsimplex_basis, src/Transform/transform_triangle.jl:22-56 */
+static void tri_dsimplex(double a, double b, int id, int jd, double *dr, double *ds) {
+    double fa = fro_jacobi_p(a, 0, 0, id), dfa = fro_djacobi_p(a, 0, 0, id);
+    double gb = fro_jacobi_p(b, 2 * id + 1, 0, jd), dgb = fro_djacobi_p(b, 2 * id + 1, 0, jd);
+    double r = dfa * gb;
+    if (id > 0) r *= pow(0.5 * (1.0 - b), id - 1);
+    double s = dfa * (gb * (0.5 * (1.0 + a)));
+    if (id > 0) s *= pow(0.5 * (1.0 - b), id - 1);
+    double tmp = dgb * pow(0.5 * (1.0 - b), id);
+    if (id > 0) tmp -= 0.5 * id * gb * pow(0.5 * (1.0 - b), id - 1);
+    s += fa * tmp;
+    r *= pow(2.0, id + 0.5);
+    s *= pow(2.0, id + 0.5);
+    *dr = r;
+    *ds = s;
+}
+
+/* vandermonde_matrix(Tri, N, r, s), src/Transform/transform.jl:36-50: mode sk
+ * over i (outer), j = 0..N-i (inner); V[pt + n*sk] */
+void fro_vandermonde_tri(int N, const double *r, const double *s, int n, double *V) {
+    int sk = 0;
+    for (int i = 0; i <= N; ++i)
+        for (int j = 0; j <= N - i; ++j, ++sk)
+            for (int q = 0; q < n; ++q) {
+                double a, b;
+                tri_rs_ab(r[q], s[q], &a, &b);
+                V[q + n * sk] = tri_simplex(a, b, i, j);
+            }
+}
+
+/* dvandermonde_matrix(Tri, N, r, s), src/Transform/transform.jl:106-127 */
+void fro_dvandermonde_tri(int N, const double *r, const double *s, int n, double *Vr, double *Vs) {
+    int sk = 0;
+    for (int i = 0; i <= N; ++i)
+        for (int j = 0; j <= N - i; ++j, ++sk)
+            for (int q = 0; q < n; ++q) {
+                double a, b;
+                tri_rs_ab(r[q], s[q], &a, &b);
+                tri_dsimplex(a, b, i, j, Vr + q + n * sk, Vs + q + n * sk);
+            }
+}
+
+/* Unit outward normals of the reference right triangle's faces 1 -> 2, 2 -> 3,
+ * 3 -> 1 (dev/wave_triangle.jl:68). */
+static const double TRI_N[3][2] = {{0.0, -1.0}, {0.70710678118654752440, 0.70710678118654752440}, {-1.0, 0.0}};
+
+/* The dudt! closure of dev/wave_triangle.jl:44-125 for u_t + a u_x + a u_y = 0.
+ * Per cell: f = iJ (a u, a u) at the solution points; face values of u and f
+ * through lf; at each flux point the Rusanov-type interaction flux of the two
+ * sides' physical fluxes J f (zero on a boundary face), back to the reference
+ * frame through iJ; du = -(dl . f) - sum over (face, point) of
+ * (n . f_int - n . f_face) phi, on cells of type 0 only (du = 0 elsewhere).
+ * Fixed evaluation order (the GPU kernel repeats it): 2-vectors A x as
+ * fma(A_12, x_2, A_11 x_1); dot products as ascending fma chains; the
+ * correction sum runs over the flux points column-major (face fastest). */
+static void tri_cell_flux(const fro_tri *t, const double *u, long c, double *f1, double *f2) {
+    const long nc = t->ncell;
+    const double i11 = t->iJ[c], i21 = t->iJ[c + nc], i12 = t->iJ[c + 2 * nc], i22 = t->iJ[c + 3 * nc];
+    for (int q = 0; q < t->np; ++q) {
+        const double fg = t->a * u[c + nc * q], gg = t->a * u[c + nc * q];
+        f1[q] = fma(i12, gg, i11 * fg);
+        f2[q] = fma(i22, gg, i21 * fg);
+    }
+}
+
+static void tri_face_values(const fro_tri *t, const double *u, const double *f1, const double *f2, long c, int f,
+                            int k, double *uf, double *ff1, double *ff2) {
+    const int np = t->np, nfp = t->nfp;
+    const double *l = t->lf + f + 3 * k; /* lf[f, k, q] at l[3*nfp*q] */
+    const long nc = t->ncell;
+    double su = u[c] * l[0], s1 = f1[0] * l[0], s2 = f2[0] * l[0];
+    for (int q = 1; q < np; ++q) {
+        const double w = l[(long)3 * nfp * q];
+        su = fma(u[c + nc * q], w, su);
+        s1 = fma(f1[q], w, s1);
+        s2 = fma(f2[q], w, s2);
+    }
+    *uf = su;
+    *ff1 = s1;
+    *ff2 = s2;
+}
+
+void fro_tri_rhs(const fro_tri *t, double *du, const double *u) {
+    const long nc = t->ncell;
+    const int np = t->np, nfp = t->nfp;
+#ifdef _OPENMP
+#pragma omp parallel for OMP_THREADS schedule(static)
+#endif
+    for (long c = 0; c < nc; ++c) {
+        double f1[64], f2[64], g1[64], g2[64], d[3 * 16];
+        if (t->ctype[c] != 0) {
+            for (int j = 0; j < np; ++j) du[c + nc * j] = 0.0;
+            continue;
+        }
+        tri_cell_flux(t, u, c, f1, f2);
+        const double J11 = t->J[c], J21 = t->J[c + nc], J12 = t->J[c + 2 * nc], J22 = t->J[c + 3 * nc];
+        const double i11 = t->iJ[c], i21 = t->iJ[c + nc], i12 = t->iJ[c + 2 * nc], i22 = t->iJ[c + 3 * nc];
+        for (int f = 0; f < 3; ++f)
+            for (int k = 0; k < nfp; ++k) {
+                const long fp = c + nc * (f + 3 * (long)k);
+                double uL, a1, a2;
+                tri_face_values(t, u, f1, f2, c, f, k, &uL, &a1, &a2);
+                const double fn_face = fma(a2, TRI_N[f][1], a1 * TRI_N[f][0]);
+                double fi1 = 0.0, fi2 = 0.0;
+                const long n = t->nbc[fp];
+                if (n >= 0) {
+                    const int nf = t->nbf[fp], nk = t->nbk[fp];
+                    double uR, b1, b2;
+                    tri_cell_flux(t, u, n, g1, g2);
+                    tri_face_values(t, u, g1, g2, n, nf, nk, &uR, &b1, &b2);
+                    const double K11 = t->J[n], K21 = t->J[n + nc], K12 = t->J[n + 2 * nc], K22 = t->J[n + 3 * nc];
+                    const double fL1 = fma(J12, a2, J11 * a1), fL2 = fma(J22, a2, J21 * a1);
+                    const double fR1 = fma(K12, b2, K11 * b1), fR2 = fma(K22, b2, K21 * b1);
+                    const double jump = uL - uR, den = jump + 1e-6;
+                    const double au1 = (fL1 - fR1) / den, au2 = (fL2 - fR2) / den;
+                    fi1 = 0.5 * (fL1 + fR1) - 0.5 * fabs(au1) * jump;
+                    fi2 = 0.5 * (fL2 + fR2) - 0.5 * fabs(au2) * jump;
+                }
+                const double h1 = fma(i12, fi2, i11 * fi1), h2 = fma(i22, fi2, i21 * fi1);
+                const double fn_int = fma(h2, TRI_N[f][1], h1 * TRI_N[f][0]);
+                d[f + 3 * k] = fn_int - fn_face;
+            }
+        for (int j = 0; j < np; ++j) {
+            const double r1 = dotw(f1, 1, t->dl + j, np, np);
+            const double r2 = dotw(f2, 1, t->dl + j + (long)np * np, np, np);
+            const double r3 = dotw(d, 1, t->phi + (long)3 * nfp * j, 1, 3 * nfp);
+            du[c + nc * j] = (-r1 - r2) + (-r3);
+        }
+    }
+}
+
+void fro_tri_erk(const fro_tri *t, double *u, double dt, int nsteps, int s, const double *A, const double *b,
+                 double *work) {
+    long n = (long)t->ncell * t->np;
+    double *st = work, *k = work + n;
+    for (int it = 0; it < nsteps; ++it) {
+        for (int i = 0; i < s; ++i) {
+            int first = 1;
+            for (int j = 0; j < i; ++j) {
+                const double a = A[i * s + j];
+                if (a == 0.0) continue;
+                for (long q = 0; q < n; ++q) st[q] = first ? a * k[j * n + q] : fma(a, k[j * n + q], st[q]);
+                first = 0;
+            }
+            if (first)
+                fro_tri_rhs(t, k + i * n, u);
+            else {
+                for (long q = 0; q < n; ++q) st[q] = fma(dt, st[q], u[q]);
+                fro_tri_rhs(t, k + i * n, st);
+            }
+        }
+        int first = 1;
+        for (int j = 0; j < s; ++j) {
+            if (b[j] == 0.0) continue;
+            for (long q = 0; q < n; ++q) st[q] = first ? b[j] * k[j * n + q] : fma(b[j], k[j * n + q], st[q]);
+            first = 0;
+        }
+        if (!first)
+            for (long q = 0; q < n; ++q) u[q] = fma(dt, st[q], u[q]);
+    }
+}

@@ -125,6 +125,23 @@ double fro_mlp_loss_grad(const double *params, const double *x, const double *la
 
 /* threads used by the OpenMP loops (0 = library default) */
 void fro_set_threads(int n);
+
+/* ---- unstructured triangles (TriFRPSpace, src/struct.jl:305-352; the advection
+ * dudt! of dev/wave_triangle.jl:44-125).  Column-major arrays, cell index fastest:
+ * u[ncell, np]; dl[np, np, 2] (dl[j, q, d] = d l_q / d r_d at point j); lf and phi
+ * [3, nfp, np]; J and iJ [ncell, 2, 2]; nbc, nbf, nbk [ncell, 3, nfp] the 0-based
+ * neighbour cell (< 0: boundary face), its face and its flux point. ---- */
+typedef struct {
+    int ncell, deg, np, nfp;
+    double a;
+    const double *dl, *lf, *phi, *J, *iJ;
+    const int *nbc, *nbf, *nbk, *ctype;
+} fro_tri;
+void fro_vandermonde_tri(int N, const double *r, const double *s, int n, double *V);
+void fro_dvandermonde_tri(int N, const double *r, const double *s, int n, double *Vr, double *Vs);
+void fro_tri_rhs(const fro_tri *t, double *du, const double *u);
+void fro_tri_erk(const fro_tri *t, double *u, double dt, int nsteps, int s, const double *A, const double *b,
+                 double *work);
 int fro_get_threads(void);
 
 #ifdef __cplusplus

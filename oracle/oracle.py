@@ -57,6 +57,12 @@ class Cfg(C.Structure):
 _lib = None
 
 
+class TriCfg(C.Structure):
+    _fields_ = [("ncell", C.c_int), ("deg", C.c_int), ("np", C.c_int), ("nfp", C.c_int), ("a", C.c_double),
+                ("dl", _D), ("lf", _D), ("phi", _D), ("J", _D), ("iJ", _D),
+                ("nbc", _I), ("nbf", _I), ("nbk", _I), ("ctype", _I)]
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -102,6 +108,10 @@ def lib():
             "fro_ib_rh": (None, [C.c_double, C.c_double, _D, _D]),
             "fro_mlp_forward": (None, [_D, _D, C.c_int, C.c_int, C.c_int, _D]),
             "fro_mlp_loss_grad": (C.c_double, [_D, _D, _D, C.c_int, C.c_int, C.c_int, _D]),
+            "fro_vandermonde_tri": (None, [C.c_int, _D, _D, C.c_int, _D]),
+            "fro_dvandermonde_tri": (None, [C.c_int, _D, _D, C.c_int, _D, _D]),
+            "fro_tri_rhs": (None, [C.POINTER(TriCfg), _D, _D]),
+            "fro_tri_erk": (None, [C.POINTER(TriCfg), _D, C.c_double, C.c_int, C.c_int, _D, _D, _D]),
             "fro_set_threads": (None, [C.c_int]),
             "fro_get_threads": (C.c_int, []),
         }
@@ -466,3 +476,76 @@ def mlp_loss_grad(params, x, labels, nin=32, nh=64):
     g = np.zeros_like(P)
     loss = lib().fro_mlp_loss_grad(_p(P), X.ctypes.data_as(_D), _p(t), X.shape[0], nin, nh, _p(g))
     return loss, g
+
+
+# ---------------------------------------------------------------- triangles
+def vandermonde_tri(N: int, r, s):
+    """vandermonde_matrix(Tri, N, r, s) (src/Transform/transform.jl:36-50) and
+    its r, s derivatives (:106-127), restated in fr_oracle.c."""
+    r, s = _f64(r), _f64(s)
+    npm = (N + 1) * (N + 2) // 2
+    V, Vr, Vs = (np.zeros((len(r), npm), order="F") for _ in range(3))
+    lib().fro_vandermonde_tri(N, _p(r), _p(s), len(r), _p(V))
+    lib().fro_dvandermonde_tri(N, _p(r), _p(s), len(r), _p(Vr), _p(Vs))
+    return V, Vr, Vs
+
+
+def triface_points(N: int):
+    """triface_quadrature(N) (src/Quadrature/quadrature.jl:86-106)."""
+    p0, w0 = gauss_legendre(N + 1)
+    pf = np.zeros((3, N + 1, 2))
+    pf[0, :, 0], pf[0, :, 1] = p0, -1.0
+    pf[1, :, 0], pf[1, :, 1] = p0[::-1], p0
+    pf[2, :, 0], pf[2, :, 1] = -1.0, p0[::-1]
+    wf = np.stack([w0, w0 * np.sqrt(2.0), w0])
+    return pf, wf
+
+
+def tri_operators(N: int, r, s):
+    """TriFRPSpace's V, dl = dlagrange(V, Vr, Vs) (V' \\ Vr[i, :] per point),
+    lf (V' \\ psi_f) and phi = correction_field(N, V)
+    (src/struct.jl:305-352, src/Polynomial/poly_triangle.jl:1-28), with numpy
+    solves on the oracle's Vandermonde matrices."""
+    V, Vr, Vs = vandermonde_tri(N, r, s)
+    npm = V.shape[0]
+    dl = np.zeros((npm, npm, 2), order="F")
+    dl[:, :, 0] = np.linalg.solve(V.T, Vr.T).T
+    dl[:, :, 1] = np.linalg.solve(V.T, Vs.T).T
+    pf, wf = triface_points(N)
+    lf = np.zeros((3, N + 1, npm), order="F")
+    phi = np.zeros((3, N + 1, npm), order="F")
+    for f in range(3):
+        psi, _, _ = vandermonde_tri(N, pf[f, :, 0], pf[f, :, 1])
+        lf[f] = np.linalg.solve(V.T, psi.T).T
+        sigma = wf[f][:, None] * psi
+        phi[f] = sigma @ V.T
+    return V, dl, lf, phi
+
+
+class TriProblem:
+    """The linear-advection dudt! of dev/wave_triangle.jl:44-125 on given
+    TriFRPSpace operators and mesh connectivity (fro_tri_rhs); u[ncell, np]."""
+
+    def __init__(self, deg, a, dl, lf, phi, J, iJ, nb_cell, nb_face, nb_point, cell_type):
+        self._keep = [np.asfortranarray(x, dtype=np.float64) for x in (dl, lf, phi, J, iJ)]
+        self._keep += [np.asfortranarray(x, dtype=np.int32) for x in (nb_cell, nb_face, nb_point, cell_type)]
+        d = self._keep
+        ncell = d[3].shape[0]
+        self.shape = (ncell, (deg + 1) * (deg + 2) // 2)
+        self.cfg = TriCfg(ncell, deg, self.shape[1], deg + 1, float(a),
+                          *(x.ctypes.data_as(_D) for x in d[:5]), *(x.ctypes.data_as(_I) for x in d[5:]))
+
+    def rhs(self, u) -> np.ndarray:
+        uf = np.asfortranarray(u, dtype=np.float64)
+        du = np.zeros(self.shape, order="F")
+        lib().fro_tri_rhs(C.byref(self.cfg), _p(du), _p(uf))
+        return du
+
+    def erk(self, u, dt: float, nsteps: int, A, b) -> np.ndarray:
+        uf = np.array(u, dtype=np.float64, order="F", copy=True)
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        s = len(b)
+        work = np.zeros((s + 1) * uf.size)
+        lib().fro_tri_erk(C.byref(self.cfg), _p(uf), float(dt), int(nsteps), s, _p(A), _p(b), _p(work))
+        return uf

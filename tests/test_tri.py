@@ -1,0 +1,239 @@
+"""Unstructured triangles: TriFRPSpace (src/struct.jl:305-352) and the
+linear-advection dudt! of dev/wave_triangle.jl:44-125.
+
+CPU: the golden tri_quadrature points (made from the reference's own qpmin.py
+by tests/golden/make_tri_quadrature.py), libfrgpu's host operators against the
+oracle's restatement, exactness of the operators, the mesh connectivity
+against the reference's coordinate matching (neighbour_fpidx), and the
+oracle's residual (uniform state kept, conservation, convergence order).
+GPU (marked): the residual and explicit Runge-Kutta steps through the C ABI
+against the oracle."""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "tri_quadrature.npz")
+
+
+@pytest.fixture(scope="module")
+def quad():
+    return np.load(GOLD)
+
+
+def _xpl(quad, deg):
+    return np.stack([quad[f"r{deg}"], quad[f"s{deg}"]], axis=1), quad[f"w{deg}"]
+
+
+def _space(frgpu, quad, nx, ny, deg, periodic=True):
+    pts, cid, key, ct = frgpu.tri_square_mesh(nx, ny, periodic=periodic)
+    xpl, wp = _xpl(quad, deg)
+    return frgpu.TriFRPSpace(pts, cid, deg, xpl, wp, key, ct)
+
+
+def _oracle_problem(oracle, sp, a):
+    return oracle.TriProblem(sp.deg, a, sp.dl, sp.lf, sp.phi, sp.J, sp.iJ, sp.nb_cell, sp.nb_face, sp.nb_point,
+                             sp.cell_type)
+
+
+def _wave(sp):
+    X, Y = sp.xpg[..., 0], sp.xpg[..., 1]
+    return np.asfortranarray(1.0 + 0.5 * np.sin(2 * np.pi * X) * np.cos(2 * np.pi * Y))
+
+
+# ---------------------------------------------------------------- CPU
+@pytest.mark.parametrize("deg", [1, 2, 3])
+def test_tri_quadrature_golden(quad, deg):
+    """The Williams-Shunn-Jameson points of tri_quadrature(deg): (deg+1)(deg+2)/2
+    points inside the reference right triangle, weights summing to 1, exact
+    for the monomials r^i s^j, i + j <= deg + 1 (the rules' degree)."""
+    xpl, w = _xpl(quad, deg)
+    r, s = xpl[:, 0], xpl[:, 1]
+    assert len(w) == (deg + 1) * (deg + 2) // 2
+    assert np.all(r > -1) and np.all(s > -1) and np.all(r + s < 0)
+    assert abs(w.sum() - 1) < 1e-14
+    # exact integrals over the right triangle of area 2, by 1D Gauss-Jacobi in a
+    # collapsed coordinate (numpy Gauss-Legendre of high order on the square map)
+    x, wx = np.polynomial.legendre.leggauss(12)
+    A, B = np.meshgrid(x, x, indexing="ij")
+    WA = np.outer(wx, wx)
+    R = (1 + A) * (1 - B) / 2 - 1
+    S = B
+    jac = (1 - B) / 2
+    for i in range(deg + 2):
+        for j in range(deg + 2 - i):
+            exact = np.sum(WA * jac * R ** i * S ** j)
+            assert abs(2 * np.dot(w, r ** i * s ** j) - exact) < 1e-13, (i, j)
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3])
+def test_tri_operators_match_oracle(frgpu, oracle, quad, deg):
+    """libfrgpu's host setup (frgpu_vandermonde_tri, frgpu_tri_operators: long
+    double Jacobi recurrences) against the oracle's C restatement of
+    transform_triangle.jl with numpy solves."""
+    xpl, _ = _xpl(quad, deg)
+    r, s = xpl[:, 0], xpl[:, 1]
+    for a, b in zip(frgpu.vandermonde_tri(deg, r, s), oracle.vandermonde_tri(deg, r, s)):
+        np.testing.assert_allclose(a, b, rtol=0, atol=5e-14)
+    for a, b in zip(frgpu.tri_operators(deg, r, s), oracle.tri_operators(deg, r, s)):
+        np.testing.assert_allclose(a, b, rtol=0, atol=5e-14)
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3])
+def test_tri_operators_exact_on_polynomials(frgpu, quad, deg):
+    """dl differentiates and lf interpolates every polynomial of degree deg
+    exactly; the modal basis is orthonormal where the rule is exact."""
+    xpl, w = _xpl(quad, deg)
+    r, s = xpl[:, 0], xpl[:, 1]
+    V, dl, lf, phi = frgpu.tri_operators(deg, r, s)
+    pf, _ = frgpu.triface_quadrature(deg)
+    for i in range(deg + 1):
+        for j in range(deg + 1 - i):
+            p = r ** i * s ** j
+            dpr = i * r ** max(i - 1, 0) * s ** j
+            dps = j * r ** i * s ** max(j - 1, 0)
+            assert np.max(np.abs(dl[:, :, 0] @ p - dpr)) < 1e-12
+            assert np.max(np.abs(dl[:, :, 1] @ p - dps)) < 1e-12
+            for f in range(3):
+                assert np.max(np.abs(lf[f] @ p - pf[f, :, 0] ** i * pf[f, :, 1] ** j)) < 1e-12
+    if deg <= 2:
+        assert np.max(np.abs(V.T @ np.diag(2 * w) @ V - np.eye(len(w)))) < 1e-13
+
+
+@pytest.mark.parametrize("periodic", [True, False])
+def test_tri_mesh_neighbours_match_coordinates(frgpu, quad, periodic):
+    """The flux-point neighbours of the mesh builder (vertex keys, opposite
+    traversal of a shared face) are the points neighbour_fpidx finds by
+    coordinates (src/Geometry/geo_neighbor.jl:49-57), up to the period."""
+    deg = 2
+    sp = _space(frgpu, quad, 5, 4, deg, periodic)
+    n = sp.nb_cell
+    assert (np.all(n >= 0) if periodic else np.any(n < 0))
+    for c in range(sp.ncell):
+        for f in range(3):
+            for k in range(deg + 1):
+                m = n[c, f, k]
+                if m < 0:
+                    assert sp.cell_type[c] == 1
+                    continue
+                d = sp.xfg[c, f, k] - sp.xfg[m, sp.nb_face[c, f, k], sp.nb_point[c, f, k]]
+                d -= np.round(d)  # periodic images of the unit square
+                assert np.max(np.abs(d)) < 1e-14
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3])
+def test_oracle_tri_free_stream_and_conservation(frgpu, oracle, quad, deg):
+    """dudt! keeps a uniform state, and on a periodic mesh the residual's
+    integral sum_c det J_c sum_j w_j du_j vanishes."""
+    sp = _space(frgpu, quad, 6, 5, deg)
+    P = _oracle_problem(oracle, sp, -1.0)
+    assert np.max(np.abs(P.rhs(np.full((sp.ncell, sp.np), 1.3, order="F")))) < 1e-13
+    du = P.rhs(_wave(sp))
+    _, w = _xpl(quad, deg)
+    assert abs(np.sum(np.linalg.det(sp.J)[:, None] * w[None, :] * du)) < 1e-12
+
+
+@pytest.mark.parametrize("deg", [1, 2])
+def test_oracle_tri_convergence(frgpu, oracle, quad, deg):
+    """The residual of sin(2 pi x) cos(2 pi y) approaches -a (u_x + u_y) at
+    order deg under refinement (a = -1 as dev/wave_triangle.jl:37)."""
+    errs = []
+    for nx in (8, 16, 32):
+        sp = _space(frgpu, quad, nx, nx, deg)
+        P = _oracle_problem(oracle, sp, -1.0)
+        X, Y = sp.xpg[..., 0], sp.xpg[..., 1]
+        u = np.sin(2 * np.pi * X) * np.cos(2 * np.pi * Y)
+        ex = 2 * np.pi * (np.cos(2 * np.pi * X) * np.cos(2 * np.pi * Y) - np.sin(2 * np.pi * X) * np.sin(2 * np.pi * Y))
+        errs.append(np.max(np.abs(P.rhs(np.asfortranarray(u)) - ex)))
+    rates = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
+    assert np.all(rates > deg - 0.15), rates
+
+
+def test_oracle_tri_boundary_cells_frozen(frgpu, oracle, quad):
+    """Cells of type 1 (with a boundary face) keep du = 0; the others see no
+    boundary face (dev/wave_triangle.jl:117-121)."""
+    sp = _space(frgpu, quad, 6, 6, 2, periodic=False)
+    du = _oracle_problem(oracle, sp, -1.0).rhs(_wave(sp))
+    assert np.all(du[sp.cell_type == 1] == 0.0)
+    assert np.any(du[sp.cell_type == 0] != 0.0)
+
+
+def test_tri_create_rejects_bad_arguments(frgpu):
+    """Argument checks of frgpu_tri_create run before any device work."""
+    from frgpu import _lib
+
+    L = _lib.lib()
+    h = C.c_void_p()
+    z = np.zeros(64)
+    zi = np.zeros(64, dtype=np.int32)
+    d, i = _lib.dptr(z), zi.ctypes.data_as(_lib._I)
+    assert L.frgpu_tri_create(4, 5, 0, 1.0, d, d, d, d, d, i, i, i, i, C.byref(h)) == _lib.ERR_ARG
+    assert "degree" in _lib.last_error()
+    assert L.frgpu_tri_create(4, 1, 0, 1.0, d, None, d, d, d, i, i, i, i, C.byref(h)) == _lib.ERR_ARG
+    assert L.frgpu_tri_create(0, 1, 0, 1.0, d, d, d, d, d, i, i, i, i, C.byref(h)) == _lib.ERR_ARG
+    assert L.frgpu_tri_step_erk(None, 1, d, d, 0.1, 1) == _lib.ERR_ARG
+
+
+# ---------------------------------------------------------------- GPU
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("deg", [1, 2, 3])
+@pytest.mark.parametrize("periodic", [True, False])
+def test_tri_rhs_matches_oracle(frgpu, oracle, quad, deg, periodic):
+    """frgpu_tri_rhs in FP64 gives the oracle's bits (same evaluation order,
+    no contracted multiply-adds); FP32K within FP32 rounding."""
+    sp = _space(frgpu, quad, 12, 9, deg, periodic)
+    u = _wave(sp)
+    ref = _oracle_problem(oracle, sp, -1.0).rhs(u)
+    prob = frgpu.TriAdvectionProblem(u, sp, -1.0)
+    assert np.array_equal(prob.rhs(u), ref)
+    p32 = frgpu.TriAdvectionProblem(u, sp, -1.0, precision="fp32k")
+    assert _rel(p32.rhs(u), ref) < 2e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("alg", ["SSPRK33", "Euler", "RK4"])
+def test_tri_steps_match_oracle(frgpu, oracle, quad, alg):
+    """Fixed explicit steps on the device state (CUDA-graph replay) against the
+    oracle's fro_tri_erk: FP64 bit-identical, FP32K (compensated update)
+    within 1e-6."""
+    deg = 3
+    sp = _space(frgpu, quad, 10, 10, deg)
+    u = _wave(sp)
+    dt = 2e-3
+    if alg == "SSPRK33":
+        A, b, m = np.array([[0, 0, 0], [1, 0, 0], [0.25, 0.25, 0]]), np.array([1 / 6, 1 / 6, 2 / 3]), None
+    else:
+        m = frgpu.Euler() if alg == "Euler" else frgpu.RK4()
+        A, b = m.A, m.b
+    ref = _oracle_problem(oracle, sp, -1.0).erk(u, dt, 5, A, b)
+    prob = frgpu.TriAdvectionProblem(u, sp, -1.0)
+    prob.step(3, dt, m)
+    prob.step(2, dt, m)
+    assert np.array_equal(prob.u, ref)
+    assert prob.launches() > 0
+    p32 = frgpu.TriAdvectionProblem(u, sp, -1.0, precision="fp32k")
+    p32.step(5, dt, m)
+    assert _rel(p32.u, ref) < 1e-6
+
+
+@pytest.mark.gpu
+def test_tri_state_round_trip_and_errors(frgpu, quad):
+    """set/get of the state is exact in FP64 and within the high + low pair in
+    FP32K; a non-finite state and a bad dt are refused."""
+    sp = _space(frgpu, quad, 6, 6, 2)
+    u = _wave(sp)
+    prob = frgpu.TriAdvectionProblem(u, sp, -1.0)
+    assert np.array_equal(prob.u, u)
+    p32 = frgpu.TriAdvectionProblem(u, sp, -1.0, precision="fp32k")
+    assert np.max(np.abs(p32.u - u)) < 1e-13
+    bad = u.copy()
+    bad[0, 0] = np.nan
+    with pytest.raises(frgpu.FRGPUError):
+        prob.u = bad
+    with pytest.raises(frgpu.FRGPUError):
+        prob.step(1, -1.0)
