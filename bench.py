@@ -531,6 +531,8 @@ def tri_entry(nx=1024, steps=20, warmup=3, reps=20, forms=("fp64", "fp32k"), cpu
     import torch
 
     import frgpu
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
     q = np.load(os.path.join(ROOT, "tests", "golden", "tri_quadrature.npz"))
