@@ -290,4 +290,60 @@ function Base.getproperty(itg::Integrator, s::Symbol)
     return getfield(itg, s)
 end
 
+# ---------------------------------------------------------------- triangles
+"""The linear-advection `dudt!` of dev/wave_triangle.jl:44-125 on the reference's
+`TriFRPSpace` `ps` (src/struct.jl:305-352), held on the GPU: `u[ncell, np]`, speed `a`.
+`ps.fpn[i, j, k] = (cell, face, point)` becomes 0-based neighbour tables (cell <= 0:
+boundary face); only cells with `ps.base.cellType == 0` are updated, as the script does."""
+mutable struct TriProblem
+    h::Ptr{Cvoid}
+    dims::Tuple{Int,Int}
+end
+
+function TriProblem(u::AbstractMatrix, ps, a; precision=:fp64)
+    ncell, np, m = size(ps.base.cellid, 1), ps.np, ps.deg + 1
+    J = Float64[ps.J[i][r, c] for i in 1:ncell, r in 1:2, c in 1:2]
+    iJ = Float64[inv(ps.J[i])[r, c] for i in 1:ncell, r in 1:2, c in 1:2]
+    nbc = Cint[ps.fpn[i, f, k][1] > 0 ? ps.fpn[i, f, k][1] - 1 : -1 for i in 1:ncell, f in 1:3, k in 1:m]
+    nbf = Cint[ps.fpn[i, f, k][1] > 0 ? ps.fpn[i, f, k][2] - 1 : -1 for i in 1:ncell, f in 1:3, k in 1:m]
+    nbk = Cint[ps.fpn[i, f, k][1] > 0 ? ps.fpn[i, f, k][3] - 1 : -1 for i in 1:ncell, f in 1:3, k in 1:m]
+    ct = Cint.(ps.base.cellType)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:frgpu_tri_create, libfrgpu), Cint,
+                (Cint, Cint, Cint, Cdouble, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble},
+                 Ptr{Cint}, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}, Ref{Ptr{Cvoid}}),
+                ncell, ps.deg, PRECISION[precision], a, Array{Float64}(ps.∂l), Array{Float64}(ps.lf),
+                Array{Float64}(ps.ϕ), J, iJ, nbc, nbf, nbk, ct, r))
+    t = TriProblem(r[], (ncell, np))
+    finalizer(x -> ccall((:frgpu_tri_destroy, libfrgpu), Cint, (Ptr{Cvoid},), x.h), t)
+    check(ccall((:frgpu_tri_set_state, libfrgpu), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), t.h, Array{Float64}(u)))
+    return t
+end
+
+"""dudt!(du, u, p, t) of dev/wave_triangle.jl on the GPU."""
+function rhs!(du, u, p::TriProblem, t)
+    dh = zeros(p.dims)
+    check(ccall((:frgpu_tri_rhs, libfrgpu), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}),
+                p.h, dh, Array{Float64}(u)))
+    du .= dh
+    return nothing
+end
+
+"""`n` fixed steps of `alg` (an `ExplicitRK` tableau, e.g. `Euler()`; `SSPRK33()`) on the state."""
+function step!(p::TriProblem, alg, dt, n::Integer=1)
+    A, b = alg isa SSPRK33 ? ([0.0 0 0; 1 0 0; 0.25 0.25 0], [1 / 6, 1 / 6, 2 / 3]) : (alg.A, alg.b)
+    check(ccall((:frgpu_tri_step_erk, libfrgpu), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Cdouble, Cint),
+                p.h, length(b), Matrix{Float64}(permutedims(A)), Vector{Float64}(b), dt, n))
+    return nothing
+end
+
+"""OrdinaryDiffEq `Euler()` as dev/wave_triangle.jl:133 steps it."""
+Euler() = ExplicitRK(zeros(1, 1), [1.0])
+
+function state(p::TriProblem)
+    out = zeros(p.dims)
+    check(ccall((:frgpu_tri_get_state, libfrgpu), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), p.h, out))
+    return out
+end
+
 end # module
