@@ -9,6 +9,8 @@ from .tri import (  # noqa: F401
     Euler,
     TriAdvectionProblem,
     TriFRPSpace,
+    boundary_cell_type,
+    read_gmsh,
     rs_jacobi,
     tri_operators,
     tri_square_mesh,

@@ -7,9 +7,10 @@ points are the caller's tri_quadrature(deg) points (src/Quadrature/
 quadrature.jl:14-71; the Williams-Shunn-Jameson sets), as the reference takes
 them.  ``TriAdvectionProblem`` is the linear-advection dudt! of
 dev/wave_triangle.jl:44-125 with its explicit time steps, all on the GPU
-through the ``frgpu_tri_*`` entry points.  ``tri_square_mesh`` builds a
-triangulated rectangle (two right triangles per square), periodic or not, in
-place of the reference's Gmsh reader.
+through the ``frgpu_tri_*`` entry points.  Meshes come from Gmsh ASCII
+files (``read_gmsh``, the reference's assets/*.msh) or from
+``tri_square_mesh`` (a triangulated rectangle, two right triangles per square,
+periodic or not).
 """
 from __future__ import annotations
 
@@ -105,6 +106,71 @@ def tri_square_mesh(nx: int, ny: int, x0=0.0, x1=1.0, y0=0.0, y1=1.0, periodic=T
     nbc, _, _ = _face_neighbours(cellid, key)
     cell_type = np.where(np.any(nbc < 0, axis=1), 1, 0).astype(np.int32)
     return points, cellid, key, cell_type
+
+
+def read_gmsh(path: str):
+    """Triangles of a Gmsh ASCII mesh (format 2.2 or 4.1), the meshes the
+    reference's examples read through KitBase's UnstructPSpace
+    (assets/*.msh): vertex coordinates [npts, 2] (z dropped) and the 0-based
+    vertex ids [ncell, 3] of every 3-node triangle (element type 2), in the
+    file's order."""
+    with open(path) as f:
+        lines = [ln.strip() for ln in f]
+    sec = {}
+    i = 0
+    while i < len(lines):
+        if lines[i].startswith("$") and not lines[i].startswith("$End"):
+            name = lines[i][1:]
+            j = lines.index("$End" + name, i)
+            sec[name] = lines[i + 1:j]
+            i = j
+        i += 1
+    if "MeshFormat" not in sec or "Nodes" not in sec or "Elements" not in sec:
+        raise ValueError(f"{path}: not a Gmsh mesh with nodes and elements")
+    version, binary = sec["MeshFormat"][0].split()[:2]
+    if binary != "0":
+        raise ValueError(f"{path}: binary Gmsh files are not read")
+    tags, xy, tris = [], [], []
+    nodes, elems = sec["Nodes"], sec["Elements"]
+    if version.startswith("4"):
+        nblocks = int(nodes[0].split()[0])
+        k = 1
+        for _ in range(nblocks):
+            _, _, param, n = (int(v) for v in nodes[k].split())
+            tags += [int(nodes[k + 1 + m]) for m in range(n)]
+            xy += [[float(v) for v in nodes[k + 1 + n + m].split()[:2]] for m in range(n)]
+            k += 1 + 2 * n
+        nblocks = int(elems[0].split()[0])
+        k = 1
+        for _ in range(nblocks):
+            _, _, etype, n = (int(v) for v in elems[k].split())
+            if etype == 2:
+                tris += [[int(v) for v in elems[k + 1 + m].split()[1:4]] for m in range(n)]
+            k += 1 + n
+    elif version.startswith("2"):
+        n = int(nodes[0])
+        for m in range(n):
+            v = nodes[1 + m].split()
+            tags.append(int(v[0]))
+            xy.append([float(v[1]), float(v[2])])
+        n = int(elems[0])
+        for m in range(n):
+            v = [int(t) for t in elems[1 + m].split()]
+            if v[1] == 2:
+                tris.append(v[3 + v[2]:6 + v[2]])
+    else:
+        raise ValueError(f"{path}: Gmsh format {version} is not read")
+    index = {t: q for q, t in enumerate(tags)}
+    cellid = np.array([[index[t] for t in c] for c in tris], dtype=np.int64).reshape(-1, 3)
+    return np.array(xy, dtype=np.float64).reshape(-1, 2), cellid
+
+
+def boundary_cell_type(cellid, key=None):
+    """Cell types as the triangle script uses them: 1 for a cell with a face on
+    the boundary (no neighbour), 0 otherwise."""
+    key = np.arange(int(np.max(cellid)) + 1) if key is None else np.asarray(key)
+    nbc, _, _ = _face_neighbours(np.asarray(cellid), key)
+    return np.where(np.any(nbc < 0, axis=1), 1, 0).astype(np.int32)
 
 
 def _face_neighbours(cellid, key):

@@ -159,6 +159,60 @@ def test_oracle_tri_boundary_cells_frozen(frgpu, oracle, quad):
     assert np.any(du[sp.cell_type == 0] != 0.0)
 
 
+def _write_gmsh(path, pts, cid, version):
+    """A Gmsh ASCII file of the triangles (plus one line element, which the
+    reader skips)."""
+    with open(path, "w") as f:
+        f.write(f"$MeshFormat\n{version} 0 8\n$EndMeshFormat\n")
+        if version == "2.2":
+            f.write(f"$Nodes\n{len(pts)}\n")
+            for q, (x, y) in enumerate(pts.tolist()):
+                f.write(f"{q + 1} {x!r} {y!r} 0\n")
+            f.write(f"$EndNodes\n$Elements\n{len(cid) + 1}\n1 1 2 0 1 1 2\n")
+            for q, c in enumerate(cid.tolist()):
+                f.write(f"{q + 2} 2 2 0 1 {c[0] + 1} {c[1] + 1} {c[2] + 1}\n")
+            f.write("$EndElements\n")
+        else:
+            f.write(f"$Nodes\n1 {len(pts)} 1 {len(pts)}\n2 1 0 {len(pts)}\n")
+            f.write("".join(f"{q + 1}\n" for q in range(len(pts))))
+            f.write("".join(f"{x!r} {y!r} 0\n" for x, y in pts.tolist()))
+            f.write(f"$EndNodes\n$Elements\n2 {len(cid) + 1} 1 {len(cid) + 1}\n1 1 1 1\n1 1 2\n")
+            f.write(f"2 1 2 {len(cid)}\n")
+            f.write("".join(f"{q + 2} {c[0] + 1} {c[1] + 1} {c[2] + 1}\n" for q, c in enumerate(cid.tolist())))
+            f.write("$EndElements\n")
+
+
+@pytest.mark.parametrize("version", ["2.2", "4.1"])
+def test_read_gmsh_round_trip(frgpu, tmp_path, version):
+    pts, cid, _, ct = frgpu.tri_square_mesh(4, 3, periodic=False)
+    path = str(tmp_path / "m.msh")
+    _write_gmsh(path, pts, cid, version)
+    p2, c2 = frgpu.read_gmsh(path)
+    assert np.array_equal(p2, pts) and np.array_equal(c2, cid)
+    assert np.array_equal(frgpu.boundary_cell_type(c2), ct)
+
+
+REFERENCE_MESH = os.path.join(os.environ.get("FR_REFERENCE", "/root/reference"), "assets", "square.msh")
+
+
+@pytest.mark.skipif(not os.path.exists(REFERENCE_MESH), reason="reference checkout not present")
+def test_reference_square_mesh(frgpu, oracle, quad):
+    """The mesh of dev/wave_triangle.jl:6 (assets/square.msh, Gmsh 4.1): every
+    triangle positively oriented, the neighbour flux points equal to the
+    coordinate matching of neighbour_fpidx, and the oracle's residual of a
+    uniform state zero."""
+    pts, cid = frgpu.read_gmsh(REFERENCE_MESH)
+    assert cid.shape == (2120, 3) and np.all(np.linalg.det(frgpu.rs_jacobi(cid, pts)) > 0)
+    xpl, wp = _xpl(quad, 2)
+    sp = frgpu.TriFRPSpace(pts, cid, 2, xpl, wp, cell_type=frgpu.boundary_cell_type(cid))
+    m = sp.nb_cell >= 0
+    c, f, k = np.nonzero(m)
+    d = sp.xfg[c, f, k] - sp.xfg[sp.nb_cell[m], sp.nb_face[m], sp.nb_point[m]]
+    assert np.max(np.abs(d)) < 1e-14
+    P = _oracle_problem(oracle, sp, -1.0)
+    assert np.max(np.abs(P.rhs(np.full((sp.ncell, sp.np), 0.7, order="F")))) < 1e-11
+
+
 def test_tri_create_rejects_bad_arguments(frgpu):
     """Argument checks of frgpu_tri_create run before any device work."""
     from frgpu import _lib
