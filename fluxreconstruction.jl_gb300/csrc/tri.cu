@@ -276,8 +276,13 @@ template <class T> int upload_plain(void **dst, const T *h, size_t n) {
 // doubles -> device array in the state's precision
 int upload_real(frgpu_tri *t, void **dst, const std::vector<double> &h) {
     if (t->esize == 8) return upload_plain<double>(dst, h.data(), h.size());
-    std::vector<float> f(h.begin(), h.end());
-    return upload_plain<float>(dst, f.data(), f.size());
+    try {
+        std::vector<float> f(h.begin(), h.end());
+        return upload_plain<float>(dst, f.data(), f.size());
+    } catch (const std::exception &e) {
+        fr_set_error(e.what());
+        return FRGPU_ERR_ARG;
+    }
 }
 
 void free_tri(frgpu_tri *t) {
@@ -318,9 +323,9 @@ FRGPU_API int frgpu_tri_operators(int deg, const double *r, const double *s, dou
     return FRGPU_OK;
 }
 
-FRGPU_API int frgpu_tri_create(int ncell, int deg, int precision, double a, const double *dl, const double *lf,
-                               const double *phi, const double *J, const double *iJ, const int *nb_cell,
-                               const int *nb_face, const int *nb_point, const int *cell_type, frgpu_tri **out) {
+static int tri_create_impl(int ncell, int deg, int precision, double a, const double *dl, const double *lf,
+                           const double *phi, const double *J, const double *iJ, const int *nb_cell,
+                           const int *nb_face, const int *nb_point, const int *cell_type, frgpu_tri **out) {
     TRI_REQ(out, "tri_create: null output handle");
     *out = nullptr;
     TRI_REQ(ncell > 0 && ncell <= (1 << 26), "tri_create: ncell must be in 1..2^26");
@@ -400,6 +405,19 @@ FRGPU_API int frgpu_tri_create(int ncell, int deg, int precision, double a, cons
     return FRGPU_OK;
 }
 
+// host allocations may throw: no exception crosses the C ABI
+FRGPU_API int frgpu_tri_create(int ncell, int deg, int precision, double a, const double *dl, const double *lf,
+                               const double *phi, const double *J, const double *iJ, const int *nb_cell,
+                               const int *nb_face, const int *nb_point, const int *cell_type, frgpu_tri **out) {
+    try {
+        return tri_create_impl(ncell, deg, precision, a, dl, lf, phi, J, iJ, nb_cell, nb_face, nb_point, cell_type,
+                               out);
+    } catch (const std::exception &e) {
+        fr_set_error(std::string("tri_create: ") + e.what());
+        return FRGPU_ERR_ARG;
+    }
+}
+
 FRGPU_API int frgpu_tri_destroy(frgpu_tri *t) {
     if (t) {
         cudaStreamSynchronize(t->stream);
@@ -447,7 +465,7 @@ FRGPU_API int frgpu_tri_rhs_device(frgpu_tri *t) {
  * s x s A, strictly lower triangular) on the device state: init(prob, alg;
  * dt, adaptive=false) + step! of OrdinaryDiffEq as dev/wave_triangle.jl:131-135
  * drives it (Euler: s = 1, A = 0, b = 1). */
-FRGPU_API int frgpu_tri_step_erk(frgpu_tri *t, int s, const double *A, const double *b, double dt, int nsteps) {
+static int tri_step_impl(frgpu_tri *t, int s, const double *A, const double *b, double dt, int nsteps) {
     TRI_REQ(t && A && b, "tri_step_erk: null argument");
     TRI_REQ(s >= 1 && s <= FR_ERK_MAXS, "tri_step_erk: stages must be in 1..16");
     TRI_REQ(nsteps >= 0, "tri_step_erk: negative step count");
@@ -516,6 +534,15 @@ FRGPU_API int frgpu_tri_step_erk(frgpu_tri *t, int s, const double *A, const dou
         return FRGPU_ERR_NONFINITE;
     }
     return FRGPU_OK;
+}
+
+FRGPU_API int frgpu_tri_step_erk(frgpu_tri *t, int s, const double *A, const double *b, double dt, int nsteps) {
+    try {
+        return tri_step_impl(t, s, A, b, dt, nsteps);
+    } catch (const std::exception &e) {
+        fr_set_error(std::string("tri_step_erk: ") + e.what());
+        return FRGPU_ERR_ARG;
+    }
 }
 
 FRGPU_API int frgpu_tri_stream(frgpu_tri *t, void **stream) {
