@@ -560,11 +560,20 @@ def tri_entry(nx=1024, steps=20, warmup=3, reps=20, forms=("fp64", "fp32k"), cpu
         prob.step(warmup, dt)
         l0 = prob.launches()
         secs_step = timer(lambda: prob.step(steps, dt)) / steps
-        rec = {"value": ndof * steps / (secs_step * steps), "unit": "DOF-updates/s", "step_ms": secs_step * 1e3,
+        rec = {"value": ndof / secs_step, "unit": "DOF-updates/s", "step_ms": secs_step * 1e3,
                "rhs_us": secs * 1e6, "rhs_dof_per_s": ndof / secs,
                "achieved_gflops": TRI_FLOP_PER_CELL_P3 * sp.ncell / secs / 1e9,
                "achieved_gbs_compulsory": TRI_BYTES_PER_CELL_P3[form] * sp.ncell / secs / 1e9,
                "launches_per_step": (prob.launches() - l0) / steps}
+        peak, kind = measured_peaks()
+        gbs = rec["achieved_gbs_compulsory"]
+        rec["roofline"] = {"bound": "fp64 pipe" if form == "fp64" else "latency (neighbour gathers)",
+                           "hbm": {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                                   "peak_kind": kind},
+                           "flops": {"achieved": rec["achieved_gflops"] / 1e3, "unit": "TFLOP/s",
+                                     "note": "FP64 against GB300's nominal 1.25 TFLOP/s FP64 (not measured)"
+                                     if form == "fp64" else "FP32 CUDA cores"},
+                           "kernel": f"k_tri_rhs<{'double' if form == 'fp64' else 'float'},3>"}
         out[form] = rec
         del prob
     if not cpu:
