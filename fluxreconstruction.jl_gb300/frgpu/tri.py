@@ -91,6 +91,8 @@ def tri_square_mesh(nx: int, ny: int, x0=0.0, x1=1.0, y0=0.0, y1=1.0, periodic=T
     [ncell, 3] (0-based), the vertex key that identifies periodic images (the
     vertex id itself when not periodic) and cell_type [ncell] (0 interior,
     1 a cell with a boundary face, as KitBase's UnstructPSpace marks them)."""
+    if nx < 1 or ny < 1 or (periodic and (nx < 3 or ny < 3)):
+        raise ValueError("need nx, ny >= 1 (>= 3 when periodic, so that every face has two distinct cells)")
     xs = np.linspace(x0, x1, nx + 1)
     ys = np.linspace(y0, y1, ny + 1)
     X, Y = np.meshgrid(xs, ys, indexing="ij")

@@ -182,6 +182,23 @@ def _write_gmsh(path, pts, cid, version):
             f.write("$EndElements\n")
 
 
+def test_tri_square_mesh_counts(frgpu):
+    """2 nx ny cells; on a periodic mesh every cell is interior, on a bounded
+    one exactly the cells with a face on the rectangle's edge have type 1; a
+    periodic mesh needs at least 3 squares per side."""
+    pts, cid, key, ct = frgpu.tri_square_mesh(5, 4, periodic=True)
+    assert cid.shape == (40, 3) and np.all(ct == 0)
+    pts, cid, key, ct = frgpu.tri_square_mesh(5, 4, periodic=False)
+    on_edge = np.zeros(len(cid), dtype=bool)
+    for c, v in enumerate(cid):
+        for a, b in ((v[0], v[1]), (v[1], v[2]), (v[2], v[0])):
+            pa, pb = pts[a], pts[b]
+            on_edge[c] |= bool(np.any((pa == pb) & ((pa == 0) | (pa == 1))))
+    assert np.array_equal(ct == 1, on_edge)
+    with pytest.raises(ValueError):
+        frgpu.tri_square_mesh(2, 5, periodic=True)
+
+
 @pytest.mark.parametrize("version", ["2.2", "4.1"])
 def test_read_gmsh_round_trip(frgpu, tmp_path, version):
     pts, cid, _, ct = frgpu.tri_square_mesh(4, 3, periodic=False)
