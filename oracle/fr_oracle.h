@@ -16,6 +16,12 @@
  * modal filter, conserve_prim, maxwellian) are not vendored in the reference,
  * so they are restated from their published methods; at that boundary parity
  * is unpinned (the reference cannot run here: no Julia).
+ * Triangles: the solution points are pinned to golden vectors generated from
+ * the reference's own src/Quadrature/qpmin.py; the triangle residual
+ * (dev/wave_triangle.jl, a script with no test or recorded output) is parity
+ * unpinned beyond its properties (uniform state kept, conservation, order of
+ * convergence).  Face normals of straight-sided quadrilaterals
+ * (dev/parallelogram.jl) likewise: pinned only by free-stream preservation.
  *
  * Array layouts are the reference's Julia column-major layouts:
  *   1D scalar      u[i, k]            -> u[i + ne*k]
