@@ -244,6 +244,14 @@ def test_tri_create_rejects_bad_arguments(frgpu):
     assert L.frgpu_tri_create(4, 1, 0, 1.0, d, None, d, d, d, i, i, i, i, C.byref(h)) == _lib.ERR_ARG
     assert L.frgpu_tri_create(0, 1, 0, 1.0, d, d, d, d, d, i, i, i, i, C.byref(h)) == _lib.ERR_ARG
     assert L.frgpu_tri_step_erk(None, 1, d, d, 0.1, 1) == _lib.ERR_ARG
+    assert L.frgpu_tri_operators(0, d, d, None, None, None, None) == _lib.ERR_ARG
+    assert L.frgpu_tri_operators(2, None, d, None, None, None, None) == _lib.ERR_ARG
+    assert L.frgpu_vandermonde_tri(2, d, d, 0, d, None, None) == _lib.ERR_ARG
+    with pytest.raises(ValueError):
+        frgpu.tri_operators(2, np.zeros(5), np.zeros(5))   # degree 2 takes 6 points
+    # coincident solution points: a singular Vandermonde matrix is refused
+    with pytest.raises(frgpu.FRGPUError):
+        frgpu.tri_operators(1, np.full(3, -0.5), np.full(3, -0.5))
 
 
 # ---------------------------------------------------------------- GPU
