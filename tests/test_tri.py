@@ -150,6 +150,23 @@ def test_oracle_tri_convergence(frgpu, oracle, quad, deg):
     assert np.all(rates > deg - 0.15), rates
 
 
+def test_oracle_tri_erk_forms(frgpu, oracle, quad):
+    """fro_tri_erk with Euler is fma(dt, L(u), u); with the SSPRK33 tableau it
+    agrees with the Shu-Osher form of the same method to round-off."""
+    sp = _space(frgpu, quad, 5, 5, 2)
+    P = _oracle_problem(oracle, sp, -1.0)
+    u = _wave(sp)
+    dt = 1e-3
+    e = P.erk(u, dt, 1, np.zeros((1, 1)), np.ones(1))
+    assert np.max(np.abs(e - (u + dt * P.rhs(u)))) < 1e-15
+    A = np.array([[0, 0, 0], [1, 0, 0], [0.25, 0.25, 0]])
+    b = np.array([1 / 6, 1 / 6, 2 / 3])
+    u1 = u + dt * P.rhs(u)
+    u2 = 0.75 * u + 0.25 * (u1 + dt * P.rhs(u1))
+    u3 = u / 3 + 2 / 3 * (u2 + dt * P.rhs(u2))
+    assert np.max(np.abs(P.erk(u, dt, 1, A, b) - u3)) < 1e-14
+
+
 def test_oracle_tri_boundary_cells_frozen(frgpu, oracle, quad):
     """Cells of type 1 (with a boundary face) keep du = 0; the others see no
     boundary face (dev/wave_triangle.jl:117-121)."""
