@@ -226,17 +226,19 @@ def test_read_gmsh_round_trip(frgpu, tmp_path, version):
     assert np.array_equal(frgpu.boundary_cell_type(c2), ct)
 
 
-REFERENCE_MESH = os.path.join(os.environ.get("FR_REFERENCE", "/root/reference"), "assets", "square.msh")
+REFERENCE_ASSETS = os.path.join(os.environ.get("FR_REFERENCE", "/root/reference"), "assets")
 
 
-@pytest.mark.skipif(not os.path.exists(REFERENCE_MESH), reason="reference checkout not present")
-def test_reference_square_mesh(frgpu, oracle, quad):
-    """The mesh of dev/wave_triangle.jl:6 (assets/square.msh, Gmsh 4.1): every
-    triangle positively oriented, the neighbour flux points equal to the
+@pytest.mark.skipif(not os.path.isdir(REFERENCE_ASSETS), reason="reference checkout not present")
+@pytest.mark.parametrize("name,ncell", [("square.msh", 2120), ("linesource.msh", 2122)])
+def test_reference_meshes(frgpu, oracle, quad, name, ncell):
+    """The reference's triangle meshes: assets/square.msh (dev/wave_triangle.jl:6)
+    and assets/linesource.msh (the TriFRPSpace of test/runtests.jl:22), Gmsh 4.1:
+    every triangle positively oriented, the neighbour flux points equal to the
     coordinate matching of neighbour_fpidx, and the oracle's residual of a
     uniform state zero."""
-    pts, cid = frgpu.read_gmsh(REFERENCE_MESH)
-    assert cid.shape == (2120, 3) and np.all(np.linalg.det(frgpu.rs_jacobi(cid, pts)) > 0)
+    pts, cid = frgpu.read_gmsh(os.path.join(REFERENCE_ASSETS, name))
+    assert cid.shape == (ncell, 3) and np.all(np.linalg.det(frgpu.rs_jacobi(cid, pts)) > 0)
     xpl, wp = _xpl(quad, 2)
     sp = frgpu.TriFRPSpace(pts, cid, 2, xpl, wp, cell_type=frgpu.boundary_cell_type(cid))
     m = sp.nb_cell >= 0
