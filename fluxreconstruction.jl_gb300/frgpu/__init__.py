@@ -49,6 +49,9 @@ from .api import (  # noqa: F401
     legendre_point,
     modal_filter_,
     poly_derivative_,
+    quad_face_normals,
+    quad_metric,
+    rs_jacobi_quad,
     shock_detector,
     solve,
     standard_lagrange,

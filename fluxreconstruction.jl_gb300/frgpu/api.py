@@ -193,6 +193,49 @@ class FRPSpace2D(_Space):
 
 
 # ---------------------------------------------------------------- stateless operators
+def rs_jacobi_quad(r, vertices) -> np.ndarray:
+    """Jacobians of bilinear quadrilaterals at the tensor points (r_k, r_l):
+    rs_jacobi(r, vertices) of src/Geometry/geo_jacobi.jl:77-108 as FRPSpace2D
+    calls it (src/struct.jl:135): vertices[nx, ny, 4, 2] counterclockwise from
+    the lower left; returns J[nx, ny, np, np, 2, 2] = [x_r x_s; y_r y_s] of
+    X = sum_a lambda_a(r, s) V_a."""
+    r = np.asarray(r, dtype=np.float64)
+    V = np.asarray(vertices, dtype=np.float64)
+    R, S = np.meshgrid(r, r, indexing="ij")          # point (k, l) at (r_k, r_l)
+    R, S = R[None, None, :, :, None], S[None, None, :, :, None]
+    v = [V[:, :, a, None, None, :] for a in range(4)]
+    Xr = (S - 1) * v[0] / 4 + (1 - S) * v[1] / 4 + (S + 1) * v[2] / 4 - (S + 1) * v[3] / 4
+    Xs = (R - 1) * v[0] / 4 - (R + 1) * v[1] / 4 + (R + 1) * v[2] / 4 + (1 - R) * v[3] / 4
+    return np.stack([Xr, Xs], axis=-1)
+
+
+def quad_metric(r, vertices) -> np.ndarray:
+    """iJ[nx, ny, np, np, 2, 2] = inv(J) at the solution points, the field
+    FRPSpace2D.iJ (src/struct.jl:135-143) that ODEProblem.set_metric takes."""
+    return np.asfortranarray(np.linalg.inv(rs_jacobi_quad(r, vertices)))
+
+
+def quad_face_normals(vertices):
+    """Unit normals of the straight faces of a structured quadrilateral mesh
+    (vertices[nx, ny, 4, 2]), in the orientation dev/parallelogram.jl uses:
+    n1[i, j] on x face i (between elements i-1 and i) pointing to increasing
+    i, n2[i, j] on y face j pointing to increasing j; shapes (nx+1, ny, 2) and
+    (nx, ny+1, 2)."""
+    V = np.asarray(vertices, dtype=np.float64)
+    nx, ny = V.shape[:2]
+    left = V[:, :, 3] - V[:, :, 0]                     # edge 1 -> 4 of each element
+    right = V[-1:, :, 2] - V[-1:, :, 1]                # edge 2 -> 3 of the last column
+    tx = np.concatenate([left, right], axis=0)
+    n1 = np.stack([tx[..., 1], -tx[..., 0]], axis=-1)
+    bottom = V[:, :, 1] - V[:, :, 0]                   # edge 1 -> 2
+    top = V[:, -1:, 2] - V[:, -1:, 3]                  # edge 4 -> 3 of the last row
+    ty = np.concatenate([bottom, top], axis=1)
+    n2 = np.stack([-ty[..., 1], ty[..., 0]], axis=-1)
+    n1 /= np.linalg.norm(n1, axis=-1, keepdims=True)
+    n2 /= np.linalg.norm(n2, axis=-1, keepdims=True)
+    return np.asfortranarray(n1), np.asfortranarray(n2)
+
+
 def interp_face_(fdelta: np.ndarray, f: np.ndarray, ll, lr) -> None:
     """interp_face!(fδ, f, ll, lr) (src/interpolate.jl:1-10): fδ[.., 0] = f·ll,
     fδ[.., 1] = f·lr, row by row for a matrix f, evaluated on the GPU."""
