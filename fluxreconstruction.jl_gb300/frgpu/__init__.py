@@ -13,6 +13,7 @@ from .tri import (  # noqa: F401
     read_gmsh,
     rs_jacobi,
     tri_operators,
+    tri_space_from_gmsh,
     tri_square_mesh,
     triface_quadrature,
     vandermonde_tri,

@@ -242,6 +242,14 @@ class TriFRPSpace:
         self.nb_point = np.where(self.nb_cell >= 0, self.nb_point, -1)
 
 
+def tri_space_from_gmsh(path: str, deg: int, xpl, wp) -> TriFRPSpace:
+    """TriFRPSpace(file, deg) (src/struct.jl:305-352) for a Gmsh ASCII file:
+    its triangles, the tri_quadrature(deg) points xpl and weights wp, and the
+    cells with a boundary face marked type 1."""
+    points, cellid = read_gmsh(path)
+    return TriFRPSpace(points, cellid, deg, xpl, wp, cell_type=boundary_cell_type(cellid))
+
+
 class TriAdvectionProblem:
     """The ODEProblem(dudt!, u, tspan, p) of dev/wave_triangle.jl:44-135
     (u_t + a u_x + a u_y = 0 on a TriFRPSpace) held on the GPU; ``u[ncell, np]``.

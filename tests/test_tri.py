@@ -224,6 +224,9 @@ def test_read_gmsh_round_trip(frgpu, tmp_path, version):
     p2, c2 = frgpu.read_gmsh(path)
     assert np.array_equal(p2, pts) and np.array_equal(c2, cid)
     assert np.array_equal(frgpu.boundary_cell_type(c2), ct)
+    xpl, wp = np.stack([[-2 / 3, 1 / 3, -2 / 3], [1 / 3, -2 / 3, -2 / 3]], axis=1), np.full(3, 1 / 3)
+    sp = frgpu.tri_space_from_gmsh(path, 1, xpl, wp)
+    assert sp.ncell == len(cid) and np.array_equal(sp.cell_type, ct)
 
 
 REFERENCE_ASSETS = os.path.join(os.environ.get("FR_REFERENCE", "/root/reference"), "assets")
