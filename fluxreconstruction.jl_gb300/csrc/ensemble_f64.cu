@@ -3,11 +3,8 @@
 #include "ensemble_kernels.cuh"
 
 template <bool LEARNED> static int launch(const EnsArgs<double> &a, int grid, size_t smem, cudaStream_t st) {
-    static size_t attr_bytes = 0; // the opt-in is raised whenever a launch needs more
-    if (smem > attr_bytes) {
-        FR_CUDA(cudaFuncSetAttribute(k_ensemble<double, LEARNED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr_bytes = smem;
-    }
+    static fr_smem_optin optin; // raised per device whenever a launch needs more
+    if (int rc = fr_raise_smem(k_ensemble<double, LEARNED>, smem, optin)) return rc;
     k_ensemble<double, LEARNED><<<grid, ENS_THREADS, smem, st>>>(a);
     FR_CUDA(cudaGetLastError());
     return FRGPU_OK;

@@ -181,15 +181,15 @@ int fr_launch_euler2d_reduce(frgpu_problem *p, const void *state, const void *lo
 // the same partial/final reduction kernels as frgpu_reduce, but its partial
 // sums live in the file-scope device array below instead of memory allocated
 // per problem.  The array is 4096 x 6 doubles (192 KiB); one partial block
-// covers one solution point q of up to NOALLOC_POINTS_PER_BLOCK elements, so a
-// call needs ceil(nx * ny / 16384) * (deg+1)^2 <= 4096 blocks: at most
-// 67,108,864 solution points (nx * ny * (deg+1)^2), and larger meshes are
-// rejected.  Every GPU that loads the library keeps the array
-// until the process exits.
+// covers one solution point q of up to NOALLOC_POINTS_PER_BLOCK = 16384
+// elements, so a call needs ceil(nx * ny / 16384) * (deg+1)^2 <= 4096 blocks,
+// and meshes that need more are rejected.  (That allows at most 67,108,864
+// solution points nx * ny * (deg+1)^2, reached when nx * ny is a multiple of
+// 16384; because of the rounding up, some smaller meshes are rejected too.)
+// Every GPU that loads the library keeps the array until the process exits.
 namespace {
 constexpr int NOALLOC_MAX_BLOCKS = 4096;
 constexpr long NOALLOC_POINTS_PER_BLOCK = (long)RED_THREADS * 64;
-constexpr int FR_MAX_DEVICES = 64;
 __device__ __align__(256) double g_noalloc_partials[NOALLOC_MAX_BLOCKS * 6];
 
 // Device address of g_noalloc_partials, looked up once per device (host code
@@ -235,6 +235,10 @@ extern "C" FRGPU_API int frgpu_reduce2d_noalloc(const void *d_state, const void 
         fr_set_error("reduce2d_noalloc: unknown precision");
         return FRGPU_ERR_ARG;
     }
+    if (precision == FRGPU_FP64 && d_lo) {
+        fr_set_error("reduce2d_noalloc: d_lo must be NULL with FRGPU_FP64 (only the FP32K form has a low part)");
+        return FRGPU_ERR_ARG;
+    }
     if (nx < 1 || ny < 1 || deg < 1 || deg > 5 || !(dx > 0) || !(dy > 0) || !(gamma > 1)) {
         fr_set_error("reduce2d_noalloc: need nx, ny >= 1, 1 <= deg <= 5, dx, dy > 0 and gamma > 1");
         return FRGPU_ERR_ARG;
@@ -245,9 +249,10 @@ extern "C" FRGPU_API int frgpu_reduce2d_noalloc(const void *d_state, const void 
     const long eblocks = (long)((plane + NOALLOC_POINTS_PER_BLOCK - 1) / NOALLOC_POINTS_PER_BLOCK);
     const long nblocks = eblocks * np * np;
     if (nblocks > NOALLOC_MAX_BLOCKS) {
-        fr_set_error("reduce2d_noalloc: " + std::to_string(npts) + " solution points exceed the maximum of " +
-                     std::to_string((long)NOALLOC_MAX_BLOCKS * NOALLOC_POINTS_PER_BLOCK) +
-                     " that the static scratch array holds");
+        fr_set_error("reduce2d_noalloc: " + std::to_string(npts) + " solution points need " +
+                     std::to_string(nblocks) + " partial blocks (ceil(nx*ny/" +
+                     std::to_string(NOALLOC_POINTS_PER_BLOCK) + ") * (deg+1)^2), which exceed the maximum of " +
+                     std::to_string(NOALLOC_MAX_BLOCKS) + " that the static scratch array holds");
         return FRGPU_ERR_ARG;
     }
     double *part = nullptr;

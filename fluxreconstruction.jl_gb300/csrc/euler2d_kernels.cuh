@@ -713,13 +713,10 @@ int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     a.be3 = (Real)p->meth.be3;
     a.s3 = (Real)p->meth.s3;
     auto kern = k_euler2d<Real, NP, FLUX, MODE, STAGE, FUSE, MET>;
-    // the dynamic shared-memory opt-in is set once per instantiation (and on
-    // every prepare pass, which precedes each graph capture)
-    static bool attr_set = false;
-    if (!attr_set || p->prepare_only) {
-        FR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::bytes));
-        attr_set = true;
-    }
+    // the dynamic shared-memory opt-in is raised once per instantiation and
+    // device (and on every prepare pass, which precedes each graph capture)
+    static fr_smem_optin optin;
+    if (int rc = fr_raise_smem(kern, S::bytes, optin, p->prepare_only)) return rc;
     if (p->prepare_only) return FRGPU_OK;
     if (FUSE) FR_CUDA(cudaMemsetAsync(p->d_count, 0, sizeof(int) * 4, p->stream));
     dim3 grid((a.nx + T::TX - 1) / T::TX, (a.ny + T::TY - 1) / T::TY);

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -97,6 +98,9 @@ constexpr int FR_RED_FINAL = FR_RED_BLOCKS * 6;
 constexpr int FR_RED_WP = FR_RED_BLOCKS * 6 + 8;
 constexpr int FR_RED_SIZE = FR_RED_BLOCKS * 6 + 8 + 64;
 
+// Devices a process may drive (per-device caches below).
+constexpr int FR_MAX_DEVICES = 64;
+
 // Current u^n buffers of a problem (FP32K ping-pongs the high part).
 inline void *fr_state_hi(frgpu_problem *p) { return p->parity ? p->s1 : p->s0; }
 inline void *fr_state_tmp(frgpu_problem *p) { return p->parity ? p->s0 : p->s1; }
@@ -109,6 +113,27 @@ int fr_cuda_fail(cudaError_t e, const char *what);
         cudaError_t _e = (call);                                                                                   \
         if (_e != cudaSuccess) return fr_cuda_fail(_e, #call);                                                     \
     } while (0)
+
+// The dynamic shared-memory opt-in of one kernel, as raised on each device:
+// cudaFuncSetAttribute acts on the current device only, so a process that
+// launches the kernel on a second GPU must raise it there too.  Static
+// instances start at zero.
+struct fr_smem_optin {
+    std::atomic<size_t> bytes[FR_MAX_DEVICES];
+};
+template <class Kern> inline int fr_raise_smem(Kern kern, size_t need, fr_smem_optin &st, bool force = false) {
+    int dev = 0;
+    FR_CUDA(cudaGetDevice(&dev));
+    const bool known = dev >= 0 && dev < FR_MAX_DEVICES;
+    if (!force && known && st.bytes[dev].load(std::memory_order_acquire) >= need) return 0;
+    FR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    if (known) {
+        size_t cur = st.bytes[dev].load(std::memory_order_acquire);
+        while (cur < need && !st.bytes[dev].compare_exchange_weak(cur, need, std::memory_order_acq_rel)) {
+        }
+    }
+    return 0;
+}
 
 // Setup math (setup.cpp)
 namespace frsetup {

@@ -624,8 +624,10 @@ FRGPU_API int frgpu_rhs(frgpu_problem *p, double *du, const double *u, double t)
     FR_CATCH
 }
 
-// Replay nsteps fused steps of the problem's method (p->meth) from the step graphs.
-static int run_fused_steps(frgpu_problem *p, double dt, int nsteps) {
+// Replay nsteps fused steps of the problem's method (p->meth) from the step
+// graphs; `wait` = 0 enqueues them and leaves the status check to the next
+// synchronising call.
+static int run_fused_steps(frgpu_problem *p, double dt, int nsteps, bool wait = true) {
     if (dt != p->host_dt) {
         FR_CUDA(cudaMemcpyAsync(p->d_dt, &dt, sizeof(double), cudaMemcpyHostToDevice, p->stream));
         FR_CUDA(cudaStreamSynchronize(p->stream));
@@ -641,7 +643,7 @@ static int run_fused_steps(frgpu_problem *p, double dt, int nsteps) {
         if (p->d.precision == FRGPU_FP32K) p->parity ^= 1;
         p->launches += p->graph_launches;
     }
-    return check_status(p);
+    return wait ? check_status(p) : FRGPU_OK;
 }
 
 static void use_method(frgpu_problem *p, const fr_method &m) {
@@ -662,6 +664,20 @@ FRGPU_API int frgpu_step_ssprk3(frgpu_problem *p, double dt, int nsteps) {
     FR_TRY
     use_method(p, fr_method());
     return run_fused_steps(p, dt, nsteps);
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_step_ssprk3_async(frgpu_problem *p, double dt, int nsteps) {
+    FR_REQ(p, "step_ssprk3_async: null problem");
+    FR_REQ(nsteps >= 0, "step_ssprk3_async: negative step count");
+    if (!(dt > 0.0) || !std::isfinite(dt)) {
+        fr_set_error("step_ssprk3_async: dt must be positive and finite");
+        return FRGPU_ERR_DT;
+    }
+    if (nsteps == 0) return FRGPU_OK;
+    FR_TRY
+    use_method(p, fr_method());
+    return run_fused_steps(p, dt, nsteps, false);
     FR_CATCH
 }
 
@@ -992,8 +1008,9 @@ FRGPU_API long frgpu_problem_launches(const frgpu_problem *p) { return p ? p->la
 
 FRGPU_API int frgpu_synchronize(frgpu_problem *p) {
     FR_REQ(p, "synchronize: null problem");
-    FR_CUDA(cudaStreamSynchronize(p->stream));
-    return FRGPU_OK;
+    FR_TRY
+    return check_status(p);
+    FR_CATCH
 }
 
 // ------------------------------------------------------------------ stateless operators

@@ -30,6 +30,8 @@ from .api import (  # noqa: F401
     L1_error,
     L2_error,
     Linf_error,
+    quadrature_L2_error,
+    refined_at_coarse_points,
     ODEProblem,
     RK4,
     SSPRK22,

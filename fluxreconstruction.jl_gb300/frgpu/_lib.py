@@ -62,6 +62,7 @@ SIGNATURES = {
     "frgpu_state_download": (C.c_int, [_VP, _D]),
     "frgpu_rhs": (C.c_int, [_VP, _D, _D, C.c_double]),
     "frgpu_step_ssprk3": (C.c_int, [_VP, C.c_double, C.c_int]),
+    "frgpu_step_ssprk3_async": (C.c_int, [_VP, C.c_double, C.c_int]),
     "frgpu_cfl_dt": (C.c_int, [_VP, C.c_double, _D]),
     "frgpu_reduce": (C.c_int, [_VP, _D, _D]),
     "frgpu_set_filter": (C.c_int, [_VP, C.c_int, C.c_double, C.c_double, C.c_double]),

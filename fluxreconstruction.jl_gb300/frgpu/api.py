@@ -301,6 +301,49 @@ def Linf_error(u, ue, dx):
     return float(np.max(np.abs(np.asarray(u) - np.asarray(ue)) * dx))
 
 
+def quadrature_L2_error(u, ue, dx, dy, w1):
+    """L2 norm of u - ue over a uniform 2D mesh by the solution points' Gauss
+    quadrature: sqrt(sum_e sum_kl w_k w_l (dx dy / 4) |u - ue|^2), for arrays
+    u[i, j, k, l] (one variable) of the reference layout; w1 are the 1D
+    Gauss-Legendre weights on [-1, 1]."""
+    e = np.asarray(u, dtype=np.float64) - np.asarray(ue, dtype=np.float64)
+    W = np.outer(w1, w1) * (dx * dy / 4.0)
+    return float(np.sqrt(np.einsum("ijkl,kl->", e * e, W)))
+
+
+def _lagrange_rows(nodes, x):
+    """rows[a, b] = l_b(x_a): the Lagrange basis of `nodes` at the points x."""
+    nodes = np.asarray(nodes, dtype=np.float64)
+    x = np.asarray(x, dtype=np.float64)
+    rows = np.ones((len(x), len(nodes)))
+    for b in range(len(nodes)):
+        for m in range(len(nodes)):
+            if m != b:
+                rows[:, b] *= (x - nodes[m]) / (nodes[b] - nodes[m])
+    return rows
+
+
+def refined_at_coarse_points(u_fine, xpl):
+    """Values at the solution points of a uniform 2D mesh of a solution computed
+    on the mesh refined twice in each direction (fine element 2i + a, 2j + b
+    inside coarse element i, j).  u_fine[I, J, k, l, m] in the reference layout;
+    xpl are the solution points on [-1, 1] of both meshes.  Coarse point r lies in
+    the fine element a = (r > 0) at the fine coordinate 2r + 1 - 2a, where the
+    fine element's Lagrange interpolant is evaluated.  Returns u[i, j, k, l, m]."""
+    xpl = np.asarray(xpl, dtype=np.float64)
+    nxf, nyf, npk, npl, nv = u_fine.shape
+    if nxf % 2 or nyf % 2:
+        raise ValueError("the fine mesh must have an even number of elements in each direction")
+    side = (xpl > 0).astype(int)
+    L = _lagrange_rows(xpl, 2 * xpl + 1 - 2 * side)
+    uf = np.asarray(u_fine, dtype=np.float64).reshape(2, nxf // 2, 2, nyf // 2, npk, npl, nv, order="F")
+    out = np.zeros((nxf // 2, nyf // 2, npk, npl, nv), order="F")
+    for k in range(npk):
+        for l in range(npl):
+            out[:, :, k, l, :] = np.einsum("K,L,IJKLm->IJm", L[k], L[l], uf[side[k], :, side[l]])
+    return out
+
+
 # ---------------------------------------------------------------- problems
 class ODEProblem:
     """The object FRAdvectionProblem / FREulerProblem return (an ODEProblem of
@@ -329,6 +372,10 @@ class ODEProblem:
         uf = _f64(u)
         if uf.shape != self.shape:
             raise ValueError(f"u has shape {uf.shape}, expected {self.shape}")
+        if isinstance(du, np.ndarray) and du.dtype == np.float64 and du.flags.f_contiguous and \
+                du.shape == self.shape and du.flags.writeable:
+            check(L.lib().frgpu_rhs(self._h, dptr(du), dptr(uf), float(t)))  # straight into the caller's array
+            return
         out = np.zeros(self.shape, order="F")
         check(L.lib().frgpu_rhs(self._h, dptr(out), dptr(uf), float(t)))
         du[...] = out
@@ -526,6 +573,15 @@ class Integrator:
         else:
             a = self.alg
             check(L.lib().frgpu_step_erk(self.prob._h, len(a.b), dptr(a.A), dptr(a.b), dt, int(n)))
+        self.t += n * dt
+
+    def step_async(self, n: int = 1, dt: float | None = None) -> None:
+        """Queue n SSPRK3 steps and return without waiting; ``synchronize()``
+        (or the next synchronous call) reports their device status."""
+        if self.alg is not None:
+            raise NotImplementedError("step_async queues the fused SSPRK3 step")
+        dt = self.dt if dt is None else float(dt)
+        check(L.lib().frgpu_step_ssprk3_async(self.prob._h, dt, int(n)))
         self.t += n * dt
 
     def set_filter(self, indicator="plain", lam=5e-4, S0=None, kappa=9.0) -> None:

@@ -226,6 +226,11 @@ class TriFRPSpace:
         self.cell_type = (np.zeros(ncell, dtype=np.int32) if cell_type is None
                           else np.asarray(cell_type, dtype=np.int32))
         self.J = rs_jacobi(self.cellid, self.points)
+        det = np.linalg.det(self.J)
+        bad = np.flatnonzero(~(det > 0))
+        if bad.size:
+            raise ValueError(f"{bad.size} cell(s) are clockwise or degenerate (det J <= 0), for example cells "
+                             f"{bad[:8].tolist()}: TriFRPSpace needs counterclockwise vertex order")
         self.iJ = np.linalg.inv(self.J)
         self.V, self.dl, self.lf, self.phi = tri_operators(deg, self.xpl[:, 0], self.xpl[:, 1])
         self.xfl, self.wf = triface_quadrature(deg)

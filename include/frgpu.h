@@ -148,6 +148,13 @@ FRGPU_API int frgpu_rhs(frgpu_problem *p, double *du, const double *u, double t)
  * are replayed from a captured CUDA graph; the post-step filter configured by
  * frgpu_set_filter runs after every step. */
 FRGPU_API int frgpu_step_ssprk3(frgpu_problem *p, double dt, int nsteps);
+/* frgpu_step_ssprk3 without waiting: the steps are queued on the problem's
+ * stream and the call returns at once (the same step!(itg) calls; a host loop
+ * can do other work, or record events, meanwhile).  The device status of
+ * these steps (non-finite or unphysical values) is reported by the next
+ * synchronising call: frgpu_synchronize, frgpu_step_ssprk3, frgpu_reduce or a
+ * state download. */
+FRGPU_API int frgpu_step_ssprk3_async(frgpu_problem *p, double dt, int nsteps);
 /* nsteps of a fixed-step explicit Runge-Kutta method given by its Butcher
  * tableau: A (s x s, row-major, strictly lower triangular) and b (s), s <= 16
  * (OrdinaryDiffEq's Midpoint, Heun, RK4, Tsit5, ... with adaptive=false, as
@@ -221,6 +228,8 @@ FRGPU_API int frgpu_problem_set_option(frgpu_problem *p, int option, int value);
 FRGPU_API int frgpu_problem_device_state(frgpu_problem *p, void **dptr, int *elem_bytes);
 FRGPU_API int frgpu_problem_stream(frgpu_problem *p, void **stream);
 FRGPU_API long frgpu_problem_launches(const frgpu_problem *p);
+/* Wait for the problem's stream; returns the status of the work queued since
+ * the last check (FRGPU_ERR_NONFINITE, FRGPU_ERR_UNPHYSICAL, ...). */
 FRGPU_API int frgpu_synchronize(frgpu_problem *p);
 
 /* ======================================================================
@@ -307,15 +316,19 @@ FRGPU_API int frgpu_ensemble_features(frgpu_ensemble *e, float *feat, int *label
  * device byte, and processes that fix their device footprint at start-up.
  * Inputs and outputs are the caller's device memory: the state d_state
  * (u[nx, ny, deg+1, deg+1, 4] in the Julia layout; double for FRGPU_FP64,
- * float for FRGPU_FP32K, with d_lo the optional float low part), the
+ * with d_lo = NULL, or float for FRGPU_FP32K, with d_lo either NULL or the
+ * float low part in the same layout, added to the state), the
  * quadrature weights d_wp[(deg+1)^2] (wp[k + (deg+1) l] = w_k w_l), and d_out[6]
  * receiving the FP64 conserved sums (4), the maximum wave speed and the
  * maximum CFL rate max((|u|+c)/dx + (|v|+c)/dy) -- the values frgpu_reduce and
  * frgpu_cfl_dt compute.  The work is queued on `stream` (NULL = legacy
  * default stream) and nothing is synchronised.  Scratch is a fixed 192 KiB
  * device array inside the library, held by every GPU that loads it until the
- * process exits; meshes above 67,108,864 solution points (nx*ny*(deg+1)^2)
- * are rejected with FRGPU_ERR_ARG.  No cudaMalloc/cudaFree is called.  The
+ * process exits.  A call needs ceil(nx*ny / 16384) * (deg+1)^2 partial blocks
+ * of it and at most 4096 fit; meshes that need more are rejected with
+ * FRGPU_ERR_ARG (at most 67,108,864 solution points nx*ny*(deg+1)^2, and
+ * fewer when nx*ny is not a multiple of 16384).  A non-NULL d_lo with
+ * FRGPU_FP64 is rejected too.  No cudaMalloc/cudaFree is called.  The
  * first call on each device looks up the array's device address, so make
  * that first call before any stream capture.  All calls share the one array:
  * calls that overlap on the GPU (different streams, or different host

@@ -863,11 +863,31 @@ void fro_ssprk3(const fro_cfg *c, double *u, double dt, int nsteps, double *work
     const double third = 1.0 / 3.0;
     for (int it = 0; it < nsteps; ++it) {
         fro_rhs(c, k, u);
+#ifdef _OPENMP
+#pragma omp parallel for OMP_THREADS schedule(static)
+#endif
         for (long q = 0; q < n; ++q) s[q] = fma(dt, k[q], u[q]);
         fro_rhs(c, k, s);
+#ifdef _OPENMP
+#pragma omp parallel for OMP_THREADS schedule(static)
+#endif
         for (long q = 0; q < n; ++q) s[q] = fma(dt, k[q], fma(3.0, u[q], s[q])) * 0.25;
         fro_rhs(c, k, s);
+#ifdef _OPENMP
+#pragma omp parallel for OMP_THREADS schedule(static)
+#endif
         for (long q = 0; q < n; ++q) u[q] = fma(2.0 * dt, k[q], fma(2.0, s[q], u[q])) * third;
+    }
+}
+
+/* The time loop of example/shock-vortex.jl:294-321 with SSPRK3 in place of
+ * Midpoint: nsteps of (one SSPRK3 step, then the indicator + :l2 filter of
+ * fro_filter2d on every element).  work holds 2 * ndof doubles. */
+void fro_ssprk3_filtered(const fro_cfg *c, double *u, double dt, int nsteps, double *work, const double *V,
+                         const double *iV, double lam, double S0, double kappa) {
+    for (int it = 0; it < nsteps; ++it) {
+        fro_ssprk3(c, u, dt, 1, work);
+        fro_filter2d(c, u, V, iV, lam, S0, kappa, NULL);
     }
 }
 

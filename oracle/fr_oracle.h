@@ -79,6 +79,9 @@ long fro_ndof(const fro_cfg *c);
 void fro_rhs(const fro_cfg *c, double *du, const double *u);
 /* Shu-Osher SSPRK3, nsteps fixed steps of size dt; work must hold 2*ndof doubles */
 void fro_ssprk3(const fro_cfg *c, double *u, double dt, int nsteps, double *work);
+/* nsteps of (SSPRK3 step, indicator + :l2 filter), example/shock-vortex.jl:294-321 */
+void fro_ssprk3_filtered(const fro_cfg *c, double *u, double dt, int nsteps, double *work, const double *V,
+                         const double *iV, double lam, double S0, double kappa);
 /* explicit Runge-Kutta of s stages (A: s x s row-major, b: s), fixed dt;
  * work must hold (s + 1) * ndof doubles */
 void fro_erk(const fro_cfg *c, double *u, double dt, int nsteps, int s, const double *A, const double *b,

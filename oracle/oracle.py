@@ -86,6 +86,8 @@ def lib():
             "fro_rhs": (None, [C.POINTER(Cfg), _D, _D]),
             "fro_ssprk3": (None, [C.POINTER(Cfg), _D, C.c_double, C.c_int, _D]),
             "fro_erk": (None, [C.POINTER(Cfg), _D, C.c_double, C.c_int, C.c_int, _D, _D, _D]),
+            "fro_ssprk3_filtered": (None, [C.POINTER(Cfg), _D, C.c_double, C.c_int, _D, _D, _D, C.c_double,
+                                           C.c_double, C.c_double]),
             "fro_filter2d": (C.c_int, [C.POINTER(Cfg), _D, _D, _D, C.c_double, C.c_double,
                                        C.c_double, _I]),
             "fro_filter1d": (C.c_int, [C.POINTER(Cfg), _D, C.c_int, _D, _D, C.c_double, _I]),
@@ -339,6 +341,18 @@ class Problem:
         uf = np.array(u, dtype=np.float64, order="F", copy=True)
         work = np.zeros(2 * uf.size)
         lib().fro_ssprk3(C.byref(self.cfg), uf.ctypes.data_as(_D), float(dt), int(nsteps), _p(work))
+        return uf
+
+    def ssprk3_filtered(self, u: np.ndarray, dt: float, nsteps: int, lam: float, S0: float,
+                        kappa: float) -> np.ndarray:
+        """nsteps of (SSPRK3 step, plain indicator + :l2 filter), the loop of
+        example/shock-vortex.jl:294-321 with SSPRK3; 2D Euler."""
+        uf = np.array(u, dtype=np.float64, order="F", copy=True)
+        work = np.zeros(2 * uf.size)
+        V = _f64(self.space.V)
+        iV = _f64(self.space.iV)
+        lib().fro_ssprk3_filtered(C.byref(self.cfg), uf.ctypes.data_as(_D), float(dt), int(nsteps), _p(work),
+                                  _p(V), _p(iV), float(lam), float(S0), float(kappa))
         return uf
 
     def erk(self, u: np.ndarray, dt: float, nsteps: int, A, b) -> np.ndarray:

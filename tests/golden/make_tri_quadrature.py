@@ -46,4 +46,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FR_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_tri_quadrature.py <reference checkout> (or set FR_REFERENCE)")
+    main(ref)

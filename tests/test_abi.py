@@ -135,3 +135,13 @@ def test_new_entry_points_reject_bad_arguments(frgpu):
     with pytest.raises(ValueError):
         frgpu.ExplicitRK([[0.0, 0.5], [0.0, 0.0]], [0.5, 0.5])   # implicit entry above the diagonal
     assert frgpu.Midpoint().A[1, 0] == 0.5 and frgpu.Tsit5().b[-1] == 0.0
+
+
+def test_allocation_free_reduction_calls_no_allocator():
+    """frgpu_reduce2d_noalloc and its helpers (the end of csrc/euler2d.cu, from
+    the scratch array's declaration on) name no device or host allocator."""
+    src = open(os.path.join(ROOT, "fluxreconstruction.jl_gb300", "csrc", "euler2d.cu")).read()
+    body = src[src.index("constexpr int NOALLOC_MAX_BLOCKS"):]
+    assert "frgpu_reduce2d_noalloc" in body
+    for call in ("cudaMalloc", "cudaFree", "malloc(", "calloc(", "new ", "std::vector", "cudaHostAlloc"):
+        assert call not in body, call

@@ -229,10 +229,24 @@ def test_read_gmsh_round_trip(frgpu, tmp_path, version):
     assert sp.ncell == len(cid) and np.array_equal(sp.cell_type, ct)
 
 
-REFERENCE_ASSETS = os.path.join(os.environ.get("FR_REFERENCE", "/root/reference"), "assets")
+# the reference checkout's meshes, when FR_REFERENCE names a checkout
+REFERENCE_ASSETS = os.path.join(os.environ["FR_REFERENCE"], "assets") if os.environ.get("FR_REFERENCE") else None
 
 
-@pytest.mark.skipif(not os.path.isdir(REFERENCE_ASSETS), reason="reference checkout not present")
+def test_clockwise_cells_are_rejected(frgpu):
+    """TriFRPSpace needs counterclockwise cells (det J > 0); a mesh with a
+    clockwise cell is refused with the cell named."""
+    pts, cid, key, ct = frgpu.tri_square_mesh(3, 3, periodic=False)
+    bad = cid.copy()
+    bad[4] = bad[4][[0, 2, 1]]
+    xpl, wp = np.stack([[-2 / 3, 1 / 3, -2 / 3], [1 / 3, -2 / 3, -2 / 3]], axis=1), np.full(3, 1 / 3)
+    frgpu.TriFRPSpace(pts, cid, 1, xpl, wp, key, ct)
+    with pytest.raises(ValueError, match=r"clockwise.*\[4\]"):
+        frgpu.TriFRPSpace(pts, bad, 1, xpl, wp, key, ct)
+
+
+@pytest.mark.skipif(REFERENCE_ASSETS is None or not os.path.isdir(REFERENCE_ASSETS),
+                    reason="set FR_REFERENCE to a reference checkout to read its meshes")
 @pytest.mark.parametrize("name,ncell", [("square.msh", 2120), ("linesource.msh", 2122)])
 def test_reference_meshes(frgpu, oracle, quad, name, ncell):
     """The reference's triangle meshes: assets/square.msh (dev/wave_triangle.jl:6)
