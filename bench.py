@@ -553,7 +553,7 @@ def density_wave_entry(args, dist, ws):
     net = learned.load_trained()
     out = {"workload": WAVE_WORKLOAD, "ndof": NDOF}
     for form, precision, indicator in (("fp32k", "fp32k", "none"), ("fp32k_learned", "fp32k", "mlp"),
-                                       ("fp64_plain", "fp64", "plain")):
+                                       ("fp64", "fp64", "none"), ("fp64_plain", "fp64", "plain")):
         prob = frgpu.FREuler2DProblem(u0, (0, 1), ps, GAMMA, flux="lf", bc="period", precision=precision)
         itg = frgpu.init(prob, dt=1.0)
         dt = itg.cfl_dt(CFL)
@@ -577,11 +577,31 @@ def density_wave_entry(args, dist, ws):
                        "kernel": "k_euler2d<float,4,LF,FP32K,stage> (fused residual + SSPRK3 stage)",
                        "workload": WAVE_WORKLOAD, "bytes_per_launch": bytes_launch,
                        "bytes_per_dof_stage": BYTES_PER_DOF_STAGE["fp32k"]}
+    p64 = FMA_PEAKS.get("fp64", 0.0)
+    fl = E2D_FP64_FLOP_PER_DOF_STAGE * NDOF / (out["fp64"]["stage_us"] * 1e-6)
+    out["fp64_roofline"] = {"bound": "fp64 pipe", "achieved": fl / 1e12, "peak": p64 / 1e12, "unit": "TFLOP/s",
+                            "frac": fl / max(p64, 1.0), "flop_per_dof_stage": E2D_FP64_FLOP_PER_DOF_STAGE,
+                            "kernel": "k_euler2d<double,4,LF,FP64,stage>",
+                            "peak_kind": "measured (frgpu_fma_peak, FP64 FMA, this run)"}
     out["accuracy_note"] = ("FP32K's error here is its rounding floor (about 2e-7 RMS in density against the exact "
                             "solution), FP64's is round-off (about 5e-13): the discretisation error of p = 3 on "
                             "512^2 over t < 0.01 is below both, so the matched-error gate applies to the shock-vortex "
                             "workload instead")
     return out
+
+
+FMA_PEAKS = {}
+
+
+def measure_fma_peaks():
+    """FP64 / FP32 / FP32-pair FMA throughput of this GPU (frgpu_fma_peak)."""
+    import frgpu
+
+    for k in ("fp64", "fp32", "fp32x2"):
+        FMA_PEAKS[k] = frgpu.fma_peak(k)
+    return {"fp64": FMA_PEAKS["fp64"] / 1e12, "fp32": FMA_PEAKS["fp32"] / 1e12, "fp32x2": FMA_PEAKS["fp32x2"] / 1e12,
+            "unit": "TFLOP/s", "how": "8 independent FMA chains per thread, 8 CTAs of 256 threads per SM, best of "
+                                      "3 CUDA-event timed launches after one warm-up"}
 
 
 def peak_kind_label(kind):
@@ -679,7 +699,12 @@ def bgk_entry(steps=400, warmup=5):
     return out
 
 
-TRI_FLOP_PER_CELL_P3 = 2800      # operations of k_tri_rhs<., 3> per cell, counted from the kernel
+# FP64 floating-point operations (dadd + dmul + 2 dfma, ncu instruction counters;
+# profiles/fp64_flops_512x512_p3.md): k_tri_rhs<double, 3> per cell, and the
+# 2D Euler stage kernel k_euler2d<double, 4, LF, FP64, stage> per DOF and stage
+# (mean of the three SSPRK3 stages on the 512 x 512 density wave)
+TRI_FLOP_PER_CELL_P3 = 3090
+E2D_FP64_FLOP_PER_DOF_STAGE = 70.8
 TRI_BYTES_PER_CELL_P3 = {"fp64": 249, "fp32k": 137}  # own state + residual + geometry + neighbour tables
 
 
@@ -725,6 +750,7 @@ def tri_entry(nx=1024, steps=20, warmup=3, reps=20, forms=("fp64", "fp32k"), cpu
         rec = {"value": ndof / secs_step, "unit": "DOF-updates/s", "step_ms": secs_step * 1e3,
                "rhs_us": secs * 1e6, "rhs_dof_per_s": ndof / secs,
                "achieved_gflops": TRI_FLOP_PER_CELL_P3 * sp.ncell / secs / 1e9,
+               "flops_per_cell": TRI_FLOP_PER_CELL_P3,
                "achieved_gbs_compulsory": TRI_BYTES_PER_CELL_P3[form] * sp.ncell / secs / 1e9,
                "launches_per_step": (prob.launches() - l0) / steps}
         peak, kind = measured_peaks()
@@ -733,7 +759,10 @@ def tri_entry(nx=1024, steps=20, warmup=3, reps=20, forms=("fp64", "fp32k"), cpu
                            "hbm": {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                                    "peak_kind": kind},
                            "flops": {"achieved": rec["achieved_gflops"] / 1e3, "unit": "TFLOP/s",
-                                     "note": "FP64 against GB300's nominal 1.25 TFLOP/s FP64 (not measured)"
+                                     "peak": FMA_PEAKS.get(form == "fp64" and "fp64" or "fp32x2", 0) / 1e12,
+                                     "frac": rec["achieved_gflops"] * 1e9 /
+                                     max(FMA_PEAKS.get(form == "fp64" and "fp64" or "fp32x2", 0), 1.0),
+                                     "note": "against the FMA throughput measured by frgpu_fma_peak in this run"
                                      if form == "fp64" else "FP32 CUDA cores"},
                            "kernel": f"k_tri_rhs<{'double' if form == 'fp64' else 'float'},3>"}
         out[form] = rec
@@ -852,6 +881,7 @@ def main():
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     if args.workload is not None:
+        measure_fma_peaks()
         if args.workload == "density_wave":
             r = density_wave_entry(args, None, 1)
         elif args.workload == "ensemble":
@@ -872,6 +902,7 @@ def main():
     sampler = ClockSampler(torch.cuda.current_device())
     if rank == 0:
         sampler.start()
+    fma_peaks = measure_fma_peaks()
     res = headline_arm(args, dist, rank, ws, dt)
     configs = {}
     if not args.no_configs:
@@ -922,6 +953,11 @@ def main():
         "roofline": dw.get("roofline"),
         "e2e": res.get("e2e"),
         "e2e_rhs": res.get("e2e_rhs"),
+        "fp64_peak_measured": fma_peaks,
+        "fp64_forms_vs_fp64_peak": {
+            "density_wave_fp64": (dw.get("fp64_roofline") or {}).get("frac"),
+            "triangles_fp64": ((configs.get("triangles_advection_2M_cells_p3") or {}).get("fp64") or {})
+            .get("roofline", {}).get("flops", {}).get("frac")},
         "gpu_launches": lrn["launches_timed"],
         "clocks": clocks,
         "cpu_baseline": cpu,

@@ -138,11 +138,11 @@ static EnsArgs<Real> ens_args(frgpu_ensemble *e, int n_cta, int n_warp, double t
     a.steps_out = e->d_steps;
     a.failed = e->d_failed;
     a.status = e->d_status;
-    a.mlp = frmlp::MLPDev{nullptr, nullptr, nullptr, nullptr};
+    a.mlp = frmlp::MLPDev{nullptr, nullptr, nullptr, nullptr, nullptr};
     if (e->mlp) {
         const fr_mlp_ptrs m = fr_mlp_device(e->mlp);
         a.mlp = frmlp::MLPDev{m.P, (const __nv_bfloat16 *)m.W1, (const __nv_bfloat16 *)m.W2,
-                              (const __nv_bfloat16 *)m.W2T};
+                              (const __nv_bfloat16 *)m.W2T, m.TC};
     }
     a.thr = e->mlp_thr;
     a.band = e->mlp_band;

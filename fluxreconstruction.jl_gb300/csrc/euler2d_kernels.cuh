@@ -603,7 +603,10 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             store_features_bf16(xs + (lane & 15) * NIN + (pr ? 16 : 0), feat);
             __syncwarp();
             Fwd f;
-            mlp_forward_tile(global_view(a.mlp), xs, f); // 12 KB of weights, L1-resident
+            // 12 KB of weights, L1-resident; warp-level mma.sync: the tcgen05 routine of the
+            // stand-alone kernel measured slower here (per-CTA TMEM allocation, weight
+            // copy and two MMA round trips for only 64 elements)
+            mlp_forward_tile(global_view(a.mlp), xs, f);
             if ((lane & 3) == 0) {
                 prob[lane >> 2] = sigmoidf_(f.logit_g);
                 prob[(lane >> 2) + 8] = sigmoidf_(f.logit_g8);
@@ -683,13 +686,13 @@ int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     }
     a.ops = make_ops<Real, NP>(p->sp);
     a.status = p->d_status;
-    a.mlp = frmlp::MLPDev{nullptr, nullptr, nullptr, nullptr};
+    a.mlp = frmlp::MLPDev{nullptr, nullptr, nullptr, nullptr, nullptr};
     a.V = a.iV = nullptr;
     a.flags = a.stats = nullptr;
     if (FUSE) {
         const fr_mlp_ptrs m = fr_mlp_device(p->mlp);
         a.mlp = frmlp::MLPDev{m.P, (const __nv_bfloat16 *)m.W1, (const __nv_bfloat16 *)m.W2,
-                              (const __nv_bfloat16 *)m.W2T};
+                              (const __nv_bfloat16 *)m.W2T, m.TC};
         fr_iv1_from_tensor(p->sp, &a.iv1.m[0][0]);
         a.ind_thr = p->mlp_thr;
         a.ind_band = p->mlp_band;

@@ -176,10 +176,12 @@ int fr_launch_filter2d(frgpu_problem *p, int indicator, double lam, double S0, d
 int fr_launch_filter1d(frgpu_problem *p, int indicator, double lam, double S0, double kappa);
 // mlp.cu
 int fr_launch_features(frgpu_problem *p, float *d_feat);
-// Device pointers of a network (FP32 parameters, BF16 W1 [64][32], W2 and W2^T [64][64]).
+// Device pointers of a network (FP32 parameters, BF16 W1 [64][32], W2 and W2^T [64][64],
+// and the copy packed for the tcgen05 path).
 struct fr_mlp_ptrs {
     const float *P;
     const void *W1, *W2, *W2T;
+    const unsigned char *TC; // packed for the tcgen05 path
 };
 fr_mlp_ptrs fr_mlp_device(const frgpu_mlp *m);
 // 1D factor iV1[i][k] (row-major 4 x 4, float) of a deg-3 2D space's tensor inverse Vandermonde matrix

@@ -1,7 +1,9 @@
 // mlp.cu -- learned troubled-cell indicator: a 32 -> 64 -> 64 -> 1 perceptron
 // (GELU, GELU, sigmoid) fed with per-element modal energies, trained and
 // evaluated by hand-written BF16-in / FP32-accumulate tensor-core kernels
-// (mma.sync m16n8k16 bf16 -> f32), and an indicator + :l2 modal filter kernel
+// (training: warp-level mma.sync m16n8k16 in the backward pass; inference and
+// the indicator: tcgen05.mma with TMEM accumulators, mlp_device.cuh), and an
+// indicator + :l2 modal filter kernel
 // that uses it in place of the modal-decay test of example/shock-vortex.jl:308-321
 // with the plain test (src/dissipation.jl:13-23) as fallback and judge.
 //
@@ -26,28 +28,30 @@ namespace {
 using namespace frmlp;
 
 // ---------------------------------------------------------------- forward (tests, evaluation)
-__global__ void __launch_bounds__(32 * WARPS) k_mlp_forward(MLPDev w, const float *__restrict__ X, long n,
-                                                          float *__restrict__ y) {
-    __shared__ __align__(16) __nv_bfloat16 xs_all[WARPS][16 * NIN];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __nv_bfloat16 *xs = xs_all[warp];
-    const long ntiles = (n + 15) / 16;
-    for (long tile = (long)blockIdx.x * WARPS + warp; tile < ntiles; tile += (long)gridDim.x * WARPS) {
-        for (int q = lane; q < 16 * NIN; q += 32) {
-            const long s = tile * 16 + q / NIN;
-            xs[q] = __float2bfloat16_rn(s < n ? X[s * NIN + q % NIN] : 0.0f);
-        }
-        __syncwarp();
-        Fwd f;
-        mlp_forward_tile(global_view(w), xs, f);
-        const int g = lane >> 2, t = lane & 3;
-        if (t == 0) {
-            const long s0 = tile * 16 + g, s1 = tile * 16 + g + 8;
-            if (s0 < n) y[s0] = sigmoidf_(f.logit_g);
-            if (s1 < n) y[s1] = sigmoidf_(f.logit_g8);
-        }
-        __syncwarp();
+// The network on n feature rows X[n][32] (FP32, rounded to BF16 as they load)
+// -> y[n] = sigmoid(logit): persistent CTAs of four warps over groups of 64
+// rows on the tcgen05 tensor cores, the same arithmetic as the indicator
+// kernels.  A wait that times out sets *status.
+__global__ void __launch_bounds__(32 * WARPS, 4) k_mlp_forward(MLPDev w, const float *__restrict__ X, long n,
+                                                             float *__restrict__ y, int *__restrict__ status) {
+    static_assert(WARPS == 4, "the tcgen05 network runs on four warps");
+    __shared__ __align__(128) unsigned char sm[TCS_BYTES];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t tmem = tc_begin(sm, w.TC, tid);
+    uint32_t phase = 0;
+    const int half = lane >> 4, r = 16 * warp + (lane & 15);
+    const float *prob = reinterpret_cast<const float *>(sm + TCS_PROB);
+    const long ngroups = (n + 63) / 64;
+    for (long grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+        const long smp = grp * 64 + r;
+        float feat[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) feat[q] = smp < n ? X[smp * NIN + 16 * half + q] : 0.0f;
+        store_features_tc(sm, r, half, feat);
+        if (!mlp_tc_forward64(sm, tmem, phase, tid)) break;
+        if (half == 0 && smp < n) y[smp] = prob[r];
     }
+    if (tc_end(sm, tmem, phase, tid) && tid == 0) atomicOr(status, frk::ST_TIMEOUT);
 }
 
 // ---------------------------------------------------------------- loss + gradient
@@ -229,10 +233,30 @@ __global__ void __launch_bounds__(32 * GWARPS) k_mlp_grad(MLPDev w, const float 
     if (threadIdx.x == 0 && lsum != 0.f) atomicAdd(loss, lsum);
 }
 
+// Parameter q of the FP32 vector into the packed network of the tcgen05 path.
+__device__ __forceinline__ void tc_pack_param(unsigned char *tc, int q, float p) {
+    if (q < OFF_B1) {
+        const int o = (q - OFF_W1) / NIN, i = (q - OFF_W1) % NIN;
+        *reinterpret_cast<__nv_bfloat16 *>(tc + TCP_W1 + core_off(o, i, NIN)) = __float2bfloat16_rn(p);
+    } else if (q < OFF_W2) {
+        reinterpret_cast<float *>(tc + TCP_B1)[q - OFF_B1] = p;
+    } else if (q < OFF_B2) {
+        const int o = (q - OFF_W2) / NH, i = (q - OFF_W2) % NH;
+        *reinterpret_cast<__nv_bfloat16 *>(tc + TCP_W2 + core_off(o, i, NH)) = __float2bfloat16_rn(p);
+    } else if (q < OFF_W3) {
+        reinterpret_cast<float *>(tc + TCP_B2)[q - OFF_B2] = p;
+    } else if (q < OFF_B3) {
+        reinterpret_cast<float *>(tc + TCP_W3)[q - OFF_W3] = p;
+    } else {
+        reinterpret_cast<float *>(tc + TCP_B3)[0] = p;
+    }
+}
+
 // Adam update of the FP32 master copy and refresh of the BF16 copies.
 __global__ void k_mlp_adam(float *__restrict__ P, float *__restrict__ m, float *__restrict__ v,
                            const float *__restrict__ grad, float lr, float b1, float b2, float eps, float c1,
-                           float c2, __nv_bfloat16 *W1, __nv_bfloat16 *W2, __nv_bfloat16 *W2T) {
+                           float c2, __nv_bfloat16 *W1, __nv_bfloat16 *W2, __nv_bfloat16 *W2T,
+                           unsigned char *TC) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= NPARAM) return;
     const float gq = grad[q];
@@ -242,6 +266,7 @@ __global__ void k_mlp_adam(float *__restrict__ P, float *__restrict__ m, float *
     v[q] = vq;
     const float p = P[q] - lr * (mq * c1) / (sqrtf(vq * c2) + eps);
     P[q] = p;
+    tc_pack_param(TC, q, p);
     const __nv_bfloat16 pb = __float2bfloat16_rn(p);
     if (q < OFF_B1) W1[frag_w1((q - OFF_W1) / NIN, (q - OFF_W1) % NIN)] = pb;
     else if (q >= OFF_W2 && q < OFF_B2) {
@@ -251,9 +276,11 @@ __global__ void k_mlp_adam(float *__restrict__ P, float *__restrict__ m, float *
     }
 }
 
-__global__ void k_mlp_refresh(const float *__restrict__ P, __nv_bfloat16 *W1, __nv_bfloat16 *W2, __nv_bfloat16 *W2T) {
+__global__ void k_mlp_refresh(const float *__restrict__ P, __nv_bfloat16 *W1, __nv_bfloat16 *W2, __nv_bfloat16 *W2T,
+                              unsigned char *TC) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= NPARAM) return;
+    tc_pack_param(TC, q, P[q]);
     const __nv_bfloat16 pb = __float2bfloat16_rn(P[q]);
     if (q < OFF_B1) W1[frag_w1((q - OFF_W1) / NIN, (q - OFF_W1) % NIN)] = pb;
     else if (q >= OFF_W2 && q < OFF_B2) {
@@ -324,50 +351,45 @@ __global__ void __launch_bounds__(128) k_features(const Real *__restrict__ u, si
 // `band` of `thr` the plain modal-decay test decides (fallback); otherwise the
 // network does.  stats: [0] troubled, [1] network vs plain disagreements
 // (misfires, judged by the plain test), [2] fallbacks.
+// The learned indicator + :l2 filter over a 2D state (np = 4), persistent: a
+// CTA of four warps takes groups of 64 consecutive elements; warp w holds
+// elements 16 w .. 16 w + 15 of the group (lanes L and L + 16 share one).  The
+// network runs on the tcgen05 tensor cores (mlp_tc_forward64, weights copied
+// once per CTA); the decision takes the plain test as fallback and judge.  The
+// next group's state values are loaded while the network runs.  A wait that
+// times out sets ST_TIMEOUT in *status and ends the CTA's work.
 template <class Real>
 __global__ void __launch_bounds__(32 * WARPS, 4) k_mlp_indicator(MLPDev w, Real *__restrict__ u, Real *__restrict__ lo,
                                                             size_t ne, const Real *__restrict__ V,
                                                             const Real *__restrict__ iV, IV1 iv, float gm1,
                                                             float thr, float band, float S0, float kappa, double lam,
-                                                            int *__restrict__ flags, int *__restrict__ stats) {
-    __shared__ __align__(16) __nv_bfloat16 xs_all[WARPS][16 * NIN];
-    __shared__ float prob_all[WARPS][16];
-    // the CTA's copy of the weights: W1, W2 (bf16) and b1, b2, w3, b3
-    __shared__ __align__(16) __nv_bfloat16 sW1[NH * NIN];
-    __shared__ __align__(16) __nv_bfloat16 sW2[NH * NH];
-    __shared__ float sb[3 * NH + 1];
-    stage_weights(w, sW1, sW2, sb);
-    __syncthreads();
-    const MLPView view = smem_view(sW1, sW2, sb);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __nv_bfloat16 *xs = xs_all[warp];
-    float *prob = prob_all[warp];
-    const size_t ntiles = (ne + 15) / 16;
+                                                            int *__restrict__ flags, int *__restrict__ stats,
+                                                            int *__restrict__ status) {
+    static_assert(WARPS == 4, "the tcgen05 network runs on four warps");
+    __shared__ __align__(128) unsigned char sm[TCS_BYTES];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t tmem = tc_begin(sm, w.TC, tid);
+    const float *prob = reinterpret_cast<const float *>(sm + TCS_PROB) + 16 * warp;
+    const size_t ngroups = (ne + 63) / 64;
     int n_trouble = 0, n_mis = 0, n_fb = 0;
     const bool pr = lane >= 16;
-    const size_t step = (size_t)gridDim.x * WARPS;
-    float raw[8][4]; // this lane's values of the tile being processed, loaded one tile ahead
-    size_t tile = (size_t)blockIdx.x * WARPS + warp;
-    if (tile < ntiles) load_raw<Real>(u, ne, tile * 16 + (lane & 15), tile * 16 + (lane & 15) < ne, pr, raw);
-    for (; tile < ntiles; tile += step) {
-        const size_t e = tile * 16 + (lane & 15);
+    uint32_t phase = 0;
+    float raw[8][4]; // this lane's values of the group being processed, loaded one group ahead
+    size_t grp = blockIdx.x;
+    if (grp < ngroups) {
+        const size_t e = grp * 64 + 16 * warp + (lane & 15);
+        load_raw<Real>(u, ne, e, e < ne, pr, raw);
+    }
+    for (; grp < ngroups; grp += gridDim.x) {
+        const size_t e = grp * 64 + 16 * warp + (lane & 15);
         float feat[16], su = 0.f;
         features_from_raw(raw, e < ne, pr, iv, gm1, feat, su);
-        // issue the next tile's loads now; they land while the network runs
-        if (tile + step < ntiles) {
-            const size_t en = (tile + step) * 16 + (lane & 15);
+        store_features_tc(sm, 16 * warp + (lane & 15), pr ? 1 : 0, feat);
+        if (grp + gridDim.x < ngroups) {
+            const size_t en = (grp + gridDim.x) * 64 + 16 * warp + (lane & 15);
             load_raw<Real>(u, ne, en, en < ne, pr, raw);
         }
-        store_features_bf16(xs + (lane & 15) * NIN + (pr ? 16 : 0), feat);
-        __syncwarp();
-        Fwd f;
-        mlp_forward_tile(view, xs, f);
-        const int g = lane >> 2, t = lane & 3;
-        if (t == 0) {
-            prob[g] = sigmoidf_(f.logit_g);
-            prob[g + 8] = sigmoidf_(f.logit_g8);
-        }
-        __syncwarp();
+        if (!mlp_tc_forward64(sm, tmem, phase, tid)) break;
         bool bad = false;
         if (!pr && e < ne) {
             const bool plain = plain_troubled(su, S0, kappa);
@@ -381,9 +403,9 @@ __global__ void __launch_bounds__(32 * WARPS, 4) k_mlp_indicator(MLPDev w, Real 
             flags[e] = bad ? 1 : 0;
         }
         // :l2 modal filter of the troubled elements
-        warp_filter_elements<Real>(__ballot_sync(0xffffffffu, bad), tile * 16, u, lo, ne, V, iV, lam);
-        __syncwarp();
+        warp_filter_elements<Real>(__ballot_sync(0xffffffffu, bad), grp * 64 + 16 * warp, u, lo, ne, V, iV, lam);
     }
+    if (tc_end(sm, tmem, phase, tid) && tid == 0) atomicOr(status, frk::ST_TIMEOUT);
     // warp-reduce the statistics, one atomic per warp
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -415,15 +437,16 @@ struct frgpu_mlp {
     cudaStream_t stream = nullptr;
     float *P = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr, *loss = nullptr;
     __nv_bfloat16 *W1 = nullptr, *W2 = nullptr, *W2T = nullptr;
+    unsigned char *TC = nullptr; // packed for the tcgen05 path (TCP_* layout)
     long step = 0;
     long launches = 0;
-    MLPDev dev() const { return MLPDev{P, W1, W2, W2T}; }
+    MLPDev dev() const { return MLPDev{P, W1, W2, W2T, TC}; }
 };
 
 static void mlp_free(frgpu_mlp *m) {
     if (!m) return;
     if (m->stream) cudaStreamSynchronize(m->stream);
-    void *b[] = {m->P, m->m, m->v, m->grad, m->loss, m->W1, m->W2, m->W2T};
+    void *b[] = {m->P, m->m, m->v, m->grad, m->loss, m->W1, m->W2, m->W2T, m->TC};
     for (void *p : b)
         if (p) cudaFree(p);
     if (m->stream) cudaStreamDestroy(m->stream);
@@ -431,7 +454,7 @@ static void mlp_free(frgpu_mlp *m) {
 }
 
 static int mlp_refresh(frgpu_mlp *m) {
-    k_mlp_refresh<<<(NPARAM + 255) / 256, 256, 0, m->stream>>>(m->P, m->W1, m->W2, m->W2T);
+    k_mlp_refresh<<<(NPARAM + 255) / 256, 256, 0, m->stream>>>(m->P, m->W1, m->W2, m->W2T, m->TC);
     FR_CUDA(cudaGetLastError());
     m->launches += 1;
     return FRGPU_OK;
@@ -476,6 +499,8 @@ FRGPU_API int frgpu_mlp_create(int seed, frgpu_mlp **out) {
         FR_CUDA(cudaMalloc(&m->W1, sizeof(__nv_bfloat16) * NH * NIN));
         FR_CUDA(cudaMalloc(&m->W2, sizeof(__nv_bfloat16) * NH * NH));
         FR_CUDA(cudaMalloc(&m->W2T, sizeof(__nv_bfloat16) * NH * NH));
+        FR_CUDA(cudaMalloc(&m->TC, TCP_BYTES));
+        FR_CUDA(cudaMemset(m->TC, 0, TCP_BYTES));
         FR_CUDA(cudaMemset(m->m, 0, sizeof(float) * NPARAM));
         FR_CUDA(cudaMemset(m->v, 0, sizeof(float) * NPARAM));
         // deterministic init: uniform(-a, a) with a = sqrt(6 / fan_in) (He-uniform), zero biases
@@ -528,15 +553,24 @@ FRGPU_API int frgpu_mlp_forward(frgpu_mlp *m, const float *x, long n, float *y) 
     }
     if (n == 0) return FRGPU_OK;
     DevBuf<float> dx, dy;
+    DevBuf<int> dst;
     int rc;
-    if ((rc = dx.alloc((size_t)n * NIN)) || (rc = dy.alloc(n))) return rc;
+    if ((rc = dx.alloc((size_t)n * NIN)) || (rc = dy.alloc(n)) || (rc = dst.alloc(1))) return rc;
+    FR_CUDA(cudaMemsetAsync(dst.p, 0, sizeof(int), m->stream));
     FR_CUDA(cudaMemcpyAsync(dx.p, x, sizeof(float) * n * NIN, cudaMemcpyHostToDevice, m->stream));
-    const int grid = (int)std::min<long>((n + 16 * WARPS - 1) / (16 * WARPS), 4096);
-    k_mlp_forward<<<grid, 32 * WARPS, 0, m->stream>>>(m->dev(), dx.p, n, dy.p);
+    // persistent: at most 4 CTAs per SM (64 tensor-memory columns each)
+    const int grid = (int)std::min<long>((n + 63) / 64, 152 * 4);
+    k_mlp_forward<<<grid, 32 * WARPS, 0, m->stream>>>(m->dev(), dx.p, n, dy.p, dst.p);
     FR_CUDA(cudaGetLastError());
     m->launches += 1;
+    int st = 0;
     FR_CUDA(cudaMemcpyAsync(y, dy.p, sizeof(float) * n, cudaMemcpyDeviceToHost, m->stream));
+    FR_CUDA(cudaMemcpyAsync(&st, dst.p, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
     FR_CUDA(cudaStreamSynchronize(m->stream));
+    if (st) {
+        fr_set_error("mlp_forward: a tensor-core wait timed out");
+        return FRGPU_ERR_TIMEOUT;
+    }
     return FRGPU_OK;
 }
 
@@ -598,7 +632,7 @@ FRGPU_API int frgpu_mlp_train(frgpu_mlp *m, const float *x, const float *t, long
             const float c1 = 1.f / (1.f - std::pow(b1, (float)m->step));
             const float c2 = 1.f / (1.f - std::pow(b2, (float)m->step));
             k_mlp_adam<<<(NPARAM + 255) / 256, 256, 0, m->stream>>>(m->P, m->m, m->v, m->grad, lr, b1, b2, eps, c1,
-                                                                     c2, m->W1, m->W2, m->W2T);
+                                                                     c2, m->W1, m->W2, m->W2T, m->TC);
             FR_CUDA(cudaGetLastError());
             m->launches += 1;
             if (loss_out) {
@@ -618,7 +652,7 @@ FRGPU_API int frgpu_mlp_train(frgpu_mlp *m, const float *x, const float *t, long
 } // extern "C"
 
 // ---- used by runtime.cu -------------------------------------------------------
-fr_mlp_ptrs fr_mlp_device(const frgpu_mlp *m) { return fr_mlp_ptrs{m->P, m->W1, m->W2, m->W2T}; }
+fr_mlp_ptrs fr_mlp_device(const frgpu_mlp *m) { return fr_mlp_ptrs{m->P, m->W1, m->W2, m->W2T, m->TC}; }
 
 // The 1D factor of the space's tensor inverse Vandermonde matrix:
 // iV[(i,0),(k,0)] = iV1[i][k] iV1[0][0], and iV1[0][0] = w_0 / sqrt(2) > 0.
@@ -670,11 +704,12 @@ int fr_launch_mlp_indicator(frgpu_problem *p, double lam, double S0, double kapp
         return FRGPU_ERR_UNSUPPORTED;
     }
     const size_t ne = (size_t)p->sp.nx * p->sp.ny;
-    const size_t ntiles = (ne + 15) / 16;
-    // persistent: as many CTAs as fit at once (4 per SM at <= 128 registers per thread)
+    const size_t ngroups = (ne + 63) / 64;
+    // persistent: as many CTAs as fit at once (4 per SM at <= 128 registers per
+    // thread; each holds 64 of the SM's 512 tensor-memory columns)
     int nsm = 152;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device);
-    const int grid = (int)std::min<size_t>((ntiles + WARPS - 1) / WARPS, (size_t)nsm * 4);
+    const int grid = (int)std::min<size_t>(ngroups, (size_t)nsm * 4);
     const float gm1 = (float)(p->d.gamma - 1.0);
     FR_CUDA(cudaMemsetAsync(p->d_count, 0, sizeof(int) * 4, p->stream));
     const MLPDev w = p->mlp->dev();
@@ -682,11 +717,11 @@ int fr_launch_mlp_indicator(frgpu_problem *p, double lam, double S0, double kapp
     if (p->d.precision == FRGPU_FP64)
         k_mlp_indicator<double><<<grid, 32 * WARPS, 0, p->stream>>>(
             w, (double *)fr_state_hi(p), nullptr, ne, (const double *)p->d_V, (const double *)p->d_iV, iv1,
-            gm1, p->mlp_thr, p->mlp_band, (float)S0, (float)kappa, lam, p->d_flags, p->d_count);
+            gm1, p->mlp_thr, p->mlp_band, (float)S0, (float)kappa, lam, p->d_flags, p->d_count, p->d_status);
     else
         k_mlp_indicator<float><<<grid, 32 * WARPS, 0, p->stream>>>(
             w, (float *)fr_state_hi(p), (float *)p->s3, ne, (const float *)p->d_V, (const float *)p->d_iV, iv1,
-            gm1, p->mlp_thr, p->mlp_band, (float)S0, (float)kappa, lam, p->d_flags, p->d_count);
+            gm1, p->mlp_thr, p->mlp_band, (float)S0, (float)kappa, lam, p->d_flags, p->d_count, p->d_status);
     FR_CUDA(cudaGetLastError());
     p->launches += 1;
     return FRGPU_OK;

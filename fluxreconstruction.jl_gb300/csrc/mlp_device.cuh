@@ -9,6 +9,7 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 
+#include "blackwell.cuh"
 #include "fr_common.cuh"
 
 namespace frmlp {
@@ -24,7 +25,10 @@ struct MLPDev {
     const __nv_bfloat16 *W1;    // W1 [64][32] in fragment order (frag_w1)
     const __nv_bfloat16 *W2;    // W2 [64][64] in fragment order (frag_w2)
     const __nv_bfloat16 *W2T;   // [64][64]  row = input unit (backward pass)
+    const unsigned char *TC;    // the network packed for the tcgen05 path (TCP_* layout)
 };
+
+
 
 // Fragment order of the BF16 weight copies: the m16n8k16 B fragments that lane
 // (g = lane / 4, t = lane % 4) needs for output tile j (units 8j..8j+7) are
@@ -200,6 +204,166 @@ __device__ __forceinline__ void stage_weights(const MLPDev &w, __nv_bfloat16 *sW
 }
 __device__ __forceinline__ MLPView smem_view(const __nv_bfloat16 *sW1, const __nv_bfloat16 *sW2, const float *sb) {
     return MLPView{sb, sb + NH, sb + 2 * NH, sb + 3 * NH, sW1, sW2};
+}
+
+// ---- the network on the 5th-generation tensor cores (tcgen05) ----------------
+// The indicator kernels run the network on groups of 64 elements with four
+// warps (128 threads).  Layer l is one M = 128, N = 64 tcgen05.mma chain
+// (K = 32 for layer 1, 64 for layer 2, 16 per instruction), BF16 operands from
+// shared memory, FP32 accumulator in 64 tensor-memory columns.  The 64 elements
+// are rows 0-63 of the A operand and again rows 64-127, so that the four warps
+// share the epilogue: warps 0-1 read rows 0-63 and take hidden units 0-31,
+// warps 2-3 read the same elements in rows 64-127 and take units 32-63 (a warp
+// reads the tensor-memory lanes of its own sub-partition).  Layer 1's epilogue
+// (bias, GELU, BF16) writes the layer-2 A operand; layer 2's (bias, GELU, dot
+// with w3) leaves half a logit per thread, and the halves meet in shared memory.
+//
+// Operands are K-major without swizzling: 8 x 8 BF16 core matrices of 128 bytes,
+// adjacent along K 128 bytes apart and along M / N (K / 8) * 128 bytes apart.
+__host__ __device__ constexpr int core_off(int r, int k, int K) {
+    return (r >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+// The packed network in global memory (bytes): W1 [64 x 32] and W2 [64 x 64]
+// as K-major B operands (rows = output units), then FP32 b1, b2, w3 and b3.
+constexpr int TCP_W1 = 0, TCP_W2 = TCP_W1 + NH * NIN * 2, TCP_B1 = TCP_W2 + NH * NH * 2, TCP_B2 = TCP_B1 + NH * 4,
+              TCP_W3 = TCP_B2 + NH * 4, TCP_B3 = TCP_W3 + NH * 4, TCP_BYTES = TCP_B3 + 16;
+// Shared memory of the tcgen05 network (bytes from a 128-byte aligned base).
+constexpr int TCS_A1 = 0;                                       // [128][32] BF16, layer-1 A
+constexpr int TCS_A2 = TCS_A1 + 128 * NIN * 2;                  // [128][64] BF16, layer-2 A
+constexpr int TCS_P = TCS_A2 + 128 * NH * 2;                    // the packed network
+constexpr int TCS_PART = TCS_P + (TCP_BYTES + 127) / 128 * 128; // [64] float half logits
+constexpr int TCS_PROB = TCS_PART + 64 * 4;                     // [64] float probabilities
+constexpr int TCS_BAR = TCS_PROB + 64 * 4;                      // mbarriers: [0] weights copied, [1] MMAs done
+constexpr int TCS_TMEM = TCS_BAR + 16;                          // TMEM address, timeout flag
+constexpr int TCS_BYTES = TCS_TMEM + 16;
+constexpr uint32_t TC_COLS = 64; // tensor-memory columns (layer 2 reuses layer 1's)
+
+// Set-up by the 128 threads (tid < 128): barriers, the bulk copy of the packed
+// network, and the tensor-memory allocation (warp 0).  Returns the TMEM address.
+__device__ __forceinline__ uint32_t tc_begin(unsigned char *sm, const unsigned char *pack, int tid) {
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + TCS_BAR);
+    uint32_t *tm = reinterpret_cast<uint32_t *>(sm + TCS_TMEM);
+    if (tid == 0) {
+        bw::mbar_init(&bar[0], 1);
+        bw::mbar_init(&bar[1], 1);
+        tm[1] = 0;
+        bw::mbar_arrive_expect_tx(&bar[0], TCP_BYTES);
+        bw::bulk_load(sm + TCS_P, pack, TCP_BYTES, &bar[0]);
+    }
+    if (tid < 32) bw::tmem_alloc(tm, TC_COLS);
+    bw::tc_fence_before();
+    bw::bar_sync(1, 128);
+    bw::tc_fence_after();
+    if (!bw::mbar_wait(&bar[0], 0)) tm[1] = 1; // the weights never arrived
+    return tm[0];
+}
+
+// End of the tcgen05 network's use: after a timeout, give the MMAs still in
+// flight a bounded time to finish; free the tensor memory (warp 0).  Returns
+// true when a wait timed out.
+__device__ __forceinline__ bool tc_end(unsigned char *sm, uint32_t tmem, uint32_t phase, int tid) {
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + TCS_BAR);
+    volatile uint32_t *tm = reinterpret_cast<uint32_t *>(sm + TCS_TMEM);
+    bw::tc_fence_before();
+    bw::bar_sync(1, 128);
+    const bool timed_out = tm[1] != 0;
+    if (timed_out && phase > 0) bw::mbar_wait(&bar[1], (phase - 1) & 1);
+    bw::tc_fence_after();
+    if (tid < 32) bw::tmem_dealloc(tmem, TC_COLS);
+    return timed_out;
+}
+
+// The 16 features of one lane as BF16 into rows r and r + 64 of the layer-1 A
+// operand: K columns 16 half .. 16 half + 15 (density half 0, pressure half 1).
+__device__ __forceinline__ void store_features_tc(unsigned char *sm, int r, int half, const float (&feat)[16]) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const float *f = feat + 8 * h;
+        const uint4 v = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]),
+                                   pack_bf16(f[6], f[7]));
+        const int k = 16 * half + 8 * h;
+        *reinterpret_cast<uint4 *>(sm + TCS_A1 + core_off(r, k, NIN)) = v;
+        *reinterpret_cast<uint4 *>(sm + TCS_A1 + core_off(r + 64, k, NIN)) = v;
+    }
+}
+
+// Forward pass of the 64 elements whose features are in A1 (all 128 threads
+// call it).  Leaves sigmoid(logit) of row r in TCS_PROB[r]; `phase` counts
+// the MMA-barrier phases used so far.  Returns false after a timed-out wait
+// (the timeout flag is set).
+__device__ __forceinline__ bool mlp_tc_forward64(unsigned char *sm, uint32_t tmem, uint32_t &phase, int tid) {
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + TCS_BAR);
+    volatile uint32_t *flag = reinterpret_cast<uint32_t *>(sm + TCS_TMEM) + 1;
+    const float *b1 = reinterpret_cast<const float *>(sm + TCS_P + TCP_B1);
+    const float *b2 = reinterpret_cast<const float *>(sm + TCS_P + TCP_B2);
+    const float *w3 = reinterpret_cast<const float *>(sm + TCS_P + TCP_W3);
+    float *part = reinterpret_cast<float *>(sm + TCS_PART), *prob = reinterpret_cast<float *>(sm + TCS_PROB);
+    const uint32_t a1 = bw::smem_addr(sm + TCS_A1), a2 = bw::smem_addr(sm + TCS_A2);
+    const uint32_t w1 = bw::smem_addr(sm + TCS_P + TCP_W1), w2 = bw::smem_addr(sm + TCS_P + TCP_W2);
+    constexpr uint32_t ID = bw::idesc_bf16_f32(128, NH);
+    const int warp = tid >> 5, lane = tid & 31;
+    const int r = (32 * warp + lane) & 63, cb = warp < 2 ? 0 : 32;
+    const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
+    // ---- layer 1: D = A1 W1^T --------------------------------------------------
+    bw::fence_async_smem(); // A1 (written by this thread) -> the MMA's async proxy
+    bw::tc_fence_before();
+    bw::bar_sync(1, 128);
+    if (*flag) return false;
+    if (tid == 0) {
+        bw::tc_fence_after();
+#pragma unroll
+        for (int s = 0; s < NIN / 16; ++s)
+            bw::mma_bf16(tmem, bw::smem_desc_kmajor(a1 + 256 * s, 128, NIN / 8 * 128),
+                         bw::smem_desc_kmajor(w1 + 256 * s, 128, NIN / 8 * 128), ID, s > 0);
+        bw::mma_commit(&bar[1]);
+    }
+    if (!bw::mbar_wait(&bar[1], phase & 1)) *flag = 1;
+    ++phase;
+    bw::tc_fence_after();
+    float v[32];
+    bw::tmem_ld32(trow + cb, v);
+    // h1 = gelu(a1 + b1) as BF16 into rows r and r + 64, K columns cb .. cb + 31 of A2
+#pragma unroll
+    for (int c = 0; c < 32; c += 8) {
+        uint32_t q[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            const float2 g = gelu2(v[c + 2 * h] + b1[cb + c + 2 * h], v[c + 2 * h + 1] + b1[cb + c + 2 * h + 1]);
+            q[h] = pack_bf16(g.x, g.y);
+        }
+        const uint4 o = make_uint4(q[0], q[1], q[2], q[3]);
+        *reinterpret_cast<uint4 *>(sm + TCS_A2 + core_off(r, cb + c, NH)) = o;
+        *reinterpret_cast<uint4 *>(sm + TCS_A2 + core_off(r + 64, cb + c, NH)) = o;
+    }
+    // ---- layer 2: D = A2 W2^T, over the same columns once every thread has read them
+    bw::fence_async_smem();
+    bw::tc_fence_before();
+    bw::bar_sync(1, 128);
+    if (*flag) return false;
+    if (tid == 0) {
+        bw::tc_fence_after();
+#pragma unroll
+        for (int s = 0; s < NH / 16; ++s)
+            bw::mma_bf16(tmem, bw::smem_desc_kmajor(a2 + 256 * s, 128, NH / 8 * 128),
+                         bw::smem_desc_kmajor(w2 + 256 * s, 128, NH / 8 * 128), ID, s > 0);
+        bw::mma_commit(&bar[1]);
+    }
+    if (!bw::mbar_wait(&bar[1], phase & 1)) *flag = 1;
+    ++phase;
+    bw::tc_fence_after();
+    bw::tmem_ld32(trow + cb, v);
+    float sg = 0.f;
+#pragma unroll
+    for (int c = 0; c < 32; c += 2) {
+        const float2 g = gelu2(v[c] + b2[cb + c], v[c + 1] + b2[cb + c + 1]);
+        sg = fmaf(g.x, w3[cb + c], fmaf(g.y, w3[cb + c + 1], sg));
+    }
+    if (warp >= 2) part[r] = sg;
+    bw::tc_fence_before();
+    bw::bar_sync(1, 128);
+    if (warp < 2) prob[r] = 1.0f / (1.0f + expf(-(sg + part[r] + *reinterpret_cast<const float *>(sm + TCS_P + TCP_B3))));
+    bw::bar_sync(1, 128);
+    return *flag == 0;
 }
 
 // ---- features and decisions of the 2D indicator (np = 4) ------------------

@@ -46,6 +46,7 @@ from .api import (  # noqa: F401
     dradau,
     dsd,
     gauss_weights,
+    fma_peak,
     init,
     interp_face_,
     lagrange_point,

@@ -89,6 +89,7 @@ SIGNATURES = {
     "frgpu_problem_stream": (C.c_int, [_VP, C.POINTER(_VP)]),
     "frgpu_problem_launches": (C.c_long, [_VP]),
     "frgpu_synchronize": (C.c_int, [_VP]),
+    "frgpu_fma_peak": (C.c_int, [C.c_int, _D]),
     "frgpu_reduce2d_noalloc": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                          C.c_double, _VP, _VP, _VP]),
     "frgpu_mlp_nparams": (C.c_int, []),

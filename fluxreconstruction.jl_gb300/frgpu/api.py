@@ -344,6 +344,14 @@ def refined_at_coarse_points(u_fine, xpl):
     return out
 
 
+def fma_peak(kind: str = "fp64") -> float:
+    """Measured fused multiply-add throughput of the current GPU in FLOP/s (an FMA
+    counts 2): "fp64", "fp32" or "fp32x2" (packed pairs)."""
+    out = C.c_double()
+    check(L.lib().frgpu_fma_peak({"fp64": 0, "fp32": 1, "fp32x2": 2}[kind], C.byref(out)))
+    return out.value
+
+
 # ---------------------------------------------------------------- problems
 class ODEProblem:
     """The object FRAdvectionProblem / FREulerProblem return (an ODEProblem of

@@ -231,6 +231,12 @@ FRGPU_API long frgpu_problem_launches(const frgpu_problem *p);
 /* Wait for the problem's stream; returns the status of the work queued since
  * the last check (FRGPU_ERR_NONFINITE, FRGPU_ERR_UNPHYSICAL, ...). */
 FRGPU_API int frgpu_synchronize(frgpu_problem *p);
+/* Fused multiply-add throughput of the current GPU, measured (FLOP/s, an FMA
+ * counted as 2): kind 0 = FP64, 1 = FP32, 2 = FP32 pairs (f32x2).  No
+ * counterpart in the reference: it is the ceiling the compute-bound forms (the
+ * FP64 residuals) are placed against.  Allocates a little scratch and times a
+ * few launches with CUDA events. */
+FRGPU_API int frgpu_fma_peak(int kind, double *flops_per_s);
 
 /* ======================================================================
  * Learned troubled-cell indicator.  Stands in for the modal-decay test

@@ -1,6 +1,6 @@
-"""The learned troubled-cell indicator: tensor-core forward/backward kernels
-against the FP64 oracle, training, the feature kernel, and the indicator +
-filter against the plain modal-decay test.
+"""The learned troubled-cell indicator: tensor-core forward (tcgen05) and
+backward (mma.sync) kernels against the FP64 oracle, training, the feature
+kernel, and the indicator + filter against the plain modal-decay test.
 
 Tolerances: the kernels take BF16 inputs and weights and round the hidden
 activations to BF16 between layers, with FP32 accumulation; the oracle runs
@@ -41,9 +41,13 @@ def test_forward_matches_oracle(frgpu, oracle):
     y = m.forward(x)
     ref = oracle.mlp_forward(rounded_params(m.params), bf16(x))
     assert y.shape == (1000,)
-    assert np.max(np.abs(y - ref)) < 2e-2
-    # ragged tail (n not a multiple of the 16-sample tile) and single samples
-    np.testing.assert_allclose(m.forward(x[:7]), y[:7], atol=1e-6)
+    err = np.abs(y - ref)
+    print(f"tcgen05 forward vs FP64 oracle: max {err.max():.2e}, mean {err.mean():.2e}")
+    assert err.max() < 2e-2
+    # every row is computed on its own: ragged groups (n not a multiple of the
+    # 64-row group) and single samples give the same values
+    for k in (1, 7, 63, 64, 65, 129):
+        np.testing.assert_allclose(m.forward(x[:k]), y[:k], rtol=0, atol=1e-6)
 
 
 def test_gradient_matches_oracle(frgpu, oracle):
@@ -151,10 +155,16 @@ def test_learned_indicator_trains_and_judges_misfires(frgpu):
     assert np.all(np.isfinite(itg.u))
 
 
-def test_fused_indicator_equals_separate_kernel(frgpu):
-    """The learned indicator inside the third SSPRK3 stage (FP32K, deg 3) and the
-    stand-alone indicator kernel after the step give the same state, flags and
-    counts, bit for bit: same features, same network arithmetic, same filter."""
+def test_fused_indicator_agrees_with_separate_kernel(frgpu):
+    """The learned indicator inside the third SSPRK3 stage (FP32K, deg 3; the
+    network as warp-level mma.sync) and the stand-alone indicator kernel after
+    the step (the network on the tcgen05 tensor cores with TMEM accumulators)
+    see the same features and weights; their FP32 accumulations differ in
+    order only.  After 400 steps of the shock-vortex problem: the troubled
+    counts within 1 %, the last step's flags equal on at least 99.9 % of the
+    elements, the states within 1e-3 RMS of max |u| (an element whose network
+    output sits at the threshold can be filtered by one and not the other), and
+    one launch fewer per step when fused."""
     from frgpu import _lib as L
     from frgpu import learned
 
@@ -169,13 +179,20 @@ def test_fused_indicator_equals_separate_kernel(frgpu):
         L.check(frgpu.lib().frgpu_problem_set_mlp(prob._h, net._h, 0.5, 0.02))
         itg.set_filter("mlp", learned.FILTER_LAMBDA, learned.filter_S0(3), learned.FILTER_KAPPA)
         l0 = itg.launches()
-        itg.step(400)
-        launches = itg.launches() - l0
+        total = 0
         st = np.zeros(3, dtype=np.int32)
-        L.check(frgpu.lib().frgpu_indicator_stats(prob._h, st.ctypes.data_as(L._I)))
-        out.append((itg.u, itg.troubled(), st, launches))
-    (u1, f1, s1, n1), (u0, f0, s0, n0) = out
-    assert np.array_equal(u1, u0)
-    assert np.array_equal(f1, f0) and np.array_equal(s1, s0)
-    assert f1.sum() > 0  # the vortex has met the shock: something was filtered
-    assert n1 < n0       # one launch fewer per step
+        for _ in range(400):
+            itg.step(1)
+            L.check(frgpu.lib().frgpu_indicator_stats(prob._h, st.ctypes.data_as(L._I)))
+            total += int(st[0])
+        launches = itg.launches() - l0
+        out.append((itg.u, itg.troubled(), total, launches))
+    (u1, f1, t1, n1), (u0, f0, t0, n0) = out
+    rms = float(np.sqrt(np.mean((u1 - u0) ** 2)) / np.max(np.abs(u0)))
+    agree = float(np.mean(f1 == f0))
+    print(f"fused (mma.sync) vs separate (tcgen05): troubled {t1} vs {t0}, flag agreement {agree:.5f}, rms {rms:.2e}")
+    assert f1.sum() > 0 and t0 > 0  # the vortex has met the shock: something was filtered
+    assert abs(t1 - t0) <= 0.01 * t0
+    assert agree >= 0.999
+    assert rms < 1e-3
+    assert n1 < n0  # one launch fewer per step
