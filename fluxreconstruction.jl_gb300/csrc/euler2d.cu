@@ -47,11 +47,19 @@ template <> struct SumAcc<float> {
 // end), the largest directional wave speed max(|u| + c, |v| + c) and the
 // largest CFL rate (|u| + c)/dx + (|v| + c)/dy.  The wave speeds are
 // evaluated in the state's precision.
+// With a per-point inverse Jacobian met (a11, a12, a21, a22 in the device
+// layout; general quadrilaterals, DEV only) every value is weighted by the
+// point's det J = 1 / (a11 a22 - a12 a21), so that the sums are integrals over
+// the physical elements (the caller then scales by 1, not by dx dy / 4), and
+// the CFL rate is (lambda_r + lambda_s) / 2 with the contravariant speeds
+// lambda_r = |a11 u + a12 v| + c |(a11, a12)|, lambda_s = |a21 u + a22 v| +
+// c |(a21, a22)| (on a rectangle, (|u| + c)/dx + (|v| + c)/dy again).
 template <class Real, bool DEV>
 __global__ void __launch_bounds__(RED_THREADS) k_reduce2d_partial(const Real *__restrict__ u, const Real *__restrict__ lo,
                                                              size_t plane, int nq, const double *__restrict__ wp,
                                                              double gamma, double idx_, double idy_,
-                                                             double *__restrict__ part) {
+                                                             double *__restrict__ part,
+                                                             const Real *__restrict__ met = nullptr) {
     // part layout: [q * gridDim.x + b][6]: 4 sums, max directional speed, max CFL rate
     const int q = blockIdx.y;
     const size_t npts = plane * nq;
@@ -74,9 +82,16 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce2d_partial(const Real *__
                 if (lo != nullptr) wl[m] = lo[t + npts * m];
             }
         }
+        Real mt[4] = {Real(0), Real(0), Real(0), Real(0)};
+        Real jac = Real(1);
+        if (DEV && met != nullptr) {
+            frk::ldg4(met + frk::e2d_index(e, q, 0, plane), mt);
+            jac = Real(1) / (mt[0] * mt[3] - mt[1] * mt[2]);
+        }
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
-            acc[m].add(w[m], wl[m]);
+            if (DEV && met != nullptr) acc[m].add(w[m] * jac, wl[m] * jac);
+            else acc[m].add(w[m], wl[m]);
             w[m] += wl[m];
         }
         const Real rinv = frk::recipR<Real>(w[0]);
@@ -85,7 +100,13 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce2d_partial(const Real *__
         const Real c = frk::sqrtP<Real>(g * p * rinv);
         const Real a = fabs(U) + c, bb = fabs(V) + c;
         smax = fmax(smax, fmax(a, bb));
-        rmax = fmax(rmax, a * ix + bb * iy);
+        if (DEV && met != nullptr) {
+            const Real lr = fabs(mt[0] * U + mt[1] * V) + c * frk::sqrtR<Real>(mt[0] * mt[0] + mt[1] * mt[1]);
+            const Real ls = fabs(mt[2] * U + mt[3] * V) + c * frk::sqrtR<Real>(mt[2] * mt[2] + mt[3] * mt[3]);
+            rmax = fmax(rmax, Real(0.5) * (lr + ls));
+        } else {
+            rmax = fmax(rmax, a * ix + bb * iy);
+        }
     }
     __shared__ double red[6][RED_THREADS / 32];
     double vals[6] = {acc[0].value(), acc[1].value(), acc[2].value(), acc[3].value(), (double)smax, (double)rmax};
@@ -150,12 +171,15 @@ int fr_launch_euler2d_reduce(frgpu_problem *p, const void *state, const void *lo
     double *fin = p->d_red + FR_RED_FINAL;
     const int nq = np * np;
     const dim3 grid(RED_BLOCKS / nq, nq);
+    // general quadrilaterals: weights det J and contravariant speeds from the metric
     if (p->d.precision == FRGPU_FP64)
-        k_reduce2d_partial<double, true><<<grid, RED_THREADS, 0, p->stream>>>((const double *)state, (const double *)lo,
-                                                                     plane, nq, wp, p->d.gamma, cfl_dx, cfl_dy, part);
+        k_reduce2d_partial<double, true><<<grid, RED_THREADS, 0, p->stream>>>(
+            (const double *)state, (const double *)lo, plane, nq, wp, p->d.gamma, cfl_dx, cfl_dy, part,
+            (const double *)p->d_met);
     else
-        k_reduce2d_partial<float, true><<<grid, RED_THREADS, 0, p->stream>>>((const float *)state, (const float *)lo,
-                                                                    plane, nq, wp, p->d.gamma, cfl_dx, cfl_dy, part);
+        k_reduce2d_partial<float, true><<<grid, RED_THREADS, 0, p->stream>>>(
+            (const float *)state, (const float *)lo, plane, nq, wp, p->d.gamma, cfl_dx, cfl_dy, part,
+            (const float *)p->d_met);
     FR_CUDA(cudaGetLastError());
     k_reduce_final<<<1, 192, 0, p->stream>>>(part, (int)(grid.x * grid.y), fin);
     FR_CUDA(cudaGetLastError());
@@ -163,7 +187,7 @@ int fr_launch_euler2d_reduce(frgpu_problem *p, const void *state, const void *lo
     double h[6];
     FR_CUDA(cudaMemcpyAsync(h, fin, sizeof(h), cudaMemcpyDeviceToHost, p->stream));
     FR_CUDA(cudaStreamSynchronize(p->stream));
-    const double area = p->sp.dx * p->sp.dy * 0.25;
+    const double area = p->d_met ? 1.0 : p->sp.dx * p->sp.dy * 0.25;
     if (out_sums)
         for (int m = 0; m < 4; ++m) out_sums[m] = h[m] * area;
     if (out_speed) {

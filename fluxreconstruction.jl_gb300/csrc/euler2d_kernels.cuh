@@ -28,6 +28,8 @@ using namespace frk;
 namespace {
 
 enum { MODE_FP64 = 0, MODE_FP32K = 1 };
+// troubled-cell indicator fused into the last stage: none, the learned network, the plain modal-decay test
+enum { FUSE_NONE = 0, FUSE_LEARNED = 1, FUSE_PLAIN = 2 };
 
 template <class Real, int NP> struct E2DArgs {
     int nx, ny;
@@ -51,6 +53,11 @@ template <class Real, int NP> struct E2DArgs {
     // nfx[2 (i + (nx + 1) j)], of y face (i, j) at nfy[2 (i + nx j)]; null: the
     // Cartesian axes with the dudt! scaling by a11 / a22
     const Real *nfx, *nfy;
+    // with normals: the face-Jacobian form of the interface-flux scales (the
+    // cylinder scripts, (inv(Ji) n) per face point): (sL, sR, sB, sT) of element e
+    // at point line q at fsc[(q ne + e) 4 + c], or null for (iJ n) at the
+    // solution points
+    const Real *fsc;
     // stage coefficients of the method (SSPRK3: c1 = 1, fa = 1, fs = 2/3,
     // g = 2, al = 2, be = 1, s3 = 1/3; two-stage methods use stages 1 and 3):
     // stage 1: FP64 u1 = u + c1 dt L(u), FP32K d1 = c1 dt L(u); stage 3 (last):
@@ -167,13 +174,16 @@ template <class Real> __device__ __forceinline__ void get4(const Real *p, int cs
 }
 
 // FP32 CTAs of up to 256 threads: registers capped so that three CTAs share an SM
-// FUSE: stage 3 of the FP32K form with np = 4 also runs the learned troubled-cell
+// FUSE: stage 3 of the FP32K form with np = 4 also runs the troubled-cell
 // indicator + :l2 filter on the elements it has just updated (the post-step
-// filter of example/shock-vortex.jl:308-321 with the network of mlp.cu).
+// filter of example/shock-vortex.jl:308-321): the learned network of mlp.cu
+// (FUSE_LEARNED), or the plain modal-decay test of src/dissipation.jl:13-23
+// (FUSE_PLAIN) on the same features, so that the two forms differ only in the
+// decision.
 // MET: per-point metric a.met (f = a11 F + a12 G, g = a21 F + a22 G; the
 // corrections scale the interface fluxes by a11 and a22 at each point, as the
 // dudt! closure of example/shock-vortex.jl:48-55, :102-115 does with iJ[i, j][k, l]).
-template <class Real, int NP, int FLUX, int MODE, int STAGE, bool FUSE = false, bool MET = false>
+template <class Real, int NP, int FLUX, int MODE, int STAGE, int FUSE = FUSE_NONE, bool MET = false>
 __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                                   sizeof(Real) == 4 && Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY <= 256 ? 3 : 1)
     k_euler2d(const E2DArgs<Real, NP> a) {
@@ -453,13 +463,24 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                 v4_fms<Real>(FL, a.iJx, fxl, aL);
                 v4_fms<Real>(FR, a.iJx, fxr, aR);
             }
+            [[maybe_unused]] Real fsL = Real(0), fsR = Real(0);
+            if constexpr (MET) {
+                if (a.fsc != nullptr) {
+                    fsL = __ldg(a.fsc + ((unsigned)l * plane + e) * 4);
+                    fsR = __ldg(a.fsc + ((unsigned)l * plane + e) * 4 + 1);
+                }
+            }
 #pragma unroll
             for (int kk = 0; kk < NP; ++kk) {
                 if constexpr (MET) {
-                    // a11 at point (kk, l); with normals (iJ n)_1 of the left and right faces
+                    // a11 at point (kk, l); with normals (iJ n)_1 of the left and right faces,
+                    // or the face-Jacobian scales of the face points
                     const unsigned at = ((unsigned)(kk + NP * l) * plane + e) * 4;
                     Real sL = __ldg(a.met + at), sR = sL;
-                    if (a.nfx != nullptr) {
+                    if (a.fsc != nullptr) {
+                        sL = fsL;
+                        sR = fsR;
+                    } else if (a.nfx != nullptr) {
                         const Real a12 = __ldg(a.met + at + 1);
                         const Real *nL = a.nfx + 2 * ((unsigned)i + (unsigned)(nx + 1) * j);
                         sL = fmaR<Real>(a12, nL[1], sR * nL[0]);
@@ -489,13 +510,24 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             v4_fms<Real>(FB, a.iJy, gyb, bB);
             v4_fms<Real>(FT, a.iJy, gyt, bT);
         }
+        [[maybe_unused]] Real fsB = Real(0), fsT = Real(0);
+        if constexpr (MET) {
+            if (a.fsc != nullptr) {
+                fsB = __ldg(a.fsc + ((unsigned)k * plane + e) * 4 + 2);
+                fsT = __ldg(a.fsc + ((unsigned)k * plane + e) * 4 + 3);
+            }
+        }
 #pragma unroll
         for (int l = 0; l < NP; ++l) {
             if constexpr (MET) {
-                // a22 at point (k, l); with normals (iJ n)_2 of the bottom and top faces
+                // a22 at point (k, l); with normals (iJ n)_2 of the bottom and top faces,
+                // or the face-Jacobian scales of the face points
                 const unsigned at = ((unsigned)(k + NP * l) * plane + e) * 4;
                 Real sB = __ldg(a.met + at + 3), sT = sB;
-                if (a.nfy != nullptr) {
+                if (a.fsc != nullptr) {
+                    sB = fsB;
+                    sT = fsT;
+                } else if (a.nfy != nullptr) {
                     const Real a21 = __ldg(a.met + at + 2);
                     const Real *nB = a.nfy + 2 * ((unsigned)i + (unsigned)nx * j), *nT = nB + 2 * nx;
                     sB = fmaR<Real>(sT, nB[1], a21 * nB[0]);
@@ -561,7 +593,7 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
                     v4_sub<Real>(y, c, lo);               // lo_new = y - (t - hi)
                     st4(a.ul + at, lo);
                     // u is dead in FP32K phase D: with the fused indicator it now holds u^{n+1}
-                    if (FUSE) put4(&SU(ey, l, k, 0, ex), CS, res);
+                    if (FUSE != FUSE_NONE) put4(&SU(ey, l, k, 0, ex), CS, res);
                 }
                 st4(a.out + at, res);
             }
@@ -577,7 +609,7 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
     // them in shared memory per CTA measured slower), the
     // decision with the plain test as fallback and judge, and the :l2 filter
     // of the troubled elements in global memory.
-    if constexpr (FUSE) {
+    if constexpr (FUSE != FUSE_NONE) {
         static_assert(NP == 4 && TX == 32 && TY == 2, "the fused indicator works on 32 x 2 tiles of np = 4");
         __syncthreads();
         const int warp = tid >> 5, lane = tid & 31;
@@ -600,28 +632,34 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             }
             float feat[16], su = 0.f;
             features_from_raw(w, ev, pr, a.iv1, (float)a.gm1, feat, su);
-            store_features_bf16(xs + (lane & 15) * NIN + (pr ? 16 : 0), feat);
-            __syncwarp();
-            Fwd f;
-            // 12 KB of weights, L1-resident; warp-level mma.sync: the tcgen05 routine of the
-            // stand-alone kernel measured slower here (per-CTA TMEM allocation, weight
-            // copy and two MMA round trips for only 64 elements)
-            mlp_forward_tile(global_view(a.mlp), xs, f);
-            if ((lane & 3) == 0) {
-                prob[lane >> 2] = sigmoidf_(f.logit_g);
-                prob[(lane >> 2) + 8] = sigmoidf_(f.logit_g8);
+            if constexpr (FUSE == FUSE_LEARNED) {
+                store_features_bf16(xs + (lane & 15) * NIN + (pr ? 16 : 0), feat);
+                __syncwarp();
+                Fwd f;
+                // 12 KB of weights, L1-resident; warp-level mma.sync: the tcgen05 routine of the
+                // stand-alone kernel measured slower here (per-CTA TMEM allocation, weight
+                // copy and two MMA round trips for only 64 elements)
+                mlp_forward_tile(global_view(a.mlp), xs, f);
+                if ((lane & 3) == 0) {
+                    prob[lane >> 2] = sigmoidf_(f.logit_g);
+                    prob[(lane >> 2) + 8] = sigmoidf_(f.logit_g8);
+                }
+                __syncwarp();
             }
-            __syncwarp();
             bool tr = false;
             int n_tr = 0, n_mis = 0, n_fb = 0;
             if (!pr && ev) {
                 const bool plain = plain_troubled(su, a.ind_S0, a.ind_kappa);
-                const float pm = prob[lane];
-                const bool fb = fabsf(pm - a.ind_thr) < a.ind_band, net = pm > a.ind_thr;
-                tr = fb ? plain : net;
+                if constexpr (FUSE == FUSE_LEARNED) {
+                    const float pm = prob[lane];
+                    const bool fb = fabsf(pm - a.ind_thr) < a.ind_band, net = pm > a.ind_thr;
+                    tr = fb ? plain : net;
+                    n_mis = net != plain;
+                    n_fb = fb;
+                } else {
+                    tr = plain;
+                }
                 n_tr = tr;
-                n_mis = net != plain;
-                n_fb = fb;
                 a.flags[(i0 + exl) + nx * (j0 + eyt)] = tr ? 1 : 0;
             }
             const size_t ebase = (size_t)(i0 + 16 * h) + (size_t)nx * (j0 + eyt);
@@ -663,7 +701,7 @@ template <class Real, int NP> Ops<Real, NP> make_ops(const frgpu_space &s) {
     return o;
 }
 
-template <class Real, int NP, int FLUX, int MODE, int STAGE, bool FUSE = false, bool MET = false>
+template <class Real, int NP, int FLUX, int MODE, int STAGE, int FUSE = FUSE_NONE, bool MET = false>
 int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     using T = Tile<Real, NP>;
     using S = Smem<Real, NP, T::TX, T::TY, Stash<MODE, STAGE>::n>;
@@ -689,13 +727,15 @@ int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     a.mlp = frmlp::MLPDev{nullptr, nullptr, nullptr, nullptr, nullptr};
     a.V = a.iV = nullptr;
     a.flags = a.stats = nullptr;
-    if (FUSE) {
+    if (FUSE == FUSE_LEARNED) {
         const fr_mlp_ptrs m = fr_mlp_device(p->mlp);
         a.mlp = frmlp::MLPDev{m.P, (const __nv_bfloat16 *)m.W1, (const __nv_bfloat16 *)m.W2,
                               (const __nv_bfloat16 *)m.W2T, m.TC};
-        fr_iv1_from_tensor(p->sp, &a.iv1.m[0][0]);
         a.ind_thr = p->mlp_thr;
         a.ind_band = p->mlp_band;
+    }
+    if (FUSE != FUSE_NONE) {
+        fr_iv1_from_tensor(p->sp, &a.iv1.m[0][0]);
         a.ind_S0 = (float)p->S0;
         a.ind_kappa = (float)p->kappa;
         a.ind_lam = p->lam;
@@ -708,6 +748,7 @@ int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     a.met = MET ? (const Real *)p->d_met : nullptr;
     a.nfx = MET ? (const Real *)p->d_nfx : nullptr;
     a.nfy = MET ? (const Real *)p->d_nfy : nullptr;
+    a.fsc = MET ? (const Real *)p->d_fsc : nullptr;
     a.c1 = (Real)p->meth.c1;
     a.fa = (Real)p->meth.fa;
     a.fs = (Real)p->meth.fs;
@@ -721,7 +762,7 @@ int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     static fr_smem_optin optin;
     if (int rc = fr_raise_smem(kern, S::bytes, optin, p->prepare_only)) return rc;
     if (p->prepare_only) return FRGPU_OK;
-    if (FUSE) FR_CUDA(cudaMemsetAsync(p->d_count, 0, sizeof(int) * 4, p->stream));
+    if (FUSE != FUSE_NONE) FR_CUDA(cudaMemsetAsync(p->d_count, 0, sizeof(int) * 4, p->stream));
     dim3 grid((a.nx + T::TX - 1) / T::TX, (a.ny + T::TY - 1) / T::TY);
     kern<<<grid, T::TX * NP * T::TY, S::bytes, p->stream>>>(a);
     FR_CUDA(cudaGetLastError());
@@ -733,12 +774,16 @@ template <class Real, int NP, int MODE, bool MET>
 int dispatch_stage(frgpu_problem *p, int stage, const void *in, const void *din, void *out) {
     const int flux = p->d.flux == FRGPU_FLUX_HLL ? FLUX_HLL : FLUX_LF;
 #define FR_ST(S)                                                                                                   \
-    return flux == FLUX_HLL ? launch_t<Real, NP, FLUX_HLL, MODE, S, false, MET>(p, in, din, out)                   \
-                            : launch_t<Real, NP, FLUX_LF, MODE, S, false, MET>(p, in, din, out)
+    return flux == FLUX_HLL ? launch_t<Real, NP, FLUX_HLL, MODE, S, FUSE_NONE, MET>(p, in, din, out)               \
+                            : launch_t<Real, NP, FLUX_LF, MODE, S, FUSE_NONE, MET>(p, in, din, out)
     if constexpr (!MET && std::is_same<Real, float>::value && NP == 4 && MODE == MODE_FP32K) {
-        if (stage == 3 && fr_fused_indicator(p))
-            return flux == FLUX_HLL ? launch_t<Real, NP, FLUX_HLL, MODE, 3, true>(p, in, din, out)
-                                    : launch_t<Real, NP, FLUX_LF, MODE, 3, true>(p, in, din, out);
+        const int fused = stage == 3 ? fr_fused_indicator(p) : FRGPU_IND_NONE;
+        if (fused == FRGPU_IND_MLP)
+            return flux == FLUX_HLL ? launch_t<Real, NP, FLUX_HLL, MODE, 3, FUSE_LEARNED>(p, in, din, out)
+                                    : launch_t<Real, NP, FLUX_LF, MODE, 3, FUSE_LEARNED>(p, in, din, out);
+        if (fused == FRGPU_IND_PLAIN)
+            return flux == FLUX_HLL ? launch_t<Real, NP, FLUX_HLL, MODE, 3, FUSE_PLAIN>(p, in, din, out)
+                                    : launch_t<Real, NP, FLUX_LF, MODE, 3, FUSE_PLAIN>(p, in, din, out);
     }
     switch (stage) {
     case 0: FR_ST(0);

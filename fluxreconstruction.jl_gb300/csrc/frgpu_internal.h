@@ -58,6 +58,7 @@ struct frgpu_problem {
     void *d_stage = nullptr;                // FP64 staging of state uploads / downloads (+ 8 bytes)
     void *d_met = nullptr;                  // 2D Euler: per-point inverse Jacobian (a11, a12, a21, a22), or null
     void *d_nfx = nullptr, *d_nfy = nullptr; // with d_met: unit normals of the x and y faces, or null
+    void *d_fsc = nullptr; // with normals: interface-flux scales (inv(Ji) n) per (point line, element), or null
     int parity = 0;                         // FP32K: which buffer holds u^n (0: s0, 1: s1)
     bool prepare_only = false;              // launchers only set kernel attributes
     // post-step filter
@@ -186,9 +187,11 @@ struct fr_mlp_ptrs {
 fr_mlp_ptrs fr_mlp_device(const frgpu_mlp *m);
 // 1D factor iV1[i][k] (row-major 4 x 4, float) of a deg-3 2D space's tensor inverse Vandermonde matrix
 void fr_iv1_from_tensor(const frgpu_space &s, float *iv1);
-// Does stage 3 of this problem run the learned indicator itself (FP32K 2D Euler,
-// deg 3, learned indicator bound and selected, fusion not switched off)?
-bool fr_fused_indicator(const frgpu_problem *p);
+// Which indicator stage 3 of this problem runs itself (FP32K 2D Euler, deg 3,
+// uniform rectangles, fusion not switched off): FRGPU_IND_MLP (a network bound
+// and selected), FRGPU_IND_PLAIN, or FRGPU_IND_NONE (the filter, if any, runs
+// as its own kernel after the step).
+int fr_fused_indicator(const frgpu_problem *p);
 int fr_launch_mlp_indicator(frgpu_problem *p, double lam, double S0, double kappa);
 // positivity-preserving limiter (limiter.cu)
 int fr_launch_limiter(frgpu_problem *p, const std::vector<double> &w, double t0);

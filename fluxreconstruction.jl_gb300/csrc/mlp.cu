@@ -669,9 +669,13 @@ static IV1 iv1_from_tensor(const frgpu_problem *p) {
     return r;
 }
 
-bool fr_fused_indicator(const frgpu_problem *p) {
-    return p->fuse_indicator && p->indicator == FRGPU_IND_MLP && p->mlp && p->d.equation == FRGPU_EULER2D &&
-           p->d.precision == FRGPU_FP32K && p->sp.np == 4 && p->d_V && p->d_iV && !p->d_met;
+int fr_fused_indicator(const frgpu_problem *p) {
+    const bool fusable = p->fuse_indicator && p->d.equation == FRGPU_EULER2D && p->d.precision == FRGPU_FP32K &&
+                         p->sp.np == 4 && p->d_V && p->d_iV && !p->d_met;
+    if (!fusable) return FRGPU_IND_NONE;
+    if (p->indicator == FRGPU_IND_MLP && p->mlp) return FRGPU_IND_MLP;
+    if (p->indicator == FRGPU_IND_PLAIN) return FRGPU_IND_PLAIN;
+    return FRGPU_IND_NONE;
 }
 
 int fr_launch_features(frgpu_problem *p, float *d_feat) {

@@ -293,7 +293,7 @@ static void free_problem(frgpu_problem *p) {
     if (p->erk_gexec) cudaGraphExecDestroy(p->erk_gexec);
     void *bufs[] = {p->s0, p->s1, p->s2, p->s3, p->d_dt, p->d_status, p->d_red, p->d_flags, p->d_count,
                     p->d_velo, p->d_w, p->d_J, p->d_V, p->d_iV, p->rhs_in, p->rhs_out, p->d_bgk_prim,
-                    p->d_bgk_frag, p->d_stage, p->d_erk, p->d_met, p->d_nfx, p->d_nfy};
+                    p->d_bgk_frag, p->d_stage, p->d_erk, p->d_met, p->d_nfx, p->d_nfy, p->d_fsc};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -882,7 +882,7 @@ FRGPU_API int frgpu_problem_set_metric(frgpu_problem *p, const double *iJ, const
     FR_REQ(iJ || !n1, "problem_set_metric: face normals need the metric");
     FR_TRY
     FR_CUDA(cudaStreamSynchronize(p->stream));
-    for (void **b : {&p->d_nfx, &p->d_nfy})
+    for (void **b : {&p->d_nfx, &p->d_nfy, &p->d_fsc})
         if (*b) {
             cudaFree(*b);
             *b = nullptr;
@@ -918,6 +918,70 @@ FRGPU_API int frgpu_problem_set_metric(frgpu_problem *p, const double *iJ, const
             int rc = upload_pairs(p, &p->d_nfx, n1, (nx + 1) * ny);
             if (!rc) rc = upload_pairs(p, &p->d_nfy, n2, nx * (ny + 1));
             if (rc) return rc;
+        }
+    }
+    p->graph_ind = -2; // force a re-capture
+    p->erk_dirty = true;
+    return FRGPU_OK;
+    FR_CATCH
+}
+
+// (inv(J) n)_comp of a 2 x 2 matrix J (column-major j00, j10, j01, j11) and a
+// vector n, in the order of the oracle's restatement
+static double inv_dot(double j00, double j10, double j01, double j11, double n0, double n1, int comp) {
+    const double det = j00 * j11 - j01 * j10;
+    return comp == 0 ? (j11 * n0 - j01 * n1) / det : (j00 * n1 - j10 * n0) / det;
+}
+
+FRGPU_API int frgpu_problem_set_face_jacobians(frgpu_problem *p, const double *Ji, const double *n1, const double *n2) {
+    FR_REQ(p, "problem_set_face_jacobians: null problem");
+    FR_REQ(p->d.equation == FRGPU_EULER2D, "problem_set_face_jacobians: 2D Euler problems only");
+    FR_REQ(p->d_met && p->d_nfx && p->d_nfy,
+           "problem_set_face_jacobians: set the metric and the face normals first (frgpu_problem_set_metric)");
+    FR_REQ(n1 && n2, "problem_set_face_jacobians: pass the face normals the metric was set with");
+    FR_TRY
+    FR_CUDA(cudaStreamSynchronize(p->stream));
+    if (p->d_fsc) {
+        cudaFree(p->d_fsc);
+        p->d_fsc = nullptr;
+    }
+    if (Ji) {
+        // host Ji[nx, ny, 4, np, 2, 2] (column-major) -> per (point line q, element e)
+        // the scales (sL, sR, sB, sT) of the element's left, right, bottom and top
+        // interface fluxes at point q of the face
+        const long nx = p->sp.nx, ny = p->sp.ny, np = p->sp.np, ne = nx * ny;
+        auto J = [&](long i, long j, int f, long k, int a, int b) {
+            return Ji[i + nx * (j + ny * (f + 4 * (k + np * (a + 2 * b))))];
+        };
+        const long nfx = (nx + 1) * ny, nfy = nx * (ny + 1);
+        std::vector<double> dev(4 * np * ne);
+        for (long j = 0; j < ny; ++j)
+            for (long i = 0; i < nx; ++i)
+                for (long q = 0; q < np; ++q) {
+                    const long e = i + nx * j;
+                    const long fl = i + (nx + 1) * j, fb = i + nx * j;
+                    // faces 1..4 of the reference (bottom, right, top, left) -> f = 0..3
+                    double *d = &dev[(q * ne + e) * 4];
+                    d[0] = inv_dot(J(i, j, 3, q, 0, 0), J(i, j, 3, q, 1, 0), J(i, j, 3, q, 0, 1), J(i, j, 3, q, 1, 1),
+                                   n1[fl], n1[fl + nfx], 0);
+                    d[1] = inv_dot(J(i, j, 1, q, 0, 0), J(i, j, 1, q, 1, 0), J(i, j, 1, q, 0, 1), J(i, j, 1, q, 1, 1),
+                                   n1[fl + 1], n1[fl + 1 + nfx], 0);
+                    d[2] = inv_dot(J(i, j, 0, q, 0, 0), J(i, j, 0, q, 1, 0), J(i, j, 0, q, 0, 1), J(i, j, 0, q, 1, 1),
+                                   n2[fb], n2[fb + nfy], 1);
+                    d[3] = inv_dot(J(i, j, 2, q, 0, 0), J(i, j, 2, q, 1, 0), J(i, j, 2, q, 0, 1), J(i, j, 2, q, 1, 1),
+                                   n2[fb + nx], n2[fb + nx + nfy], 1);
+                    for (int c = 0; c < 4; ++c)
+                        if (!std::isfinite(d[c])) {
+                            fr_set_error("problem_set_face_jacobians: singular face Jacobian or non-finite value");
+                            return FRGPU_ERR_ARG;
+                        }
+                }
+        FR_CUDA(cudaMalloc(&p->d_fsc, dev.size() * p->esize));
+        if (p->esize == 8) {
+            FR_CUDA(cudaMemcpy(p->d_fsc, dev.data(), sizeof(double) * dev.size(), cudaMemcpyHostToDevice));
+        } else {
+            std::vector<float> f(dev.begin(), dev.end());
+            FR_CUDA(cudaMemcpy(p->d_fsc, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice));
         }
     }
     p->graph_ind = -2; // force a re-capture

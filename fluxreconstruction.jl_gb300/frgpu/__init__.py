@@ -53,6 +53,7 @@ from .api import (  # noqa: F401
     legendre_point,
     modal_filter_,
     poly_derivative_,
+    quad_face_jacobians,
     quad_face_normals,
     quad_metric,
     rs_jacobi_quad,

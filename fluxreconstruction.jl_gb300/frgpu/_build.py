@@ -17,8 +17,10 @@ LIB = os.path.join(PKG_ROOT, "libfrgpu.so")
 INCLUDE = os.path.join(os.path.dirname(PKG_ROOT), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code contracts no multiply-adds either (-ffp-contract=off), so that host
+# arithmetic (setup math, metric scales) gives the same bits on x86 and Arm
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
-              "-Xcompiler", "-fvisibility=hidden", "-I", INCLUDE]
+              "-Xcompiler", "-fvisibility=hidden", "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE]
 
 
 def _nvcc() -> str:

@@ -72,6 +72,7 @@ SIGNATURES = {
     "frgpu_positive_limiter": (C.c_int, [_VP, _D, C.c_double, _I]),
     "frgpu_step_erk": (C.c_int, [_VP, C.c_int, _D, _D, C.c_double, C.c_int]),
     "frgpu_problem_set_metric": (C.c_int, [_VP, _D, _D, _D]),
+    "frgpu_problem_set_face_jacobians": (C.c_int, [_VP, _D, _D, _D]),
     "frgpu_vandermonde_tri": (C.c_int, [C.c_int, _D, _D, C.c_int, _D, _D, _D]),
     "frgpu_tri_operators": (C.c_int, [C.c_int, _D, _D, _D, _D, _D, _D]),
     "frgpu_tri_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, _D, _D, _D, _D, _D, _I, _I, _I, _I,

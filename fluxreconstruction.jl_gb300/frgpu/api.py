@@ -215,6 +215,30 @@ def quad_metric(r, vertices) -> np.ndarray:
     return np.asfortranarray(np.linalg.inv(rs_jacobi_quad(r, vertices)))
 
 
+def quad_face_jacobians(r, vertices) -> np.ndarray:
+    """FRPSpace2D's face Jacobians Ji[i, j][f, k] (src/struct.jl:145-158) as an
+    array Ji[nx, ny, 4, np, 2, 2], built as the reference builds them: the face
+    coordinates ri[f, :], si[f, :] (face 1: (r, 0); 2: (1, r); 3: (reversed r, 1);
+    4: (0, reversed r)) go through rs_jacobi(ri, si, vertices), whose matrix method
+    (src/Geometry/geo_jacobi.jl) indexes ri[i], si[i] linearly over the face
+    index i only, so every point k of face f gets the Jacobian at (ri[f, 1],
+    si[f, 1]): (r_1, 0), (1, r_1), (r_np, 1), (0, r_np).  On a parallelogram J
+    is the same everywhere, so these equal the Jacobian on the faces."""
+    r = np.asarray(r, dtype=np.float64)
+    V = np.asarray(vertices, dtype=np.float64)
+    nx, ny = V.shape[:2]
+    n = len(r)
+    pts = [(r[0], 0.0), (1.0, r[0]), (r[-1], 1.0), (0.0, r[-1])]
+    v = [V[:, :, a, :] for a in range(4)]
+    Ji = np.zeros((nx, ny, 4, n, 2, 2), order="F")
+    for f, (R, S) in enumerate(pts):
+        Xr = (S - 1) * v[0] / 4 + (1 - S) * v[1] / 4 + (S + 1) * v[2] / 4 - (S + 1) * v[3] / 4
+        Xs = (R - 1) * v[0] / 4 - (R + 1) * v[1] / 4 + (R + 1) * v[2] / 4 + (1 - R) * v[3] / 4
+        Ji[:, :, f, :, :, 0] = Xr[:, :, None, :]
+        Ji[:, :, f, :, :, 1] = Xs[:, :, None, :]
+    return Ji
+
+
 def quad_face_normals(vertices):
     """Unit normals of the straight faces of a structured quadrilateral mesh
     (vertices[nx, ny, 4, 2]), in the orientation dev/parallelogram.jl uses:
@@ -393,11 +417,14 @@ class ODEProblem:
         self.f(du, u, self, t)
         return du
 
-    def set_metric(self, iJ, n1=None, n2=None) -> None:
+    def set_metric(self, iJ, n1=None, n2=None, Ji=None) -> None:
         """Per-point inverse Jacobian (FRPSpace2D's iJ[i, j][k, l],
         src/struct.jl:135-158) as an array [nx, ny, np, np, 2, 2], and optionally
         the unit normals of the x faces n1[nx+1, ny, 2] and the y faces
         n2[nx, ny+1, 2] (straight-sided quadrilaterals, dev/parallelogram.jl:115-160);
+        with the normals, optionally the face Jacobians Ji[nx, ny, 4, np, 2, 2]
+        (FRPSpace2D's Ji, src/struct.jl:145-158; quad_face_jacobians) for the
+        face-Jacobian interface-flux scaling of dev/cylinder2.jl:147-150;
         None returns to the uniform rectangles."""
         if iJ is None:
             check(L.lib().frgpu_problem_set_metric(self._h, None, None, None))
@@ -414,6 +441,12 @@ class ODEProblem:
         if b1.shape != (nx + 1, ny, 2) or b2.shape != (nx, ny + 1, 2):
             raise ValueError("face normals must have shapes (nx+1, ny, 2) and (nx, ny+1, 2)")
         check(L.lib().frgpu_problem_set_metric(self._h, dptr(a), dptr(b1), dptr(b2)))
+        if Ji is not None:
+            c = np.asfortranarray(np.asarray(Ji, dtype=np.float64))
+            if c.shape != (nx, ny, 4, self.shape[2], 2, 2):
+                raise ValueError("Ji must have shape (nx, ny, 4, np, 2, 2)")
+            self._keep_ji = c
+            check(L.lib().frgpu_problem_set_face_jacobians(self._h, dptr(c), dptr(b1), dptr(b2)))
 
     def set_option(self, option: int, value: int) -> None:
         """Kernel choice for measurements (frgpu_problem_set_option), e.g.

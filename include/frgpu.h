@@ -163,7 +163,10 @@ FRGPU_API int frgpu_step_ssprk3_async(frgpu_problem *p, double dt, int nsteps);
  * filter configured for the problem run before and after every step, as with
  * frgpu_step_ssprk3.  Steps are replayed from a captured CUDA graph. */
 FRGPU_API int frgpu_step_erk(frgpu_problem *p, int s, const double *A, const double *b, double dt, int nsteps);
-/* dt = cfl / max over points of sum_d (|u_d| + c)/dx_d (FP64 max-reduction on the GPU) */
+/* dt = cfl / max over points of sum_d (|u_d| + c)/dx_d (FP64 max-reduction on the GPU);
+ * with a per-point metric (frgpu_problem_set_metric) the rate at a point is
+ * (lambda_r + lambda_s)/2 with the contravariant speeds lambda_r = |a11 u + a12 v|
+ * + c |(a11, a12)| and lambda_s = |a21 u + a22 v| + c |(a21, a22)|. */
 FRGPU_API int frgpu_cfl_dt(frgpu_problem *p, double cfl, double *dt);
 /* FP64 conserved sums (quadrature-weighted, per variable) and max wave speed */
 FRGPU_API int frgpu_reduce(frgpu_problem *p, double *sums, double *maxspeed);
@@ -202,6 +205,16 @@ FRGPU_API int frgpu_positive_limiter(frgpu_problem *p, const double *weights, do
  * iJ = NULL returns to the uniform rectangles of the space (iJ = diag(2/dx,
  * 2/dy)); 2D Euler only.  The learned indicator then runs as its own kernel. */
 FRGPU_API int frgpu_problem_set_metric(frgpu_problem *p, const double *iJ, const double *n1, const double *n2);
+/* The face-Jacobian form of the interface-flux scaling of the reference's
+ * quadrilateral cylinder scripts (dev/cylinder2.jl:147-150, dev/cylinder3.jl:
+ * 147-150; commented out in dev/curve_euler.jl:130-133): the interface flux of
+ * face point q is scaled by (inv(Ji[i, j][f, q]) n)_1 on x faces (f = left 4,
+ * right 2) and (inv(Ji[i, j][f, q]) n)_2 on y faces (f = bottom 1, top 3), with
+ * the face Jacobians Ji of FRPSpace2D (src/struct.jl:145-158) passed as
+ * Ji[nx, ny, 4, np, 2, 2] (column-major) and the unit normals n1, n2 the metric
+ * was set with.  Needs frgpu_problem_set_metric with normals first; Ji = NULL
+ * returns to the (iJ n) scaling at the solution points. */
+FRGPU_API int frgpu_problem_set_face_jacobians(frgpu_problem *p, const double *Ji, const double *n1, const double *n2);
 /* Run the limiter before every step of frgpu_step_ssprk3 (the loop of
  * example/shock-vortex.jl:297-303); on = 0 turns it off. */
 FRGPU_API int frgpu_set_limiter(frgpu_problem *p, int on, const double *weights, double t0);
@@ -210,9 +223,9 @@ FRGPU_API int frgpu_troubled_flags(frgpu_problem *p, int *flags, long n);
 /* Kernel choices for measurements; no counterpart in the reference.
  * FRGPU_OPT_BGK_TENSOR: 1 (default) runs the FP32 BGK transport as a TF32-split
  * tensor-core product, 0 on the CUDA cores.
- * FRGPU_OPT_FUSED_INDICATOR: 1 (default) runs the learned indicator + filter of
- * an FP32K deg-3 2D Euler problem inside its third SSPRK3 stage, 0 as a kernel
- * of its own after the step.
+ * FRGPU_OPT_FUSED_INDICATOR: 1 (default) runs the indicator (learned or plain)
+ * + filter of an FP32K deg-3 2D Euler problem inside its third SSPRK3 stage, 0
+ * as a kernel of its own after the step.
  * FRGPU_OPT_FUSED_TWO_STAGE: 1 (default) runs two-stage tableaux of
  * frgpu_step_erk (Midpoint, Heun, ...) on a 2D Euler problem fused into the
  * stage kernel, 0 through the generic residual + combination kernels.

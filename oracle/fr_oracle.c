@@ -583,6 +583,17 @@ static void e2d_fill_ghosts(const fro_cfg *c, const double *u, e2d_work *w) {
 /* Interface flux across a face with unit normal n (example
  * dev/parallelogram.jl:115-133): both states to the face frame (momentum along n
  * and along t = (-ny, nx)), the x-direction flux, back to the global frame. */
+/* (inv(J) n)_comp for the face Jacobian J = Ji[i, j][f, pt] (2 x 2, column-major
+ * entries of the host array Ji[nx, ny, 4, np, 2, 2]): inv(J) = [j11 -j01; -j10 j00] / det */
+static double ji_dot(const fro_cfg *c, long i, long j, int f, long pt, double n0, double n1, int comp) {
+    const long nx = c->nx, ny = c->ny, np = c->np;
+    const long base = i + nx * (j + ny * (f + 4 * pt)), blk = nx * ny * 4 * np;
+    const double j00 = c->Ji[base], j10 = c->Ji[base + blk], j01 = c->Ji[base + 2 * blk],
+                 j11 = c->Ji[base + 3 * blk];
+    const double det = j00 * j11 - j01 * j10;
+    return comp == 0 ? (j11 * n0 - j01 * n1) / det : (j00 * n1 - j10 * n0) / det;
+}
+
 static void face_flux_n(const fro_cfg *c, const double *wL, const double *wR, double nx_, double ny_, double *fw) {
     double l[4], r[4], f[4];
     l[0] = wL[0]; l[1] = fma(wL[2], ny_, wL[1] * nx_); l[2] = fma(-wL[1], ny_, wL[2] * nx_); l[3] = wL[3];
@@ -753,6 +764,17 @@ static void rhs_euler2d(const fro_cfg *c, double *du, const double *u) {
                             const long fb = i + (long)nx * j, nf = (long)nx * (ny + 1);
                             sB = fma(a22, c->n2[fb + nf], a21 * c->n2[fb]);
                             sT = fma(a22, c->n2[fb + nx + nf], a21 * c->n2[fb + nx]);
+                        }
+                        if (c->Ji && c->n1 && c->n2) {
+                            /* dev/cylinder2.jl:147-150: (inv(Ji[i, j][f, pt]) n)_1 on the left (face 4)
+                             * and right (face 2) faces at row l, (inv(Ji) n)_2 on the bottom (face 1)
+                             * and top (face 3) faces at column k */
+                            const long fl = i + (long)(nx + 1) * j, nfx = (long)(nx + 1) * ny;
+                            const long fb = i + (long)nx * j, nfy = (long)nx * (ny + 1);
+                            sL = ji_dot(c, i, j, 3, l, c->n1[fl], c->n1[fl + nfx], 0);
+                            sR = ji_dot(c, i, j, 1, l, c->n1[fl + 1], c->n1[fl + 1 + nfx], 0);
+                            sB = ji_dot(c, i, j, 0, k, c->n2[fb], c->n2[fb + nfy], 1);
+                            sT = ji_dot(c, i, j, 2, k, c->n2[fb + nx], c->n2[fb + nx + nfy], 1);
                         }
                     }
                     double aL = fxl * sL - ff[(3 * np + l) * 4 + m];

@@ -73,6 +73,9 @@ typedef struct {
                                   (column-major) or NULL for diag(iJx, iJy) */
     const double *n1, *n2;     /* 2D with iJ: unit normals of the x faces [nx+1, ny, 2] and
                                   the y faces [nx, ny+1, 2], or NULL for the Cartesian axes */
+    const double *Ji;          /* 2D with iJ and normals: face Jacobians [nx, ny, 4, np, 2, 2]
+                                  (FRPSpace2D's Ji, src/struct.jl:145-158) for the interface-flux
+                                  scales of dev/cylinder2.jl:147-150, or NULL */
 } fro_cfg;
 
 long fro_ndof(const fro_cfg *c);

@@ -50,7 +50,7 @@ class Cfg(C.Structure):
         ("iJx", C.c_double), ("iJy", C.c_double),
         ("ll", _D), ("lr", _D), ("lpdm", _D), ("dgl", _D), ("dgr", _D),
         ("velo", _D), ("weights", _D),
-        ("iJ", _D), ("n1", _D), ("n2", _D),
+        ("iJ", _D), ("n1", _D), ("n2", _D), ("Ji", _D),
     ]
 
 
@@ -304,11 +304,12 @@ class Problem:
         self.space = space
         self.kind = kind
 
-    def set_metric(self, iJ, n1=None, n2=None) -> None:
+    def set_metric(self, iJ, n1=None, n2=None, Ji=None) -> None:
         """2D: per-point inverse Jacobian iJ[nx, ny, np, np, 2, 2] (None: diag(iJx,
         iJy)), and optionally the unit normals of the x faces n1[nx+1, ny, 2] and
-        the y faces n2[nx, ny+1, 2] (None: the Cartesian axes)."""
-        self.cfg.iJ = self.cfg.n1 = self.cfg.n2 = None
+        the y faces n2[nx, ny+1, 2] (None: the Cartesian axes), and with them the
+        face Jacobians Ji[nx, ny, 4, np, 2, 2] of the cylinder scripts' scaling."""
+        self.cfg.iJ = self.cfg.n1 = self.cfg.n2 = self.cfg.Ji = None
         if iJ is None:
             return
 
@@ -320,6 +321,8 @@ class Problem:
         self.cfg.iJ = keep(iJ)
         if n1 is not None:
             self.cfg.n1, self.cfg.n2 = keep(n1), keep(n2)
+            if Ji is not None:
+                self.cfg.Ji = keep(Ji)
 
     def shape(self):
         c = self.cfg

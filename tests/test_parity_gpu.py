@@ -651,6 +651,94 @@ def test_metric_general_matches_oracle(frgpu, oracle, flux):
     assert rel(prob.rhs(u), P.rhs(u)) < RTOL64
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("fp32k", 1e-6)])
+def test_metric_reductions_use_the_metric(frgpu, precision, tol):
+    """With a per-point metric the conserved sums integrate over the physical
+    elements (weights w_k w_l det J at each point) and the CFL rate uses the
+    contravariant speeds, (lambda_r + lambda_s)/2 with lambda_r = |a11 u + a12 v|
+    + c |(a11, a12)| and lambda_s = |a21 u + a22 v| + c |(a21, a22)|; the
+    rectangles' own metric gives the rectangles' sums and dt."""
+    ps = frgpu.FRPSpace2D(0, 1, 24, 0, 1, 20, 3)
+    u = wave2d(ps.xpg)
+    iJ = _metric(ps)
+    prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf", bc="period", precision=precision)
+    prob.set_metric(iJ)
+    itg = frgpu.init(prob, dt=1e-4)
+    sums, _ = itg.reduce()
+    a11, a12, a21, a22 = iJ[..., 0, 0], iJ[..., 0, 1], iJ[..., 1, 0], iJ[..., 1, 1]
+    detJ = 1.0 / (a11 * a22 - a12 * a21)
+    ref = np.array([np.sum(ps.wp[None, None] * u[..., m] * detJ) for m in range(4)])
+    np.testing.assert_allclose(sums, ref, rtol=tol, atol=0)
+    U, V = u[..., 1] / u[..., 0], u[..., 2] / u[..., 0]
+    c = np.sqrt(1.4 * 0.4 * (u[..., 3] - 0.5 * u[..., 0] * (U * U + V * V)) / u[..., 0])
+    lr = np.abs(a11 * U + a12 * V) + c * np.hypot(a11, a12)
+    ls = np.abs(a21 * U + a22 * V) + c * np.hypot(a21, a22)
+    assert abs(itg.cfl_dt(0.1) - 0.1 / np.max(0.5 * (lr + ls))) <= tol * 0.1 / np.max(0.5 * (lr + ls))
+    # the rectangles' own metric: the rectangles' sums and dt
+    plain = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf", bc="period", precision=precision)
+    ip = frgpu.init(plain, dt=1e-4)
+    diag = np.zeros_like(iJ)
+    diag[..., 0, 0], diag[..., 1, 1] = 2 / ps.dx, 2 / ps.dy
+    prob.set_metric(diag)
+    np.testing.assert_allclose(itg.reduce()[0], ip.reduce()[0], rtol=tol, atol=0)
+    assert abs(itg.cfl_dt(0.1) - ip.cfl_dt(0.1)) <= tol * ip.cfl_dt(0.1)
+
+
+def _mapped_vertices(nx, ny, mapping):
+    """vertices[nx, ny, 4, 2] of the cells of the unit square under `mapping`,
+    counterclockwise from the lower left."""
+    X, Y = np.linspace(0, 1, nx + 1), np.linspace(0, 1, ny + 1)
+    V = np.zeros((nx, ny, 4, 2))
+    for a, (di, dj) in enumerate(((0, 0), (1, 0), (1, 1), (0, 1))):
+        xx, yy = np.meshgrid(X[di:nx + di], Y[dj:ny + dj], indexing="ij")
+        V[:, :, a, 0], V[:, :, a, 1] = mapping(xx, yy)
+    return V
+
+
+@pytest.mark.parametrize("flux", ["lf", "hll"])
+def test_metric_face_jacobians_match_oracle(frgpu, oracle, flux):
+    """The face-Jacobian scaling of the interface fluxes (dev/cylinder2.jl:147-150
+    with FRPSpace2D's face Jacobians Ji, src/struct.jl:145-158): on a bilinear,
+    non-affine mesh the residual and three SSPRK3 steps match the oracle in
+    FP64 (1e-12); on parallelograms (where Ji is the exact face Jacobian) a
+    uniform flow stays uniform in FP64 and FP32K."""
+    nx, ny, deg = 20, 12, 3
+    ps = frgpu.FRPSpace2D(0, 1, nx, 0, 1, ny, deg)
+    po = oracle_space2d(ps, 0, 1, nx, 0, 1, ny, deg)
+    V = _mapped_vertices(nx, ny, lambda x, y: (x + 0.04 * np.sin(np.pi * y) * x, y + 0.05 * x * y))
+    iJ = frgpu.quad_metric(ps.xpl, V)
+    n1, n2 = frgpu.quad_face_normals(V)
+    Ji = frgpu.quad_face_jacobians(ps.xpl, V)
+    u = wave2d(ps.xpg)
+    P = oracle.Problem(oracle.EULER2D, po, gamma=1.4, flux=oracle.FLUX_HLL if flux == "hll" else oracle.FLUX_LF)
+    P.set_metric(iJ, n1, n2, Ji)
+    prob = frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux=flux, bc="period")
+    prob.set_metric(iJ, n1, n2, Ji)
+    g, o = prob.rhs(u), P.rhs(u)
+    print(f"face Jacobians {flux}: residual bit-identical {np.array_equal(g, o)}")
+    assert rel(g, o) < RTOL64
+    # a different scaling than (iJ n) at the solution points
+    P2 = oracle.Problem(oracle.EULER2D, po, gamma=1.4, flux=oracle.FLUX_HLL if flux == "hll" else oracle.FLUX_LF)
+    P2.set_metric(iJ, n1, n2)
+    assert rel(P2.rhs(u), o) > 1e-6
+    dt = 1e-4
+    itg = frgpu.init(prob, dt=dt)
+    itg.step(3)
+    assert rel(itg.u, P.ssprk3(u, dt, 3)) < RTOL64
+    # parallelograms: free stream
+    s_, t_ = 0.3, -0.2
+    Vp = _mapped_vertices(nx, ny, lambda x, y: (x + s_ * y, y + t_ * x))
+    uni = np.zeros(ps.xpg.shape[:4] + (4,), order="F")
+    uni[..., 0], uni[..., 1], uni[..., 2], uni[..., 3] = 1.2, 0.3, -0.2, 2.9
+    m1, m2 = frgpu.quad_face_normals(Vp)
+    for precision, tol in (("fp64", 1e-12), ("fp32k", 1e-5)):
+        pp = frgpu.FREuler2DProblem(uni, (0, 1), ps, 1.4, flux=flux, bc="period", precision=precision)
+        pp.set_metric(frgpu.quad_metric(ps.xpl, Vp), m1, m2, frgpu.quad_face_jacobians(ps.xpl, Vp))
+        ip = frgpu.init(pp, dt=1e-4)
+        ip.step(5)
+        assert np.max(np.abs(ip.u - uni)) < tol
+
+
 def _parallelogram(ps, s=0.3, t=-0.2):
     """Metric and unit face normals of the affine mesh x = X + s Y, y = Y + t X:
     iJ = J^-1 with J = [[dx/2, s dy/2], [t dx/2, dy/2]] at every point, x faces

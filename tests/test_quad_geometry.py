@@ -74,3 +74,41 @@ def test_bilinear_jacobian_matches_finite_differences(frgpu, deg):
             ds = (X(rk, sl + h) - X(rk, sl - h)) / (2 * h)
             np.testing.assert_allclose(J[k, l], np.stack([dr, ds], axis=-1), atol=1e-9)
     assert np.ptp(J[..., 0, 0]) > 1e-3   # not constant
+
+
+def test_face_jacobians_follow_the_reference_construction(frgpu, oracle):
+    """FRPSpace2D's Ji (src/struct.jl:145-158): on a parallelogram mesh every
+    face Jacobian is the constant J, and the oracle's residual with the
+    face-Jacobian scaling of dev/cylinder2.jl:147-150 keeps a uniform flow; on a
+    bilinear cell the four face matrices are rs_jacobi at (r_1, 0), (1, r_1),
+    (r_np, 1) and (0, r_np), the points the reference's linear indexing of
+    ri, si selects, the same for every point of a face."""
+    s, t = 0.3, -0.2
+    nx, ny, deg = 5, 4, 3
+    V = _vertices(nx, ny, lambda x, y: (x + s * y, y + t * x))
+    r = frgpu.legendre_point(deg)
+    Ji = frgpu.quad_face_jacobians(r, V)
+    assert Ji.shape == (nx, ny, 4, deg + 1, 2, 2)
+    want = np.array([[0.5 / nx, s * 0.5 / ny], [t * 0.5 / nx, 0.5 / ny]])
+    np.testing.assert_allclose(Ji, np.broadcast_to(want, Ji.shape), atol=1e-15)
+    O = oracle
+    sp = O.Space2D(0, 1, nx, 0, 1, ny, deg)
+    pr = O.Problem(O.EULER2D, sp, gamma=1.4, flux=O.FLUX_HLL)
+    u = np.zeros((nx, ny, deg + 1, deg + 1, 4), order="F")
+    u[..., 0], u[..., 1], u[..., 2], u[..., 3] = 1.2, 0.3, -0.2, 2.9
+    n1, n2 = frgpu.quad_face_normals(V)
+    pr.set_metric(frgpu.quad_metric(r, V), n1, n2, Ji)
+    assert np.max(np.abs(pr.rhs(u))) < 1e-12
+    # a bilinear cell: the evaluation points of the reference
+    B = np.array([[[[0.0, 0.0], [1.0, 0.1], [1.3, 1.2], [-0.1, 0.9]]]])
+    Jb = frgpu.quad_face_jacobians(r, B)[0, 0]
+
+    def J_at(rr, ss):
+        v = B[0, 0]
+        xr = (ss - 1) * v[0] / 4 + (1 - ss) * v[1] / 4 + (ss + 1) * v[2] / 4 - (ss + 1) * v[3] / 4
+        xs = (rr - 1) * v[0] / 4 - (rr + 1) * v[1] / 4 + (rr + 1) * v[2] / 4 + (1 - rr) * v[3] / 4
+        return np.stack([xr, xs], axis=-1)
+
+    for f, (rr, ss) in enumerate([(r[0], 0.0), (1.0, r[0]), (r[-1], 1.0), (0.0, r[-1])]):
+        for k in range(deg + 1):
+            np.testing.assert_allclose(Jb[f, k], J_at(rr, ss), atol=1e-15)
