@@ -600,6 +600,36 @@ def density_wave_entry(args, dist, ws):
 FMA_PEAKS = {}
 
 
+def indicator_entry(steps=50, warmup=5):
+    """The troubled-cell indicators on the shock-vortex workload (400 x 200, p = 3,
+    FP32K): ms per SSPRK3 step (L2 flushed before each) with the learned network
+    fused into the third stage (warp-level mma.sync), with the network as a
+    kernel of its own after the step (tcgen05 tensor cores, TMEM accumulators),
+    and with the plain modal-decay test fused."""
+    import torch
+
+    import frgpu
+    from frgpu import _lib as L
+    from frgpu import learned
+
+    ps = learned.config3_space()
+    net = learned.load_trained()
+    xpg, dx, dy = sv_space_host()
+    dt = host_cfl_dt(shock_vortex_initial(xpg)[0], dx, dy)
+    flush = L2Flush()
+    out = {"workload": WORKLOAD}
+    for name, ind, fuse in (("learned_fused_mma_sync", "mlp", 1), ("learned_separate_tcgen05", "mlp", 0),
+                            ("plain_fused", "plain", 1)):
+        prob, itg = sv_problem(ps, "fp32k", ind, net, dt)
+        prob.set_option(L.OPT_FUSED_INDICATOR, fuse)
+        itg.step(warmup)
+        itg.synchronize()
+        st = torch.cuda.ExternalStream(itg.stream())
+        out[name] = {"ms_per_step": flushed_steps(itg, steps, st, flush) / steps * 1e3}
+        del itg, prob
+    return out
+
+
 def measure_fma_peaks():
     """FP64 / FP32 / FP32-pair FMA throughput of this GPU (frgpu_fma_peak)."""
     import frgpu
@@ -876,7 +906,7 @@ def main():
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the density-wave, ensemble, BGK and triangle entries")
     # profiling aid: run one workload alone (small sizes through --steps / --instances)
-    ap.add_argument("--workload", choices=["density_wave", "ensemble", "bgk", "triangles"], default=None)
+    ap.add_argument("--workload", choices=["density_wave", "ensemble", "bgk", "triangles", "indicator"], default=None)
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--tri-nx", type=int, default=1024, help="triangles: squares per side (2 nx^2 cells)")
     args = ap.parse_args()
@@ -898,6 +928,8 @@ def main():
             r = density_wave_entry(args, None, 1)
         elif args.workload == "ensemble":
             r = ensemble_entry(n=args.instances, t_end=0.5)
+        elif args.workload == "indicator":
+            r = indicator_entry(steps=args.steps, warmup=args.warmup)
         elif args.workload == "triangles":
             # FP32K first, so that a profiler's first residual launch is the FP32K one
             r = tri_entry(nx=args.tri_nx, steps=args.steps, warmup=args.warmup, reps=args.steps,
@@ -920,6 +952,7 @@ def main():
     if not args.no_configs:
         # the other workloads of the spec, each on its own clock (not part of `value`)
         for name, fn in (("density_wave_512x512_p3", lambda: density_wave_entry(args, dist, ws)),
+                         ("indicators_400x200_p3", indicator_entry),
                          ("burgers_ensemble_4096", ensemble_entry), ("bgk_256x512_p3", bgk_entry),
                          ("triangles_advection_2M_cells_p3", tri_entry)):
             try:
