@@ -754,7 +754,7 @@ def tri_entry(nx=1024, steps=20, warmup=3, reps=20, forms=("fp64", "fp32k"), cpu
     """Unstructured triangles: the linear-advection dudt! of
     dev/wave_triangle.jl:44-125 (a = -1) on a periodic triangulated unit square
     of 2 nx^2 right triangles, p = 3 (10 Williams-Shunn-Jameson points per
-    cell, the golden tri_quadrature(3) points), SSPRK3 at dt = 0.05 h.  Timed:
+    cell, tri_quadrature(3)), SSPRK3 at dt = 0.05 h.  Timed:
     `reps` residuals of the device state and `steps` SSPRK3 steps, per form;
     the oracle's residual on all host cores over a 128 x 128 sample beside it."""
     import torch
@@ -764,13 +764,11 @@ def tri_entry(nx=1024, steps=20, warmup=3, reps=20, forms=("fp64", "fp32k"), cpu
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
-    q = np.load(os.path.join(ROOT, "tests", "golden", "tri_quadrature.npz"))
     deg = 3
-    xpl, wp = np.stack([q["r3"], q["s3"]], axis=1), q["w3"]
 
     def space(n):
         pts, cid, key, ct = frgpu.tri_square_mesh(n, n, periodic=True)
-        return frgpu.TriFRPSpace(pts, cid, deg, xpl, wp, key, ct)
+        return frgpu.TriFRPSpace(pts, cid, deg, key=key, cell_type=ct)
 
     sp = space(nx)
     X, Y = sp.xpg[..., 0], sp.xpg[..., 1]

@@ -15,7 +15,9 @@ from .tri import (  # noqa: F401
     tri_operators,
     tri_space_from_gmsh,
     tri_square_mesh,
+    tri_quadrature,
     triface_quadrature,
+    xy_rs,
     vandermonde_tri,
 )
 from .api import (  # noqa: F401

@@ -3,9 +3,8 @@
 ``TriFRPSpace`` mirrors the reference's TriFRPSpace (src/struct.jl:305-352)
 for a mesh given as vertex coordinates and cell vertex ids; its operators come
 from libfrgpu's host setup math (``frgpu_tri_operators``).  The solution
-points are the caller's tri_quadrature(deg) points (src/Quadrature/
-quadrature.jl:14-71; the Williams-Shunn-Jameson sets), as the reference takes
-them.  ``TriAdvectionProblem`` is the linear-advection dudt! of
+points are tri_quadrature(deg) (src/Quadrature/quadrature.jl:14-71; the
+Williams-Shunn-Jameson rules), unless the caller passes its own.  ``TriAdvectionProblem`` is the linear-advection dudt! of
 dev/wave_triangle.jl:44-125 with its explicit time steps, all on the GPU
 through the ``frgpu_tri_*`` entry points.  Meshes come from Gmsh ASCII
 files (``read_gmsh``, the reference's assets/*.msh) or from
@@ -15,6 +14,7 @@ periodic or not).
 from __future__ import annotations
 
 import ctypes as C
+from fractions import Fraction
 
 import numpy as np
 
@@ -24,6 +24,89 @@ from ._lib import check, dptr
 
 def _ip(a):
     return a.ctypes.data_as(L._I)
+
+
+# Williams-Shunn-Jameson rules (D. M. Williams, L. Shunn, A. Jameson, "Symmetric
+# quadrature rules for simplexes based on sphere close packed lattice
+# arrangements", J. Comput. Appl. Math. 266 (2014) 18-38) in barycentric orbits:
+# tri_quadrature(deg) takes the rule with deg + 1 points per edge (the
+# reference's src/Quadrature/williams_shunn_jameson_{2,3,4} schemes).  Each orbit
+# is (kind, weights, parameters...) with one weight and parameter per orbit of
+# that kind.  Degree 1 is the interior three-point rule (a = 1/6) and degree 2
+# the unique symmetric six-point rule of degree 4; degree 3 is the published
+# member of the one-parameter family of symmetric ten-point rules of degree 5,
+# as printed (the points define the discretisation, so they have to be the same).
+_WSJ_ORBITS = {
+    1: (("d3_aa", (Fraction(1, 3),), (Fraction(1, 6),)),),
+    2: (("d3_aa", (0.1099517436553219, 0.2233815896780114), (0.09157621350977073, 0.4459484909159649)),),
+    3: (("centroid", (0.2015429868248577,)),
+        ("d3_aa", (0.04195551878545865,), (0.05556405873493273,)),
+        ("d3_ab", (0.1120984094697944,), (0.2955337173474313,), (0.6342107415763597,))),
+}
+
+
+def _wsj_points(deg: int):
+    """Barycentric points [n, 3] and weights [n] (summing to 1) of the rule for
+    degree deg, orbit by orbit; inside an orbit kind, point-major across its
+    orbits (the reference's expansion order, which fixes the point order)."""
+    if deg not in _WSJ_ORBITS:
+        raise ValueError(f"tri_quadrature is built for degrees {sorted(_WSJ_ORBITS)}, not {deg}")
+    pts, wts = [], []
+    for kind, w, *par in _WSJ_ORBITS[deg]:
+        # object arrays: exact for the Fraction entries, IEEE double for the rest
+        w = np.asarray(w, dtype=object)
+        par = [np.asarray(q, dtype=object) for q in par]
+        if kind == "centroid":
+            orb = [np.full((len(w), 3), Fraction(1, 3), dtype=object)]
+        elif kind == "d3_aa":
+            a = par[0]
+            b = 1 - 2 * a
+            orb = [np.stack(t, axis=1) for t in ((a, a, b), (a, b, a), (b, a, a))]
+        else:  # d3_ab
+            a, b = par
+            c = 1 - a - b
+            orb = [np.stack(t, axis=1) for t in ((a, b, c), (c, a, b), (b, c, a), (b, a, c), (c, b, a), (a, c, b))]
+        for o in orb:
+            pts.append(o)
+            wts.append(w)
+    return np.concatenate(pts).astype(np.float64), np.concatenate(wts).astype(np.float64)
+
+
+def xy_rs(x, y):
+    """xy_rs (src/Geometry/geo_transform.jl:65-73): the equilateral triangle with
+    vertices (-1, -1/sqrt 3), (1, -1/sqrt 3), (0, 2/sqrt 3) -> the reference right
+    triangle (r, s)."""
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    L1 = (np.sqrt(3.0) * y + 1.0) / 3.0
+    L2 = (-3.0 * x - np.sqrt(3.0) * y + 2.0) / 6.0
+    L3 = (3.0 * x - np.sqrt(3.0) * y + 2.0) / 6.0
+    return -L2 + L3 - L1, -L2 - L3 + L1
+
+
+def tri_quadrature(deg: int, vertices=None, transform: bool = True):
+    """tri_quadrature(deg; vertices, transform) (src/Quadrature/quadrature.jl:14-71):
+    the (deg+1)(deg+2)/2 Williams-Shunn-Jameson solution points of a triangle and
+    their weights (summing to 1).  The barycentric points are placed in the
+    triangle with the given vertices (default: the equilateral triangle
+    (-1, -1/sqrt 3), (1, -1/sqrt 3), (0, 2/sqrt 3)) through the trilinear ->
+    Cartesian map (a x p1 + b y p2 + c z p3) / (a x + b y + c z), a, b, c the
+    lengths of the sides opposite p1, p2, p3; with transform the result is mapped
+    to the reference right triangle by xy_rs.  Returns points [n, 2], weights [n].
+    Degrees 1-3, those the triangle residual kernel is built for."""
+    if vertices is None:
+        vertices = ((-1.0, -1 / np.sqrt(3.0)), (1.0, -1 / np.sqrt(3.0)), (0.0, 2 / np.sqrt(3.0)))
+    p1, p2, p3 = (np.asarray(v, dtype=np.float64) for v in vertices)
+    a = np.linalg.norm(p2 - p3)
+    b = np.linalg.norm(p3 - p1)
+    c = np.linalg.norm(p2 - p1)
+    bary, w = _wsj_points(deg)
+    x, y, z = bary[:, 0:1], bary[:, 1:2], bary[:, 2:3]
+    pts = (a * x * p1 + b * y * p2 + c * z * p3) / (a * x + b * y + c * z)
+    if transform:
+        r, s = xy_rs(pts[:, 0], pts[:, 1])
+        pts = np.stack([r, s], axis=1)
+    return pts, w
 
 
 def triface_quadrature(deg: int):
@@ -204,18 +287,21 @@ def _face_neighbours(cellid, key):
 class TriFRPSpace:
     """TriFRPSpace(file, deg) of src/struct.jl:305-352 for a mesh in memory:
     points [npts, 2], cellid [ncell, 3] (0-based, counterclockwise), the
-    solution points xpl[np, 2] and weights wp[np] of tri_quadrature(deg), and
+    solution points xpl[np, 2] and weights wp[np] (default: tri_quadrature(deg)), and
     optionally a vertex key identifying periodic images and the cell types.
     Fields as the reference names them: J, iJ, xpl, wp, xpg, xfl, xfg, wf, V,
     dl (the reference's ∂l), lf, phi (ϕ), and fpn as the three arrays
     nb_cell, nb_face, nb_point [ncell, 3, deg+1] (0-based neighbour_fpidx,
     src/Geometry/geo_neighbor.jl:8-60; nb_cell = -1 on a boundary face)."""
 
-    def __init__(self, points, cellid, deg: int, xpl, wp, key=None, cell_type=None):
+    def __init__(self, points, cellid, deg: int, xpl=None, wp=None, key=None, cell_type=None):
         self.points = np.asarray(points, dtype=np.float64)
         self.cellid = np.asarray(cellid, dtype=np.int64)
         self.deg = deg
         self.np = (deg + 1) * (deg + 2) // 2
+        if xpl is None:
+            xpl, wq = tri_quadrature(deg)
+            wp = wq if wp is None else wp
         self.xpl = np.asarray(xpl, dtype=np.float64)
         self.wp = np.asarray(wp, dtype=np.float64)
         if self.xpl.shape != (self.np, 2):
@@ -247,10 +333,10 @@ class TriFRPSpace:
         self.nb_point = np.where(self.nb_cell >= 0, self.nb_point, -1)
 
 
-def tri_space_from_gmsh(path: str, deg: int, xpl, wp) -> TriFRPSpace:
+def tri_space_from_gmsh(path: str, deg: int, xpl=None, wp=None) -> TriFRPSpace:
     """TriFRPSpace(file, deg) (src/struct.jl:305-352) for a Gmsh ASCII file:
-    its triangles, the tri_quadrature(deg) points xpl and weights wp, and the
-    cells with a boundary face marked type 1."""
+    its triangles, the solution points xpl and weights wp (default:
+    tri_quadrature(deg)), and the cells with a boundary face marked type 1."""
     points, cellid = read_gmsh(path)
     return TriFRPSpace(points, cellid, deg, xpl, wp, cell_type=boundary_cell_type(cellid))
 

@@ -2,7 +2,8 @@
 linear-advection dudt! of dev/wave_triangle.jl:44-125.
 
 CPU: the golden tri_quadrature points (made from the reference's own qpmin.py
-by tests/golden/make_tri_quadrature.py), libfrgpu's host operators against the
+by tests/golden/make_tri_quadrature.py) and the library's tri_quadrature
+against them, libfrgpu's host operators against the
 oracle's restatement, exactness of the operators, the mesh connectivity
 against the reference's coordinate matching (neighbour_fpidx), and the
 oracle's residual (uniform state kept, conservation, convergence order).
@@ -43,6 +44,39 @@ def _wave(sp):
 
 
 # ---------------------------------------------------------------- CPU
+@pytest.mark.parametrize("deg", [1, 2, 3])
+def test_library_tri_quadrature_is_the_golden_rule(frgpu, quad, deg):
+    """frgpu.tri_quadrature(deg), the library's Williams-Shunn-Jameson table
+    expanded by its own symmetry code and mapped by trilinear -> Cartesian ->
+    xy_rs, reproduces the reference's qpmin.py points and weights bit for bit,
+    in the same order; TriFRPSpace takes it by default."""
+    xpl, w = _xpl(quad, deg)
+    p, wl = frgpu.tri_quadrature(deg)
+    np.testing.assert_array_equal(p, xpl)
+    np.testing.assert_array_equal(wl, w)
+    pts, cid, key, ct = frgpu.tri_square_mesh(3, 3, periodic=True)
+    np.testing.assert_array_equal(frgpu.TriFRPSpace(pts, cid, deg, key=key, cell_type=ct).xpl, xpl)
+
+
+def test_tri_quadrature_vertices_and_degrees(frgpu):
+    """Other vertices: the points land inside that triangle with the same
+    barycentric weights (transform=False keeps x, y); degrees the triangle
+    kernel has no instance for are refused."""
+    v = ((0.0, 0.0), (3.0, 0.0), (1.0, 2.0))
+    p, w = frgpu.tri_quadrature(3, vertices=v, transform=False)
+    A = np.array([[v[1][0] - v[0][0], v[2][0] - v[0][0]], [v[1][1] - v[0][1], v[2][1] - v[0][1]]])
+    lam = np.linalg.solve(A, (p - np.asarray(v[0])).T).T
+    assert np.all(lam > 0) and np.all(lam.sum(axis=1) < 1)
+    assert abs(w.sum() - 1) < 1e-15
+    # on the default equilateral triangle the trilinear map is the barycentric one
+    pe, _ = frgpu.tri_quadrature(3, transform=False)
+    r, s = frgpu.xy_rs(pe[:, 0], pe[:, 1])
+    np.testing.assert_array_equal(np.stack([r, s], axis=1), frgpu.tri_quadrature(3)[0])
+    for bad in (0, 4):
+        with pytest.raises(ValueError):
+            frgpu.tri_quadrature(bad)
+
+
 @pytest.mark.parametrize("deg", [1, 2, 3])
 def test_tri_quadrature_golden(quad, deg):
     """The Williams-Shunn-Jameson points of tri_quadrature(deg): (deg+1)(deg+2)/2
