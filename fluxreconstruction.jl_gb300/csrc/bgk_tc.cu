@@ -75,7 +75,8 @@ __device__ __forceinline__ void acc2(float &s, float &e, float x) {
 template <int NP>
 __global__ void __launch_bounds__(32 * MW) k_bgk_moments(const float *__restrict__ uin, const float *__restrict__ din,
                                                         const float *__restrict__ velo, const float *__restrict__ w,
-                                                        int ne, int nv, float *__restrict__ prim, int *status) {
+                                                        int ne, int nv, float *__restrict__ prim, int *status,
+                                                        int closure, double a_adv) {
     const int row = blockIdx.x * MW + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (row >= ne * NP) return; // whole warp
     const size_t base = (size_t)row * nv;
@@ -96,9 +97,10 @@ __global__ void __launch_bounds__(32 * MW) k_bgk_moments(const float *__restrict
         m2 += __shfl_xor_sync(0xffffffffu, m2, off);
     }
     if (lane == 0) {
-        // conserve_prim(w, gamma = 3), 1D: U = m/rho, lambda = rho / (4 (E - m^2 / (2 rho))), E = m2 / 2
-        const double U = m1 / m0;
-        const double lam = 0.25 * m0 / (0.5 * m2 - 0.5 * m1 * U);
+        // closure 0: conserve_prim(w, gamma = 3), 1D: U = m/rho, lambda = rho / (4 (E - m^2 / (2 rho))),
+        // E = m2 / 2; closure 1: prim = [rho, a, 1]
+        const double U = closure ? a_adv : m1 / m0;
+        const double lam = closure ? 1.0 : 0.25 * m0 / (0.5 * m2 - 0.5 * m1 * U);
         prim[3 * row] = (float)m0;
         prim[3 * row + 1] = (float)U;
         prim[3 * row + 2] = (float)lam;
@@ -199,7 +201,8 @@ int launch_tc(frgpu_problem *p, int stage, const void *in, const void *din, void
     const int ne = p->sp.nx, nv = p->d.nvel;
     const float *uin = (const float *)in, *dn = (const float *)din;
     k_bgk_moments<NP><<<(ne * NP + MW - 1) / MW, 32 * MW, 0, p->stream>>>(
-        uin, dn, (const float *)p->d_velo, (const float *)p->d_w, ne, nv, p->d_bgk_prim, p->d_status);
+        uin, dn, (const float *)p->d_velo, (const float *)p->d_w, ne, nv, p->d_bgk_prim, p->d_status, p->bgk_closure,
+        p->d.a);
     FR_CUDA(cudaGetLastError());
     TCArgs a;
     a.ne = ne;

@@ -157,3 +157,224 @@ int fr_enqueue_erk_step(frgpu_problem *p, int (*launch_residual)(frgpu_problem *
     ProblemResidual ctx{p, launch_residual};
     return fr_erk_enqueue_raw(r, problem_residual, &ctx);
 }
+
+// ---------------------------------------------------------------- stabilised steps
+// Three-term recurrence of m stages (ROCK2/ROCK4, RKC) in increment form: with
+// D_0 = 0 and Y_j = u + D_j,
+//   D_j = alpha_j D_{j-1} + beta_j D_{j-2} + dt (mu_j f(Y_{j-1}) + delta_j f(u)),
+// which is Y_j = alpha_j Y_{j-1} + beta_j Y_{j-2} + (1 - alpha_j - beta_j) u +
+// dt (mu_j f(Y_{j-1}) + delta_j f(u)) written for the increments (D_{-1} = 0).
+// Evaluation order: t = mu F; t = fma(delta, F0, t) when delta != 0; t = dt t;
+// t = fma(beta, D_{j-2}, t) when j >= 3 and beta != 0; t = fma(alpha, D_{j-1}, t)
+// when j >= 2 and alpha != 0.  Then an explicit finishing tableau (A, b) of sf
+// stages from g = Y_m: stage input u + fma(dt, acc, D_m) (Y_m when the row of A
+// is zero), and the step u <- u + fma(dt, acc_b, D_m); FP32K adds that
+// increment to the high + low pair with the compensated sum.  FP64 is
+// bit-identical to the oracle's fro_rock.
+namespace {
+
+template <class Real>
+__global__ void __launch_bounds__(256) k_rock_rec(const Real *__restrict__ u, const Real *__restrict__ F,
+                                                  const Real *__restrict__ F0, const Real *__restrict__ d1,
+                                                  const Real *__restrict__ d2, size_t n, Real alpha, Real beta,
+                                                  Real mu, Real delta, const double *dtp, Real *__restrict__ dout,
+                                                  Real *__restrict__ yout) {
+    const Real dt = (Real)*dtp;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        Real t = mu * __ldg(F + q);
+        if (F0) t = frk::fmaR<Real>(delta, __ldg(F0 + q), t);
+        t = dt * t;
+        if (d2) t = frk::fmaR<Real>(beta, __ldg(d2 + q), t);
+        if (d1) t = frk::fmaR<Real>(alpha, __ldg(d1 + q), t);
+        dout[q] = t;
+        yout[q] = __ldg(u + q) + t;
+    }
+}
+
+template <class Real>
+__global__ void __launch_bounds__(256) k_rock_fin(const Real *__restrict__ u, const Real *__restrict__ dm,
+                                                  const Real *__restrict__ k, size_t kstride, size_t n,
+                                                  const Comb<Real> c, const double *dtp, Real *__restrict__ out) {
+    const Real dt = (Real)*dtp;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+        out[q] = __ldg(u + q) + frk::fmaR<Real>(dt, comb_acc<Real>(k, kstride, q, c), __ldg(dm + q));
+}
+
+template <class Real>
+__global__ void __launch_bounds__(256) k_rock_update(Real *__restrict__ u, Real *__restrict__ lo,
+                                                     const Real *__restrict__ dm, const Real *__restrict__ k,
+                                                     size_t kstride, size_t n, const Comb<Real> c,
+                                                     const double *dtp, int *status) {
+    const Real dt = (Real)*dtp;
+    bool bad = false;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const Real t = c.nt ? frk::fmaR<Real>(dt, comb_acc<Real>(k, kstride, q, c), dm[q]) : dm[q];
+        Real v;
+        if (lo == nullptr) {
+            v = u[q] + t;
+        } else {
+            const Real hi = u[q], y = t + lo[q];
+            v = hi + y;
+            lo[q] = y - (v - hi);
+        }
+        u[q] = v;
+        bad |= !isfinite(v);
+    }
+    if (bad) atomicOr(status, frk::ST_NONFINITE);
+}
+
+template <class Real>
+int rock_enqueue_t(const fr_rock_raw &r, int (*residual)(void *, const void *, void *), void *ctx) {
+    const size_t n = r.n;
+    Real *buf = (Real *)r.buf;
+    Real *D[3] = {buf, buf + n, buf + 2 * n};
+    Real *F0 = buf + 3 * n, *F = buf + 4 * n, *Y = buf + 5 * n, *S = buf + 6 * n, *K = buf + 7 * n;
+    Real *u = (Real *)r.u;
+    const int g = grid_for(n);
+    int rc;
+    if ((rc = residual(ctx, u, F0))) return rc;
+    auto Dj = [&](int j) { return D[j % 3]; };
+    for (int j = 1; j <= r.m; ++j) {
+        if (j >= 2 && (rc = residual(ctx, Y, F))) return rc;
+        if (!r.prepare_only) {
+            const double al = r.alpha[j - 1], be = r.beta[j - 1], mu = r.mu[j - 1], de = r.delta[j - 1];
+            k_rock_rec<Real><<<g, 256, 0, r.stream>>>(u, j == 1 ? F0 : F, de != 0.0 ? F0 : nullptr,
+                                                      (j >= 2 && al != 0.0) ? Dj(j - 1) : nullptr,
+                                                      (j >= 3 && be != 0.0) ? Dj(j - 2) : nullptr, n, (Real)al,
+                                                      (Real)be, (Real)mu, (Real)de, r.d_dt, Dj(j), Y);
+            FR_CUDA(cudaGetLastError());
+            *r.launches += 1;
+        }
+    }
+    const Real *Dm = Dj(r.m);
+    for (int i = 0; i < r.sf; ++i) {
+        const double *Ai = &r.A[(size_t)i * r.sf];
+        const Comb<Real> c = comb_of<Real>(Ai, i);
+        const Real *in = Y;
+        if (c.nt > 0) {
+            if (!r.prepare_only) {
+                k_rock_fin<Real><<<g, 256, 0, r.stream>>>(u, Dm, K, n, n, c, r.d_dt, S);
+                FR_CUDA(cudaGetLastError());
+                *r.launches += 1;
+            }
+            in = S;
+        }
+        if ((rc = residual(ctx, in, K + (size_t)i * n))) return rc;
+    }
+    if (r.prepare_only) return FRGPU_OK;
+    const Comb<Real> cb = r.sf > 0 ? comb_of<Real>(r.b, r.sf) : Comb<Real>{};
+    k_rock_update<Real><<<g, 256, 0, r.stream>>>(u, (Real *)r.lo, Dm, K, n, n, cb, r.d_dt, r.d_status);
+    FR_CUDA(cudaGetLastError());
+    *r.launches += 1;
+    return FRGPU_OK;
+}
+
+// ---- nonlinear power method helpers ----
+// out = x + c y (y = null: out = x + c x)
+template <class Real>
+__global__ void __launch_bounds__(256) k_axpy(Real *__restrict__ out, const Real *__restrict__ x,
+                                              const Real *__restrict__ y, double c, size_t n) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const Real yq = y ? y[q] : x[q];
+        out[q] = x[q] + (Real)c * yq;
+    }
+}
+
+// out = x - y
+template <class Real>
+__global__ void __launch_bounds__(256) k_sub(Real *__restrict__ out, const Real *__restrict__ x,
+                                             const Real *__restrict__ y, size_t n) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+        out[q] = x[q] - y[q];
+}
+
+// per-block partial sums of (x - y)^2 (y = null: x^2) in FP64, fixed order
+template <class Real>
+__global__ void __launch_bounds__(256) k_norm2_part(const Real *__restrict__ x, const Real *__restrict__ y, size_t n,
+                                                    double *__restrict__ part) {
+    __shared__ double s[8];
+    double acc = 0.0;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const double d = y ? (double)x[q] - (double)y[q] : (double)x[q];
+        acc = fma(d, d, acc);
+    }
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < 8; ++w) t += s[w];
+        part[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_norm2_final(const double *__restrict__ part, int nb, double *__restrict__ out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double t = 0.0;
+        for (int b = 0; b < nb; ++b) t += part[b];
+        *out = sqrt(t);
+    }
+}
+
+template <class Real> __global__ void __launch_bounds__(256) k_fill(Real *__restrict__ v, double c, size_t n) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+        v[q] = (Real)c;
+}
+
+// flip one component of v about u: v[i] = u[i] - (v[i] - u[i])
+template <class Real> __global__ void k_flip(Real *v, const Real *u, size_t i) { v[i] = u[i] - (v[i] - u[i]); }
+
+} // namespace
+
+int fr_rock_enqueue_raw(const fr_rock_raw &r, int (*residual)(void *, const void *, void *), void *ctx) {
+    return r.f32 ? rock_enqueue_t<float>(r, residual, ctx) : rock_enqueue_t<double>(r, residual, ctx);
+}
+
+int fr_vec_axpy(cudaStream_t st, bool f32, size_t n, void *out, const void *x, const void *y, double c) {
+    if (f32)
+        k_axpy<float><<<grid_for(n), 256, 0, st>>>((float *)out, (const float *)x, (const float *)y, c, n);
+    else
+        k_axpy<double><<<grid_for(n), 256, 0, st>>>((double *)out, (const double *)x, (const double *)y, c, n);
+    FR_CUDA(cudaGetLastError());
+    return FRGPU_OK;
+}
+
+int fr_vec_sub(cudaStream_t st, bool f32, size_t n, void *out, const void *x, const void *y) {
+    if (f32)
+        k_sub<float><<<grid_for(n), 256, 0, st>>>((float *)out, (const float *)x, (const float *)y, n);
+    else
+        k_sub<double><<<grid_for(n), 256, 0, st>>>((double *)out, (const double *)x, (const double *)y, n);
+    FR_CUDA(cudaGetLastError());
+    return FRGPU_OK;
+}
+
+int fr_vec_fill(cudaStream_t st, bool f32, size_t n, void *v, double c) {
+    if (f32)
+        k_fill<float><<<grid_for(n), 256, 0, st>>>((float *)v, c, n);
+    else
+        k_fill<double><<<grid_for(n), 256, 0, st>>>((double *)v, c, n);
+    FR_CUDA(cudaGetLastError());
+    return FRGPU_OK;
+}
+
+int fr_vec_flip(cudaStream_t st, bool f32, void *v, const void *u, size_t i) {
+    if (f32)
+        k_flip<float><<<1, 1, 0, st>>>((float *)v, (const float *)u, i);
+    else
+        k_flip<double><<<1, 1, 0, st>>>((double *)v, (const double *)u, i);
+    FR_CUDA(cudaGetLastError());
+    return FRGPU_OK;
+}
+
+// ||x - y||_2 (y = null: ||x||_2) into *d_out; d_part holds FR_RED_BLOCKS doubles
+int fr_vec_norm2(cudaStream_t st, bool f32, size_t n, const void *x, const void *y, double *d_part, double *d_out) {
+    const int nb = grid_for(n) < FR_RED_BLOCKS ? grid_for(n) : FR_RED_BLOCKS;
+    if (f32)
+        k_norm2_part<float><<<nb, 256, 0, st>>>((const float *)x, (const float *)y, n, d_part);
+    else
+        k_norm2_part<double><<<nb, 256, 0, st>>>((const double *)x, (const double *)y, n, d_part);
+    FR_CUDA(cudaGetLastError());
+    k_norm2_final<<<1, 32, 0, st>>>(d_part, nb, d_out);
+    FR_CUDA(cudaGetLastError());
+    return FRGPU_OK;
+}

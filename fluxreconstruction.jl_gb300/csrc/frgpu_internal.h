@@ -67,6 +67,7 @@ struct frgpu_problem {
     const frgpu_mlp *mlp = nullptr; // learned indicator (borrowed)
     float mlp_thr = 0.5f, mlp_band = 0.0f;
     int bgk_tensor = 1;             // FP32 BGK transport on the tensor cores
+    int bgk_closure = 0;            // BGK Maxwellian: 0 conserve_prim(w, 3), 1 prim = [rho, a, 1]
     int fuse_indicator = 1;         // FP32K 2D: learned indicator inside stage 3
     int fuse_erk = 1;               // 2D Euler: two-stage tableaux fused into the stage kernel
     fr_method meth;                 // coefficients of the fused step
@@ -81,6 +82,21 @@ struct frgpu_problem {
     cudaGraphExec_t erk_gexec = nullptr;
     long erk_launches = 0; // kernels per captured ERK step
     bool erk_dirty = true;
+    const void *erk_hi = nullptr; // the high part the ERK graph updates
+    // stabilised stepping (erk.cu): buffers, captured step graphs per coefficient set
+    void *d_rock = nullptr;
+    size_t rock_cap = 0; // values d_rock holds
+    struct rock_graph {
+        std::vector<double> key;
+        const void *hi; // the high part it updates
+        cudaGraphExec_t gexec;
+        long launches;
+    };
+    std::vector<rock_graph> rock_graphs; // most recently used last
+    // nonlinear power method: direction of the last estimate, work vectors, norm partials
+    void *d_eig = nullptr; // 4 n values: direction, v, f(u), f(v)
+    bool have_eig = false;
+    double *d_eig_red = nullptr; // FR_RED_BLOCKS partials + 1 result
     float *d_bgk_prim = nullptr;    // FP32 BGK: (rho, U, lambda) per (element, point), from the moments
     uint32_t *d_bgk_frag = nullptr; // FP32 BGK: TF32 A fragments of the transport operator (both signs, split)
     // captured step graph
@@ -93,6 +109,8 @@ struct frgpu_problem {
 
 constexpr int FR_NCOUNT = 8, FR_COUNT_LIMITER = 4; // d_count entries
 constexpr int FR_ERK_MAXS = 16;                     // stages of an explicit Runge-Kutta tableau
+constexpr int FR_ROCK_MAXM = 4096;                  // recurrence stages of a stabilised step
+constexpr int FR_ROCK_GRAPHS = 8;                   // stabilised-step graphs kept per problem
 constexpr int FR_RED_BLOCKS = 608; // reduction partial blocks (4 x 152 SMs)
 // d_red layout: [FR_RED_BLOCKS*6 partials][8 final][64 quadrature weights]
 constexpr int FR_RED_FINAL = FR_RED_BLOCKS * 6;
@@ -214,3 +232,27 @@ struct fr_erk_raw {
     long *launches;             // incremented per kernel enqueued
 };
 int fr_erk_enqueue_raw(const fr_erk_raw &r, int (*residual)(void *, const void *, void *), void *ctx);
+// One stabilised step (three-term recurrence + finishing tableau) over raw
+// device buffers (erk.cu).
+struct fr_rock_raw {
+    cudaStream_t stream;
+    int m;                                       // recurrence stages
+    const double *alpha, *beta, *mu, *delta;     // host coefficients [m]
+    int sf;                                      // finishing stages (0: none)
+    const double *A, *b;                         // host finishing tableau, A row-major sf x sf
+    size_t n;                                    // values in the state
+    bool f32;                                    // FP32 state with compensated update into lo
+    void *u, *lo;                                // state (high part) and FP32 low part (null for FP64)
+    char *buf;                                   // (7 + sf) n values: D x 3, F0, F, Y, stage input, k_0..
+    const double *d_dt;
+    int *d_status;
+    bool prepare_only;
+    long *launches;
+};
+int fr_rock_enqueue_raw(const fr_rock_raw &r, int (*residual)(void *, const void *, void *), void *ctx);
+// vector helpers of the nonlinear power method (erk.cu)
+int fr_vec_axpy(cudaStream_t st, bool f32, size_t n, void *out, const void *x, const void *y, double c);
+int fr_vec_sub(cudaStream_t st, bool f32, size_t n, void *out, const void *x, const void *y);
+int fr_vec_fill(cudaStream_t st, bool f32, size_t n, void *v, double c);
+int fr_vec_flip(cudaStream_t st, bool f32, void *v, const void *u, size_t i);
+int fr_vec_norm2(cudaStream_t st, bool f32, size_t n, const void *x, const void *y, double *d_part, double *d_out);

@@ -282,6 +282,12 @@ FRGPU_API void frgpu_space_destroy(frgpu_space *s) { delete s; }
 } // extern "C"
 
 // ------------------------------------------------------------------ problems
+static void drop_rock_graphs(frgpu_problem *p) {
+    for (auto &g : p->rock_graphs)
+        if (g.gexec) cudaGraphExecDestroy(g.gexec);
+    p->rock_graphs.clear();
+}
+
 static void free_problem(frgpu_problem *p) {
     if (!p) return;
     int cur = 0;
@@ -291,9 +297,11 @@ static void free_problem(frgpu_problem *p) {
     for (auto &g : p->gexec)
         if (g) cudaGraphExecDestroy(g);
     if (p->erk_gexec) cudaGraphExecDestroy(p->erk_gexec);
-    void *bufs[] = {p->s0, p->s1, p->s2, p->s3, p->d_dt, p->d_status, p->d_red, p->d_flags, p->d_count,
-                    p->d_velo, p->d_w, p->d_J, p->d_V, p->d_iV, p->rhs_in, p->rhs_out, p->d_bgk_prim,
-                    p->d_bgk_frag, p->d_stage, p->d_erk, p->d_met, p->d_nfx, p->d_nfy, p->d_fsc};
+    drop_rock_graphs(p);
+    void *bufs[] = {p->s0,     p->s1,      p->s2,         p->s3,      p->d_dt,      p->d_status, p->d_red,
+                    p->d_flags, p->d_count, p->d_velo,     p->d_w,     p->d_J,       p->d_V,      p->d_iV,
+                    p->rhs_in, p->rhs_out, p->d_bgk_prim, p->d_bgk_frag, p->d_stage, p->d_erk,   p->d_met,
+                    p->d_nfx,  p->d_nfy,   p->d_fsc,      p->d_rock,  p->d_eig,     p->d_eig_red};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -414,6 +422,7 @@ static int build_erk_graph(frgpu_problem *p) {
     cudaGraphDestroy(g);
     if (ce != cudaSuccess) return fr_cuda_fail(ce, "cudaGraphInstantiate");
     p->erk_dirty = false;
+    p->erk_hi = fr_state_hi(p);
     return FRGPU_OK;
 }
 
@@ -731,6 +740,9 @@ FRGPU_API int frgpu_step_erk(frgpu_problem *p, int s, const double *A, const dou
         p->erk_cap = s;
         p->erk_dirty = true;
     }
+    // the graph updates the high part in place: FP32K SSPRK3 steps in between
+    // may have moved it to the other buffer
+    if (fr_state_hi(p) != p->erk_hi) p->erk_dirty = true;
     if (p->erk_dirty || !p->erk_gexec) {
         int rc = build_erk_graph(p);
         if (rc) return rc;
@@ -739,6 +751,215 @@ FRGPU_API int frgpu_step_erk(frgpu_problem *p, int s, const double *A, const dou
         FR_CUDA(cudaGraphLaunch(p->erk_gexec, p->stream));
         p->launches += p->erk_launches;
     }
+    return check_status(p);
+    FR_CATCH
+}
+
+// ---------------------------------------------------------------- stabilised steps
+static int residual_ctx(void *ctx, const void *in, void *out) { return residual_into((frgpu_problem *)ctx, in, out); }
+
+// One stabilised step (limiter before it, filter after it, as for ERK).
+static int enqueue_rock(frgpu_problem *p, fr_rock_raw r) {
+    int rc;
+    if (p->limiter && (rc = fr_launch_limiter(p, p->lim_w, p->lim_t0))) return rc;
+    r.prepare_only = p->prepare_only;
+    if ((rc = fr_rock_enqueue_raw(r, residual_ctx, p))) return rc;
+    if (p->indicator != FRGPU_IND_NONE) {
+        rc = p->sp.dim == 2 ? fr_launch_filter2d(p, p->indicator, p->lam, p->S0, p->kappa)
+                            : fr_launch_filter1d(p, p->indicator, p->lam, p->S0, p->kappa);
+        if (rc) return rc;
+    }
+    return FRGPU_OK;
+}
+
+FRGPU_API int frgpu_step_rock(frgpu_problem *p, int m, const double *alpha, const double *beta, const double *mu,
+                              const double *delta, int sf, const double *A, const double *b, double dt, int nsteps) {
+    FR_REQ(p && alpha && beta && mu && delta, "step_rock: null coefficient array");
+    FR_REQ(m >= 1 && m <= FR_ROCK_MAXM, "step_rock: need 1 <= recurrence stages <= 4096");
+    FR_REQ(sf >= 0 && sf <= FR_ERK_MAXS, "step_rock: need 0 <= finishing stages <= 16");
+    FR_REQ(sf == 0 || (A && b), "step_rock: null finishing tableau");
+    FR_REQ(nsteps >= 0, "step_rock: negative step count");
+    for (int j = 0; j < m; ++j)
+        FR_REQ(std::isfinite(alpha[j]) && std::isfinite(beta[j]) && std::isfinite(mu[j]) && std::isfinite(delta[j]),
+               "step_rock: recurrence coefficients must be finite");
+    for (int i = 0; i < sf; ++i) {
+        FR_REQ(std::isfinite(b[i]), "step_rock: finishing weights must be finite");
+        for (int j = 0; j < sf; ++j) {
+            FR_REQ(std::isfinite(A[i * sf + j]), "step_rock: finishing tableau must be finite");
+            FR_REQ(j < i || A[i * sf + j] == 0.0, "step_rock: the finishing tableau must be explicit");
+        }
+    }
+    if (!(dt > 0.0) || !std::isfinite(dt)) {
+        fr_set_error("step_rock: dt must be positive and finite");
+        return FRGPU_ERR_DT;
+    }
+    if (nsteps == 0) return FRGPU_OK;
+    FR_TRY
+    if (dt != p->host_dt) {
+        FR_CUDA(cudaMemcpyAsync(p->d_dt, &dt, sizeof(double), cudaMemcpyHostToDevice, p->stream));
+        FR_CUDA(cudaStreamSynchronize(p->stream));
+        p->host_dt = dt;
+    }
+    const size_t need = (size_t)(7 + sf) * p->ndof;
+    if (need > p->rock_cap) {
+        FR_CUDA(cudaStreamSynchronize(p->stream));
+        drop_rock_graphs(p);
+        if (p->d_rock) cudaFree(p->d_rock);
+        p->d_rock = nullptr;
+        p->rock_cap = 0;
+        FR_CUDA(cudaMalloc(&p->d_rock, need * p->esize));
+        p->rock_cap = need;
+    }
+    std::vector<double> key;
+    key.reserve(2 + 4 * (size_t)m + (size_t)sf * (sf + 1));
+    key.push_back(m);
+    key.push_back(sf);
+    for (const double *c : {alpha, beta, mu, delta}) key.insert(key.end(), c, c + m);
+    if (sf) {
+        key.insert(key.end(), A, A + (size_t)sf * sf);
+        key.insert(key.end(), b, b + sf);
+    }
+    const bool f32 = p->d.precision == FRGPU_FP32K;
+    void *hi = fr_state_hi(p);
+    int gi = -1;
+    for (size_t k = 0; k < p->rock_graphs.size(); ++k)
+        if (p->rock_graphs[k].hi == hi && p->rock_graphs[k].key == key) gi = (int)k;
+    if (gi >= 0) { // most recently used last
+        std::rotate(p->rock_graphs.begin() + gi, p->rock_graphs.begin() + gi + 1, p->rock_graphs.end());
+    } else {
+        fr_rock_raw r;
+        r.stream = p->stream;
+        r.m = m;
+        r.alpha = alpha;
+        r.beta = beta;
+        r.mu = mu;
+        r.delta = delta;
+        r.sf = sf;
+        r.A = A;
+        r.b = b;
+        r.n = (size_t)p->ndof;
+        r.f32 = f32;
+        r.u = hi;
+        r.lo = f32 ? p->s3 : nullptr;
+        r.buf = (char *)p->d_rock;
+        r.d_dt = p->d_dt;
+        r.d_status = p->d_status;
+        r.prepare_only = false;
+        r.launches = &p->launches;
+        p->prepare_only = true;
+        int rc = enqueue_rock(p, r);
+        p->prepare_only = false;
+        if (rc) return rc;
+        const long before = p->launches;
+        cudaGraph_t g = nullptr;
+        FR_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+        rc = enqueue_rock(p, r);
+        cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
+        const long nl = p->launches - before;
+        p->launches = before;
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (ce != cudaSuccess) return fr_cuda_fail(ce, "cudaStreamEndCapture");
+        cudaGraphExec_t ge = nullptr;
+        ce = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return fr_cuda_fail(ce, "cudaGraphInstantiate");
+        if ((int)p->rock_graphs.size() >= FR_ROCK_GRAPHS) {
+            FR_CUDA(cudaStreamSynchronize(p->stream));
+            cudaGraphExecDestroy(p->rock_graphs.front().gexec);
+            p->rock_graphs.erase(p->rock_graphs.begin());
+        }
+        p->rock_graphs.push_back({std::move(key), hi, ge, nl});
+    }
+    const frgpu_problem::rock_graph &g = p->rock_graphs.back();
+    for (int it = 0; it < nsteps; ++it) {
+        FR_CUDA(cudaGraphLaunch(g.gexec, p->stream));
+        p->launches += g.launches;
+    }
+    return check_status(p);
+    FR_CATCH
+}
+
+// Nonlinear power method for the spectral radius of the Jacobian of the
+// residual at the current state (the estimate of the RKC code, B. P. Sommeijer,
+// L. F. Shampine, J. G. Verwer, J. Comput. Appl. Math. 88 (1997) 315-326, that
+// the ROCK methods use): v = u + dynrm d / |d|, sigma = |f(v) - f(u)| / dynrm,
+// v <- u + (f(v) - f(u)) dynrm / |f(v) - f(u)| until sigma changes by at most
+// 1 %, rho = 1.2 sigma.  d starts from the previous call's direction, else f(u).
+FRGPU_API int frgpu_spectral_radius(frgpu_problem *p, int maxiter, double *rho, int *iters) {
+    FR_REQ(p && rho, "spectral_radius: null argument");
+    FR_REQ(maxiter >= 1 && maxiter <= 10000, "spectral_radius: need 1 <= maxiter <= 10000");
+    FR_TRY
+    const bool f32 = p->d.precision == FRGPU_FP32K;
+    const size_t n = (size_t)p->ndof, es = p->esize;
+    if (!p->d_eig) {
+        FR_CUDA(cudaMalloc(&p->d_eig, 4 * n * es));
+        FR_CUDA(cudaMalloc((void **)&p->d_eig_red, sizeof(double) * (FR_RED_BLOCKS + 1)));
+        p->have_eig = false;
+    }
+    char *base = (char *)p->d_eig;
+    void *dir = base, *v = base + n * es, *fu = base + 2 * n * es, *fv = base + 3 * n * es;
+    const void *u = fr_state_hi(p);
+    cudaStream_t st = p->stream;
+    int rc;
+    auto norm = [&](const void *x, const void *y, double *out) -> int {
+        int r = fr_vec_norm2(st, f32, n, x, y, p->d_eig_red, p->d_eig_red + FR_RED_BLOCKS);
+        if (r) return r;
+        p->launches += 2;
+        FR_CUDA(cudaMemcpyAsync(out, p->d_eig_red + FR_RED_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, st));
+        FR_CUDA(cudaStreamSynchronize(st));
+        return FRGPU_OK;
+    };
+    const double uround = f32 ? 0x1p-24 : 0x1p-53, sq = std::sqrt(uround);
+    if ((rc = residual_into(p, u, fu))) return rc;
+    const void *d0 = p->have_eig ? dir : fu;
+    double ynrm = 0, vnrm = 0, dynrm;
+    if ((rc = norm(u, nullptr, &ynrm)) || (rc = norm(d0, nullptr, &vnrm))) return rc;
+    if (ynrm != 0.0 && vnrm != 0.0) {
+        dynrm = ynrm * sq;
+        rc = fr_vec_axpy(st, f32, n, v, u, d0, dynrm / vnrm);
+    } else if (ynrm != 0.0) {
+        dynrm = ynrm * sq;
+        rc = fr_vec_axpy(st, f32, n, v, u, nullptr, sq);
+    } else if (vnrm != 0.0) {
+        dynrm = uround;
+        rc = fr_vec_axpy(st, f32, n, v, u, d0, dynrm / vnrm);
+    } else {
+        dynrm = uround;
+        rc = fr_vec_fill(st, f32, n, v, dynrm / std::sqrt((double)n));
+    }
+    if (rc) return rc;
+    p->launches += 1;
+    double sigma = 0.0;
+    int it = 1, converged = 0;
+    for (; it <= maxiter; ++it) {
+        if ((rc = residual_into(p, v, fv))) return rc;
+        double dfnrm = 0.0;
+        if ((rc = norm(fv, fu, &dfnrm))) return rc;
+        const double sigmal = sigma;
+        sigma = dfnrm / dynrm;
+        if (it >= 2 && std::fabs(sigma - sigmal) <= std::max(sigma, 1e-300) * 0.01) {
+            converged = 1;
+            break;
+        }
+        if (it == maxiter) break;
+        if (dfnrm != 0.0) {
+            if ((rc = fr_vec_sub(st, f32, n, fv, fv, fu)) || (rc = fr_vec_axpy(st, f32, n, v, u, fv, dynrm / dfnrm)))
+                return rc;
+            p->launches += 2;
+        } else {
+            if ((rc = fr_vec_flip(st, f32, v, u, (size_t)it % n))) return rc;
+            p->launches += 1;
+        }
+    }
+    if ((rc = fr_vec_sub(st, f32, n, dir, v, u))) return rc;
+    p->launches += 1;
+    FR_CUDA(cudaStreamSynchronize(st));
+    p->have_eig = true;
+    *rho = 1.2 * sigma;
+    if (iters) *iters = converged ? it : -it;
     return check_status(p);
     FR_CATCH
 }
@@ -803,19 +1024,23 @@ FRGPU_API int frgpu_set_filter(frgpu_problem *p, int indicator, double lam, doub
     p->kappa = kappa;
     p->graph_ind = -2; // force a re-capture
     p->erk_dirty = true;
+    drop_rock_graphs(p);
     return FRGPU_OK;
 }
 
 FRGPU_API int frgpu_problem_set_option(frgpu_problem *p, int option, int value) {
     FR_REQ(p, "set_option: null problem");
     FR_REQ(option == FRGPU_OPT_BGK_TENSOR || option == FRGPU_OPT_FUSED_INDICATOR ||
-               option == FRGPU_OPT_FUSED_TWO_STAGE,
+               option == FRGPU_OPT_FUSED_TWO_STAGE || option == FRGPU_OPT_BGK_CLOSURE,
            "set_option: unknown option");
+    FR_REQ(option != FRGPU_OPT_BGK_CLOSURE || value == 0 || value == 1, "set_option: BGK closure is 0 or 1");
     if (option == FRGPU_OPT_BGK_TENSOR) p->bgk_tensor = value != 0;
+    if (option == FRGPU_OPT_BGK_CLOSURE) p->bgk_closure = value;
     if (option == FRGPU_OPT_FUSED_INDICATOR) p->fuse_indicator = value != 0;
     if (option == FRGPU_OPT_FUSED_TWO_STAGE) p->fuse_erk = value != 0;
     p->graph_ind = -2; // force a re-capture
     p->erk_dirty = true;
+    drop_rock_graphs(p);
     return FRGPU_OK;
 }
 
@@ -922,6 +1147,7 @@ FRGPU_API int frgpu_problem_set_metric(frgpu_problem *p, const double *iJ, const
     }
     p->graph_ind = -2; // force a re-capture
     p->erk_dirty = true;
+    drop_rock_graphs(p);
     return FRGPU_OK;
     FR_CATCH
 }
@@ -986,6 +1212,7 @@ FRGPU_API int frgpu_problem_set_face_jacobians(frgpu_problem *p, const double *J
     }
     p->graph_ind = -2; // force a re-capture
     p->erk_dirty = true;
+    drop_rock_graphs(p);
     return FRGPU_OK;
     FR_CATCH
 }
@@ -1004,6 +1231,7 @@ FRGPU_API int frgpu_set_limiter(frgpu_problem *p, int on, const double *weights,
     p->limiter = on != 0;
     p->graph_ind = -2; // force a re-capture
     p->erk_dirty = true;
+    drop_rock_graphs(p);
     return FRGPU_OK;
 }
 
@@ -1016,6 +1244,7 @@ FRGPU_API int frgpu_problem_set_mlp(frgpu_problem *p, const frgpu_mlp *m, double
     p->mlp_band = (float)band;
     p->graph_ind = -2; // the captured step refers to the network: re-capture
     p->erk_dirty = true;
+    drop_rock_graphs(p);
     return FRGPU_OK;
 }
 

@@ -265,6 +265,8 @@ template <class Real, int NP> struct BGKArgs {
     const Real *J;
     const Real *velo, *w;
     Real tau;
+    int closure;  // 0: conserve_prim(w, 3); 1: prim = [rho, a_adv, 1]
+    double a_adv;
     Ops<Real, NP> ops;
     int *status;
 };
@@ -310,9 +312,10 @@ __global__ void __launch_bounds__(NTB) k_bgk1d(const BGKArgs<Real, NP> a) {
             w2 += s_red[k * 3 + 2][wq];
         }
         w2 *= 0.5;
-        // conserve_prim(w, gamma = 3) (1D): lambda = 0.5 rho / (gamma - 1) / (E - m^2 / (2 rho))
-        const double U = w1 / w0;
-        const double lam = 0.5 * w0 / 2.0 / (w2 - 0.5 * w1 * w1 / w0);
+        // closure 0: conserve_prim(w, gamma = 3) (1D): lambda = 0.5 rho / (gamma - 1) / (E - m^2 / (2 rho));
+        // closure 1: prim = [rho, a, 1] (example/advection_kinetic.jl:80-86)
+        const double U = a.closure ? a.a_adv : w1 / w0;
+        const double lam = a.closure ? 1.0 : 0.5 * w0 / 2.0 / (w2 - 0.5 * w1 * w1 / w0);
         s_prim[k][0] = (Real)w0;
         s_prim[k][1] = (Real)U;
         s_prim[k][2] = (Real)lam;
@@ -440,6 +443,8 @@ int launch_bgk_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     a.velo = (const Real *)p->d_velo;
     a.w = (const Real *)p->d_w;
     a.tau = (Real)p->d.tau;
+    a.closure = p->bgk_closure;
+    a.a_adv = p->d.a;
     a.ops = make_ops1<Real, NP>(p->sp);
     a.status = p->d_status;
     k_bgk1d<Real, NP, MODE, STAGE><<<a.ne, NTB, 0, p->stream>>>(a);

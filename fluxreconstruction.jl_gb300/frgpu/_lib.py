@@ -19,7 +19,7 @@ FP64, FP32K = 0, 1
 BC_PERIODIC, BC_COPY, BC_FIXED, BC_DIRICHLET = 0, 1, 2, 3
 RADAU, SD, HUYNH = 0, 1, 2
 IND_NONE, IND_PLAIN, IND_MLP = 0, 1, 2
-OPT_BGK_TENSOR, OPT_FUSED_INDICATOR, OPT_FUSED_TWO_STAGE = 1, 2, 3
+OPT_BGK_TENSOR, OPT_FUSED_INDICATOR, OPT_FUSED_TWO_STAGE, OPT_BGK_CLOSURE = 1, 2, 3, 4
 
 _D = C.POINTER(C.c_double)
 _F = C.POINTER(C.c_float)
@@ -71,6 +71,8 @@ SIGNATURES = {
     "frgpu_troubled_flags": (C.c_int, [_VP, _I, C.c_long]),
     "frgpu_positive_limiter": (C.c_int, [_VP, _D, C.c_double, _I]),
     "frgpu_step_erk": (C.c_int, [_VP, C.c_int, _D, _D, C.c_double, C.c_int]),
+    "frgpu_step_rock": (C.c_int, [_VP, C.c_int, _D, _D, _D, _D, C.c_int, _D, _D, C.c_double, C.c_int]),
+    "frgpu_spectral_radius": (C.c_int, [_VP, C.c_int, _D, _I]),
     "frgpu_problem_set_metric": (C.c_int, [_VP, _D, _D, _D]),
     "frgpu_problem_set_face_jacobians": (C.c_int, [_VP, _D, _D, _D]),
     "frgpu_vandermonde_tri": (C.c_int, [C.c_int, _D, _D, C.c_int, _D, _D, _D]),

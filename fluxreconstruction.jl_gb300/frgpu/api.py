@@ -506,15 +506,24 @@ def FREuler2DProblem(u, tspan, ps: FRPSpace2D, gamma, flux="hll", bc="period", f
     return ODEProblem(ps, d, u, tspan, (ps.nx, ps.ny, n, n, 4))
 
 
-def FRBGKProblem(u, tspan, ps: FRPSpace1D, velo, weights, tau, precision="fp64") -> ODEProblem:
+def FRBGKProblem(u, tspan, ps: FRPSpace1D, velo, weights, tau, precision="fp64", closure="conserve_prim",
+                 a=1.0) -> ODEProblem:
     """The 1D1V BGK ``mol!`` closure of example/bgk_wave.jl:69-129 (kinetic
-    upwind flux, Maxwellian relaxation with time tau, periodic)."""
+    upwind flux, Maxwellian relaxation with time tau, periodic).  With
+    closure="density" the Maxwellian is that of example/advection_kinetic.jl:
+    73-128, prim = [rho, a, 1] from the density alone (the problem that script
+    steps with ROCK4)."""
+    if closure not in ("conserve_prim", "density"):
+        raise ValueError("closure is 'conserve_prim' or 'density'")
     velo = np.ascontiguousarray(velo, dtype=np.float64)
     weights = np.ascontiguousarray(weights, dtype=np.float64)
-    d = _desc(L.BGK1D, flux=L.FLUX_UPWIND, precision=precision, tau=tau)
+    d = _desc(L.BGK1D, flux=L.FLUX_UPWIND, precision=precision, tau=tau, a=a)
     d.nvel = len(velo)
     d.velo, d.weights = dptr(velo), dptr(weights)
-    return ODEProblem(ps, d, u, tspan, (ps.nx, len(velo), ps.np), keep=(velo, weights))
+    prob = ODEProblem(ps, d, u, tspan, (ps.nx, len(velo), ps.np), keep=(velo, weights))
+    if closure == "density":
+        prob.set_option(L.OPT_BGK_CLOSURE, 1)
+    return prob
 
 
 class SSPRK33:
@@ -574,6 +583,102 @@ def Tsit5() -> ExplicitRK:
     return ExplicitRK(a, np.append(a[6, :6], 0.0), "Tsit5")
 
 
+class Stabilized:
+    """A stabilised explicit method: a three-term recurrence of m stages and an
+    explicit finishing tableau, stepped by frgpu_step_rock (the structure of
+    OrdinaryDiffEq's ROCK2/ROCK4, example/advection_kinetic.jl:133-146, and of
+    the Runge-Kutta-Chebyshev methods).  ``coefficients(z)`` maps z = dt * rho,
+    rho the spectral-radius estimate taken before every step (as the ROCK
+    methods do), to (alpha, beta, mu, delta, A, b) of the increment form
+    D_j = alpha_j D_{j-1} + beta_j D_{j-2} + dt (mu_j f(u + D_{j-1}) + delta_j f(u))."""
+
+    def __init__(self, coefficients, name: str = "Stabilized", maxiter: int = 50):
+        self.coefficients = coefficients
+        self.name = name
+        self.maxiter = int(maxiter)
+
+    def __repr__(self):
+        return f"{self.name}()"
+
+
+def rkc2_coefficients(s: int, eps: float = 2 / 13):
+    """Second-order Runge-Kutta-Chebyshev method of s >= 2 stages with damping
+    eps (B. P. Sommeijer, L. F. Shampine, J. G. Verwer, J. Comput. Appl. Math. 88
+    (1997) 315-326): with w0 = 1 + eps/s^2, w1 = T_s'(w0)/T_s''(w0), b_j =
+    T_j''(w0)/T_j'(w0)^2 (b_0 = b_1 = b_2), a_j = 1 - b_j T_j(w0):
+    Y_1 = u + mu~_1 dt f(u), mu~_1 = b_1 w1, and for j >= 2
+    Y_j = (1 - mu_j - nu_j) u + mu_j Y_{j-1} + nu_j Y_{j-2} + mu~_j dt f(Y_{j-1})
+          + gamma~_j dt f(u),
+    mu_j = 2 b_j w0 / b_{j-1}, nu_j = -b_j / b_{j-2}, mu~_j = 2 b_j w1 / b_{j-1},
+    gamma~_j = -a_{j-1} mu~_j.  Returns (alpha, beta, mu, delta) of the increment
+    form and the real stability bound (w0 + 1) T_s''(w0) / T_s'(w0)."""
+    if s < 2:
+        raise ValueError("RKC2 needs s >= 2 stages")
+    w0 = 1.0 + eps / (s * s)
+    T = np.zeros(s + 1)
+    dT = np.zeros(s + 1)
+    d2T = np.zeros(s + 1)
+    T[0], T[1], dT[1] = 1.0, w0, 1.0
+    for j in range(2, s + 1):
+        T[j] = 2 * w0 * T[j - 1] - T[j - 2]
+        dT[j] = 2 * T[j - 1] + 2 * w0 * dT[j - 1] - dT[j - 2]
+        d2T[j] = 4 * dT[j - 1] + 2 * w0 * d2T[j - 1] - d2T[j - 2]
+    w1 = dT[s] / d2T[s]
+    b = np.zeros(s + 1)
+    b[2:] = d2T[2:] / dT[2:] ** 2
+    b[0] = b[1] = b[2]
+    a = 1.0 - b * T
+    alpha, beta, mu, delta = (np.zeros(s) for _ in range(4))
+    mu[0] = b[1] * w1
+    for j in range(2, s + 1):
+        alpha[j - 1] = 2 * b[j] * w0 / b[j - 1]
+        beta[j - 1] = -b[j] / b[j - 2]
+        mu[j - 1] = 2 * b[j] * w1 / b[j - 1]
+        delta[j - 1] = -a[j - 1] * mu[j - 1]
+    return alpha, beta, mu, delta, (w0 + 1) * d2T[s] / dT[s]
+
+
+def RKC2(eps: float = 2 / 13, smax: int = 4096, maxiter: int = 50) -> Stabilized:
+    """RKC2 with the fewest stages s >= 2 whose stability bound covers
+    dt * rho (rho from the power method, which includes the 1.2 safety factor)."""
+    cache = {}
+
+    def coefficients(z):
+        s = 2
+        while True:
+            if s not in cache:
+                cache[s] = rkc2_coefficients(s, eps)
+            if cache[s][4] >= z or s >= smax:
+                break
+            s = max(s + 1, int(s * 1.1))
+        if cache[s][4] < z:
+            raise ValueError(f"dt * rho = {z:.4g} needs more than {smax} RKC2 stages")
+        al, be, mu, de, _ = cache[s]
+        return al, be, mu, de, None, None
+
+    return Stabilized(coefficients, "RKC2", maxiter)
+
+
+def ROCK(select, name: str = "ROCK", maxiter: int = 50) -> Stabilized:
+    """A ROCK2/ROCK4-type method from the caller's tables: ``select(z)`` returns
+    (mu[m], kappa[m], A, b) for z = dt * rho: the recurrence Y_1 = u + dt mu_1 f(u),
+    Y_j = dt mu_j f(Y_{j-1}) + (1 + kappa_j) Y_{j-1} - kappa_j Y_{j-2} (kappa_1
+    unused) and the finishing procedure (A, b) of the chosen degree.  For ROCK4
+    these are OrdinaryDiffEq's tables (the recurrence coefficients recf of the
+    degree chosen for z and its finishing procedure fpa, fpb), which stay with
+    the caller."""
+
+    def coefficients(z):
+        mu, kappa, A, b = select(z)
+        mu = np.asarray(mu, dtype=np.float64)
+        kappa = np.asarray(kappa, dtype=np.float64)
+        alpha, beta = 1.0 + kappa, -kappa
+        alpha[0] = beta[0] = 0.0
+        return alpha, beta, mu, np.zeros_like(mu), A, b
+
+    return Stabilized(coefficients, name, maxiter)
+
+
 class Integrator:
     """Device-resident integrator: ``itg.u`` reads the state back, ``step_(itg)``
     advances one step of ``dt`` on the GPU (OrdinaryDiffEq's init/step! API)."""
@@ -582,7 +687,8 @@ class Integrator:
         self.prob = prob
         self.dt = float(dt)
         self.t = prob.tspan[0]
-        self.alg = alg if isinstance(alg, ExplicitRK) else None
+        self.alg = alg if isinstance(alg, (ExplicitRK, Stabilized)) else None
+        self.stages = []  # stabilised methods: recurrence stages taken per step
         check(L.lib().frgpu_state_upload(prob._h, dptr(prob.u0)))
 
     @property
@@ -611,9 +717,43 @@ class Integrator:
         dt = self.dt if dt is None else float(dt)
         if self.alg is None:
             check(L.lib().frgpu_step_ssprk3(self.prob._h, dt, int(n)))
+        elif isinstance(self.alg, Stabilized):
+            for _ in range(int(n)):
+                rho, _ = self.spectral_radius(self.alg.maxiter)
+                self.step_rock(*self.alg.coefficients(dt * rho), dt=dt)
+                self.t -= dt
         else:
             a = self.alg
             check(L.lib().frgpu_step_erk(self.prob._h, len(a.b), dptr(a.A), dptr(a.b), dt, int(n)))
+        self.t += n * dt
+
+    def spectral_radius(self, maxiter: int = 50):
+        """(rho, iterations) of frgpu_spectral_radius at the current state: the
+        nonlinear power-method estimate of the residual Jacobian's spectral
+        radius, times 1.2; iterations < 0 when it did not settle."""
+        rho = C.c_double(0.0)
+        it = C.c_int(0)
+        check(L.lib().frgpu_spectral_radius(self.prob._h, int(maxiter), C.byref(rho), C.byref(it)))
+        return rho.value, it.value
+
+    def step_rock(self, alpha, beta, mu, delta, A=None, b=None, n: int = 1, dt: float | None = None) -> None:
+        """n stabilised steps with fixed coefficients (frgpu_step_rock)."""
+        dt = self.dt if dt is None else float(dt)
+        co = [np.ascontiguousarray(x, dtype=np.float64) for x in (alpha, beta, mu, delta)]
+        m = len(co[0])
+        if any(len(x) != m for x in co):
+            raise ValueError("alpha, beta, mu, delta need the same length")
+        if b is None:
+            sf, Ap, bp = 0, None, None
+        else:
+            A = np.ascontiguousarray(A, dtype=np.float64)
+            b = np.ascontiguousarray(b, dtype=np.float64)
+            sf = len(b)
+            if A.shape != (sf, sf):
+                raise ValueError("the finishing tableau needs A of shape (len(b), len(b))")
+            Ap, bp = dptr(A), dptr(b)
+        check(L.lib().frgpu_step_rock(self.prob._h, m, *(dptr(x) for x in co), sf, Ap, bp, dt, int(n)))
+        self.stages.append(m)
         self.t += n * dt
 
     def step_async(self, n: int = 1, dt: float | None = None) -> None:
@@ -689,10 +829,12 @@ class Integrator:
 
 def init(prob: ODEProblem, alg=None, *, dt: float, adaptive: bool = False, **kwargs) -> Integrator:
     """init(prob, alg; adaptive=false, dt) (OrdinaryDiffEq): SSPRK33 (default,
-    fused into the residual kernels) or an explicit tableau (Midpoint(), RK4(),
-    Tsit5(), ... or ExplicitRK(A, b))."""
-    if alg is not None and not isinstance(alg, (SSPRK33, ExplicitRK)) and alg is not SSPRK33:
-        raise NotImplementedError("the device integrator implements SSPRK33 and explicit Runge-Kutta tableaux")
+    fused into the residual kernels), an explicit tableau (Midpoint(), RK4(),
+    Tsit5(), ... or ExplicitRK(A, b)) or a stabilised method (RKC2(), or ROCK(...)
+    with the caller's ROCK4 tables)."""
+    if alg is not None and not isinstance(alg, (SSPRK33, ExplicitRK, Stabilized)) and alg is not SSPRK33:
+        raise NotImplementedError("the device integrator implements SSPRK33, explicit Runge-Kutta tableaux and "
+                                  "stabilised (ROCK / RKC) methods")
     if adaptive:
         raise NotImplementedError("fixed time steps only (adaptive=false)")
     return Integrator(prob, dt, alg)

@@ -142,13 +142,18 @@ end
 """The `mol!` closure of example/bgk_wave.jl:69-129 (1D1V BGK, kinetic upwind flux,
 relaxation time τ) on the reference's FRPSpace1D and velocity grid `velo`/`weights`;
 `f[i, v, k]` is the reference's layout.  `precision=:fp32k` runs the transport on the
-tensor cores."""
-function FRBGKProblem(f::AbstractArray{<:Real,3}, tspan, ps, velo, weights, τ; precision=:fp64)
+tensor cores.  `closure=:density` takes the Maxwellian of example/advection_kinetic.jl:73-128,
+prim = [ρ, a, 1] from the density alone."""
+function FRBGKProblem(f::AbstractArray{<:Real,3}, tspan, ps, velo, weights, τ; precision=:fp64,
+                      closure=:conserve_prim, a=1.0)
     v = collect(Float64, velo)
     w = collect(Float64, weights)
     d = ProblemDesc(BGK1D, FLUX[:upwind], PRECISION[precision], ntuple(_ -> BC[:period], 4),
-                    NTuple{16,Cdouble}(zeros(16)), 1.0, 3.0, τ, length(v), pointer(v), pointer(w), 1e-8, 1e-6)
+                    NTuple{16,Cdouble}(zeros(16)), a, 3.0, τ, length(v), pointer(v), pointer(w), 1e-8, 1e-6)
     p = GC.@preserve v w Problem(Space(ps), d, size(f))
+    if closure === :density
+        check(ccall((:frgpu_problem_set_option, libfrgpu), Cint, (Ptr{Cvoid}, Cint, Cint), p.h, 4, 1))
+    end
     return ODEProblem(rhs!, Array{Float64}(f), tspan, p)
 end
 
@@ -250,20 +255,50 @@ function Tsit5()
     return ExplicitRK(A, [A[7, 1:6]; 0.0])
 end
 
+"""A ROCK2/ROCK4-type method stepped by `frgpu_step_rock`: before every step the
+spectral radius ρ of the residual's Jacobian is estimated on the device
+(`frgpu_spectral_radius`) and `select(dt * ρ)` returns `(μ, κ, A, b)`: the recurrence
+Y₁ = u + dt μ₁ f(u), Yⱼ = dt μⱼ f(Yⱼ₋₁) + (1 + κⱼ) Yⱼ₋₁ - κⱼ Yⱼ₋₂ and the finishing
+tableau of the chosen degree.  For ROCK4 (example/advection_kinetic.jl:133-146) `select`
+reads OrdinaryDiffEq's ROCK4 tables (the recurrence coefficients and finishing
+procedure of the degree it chooses for dt ρ)."""
+struct ROCK
+    select::Function
+    maxiter::Int
+end
+ROCK(select) = ROCK(select, 50)
+
 mutable struct Integrator
     p::Problem
     t::Float64
     dt::Float64
-    alg::Union{Nothing,ExplicitRK}
+    alg::Union{Nothing,ExplicitRK,ROCK}
 end
 
 """init(prob, SSPRK33(); dt) or init(prob, Midpoint(); dt): upload u0 once; the state
 stays on the device."""
-function init(prob::ODEProblem, alg::Union{SSPRK33,ExplicitRK}; dt, adaptive=false, kwargs...)
+function init(prob::ODEProblem, alg::Union{SSPRK33,ExplicitRK,ROCK}; dt, adaptive=false, kwargs...)
     adaptive && error("FRGPU integrates with fixed dt")
     p = prob.p::Problem
     check(ccall((:frgpu_state_upload, libfrgpu), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), p.h, Array{Float64}(prob.u0)))
-    return Integrator(p, prob.tspan[1], dt, alg isa ExplicitRK ? alg : nothing)
+    return Integrator(p, prob.tspan[1], dt, alg isa SSPRK33 ? nothing : alg)
+end
+
+function rock_step!(itg::Integrator, a::ROCK)
+    ρ = Ref{Cdouble}(0)
+    iters = Ref{Cint}(0)
+    check(ccall((:frgpu_spectral_radius, libfrgpu), Cint, (Ptr{Cvoid}, Cint, Ref{Cdouble}, Ref{Cint}),
+                itg.p.h, a.maxiter, ρ, iters))
+    μ, κ, A, b = a.select(itg.dt * ρ[])
+    m = length(μ)
+    α = [0.0; 1.0 .+ κ[2:end]]
+    β = [0.0; -κ[2:end]]
+    δ = zeros(m)
+    Ar = Matrix{Float64}(permutedims(A))   # row-major for the C ABI
+    check(ccall((:frgpu_step_rock, libfrgpu), Cint,
+                (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Cint, Ptr{Cdouble},
+                 Ptr{Cdouble}, Cdouble, Cint),
+                itg.p.h, m, α, β, collect(Float64, μ), δ, length(b), Ar, collect(Float64, b), itg.dt, 1))
 end
 
 """step!(itg): one SSPRK3 step on the device (a captured CUDA graph)."""
@@ -271,6 +306,10 @@ function step!(itg::Integrator, n::Integer=1)
     a = getfield(itg, :alg)
     if a === nothing
         check(ccall((:frgpu_step_ssprk3, libfrgpu), Cint, (Ptr{Cvoid}, Cdouble, Cint), itg.p.h, itg.dt, n))
+    elseif a isa ROCK
+        for _ in 1:n
+            rock_step!(itg, a)
+        end
     else
         A = Matrix{Float64}(permutedims(a.A))   # row-major for the C ABI
         check(ccall((:frgpu_step_erk, libfrgpu), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Cdouble, Cint),

@@ -58,7 +58,12 @@ enum frgpu_bc {
 };
 enum frgpu_correction { FRGPU_RADAU = 0, FRGPU_SD = 1, FRGPU_HUYNH = 2 };
 enum frgpu_indicator { FRGPU_IND_NONE = 0, FRGPU_IND_PLAIN = 1, FRGPU_IND_MLP = 2 };
-enum frgpu_option { FRGPU_OPT_BGK_TENSOR = 1, FRGPU_OPT_FUSED_INDICATOR = 2, FRGPU_OPT_FUSED_TWO_STAGE = 3 };
+enum frgpu_option {
+    FRGPU_OPT_BGK_TENSOR = 1,
+    FRGPU_OPT_FUSED_INDICATOR = 2,
+    FRGPU_OPT_FUSED_TWO_STAGE = 3,
+    FRGPU_OPT_BGK_CLOSURE = 4
+};
 
 typedef struct frgpu_space frgpu_space;
 typedef struct frgpu_problem frgpu_problem;
@@ -163,6 +168,34 @@ FRGPU_API int frgpu_step_ssprk3_async(frgpu_problem *p, double dt, int nsteps);
  * filter configured for the problem run before and after every step, as with
  * frgpu_step_ssprk3.  Steps are replayed from a captured CUDA graph. */
 FRGPU_API int frgpu_step_erk(frgpu_problem *p, int s, const double *A, const double *b, double dt, int nsteps);
+/* nsteps of a stabilised explicit method: a three-term recurrence of m stages
+ * followed by an explicit finishing tableau (the structure of OrdinaryDiffEq's
+ * ROCK2 / ROCK4, as example/advection_kinetic.jl:133-146 steps with ROCK4 at
+ * fixed dt, and of the Runge-Kutta-Chebyshev methods).  With D_0 = 0 and
+ * Y_j = u + D_j,
+ *   D_j = alpha_j D_{j-1} + beta_j D_{j-2} + dt (mu_j f(Y_{j-1}) + delta_j f(u)),
+ * j = 1..m (D_{-1} = 0), which is the recurrence
+ *   Y_j = alpha_j Y_{j-1} + beta_j Y_{j-2} + (1 - alpha_j - beta_j) u
+ *         + dt (mu_j f(Y_{j-1}) + delta_j f(u))
+ * in increments.  ROCK4's stages are alpha_j = 1 + kappa_j, beta_j = -kappa_j,
+ * delta_j = 0 with its (mu_j, kappa_j) (alpha_1 = beta_1 = 0); RKC's are its
+ * (mu_j, nu_j, mu~_j, gamma~_j) as (alpha, beta, mu, delta).  Then sf finishing
+ * stages (sf = 0: none) k_i = f(Y_m + dt sum_{l<i} a_il k_l), and
+ * u <- u + D_m + dt sum_i b_i k_i.  The coefficient arrays have m entries; A is
+ * sf x sf row-major, strictly lower triangular; m <= 4096, sf <= 16.  The
+ * caller chooses m and the coefficients for dt times the spectral radius
+ * (frgpu_spectral_radius); ROCK4's tables stay with the caller (OrdinaryDiffEq
+ * holds them).  The limiter and filter run around every step as with
+ * frgpu_step_erk; steps replay captured graphs (the last 8 coefficient sets). */
+FRGPU_API int frgpu_step_rock(frgpu_problem *p, int m, const double *alpha, const double *beta, const double *mu,
+                              const double *delta, int sf, const double *A, const double *b, double dt, int nsteps);
+/* Spectral radius of the Jacobian of the residual at the current state, by the
+ * nonlinear power method of the RKC code (the eigenvalue estimate the ROCK
+ * methods take each step): at most maxiter residual evaluations, stopping when
+ * the estimate changes by at most 1 %; rho = 1.2 x the estimate.  The direction
+ * is kept for the next call.  iters receives the iterations used (negative when
+ * the estimate did not settle within maxiter; rho is then the last estimate). */
+FRGPU_API int frgpu_spectral_radius(frgpu_problem *p, int maxiter, double *rho, int *iters);
 /* dt = cfl / max over points of sum_d (|u_d| + c)/dx_d (FP64 max-reduction on the GPU);
  * with a per-point metric (frgpu_problem_set_metric) the rate at a point is
  * (lambda_r + lambda_s)/2 with the contravariant speeds lambda_r = |a11 u + a12 v|
@@ -229,6 +262,11 @@ FRGPU_API int frgpu_troubled_flags(frgpu_problem *p, int *flags, long n);
  * FRGPU_OPT_FUSED_TWO_STAGE: 1 (default) runs two-stage tableaux of
  * frgpu_step_erk (Midpoint, Heun, ...) on a 2D Euler problem fused into the
  * stage kernel, 0 through the generic residual + combination kernels.
+ * FRGPU_OPT_BGK_CLOSURE: the Maxwellian of a BGK problem.  0 (default): from
+ * the moments through conserve_prim(w, 3) (example/bgk_wave.jl:76-81); 1: the
+ * density-only closure prim = [rho, a, 1], M = rho sqrt(1/pi) exp(-(v - a)^2),
+ * a the problem's advection speed (example/advection_kinetic.jl:80-87, the
+ * problem that script steps with ROCK4).
  * The next step re-captures its graph. */
 FRGPU_API int frgpu_problem_set_option(frgpu_problem *p, int option, int value);
 /* Device pointer to the primary state array and its element type size

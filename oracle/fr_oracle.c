@@ -837,9 +837,11 @@ static void rhs_bgk1d(const fro_cfg *c, double *du, const double *u) {
                 w2 += c->weights[v] * (c->velo[v] * c->velo[v]) * x;
             }
             w2 *= 0.5;
-            /* conserve_prim(w, gamma = 3): lambda = 0.5 rho / (gamma-1) / (E - 0.5 m^2/rho) */
-            double rho = w0, U = w1 / w0;
-            double lam = 0.5 * w0 / (3.0 - 1.0) / (w2 - 0.5 * w1 * w1 / w0);
+            /* conserve_prim(w, gamma = 3): lambda = 0.5 rho / (gamma-1) / (E - 0.5 m^2/rho);
+             * closure 1, example/advection_kinetic.jl:80-86: rho = sum(u .* weights),
+             * prim = [rho, a, 1] */
+            double rho = w0, U = c->bgk_closure ? c->a : w1 / w0;
+            double lam = c->bgk_closure ? 1.0 : 0.5 * w0 / (3.0 - 1.0) / (w2 - 0.5 * w1 * w1 / w0);
             for (int v = 0; v < nv; ++v) {
                 double dv = c->velo[v] - U;
                 M[v + nv * k] = rho * sqrt(lam / M_PI) * exp(-lam * dv * dv);
@@ -948,6 +950,127 @@ void fro_erk(const fro_cfg *c, double *u, double dt, int nsteps, int s, const do
         if (!first)
             for (long q = 0; q < n; ++q) u[q] = fma(dt, st[q], u[q]);
     }
+}
+
+/* Stabilised step (the recurrence + finishing structure of OrdinaryDiffEq's
+ * ROCK2/ROCK4 and of RKC, as example/advection_kinetic.jl:133-146 steps with
+ * ROCK4), restated in increment form: D_0 = 0, Y_j = u + D_j,
+ *   D_j = alpha_j D_{j-1} + beta_j D_{j-2} + dt (mu_j f(Y_{j-1}) + delta_j f(u)),
+ * with the operations in this order: t = mu F; t = fma(delta, F0, t) if
+ * delta != 0; t = dt t; t = fma(beta, D_{j-2}, t) if j >= 3 and beta != 0;
+ * t = fma(alpha, D_{j-1}, t) if j >= 2 and alpha != 0.  Finishing stages from
+ * Y_m: input u + fma(dt, acc, D_m) (Y_m for a zero row), the step
+ * u + fma(dt, acc_b, D_m) (u + D_m without weights).  acc is the chain of erk
+ * (first nonzero term a k, then fma).  work: (7 + sf) * ndof doubles. */
+void fro_rock(const fro_cfg *c, double *u, double dt, int nsteps, int m, const double *alpha, const double *beta,
+              const double *mu, const double *delta, int sf, const double *A, const double *b, double *work) {
+    long n = fro_ndof(c);
+    double *D[3] = {work, work + n, work + 2 * n};
+    double *F0 = work + 3 * n, *F = work + 4 * n, *Y = work + 5 * n, *S = work + 6 * n, *K = work + 7 * n;
+    for (int it = 0; it < nsteps; ++it) {
+        fro_rhs(c, F0, u);
+        for (int j = 1; j <= m; ++j) {
+            if (j >= 2) fro_rhs(c, F, Y);
+            const double *Fj = j == 1 ? F0 : F;
+            const double al = alpha[j - 1], be = beta[j - 1], mj = mu[j - 1], de = delta[j - 1];
+            double *Dj = D[j % 3];
+            const double *D1 = D[(j - 1) % 3], *D2 = D[(j + 1) % 3];
+            for (long q = 0; q < n; ++q) {
+                double t = mj * Fj[q];
+                if (de != 0.0) t = fma(de, F0[q], t);
+                t = dt * t;
+                if (j >= 3 && be != 0.0) t = fma(be, D2[q], t);
+                if (j >= 2 && al != 0.0) t = fma(al, D1[q], t);
+                Dj[q] = t;
+                Y[q] = u[q] + t;
+            }
+        }
+        const double *Dm = D[m % 3];
+        for (int i = 0; i < sf; ++i) {
+            int first = 1;
+            for (int l = 0; l < i; ++l) {
+                const double a = A[i * sf + l];
+                if (a == 0.0) continue;
+                for (long q = 0; q < n; ++q) S[q] = first ? a * K[l * n + q] : fma(a, K[l * n + q], S[q]);
+                first = 0;
+            }
+            if (first)
+                fro_rhs(c, K + i * n, Y);
+            else {
+                for (long q = 0; q < n; ++q) S[q] = u[q] + fma(dt, S[q], Dm[q]);
+                fro_rhs(c, K + i * n, S);
+            }
+        }
+        int first = 1;
+        for (int i = 0; i < sf; ++i) {
+            if (b[i] == 0.0) continue;
+            for (long q = 0; q < n; ++q) S[q] = first ? b[i] * K[i * n + q] : fma(b[i], K[i * n + q], S[q]);
+            first = 0;
+        }
+        for (long q = 0; q < n; ++q) u[q] = u[q] + (first ? Dm[q] : fma(dt, S[q], Dm[q]));
+    }
+}
+
+static double norm2_diff(const double *x, const double *y, long n) {
+    double t = 0.0;
+    for (long q = 0; q < n; ++q) {
+        double d = y ? x[q] - y[q] : x[q];
+        t = fma(d, d, t);
+    }
+    return sqrt(t);
+}
+
+/* Nonlinear power method of the RKC code (Sommeijer, Shampine, Verwer, J.
+ * Comput. Appl. Math. 88 (1997) 315-326), the spectral-radius estimate of the
+ * ROCK methods: v = u + dynrm d/|d| (dynrm = |u| sqrt(eps)), sigma =
+ * |f(v) - f(u)| / dynrm, v <- u + (f(v) - f(u)) dynrm / |f(v) - f(u)| until
+ * sigma changes by at most 1 %; rho = 1.2 sigma.  dir (ndof) holds the start
+ * direction when *have is set and receives v - u; work: 3 * ndof doubles.
+ * Returns the iterations used (negative when not settled). */
+int fro_spectral_radius(const fro_cfg *c, const double *u, int maxiter, double *dir, int *have, double *rho,
+                        double *work) {
+    long n = fro_ndof(c);
+    double *v = work, *fu = work + n, *fv = work + 2 * n;
+    const double uround = 0x1p-53, sq = sqrt(uround);
+    fro_rhs(c, fu, u);
+    const double *d0 = *have ? dir : fu;
+    double ynrm = norm2_diff(u, NULL, n), vnrm = norm2_diff(d0, NULL, n), dynrm;
+    if (ynrm != 0.0 && vnrm != 0.0) {
+        dynrm = ynrm * sq;
+        for (long q = 0; q < n; ++q) v[q] = u[q] + (dynrm / vnrm) * d0[q];
+    } else if (ynrm != 0.0) {
+        dynrm = ynrm * sq;
+        for (long q = 0; q < n; ++q) v[q] = u[q] + sq * u[q];
+    } else if (vnrm != 0.0) {
+        dynrm = uround;
+        for (long q = 0; q < n; ++q) v[q] = u[q] + (dynrm / vnrm) * d0[q];
+    } else {
+        dynrm = uround;
+        for (long q = 0; q < n; ++q) v[q] = dynrm / sqrt((double)n);
+    }
+    double sigma = 0.0;
+    int it = 1, converged = 0;
+    for (; it <= maxiter; ++it) {
+        fro_rhs(c, fv, v);
+        double dfnrm = norm2_diff(fv, fu, n);
+        double sigmal = sigma;
+        sigma = dfnrm / dynrm;
+        if (it >= 2 && fabs(sigma - sigmal) <= fmax(sigma, 1e-300) * 0.01) {
+            converged = 1;
+            break;
+        }
+        if (it == maxiter) break;
+        if (dfnrm != 0.0) {
+            for (long q = 0; q < n; ++q) v[q] = u[q] + (dynrm / dfnrm) * (fv[q] - fu[q]);
+        } else {
+            long i = it % n;
+            v[i] = u[i] - (v[i] - u[i]);
+        }
+    }
+    for (long q = 0; q < n; ++q) dir[q] = v[q] - u[q];
+    *have = 1;
+    *rho = 1.2 * sigma;
+    return converged ? it : -it;
 }
 
 /* ------------------------------------------------------------------------

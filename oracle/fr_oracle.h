@@ -76,6 +76,8 @@ typedef struct {
     const double *Ji;          /* 2D with iJ and normals: face Jacobians [nx, ny, 4, np, 2, 2]
                                   (FRPSpace2D's Ji, src/struct.jl:145-158) for the interface-flux
                                   scales of dev/cylinder2.jl:147-150, or NULL */
+    int bgk_closure;           /* BGK Maxwellian: 0 conserve_prim(w, 3) (bgk_wave.jl),
+                                  1 prim = [rho, a, 1] (advection_kinetic.jl) */
 } fro_cfg;
 
 long fro_ndof(const fro_cfg *c);
@@ -89,6 +91,16 @@ void fro_ssprk3_filtered(const fro_cfg *c, double *u, double dt, int nsteps, dou
  * work must hold (s + 1) * ndof doubles */
 void fro_erk(const fro_cfg *c, double *u, double dt, int nsteps, int s, const double *A, const double *b,
              double *work);
+
+/* stabilised step: m-stage three-term recurrence in increment form + explicit
+ * finishing tableau (sf stages); work must hold (7 + sf) * ndof doubles */
+void fro_rock(const fro_cfg *c, double *u, double dt, int nsteps, int m, const double *alpha, const double *beta,
+              const double *mu, const double *delta, int sf, const double *A, const double *b, double *work);
+/* spectral radius of the residual's Jacobian by the nonlinear power method;
+ * dir (ndof) in/out, work 3 * ndof doubles; returns iterations (negative when
+ * not settled) */
+int fro_spectral_radius(const fro_cfg *c, const double *u, int maxiter, double *dir, int *have, double *rho,
+                        double *work);
 
 /* ---- troubled-cell indicator and modal filter ---- */
 /* 2D, per step: detect on rho with iV (np^2 x np^2), filter all 4 variables

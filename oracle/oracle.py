@@ -51,6 +51,7 @@ class Cfg(C.Structure):
         ("ll", _D), ("lr", _D), ("lpdm", _D), ("dgl", _D), ("dgr", _D),
         ("velo", _D), ("weights", _D),
         ("iJ", _D), ("n1", _D), ("n2", _D), ("Ji", _D),
+        ("bgk_closure", C.c_int),
     ]
 
 
@@ -86,6 +87,9 @@ def lib():
             "fro_rhs": (None, [C.POINTER(Cfg), _D, _D]),
             "fro_ssprk3": (None, [C.POINTER(Cfg), _D, C.c_double, C.c_int, _D]),
             "fro_erk": (None, [C.POINTER(Cfg), _D, C.c_double, C.c_int, C.c_int, _D, _D, _D]),
+            "fro_rock": (None, [C.POINTER(Cfg), _D, C.c_double, C.c_int, C.c_int, _D, _D, _D, _D, C.c_int, _D, _D,
+                                _D]),
+            "fro_spectral_radius": (C.c_int, [C.POINTER(Cfg), _D, C.c_int, _D, C.POINTER(C.c_int), _D, _D]),
             "fro_ssprk3_filtered": (None, [C.POINTER(Cfg), _D, C.c_double, C.c_int, _D, _D, _D, C.c_double,
                                            C.c_double, C.c_double]),
             "fro_filter2d": (C.c_int, [C.POINTER(Cfg), _D, _D, _D, C.c_double, C.c_double,
@@ -268,9 +272,10 @@ class Problem:
 
     def __init__(self, kind, space, *, flux=FLUX_ROE, a=1.0, gamma=1.4, tau=1e-2, bc=BC_PERIODIC,
                  bcs=None, fixed_states=None, velo=None, weights=None, eps_interior=1e-8,
-                 eps_periodic=1e-6):
+                 eps_periodic=1e-6, bgk_closure=0):
         c = Cfg()
         c.kind, c.flux = kind, flux
+        c.bgk_closure = bgk_closure
         c.nx = space.nx
         c.ny = getattr(space, "ny", 1)
         c.np = space.np
@@ -367,6 +372,32 @@ class Problem:
         work = np.zeros((s + 1) * uf.size)
         lib().fro_erk(C.byref(self.cfg), uf.ctypes.data_as(_D), float(dt), int(nsteps), s, _p(A), _p(b), _p(work))
         return uf
+
+    def rock(self, u: np.ndarray, dt: float, nsteps: int, alpha, beta, mu, delta, A=None, b=None) -> np.ndarray:
+        """Stabilised step: the m-stage recurrence (alpha, beta, mu, delta) in
+        increment form and the finishing tableau (A, b) (fro_rock)."""
+        uf = np.array(u, dtype=np.float64, order="F", copy=True)
+        co = [np.ascontiguousarray(x, dtype=np.float64) for x in (alpha, beta, mu, delta)]
+        m = len(co[0])
+        A = np.zeros((0, 0)) if A is None else np.ascontiguousarray(A, dtype=np.float64)
+        b = np.zeros(0) if b is None else np.ascontiguousarray(b, dtype=np.float64)
+        sf = len(b)
+        work = np.zeros((7 + sf) * uf.size)
+        lib().fro_rock(C.byref(self.cfg), uf.ctypes.data_as(_D), float(dt), int(nsteps), m, *(_p(x) for x in co), sf,
+                       _p(A) if sf else None, _p(b) if sf else None, _p(work))
+        return uf
+
+    def spectral_radius(self, u: np.ndarray, maxiter: int = 50, direction=None):
+        """Nonlinear power-method estimate (fro_spectral_radius): returns
+        (rho, iterations, direction); pass direction back to start from it."""
+        uf = np.array(u, dtype=np.float64, order="F", copy=True)
+        have = C.c_int(0 if direction is None else 1)
+        d = np.zeros(uf.size) if direction is None else np.array(direction, dtype=np.float64, copy=True)
+        rho = C.c_double(0.0)
+        work = np.zeros(3 * uf.size)
+        it = lib().fro_spectral_radius(C.byref(self.cfg), uf.ctypes.data_as(_D), int(maxiter), _p(d), C.byref(have),
+                                       C.byref(rho), _p(work))
+        return rho.value, it, d
 
     def filter2d(self, u: np.ndarray, lam: float, S0: float, kappa: float):
         uf = np.array(u, dtype=np.float64, order="F", copy=True)
