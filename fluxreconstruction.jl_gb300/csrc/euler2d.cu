@@ -153,6 +153,7 @@ __global__ void __launch_bounds__(192) k_reduce_final(const double *__restrict__
 } // namespace
 
 int fr_launch_euler2d(frgpu_problem *p, int stage, const void *in, const void *din, void *out) {
+    if (p->d.flux == FRGPU_FLUX_CENTRAL) return fr_launch_central2d(p, stage, in, out);
     if (p->d_met) {
         if (p->d.precision == FRGPU_FP64) return fr_euler2d_met_fp64(p, stage, in, din, out);
         return fr_euler2d_met_fp32k(p, stage, in, din, out);

@@ -68,6 +68,9 @@ struct frgpu_problem {
     float mlp_thr = 0.5f, mlp_band = 0.0f;
     int bgk_tensor = 1;             // FP32 BGK transport on the tensor cores
     int bgk_closure = 0;            // BGK Maxwellian: 0 conserve_prim(w, 3), 1 prim = [rho, a, 1]
+    double flux_c = 0.0;            // FRGPU_FLUX_CENTRAL dissipation coefficient
+    void *d_c2 = nullptr;           // FRGPU_FLUX_CENTRAL work: transformed fluxes and face traces
+    size_t c2_cap = 0;              // values d_c2 holds
     int fuse_indicator = 1;         // FP32K 2D: learned indicator inside stage 3
     int fuse_erk = 1;               // 2D Euler: two-stage tableaux fused into the stage kernel
     fr_method meth;                 // coefficients of the fused step
@@ -251,6 +254,8 @@ struct fr_rock_raw {
 };
 int fr_rock_enqueue_raw(const fr_rock_raw &r, int (*residual)(void *, const void *, void *), void *ctx);
 // vector helpers of the nonlinear power method (erk.cu)
+// residual of a FRGPU_FLUX_CENTRAL 2D problem (central2d.cu)
+int fr_launch_central2d(frgpu_problem *p, int stage, const void *in, void *out);
 int fr_vec_axpy(cudaStream_t st, bool f32, size_t n, void *out, const void *x, const void *y, double c);
 int fr_vec_sub(cudaStream_t st, bool f32, size_t n, void *out, const void *x, const void *y);
 int fr_vec_fill(cudaStream_t st, bool f32, size_t n, void *v, double c);

@@ -301,7 +301,7 @@ static void free_problem(frgpu_problem *p) {
     void *bufs[] = {p->s0,     p->s1,      p->s2,         p->s3,      p->d_dt,      p->d_status, p->d_red,
                     p->d_flags, p->d_count, p->d_velo,     p->d_w,     p->d_J,       p->d_V,      p->d_iV,
                     p->rhs_in, p->rhs_out, p->d_bgk_prim, p->d_bgk_frag, p->d_stage, p->d_erk,   p->d_met,
-                    p->d_nfx,  p->d_nfy,   p->d_fsc,      p->d_rock,  p->d_eig,     p->d_eig_red};
+                    p->d_nfx,  p->d_nfy,   p->d_fsc,      p->d_rock,  p->d_eig,     p->d_eig_red, p->d_c2};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -486,9 +486,18 @@ FRGPU_API int frgpu_problem_create(const frgpu_space *s, const frgpu_problem_des
     if (eq == FRGPU_BGK1D)
         FR_REQ(d->nvel >= 1 && d->velo && d->weights && d->tau > 0, "problem_create: BGK needs nvel, velo, weights, tau");
     if (eq == FRGPU_EULER2D) {
-        for (int side = 0; side < 4; ++side)
-            FR_REQ(d->bc[side] == FRGPU_BC_PERIODIC || d->bc[side] == FRGPU_BC_COPY || d->bc[side] == FRGPU_BC_FIXED,
-                   "problem_create: 2D boundaries are periodic, copy or fixed");
+        FR_REQ(d->flux == FRGPU_FLUX_LF || d->flux == FRGPU_FLUX_HLL || d->flux == FRGPU_FLUX_CENTRAL,
+               "problem_create: 2D Euler fluxes are LF, HLL or central");
+        if (d->flux == FRGPU_FLUX_CENTRAL) {
+            for (int side = 0; side < 4; ++side)
+                FR_REQ(d->bc[side] == FRGPU_BC_PERIODIC || d->bc[side] == FRGPU_BC_DIRICHLET,
+                       "problem_create: with the central flux the boundaries are periodic or Dirichlet");
+        } else {
+            for (int side = 0; side < 4; ++side)
+                FR_REQ(d->bc[side] == FRGPU_BC_PERIODIC || d->bc[side] == FRGPU_BC_COPY ||
+                           d->bc[side] == FRGPU_BC_FIXED,
+                       "problem_create: 2D boundaries are periodic, copy or fixed");
+        }
         FR_REQ((d->bc[0] == FRGPU_BC_PERIODIC) == (d->bc[1] == FRGPU_BC_PERIODIC) &&
                    (d->bc[2] == FRGPU_BC_PERIODIC) == (d->bc[3] == FRGPU_BC_PERIODIC),
                "problem_create: periodic boundaries come in pairs");
@@ -705,7 +714,8 @@ FRGPU_API int frgpu_step_erk(frgpu_problem *p, int s, const double *A, const dou
     FR_TRY
     // two-stage methods on the 2D Euler problem run fused into the stage kernel
     // (stages 1 and 3 with the method's coefficients, see fr_method)
-    if (p->d.equation == FRGPU_EULER2D && s == 2 && A[2] != 0.0 && b[1] != 0.0 && p->fuse_erk) {
+    if (p->d.equation == FRGPU_EULER2D && s == 2 && A[2] != 0.0 && b[1] != 0.0 && p->fuse_erk &&
+        p->d.flux != FRGPU_FLUX_CENTRAL) {
         const double a21 = A[2], b1 = b[0], b2 = b[1];
         fr_method m;
         m.stages = 2;
@@ -1040,6 +1050,15 @@ FRGPU_API int frgpu_problem_set_option(frgpu_problem *p, int option, int value) 
     if (option == FRGPU_OPT_FUSED_TWO_STAGE) p->fuse_erk = value != 0;
     p->graph_ind = -2; // force a re-capture
     p->erk_dirty = true;
+    drop_rock_graphs(p);
+    return FRGPU_OK;
+}
+
+FRGPU_API int frgpu_problem_set_flux_dissipation(frgpu_problem *p, double c) {
+    FR_REQ(p, "set_flux_dissipation: null problem");
+    FR_REQ(std::isfinite(c) && c >= 0.0, "set_flux_dissipation: need a finite c >= 0");
+    p->flux_c = c;
+    p->erk_dirty = true; // the coefficient is baked into the captured kernels
     drop_rock_graphs(p);
     return FRGPU_OK;
 }

@@ -36,7 +36,7 @@ def _extra_flags(src: str) -> list[str]:
     which the oracle performs in the same order, so the FP64 path reproduces
     the oracle bit for bit.  The FP32 units keep the default contraction."""
     name = os.path.basename(src)
-    if name.endswith("_f64.cu") or name in ("filter.cu", "limiter.cu", "erk.cu", "tri.cu"):
+    if name.endswith("_f64.cu") or name in ("filter.cu", "limiter.cu", "erk.cu", "tri.cu", "central2d.cu"):
         return ["-fmad=false"]
     return []
 

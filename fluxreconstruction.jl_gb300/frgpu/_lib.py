@@ -14,7 +14,7 @@ OK = 0
 ERR_ARG, ERR_CUDA, ERR_NONFINITE, ERR_UNPHYSICAL, ERR_DT, ERR_TIMEOUT, ERR_UNSUPPORTED = -1, -2, -3, -4, -5, -6, -7
 
 ADVECTION, BURGERS, EULER1D, EULER2D, BGK1D = 0, 1, 2, 3, 4
-FLUX_ROE, FLUX_LF, FLUX_HLL, FLUX_UPWIND = 0, 1, 2, 3
+FLUX_ROE, FLUX_LF, FLUX_HLL, FLUX_UPWIND, FLUX_CENTRAL = 0, 1, 2, 3, 4
 FP64, FP32K = 0, 1
 BC_PERIODIC, BC_COPY, BC_FIXED, BC_DIRICHLET = 0, 1, 2, 3
 RADAU, SD, HUYNH = 0, 1, 2
@@ -71,6 +71,7 @@ SIGNATURES = {
     "frgpu_troubled_flags": (C.c_int, [_VP, _I, C.c_long]),
     "frgpu_positive_limiter": (C.c_int, [_VP, _D, C.c_double, _I]),
     "frgpu_step_erk": (C.c_int, [_VP, C.c_int, _D, _D, C.c_double, C.c_int]),
+    "frgpu_problem_set_flux_dissipation": (C.c_int, [_VP, C.c_double]),
     "frgpu_step_rock": (C.c_int, [_VP, C.c_int, _D, _D, _D, _D, C.c_int, _D, _D, C.c_double, C.c_int]),
     "frgpu_spectral_radius": (C.c_int, [_VP, C.c_int, _D, _I]),
     "frgpu_problem_set_metric": (C.c_int, [_VP, _D, _D, _D]),

@@ -30,7 +30,8 @@ from ._lib import check, dptr
 _CORR = {"radau": L.RADAU, "sd": L.SD, "huynh": L.HUYNH}
 _BC = {"period": L.BC_PERIODIC, "periodic": L.BC_PERIODIC, "copy": L.BC_COPY, "extra": L.BC_COPY,
        "fix": L.BC_FIXED, "fixed": L.BC_FIXED, "dirichlet": L.BC_DIRICHLET}
-_FLUX = {"roe": L.FLUX_ROE, "lf": L.FLUX_LF, "lax": L.FLUX_LF, "hll": L.FLUX_HLL, "upwind": L.FLUX_UPWIND}
+_FLUX = {"roe": L.FLUX_ROE, "lf": L.FLUX_LF, "lax": L.FLUX_LF, "hll": L.FLUX_HLL, "upwind": L.FLUX_UPWIND,
+         "central": L.FLUX_CENTRAL}
 _PREC = {"fp64": L.FP64, "fp32k": L.FP32K, "fp32": L.FP32K}
 _IND = {"none": L.IND_NONE, "plain": L.IND_PLAIN, "mlp": L.IND_MLP}
 
@@ -448,6 +449,10 @@ class ODEProblem:
             self._keep_ji = c
             check(L.lib().frgpu_problem_set_face_jacobians(self._h, dptr(c), dptr(b1), dptr(b2)))
 
+    def set_flux_dissipation(self, c: float) -> None:
+        """Dissipation coefficient of flux="central" (dev/curve_euler.jl's 40 dt)."""
+        check(L.lib().frgpu_problem_set_flux_dissipation(self._h, float(c)))
+
     def set_option(self, option: int, value: int) -> None:
         """Kernel choice for measurements (frgpu_problem_set_option), e.g.
         ``set_option(L.OPT_BGK_TENSOR, 0)`` for the CUDA-core BGK transport."""
@@ -498,7 +503,10 @@ def FREuler2DProblem(u, tspan, ps: FRPSpace2D, gamma, flux="hll", bc="period", f
                      precision="fp64") -> ODEProblem:
     """The 2D Euler ``dudt!`` closure of example/shock-vortex.jl:26-118 as an
     ODEProblem.  ``bc`` is one kind for all sides or (left, right, bottom, top);
-    ``fixed_states`` gives the conserved ghost state of each fixed side."""
+    ``fixed_states`` gives the conserved ghost state of each fixed side.
+    flux="central" is the dudt! of dev/curve_euler.jl (with set_metric and
+    set_flux_dissipation; sides "period" or "dirichlet", the latter keeping the
+    elements along it at du = 0)."""
     bcs = (bc,) * 4 if isinstance(bc, str) else tuple(bc)
     d = _desc(L.EULER2D, flux=_FLUX[flux], precision=precision, bcs=tuple(_BC[b] for b in bcs), gamma=gamma,
               fixed_states=fixed_states)

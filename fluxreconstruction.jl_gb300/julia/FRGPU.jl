@@ -26,7 +26,7 @@ using OrdinaryDiffEq: ODEProblem
 const libfrgpu = get(ENV, "FRGPU_LIB", joinpath(@__DIR__, "..", "libfrgpu.so"))
 
 const ADVECTION, BURGERS, EULER1D, EULER2D, BGK1D = Cint(0), Cint(1), Cint(2), Cint(3), Cint(4)
-const FLUX = Dict(:roe => Cint(0), :lf => Cint(1), :hll => Cint(2), :upwind => Cint(3))
+const FLUX = Dict(:roe => Cint(0), :lf => Cint(1), :hll => Cint(2), :upwind => Cint(3), :central => Cint(4))
 const BC = Dict(:period => Cint(0), :copy => Cint(1), :fix => Cint(2), :dirichlet => Cint(3))
 const PRECISION = Dict(:fp64 => Cint(0), :fp32k => Cint(1))
 
@@ -219,6 +219,12 @@ function set_metric!(prob, iJ; n1=nothing, n2=nothing)
 end
 
 """interp_face!(fδ, f, ll, lr) of src/interpolate.jl:1-10, evaluated on the GPU."""
+"""Dissipation coefficient c of `flux=:central`, the interaction flux of
+dev/curve_euler.jl (the script's 40 dt)."""
+function set_flux_dissipation!(prob, c)
+    check(ccall((:frgpu_problem_set_flux_dissipation, libfrgpu), Cint, (Ptr{Cvoid}, Cdouble), (prob.p::Problem).h, c))
+end
+
 function interp_face!(fδ, f::AbstractMatrix, ll, lr)
     fh = Matrix{Float64}(f)
     out = zeros(size(f, 1), 2)

@@ -45,7 +45,22 @@ enum frgpu_equation {
     FRGPU_EULER2D = 3,   /* 2D Euler                shock-vortex.jl:26-118   */
     FRGPU_BGK1D = 4      /* 1D1V BGK                bgk_wave.jl:69-129       */
 };
-enum frgpu_flux { FRGPU_FLUX_ROE = 0, FRGPU_FLUX_LF = 1, FRGPU_FLUX_HLL = 2, FRGPU_FLUX_UPWIND = 3 };
+enum frgpu_flux {
+    FRGPU_FLUX_ROE = 0,
+    FRGPU_FLUX_LF = 1,
+    FRGPU_FLUX_HLL = 2,
+    FRGPU_FLUX_UPWIND = 3,
+    /* 2D Euler with a per-point metric: the interaction flux of the active
+     * dudt! of dev/curve_euler.jl:93-117, F* = 0.5 (f_L + f_R) - c (u_R - u_L)
+     * on the face traces of the transformed flux (x faces its first, y faces its
+     * second component) and of u, with a fixed dissipation coefficient c
+     * (frgpu_problem_set_flux_dissipation; the script's 40 dt); the traces
+     * enter the corrections unscaled.  Sides are periodic or Dirichlet (the
+     * elements along a Dirichlet side keep du = 0, the script's interior-only
+     * update).  Residual evaluations only: step with frgpu_step_erk (the script
+     * uses Midpoint) or frgpu_step_rock. */
+    FRGPU_FLUX_CENTRAL = 4
+};
 enum frgpu_precision {
     FRGPU_FP64 = 0, /* plain FP64 residual and stage combination            */
     FRGPU_FP32K = 1 /* FP32 residual, compensated (Kahan) stage combination  */
@@ -248,6 +263,9 @@ FRGPU_API int frgpu_problem_set_metric(frgpu_problem *p, const double *iJ, const
  * was set with.  Needs frgpu_problem_set_metric with normals first; Ji = NULL
  * returns to the (iJ n) scaling at the solution points. */
 FRGPU_API int frgpu_problem_set_face_jacobians(frgpu_problem *p, const double *Ji, const double *n1, const double *n2);
+/* Dissipation coefficient c >= 0 of FRGPU_FLUX_CENTRAL (dev/curve_euler.jl uses
+ * 40 dt with its dt = 0.002). */
+FRGPU_API int frgpu_problem_set_flux_dissipation(frgpu_problem *p, double c);
 /* Run the limiter before every step of frgpu_step_ssprk3 (the loop of
  * example/shock-vortex.jl:297-303); on = 0 turns it off. */
 FRGPU_API int frgpu_set_limiter(frgpu_problem *p, int on, const double *weights, double t0);

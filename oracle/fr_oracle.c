@@ -608,6 +608,18 @@ static void face_flux_n(const fro_cfg *c, const double *wL, const double *wR, do
     fw[3] = f[3];
 }
 
+/* FRO_FLUX_CENTRAL: the transformed-flux traces of the element at ghost-layer
+ * coordinates (ig, jg); a ghost across a periodic side is its periodic partner
+ * (across a Dirichlet side the trace is never used: zeros). */
+static const double *central_fface(const fro_cfg *c, const e2d_work *w, int ig, int jg) {
+    const int nx = c->nx, ny = c->ny, FS = 4 * w->np * 4;
+    if (ig == 0 && c->bc[0] == FRO_BC_PERIODIC) ig = nx;
+    if (ig == nx + 1 && c->bc[1] == FRO_BC_PERIODIC) ig = 1;
+    if (jg == 0 && c->bc[2] == FRO_BC_PERIODIC) jg = ny;
+    if (jg == ny + 1 && c->bc[3] == FRO_BC_PERIODIC) jg = 1;
+    return w->fface + ((long)jg * w->nxg + ig) * FS;
+}
+
 static void rhs_euler2d(const fro_cfg *c, double *du, const double *u) {
     int nx = c->nx, ny = c->ny, np = c->np;
     double g = c->gamma;
@@ -620,7 +632,7 @@ static void rhs_euler2d(const fro_cfg *c, double *du, const double *u) {
     int FS = 4 * np * 4; /* per element face block: face, pt, m */
     w.ug = (double *)malloc(sizeof(double) * ng * w.E);
     w.uface = (double *)malloc(sizeof(double) * ng * FS);
-    w.fface = (double *)malloc(sizeof(double) * ng * FS);
+    w.fface = (double *)calloc((size_t)ng * FS, sizeof(double));
     w.fvol = (double *)malloc(sizeof(double) * (long)nx * ny * 2 * w.E);
     w.fxi = (double *)malloc(sizeof(double) * (long)(nx + 1) * ny * np * 4);
     w.fyi = (double *)malloc(sizeof(double) * (long)nx * (ny + 1) * np * 4);
@@ -699,7 +711,14 @@ static void rhs_euler2d(const fro_cfg *c, double *du, const double *u) {
             const double *R = w.uface + ((long)(j + 1) * nxg + i + 1) * FS; /* element i */
             for (int k = 0; k < np; ++k) {
                 double *fw = w.fxi + (((long)j * (nx + 1) + i) * np + k) * 4;
-                if (c->iJ && c->n1) {
+                if (c->flux == FRO_FLUX_CENTRAL) {
+                    /* dev/curve_euler.jl:93-104: 0.5 (f_face[i-1, j, 2] + f_face[i, j, 4]) (first
+                     * component) - c (u_face[i, j, 4] - u_face[i-1, j, 2]) */
+                    const double *fL = central_fface(c, &w, i, j + 1), *fR = central_fface(c, &w, i + 1, j + 1);
+                    for (int m = 0; m < 4; ++m)
+                        fw[m] = 0.5 * (fL[(1 * np + k) * 4 + m] + fR[(3 * np + k) * 4 + m]) -
+                                c->flux_c * (R[(3 * np + k) * 4 + m] - L[(1 * np + k) * 4 + m]);
+                } else if (c->iJ && c->n1) {
                     const long f = i + (long)(nx + 1) * j, nf = (long)(nx + 1) * ny;
                     face_flux_n(c, L + (1 * np + k) * 4, R + (3 * np + k) * 4, c->n1[f], c->n1[f + nf], fw);
                 } else if (c->flux == FRO_FLUX_HLL)
@@ -717,7 +736,13 @@ static void rhs_euler2d(const fro_cfg *c, double *du, const double *u) {
             const double *T = w.uface + ((long)(j + 1) * nxg + i + 1) * FS; /* element j */
             for (int k = 0; k < np; ++k) {
                 double *fw = w.fyi + (((long)j * nx + i) * np + k) * 4;
-                if (c->iJ && c->n2) {
+                if (c->flux == FRO_FLUX_CENTRAL) {
+                    /* dev/curve_euler.jl:106-117 (second component, faces 3 below and 1 above) */
+                    const double *fB = central_fface(c, &w, i + 1, j), *fT = central_fface(c, &w, i + 1, j + 1);
+                    for (int m = 0; m < 4; ++m)
+                        fw[m] = 0.5 * (fB[(2 * np + k) * 4 + m] + fT[(0 * np + k) * 4 + m]) -
+                                c->flux_c * (T[(0 * np + k) * 4 + m] - B[(2 * np + k) * 4 + m]);
+                } else if (c->iJ && c->n2) {
                     const long f = i + (long)nx * j, nf = (long)nx * (ny + 1);
                     face_flux_n(c, B + (2 * np + k) * 4, T + (0 * np + k) * 4, c->n2[f], c->n2[f + nf], fw);
                 } else if (c->flux == FRO_FLUX_HLL)
@@ -749,7 +774,17 @@ static void rhs_euler2d(const fro_cfg *c, double *du, const double *u) {
                     /* interface-flux scales: iJx, iJy; per point a11, a22 (shock-vortex.jl:104-111);
                      * with face normals (iJ n)_1 and (iJ n)_2 of each face (dev/parallelogram.jl:149-160) */
                     double sL = c->iJx, sR = c->iJx, sB = c->iJy, sT = c->iJy;
-                    if (c->iJ) {
+                    if (c->flux == FRO_FLUX_CENTRAL) {
+                        /* the traces of the transformed flux enter unscaled; the elements
+                         * along a Dirichlet side are not updated (dev/curve_euler.jl:119-149
+                         * runs over the interior elements only) */
+                        sL = sR = sB = sT = 1.0;
+                        if ((i == 0 && c->bc[0] == FRO_BC_DIRICHLET) || (i == nx - 1 && c->bc[1] == FRO_BC_DIRICHLET) ||
+                            (j == 0 && c->bc[2] == FRO_BC_DIRICHLET) || (j == ny - 1 && c->bc[3] == FRO_BC_DIRICHLET)) {
+                            du[i + (long)nx * j + nn * (k + np * (l + (long)np * m))] = 0.0;
+                            continue;
+                        }
+                    } else if (c->iJ) {
                         const long at = ei + nn * (k + (long)np * l), blk = nn * np * np;
                         const double a11 = c->iJ[at], a21 = c->iJ[at + blk], a12 = c->iJ[at + 2 * blk],
                                      a22 = c->iJ[at + 3 * blk];

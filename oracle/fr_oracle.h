@@ -55,7 +55,7 @@ int fro_shock_detector(double Se, int deg, double S0, double kappa);
 
 /* ---- residual configuration ---- */
 enum { FRO_ADVECTION = 0, FRO_BURGERS = 1, FRO_EULER1D = 2, FRO_EULER2D = 3, FRO_BGK1D = 4 };
-enum { FRO_FLUX_ROE = 0, FRO_FLUX_LF = 1, FRO_FLUX_HLL = 2, FRO_FLUX_UPWIND = 3 };
+enum { FRO_FLUX_ROE = 0, FRO_FLUX_LF = 1, FRO_FLUX_HLL = 2, FRO_FLUX_UPWIND = 3, FRO_FLUX_CENTRAL = 4 };
 enum { FRO_BC_PERIODIC = 0, FRO_BC_COPY = 1, FRO_BC_FIXED = 2, FRO_BC_DIRICHLET = 3 };
 
 typedef struct {
@@ -78,6 +78,7 @@ typedef struct {
                                   scales of dev/cylinder2.jl:147-150, or NULL */
     int bgk_closure;           /* BGK Maxwellian: 0 conserve_prim(w, 3) (bgk_wave.jl),
                                   1 prim = [rho, a, 1] (advection_kinetic.jl) */
+    double flux_c;             /* FRO_FLUX_CENTRAL: dissipation coefficient c */
 } fro_cfg;
 
 long fro_ndof(const fro_cfg *c);

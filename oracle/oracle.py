@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(HERE, "liboracle.so")
 SRC = os.path.join(HERE, "fr_oracle.c")
 
 ADVECTION, BURGERS, EULER1D, EULER2D, BGK1D = 0, 1, 2, 3, 4
-FLUX_ROE, FLUX_LF, FLUX_HLL, FLUX_UPWIND = 0, 1, 2, 3
+FLUX_ROE, FLUX_LF, FLUX_HLL, FLUX_UPWIND, FLUX_CENTRAL = 0, 1, 2, 3, 4
 BC_PERIODIC, BC_COPY, BC_FIXED, BC_DIRICHLET = 0, 1, 2, 3
 
 
@@ -52,6 +52,7 @@ class Cfg(C.Structure):
         ("velo", _D), ("weights", _D),
         ("iJ", _D), ("n1", _D), ("n2", _D), ("Ji", _D),
         ("bgk_closure", C.c_int),
+        ("flux_c", C.c_double),
     ]
 
 
@@ -272,10 +273,11 @@ class Problem:
 
     def __init__(self, kind, space, *, flux=FLUX_ROE, a=1.0, gamma=1.4, tau=1e-2, bc=BC_PERIODIC,
                  bcs=None, fixed_states=None, velo=None, weights=None, eps_interior=1e-8,
-                 eps_periodic=1e-6, bgk_closure=0):
+                 eps_periodic=1e-6, bgk_closure=0, flux_c=0.0):
         c = Cfg()
         c.kind, c.flux = kind, flux
         c.bgk_closure = bgk_closure
+        c.flux_c = flux_c
         c.nx = space.nx
         c.ny = getattr(space, "ny", 1)
         c.np = space.np
