@@ -7,7 +7,7 @@ points are tri_quadrature(deg) (src/Quadrature/quadrature.jl:14-71; the
 Williams-Shunn-Jameson rules), unless the caller passes its own.  ``TriAdvectionProblem`` is the linear-advection dudt! of
 dev/wave_triangle.jl:44-125 with its explicit time steps, all on the GPU
 through the ``frgpu_tri_*`` entry points.  Meshes come from Gmsh ASCII
-files (``read_gmsh``, the reference's assets/*.msh) or from
+files (``read_gmsh``, the reference's assets/*.msh), SU2 files (``read_su2``) or from
 ``tri_square_mesh`` (a triangulated rectangle, two right triangles per square,
 periodic or not).
 """
@@ -248,6 +248,53 @@ def read_gmsh(path: str):
     index = {t: q for q, t in enumerate(tags)}
     cellid = np.array([[index[t] for t in c] for c in tris], dtype=np.int64).reshape(-1, 3)
     return np.array(xy, dtype=np.float64).reshape(-1, 2), cellid
+
+
+def read_su2(path: str):
+    """Triangles of an SU2 ASCII mesh (the reference's assets/linesource.su2):
+    vertex coordinates [npts, 2], the 0-based vertex ids [ncell, 3] of every
+    triangle (element type 5) in the file's order, and the boundary markers as
+    {tag: edges [n, 2]} (line elements, type 3).  Other element types are
+    skipped."""
+    with open(path) as f:
+        toks = [ln.split("%")[0].strip() for ln in f]
+    lines = [t for t in toks if t]
+    xy, tris, markers = None, [], {}
+    i = 0
+
+    def value(line):
+        return line.split("=", 1)[1].split()
+
+    while i < len(lines):
+        key = lines[i].split("=", 1)[0].strip().upper() if "=" in lines[i] else ""
+        if key == "NDIME":
+            if int(value(lines[i])[0]) != 2:
+                raise ValueError(f"{path}: only 2D SU2 meshes are read")
+            i += 1
+        elif key == "NELEM":
+            n = int(value(lines[i])[0])
+            for ln in lines[i + 1:i + 1 + n]:
+                v = [int(t) for t in ln.split()]
+                if v[0] == 5:
+                    tris.append(v[1:4])
+            i += 1 + n
+        elif key == "NPOIN":
+            n = int(value(lines[i])[0])
+            xy = [[float(t) for t in ln.split()[:2]] for ln in lines[i + 1:i + 1 + n]]
+            i += 1 + n
+        elif key == "MARKER_TAG":
+            tag = value(lines[i])[0] if value(lines[i]) else ""
+            n = int(value(lines[i + 1])[0])
+            edges = [[int(t) for t in ln.split()[1:3]] for ln in lines[i + 2:i + 2 + n]
+                     if int(ln.split()[0]) == 3]
+            markers[tag] = np.array(edges, dtype=np.int64).reshape(-1, 2)
+            i += 2 + n
+        else:
+            i += 1
+    if xy is None or not tris:
+        raise ValueError(f"{path}: no points or no triangles")
+    return (np.array(xy, dtype=np.float64).reshape(-1, 2), np.array(tris, dtype=np.int64).reshape(-1, 3),
+            markers)
 
 
 def boundary_cell_type(cellid, key=None):

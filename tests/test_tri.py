@@ -263,6 +263,39 @@ def test_read_gmsh_round_trip(frgpu, tmp_path, version):
     assert sp.ncell == len(cid) and np.array_equal(sp.cell_type, ct)
 
 
+def _write_su2(path, pts, cid, edges):
+    with open(path, "w") as f:
+        f.write("% a triangulated rectangle\nNDIME= 2\n")
+        f.write(f"NELEM= {len(cid)}\n")
+        for c, v in enumerate(cid):
+            f.write(f"5 {v[0]} {v[1]} {v[2]} {c}\n")
+        f.write(f"NPOIN= {len(pts)}\n")
+        for q, p in enumerate(pts):
+            f.write(f"{float(p[0])!r} {float(p[1])!r} {q}\n")
+        f.write("NMARK= 1\nMARKER_TAG= wall\n")
+        f.write(f"MARKER_ELEMS= {len(edges)}\n")
+        for a, b in edges:
+            f.write(f"3 {a} {b}\n")
+
+
+def test_read_su2_round_trip(frgpu, tmp_path):
+    """SU2: triangles, points and the boundary marker's edges come back; the
+    marker's edges are exactly the faces with no neighbour."""
+    pts, cid, _, ct = frgpu.tri_square_mesh(4, 3, periodic=False)
+    faces = {}
+    for v in cid:
+        for a, b in ((v[0], v[1]), (v[1], v[2]), (v[2], v[0])):
+            faces[tuple(sorted((a, b)))] = faces.get(tuple(sorted((a, b))), 0) + 1
+    edges = sorted(f for f, n in faces.items() if n == 1)
+    path = str(tmp_path / "m.su2")
+    _write_su2(path, pts, cid, edges)
+    p2, c2, mk = frgpu.read_su2(path)
+    assert np.array_equal(p2, pts) and np.array_equal(c2, cid)
+    assert list(mk) == ["wall"] and np.array_equal(mk["wall"], np.array(edges))
+    sp = frgpu.TriFRPSpace(p2, c2, 2, cell_type=frgpu.boundary_cell_type(c2))
+    assert int((sp.nb_cell[:, :, 0] < 0).sum()) == len(edges)
+
+
 # the reference checkout's meshes, when FR_REFERENCE names a checkout
 REFERENCE_ASSETS = os.path.join(os.environ["FR_REFERENCE"], "assets") if os.environ.get("FR_REFERENCE") else None
 
@@ -277,6 +310,18 @@ def test_clockwise_cells_are_rejected(frgpu):
     frgpu.TriFRPSpace(pts, cid, 1, xpl, wp, key, ct)
     with pytest.raises(ValueError, match=r"clockwise.*\[4\]"):
         frgpu.TriFRPSpace(pts, bad, 1, xpl, wp, key, ct)
+
+
+@pytest.mark.skipif(REFERENCE_ASSETS is None or not os.path.isdir(REFERENCE_ASSETS),
+                    reason="set FR_REFERENCE to a reference checkout to read its meshes")
+def test_reference_su2_mesh(frgpu):
+    """assets/linesource.su2: 8442 positively oriented triangles on 4342 points;
+    its marker holds the 240 faces that have no neighbour."""
+    pts, cid, mk = frgpu.read_su2(os.path.join(REFERENCE_ASSETS, "linesource.su2"))
+    assert cid.shape == (8442, 3) and pts.shape == (4342, 2)
+    assert np.all(np.linalg.det(frgpu.rs_jacobi(cid, pts)) > 0)
+    sp = frgpu.TriFRPSpace(pts, cid, 1, cell_type=frgpu.boundary_cell_type(cid))
+    assert sum(len(e) for e in mk.values()) == int((sp.nb_cell[:, :, 0] < 0).sum()) == 240
 
 
 @pytest.mark.skipif(REFERENCE_ASSETS is None or not os.path.isdir(REFERENCE_ASSETS),
