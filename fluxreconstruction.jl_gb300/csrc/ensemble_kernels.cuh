@@ -314,6 +314,16 @@ __device__ void ens_run(const EnsArgs<Real> &a, int id, Real *s_t, double *s_red
     }
     const double deg = NP - 1;
     double dt = a.cfl * in.dx / ((2.0 * deg + 1.0) * fmax(mx, 1e-300));
+    // a state so large (or infinite) that its CFL step count has no int: stopped
+    // before its first step, failed = -1 (the whole group sees the same mx)
+    if (!(a.t_end / dt < 2.0e9)) {
+        if (r == 0) {
+            a.failed[id] = -1;
+            a.steps_out[id] = 0;
+            a.dt_out[id] = dt;
+        }
+        return;
+    }
     const long nfull = (long)floor(a.t_end / dt);
     const double last = a.t_end - (double)nfull * dt;
     const long nsteps = nfull + (last > 0.0 ? 1 : 0);

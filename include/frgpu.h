@@ -373,9 +373,11 @@ FRGPU_API int frgpu_ensemble_set_mlp(frgpu_ensemble *e, const frgpu_mlp *m, doub
  * stats[0] troubled, [1] misfires (network != plain test), [2] fallbacks, [3] judged. */
 FRGPU_API int frgpu_ensemble_indicator_stats(frgpu_ensemble *e, long long *stats);
 /* Instances stopped because their state turned non-finite: flags[i] = the
- * step (1-based) after which instance i stopped, 0 otherwise (flags may be
- * NULL).  Returns their number.  frgpu_ensemble_run stops such an instance and
- * carries on with the others; it stays stopped until its state is set again. */
+ * step (1-based) after which instance i stopped, -1 when it was not started
+ * because its CFL step count t_end / dt exceeds 2e9 (a state of huge or
+ * infinite magnitude), 0 otherwise (flags may be NULL).  Returns their number.
+ * frgpu_ensemble_run stops such an instance and carries on with the others; it
+ * stays stopped until its state is set again. */
 FRGPU_API int frgpu_ensemble_failed(frgpu_ensemble *e, int *flags);
 /* Total element count over all instances. */
 FRGPU_API long frgpu_ensemble_nelem(const frgpu_ensemble *e);

@@ -172,17 +172,28 @@ def test_trained_burgers1d_indicator_agrees_with_plain(frgpu):
 
 
 def test_non_finite_instance_stops_alone(frgpu, oracle):
-    """With the reference's filter strength (lambda = dt e^(0.875 deg) 0.15) the
-    2048-element p = 2 instance blows up before t = 0.3, on the GPU and in the
-    oracle alike.  It stops there, the other 15 instances finish and still
-    match the oracle bit for bit, and setting its state again revives it."""
+    """An instance whose state turns non-finite (here: one value of the
+    2048-element p = 2 instance set to NaN on the host before the run) stops
+    after its first step; the other 15 instances finish and still match the
+    oracle bit for bit, and setting its state again revives it."""
     e = small_ensemble(frgpu, "fp64")
     u0 = [e.get_state(i) for i in range(e.n)]
+    bad = u0[11].copy()
+    bad.flat[1000] = np.nan
+    e.set_state(11, bad)
     e.run(0.3, filter=True)
     f = e.failed()
-    assert np.flatnonzero(f).tolist() == [11]
+    assert np.flatnonzero(f).tolist() == [11] and f[11] == 1
     for i in (0, 4, 12, 15):
         ref, _, _ = oracle_run(oracle, frgpu, int(e.ne[i]), int(e.deg[i]), u0[i], 0.3, 0.4, True)
         assert np.array_equal(e.get_state(i), ref), i
     e.set_state(11, u0[11])
     assert e.failed()[11] == 0
+    # a state of huge magnitude would need more than 2e9 CFL steps: not started
+    big = u0[3].copy()
+    big.flat[7] = 1e200
+    e.set_state(3, big)
+    e.run(0.01, filter=True)
+    f = e.failed()
+    assert f[3] == -1 and np.flatnonzero(f).tolist() == [3]
+    assert e.stats()["steps"][3] == 0
