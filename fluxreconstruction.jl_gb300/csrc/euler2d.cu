@@ -54,12 +54,44 @@ template <> struct SumAcc<float> {
 // the CFL rate is (lambda_r + lambda_s) / 2 with the contravariant speeds
 // lambda_r = |a11 u + a12 v| + c |(a11, a12)|, lambda_s = |a21 u + a22 v| +
 // c |(a21, a22)| (on a rectangle, (|u| + c)/dx + (|v| + c)/dy again).
+// Final pass over the per-block partials: warp v (of 6) combines value v, each
+// lane over a fixed strided subset of the blocks, then a fixed butterfly: the
+// same order every call, so the result is deterministic.  Loads bypass L1
+// (the partials were written by other SMs).
+__device__ __forceinline__ double final_value(const double *__restrict__ part, int nblocks, int v) {
+    const int lane = threadIdx.x & 31;
+    double x = 0.0; // sums start at 0; the maxima are of non-negative speeds
+    // a lane takes blocks lane, lane + 32, ... in ascending order; the loads of
+    // a batch are all issued before the first of them is used
+    constexpr int B = 20;
+    for (int b0 = 0; b0 < nblocks; b0 += 32 * B) {
+        double y[B];
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+            const int b = b0 + lane + 32 * k;
+            y[k] = b < nblocks ? __ldcg(part + b * 6 + v) : 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < B; ++k)
+            if (b0 + lane + 32 * k < nblocks) x = v < 4 ? x + y[k] : fmax(x, y[k]);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const double y = __shfl_xor_sync(0xffffffffu, x, off);
+        x = v < 4 ? x + y : fmax(x, y);
+    }
+    return x;
+}
+
 template <class Real, bool DEV>
-__global__ void __launch_bounds__(RED_THREADS) k_reduce2d_partial(const Real *__restrict__ u, const Real *__restrict__ lo,
+__global__ void __launch_bounds__(RED_THREADS, sizeof(Real) == 4 ? 4 : 2) k_reduce2d_partial(const Real *__restrict__ u, const Real *__restrict__ lo,
                                                              size_t plane, int nq, const double *__restrict__ wp,
                                                              double gamma, double idx_, double idy_,
                                                              double *__restrict__ part,
-                                                             const Real *__restrict__ met = nullptr) {
+                                                             const Real *__restrict__ met = nullptr,
+                                                             unsigned *cnt = nullptr, double *fin = nullptr,
+                                                             double *hfin = nullptr, const int *dstatus = nullptr,
+                                                             int *hstatus = nullptr) {
     // part layout: [q * gridDim.x + b][6]: 4 sums, max directional speed, max CFL rate
     const int q = blockIdx.y;
     const size_t npts = plane * nq;
@@ -68,44 +100,55 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce2d_partial(const Real *__
     const Real g = (Real)gamma, gm1 = (Real)(gamma - 1.0), ix = (Real)idx_, iy = (Real)idy_;
     SumAcc<Real> acc[4];
     Real smax = Real(0), rmax = Real(0);
-    for (size_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        Real w[4], wl[4] = {Real(0), Real(0), Real(0), Real(0)};
-        if (DEV) {
-            const size_t at = frk::e2d_index(e, q, 0, plane);
-            frk::ldg4(u + at, w);
-            if (lo != nullptr) frk::ldg4(lo + at, wl);
-        } else {
-            const size_t t = e + plane * q;
+    constexpr int UN = 2; // elements whose loads are issued together (4 measured slower: occupancy)
+    for (size_t eb = e0 + threadIdx.x; eb < e1; eb += UN * blockDim.x) {
+        Real W[UN][4], WL[UN][4], MT[UN][4];
 #pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                w[m] = u[t + npts * m];
-                if (lo != nullptr) wl[m] = lo[t + npts * m];
+        for (int t = 0; t < UN; ++t) {
+            const size_t e = eb + (size_t)t * blockDim.x;
+#pragma unroll
+            for (int m = 0; m < 4; ++m) W[t][m] = WL[t][m] = MT[t][m] = Real(0);
+            if (e >= e1) continue;
+            if (DEV) {
+                const size_t at = frk::e2d_index(e, q, 0, plane);
+                frk::ldg4(u + at, W[t]);
+                if (lo != nullptr) frk::ldg4(lo + at, WL[t]);
+                if (met != nullptr) frk::ldg4(met + at, MT[t]);
+            } else {
+                const size_t tt = e + plane * q;
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    W[t][m] = u[tt + npts * m];
+                    if (lo != nullptr) WL[t][m] = lo[tt + npts * m];
+                }
             }
         }
-        Real mt[4] = {Real(0), Real(0), Real(0), Real(0)};
-        Real jac = Real(1);
-        if (DEV && met != nullptr) {
-            frk::ldg4(met + frk::e2d_index(e, q, 0, plane), mt);
-            jac = Real(1) / (mt[0] * mt[3] - mt[1] * mt[2]);
-        }
+        // the elements in ascending order, as one element per iteration would take them
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            if (DEV && met != nullptr) acc[m].add(w[m] * jac, wl[m] * jac);
-            else acc[m].add(w[m], wl[m]);
-            w[m] += wl[m];
-        }
-        const Real rinv = frk::recipR<Real>(w[0]);
-        const Real U = w[1] * rinv, V = w[2] * rinv;
-        const Real p = gm1 * (w[3] - Real(0.5) * (w[1] * U + w[2] * V));
-        const Real c = frk::sqrtP<Real>(g * p * rinv);
-        const Real a = fabs(U) + c, bb = fabs(V) + c;
-        smax = fmax(smax, fmax(a, bb));
-        if (DEV && met != nullptr) {
-            const Real lr = fabs(mt[0] * U + mt[1] * V) + c * frk::sqrtR<Real>(mt[0] * mt[0] + mt[1] * mt[1]);
-            const Real ls = fabs(mt[2] * U + mt[3] * V) + c * frk::sqrtR<Real>(mt[2] * mt[2] + mt[3] * mt[3]);
-            rmax = fmax(rmax, Real(0.5) * (lr + ls));
-        } else {
-            rmax = fmax(rmax, a * ix + bb * iy);
+        for (int t = 0; t < UN; ++t) {
+            if (eb + (size_t)t * blockDim.x >= e1) break;
+            Real *w = W[t], *wl = WL[t], *mt = MT[t];
+            Real jac = Real(1);
+            if (DEV && met != nullptr) jac = Real(1) / (mt[0] * mt[3] - mt[1] * mt[2]);
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                if (DEV && met != nullptr) acc[m].add(w[m] * jac, wl[m] * jac);
+                else acc[m].add(w[m], wl[m]);
+                w[m] += wl[m];
+            }
+            const Real rinv = frk::recipR<Real>(w[0]);
+            const Real U = w[1] * rinv, V = w[2] * rinv;
+            const Real p = gm1 * (w[3] - Real(0.5) * (w[1] * U + w[2] * V));
+            const Real c = frk::sqrtP<Real>(g * p * rinv);
+            const Real a = fabs(U) + c, bb = fabs(V) + c;
+            smax = fmax(smax, fmax(a, bb));
+            if (DEV && met != nullptr) {
+                const Real lr = fabs(mt[0] * U + mt[1] * V) + c * frk::sqrtR<Real>(mt[0] * mt[0] + mt[1] * mt[1]);
+                const Real ls = fabs(mt[2] * U + mt[3] * V) + c * frk::sqrtR<Real>(mt[2] * mt[2] + mt[3] * mt[3]);
+                rmax = fmax(rmax, Real(0.5) * (lr + ls));
+            } else {
+                rmax = fmax(rmax, a * ix + bb * iy);
+            }
         }
     }
     __shared__ double red[6][RED_THREADS / 32];
@@ -126,21 +169,28 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce2d_partial(const Real *__
         for (int w = 1; w < RED_THREADS / 32; ++w) x = v < 4 ? x + red[v][w] : fmax(x, red[v][w]);
         part[((size_t)q * gridDim.x + blockIdx.x) * 6 + v] = v < 4 ? x * wp[q] : x;
     }
-}
-
-// Final pass over the per-block partials: warp v (of 6) combines value v, each
-// lane over a fixed strided subset of the blocks, then a fixed butterfly: the
-// same order every call, so the result is deterministic.
-__device__ __forceinline__ double final_value(const double *__restrict__ part, int nblocks, int v) {
-    const int lane = threadIdx.x & 31;
-    double x = 0.0; // sums start at 0; the maxima are of non-negative speeds
-    for (int b = lane; b < nblocks; b += 32) x = v < 4 ? x + part[b * 6 + v] : fmax(x, part[b * 6 + v]);
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const double y = __shfl_xor_sync(0xffffffffu, x, off);
-        x = v < 4 ? x + y : fmax(x, y);
+    if (cnt == nullptr) return;
+    // the last block to finish combines every block's partials (the order of
+    // the final pass is fixed, so the result does not depend on which block it is)
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(cnt, 1u) == gridDim.x * gridDim.y - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int v = threadIdx.x >> 5;
+    if (v < 6) {
+        const double x = final_value(part, (int)(gridDim.x * gridDim.y), v);
+        if ((threadIdx.x & 31) == 0) {
+            fin[v] = x;
+            if (hfin) hfin[v] = x; // straight into the caller's page-locked host words
+        }
     }
-    return x;
+    if (threadIdx.x == 0) {
+        if (hstatus) *hstatus = __ldcg(dstatus);
+        *cnt = 0u; // ready for the next launch
+    }
 }
 
 __global__ void __launch_bounds__(192) k_reduce_final(const double *__restrict__ part, int nblocks,
@@ -163,8 +213,17 @@ int fr_launch_euler2d(frgpu_problem *p, int stage, const void *in, const void *d
 }
 
 // out (device, 6 doubles at p->d_red + RED_BLOCKS*6): sums[4], max speed, max CFL rate.
-int fr_launch_euler2d_reduce(frgpu_problem *p, const void *state, const void *lo, double *out_sums,
-                             double *out_speed, double cfl_dx, double cfl_dy) {
+void fr_drop_reduce_graphs(frgpu_problem *p) {
+    for (auto &g : p->red_graphs) {
+        if (g.gexec) cudaGraphExecDestroy(g.gexec);
+        g.gexec = nullptr;
+        g.state = nullptr;
+    }
+}
+
+// partial + final kernels, then the 6 results and the status word copied to
+// the problem's page-locked host words
+static int enqueue_reduce(frgpu_problem *p, const void *state, const void *lo, double cfl_dx, double cfl_dy) {
     const size_t plane = (size_t)p->sp.nx * p->sp.ny;
     const int np = p->sp.np;
     double *wp = p->d_red + FR_RED_WP;
@@ -173,21 +232,61 @@ int fr_launch_euler2d_reduce(frgpu_problem *p, const void *state, const void *lo
     const int nq = np * np;
     const dim3 grid(RED_BLOCKS / nq, nq);
     // general quadrilaterals: weights det J and contravariant speeds from the metric
+    // the spare final slot 7 holds the last-block counter (zeroed with d_red, reset by the kernel);
+    // the results and the status word go to the page-locked host words from the kernel itself
+    unsigned *cnt = reinterpret_cast<unsigned *>(fin + 7);
+    frgpu_problem::host_words *hw = nullptr;
+    FR_CUDA(cudaHostGetDevicePointer((void **)&hw, p->h_words, 0));
     if (p->d.precision == FRGPU_FP64)
         k_reduce2d_partial<double, true><<<grid, RED_THREADS, 0, p->stream>>>(
             (const double *)state, (const double *)lo, plane, nq, wp, p->d.gamma, cfl_dx, cfl_dy, part,
-            (const double *)p->d_met);
+            (const double *)p->d_met, cnt, fin, hw->red, p->d_status, &hw->status);
     else
         k_reduce2d_partial<float, true><<<grid, RED_THREADS, 0, p->stream>>>(
             (const float *)state, (const float *)lo, plane, nq, wp, p->d.gamma, cfl_dx, cfl_dy, part,
-            (const float *)p->d_met);
+            (const float *)p->d_met, cnt, fin, hw->red, p->d_status, &hw->status);
     FR_CUDA(cudaGetLastError());
-    k_reduce_final<<<1, 192, 0, p->stream>>>(part, (int)(grid.x * grid.y), fin);
-    FR_CUDA(cudaGetLastError());
-    p->launches += 2;
-    double h[6];
-    FR_CUDA(cudaMemcpyAsync(h, fin, sizeof(h), cudaMemcpyDeviceToHost, p->stream));
+    return FRGPU_OK;
+}
+
+int fr_launch_euler2d_reduce(frgpu_problem *p, const void *state, const void *lo, double *out_sums,
+                             double *out_speed, double cfl_dx, double cfl_dy, int *status) {
+    // the callers pass the rectangles' 1/dx, 1/dy: the graph of a state buffer
+    // holds them as its kernel arguments
+    if (cfl_dx != 1.0 / p->sp.dx || cfl_dy != 1.0 / p->sp.dy) {
+        int rc = enqueue_reduce(p, state, lo, cfl_dx, cfl_dy);
+        if (rc) return rc;
+    } else {
+        frgpu_problem::red_graph *g = nullptr;
+        for (auto &r : p->red_graphs)
+            if (r.gexec && r.state == state) g = &r;
+        if (!g) {
+            g = p->red_graphs[0].gexec ? &p->red_graphs[1] : &p->red_graphs[0];
+            if (g->gexec) {
+                FR_CUDA(cudaStreamSynchronize(p->stream));
+                cudaGraphExecDestroy(g->gexec);
+                g->gexec = nullptr;
+            }
+            cudaGraph_t graph = nullptr;
+            FR_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+            int rc = enqueue_reduce(p, state, lo, cfl_dx, cfl_dy);
+            cudaError_t ce = cudaStreamEndCapture(p->stream, &graph);
+            if (rc) {
+                if (graph) cudaGraphDestroy(graph);
+                return rc;
+            }
+            if (ce != cudaSuccess) return fr_cuda_fail(ce, "cudaStreamEndCapture");
+            ce = cudaGraphInstantiate(&g->gexec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (ce != cudaSuccess) return fr_cuda_fail(ce, "cudaGraphInstantiate");
+            g->state = state;
+        }
+        FR_CUDA(cudaGraphLaunch(g->gexec, p->stream));
+    }
+    p->launches += 1;
     FR_CUDA(cudaStreamSynchronize(p->stream));
+    const double *h = p->h_words->red;
+    if (status) *status = p->h_words->status;
     const double area = p->d_met ? 1.0 : p->sp.dx * p->sp.dy * 0.25;
     if (out_sums)
         for (int m = 0; m < 4; ++m) out_sums[m] = h[m] * area;

@@ -68,6 +68,18 @@ struct frgpu_problem {
     float mlp_thr = 0.5f, mlp_band = 0.0f;
     int bgk_tensor = 1;             // FP32 BGK transport on the tensor cores
     int bgk_closure = 0;            // BGK Maxwellian: 0 conserve_prim(w, 3), 1 prim = [rho, a, 1]
+    // page-locked host words the status and reduction results come back into
+    // (one copy engine transfer each, no staging through pageable memory)
+    struct host_words {
+        double red[6];
+        int status;
+    } *h_words = nullptr;
+    // captured reductions (kernels + copies of the results and the status word),
+    // one per state buffer the FP32K high part alternates between
+    struct red_graph {
+        const void *state;
+        cudaGraphExec_t gexec;
+    } red_graphs[2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     double flux_c = 0.0;            // FRGPU_FLUX_CENTRAL dissipation coefficient
     void *d_c2 = nullptr;           // FRGPU_FLUX_CENTRAL work: transformed fluxes and face traces
     size_t c2_cap = 0;              // values d_c2 holds
@@ -178,8 +190,11 @@ void build_2d(frgpu_space &s);
 // Kernel launchers (return FRGPU_OK or an error; stage 0 = residual only)
 // euler2d.cu
 int fr_launch_euler2d(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
+// the sums and speeds; with status non-null the device status word comes back
+// in the same synchronisation.  Replayed from a captured graph per state buffer.
+void fr_drop_reduce_graphs(frgpu_problem *p);
 int fr_launch_euler2d_reduce(frgpu_problem *p, const void *state, const void *lo, double *out_sums,
-                             double *out_speed, double cfl_dx, double cfl_dy);
+                             double *out_speed, double cfl_dx, double cfl_dy, int *status = nullptr);
 // scalar1d.cu
 int fr_launch_scalar1d(frgpu_problem *p, int stage, const void *in, const void *din, void *out);
 int fr_launch_euler1d(frgpu_problem *p, int stage, const void *in, const void *din, void *out);

@@ -298,6 +298,7 @@ static void free_problem(frgpu_problem *p) {
         if (g) cudaGraphExecDestroy(g);
     if (p->erk_gexec) cudaGraphExecDestroy(p->erk_gexec);
     drop_rock_graphs(p);
+    fr_drop_reduce_graphs(p);
     void *bufs[] = {p->s0,     p->s1,      p->s2,         p->s3,      p->d_dt,      p->d_status, p->d_red,
                     p->d_flags, p->d_count, p->d_velo,     p->d_w,     p->d_J,       p->d_V,      p->d_iV,
                     p->rhs_in, p->rhs_out, p->d_bgk_prim, p->d_bgk_frag, p->d_stage, p->d_erk,   p->d_met,
@@ -305,6 +306,7 @@ static void free_problem(frgpu_problem *p) {
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (p->stream) cudaStreamDestroy(p->stream);
+    if (p->h_words) cudaFreeHost(p->h_words);
     cudaSetDevice(cur);
     delete p;
 }
@@ -320,10 +322,8 @@ static int upload_vec(frgpu_problem *p, void **dst, const std::vector<double> &s
     return p->esize == 8 ? upload_as<double>(dst, src) : upload_as<float>(dst, src);
 }
 
-static int check_status(frgpu_problem *p) {
-    int st = 0;
-    FR_CUDA(cudaMemcpyAsync(&st, p->d_status, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
-    FR_CUDA(cudaStreamSynchronize(p->stream));
+// The error a device status word st stands for (0: none); resets the word.
+static int status_error(frgpu_problem *p, int st) {
     if (st == 0) return FRGPU_OK;
     FR_CUDA(cudaMemsetAsync(p->d_status, 0, sizeof(int), p->stream));
     if (st & 1) {
@@ -336,6 +336,12 @@ static int check_status(frgpu_problem *p) {
     }
     fr_set_error("device-side wait timed out");
     return FRGPU_ERR_TIMEOUT;
+}
+
+static int check_status(frgpu_problem *p) {
+    FR_CUDA(cudaMemcpyAsync(&p->h_words->status, p->d_status, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+    FR_CUDA(cudaStreamSynchronize(p->stream));
+    return status_error(p, p->h_words->status);
 }
 
 static int launch_stage(frgpu_problem *p, int stage, const void *in, const void *din, void *out) {
@@ -560,6 +566,8 @@ FRGPU_API int frgpu_problem_create(const frgpu_space *s, const frgpu_problem_des
             FR_CUDA(cudaMemset(p->d_dt, 0, sizeof(double)));
             FR_CUDA(cudaMalloc(&p->d_status, sizeof(int)));
             FR_CUDA(cudaMemset(p->d_status, 0, sizeof(int)));
+            FR_CUDA(cudaMallocHost((void **)&p->h_words, sizeof(frgpu_problem::host_words)));
+            p->h_words->status = 0;
             FR_CUDA(cudaMalloc(&p->d_red, sizeof(double) * FR_RED_SIZE));
             FR_CUDA(cudaMemset(p->d_red, 0, sizeof(double) * FR_RED_SIZE));
             const size_t ne = (size_t)s->nx * s->ny;
@@ -982,11 +990,34 @@ FRGPU_API int frgpu_reduce(frgpu_problem *p, double *sums, double *maxspeed) {
     }
     FR_TRY
     double sp[2];
+    int st = 0;
     int rc = fr_launch_euler2d_reduce(p, fr_state_hi(p), p->d.precision == FRGPU_FP32K ? p->s3 : nullptr, sums, sp,
-                                      1.0 / p->sp.dx, 1.0 / p->sp.dy);
+                                      1.0 / p->sp.dx, 1.0 / p->sp.dy, &st);
     if (rc) return rc;
     if (maxspeed) *maxspeed = sp[0];
-    return FRGPU_OK;
+    // the status of steps queued before (frgpu_step_ssprk3_async) comes back with the sums
+    return status_error(p, st);
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_step_ssprk3_reduce(frgpu_problem *p, double dt, int nsteps, double *sums, double *maxspeed) {
+    FR_REQ(p, "step_ssprk3_reduce: null problem");
+    FR_REQ(nsteps >= 0, "step_ssprk3_reduce: negative step count");
+    if (p->d.equation != FRGPU_EULER2D) {
+        fr_set_error("step_ssprk3_reduce: implemented for the 2D Euler problem");
+        return FRGPU_ERR_UNSUPPORTED;
+    }
+    if (!(dt > 0.0) || !std::isfinite(dt)) {
+        fr_set_error("step_ssprk3_reduce: dt must be positive and finite");
+        return FRGPU_ERR_DT;
+    }
+    FR_TRY
+    if (nsteps > 0) {
+        use_method(p, fr_method());
+        int rc = run_fused_steps(p, dt, nsteps, false);
+        if (rc) return rc;
+    }
+    return frgpu_reduce(p, sums, maxspeed);
     FR_CATCH
 }
 
@@ -1126,6 +1157,7 @@ FRGPU_API int frgpu_problem_set_metric(frgpu_problem *p, const double *iJ, const
     FR_REQ(iJ || !n1, "problem_set_metric: face normals need the metric");
     FR_TRY
     FR_CUDA(cudaStreamSynchronize(p->stream));
+    fr_drop_reduce_graphs(p); // they hold the metric buffer's address
     for (void **b : {&p->d_nfx, &p->d_nfy, &p->d_fsc})
         if (*b) {
             cudaFree(*b);

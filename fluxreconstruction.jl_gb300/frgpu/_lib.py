@@ -72,6 +72,7 @@ SIGNATURES = {
     "frgpu_positive_limiter": (C.c_int, [_VP, _D, C.c_double, _I]),
     "frgpu_step_erk": (C.c_int, [_VP, C.c_int, _D, _D, C.c_double, C.c_int]),
     "frgpu_problem_set_flux_dissipation": (C.c_int, [_VP, C.c_double]),
+    "frgpu_step_ssprk3_reduce": (C.c_int, [_VP, C.c_double, C.c_int, _D, _D]),
     "frgpu_step_rock": (C.c_int, [_VP, C.c_int, _D, _D, _D, _D, C.c_int, _D, _D, C.c_double, C.c_int]),
     "frgpu_spectral_radius": (C.c_int, [_VP, C.c_int, _D, _I]),
     "frgpu_problem_set_metric": (C.c_int, [_VP, _D, _D, _D]),

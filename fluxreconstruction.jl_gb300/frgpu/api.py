@@ -823,6 +823,18 @@ class Integrator:
         check(L.lib().frgpu_reduce(self.prob._h, dptr(sums), C.byref(ms)))
         return sums, ms.value
 
+    def step_reduce(self, n: int = 1, dt: float | None = None):
+        """n SSPRK3 steps, then the FP64 conserved sums and the maximum wave
+        speed, with one synchronisation (frgpu_step_ssprk3_reduce)."""
+        if self.alg is not None:
+            raise NotImplementedError("step_reduce runs the fused SSPRK3 step")
+        dt = self.dt if dt is None else float(dt)
+        sums = np.zeros(4)
+        ms = C.c_double()
+        check(L.lib().frgpu_step_ssprk3_reduce(self.prob._h, dt, int(n), dptr(sums), C.byref(ms)))
+        self.t += n * dt
+        return sums, ms.value
+
     def stream(self) -> int:
         s = C.c_void_p()
         check(L.lib().frgpu_problem_stream(self.prob._h, C.byref(s)))

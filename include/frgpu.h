@@ -216,8 +216,15 @@ FRGPU_API int frgpu_spectral_radius(frgpu_problem *p, int maxiter, double *rho, 
  * (lambda_r + lambda_s)/2 with the contravariant speeds lambda_r = |a11 u + a12 v|
  * + c |(a11, a12)| and lambda_s = |a21 u + a22 v| + c |(a21, a22)|. */
 FRGPU_API int frgpu_cfl_dt(frgpu_problem *p, double cfl, double *dt);
-/* FP64 conserved sums (quadrature-weighted, per variable) and max wave speed */
+/* FP64 conserved sums (quadrature-weighted, per variable) and max wave speed.
+ * The device status word comes back in the same synchronisation: the error of
+ * steps queued before (frgpu_step_ssprk3_async) is returned here, after the
+ * sums are written. */
 FRGPU_API int frgpu_reduce(frgpu_problem *p, double *sums, double *maxspeed);
+/* nsteps of frgpu_step_ssprk3 followed by frgpu_reduce, with one
+ * synchronisation: the step!(itg) of a loop that reads back the conserved sums
+ * and the wave speed after every step.  Returns the steps' status. */
+FRGPU_API int frgpu_step_ssprk3_reduce(frgpu_problem *p, double dt, int nsteps, double *sums, double *maxspeed);
 /* Post-step troubled-cell indicator + :l2 modal filter, example/shock-vortex.jl:308-321
  * (2D, detection on density, S0/kappa as given) and example/euler_highlevel.jl:37-52 (1D).
  * indicator = FRGPU_IND_NONE disables it. */

@@ -401,6 +401,33 @@ def test_nonfinite_and_unphysical_states_are_reported(frgpu):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32k"])
+def test_async_steps_report_through_reduce(frgpu, oracle, precision):
+    """step_async queues the steps; frgpu_reduce returns their status with the
+    sums (one synchronisation): a good run gives the oracle's sums, an
+    unphysical state raises at the reduce and the problem stays usable."""
+    ps = frgpu.FRPSpace2D(0, 1, 24, 0, 1, 20, 3)
+    po = oracle_space2d(ps, 0, 1, 24, 0, 1, 20, 3)
+    u = wave2d(ps.xpg)
+    itg = frgpu.init(frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf", precision=precision), dt=1e-3)
+    for _ in range(4):
+        itg.step_async(1)
+        sums, _ = itg.reduce()
+    ref = oracle.Problem(oracle.EULER2D, po, gamma=1.4, flux=oracle.FLUX_LF).ssprk3(u, 1e-3, 4)
+    exact = [np.sum(ref[..., m] * ps.wp[None, None]) * ps.dx * ps.dy / 4 for m in range(4)]
+    np.testing.assert_allclose(sums, exact, rtol=1e-12 if precision == "fp64" else 1e-6)
+    neg = u.copy(order="F")
+    neg[5, 5, :, :, 0] = -1.0
+    itg.u = neg
+    itg.step_async(1)
+    with pytest.raises(frgpu.FRGPUError) as e:
+        itg.reduce()
+    assert e.value.code in (-3, -4)
+    itg.u = u
+    itg.step_async(1)
+    itg.reduce()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32k"])
 @pytest.mark.parametrize("nx,ny,deg", [(37, 5, 2), (33, 3, 3), (1, 1, 3)])
 def test_euler2d_state_transfer_round_trip(frgpu, precision, nx, ny, deg):
     """Host u[i, j, k, l, m] -> the point-vector device layout -> host: exact in
