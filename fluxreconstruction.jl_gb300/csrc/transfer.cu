@@ -7,7 +7,9 @@
 // differ on the device: BGK f[i, v, k] -> u[(i * np + k) * nvel + v], and the
 // 2D Euler u[i, j, k, l, m] -> the point-vector layout of e2d_index.
 // Downloads run the reverse kernel (hi + lo in FP64) and one cudaMemcpy back.
-// No per-element host loop.
+// A page-locked (or registered) host array skips the staging copy: the kernels
+// read or write it in place through its device mapping.  No per-element host
+// loop.
 #include <string>
 
 #include "fr_common.cuh"
@@ -118,27 +120,43 @@ int grid_for(long n) {
 
 // Host u (FP64, reference layout) -> device hi (and lo for FP32K); rejects
 // non-finite values with FRGPU_ERR_NONFINITE naming the first bad index.
+// The device address of a page-locked (or registered) host array, or null for
+// pageable memory: the conversion kernels then read or write the caller's
+// array directly over the CPU-GPU link instead of through the staging copy.
+static void *mapped(const void *host) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+        cudaGetLastError(); // a pageable pointer is no error here
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 int fr_put_state(frgpu_problem *p, const double *u, void *hi, void *lo) {
     int rc = stage_buffer(p);
     if (rc) return rc;
     double *stage = (double *)p->d_stage;
     unsigned long long *first_bad = reinterpret_cast<unsigned long long *>(stage + p->ndof);
     const unsigned long long none = ~0ull;
-    FR_CUDA(cudaMemcpyAsync(stage, u, sizeof(double) * (size_t)p->ndof, cudaMemcpyHostToDevice, p->stream));
+    const double *src = (const double *)mapped(u);
+    if (!src) {
+        FR_CUDA(cudaMemcpyAsync(stage, u, sizeof(double) * (size_t)p->ndof, cudaMemcpyHostToDevice, p->stream));
+        src = stage;
+    }
     FR_CUDA(cudaMemcpyAsync(first_bad, &none, sizeof(none), cudaMemcpyHostToDevice, p->stream));
     const Layout L = layout_of(p);
     if (L.kind == LAYOUT_E2D) {
         const long nq = L.np * L.np;
         const dim3 grid((unsigned)((L.ne + 255) / 256), (unsigned)nq);
         if (p->esize == 8)
-            k_upload_e2d<double><<<grid, 256, 0, p->stream>>>(stage, (double *)hi, nullptr, L.ne, nq, first_bad);
+            k_upload_e2d<double><<<grid, 256, 0, p->stream>>>(src, (double *)hi, nullptr, L.ne, nq, first_bad);
         else
-            k_upload_e2d<float><<<grid, 256, 0, p->stream>>>(stage, (float *)hi, (float *)lo, L.ne, nq, first_bad);
+            k_upload_e2d<float><<<grid, 256, 0, p->stream>>>(src, (float *)hi, (float *)lo, L.ne, nq, first_bad);
     } else if (p->esize == 8)
-        k_upload<double><<<grid_for(p->ndof), 256, 0, p->stream>>>(stage, (double *)hi, nullptr, p->ndof, L,
+        k_upload<double><<<grid_for(p->ndof), 256, 0, p->stream>>>(src, (double *)hi, nullptr, p->ndof, L,
                                                                      first_bad);
     else
-        k_upload<float><<<grid_for(p->ndof), 256, 0, p->stream>>>(stage, (float *)hi, (float *)lo, p->ndof, L,
+        k_upload<float><<<grid_for(p->ndof), 256, 0, p->stream>>>(src, (float *)hi, (float *)lo, p->ndof, L,
                                                                     first_bad);
     FR_CUDA(cudaGetLastError());
     unsigned long long bad = none;
@@ -155,7 +173,9 @@ int fr_put_state(frgpu_problem *p, const double *u, void *hi, void *lo) {
 int fr_get_state(frgpu_problem *p, const void *hi, const void *lo, double *u) {
     int rc = stage_buffer(p);
     if (rc) return rc;
-    double *stage = (double *)p->d_stage;
+    double *dst = (double *)mapped(u);
+    const bool direct = dst != nullptr;
+    double *stage = direct ? dst : (double *)p->d_stage;
     const Layout L = layout_of(p);
     if (L.kind == LAYOUT_E2D) {
         const long nq = L.np * L.np;
@@ -170,7 +190,8 @@ int fr_get_state(frgpu_problem *p, const void *hi, const void *lo, double *u) {
         k_download<float><<<grid_for(p->ndof), 256, 0, p->stream>>>((const float *)hi, (const float *)lo, stage,
                                                                       p->ndof, L);
     FR_CUDA(cudaGetLastError());
-    FR_CUDA(cudaMemcpyAsync(u, stage, sizeof(double) * (size_t)p->ndof, cudaMemcpyDeviceToHost, p->stream));
+    if (!direct)
+        FR_CUDA(cudaMemcpyAsync(u, stage, sizeof(double) * (size_t)p->ndof, cudaMemcpyDeviceToHost, p->stream));
     FR_CUDA(cudaStreamSynchronize(p->stream));
     return FRGPU_OK;
 }

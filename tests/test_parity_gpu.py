@@ -425,6 +425,13 @@ def test_async_steps_report_through_reduce(frgpu, oracle, precision):
     itg.u = u
     itg.step_async(1)
     itg.reduce()
+    # frgpu_step_ssprk3_reduce: the same steps and sums in one call
+    a = frgpu.init(frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf", precision=precision), dt=1e-3)
+    b = frgpu.init(frgpu.FREuler2DProblem(u, (0, 1), ps, 1.4, flux="lf", precision=precision), dt=1e-3)
+    sa, ma = a.step_reduce(3)
+    b.step(3)
+    sb, mb = b.reduce()
+    assert np.array_equal(sa, sb) and ma == mb and np.array_equal(a.u, b.u)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32k"])
@@ -452,6 +459,24 @@ def test_euler2d_state_transfer_round_trip(frgpu, precision, nx, ny, deg):
     assert e.value.code == -3
     flat = np.ravel_multi_index((nx - 1, ny - 1, deg, 0, 2), u.shape, order="F")
     assert f"index {flat}" in str(e.value)
+    # page-locked host arrays take the direct path (the conversion kernels read
+    # and write them through their device mapping): the same values come back,
+    # and a non-finite value is reported the same way
+    import torch
+
+    def pinned():
+        t = torch.empty(u.size, dtype=torch.float64, pin_memory=True)
+        return t, t.numpy().reshape(u.shape, order="F")
+
+    ti, hin = pinned()
+    hin[...] = u
+    to, hout = pinned()
+    itg.u = hin
+    assert np.array_equal(itg.read_u(hout), back)
+    hin[nx - 1, ny - 1, deg, 0, 2] = np.nan
+    with pytest.raises(frgpu.FRGPUError) as e:
+        itg.u = hin
+    assert e.value.code == -3 and f"index {flat}" in str(e.value)
 
 
 # ---------------------------------------------------------------- positivity-preserving limiter
