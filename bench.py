@@ -742,6 +742,104 @@ def bgk_entry(steps=400, warmup=5):
     return out
 
 
+def dev_scripts_entry(cpu=True):
+    """Two reference scripts through their drop-in paths, FP64, wall clock per
+    step on the device against the oracle on all host cores:
+    * example/advection_kinetic.jl: the kinetic problem (100 elements on
+      [-1, 1], p = 2, 28 velocities, density-only BGK closure, tau = 0.002) to
+      t = 0.5 at the script's dt = 0.0005 with a stabilised method (RKC2: the
+      spectral radius by the power method, then the stage count, every step, as
+      ROCK4 does); 1000 steps on the GPU, a 100-step sample on the oracle;
+    * dev/curve_euler.jl: the polar grid's 58 x 48 active elements, p = 2, its
+      central flux with c = 40 dt, Midpoint at dt = 0.002, the script's 50 steps
+      (the oracle runs the same 50; the two final states are compared)."""
+    import frgpu
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    out = {}
+    # advection_kinetic.jl
+    nx, deg, nu = 100, 2, 28
+    ps = frgpu.FRPSpace1D(-1, 1, nx, deg)
+    dv = 10 / nu
+    v = -5 + (np.arange(nu) + 0.5) * dv
+    w = np.full(nu, dv)
+    rho0 = 1 - np.sin(np.pi * ps.xpg)
+    f = np.zeros((nx, nu, deg + 1), order="F")
+    for k in range(deg + 1):
+        f[:, :, k] = rho0[:, k, None] * np.sqrt(1 / np.pi) * np.exp(-(v[None, :] - 1.0) ** 2)
+    dt, n = 0.0005, 1000
+    itg = frgpu.init(frgpu.FRBGKProblem(f, (0, 0.5), ps, v, w, 0.002, closure="density", a=1.0), frgpu.RKC2(),
+                     dt=dt)
+    itg.step(5)
+    itg.u = f
+    itg.stages = []
+    t0 = time.perf_counter()
+    itg.step(n)
+    gpu_s = time.perf_counter() - t0
+    rec = {"workload": "advection_kinetic.jl: 100 el x 28 vel, p=2, tau=0.002, RKC2 at dt=0.0005 to t=0.5",
+           "ndof": int(f.size), "steps": n, "gpu_ms_per_step": gpu_s / n * 1e3,
+           "stages_used": sorted(set(int(x) for x in itg.stages)),
+           "gpu_dof_updates_per_s": f.size * float(np.mean(itg.stages)) * n / gpu_s}
+    if cpu:
+        po = same_ops(O.Space1D(-1, 1, nx, deg), ps)
+        po.J = np.array(ps.J)
+        P = O.Problem(O.BGK1D, po, tau=0.002, a=1.0, velo=v, weights=w, bgk_closure=1)
+        alg = frgpu.RKC2()
+        u, d = f.copy(order="F"), None
+        m = 100
+        t0 = time.perf_counter()
+        for _ in range(m):
+            r, _, d = P.spectral_radius(u, alg.maxiter, d)
+            al, be, mu, de, _, _ = alg.coefficients(dt * r)
+            u = P.rock(u, dt, 1, al, be, mu, de)
+        rec["cpu_ms_per_step"] = (time.perf_counter() - t0) / m * 1e3
+        rec["cpu_sample"] = f"{m} steps on the oracle, {O.get_threads()} threads"
+        rec["gpu_vs_cpu"] = rec["cpu_ms_per_step"] / rec["gpu_ms_per_step"]
+    out["advection_kinetic"] = rec
+    # curve_euler.jl
+    nr, nt, deg = 60, 50, 2
+    G_CURVE, C_DISS = 5 / 3, 40 * 0.002
+    ps2 = frgpu.FRPSpace2D(0, 1, nr, 0, 1, nt, deg)
+    V = frgpu.polar_vertices(1.0, 6.0, nr, 0.0, np.pi, nt)
+    iJ = frgpu.quad_metric(ps2.xpl, V)
+    xpg = frgpu.quad_points(ps2.xpl, V)
+    # the script's u0: a density bump at (0, 3), at rest, prim = [rho, 0, 0, 1] (p = rho / 2)
+    rho = np.maximum(np.exp(-10 * (xpg[..., 0] ** 2 + (xpg[..., 1] - 3.0) ** 2)), 1e-2)
+    u0 = np.zeros(rho.shape + (4,), order="F")
+    u0[..., 0] = rho
+    u0[..., 3] = 0.5 * rho / (G_CURVE - 1)
+    ub = np.asfortranarray(u0[:nr - 2, :nt - 2])
+    iJb = np.asfortranarray(iJ[:nr - 2, :nt - 2])
+    psb = frgpu.FRPSpace2D(0, 1, nr - 2, 0, 1, nt - 2, deg)
+    prob = frgpu.FREuler2DProblem(ub, (0, 1), psb, G_CURVE, flux="central", bc="dirichlet")
+    prob.set_metric(iJb)
+    prob.set_flux_dissipation(C_DISS)
+    mid = frgpu.Midpoint()
+    itg = frgpu.init(prob, mid, dt=0.002)
+    itg.step(3)
+    itg.u = ub
+    itg.synchronize()
+    t0 = time.perf_counter()
+    itg.step(50)
+    itg.synchronize()
+    gpu_s = time.perf_counter() - t0
+    rec = {"workload": "curve_euler.jl: 58 x 48 active elements of the polar grid, p=2, central flux, Midpoint "
+                       "at dt=0.002, 50 steps", "ndof": int(ub.size), "gpu_ms_per_step": gpu_s / 50 * 1e3}
+    if cpu:
+        po2 = same_ops(O.Space2D(0, 1, nr - 2, 0, 1, nt - 2, deg), psb)
+        P2 = O.Problem(O.EULER2D, po2, gamma=G_CURVE, flux=O.FLUX_CENTRAL, bc=O.BC_DIRICHLET, flux_c=C_DISS)
+        P2.set_metric(iJb)
+        t0 = time.perf_counter()
+        ref = P2.erk(ub, 0.002, 50, mid.A, mid.b)
+        rec["cpu_ms_per_step"] = (time.perf_counter() - t0) / 50 * 1e3
+        rec["gpu_vs_cpu"] = rec["cpu_ms_per_step"] / rec["gpu_ms_per_step"]
+        rec["bit_identical_to_oracle"] = bool(np.array_equal(itg.u, ref))
+    out["curve_euler"] = rec
+    return out
+
+
 # FP64 floating-point operations (dadd + dmul + 2 dfma, ncu instruction counters;
 # profiles/fp64_flops_512x512_p3.md): k_tri_rhs<double, 3> per cell, and the
 # 2D Euler stage kernel k_euler2d<double, 4, LF, FP64, stage> per DOF and stage
@@ -953,7 +1051,8 @@ def main():
         for name, fn in (("density_wave_512x512_p3", lambda: density_wave_entry(args, dist, ws)),
                          ("indicators_400x200_p3", indicator_entry),
                          ("burgers_ensemble_4096", ensemble_entry), ("bgk_256x512_p3", bgk_entry),
-                         ("triangles_advection_2M_cells_p3", tri_entry)):
+                         ("triangles_advection_2M_cells_p3", tri_entry),
+                         ("reference_scripts_rock_curve", dev_scripts_entry)):
             try:
                 configs[name] = fn()
             except Exception as e:  # report, do not lose the headline line

@@ -288,11 +288,24 @@ __global__ void __launch_bounds__(256) k_sub(Real *__restrict__ out, const Real 
         out[q] = x[q] - y[q];
 }
 
-// per-block partial sums of (x - y)^2 (y = null: x^2) in FP64, fixed order
+// out = x + c (a - b) (x = null: c (a - b))
 template <class Real>
-__global__ void __launch_bounds__(256) k_norm2_part(const Real *__restrict__ x, const Real *__restrict__ y, size_t n,
-                                                    double *__restrict__ part) {
+__global__ void __launch_bounds__(256) k_axpy_diff(Real *__restrict__ out, const Real *__restrict__ x,
+                                                   const Real *__restrict__ a, const Real *__restrict__ b, double c,
+                                                   size_t n) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+        out[q] = (x ? x[q] : Real(0)) + (Real)c * (a[q] - b[q]);
+}
+
+// ||x - y||_2 (y = null: ||x||_2) in FP64: per-block partial sums in a fixed
+// order, and the last block to finish sums the partials in block order and
+// writes the root to host_out (a page-locked word through its device mapping)
+template <class Real>
+__global__ void __launch_bounds__(256) k_norm2(const Real *__restrict__ x, const Real *__restrict__ y, size_t n,
+                                               double *__restrict__ part, unsigned *cnt, double *host_out,
+                                               const int *dstatus, int *host_status) {
     __shared__ double s[8];
+    __shared__ bool last;
     double acc = 0.0;
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
         const double d = y ? (double)x[q] - (double)y[q] : (double)x[q];
@@ -305,15 +318,17 @@ __global__ void __launch_bounds__(256) k_norm2_part(const Real *__restrict__ x, 
         double t = 0.0;
         for (int w = 0; w < 8; ++w) t += s[w];
         part[blockIdx.x] = t;
+        __threadfence();
+        last = atomicAdd(cnt, 1u) == gridDim.x - 1;
     }
-}
-
-__global__ void k_norm2_final(const double *__restrict__ part, int nb, double *__restrict__ out) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double t = 0.0;
-        for (int b = 0; b < nb; ++b) t += part[b];
-        *out = sqrt(t);
-    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    double t = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) t += __ldcg(part + b);
+    *host_out = sqrt(t);
+    *host_status = __ldcg(dstatus); // the device status word as of this norm
+    *cnt = 0u;                      // ready for the next launch
 }
 
 template <class Real> __global__ void __launch_bounds__(256) k_fill(Real *__restrict__ v, double c, size_t n) {
@@ -339,11 +354,14 @@ int fr_vec_axpy(cudaStream_t st, bool f32, size_t n, void *out, const void *x, c
     return FRGPU_OK;
 }
 
-int fr_vec_sub(cudaStream_t st, bool f32, size_t n, void *out, const void *x, const void *y) {
+int fr_vec_axpy_diff(cudaStream_t st, bool f32, size_t n, void *out, const void *x, const void *a, const void *b,
+                     double c) {
     if (f32)
-        k_sub<float><<<grid_for(n), 256, 0, st>>>((float *)out, (const float *)x, (const float *)y, n);
+        k_axpy_diff<float><<<grid_for(n), 256, 0, st>>>((float *)out, (const float *)x, (const float *)a,
+                                                        (const float *)b, c, n);
     else
-        k_sub<double><<<grid_for(n), 256, 0, st>>>((double *)out, (const double *)x, (const double *)y, n);
+        k_axpy_diff<double><<<grid_for(n), 256, 0, st>>>((double *)out, (const double *)x, (const double *)a,
+                                                         (const double *)b, c, n);
     FR_CUDA(cudaGetLastError());
     return FRGPU_OK;
 }
@@ -366,15 +384,23 @@ int fr_vec_flip(cudaStream_t st, bool f32, void *v, const void *u, size_t i) {
     return FRGPU_OK;
 }
 
-// ||x - y||_2 (y = null: ||x||_2) into *d_out; d_part holds FR_RED_BLOCKS doubles
-int fr_vec_norm2(cudaStream_t st, bool f32, size_t n, const void *x, const void *y, double *d_part, double *d_out) {
+// ||x - y||_2 (y = null: ||x||_2) into the page-locked host word host_out and
+// the device status word into host_status (their device mappings are taken
+// here); d_part holds FR_RED_BLOCKS doubles, cnt a zeroed counter the kernel
+// leaves at zero
+int fr_vec_norm2(cudaStream_t st, bool f32, size_t n, const void *x, const void *y, double *d_part, unsigned *cnt,
+                 double *host_out, const int *d_status, int *host_status) {
+    double *dev_out = nullptr;
+    int *dev_status = nullptr;
+    FR_CUDA(cudaHostGetDevicePointer((void **)&dev_out, host_out, 0));
+    FR_CUDA(cudaHostGetDevicePointer((void **)&dev_status, host_status, 0));
     const int nb = grid_for(n) < FR_RED_BLOCKS ? grid_for(n) : FR_RED_BLOCKS;
     if (f32)
-        k_norm2_part<float><<<nb, 256, 0, st>>>((const float *)x, (const float *)y, n, d_part);
+        k_norm2<float><<<nb, 256, 0, st>>>((const float *)x, (const float *)y, n, d_part, cnt, dev_out, d_status,
+                                           dev_status);
     else
-        k_norm2_part<double><<<nb, 256, 0, st>>>((const double *)x, (const double *)y, n, d_part);
-    FR_CUDA(cudaGetLastError());
-    k_norm2_final<<<1, 32, 0, st>>>(d_part, nb, d_out);
+        k_norm2<double><<<nb, 256, 0, st>>>((const double *)x, (const double *)y, n, d_part, cnt, dev_out,
+                                            d_status, dev_status);
     FR_CUDA(cudaGetLastError());
     return FRGPU_OK;
 }

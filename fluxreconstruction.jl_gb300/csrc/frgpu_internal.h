@@ -72,6 +72,7 @@ struct frgpu_problem {
     // (one copy engine transfer each, no staging through pageable memory)
     struct host_words {
         double red[6];
+        double norm[2]; // power-method norms
         int status;
     } *h_words = nullptr;
     // captured reductions (kernels + copies of the results and the status word),
@@ -111,7 +112,7 @@ struct frgpu_problem {
     // nonlinear power method: direction of the last estimate, work vectors, norm partials
     void *d_eig = nullptr; // 4 n values: direction, v, f(u), f(v)
     bool have_eig = false;
-    double *d_eig_red = nullptr; // FR_RED_BLOCKS partials + 1 result
+    double *d_eig_red = nullptr; // FR_RED_BLOCKS partials + the last-block counter
     float *d_bgk_prim = nullptr;    // FP32 BGK: (rho, U, lambda) per (element, point), from the moments
     uint32_t *d_bgk_frag = nullptr; // FP32 BGK: TF32 A fragments of the transport operator (both signs, split)
     // captured step graph
@@ -272,7 +273,9 @@ int fr_rock_enqueue_raw(const fr_rock_raw &r, int (*residual)(void *, const void
 // residual of a FRGPU_FLUX_CENTRAL 2D problem (central2d.cu)
 int fr_launch_central2d(frgpu_problem *p, int stage, const void *in, void *out);
 int fr_vec_axpy(cudaStream_t st, bool f32, size_t n, void *out, const void *x, const void *y, double c);
-int fr_vec_sub(cudaStream_t st, bool f32, size_t n, void *out, const void *x, const void *y);
+int fr_vec_axpy_diff(cudaStream_t st, bool f32, size_t n, void *out, const void *x, const void *a, const void *b,
+                     double c); // out = x + c (a - b)
 int fr_vec_fill(cudaStream_t st, bool f32, size_t n, void *v, double c);
 int fr_vec_flip(cudaStream_t st, bool f32, void *v, const void *u, size_t i);
-int fr_vec_norm2(cudaStream_t st, bool f32, size_t n, const void *x, const void *y, double *d_part, double *d_out);
+int fr_vec_norm2(cudaStream_t st, bool f32, size_t n, const void *x, const void *y, double *d_part, unsigned *cnt,
+                 double *host_out, const int *d_status, int *host_status);

@@ -915,6 +915,7 @@ FRGPU_API int frgpu_spectral_radius(frgpu_problem *p, int maxiter, double *rho, 
     if (!p->d_eig) {
         FR_CUDA(cudaMalloc(&p->d_eig, 4 * n * es));
         FR_CUDA(cudaMalloc((void **)&p->d_eig_red, sizeof(double) * (FR_RED_BLOCKS + 1)));
+        FR_CUDA(cudaMemset(p->d_eig_red + FR_RED_BLOCKS, 0, sizeof(double))); // the norms' last-block counter
         p->have_eig = false;
     }
     char *base = (char *)p->d_eig;
@@ -922,19 +923,22 @@ FRGPU_API int frgpu_spectral_radius(frgpu_problem *p, int maxiter, double *rho, 
     const void *u = fr_state_hi(p);
     cudaStream_t st = p->stream;
     int rc;
-    auto norm = [&](const void *x, const void *y, double *out) -> int {
-        int r = fr_vec_norm2(st, f32, n, x, y, p->d_eig_red, p->d_eig_red + FR_RED_BLOCKS);
+    unsigned *cnt = reinterpret_cast<unsigned *>(p->d_eig_red + FR_RED_BLOCKS);
+    // the norm lands in page-locked host word `slot`; `wait` synchronises
+    auto norm = [&](const void *x, const void *y, int slot, bool wait) -> int {
+        int r = fr_vec_norm2(st, f32, n, x, y, p->d_eig_red, cnt, &p->h_words->norm[slot], p->d_status,
+                             &p->h_words->status);
         if (r) return r;
-        p->launches += 2;
-        FR_CUDA(cudaMemcpyAsync(out, p->d_eig_red + FR_RED_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, st));
-        FR_CUDA(cudaStreamSynchronize(st));
+        p->launches += 1;
+        if (wait) FR_CUDA(cudaStreamSynchronize(st));
         return FRGPU_OK;
     };
     const double uround = f32 ? 0x1p-24 : 0x1p-53, sq = std::sqrt(uround);
     if ((rc = residual_into(p, u, fu))) return rc;
     const void *d0 = p->have_eig ? dir : fu;
-    double ynrm = 0, vnrm = 0, dynrm;
-    if ((rc = norm(u, nullptr, &ynrm)) || (rc = norm(d0, nullptr, &vnrm))) return rc;
+    double dynrm;
+    if ((rc = norm(u, nullptr, 0, false)) || (rc = norm(d0, nullptr, 1, true))) return rc;
+    const double ynrm = p->h_words->norm[0], vnrm = p->h_words->norm[1];
     if (ynrm != 0.0 && vnrm != 0.0) {
         dynrm = ynrm * sq;
         rc = fr_vec_axpy(st, f32, n, v, u, d0, dynrm / vnrm);
@@ -954,8 +958,8 @@ FRGPU_API int frgpu_spectral_radius(frgpu_problem *p, int maxiter, double *rho, 
     int it = 1, converged = 0;
     for (; it <= maxiter; ++it) {
         if ((rc = residual_into(p, v, fv))) return rc;
-        double dfnrm = 0.0;
-        if ((rc = norm(fv, fu, &dfnrm))) return rc;
+        if ((rc = norm(fv, fu, 0, true))) return rc;
+        const double dfnrm = p->h_words->norm[0];
         const double sigmal = sigma;
         sigma = dfnrm / dynrm;
         if (it >= 2 && std::fabs(sigma - sigmal) <= std::max(sigma, 1e-300) * 0.01) {
@@ -964,21 +968,20 @@ FRGPU_API int frgpu_spectral_radius(frgpu_problem *p, int maxiter, double *rho, 
         }
         if (it == maxiter) break;
         if (dfnrm != 0.0) {
-            if ((rc = fr_vec_sub(st, f32, n, fv, fv, fu)) || (rc = fr_vec_axpy(st, f32, n, v, u, fv, dynrm / dfnrm)))
-                return rc;
-            p->launches += 2;
+            if ((rc = fr_vec_axpy_diff(st, f32, n, v, u, fv, fu, dynrm / dfnrm))) return rc;
+            p->launches += 1;
         } else {
             if ((rc = fr_vec_flip(st, f32, v, u, (size_t)it % n))) return rc;
             p->launches += 1;
         }
     }
-    if ((rc = fr_vec_sub(st, f32, n, dir, v, u))) return rc;
+    // the direction for the next call; the status word came back with the last norm
+    if ((rc = fr_vec_axpy_diff(st, f32, n, dir, nullptr, v, u, 1.0))) return rc;
     p->launches += 1;
-    FR_CUDA(cudaStreamSynchronize(st));
     p->have_eig = true;
     *rho = 1.2 * sigma;
     if (iters) *iters = converged ? it : -it;
-    return check_status(p);
+    return status_error(p, p->h_words->status);
     FR_CATCH
 }
 

@@ -210,6 +210,36 @@ def rs_jacobi_quad(r, vertices) -> np.ndarray:
     return np.stack([Xr, Xs], axis=-1)
 
 
+def quad_points(r, vertices) -> np.ndarray:
+    """xpg[nx, ny, np, np, 2] of FRPSpace2D(base, deg) for a mesh of bilinear
+    quadrilaterals (src/struct.jl:161-175): the solution points (r_k, r_l) mapped
+    by X = sum_a lambda_a(r, s) V_a, vertices[nx, ny, 4, 2] counterclockwise
+    from the lower left."""
+    r = np.asarray(r, dtype=np.float64)
+    V = np.asarray(vertices, dtype=np.float64)
+    R, S = np.meshgrid(r, r, indexing="ij")
+    R, S = R[None, None, :, :, None], S[None, None, :, :, None]
+    v = [V[:, :, a, None, None, :] for a in range(4)]
+    return ((R - 1) * (S - 1) / 4 * v[0] + (R + 1) * (1 - S) / 4 * v[1] + (R + 1) * (S + 1) / 4 * v[2]
+            + (1 - R) * (S + 1) / 4 * v[3])
+
+
+def polar_vertices(r0, r1, nr, t0, t1, nt) -> np.ndarray:
+    """Cell corners vertices[nr, nt, 4, 2] of the polar grid r0 <= r <= r1,
+    t0 <= theta <= t1 with nr x nt cells (KitBase.CSpace2D, the grid of
+    dev/curve_euler.jl and the cylinder scripts), counterclockwise from
+    (r_i, theta_j)."""
+    r = np.linspace(r0, r1, nr + 1)
+    t = np.linspace(t0, t1, nt + 1)
+    V = np.zeros((nr, nt, 4, 2))
+    for a, (di, dj) in enumerate([(0, 0), (1, 0), (1, 1), (0, 1)]):
+        R = r[di:di + nr][:, None]
+        T = t[dj:dj + nt][None, :]
+        V[:, :, a, 0] = R * np.cos(T)
+        V[:, :, a, 1] = R * np.sin(T)
+    return V
+
+
 def quad_metric(r, vertices) -> np.ndarray:
     """iJ[nx, ny, np, np, 2, 2] = inv(J) at the solution points, the field
     FRPSpace2D.iJ (src/struct.jl:135-143) that ODEProblem.set_metric takes."""

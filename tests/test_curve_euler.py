@@ -19,29 +19,6 @@ GAMMA = 5 / 3  # the script's Gas(..., 5/3, ...)
 C_DISS = 40 * 0.002  # 40 dt with the script's dt = 0.002
 
 
-def polar_vertices(r0, r1, nr, t0, t1, nt):
-    """Corners of the polar grid's cells, counterclockwise from (r_i, theta_j):
-    vertices[nr, nt, 4, 2]."""
-    r = np.linspace(r0, r1, nr + 1)
-    t = np.linspace(t0, t1, nt + 1)
-    V = np.zeros((nr, nt, 4, 2))
-    for a, (di, dj) in enumerate([(0, 0), (1, 0), (1, 1), (0, 1)]):
-        R = r[di:di + nr][:, None]
-        T = t[dj:dj + nt][None, :]
-        V[:, :, a, 0] = R * np.cos(T)
-        V[:, :, a, 1] = R * np.sin(T)
-    return V
-
-
-def bilinear_points(r, V):
-    """xpg[nr, nt, np, np, 2] of FRPSpace2D (src/struct.jl:161-175)."""
-    R, S = np.meshgrid(r, r, indexing="ij")
-    R, S = R[None, None, :, :, None], S[None, None, :, :, None]
-    v = [V[:, :, a, None, None, :] for a in range(4)]
-    return ((R - 1) * (S - 1) / 4 * v[0] + (R + 1) * (1 - S) / 4 * v[1] + (R + 1) * (S + 1) / 4 * v[2]
-            + (1 - R) * (S + 1) / 4 * v[3])
-
-
 def initial_state(xpg):
     """u0 of the script (lines 46-51): a density bump at (0, 3), at rest,
     prim = [rho, 0, 0, 1] (lambda = rho / (2 p) = 1, so p = rho / 2)."""
@@ -116,9 +93,9 @@ def script_dudt(u, iJ, ll, lr, dhl, dhr, lpdm, c):
 
 def polar_case(frgpu, nr=12, nt=10, deg=2):
     ps = frgpu.FRPSpace2D(0, 1, nr, 0, 1, nt, deg)  # operators only; the geometry comes from V
-    V = polar_vertices(1.0, 6.0, nr, 0.0, np.pi, nt)
+    V = frgpu.polar_vertices(1.0, 6.0, nr, 0.0, np.pi, nt)
     iJ = frgpu.quad_metric(ps.xpl, V)
-    u = initial_state(bilinear_points(ps.xpl, V))
+    u = initial_state(frgpu.quad_points(ps.xpl, V))
     return ps, V, iJ, u
 
 
