@@ -944,7 +944,7 @@ def headline_cpu(dt, nsteps, gpu_space=None, nthreads=None):
     u, upstream = shock_vortex_initial(xpg)
     P = O.Problem(O.EULER2D, po, gamma=GAMMA, flux=O.FLUX_HLL,
                   bcs=[O.BC_FIXED, O.BC_COPY, O.BC_COPY, O.BC_COPY],
-                  fixed_states=[upstream, [0] * 4, [0] * 4, [0] * 4])
+                  fixed_states=[upstream, [0] * 4, [0] * 4, [0] * 4], ghosts_per_step=1)
     t0 = time.perf_counter()
     uf = P.ssprk3_filtered(u, dt, nsteps, LAM, S0, KAPPA)
     secs = time.perf_counter() - t0
@@ -969,7 +969,7 @@ def reference_arm(args):
     u, upstream = shock_vortex_initial(po.xpg)
     P = O.Problem(O.EULER2D, po, gamma=GAMMA, flux=O.FLUX_HLL,
                   bcs=[O.BC_FIXED, O.BC_COPY, O.BC_COPY, O.BC_COPY],
-                  fixed_states=[upstream, [0] * 4, [0] * 4, [0] * 4])
+                  fixed_states=[upstream, [0] * 4, [0] * 4, [0] * 4], ghosts_per_step=1)
     K = max(1, args.steps)
     if args.warmup:
         u = P.ssprk3_filtered(u, dt, args.warmup, LAM, S0, KAPPA)

@@ -41,6 +41,10 @@ template <class Real, int NP> struct E2DArgs {
     const double *dtp;
     Real iJx, iJy, gamma, gm1;
     int bc[4];
+    // ghosts refreshed once per step (the reference scripts copy their ghost
+    // layers after each step): in the later stages of a step the periodic and
+    // copy neighbours outside the domain are read from u^n, not the stage input
+    int lag;
     Real fixed[4][4];
     Ops<Real, NP> ops;
     int *status;
@@ -296,9 +300,13 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             int jo;
             if (resolve(jn, ny, a.bc[2], a.bc[3], jo)) {
                 const unsigned en = (unsigned)(i0 + hx) + (unsigned)nx * jo;
+                // a ghost outside the domain with ghosts refreshed once per step: u^n
+                const bool lag = STAGE >= 2 && a.lag && (jn < 0 || jn >= ny);
+                const Real *src = MODE == MODE_FP64 && lag ? a.un : uin;
+                const Real *dsrc = lag ? nullptr : din;
                 Real v[NP][4], h[4];
 #pragma unroll
-                for (int l = 0; l < NP; ++l) ld_state4(uin, din, ((unsigned)(hk + NP * l) * plane + en) * 4, v[l]);
+                for (int l = 0; l < NP; ++l) ld_state4(src, dsrc, ((unsigned)(hk + NP * l) * plane + en) * 4, v[l]);
                 v4_dotw<Real, NP>(v, w, h);
                 put4(&SHY(side, hk, 0, hx), CS, h);
             } else {
@@ -324,9 +332,12 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             int io;
             if (resolve(in_, nx, a.bc[0], a.bc[1], io)) {
                 const unsigned en = (unsigned)io + (unsigned)nx * (j0 + hy);
+                const bool lag = STAGE >= 2 && a.lag && (in_ < 0 || in_ >= nx);
+                const Real *src = MODE == MODE_FP64 && lag ? a.un : uin;
+                const Real *dsrc = lag ? nullptr : din;
                 Real v[NP][4], h[4];
 #pragma unroll
-                for (int k = 0; k < NP; ++k) ld_state4(uin, din, ((unsigned)(k + NP * hl) * plane + en) * 4, v[k]);
+                for (int k = 0; k < NP; ++k) ld_state4(src, dsrc, ((unsigned)(k + NP * hl) * plane + en) * 4, v[k]);
                 v4_dotw<Real, NP>(v, w, h);
                 put4(&SHX(side, hy, hl, 0), CSX, h);
             } else {
@@ -722,6 +733,7 @@ int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
         a.bc[s] = p->d.bc[s];
         for (int m = 0; m < 4; ++m) a.fixed[s][m] = (Real)p->d.fixed_state[s][m];
     }
+    a.lag = p->ghosts_per_step;
     a.ops = make_ops<Real, NP>(p->sp);
     a.status = p->d_status;
     a.mlp = frmlp::MLPDev{nullptr, nullptr, nullptr, nullptr, nullptr};

@@ -1075,11 +1075,13 @@ FRGPU_API int frgpu_set_filter(frgpu_problem *p, int indicator, double lam, doub
 FRGPU_API int frgpu_problem_set_option(frgpu_problem *p, int option, int value) {
     FR_REQ(p, "set_option: null problem");
     FR_REQ(option == FRGPU_OPT_BGK_TENSOR || option == FRGPU_OPT_FUSED_INDICATOR ||
-               option == FRGPU_OPT_FUSED_TWO_STAGE || option == FRGPU_OPT_BGK_CLOSURE,
+               option == FRGPU_OPT_FUSED_TWO_STAGE || option == FRGPU_OPT_BGK_CLOSURE ||
+               option == FRGPU_OPT_GHOSTS_PER_STEP,
            "set_option: unknown option");
     FR_REQ(option != FRGPU_OPT_BGK_CLOSURE || value == 0 || value == 1, "set_option: BGK closure is 0 or 1");
     if (option == FRGPU_OPT_BGK_TENSOR) p->bgk_tensor = value != 0;
     if (option == FRGPU_OPT_BGK_CLOSURE) p->bgk_closure = value;
+    if (option == FRGPU_OPT_GHOSTS_PER_STEP) p->ghosts_per_step = value != 0;
     if (option == FRGPU_OPT_FUSED_INDICATOR) p->fuse_indicator = value != 0;
     if (option == FRGPU_OPT_FUSED_TWO_STAGE) p->fuse_erk = value != 0;
     p->graph_ind = -2; // force a re-capture

@@ -19,7 +19,7 @@ FP64, FP32K = 0, 1
 BC_PERIODIC, BC_COPY, BC_FIXED, BC_DIRICHLET = 0, 1, 2, 3
 RADAU, SD, HUYNH = 0, 1, 2
 IND_NONE, IND_PLAIN, IND_MLP = 0, 1, 2
-OPT_BGK_TENSOR, OPT_FUSED_INDICATOR, OPT_FUSED_TWO_STAGE, OPT_BGK_CLOSURE = 1, 2, 3, 4
+OPT_BGK_TENSOR, OPT_FUSED_INDICATOR, OPT_FUSED_TWO_STAGE, OPT_BGK_CLOSURE, OPT_GHOSTS_PER_STEP = 1, 2, 3, 4, 5
 
 _D = C.POINTER(C.c_double)
 _F = C.POINTER(C.c_float)

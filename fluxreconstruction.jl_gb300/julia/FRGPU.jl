@@ -133,9 +133,14 @@ end
 """The `dudt!` of example/shock-vortex.jl:26-118 on the interior u[1:nx, 1:ny, :, :, :];
 `bc` = (left, right, bottom, top) kinds, `fixed` the 4x4 conserved ghost states."""
 function FREuler2DProblem(u::AbstractArray{<:Real,5}, tspan, ps, γ; flux=:hll, bc=(:period, :period, :period, :period),
-                          fixed=zeros(16), precision=:fp64)
+                          fixed=zeros(16), precision=:fp64, ghosts_per_step=false)
     bcs = ntuple(i -> BC[bc[i]], 4)
     p = Problem(Space2D(ps), desc(EULER2D, FLUX[flux], PRECISION[precision], bcs; γ=γ, fixed=fixed), size(u))
+    # ghosts_per_step: the periodic and copy ghosts keep the step's start values
+    # through the step, as the scripts refresh their ghost layers once per step
+    if ghosts_per_step
+        check(ccall((:frgpu_problem_set_option, libfrgpu), Cint, (Ptr{Cvoid}, Cint, Cint), p.h, 5, 1))
+    end
     return ODEProblem(rhs!, Array{Float64}(u), tspan, p)
 end
 

@@ -77,7 +77,8 @@ enum frgpu_option {
     FRGPU_OPT_BGK_TENSOR = 1,
     FRGPU_OPT_FUSED_INDICATOR = 2,
     FRGPU_OPT_FUSED_TWO_STAGE = 3,
-    FRGPU_OPT_BGK_CLOSURE = 4
+    FRGPU_OPT_BGK_CLOSURE = 4,
+    FRGPU_OPT_GHOSTS_PER_STEP = 5
 };
 
 typedef struct frgpu_space frgpu_space;
@@ -292,6 +293,13 @@ FRGPU_API int frgpu_troubled_flags(frgpu_problem *p, int *flags, long n);
  * density-only closure prim = [rho, a, 1], M = rho sqrt(1/pi) exp(-(v - a)^2),
  * a the problem's advection speed (example/advection_kinetic.jl:80-87, the
  * problem that script steps with ROCK4).
+ * FRGPU_OPT_GHOSTS_PER_STEP: 2D Euler.  0 (default): the periodic and copy
+ * neighbours outside the domain follow every stage's input.  1: they keep the
+ * values of the step's start through the step, as the reference scripts
+ * refresh their ghost layers once per step (example/shock-vortex.jl:323-330,
+ * example/euler2d_wave.jl:125-135; dudt! leaves du = 0 on the ghosts).  It
+ * applies to the fused steps (frgpu_step_ssprk3 and two-stage frgpu_step_erk);
+ * residual evaluations (frgpu_rhs, longer tableaux) have no step start.
  * The next step re-captures its graph. */
 FRGPU_API int frgpu_problem_set_option(frgpu_problem *p, int option, int value);
 /* Device pointer to the primary state array and its element type size

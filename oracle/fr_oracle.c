@@ -535,9 +535,24 @@ typedef struct {
     double *fyi;   /* [j(0..ny)][i][pt][m] */
 } e2d_work;
 
+/* element (i, j) (0-based) of a state in the reference layout into an
+ * element block of the ghost-extended work array */
+static void e2d_copy_elem(const fro_cfg *c, const double *u, int i, int j, double *dst) {
+    const int nx = c->nx, np = c->np;
+    const long nn = (long)nx * c->ny;
+    for (int m = 0; m < 4; ++m)
+        for (int l = 0; l < np; ++l)
+            for (int k = 0; k < np; ++k)
+                dst[(m * np + l) * np + k] = u[i + (long)nx * j + nn * (k + np * (l + (long)np * m))];
+}
+
 static void e2d_fill_ghosts(const fro_cfg *c, const double *u, e2d_work *w) {
     int nx = c->nx, ny = c->ny, np = c->np, E = w->E, nxg = w->nxg;
     long nn = (long)nx * ny;
+    /* with ghosts refreshed once per step the periodic and copy ghosts come from
+     * the step's start state (the scripts' dudt! leaves du = 0 on the ghosts,
+     * which they copy after each step) */
+    const double *gs = c->ghost_src;
 #ifdef _OPENMP
 #pragma omp parallel for OMP_THREADS
 #endif
@@ -560,7 +575,10 @@ static void e2d_fill_ghosts(const fro_cfg *c, const double *u, e2d_work *w) {
                     for (int q = 0; q < np * np; ++q) dst[m * np * np + q] = c->fixed_state[side][m];
             } else {
                 int src_i = bc == FRO_BC_PERIODIC ? (side == 0 ? nx : 1) : (side == 0 ? 1 : nx);
-                memcpy(dst, w->ug + ((long)j * nxg + src_i) * E, sizeof(double) * E);
+                if (gs)
+                    e2d_copy_elem(c, gs, src_i - 1, j - 1, dst);
+                else
+                    memcpy(dst, w->ug + ((long)j * nxg + src_i) * E, sizeof(double) * E);
             }
         }
     }
@@ -574,7 +592,10 @@ static void e2d_fill_ghosts(const fro_cfg *c, const double *u, e2d_work *w) {
                     for (int q = 0; q < np * np; ++q) dst[m * np * np + q] = c->fixed_state[side][m];
             } else {
                 int src_j = bc == FRO_BC_PERIODIC ? (side == 2 ? ny : 1) : (side == 2 ? 1 : ny);
-                memcpy(dst, w->ug + ((long)src_j * nxg + i) * E, sizeof(double) * E);
+                if (gs)
+                    e2d_copy_elem(c, gs, i - 1, src_j - 1, dst);
+                else
+                    memcpy(dst, w->ug + ((long)src_j * nxg + i) * E, sizeof(double) * E);
             }
         }
     }
@@ -920,18 +941,20 @@ void fro_ssprk3(const fro_cfg *c, double *u, double dt, int nsteps, double *work
     long n = fro_ndof(c);
     double *s = work, *k = work + n;
     const double third = 1.0 / 3.0;
+    fro_cfg cl = *c; /* the later stages: ghosts from u^n when refreshed once per step */
+    cl.ghost_src = c->kind == FRO_EULER2D && c->ghosts_per_step ? u : NULL;
     for (int it = 0; it < nsteps; ++it) {
         fro_rhs(c, k, u);
 #ifdef _OPENMP
 #pragma omp parallel for OMP_THREADS schedule(static)
 #endif
         for (long q = 0; q < n; ++q) s[q] = fma(dt, k[q], u[q]);
-        fro_rhs(c, k, s);
+        fro_rhs(&cl, k, s);
 #ifdef _OPENMP
 #pragma omp parallel for OMP_THREADS schedule(static)
 #endif
         for (long q = 0; q < n; ++q) s[q] = fma(dt, k[q], fma(3.0, u[q], s[q])) * 0.25;
-        fro_rhs(c, k, s);
+        fro_rhs(&cl, k, s);
 #ifdef _OPENMP
 #pragma omp parallel for OMP_THREADS schedule(static)
 #endif
@@ -960,6 +983,10 @@ void fro_erk(const fro_cfg *c, double *u, double dt, int nsteps, int s, const do
              double *work) {
     long n = fro_ndof(c);
     double *st = work, *k = work + n;
+    /* two-stage methods run fused on the GPU, where ghosts refreshed once per
+     * step apply: their second stage takes the ghosts from u^n */
+    fro_cfg cl = *c;
+    cl.ghost_src = c->kind == FRO_EULER2D && c->ghosts_per_step && s == 2 ? u : NULL;
     for (int it = 0; it < nsteps; ++it) {
         for (int i = 0; i < s; ++i) {
             int first = 1;
@@ -973,7 +1000,7 @@ void fro_erk(const fro_cfg *c, double *u, double dt, int nsteps, int s, const do
                 fro_rhs(c, k + i * n, u);
             else {
                 for (long q = 0; q < n; ++q) st[q] = fma(dt, st[q], u[q]);
-                fro_rhs(c, k + i * n, st);
+                fro_rhs(&cl, k + i * n, st);
             }
         }
         int first = 1;

@@ -79,6 +79,10 @@ typedef struct {
     int bgk_closure;           /* BGK Maxwellian: 0 conserve_prim(w, 3) (bgk_wave.jl),
                                   1 prim = [rho, a, 1] (advection_kinetic.jl) */
     double flux_c;             /* FRO_FLUX_CENTRAL: dissipation coefficient c */
+    int ghosts_per_step;       /* 2D: periodic and copy ghosts hold the step's start values through
+                                  the step (the scripts refresh their ghost layers once per step);
+                                  applies in fro_ssprk3 and two-stage fro_erk */
+    const double *ghost_src;   /* internal: the state the ghosts are copied from (NULL: the input) */
 } fro_cfg;
 
 long fro_ndof(const fro_cfg *c);

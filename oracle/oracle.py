@@ -53,6 +53,8 @@ class Cfg(C.Structure):
         ("iJ", _D), ("n1", _D), ("n2", _D), ("Ji", _D),
         ("bgk_closure", C.c_int),
         ("flux_c", C.c_double),
+        ("ghosts_per_step", C.c_int),
+        ("ghost_src", _D),
     ]
 
 
@@ -273,11 +275,12 @@ class Problem:
 
     def __init__(self, kind, space, *, flux=FLUX_ROE, a=1.0, gamma=1.4, tau=1e-2, bc=BC_PERIODIC,
                  bcs=None, fixed_states=None, velo=None, weights=None, eps_interior=1e-8,
-                 eps_periodic=1e-6, bgk_closure=0, flux_c=0.0):
+                 eps_periodic=1e-6, bgk_closure=0, flux_c=0.0, ghosts_per_step=0):
         c = Cfg()
         c.kind, c.flux = kind, flux
         c.bgk_closure = bgk_closure
         c.flux_c = flux_c
+        c.ghosts_per_step = ghosts_per_step
         c.nx = space.nx
         c.ny = getattr(space, "ny", 1)
         c.np = space.np

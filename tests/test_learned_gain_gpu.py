@@ -6,9 +6,10 @@ src/dissipation.jl:13-23) with the :l2 filter after every step
 of the FP32K kernel on the same features, so the comparison isolates the
 decision.  Workload: the shock-vortex problem (400 x 200, p = 3, HLL) at two
 vortex strengths, 600 steps from the initial state (the vortex meets the shock
-near step 150).  Accuracy: the L2 error of the density against a converged
-FP64 solution (the FP64 form, plain indicator, on the 2x refined mesh with
-half the step, evaluated at the coarse solution points).
+near step 150), with the ghosts refreshed once per step as the script does.
+Accuracy: the L2 error of the density against a converged FP64 solution (the
+FP64 form, plain indicator, on the 2x refined mesh with half the step,
+evaluated at the coarse solution points).
 
 Measured, and asserted here:
 * the indicator matters: without it the run loses positivity before step 600;

@@ -90,9 +90,10 @@ def vortex400(frgpu, oracle):
     ps = learned.config3_space()
     po = oracle_space2d(ps, 0, 2, 400, 0, 1, 200, 3)
     u, upstream = learned.shock_vortex_state(ps.xpg, 0.25)
+    # ghosts refreshed once per step, as the problem the library builds for this workload
     P = oracle.Problem(oracle.EULER2D, po, gamma=1.4, flux=oracle.FLUX_HLL,
                        bcs=[oracle.BC_FIXED, oracle.BC_COPY, oracle.BC_COPY, oracle.BC_COPY],
-                       fixed_states=[upstream, [0] * 4, [0] * 4, [0] * 4])
+                       fixed_states=[upstream, [0] * 4, [0] * 4, [0] * 4], ghosts_per_step=1)
     dt = _cfl_dt(u, ps.dx, ps.dy)
     return ps, u, P, dt
 
