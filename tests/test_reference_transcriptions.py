@@ -5,8 +5,8 @@ oracle):
   example/advection_kinetic.jl:73-128, with the scripts' own periodic face
   tables e2f / f2e (the conserve_prim(w, 3) closure and the density-only
   closure prim = [rho, a, 1]);
-* the library's frode_advection! (config 1) with its periodic and Dirichlet
-  boundary functions.
+* the library's frode_advection! (config 1) and frode_euler! with their
+  periodic and Dirichlet boundary functions.
 The 2D transcriptions sit beside their tests: tests/test_shock_vortex_script.py
 (example/shock-vortex.jl) and tests/test_curve_euler.py (dev/curve_euler.jl)."""
 import numpy as np
@@ -185,4 +185,86 @@ def test_oracle_advection_residual_is_frode_advection(frgpu, oracle, bc, deg):
     ref = frode_advection(u, np.full(nx, 0.5 / nx), np.asarray(ps.ll), np.asarray(ps.lr), np.asarray(ps.dl),
                           np.asarray(ps.dhl), np.asarray(ps.dhr), 1.0, bc)
     P = oracle.Problem(oracle.ADVECTION, po, a=1.0, bc=oracle.BC_PERIODIC if bc == "period" else oracle.BC_DIRICHLET)
+    np.testing.assert_allclose(P.rhs(u), ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+
+
+def hll_1d(wL, wR, g):
+    """HLL with Davis wave speeds, 1D (the restatement of KitBase.flux_hll!)."""
+    def parts(w):
+        rho, m, E = w
+        U = m / rho
+        p = (g - 1) * (E - 0.5 * m * U)
+        return np.array([m, m * U + p, (E + p) * U]), U, np.sqrt(g * p / rho)
+
+    fL, uL, cL = parts(wL)
+    fR, uR, cR = parts(wR)
+    sl, sr = min(uL - cL, uR - cR), max(uL + cL, uR + cR)
+    if sl >= 0:
+        return fL
+    if sr <= 0:
+        return fR
+    return (sr * fL - sl * fR + sl * sr * (wR - wL)) / (sr - sl)
+
+
+def frode_euler(u, J, ll, lr, lpdm, dgl, dgr, g, bc):
+    """frode_euler! (src/Equation/eq_euler.jl:29-73) with period_euler! /
+    dirichlet_euler! (:75-98)."""
+    ncell, nsp, _ = u.shape
+    f = np.zeros_like(u)
+    for j in range(nsp):
+        for i in range(ncell):
+            rho, m, E = u[i, j]
+            U = m / rho
+            p = (g - 1) * (E - 0.5 * m * U)
+            f[i, j] = np.array([m, m * U + p, (E + p) * U]) / J[i]
+    u_face = np.zeros((ncell, 2, 3))
+    f_face = np.zeros((ncell, 2, 3))
+    for k in range(3):
+        u_face[:, 0, k] = u[:, :, k] @ ll
+        f_face[:, 0, k] = f[:, :, k] @ ll
+        u_face[:, 1, k] = u[:, :, k] @ lr
+        f_face[:, 1, k] = f[:, :, k] @ lr
+    f_int = np.zeros((ncell + 1, 3))
+    for i in range(1, ncell):
+        f_int[i] = hll_1d(u_face[i - 1, 1], u_face[i, 0], g)
+    rhs1 = np.zeros_like(u)
+    for k in range(3):
+        rhs1[:, :, k] = f[:, :, k] @ lpdm.T
+    du = np.zeros_like(u)
+
+    def combine(i):
+        for p in range(nsp):
+            for k in range(3):
+                du[i, p, k] = -(rhs1[i, p, k] + (f_int[i, k] / J[i] - f_face[i, 0, k]) * dgl[p]
+                                + (f_int[i + 1, k] / J[i] - f_face[i, 1, k]) * dgr[p])
+
+    for i in range(1, ncell - 1):
+        combine(i)
+    if bc == "period":
+        f_int[0] = hll_1d(u_face[ncell - 1, 1], u_face[0, 0], g)
+        f_int[ncell] = hll_1d(u_face[ncell - 1, 1], u_face[0, 0], g)
+        for i in (0, ncell - 1):
+            combine(i)
+    return du
+
+
+@pytest.mark.parametrize("bc", ["period", "dirichlet"])
+@pytest.mark.parametrize("deg", [1, 2, 3])
+def test_oracle_euler1d_residual_is_frode_euler(frgpu, oracle, bc, deg):
+    """The 1D Euler residual of euler_highlevel.jl's FREulerProblem against the
+    oracle (HLL restated, as in the 2D transcription)."""
+    nx, g = 29, 1.4
+    ps = frgpu.FRPSpace1D(0, 1, nx, deg)
+    po = oracle_space1d(ps, 0, 1, nx, deg)
+    x = np.asarray(ps.xpg)
+    rng = np.random.default_rng(11 + deg)
+    rho = 1 + 0.2 * np.sin(2 * np.pi * x) + 0.01 * rng.standard_normal(x.shape)
+    U = 0.5 + 0.1 * np.cos(2 * np.pi * x)
+    p = 1 + 0.1 * np.sin(4 * np.pi * x)
+    u = np.zeros(x.shape + (3,), order="F")
+    u[..., 0], u[..., 1], u[..., 2] = rho, rho * U, p / (g - 1) + 0.5 * rho * U * U
+    ref = frode_euler(u, np.full(nx, 0.5 / nx), np.asarray(ps.ll), np.asarray(ps.lr), np.asarray(ps.dl),
+                      np.asarray(ps.dhl), np.asarray(ps.dhr), g, bc)
+    P = oracle.Problem(oracle.EULER1D, po, gamma=g, flux=oracle.FLUX_HLL,
+                       bc=oracle.BC_PERIODIC if bc == "period" else oracle.BC_DIRICHLET)
     np.testing.assert_allclose(P.rhs(u), ref, rtol=0, atol=1e-12 * np.abs(ref).max())
