@@ -6,13 +6,14 @@ oracle):
   tables e2f / f2e (the conserve_prim(w, 3) closure and the density-only
   closure prim = [rho, a, 1]);
 * the library's frode_advection! (config 1) and frode_euler! with their
-  periodic and Dirichlet boundary functions.
+  periodic and Dirichlet boundary functions;
+* the indicator + :l2 filter loop of example/shock-vortex.jl:308-321.
 The 2D transcriptions sit beside their tests: tests/test_shock_vortex_script.py
 (example/shock-vortex.jl) and tests/test_curve_euler.py (dev/curve_euler.jl)."""
 import numpy as np
 import pytest
 
-from test_parity_gpu import oracle_space1d
+from test_parity_gpu import oracle_space1d, oracle_space2d
 
 
 def face_tables(nx):
@@ -268,3 +269,53 @@ def test_oracle_euler1d_residual_is_frode_euler(frgpu, oracle, bc, deg):
     P = oracle.Problem(oracle.EULER1D, po, gamma=g, flux=oracle.FLUX_HLL,
                        bc=oracle.BC_PERIODIC if bc == "period" else oracle.BC_DIRICHLET)
     np.testing.assert_allclose(P.rhs(u), ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+
+
+def script_filter_loop(u, V, iV, deg, lam=5e-4, kappa=9.0):
+    """The indicator + filter loop of example/shock-vortex.jl:308-321 (its 1:3
+    blocks are p = 2), with shock_detector (src/dissipation.jl:13-23) and
+    KitBase's :l2 modal_filter! restated (u_q / (1 + lam q^2 (q + 1)^2) on the
+    flat mode index)."""
+    import math
+
+    u = u.copy()
+    flags = np.zeros(u.shape[:2], dtype=int)
+    S0 = -3.0 * math.log10(deg)
+    q = np.arange(u.shape[2] * u.shape[3])
+    for i in range(u.shape[0]):
+        for j in range(u.shape[1]):
+            uh = iV @ u[i, j, :, :, 0].ravel(order="F")
+            su = uh[-1] ** 2 / np.sum(uh ** 2)
+            Se = math.log10(su) if su > 0 else -math.inf
+            if Se < S0 - kappa:
+                sigma = 1.0
+            elif S0 - kappa <= Se < S0 + kappa:
+                sigma = 0.5 * (1.0 - math.sin(0.5 * math.pi * (Se - S0) / kappa))
+            else:
+                sigma = 0.0
+            if sigma < 0.99:
+                flags[i, j] = 1
+                for s in range(4):
+                    uh = iV @ u[i, j, :, :, s].ravel(order="F")
+                    uh = uh / (1 + lam * (q * q) * (q + 1) ** 2)
+                    u[i, j, :, :, s] = (V @ uh).reshape(u.shape[2], u.shape[3], order="F")
+    return u, flags
+
+
+def test_oracle_filter_is_the_script_loop(frgpu, oracle):
+    """The post-step filter of the shock-vortex script (p = 2, lambda = 5e-4,
+    kappa = 9) on a state with smooth and discontinuous elements: the same
+    elements flagged and the same filtered state as the oracle."""
+    nx, ny, deg = 12, 7, 2
+    ps = frgpu.FRPSpace2D(0, 2, nx, 0, 1, ny, deg)
+    po = oracle_space2d(ps, 0, 2, nx, 0, 1, ny, deg)
+    X, Y = ps.xpg[..., 0], ps.xpg[..., 1]
+    rho = np.where(X < 0.7 + 0.3 * Y, 1.0, 1.6) + 0.05 * np.sin(5 * X) * np.cos(3 * Y)
+    u = np.zeros(X.shape + (4,), order="F")
+    u[..., 0], u[..., 1], u[..., 2], u[..., 3] = rho, 0.3 * rho, 0.1 * rho, 2.5 + 0.05 * rho
+    ref, ref_flags = script_filter_loop(u, np.asarray(ps.V), np.asarray(ps.iV), deg)
+    P = oracle.Problem(oracle.EULER2D, po, gamma=1.4, flux=oracle.FLUX_HLL)
+    got, flags, n = P.filter2d(u, 5e-4, -3.0 * np.log10(deg), 9.0)
+    assert 0 < n < nx * ny
+    np.testing.assert_array_equal(flags, ref_flags)
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-13)
