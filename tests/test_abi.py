@@ -145,3 +145,27 @@ def test_allocation_free_reduction_calls_no_allocator():
     assert "frgpu_reduce2d_noalloc" in body
     for call in ("cudaMalloc", "cudaFree", "malloc(", "calloc(", "new ", "std::vector", "cudaHostAlloc"):
         assert call not in body, call
+
+
+def _c_param_counts():
+    """{name: number of parameters} of every FRGPU_API declaration."""
+    text = re.sub(r"/\*.*?\*/", " ", open(HEADER).read(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"FRGPU_API\s+[\w\s\*]+?\b(frgpu_\w+)\s*\(([^)]*)\)", text):
+        params = [p.strip() for p in m.group(2).split(",") if p.strip() and p.strip() != "void"]
+        out[m.group(1)] = len(params)
+    return out
+
+
+def test_julia_binding_calls_declared_entry_points():
+    """Every ccall of the Julia shim (julia/FRGPU.jl) names an entry point that
+    include/frgpu.h declares, with as many argument types as the C function has
+    parameters."""
+    jl = open(os.path.join(ROOT, "fluxreconstruction.jl_gb300", "julia", "FRGPU.jl")).read()
+    counts = _c_param_counts()
+    calls = re.findall(r"ccall\(\(:(frgpu_\w+),\s*libfrgpu\),\s*[\w{}]+,\s*\(([^()]*(?:\([^()]*\)[^()]*)*)\)", jl)
+    assert len(calls) >= 20
+    for name, types in calls:
+        assert name in counts, name
+        n = len([t for t in types.split(",") if t.strip()])
+        assert n == counts[name], (name, n, counts[name])
