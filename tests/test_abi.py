@@ -157,14 +157,15 @@ def _c_param_counts():
     return out
 
 
-def test_julia_binding_calls_declared_entry_points():
-    """Every ccall of the Julia shim (julia/FRGPU.jl) names an entry point that
-    include/frgpu.h declares, with as many argument types as the C function has
-    parameters."""
-    jl = open(os.path.join(ROOT, "fluxreconstruction.jl_gb300", "julia", "FRGPU.jl")).read()
+@pytest.mark.parametrize("path", [("fluxreconstruction.jl_gb300", "julia", "FRGPU.jl"), ("INTEGRATION.md",)])
+def test_julia_binding_calls_declared_entry_points(path):
+    """Every ccall of the Julia shim (julia/FRGPU.jl) and of the integration
+    notes names an entry point that include/frgpu.h declares, with as many
+    argument types as the C function has parameters."""
+    jl = open(os.path.join(ROOT, *path)).read()
     counts = _c_param_counts()
     calls = re.findall(r"ccall\(\(:(frgpu_\w+),\s*libfrgpu\),\s*[\w{}]+,\s*\(([^()]*(?:\([^()]*\)[^()]*)*)\)", jl)
-    assert len(calls) >= 20
+    assert len(calls) >= 20 and len(calls) == len(re.findall(r"ccall\(\(:frgpu_", jl))
     for name, types in calls:
         assert name in counts, name
         n = len([t for t in types.split(",") if t.strip()])
