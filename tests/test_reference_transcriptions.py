@@ -7,7 +7,8 @@ oracle):
   closure prim = [rho, a, 1]);
 * the library's frode_advection! (config 1) and frode_euler! with their
   periodic and Dirichlet boundary functions;
-* the indicator + :l2 filter loop of example/shock-vortex.jl:308-321.
+* the indicator + :l2 filter loop of example/shock-vortex.jl:308-321;
+* the scalar positive_limiter (src/dissipation.jl:38-58).
 The 2D transcriptions sit beside their tests: tests/test_shock_vortex_script.py
 (example/shock-vortex.jl) and tests/test_curve_euler.py (dev/curve_euler.jl)."""
 import numpy as np
@@ -319,3 +320,40 @@ def test_oracle_filter_is_the_script_loop(frgpu, oracle):
     assert 0 < n < nx * ny
     np.testing.assert_array_equal(flags, ref_flags)
     np.testing.assert_allclose(got, ref, rtol=0, atol=1e-13)
+
+
+def positive_limiter_vector(u, weights, ll, lr):
+    """positive_limiter(u::AbstractVector, weights, ll, lr) (src/dissipation.jl:38-58)."""
+    u = u.copy()
+    um = np.sum(u * weights) / np.sum(weights)
+    ub = [np.dot(u, ll), np.dot(u, lr)]
+    eps = min(1e-13, um)
+    theta = min(min(ub), np.min(u))
+    t = min((um - eps) / (um - theta + 1e-8), 1.0)
+    assert 0 < t <= 1
+    return t * (u - um) + um
+
+
+def test_oracle_limiter_is_positive_limiter(frgpu, oracle):
+    """The scalar positive_limiter against the oracle's restatement: elements
+    whose traces dip below zero are pulled toward their mean, the others stay.
+    (The Euler form cannot be run as the reference writes it once it acts: a
+    negative density at a trace sends it into the energy corrector, whose
+    `minimum(tj, t0)` (src/dissipation.jl:116, :199) has no method; the oracle
+    restates the intended t2 = min(minimum(tj), t0).)"""
+    nx, deg = 24, 3
+    ps = frgpu.FRPSpace1D(0, 1, nx, deg)
+    po = oracle_space1d(ps, 0, 1, nx, deg)
+    ll, lr, w = np.asarray(ps.ll), np.asarray(ps.lr), np.asarray(ps.wp) / 2.0
+    rng = np.random.default_rng(9)
+    # per element a positive mean m with a linear slope A (up to 1.5 m): the
+    # traces of the steeper elements go negative
+    xi = np.asarray(ps.xpl)[None, :]
+    m = rng.uniform(0.2, 1.0, (nx, 1))
+    A = rng.uniform(0.0, 1.5, (nx, 1)) * m
+    s = np.asfortranarray(m + A * xi)
+    ref = np.stack([positive_limiter_vector(s[i], w, ll, lr) for i in range(nx)])
+    got, _ = oracle.Problem(oracle.ADVECTION, po, a=1.0).positive_limiter(s, w)
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-14)
+    limited = np.abs(ref - s).max(axis=1) > 1e-12
+    assert 0 < limited.sum() < nx
