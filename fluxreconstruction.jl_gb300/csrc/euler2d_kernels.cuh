@@ -44,6 +44,8 @@ template <class Real, int NP> struct E2DArgs {
     // ghosts refreshed once per step (the reference scripts copy their ghost
     // layers after each step): in the later stages of a step the periodic and
     // copy neighbours outside the domain are read from u^n, not the stage input
+    // (stage 0, a residual evaluation inside an explicit or stabilised step:
+    // from un, the step's start state)
     int lag;
     Real fixed[4][4];
     Ops<Real, NP> ops;
@@ -301,8 +303,8 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             if (resolve(jn, ny, a.bc[2], a.bc[3], jo)) {
                 const unsigned en = (unsigned)(i0 + hx) + (unsigned)nx * jo;
                 // a ghost outside the domain with ghosts refreshed once per step: u^n
-                const bool lag = STAGE >= 2 && a.lag && (jn < 0 || jn >= ny);
-                const Real *src = MODE == MODE_FP64 && lag ? a.un : uin;
+                const bool lag = (STAGE >= 2 || STAGE == 0) && a.lag && (jn < 0 || jn >= ny);
+                const Real *src = (MODE == MODE_FP64 || STAGE == 0) && lag ? a.un : uin;
                 const Real *dsrc = lag ? nullptr : din;
                 Real v[NP][4], h[4];
 #pragma unroll
@@ -332,8 +334,8 @@ __global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
             int io;
             if (resolve(in_, nx, a.bc[0], a.bc[1], io)) {
                 const unsigned en = (unsigned)io + (unsigned)nx * (j0 + hy);
-                const bool lag = STAGE >= 2 && a.lag && (in_ < 0 || in_ >= nx);
-                const Real *src = MODE == MODE_FP64 && lag ? a.un : uin;
+                const bool lag = (STAGE >= 2 || STAGE == 0) && a.lag && (in_ < 0 || in_ >= nx);
+                const Real *src = (MODE == MODE_FP64 || STAGE == 0) && lag ? a.un : uin;
                 const Real *dsrc = lag ? nullptr : din;
                 Real v[NP][4], h[4];
 #pragma unroll
@@ -734,6 +736,10 @@ int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
         for (int m = 0; m < 4; ++m) a.fixed[s][m] = (Real)p->d.fixed_state[s][m];
     }
     a.lag = p->ghosts_per_step;
+    if (STAGE == 0) { // a residual inside a step: the step's start state, when the stepper gives one
+        a.lag = p->ghosts_per_step && p->lag_src != nullptr;
+        if (a.lag) a.un = (const Real *)p->lag_src;
+    }
     a.ops = make_ops<Real, NP>(p->sp);
     a.status = p->d_status;
     a.mlp = frmlp::MLPDev{nullptr, nullptr, nullptr, nullptr, nullptr};

@@ -68,7 +68,8 @@ struct frgpu_problem {
     float mlp_thr = 0.5f, mlp_band = 0.0f;
     int bgk_tensor = 1;             // FP32 BGK transport on the tensor cores
     int bgk_closure = 0;            // BGK Maxwellian: 0 conserve_prim(w, 3), 1 prim = [rho, a, 1]
-    int ghosts_per_step = 0;        // 2D fused steps: ghost neighbours from u^n in the later stages
+    int ghosts_per_step = 0;        // 2D steps: ghost neighbours from u^n in the later stages
+    const void *lag_src = nullptr;  // while an explicit / stabilised step is enqueued: its u^n
     // page-locked host words the status and reduction results come back into
     // (one copy engine transfer each, no staging through pageable memory)
     struct host_words {

@@ -389,10 +389,18 @@ static int enqueue_step(frgpu_problem *p) {
 // One explicit Runge-Kutta step (limiter before it, filter after it).
 static int residual_into(frgpu_problem *p, const void *in, void *out) { return launch_stage(p, 0, in, nullptr, out); }
 
+// u^n of a step, for residual evaluations whose ghosts stay at the step's start
+static const void *step_start_state(frgpu_problem *p) {
+    return p->ghosts_per_step && p->d.equation == FRGPU_EULER2D ? fr_state_hi(p) : nullptr;
+}
+
 static int enqueue_erk(frgpu_problem *p) {
     int rc;
     if (p->limiter && (rc = fr_launch_limiter(p, p->lim_w, p->lim_t0))) return rc;
-    if ((rc = fr_enqueue_erk_step(p, residual_into))) return rc;
+    p->lag_src = step_start_state(p);
+    rc = fr_enqueue_erk_step(p, residual_into);
+    p->lag_src = nullptr;
+    if (rc) return rc;
     if (p->indicator != FRGPU_IND_NONE) {
         // the high part stays in place (no parity flip); the learned indicator
         // runs as its own kernel (its fused form lives in SSPRK3's stage 3)
@@ -781,7 +789,10 @@ static int enqueue_rock(frgpu_problem *p, fr_rock_raw r) {
     int rc;
     if (p->limiter && (rc = fr_launch_limiter(p, p->lim_w, p->lim_t0))) return rc;
     r.prepare_only = p->prepare_only;
-    if ((rc = fr_rock_enqueue_raw(r, residual_ctx, p))) return rc;
+    p->lag_src = step_start_state(p);
+    rc = fr_rock_enqueue_raw(r, residual_ctx, p);
+    p->lag_src = nullptr;
+    if (rc) return rc;
     if (p->indicator != FRGPU_IND_NONE) {
         rc = p->sp.dim == 2 ? fr_launch_filter2d(p, p->indicator, p->lam, p->S0, p->kappa)
                             : fr_launch_filter1d(p, p->indicator, p->lam, p->S0, p->kappa);

@@ -298,8 +298,8 @@ FRGPU_API int frgpu_troubled_flags(frgpu_problem *p, int *flags, long n);
  * values of the step's start through the step, as the reference scripts
  * refresh their ghost layers once per step (example/shock-vortex.jl:323-330,
  * example/euler2d_wave.jl:125-135; dudt! leaves du = 0 on the ghosts).  It
- * applies to the fused steps (frgpu_step_ssprk3 and two-stage frgpu_step_erk);
- * residual evaluations (frgpu_rhs, longer tableaux) have no step start.
+ * applies to every step (frgpu_step_ssprk3, frgpu_step_erk, frgpu_step_rock);
+ * a lone residual evaluation (frgpu_rhs) has no step start.
  * The next step re-captures its graph. */
 FRGPU_API int frgpu_problem_set_option(frgpu_problem *p, int option, int value);
 /* Device pointer to the primary state array and its element type size

@@ -983,10 +983,9 @@ void fro_erk(const fro_cfg *c, double *u, double dt, int nsteps, int s, const do
              double *work) {
     long n = fro_ndof(c);
     double *st = work, *k = work + n;
-    /* two-stage methods run fused on the GPU, where ghosts refreshed once per
-     * step apply: their second stage takes the ghosts from u^n */
+    /* ghosts refreshed once per step: the stages after the first take them from u^n */
     fro_cfg cl = *c;
-    cl.ghost_src = c->kind == FRO_EULER2D && c->ghosts_per_step && s == 2 ? u : NULL;
+    cl.ghost_src = c->kind == FRO_EULER2D && c->ghosts_per_step ? u : NULL;
     for (int it = 0; it < nsteps; ++it) {
         for (int i = 0; i < s; ++i) {
             int first = 1;
@@ -1029,10 +1028,12 @@ void fro_rock(const fro_cfg *c, double *u, double dt, int nsteps, int m, const d
     long n = fro_ndof(c);
     double *D[3] = {work, work + n, work + 2 * n};
     double *F0 = work + 3 * n, *F = work + 4 * n, *Y = work + 5 * n, *S = work + 6 * n, *K = work + 7 * n;
+    fro_cfg cl = *c; /* stage inputs: ghosts from u^n when refreshed once per step */
+    cl.ghost_src = c->kind == FRO_EULER2D && c->ghosts_per_step ? u : NULL;
     for (int it = 0; it < nsteps; ++it) {
         fro_rhs(c, F0, u);
         for (int j = 1; j <= m; ++j) {
-            if (j >= 2) fro_rhs(c, F, Y);
+            if (j >= 2) fro_rhs(&cl, F, Y);
             const double *Fj = j == 1 ? F0 : F;
             const double al = alpha[j - 1], be = beta[j - 1], mj = mu[j - 1], de = delta[j - 1];
             double *Dj = D[j % 3];
@@ -1057,10 +1058,10 @@ void fro_rock(const fro_cfg *c, double *u, double dt, int nsteps, int m, const d
                 first = 0;
             }
             if (first)
-                fro_rhs(c, K + i * n, Y);
+                fro_rhs(&cl, K + i * n, Y);
             else {
                 for (long q = 0; q < n; ++q) S[q] = u[q] + fma(dt, S[q], Dm[q]);
-                fro_rhs(c, K + i * n, S);
+                fro_rhs(&cl, K + i * n, S);
             }
         }
         int first = 1;

@@ -81,7 +81,7 @@ typedef struct {
     double flux_c;             /* FRO_FLUX_CENTRAL: dissipation coefficient c */
     int ghosts_per_step;       /* 2D: periodic and copy ghosts hold the step's start values through
                                   the step (the scripts refresh their ghost layers once per step);
-                                  applies in fro_ssprk3 and two-stage fro_erk */
+                                  applies in fro_ssprk3, fro_erk and fro_rock */
     const double *ghost_src;   /* internal: the state the ghosts are copied from (NULL: the input) */
 } fro_cfg;
 

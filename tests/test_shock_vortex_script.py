@@ -200,3 +200,24 @@ def test_ghosts_per_step_bit_identical(frgpu, oracle, deg):
     it32 = frgpu.init(gpu_problem(frgpu, u, ps, "fp32k"), dt=dt)
     it32.step(6)
     assert np.abs(it32.u - ref).max() < 2e-6 * np.abs(ref).max()
+
+
+@pytest.mark.gpu
+def test_ghosts_per_step_in_every_stepper(frgpu, oracle):
+    """The generic explicit step (RK4) and a stabilised step keep the ghosts at
+    the step's start as well: FP64 bit-identical to the oracle's fro_erk /
+    fro_rock with ghosts refreshed once per step; per-stage ghosts differ."""
+    ps, u = case(frgpu, nx=32, ny=18, deg=3)
+    dt = 1e-3
+    rk4 = frgpu.RK4()
+    it = frgpu.init(gpu_problem(frgpu, u, ps), rk4, dt=dt)
+    it.step(4)
+    ref = oracle_problem(oracle, ps, 1).erk(u, dt, 4, rk4.A, rk4.b)
+    np.testing.assert_array_equal(it.u, ref)
+    assert np.abs(oracle_problem(oracle, ps, 0).erk(u, dt, 4, rk4.A, rk4.b) - ref).max() > 0
+    al, be, mu, de, _ = frgpu.rkc2_coefficients(5)
+    A = np.array([[0, 0], [0.5, 0]], dtype=float)
+    b = np.array([0.0, 1.0])
+    itr = frgpu.init(gpu_problem(frgpu, u, ps), dt=dt)
+    itr.step_rock(al, be, mu, de, A, b, n=3)
+    np.testing.assert_array_equal(itr.u, oracle_problem(oracle, ps, 1).rock(u, dt, 3, al, be, mu, de, A, b))
