@@ -322,13 +322,29 @@ __global__ void __launch_bounds__(256) k_norm2(const Real *__restrict__ x, const
         last = atomicAdd(cnt, 1u) == gridDim.x - 1;
     }
     __syncthreads();
-    if (!last || threadIdx.x != 0) return;
+    if (!last || threadIdx.x >= 32) return;
     __threadfence();
+    // warp 0 of the last block: lane l sums blocks l, l + 32, ... (loads issued
+    // together, 19 per lane at most), then a fixed butterfly
+    const int lane = threadIdx.x;
     double t = 0.0;
-    for (unsigned b = 0; b < gridDim.x; ++b) t += __ldcg(part + b);
-    *host_out = sqrt(t);
-    *host_status = __ldcg(dstatus); // the device status word as of this norm
-    *cnt = 0u;                      // ready for the next launch
+    constexpr int B = 20;
+    for (unsigned b0 = 0; b0 < gridDim.x; b0 += 32 * B) {
+        double y[B];
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+            const unsigned b = b0 + lane + 32 * k;
+            y[k] = b < gridDim.x ? __ldcg(part + b) : 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < B; ++k) t += y[k];
+    }
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    if (lane == 0) {
+        *host_out = sqrt(t);
+        *host_status = __ldcg(dstatus); // the device status word as of this norm
+        *cnt = 0u;                      // ready for the next launch
+    }
 }
 
 template <class Real> __global__ void __launch_bounds__(256) k_fill(Real *__restrict__ v, double c, size_t n) {
