@@ -82,8 +82,8 @@ S0 = -3.0 * math.log10(DEG)
 BYTES_PER_DOF_STAGE = {"fp32k": 4 * 8 / 3, "fp64": 8 * 8 / 3}
 # DRAM bytes (read + write) per stage launch of the bare FP32K stage kernel on
 # the 512 x 512 density wave, mean over the three SSPRK3 stages, from the ncu
-# capture summarised in profiles/euler2d_stage_512x512_p3.md.
-NCU_TRAFFIC_PER_LAUNCH = {"fp32k": 188.7e6, "fp64": None}
+# capture summarised in profiles/euler2d_stage_tiles16x4_512x512_p3.md.
+NCU_TRAFFIC_PER_LAUNCH = {"fp32k": 187.0e6, "fp64": None}
 L2_FLUSH_BYTES = 512 << 20  # four times the 129 MB L2
 
 

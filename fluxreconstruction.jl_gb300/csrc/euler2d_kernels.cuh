@@ -6,8 +6,9 @@
 // element and applies one Shu-Osher SSPRK3 stage update to it.  The state is
 // in the point-vector device layout (e2d_index: the 4 variables of a solution
 // point together, element index fastest within a point's plane), so a thread
-// moves a point with one 16-byte access and a warp of 32 consecutive elements
-// reads a point plane with one contiguous 512-byte (FP32) or 1 KB (FP64) access.
+// moves a point with one 16-byte access and the TX consecutive elements of a
+// tile row read a point plane with one contiguous TX x 16-byte access (256 or
+// 512 bytes in FP32, 1 KB in FP64).
 //
 // CTA = TX x TY elements.  Thread (ex, ln, ey) is first an "x-line" thread
 // (element ex, row s = ln: it owns the NP points along r) and later a
@@ -81,18 +82,23 @@ template <class Real, int NP> struct E2DArgs {
     int *flags, *stats;
 };
 
-template <class Real, int NP> struct Tile;
-// Tile shapes: TX elements along x (one warp), TY rows.
+template <class Real, int NP, int FUSE = 0, int STAGE = 0> struct Tile;
+// Tile shapes: TX elements along x, TY rows; TX x NP x TY threads.
 // Shared memory per CTA (see Smem below) stays under 227 KB:
 // FP64 NP=3/TY=4 158 KB, NP=4/TY=2 122 KB, NP=5/TY=1 98 KB, NP=6/TY=1 130 KB;
 // FP32 NP=2/TY=8 86 KB, NP=4/TY=2 61 KB, NP=6/TY=1 65 KB.
-template <int NP> struct Tile<double, NP> {
+template <int NP, int FUSE, int STAGE> struct Tile<double, NP, FUSE, STAGE> {
     static constexpr int TX = 32;
     static constexpr int TY = NP <= 3 ? 4 : (NP == 4 ? 2 : 1);
 };
-template <int NP> struct Tile<float, NP> {
-    static constexpr int TX = 32;
-    static constexpr int TY = NP <= 2 ? 8 : (NP <= 4 ? 2 : 1);
+// FP32 np = 4: the residual and stages 1-2 take 16 x 4 tiles (40 halo traces per
+// 64 elements instead of 68: 7 % and 3 % faster than 32 x 2 on the 512^2 density
+// wave); stage 3, which also streams the low part, and the fused indicator keep
+// 32 x 2 (8 x 8 tiles measured slower in every stage).
+template <int NP, int FUSE, int STAGE> struct Tile<float, NP, FUSE, STAGE> {
+    static constexpr bool V = NP == 4 && FUSE == 0 && STAGE != 3;
+    static constexpr int TX = V ? 16 : 32;
+    static constexpr int TY = V ? 4 : (NP <= 2 ? 8 : (NP <= 4 ? 2 : 1));
 };
 
 // NST: state-sized stash arrays holding the stage update's extra inputs,
@@ -190,10 +196,10 @@ template <class Real> __device__ __forceinline__ void get4(const Real *p, int cs
 // corrections scale the interface fluxes by a11 and a22 at each point, as the
 // dudt! closure of example/shock-vortex.jl:48-55, :102-115 does with iJ[i, j][k, l]).
 template <class Real, int NP, int FLUX, int MODE, int STAGE, int FUSE = FUSE_NONE, bool MET = false>
-__global__ void __launch_bounds__(Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY,
-                                  sizeof(Real) == 4 && Tile<Real, NP>::TX * NP * Tile<Real, NP>::TY <= 256 ? 3 : 1)
+__global__ void __launch_bounds__(Tile<Real, NP, FUSE, STAGE>::TX * NP * Tile<Real, NP, FUSE, STAGE>::TY,
+                                  sizeof(Real) == 4 && Tile<Real, NP, FUSE, STAGE>::TX * NP * Tile<Real, NP, FUSE, STAGE>::TY <= 256 ? 3 : 1)
     k_euler2d(const E2DArgs<Real, NP> a) {
-    constexpr int TX = Tile<Real, NP>::TX, TY = Tile<Real, NP>::TY;
+    constexpr int TX = Tile<Real, NP, FUSE, STAGE>::TX, TY = Tile<Real, NP, FUSE, STAGE>::TY;
     constexpr int NT = TX * NP * TY;
     constexpr int NST = Stash<MODE, STAGE>::n;
     using S = Smem<Real, NP, TX, TY, NST>;
@@ -716,7 +722,7 @@ template <class Real, int NP> Ops<Real, NP> make_ops(const frgpu_space &s) {
 
 template <class Real, int NP, int FLUX, int MODE, int STAGE, int FUSE = FUSE_NONE, bool MET = false>
 int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
-    using T = Tile<Real, NP>;
+    using T = Tile<Real, NP, FUSE, STAGE>;
     using S = Smem<Real, NP, T::TX, T::TY, Stash<MODE, STAGE>::n>;
     E2DArgs<Real, NP> a;
     a.nx = p->sp.nx;
