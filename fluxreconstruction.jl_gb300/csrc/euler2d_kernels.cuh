@@ -651,26 +651,31 @@ __global__ void __launch_bounds__(Tile<Real, NP, FUSE, STAGE>::TX * NP * Tile<Re
             }
             float feat[16], su = 0.f;
             features_from_raw(w, ev, pr, a.iv1, (float)a.gm1, feat, su);
+            // elements the network is consulted for (su is valid on the lower lanes)
+            [[maybe_unused]] const bool cand = !pr && ev && !below_floor(su, a.ind_S0, a.ind_kappa);
             if constexpr (FUSE == FUSE_LEARNED) {
-                store_features_bf16(xs + (lane & 15) * NIN + (pr ? 16 : 0), feat);
-                __syncwarp();
-                Fwd f;
-                // 12 KB of weights, L1-resident; warp-level mma.sync: the tcgen05 routine of the
-                // stand-alone kernel measured slower here (per-CTA TMEM allocation, weight
-                // copy and two MMA round trips for only 64 elements)
-                mlp_forward_tile(global_view(a.mlp), xs, f);
-                if ((lane & 3) == 0) {
-                    prob[lane >> 2] = sigmoidf_(f.logit_g);
-                    prob[(lane >> 2) + 8] = sigmoidf_(f.logit_g8);
+                // a warp whose 16 elements are all below the smooth floor skips the network
+                if (__any_sync(0xffffffffu, cand)) {
+                    store_features_bf16(xs + (lane & 15) * NIN + (pr ? 16 : 0), feat);
+                    __syncwarp();
+                    Fwd f;
+                    // 12 KB of weights, L1-resident; warp-level mma.sync: the tcgen05 routine of the
+                    // stand-alone kernel measured slower here (per-CTA TMEM allocation, weight
+                    // copy and two MMA round trips for only 64 elements)
+                    mlp_forward_tile(global_view(a.mlp), xs, f);
+                    if ((lane & 3) == 0) {
+                        prob[lane >> 2] = sigmoidf_(f.logit_g);
+                        prob[(lane >> 2) + 8] = sigmoidf_(f.logit_g8);
+                    }
+                    __syncwarp();
                 }
-                __syncwarp();
             }
             bool tr = false;
             int n_tr = 0, n_mis = 0, n_fb = 0;
             if (!pr && ev) {
                 const bool plain = plain_troubled(su, a.ind_S0, a.ind_kappa);
                 if constexpr (FUSE == FUSE_LEARNED) {
-                    const float pm = prob[lane];
+                    const float pm = cand ? prob[lane] : 0.f;
                     const bool fb = fabsf(pm - a.ind_thr) < a.ind_band, net = pm > a.ind_thr;
                     tr = fb ? plain : net;
                     n_mis = net != plain;

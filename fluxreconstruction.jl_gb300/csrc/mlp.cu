@@ -349,7 +349,8 @@ __global__ void __launch_bounds__(128) k_features(const Real *__restrict__ u, si
 // Learned indicator + :l2 modal filter on a 2D Euler state (np = 4).  Per
 // element: features -> MLP -> probability.  Where the probability is within
 // `band` of `thr` the plain modal-decay test decides (fallback); otherwise the
-// network does.  stats: [0] troubled, [1] network vs plain disagreements
+// network does, except below the smooth floor (below_floor) where the element
+// is smooth.  stats: [0] troubled, [1] network vs plain disagreements
 // (misfires, judged by the plain test), [2] fallbacks.
 // The learned indicator + :l2 filter over a 2D state (np = 4), persistent: a
 // CTA of four warps takes groups of 64 consecutive elements; warp w holds
@@ -393,7 +394,7 @@ __global__ void __launch_bounds__(32 * WARPS, 4) k_mlp_indicator(MLPDev w, Real 
         bool bad = false;
         if (!pr && e < ne) {
             const bool plain = plain_troubled(su, S0, kappa);
-            const float pm = prob[lane];
+            const float pm = below_floor(su, S0, kappa) ? 0.f : prob[lane];
             const bool fallback = fabsf(pm - thr) < band;
             const bool net = pm > thr;
             bad = fallback ? plain : net;

@@ -437,6 +437,12 @@ __device__ __forceinline__ void features_from_raw(const float (&w)[8][4], bool v
     modal_features16(v, valid, iv, feat, su);
 }
 
+// Where the modal decay leaves no doubt, below the plain test's sigma = 1 region
+// (Se = log10 su < S0 - kappa: smooth, with more than a decade of margin to the
+// plain decision at Se = S0 - 0.87 kappa), the learned indicator takes the element
+// as smooth without consulting the network; the network decides everywhere else.
+__device__ __forceinline__ bool below_floor(float su, float S0, float kappa) { return log10f(su) < S0 - kappa; }
+
 // The plain modal-decay test (shock_detector, src/dissipation.jl:13-23) in FP32.
 __device__ __forceinline__ bool plain_troubled(float su, float S0, float kappa) {
     const float Se = log10f(su);

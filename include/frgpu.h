@@ -345,7 +345,9 @@ FRGPU_API int frgpu_mlp_train(frgpu_mlp *m, const float *x, const float *t, long
                               int seed, float *loss_out);
 /* Bind a network to a 2D Euler problem (deg = 3) for FRGPU_IND_MLP: an element
  * is troubled when the network's probability exceeds `threshold`; within
- * `band` of the threshold the plain modal-decay test decides (fallback).  The
+ * `band` of the threshold the plain modal-decay test decides (fallback).  An
+ * element whose modal decay lies below the plain test's sigma = 1 region
+ * (log10 su < S0 - kappa) is smooth without consulting the network.  The
  * network is borrowed and must outlive its use. */
 FRGPU_API int frgpu_problem_set_mlp(frgpu_problem *p, const frgpu_mlp *m, double threshold, double band);
 /* The 32 indicator inputs of every element of the current state, feat[ne][32]. */
