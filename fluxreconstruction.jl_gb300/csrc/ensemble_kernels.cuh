@@ -190,10 +190,11 @@ __device__ __forceinline__ void ens_feature_row(const Real (&h)[NP], Real tot, _
 }
 
 // Modal coefficients, energy and plain modal-decay decision of element i
-// (example/euler_highlevel.jl:37-52, the same arithmetic as ens_filter).
+// (example/euler_highlevel.jl:37-52, the same arithmetic as ens_filter); below is
+// set when Se lies below S0 - kappa, where the test's sigma is exactly 1 (smooth).
 template <class Real, int NP>
 __device__ __forceinline__ bool ens_modes(const Real *__restrict__ u, int ne, int i, const EnsOps<Real> &op,
-                                          Real (&h)[NP], Real &tot) {
+                                          Real (&h)[NP], Real &tot, bool &below) {
     const int d = NP - 2;
     const int deg = NP - 1;
     const double S0 = -3.0 * log10((double)deg), kappa = 4.0;
@@ -212,13 +213,21 @@ __device__ __forceinline__ bool ens_modes(const Real *__restrict__ u, int ne, in
     const double su = (double)(h[NP - 1] * h[NP - 1]) / ((double)tot + 1e-6);
     const double Se = log10(su);
     double sigma;
-    if (Se < S0 - kappa)
+    below = Se < S0 - kappa;
+    if (below)
         sigma = 1.0;
     else if (S0 - kappa <= Se && Se < S0 + kappa)
         sigma = 0.5 * (1.0 - sin(0.5 * 3.14159265358979323846 * (Se - S0) / kappa));
     else
         sigma = 0.0;
     return sigma < 0.99;
+}
+
+template <class Real, int NP>
+__device__ __forceinline__ bool ens_modes(const Real *__restrict__ u, int ne, int i, const EnsOps<Real> &op,
+                                          Real (&h)[NP], Real &tot) {
+    bool below;
+    return ens_modes<Real, NP>(u, ne, i, op, h, tot, below);
 }
 
 // :l2 filter of one element's modes h back into u (as ens_filter).
@@ -248,34 +257,47 @@ __device__ void ens_filter(Real *__restrict__ u, int ne, double lam, const EnsOp
 }
 
 // Learned indicator + :l2 filter on one instance: each warp of the group takes
-// tiles of 16 elements (lanes 0-15 own one element each).
+// 32 elements at a time (one per lane) and runs the network on each half of 16
+// that holds an element outside the plain test's sigma = 1 region. Elements in
+// that region are smooth without the network (they count as network decisions
+// agreeing with the plain test). The network is row-independent, so every
+// element gets the same probability whatever else shares its half.
 template <class Real, int NP, int G>
 __device__ void ens_filter_learned(Real *__restrict__ u, int ne, double lam, const EnsOps<Real> &op, int r,
                                    const EnsLearn &L, unsigned long long (&cnt)[4]) {
     const int lane = r & 31;
     constexpr int NW = G / 32;
-    for (int tile = r >> 5; tile * 16 < ne; tile += NW) {
-        const int i = tile * 16 + (lane & 15);
-        const bool mine = lane < 16 && i < ne;
+    for (int tile = r >> 5; tile * 32 < ne; tile += NW) {
+        const int i = tile * 32 + lane;
+        const bool mine = i < ne;
         Real h[NP], tot = Real(0);
-        bool plain = false;
-        if (mine) {
-            plain = ens_modes<Real, NP>(u, ne, i, op, h, tot);
-            ens_feature_row<Real, NP>(h, tot, L.xs + lane * frmlp::NIN);
-        } else if (lane < 16) {
+        bool plain = false, below = true;
+        if (mine) plain = ens_modes<Real, NP>(u, ne, i, op, h, tot, below);
+        const bool cand = mine && !below;
+        const unsigned cm = __ballot_sync(0xffffffffu, cand);
+        float pm = 0.f;
+#pragma unroll 1
+        for (int half = 0; half < 2; ++half) {
+            if (!((cm >> (16 * half)) & 0xffffu)) continue; // warp-uniform
+            const bool row = (lane >> 4) == half;
+            if (row && mine) {
+                ens_feature_row<Real, NP>(h, tot, L.xs + (lane & 15) * frmlp::NIN);
+            } else if (row) {
 #pragma unroll
-            for (int q = 0; q < frmlp::NIN; ++q) L.xs[lane * frmlp::NIN + q] = __float2bfloat16_rn(0.f);
+                for (int q = 0; q < frmlp::NIN; ++q) L.xs[(lane & 15) * frmlp::NIN + q] = __float2bfloat16_rn(0.f);
+            }
+            __syncwarp();
+            frmlp::Fwd f;
+            frmlp::mlp_forward_tile(L.view, L.xs, f);
+            if ((lane & 3) == 0) {
+                L.prob[lane >> 2] = frmlp::sigmoidf_(f.logit_g);
+                L.prob[(lane >> 2) + 8] = frmlp::sigmoidf_(f.logit_g8);
+            }
+            __syncwarp();
+            if (row && cand) pm = L.prob[lane & 15];
+            __syncwarp(); // the other half reuses the feature and probability tiles
         }
-        __syncwarp();
-        frmlp::Fwd f;
-        frmlp::mlp_forward_tile(L.view, L.xs, f);
-        if ((lane & 3) == 0) {
-            L.prob[lane >> 2] = frmlp::sigmoidf_(f.logit_g);
-            L.prob[(lane >> 2) + 8] = frmlp::sigmoidf_(f.logit_g8);
-        }
-        __syncwarp();
         if (mine) {
-            const float pm = L.prob[lane];
             const bool fb = fabsf(pm - L.thr) < L.band, net = pm > L.thr;
             const bool bad = fb ? plain : net;
             cnt[0] += bad;
@@ -378,7 +400,7 @@ template <class Real> constexpr size_t ens_smem_bytes() {
 // LEARNED: the post-step indicator is the network (a.mlp set); a separate
 // instantiation, so that the plain kernel keeps its register budget.
 template <class Real, bool LEARNED>
-__global__ void __launch_bounds__(ENS_THREADS) k_ensemble(const EnsArgs<Real> a) {
+__global__ void __launch_bounds__(ENS_THREADS, sizeof(Real) == 4 ? 2 : 1) k_ensemble(const EnsArgs<Real> a) {
     extern __shared__ __align__(16) unsigned char ens_smem[];
     Real *s_all = reinterpret_cast<Real *>(ens_smem);
     __shared__ double s_red[ENS_WARPS];

@@ -134,8 +134,10 @@ def test_ensemble_features_and_labels_match_oracle(frgpu, oracle):
 
 
 def test_learned_full_fallback_equals_plain(frgpu):
-    """band = 0.5 sends every element to the plain test: the learned path must
-    then reproduce the plain indicator + filter bit for bit (FP64)."""
+    """band = 0.5 sends every element the network is consulted for to the
+    plain test, and the elements in the plain test's sigma = 1 region are smooth
+    without the network: the learned path must then reproduce the plain
+    indicator + filter bit for bit (FP64)."""
     from frgpu import learned
 
     outs = []
@@ -147,7 +149,9 @@ def test_learned_full_fallback_equals_plain(frgpu):
         outs.append([e.get_state(i) for i in range(e.n)])
         if mode == "mlp":
             st = e.indicator_stats()
-            assert st["fallbacks"] == st["judged"] > 0 and st["troubled"] > 0
+            # floor elements are network decisions that agree with the plain test
+            assert 0 < st["fallbacks"] < st["judged"] and st["troubled"] > 0
+            assert st["misfires"] <= st["fallbacks"]
     for a, b in zip(*outs):
         assert np.array_equal(a, b)
 
