@@ -59,8 +59,14 @@ __device__ __forceinline__ void cell_flux(const TriArgs<Real> &a, unsigned c, Re
     }
 }
 
+// FP32: five 128-thread blocks per SM (96 registers, about 180 bytes of spill
+// at p = 3) hide the neighbour gathers better than three blocks at the 152
+// registers the unbounded build takes (386 against 545 us at 2 M cells, p = 3;
+// six blocks at 80 registers spill more: 403 us).  FP64 (206 registers at
+// p = 3) keeps two blocks: it is bound by the FP64 pipe, and capping its
+// registers spills kilobytes.
 template <class Real, int N>
-__global__ void __launch_bounds__(128) k_tri_rhs(const TriArgs<Real> a) {
+__global__ void __launch_bounds__(128, sizeof(Real) == 4 ? 5 : 1) k_tri_rhs(const TriArgs<Real> a) {
     constexpr int NP = (N + 1) * (N + 2) / 2, NFP = 3 * (N + 1);
     constexpr int NOPS = 2 * NP * NP + 2 * NFP * NP;
     __shared__ Real s_ops[NOPS];
