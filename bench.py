@@ -720,8 +720,8 @@ def bgk_entry(steps=400, warmup=5):
 
     for kn in (1e-2, 1e-4):
         rec = {}
-        for form, precision, tensor in (("fp32_tensor", "fp32k", 1), ("fp32_cuda_cores", "fp32k", 0),
-                                        ("fp64", "fp64", 0)):
+        for form, precision, tensor in (("fp32_tensor", "fp32k", 1), ("fp32_tcgen05", "fp32k", 2),
+                                        ("fp32_cuda_cores", "fp32k", 0), ("fp64", "fp64", 0)):
             prob = frgpu.FRBGKProblem(f, (0, 1), ps, v, w, kn, precision=precision)
             if precision == "fp32k":
                 prob.set_option(L.OPT_BGK_TENSOR, tensor)
@@ -735,7 +735,7 @@ def bgk_entry(steps=400, warmup=5):
             itg.step(nfull)
             rec[form]["moments"] = moments(itg.u)
         ref = rec["fp64"].pop("moments")
-        for form in ("fp32_tensor", "fp32_cuda_cores"):
+        for form in ("fp32_tensor", "fp32_tcgen05", "fp32_cuda_cores"):
             m = rec[form].pop("moments")
             rec[form]["moment_rel_err_vs_fp64"] = [float(np.max(np.abs(m[q] - ref[q])) / np.max(np.abs(ref[q])))
                                                    for q in range(3)]

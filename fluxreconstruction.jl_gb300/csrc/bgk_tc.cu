@@ -15,6 +15,11 @@
 // (the split product of Ootomo and Yokota, "Recovering single precision accuracy
 // from Tensor Cores while surpassing the FP32 theoretical peak performance", 2022).
 // The A fragments of both signs, split, are built once per problem on the host.
+// A second form (k_bgk1d_umma, FRGPU_OPT_BGK_TENSOR = 2) runs the same split
+// product on the 5th-generation tensor cores, 128 velocities per CTA; it adds
+// the same terms in the same order and gives the same bits, but on the 512-
+// velocity workload it has 4x fewer, longer-lived CTAs whose load -> MMA ->
+// epilogue chain the SM cannot overlap, and takes 74 against 52 us per step.
 //
 // The BGK collision term (M - u)/tau needs the moments (rho, rho U, E) of every
 // (element, point) over all velocities and conserve_prim at gamma = 3
@@ -27,6 +32,7 @@
 #include <cstring>
 #include <vector>
 
+#include "blackwell.cuh"
 #include "fr_stage.cuh"
 #include "frgpu_internal.h"
 
@@ -118,9 +124,135 @@ struct TCArgs {
     const float *velo;
     const float *prim;
     const uint4 *frag; // [sign][big/small][ks][lane] (4 words each)
+    const uint32_t *uop; // tcgen05 B operands: [sign][big/small][UN x K core layout]
     float tau;
     int *status;
 };
+
+// ---- the same tile product on the 5th-generation tensor cores (tcgen05) ------
+// One CTA of 128 threads per tile of EB elements x UM = 128 velocities, the
+// product transposed so that velocities run along M:
+//   D[v][r] = sum_kk P[v][kk] A[r][kk],  P[v][kk] = u_k(e) / J_e (e = i0 + kk / np - 1, k = kk % np),
+// one tcgen05.mma.kind::tf32 chain per velocity sign present in the tile (M = 128,
+// N = UN = 16 tile rows, K = 8 per instruction over the tile's 8 KS source rows),
+// with the three-term split P A ~ Pb As + Ps Ab + Pb Ab; FP32 accumulators in
+// tensor-memory columns 16 s .. 16 s + 15.  Thread t owns velocity v0 + t: it
+// builds row t of P (big and small parts) in shared memory, and reads back row t
+// of D (its warp's own tensor-memory lanes) for the epilogue.  Operands are
+// K-major without swizzling: 8 x 4 TF32 core matrices of 128 bytes, adjacent
+// along K 128 bytes apart and along M / N (K / 4) * 128 bytes apart.
+constexpr int UM = 128, UN = 16, UK_MAX = 8 * KS_MAX;
+constexpr int UT = 4 * UM; // threads per CTA: four per velocity in the epilogue
+constexpr int UOP_WORDS = 4 * UN * UK_MAX;
+__host__ __device__ constexpr int ucore(int r, int k, int K) {
+    return (r >> 3) * (K / 4) * 32 + (k >> 2) * 32 + (r & 7) * 4 + (k & 3); // 4-byte words
+}
+
+template <int NP, int STAGE>
+__global__ void __launch_bounds__(UT) k_bgk1d_umma(const TCArgs a) {
+    constexpr BTile T = btile(NP);
+    constexpr int K = 8 * T.KS;
+    constexpr int RG = (T.ROWS + 3) / 4; // rows per warp group in the epilogue
+    static_assert(T.ROWS <= UN && K <= UK_MAX, "tile larger than the tcgen05 operands");
+    __shared__ __align__(1024) uint32_t s_pb[UM * K];
+    __shared__ __align__(1024) uint32_t s_ps[UM * K];
+    __shared__ __align__(128) uint32_t s_op[4 * UN * K];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ uint32_t s_tm;
+    const int tid = threadIdx.x, warp = tid >> 5, grp = tid / UM;
+    const int ne = a.ne, nv = a.nvel;
+    const int i0 = blockIdx.x * T.EB;
+    // P: thread (grp, t) builds the K chunks grp, grp + 4, ... of row t (velocity v0 + t)
+    {
+        const int t = tid % UM, v = blockIdx.y * UM + t;
+        const bool v_ok = v < nv;
+        for (int c = grp; c < K / 4; c += 4) {
+            uint32_t hb[4], hs[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int k2 = 4 * c + j;
+                float x = 0.f;
+                if (v_ok && k2 < T.KR) {
+                    const int e = wrapn(i0 + k2 / NP - 1, ne);
+                    x = ld_state(a.uin, a.din, ((size_t)e * NP + k2 % NP) * nv + v) / __ldg(a.J + e);
+                }
+                hb[j] = tf32_of(x);
+                hs[j] = tf32_of(x - __uint_as_float(hb[j]));
+            }
+            *reinterpret_cast<uint4 *>(s_pb + ucore(t, 4 * c, K)) = make_uint4(hb[0], hb[1], hb[2], hb[3]);
+            *reinterpret_cast<uint4 *>(s_ps + ucore(t, 4 * c, K)) = make_uint4(hs[0], hs[1], hs[2], hs[3]);
+        }
+    }
+    for (int q = tid; q < 4 * UN * K; q += UT) s_op[q] = __ldg(a.uop + q);
+    // the epilogue's velocity: warp w reads tensor-memory lanes 32 (w % 4) ..
+    const int v = blockIdx.y * UM + 32 * (warp & 3) + (tid & 31);
+    const bool v_ok = v < nv;
+    const float vel = v_ok ? __ldg(a.velo + v) : 0.f;
+    if (tid == 0) bw::mbar_init(&s_bar, 1);
+    if (warp == 0) bw::tmem_alloc(&s_tm, 32);
+    bw::fence_async_smem(); // P and the operator (written by this thread) -> the MMA's async proxy
+    bw::tc_fence_before();
+    const int any_pos = __syncthreads_or(v_ok && vel > 0.f);
+    const int any_neg = __syncthreads_or(v_ok && !(vel > 0.f));
+    bw::tc_fence_after();
+    const uint32_t tmem = s_tm;
+    if (tid == 0) {
+        constexpr uint32_t ID = bw::idesc_tf32_f32(UM, UN);
+        constexpr uint32_t SBO = (K / 4) * 128;
+        const uint32_t pb = bw::smem_addr(s_pb), ps = bw::smem_addr(s_ps), op = bw::smem_addr(s_op);
+#pragma unroll
+        for (int sg = 0; sg < 2; ++sg) {
+            if (!(sg == 1 ? any_pos : any_neg)) continue;
+            const uint32_t d = tmem + 16 * sg;
+            const uint32_t ob = op + (uint32_t)((sg * 2 + 0) * UN * K * 4), os = op + (uint32_t)((sg * 2 + 1) * UN * K * 4);
+#pragma unroll
+            for (int ks = 0; ks < T.KS; ++ks) {
+                const uint32_t off = 256 * ks; // two core matrices (K = 8) per instruction
+                bw::mma_tf32(d, bw::smem_desc_kmajor(pb + off, 128, SBO), bw::smem_desc_kmajor(os + off, 128, SBO), ID,
+                             ks > 0);
+                bw::mma_tf32(d, bw::smem_desc_kmajor(ps + off, 128, SBO), bw::smem_desc_kmajor(ob + off, 128, SBO), ID,
+                             true);
+                bw::mma_tf32(d, bw::smem_desc_kmajor(pb + off, 128, SBO), bw::smem_desc_kmajor(ob + off, 128, SBO), ID,
+                             true);
+            }
+        }
+        bw::mma_commit(&s_bar);
+    }
+    const bool done = bw::mbar_wait(&s_bar, 0);
+    bw::tc_fence_after();
+    int bad = 0;
+    if (done) {
+        float acc[32];
+        bw::tmem_ld32(tmem + ((uint32_t)(32 * (warp & 3)) << 16), acc);
+        const float dt = (float)(*a.dtp);
+        const float pi_inv = 0.31830988618379067154f, itau = 1.0f / a.tau;
+        const int sg = vel > 0.f ? 1 : 0;
+#pragma unroll
+        for (int q = 0; q < RG; ++q) {
+            const int r = RG * (warp >> 2) + q;
+            const int e = i0 + r / NP, m = r % NP;
+            if (r >= T.ROWS || e >= ne || !v_ok) continue;
+            const float tr = sg ? acc[16 + r] : acc[r];
+            const size_t idx = ((size_t)e * NP + m) * nv + v;
+            const float u = ld_state(a.uin, a.din, idx);
+            const float *pr = a.prim + 3 * ((size_t)e * NP + m);
+            const float rho = __ldg(pr), U = __ldg(pr + 1), lam = __ldg(pr + 2);
+            const float dv = vel - U;
+            const float M = rho * sqrtf(lam * pi_inv) * expf(-lam * dv * dv);
+            const float du = fmaf(-vel, tr, (M - u) * itau);
+            const float res = stage_update<float, MODE_FP32K, STAGE>(du, u, dt, idx, a.un, a.uin, a.din, a.out, a.ul);
+            if (!isfinite(res)) bad |= ST_NONFINITE;
+        }
+    } else {
+        bad |= ST_TIMEOUT;
+        bw::mbar_wait(&s_bar, 0); // a bounded second wait for the MMAs still in flight
+    }
+    bw::tc_fence_before();
+    __syncthreads();
+    bw::tc_fence_after();
+    if (warp == 0) bw::tmem_dealloc(tmem, 32);
+    if (bad) atomicOr(a.status, bad);
+}
 
 template <int NP, int STAGE>
 __global__ void __launch_bounds__(32 * TCW) k_bgk1d_tc(const TCArgs a) {
@@ -217,8 +349,22 @@ int launch_tc(frgpu_problem *p, int stage, const void *in, const void *din, void
     a.velo = (const float *)p->d_velo;
     a.prim = p->d_bgk_prim;
     a.frag = reinterpret_cast<const uint4 *>(p->d_bgk_frag);
+    a.uop = p->d_bgk_frag + FRAG_WORDS;
     a.tau = (float)p->d.tau;
     a.status = p->d_status;
+    if (p->bgk_tensor == 2) {
+        const dim3 ug((ne + T.EB - 1) / T.EB, (nv + UM - 1) / UM);
+        switch (stage) {
+        case 0: k_bgk1d_umma<NP, 0><<<ug, UT, 0, p->stream>>>(a); break;
+        case 1: k_bgk1d_umma<NP, 1><<<ug, UT, 0, p->stream>>>(a); break;
+        case 2: k_bgk1d_umma<NP, 2><<<ug, UT, 0, p->stream>>>(a); break;
+        case 3: k_bgk1d_umma<NP, 3><<<ug, UT, 0, p->stream>>>(a); break;
+        default: fr_set_error("BGK residual: bad stage"); return FRGPU_ERR_ARG;
+        }
+        FR_CUDA(cudaGetLastError());
+        p->launches += 2;
+        return FRGPU_OK;
+    }
     const dim3 grid((ne + T.EB - 1) / T.EB, (nv + 8 * TCW - 1) / (8 * TCW));
     switch (stage) {
     case 0: k_bgk1d_tc<NP, 0><<<grid, 32 * TCW, 0, p->stream>>>(a); break;
@@ -268,8 +414,21 @@ int fr_bgk_tc_setup(frgpu_problem *p) {
                     frag[(((sg * 2 + 1) * KS_MAX + ks) * 32 + lane) * 4 + q] = tf32_host(x - bf);
                 }
             }
-    FR_CUDA(cudaMalloc(&p->d_bgk_frag, sizeof(uint32_t) * FRAG_WORDS));
-    FR_CUDA(cudaMemcpy(p->d_bgk_frag, frag.data(), sizeof(uint32_t) * FRAG_WORDS, cudaMemcpyHostToDevice));
+    // the tcgen05 B operands: rows r of the same operator, K-major core layout
+    const int K = 8 * T.KS;
+    frag.resize(FRAG_WORDS + UOP_WORDS, 0u);
+    for (int sg = 0; sg < 2; ++sg)
+        for (int r = 0; r < UN; ++r)
+            for (int kk = 0; kk < K; ++kk) {
+                const float x = (float)A(sg, r, kk);
+                const uint32_t big = tf32_host(x);
+                float bf;
+                std::memcpy(&bf, &big, 4);
+                frag[FRAG_WORDS + (sg * 2 + 0) * UN * K + ucore(r, kk, K)] = big;
+                frag[FRAG_WORDS + (sg * 2 + 1) * UN * K + ucore(r, kk, K)] = tf32_host(x - bf);
+            }
+    FR_CUDA(cudaMalloc(&p->d_bgk_frag, sizeof(uint32_t) * frag.size()));
+    FR_CUDA(cudaMemcpy(p->d_bgk_frag, frag.data(), sizeof(uint32_t) * frag.size(), cudaMemcpyHostToDevice));
     FR_CUDA(cudaMalloc(&p->d_bgk_prim, sizeof(float) * 3 * (size_t)s.nx * np));
     FR_CUDA(cudaMemset(p->d_bgk_prim, 0, sizeof(float) * 3 * (size_t)s.nx * np));
     return FRGPU_OK;

@@ -1090,7 +1090,8 @@ FRGPU_API int frgpu_problem_set_option(frgpu_problem *p, int option, int value) 
                option == FRGPU_OPT_GHOSTS_PER_STEP,
            "set_option: unknown option");
     FR_REQ(option != FRGPU_OPT_BGK_CLOSURE || value == 0 || value == 1, "set_option: BGK closure is 0 or 1");
-    if (option == FRGPU_OPT_BGK_TENSOR) p->bgk_tensor = value != 0;
+    FR_REQ(option != FRGPU_OPT_BGK_TENSOR || (value >= 0 && value <= 2), "set_option: BGK tensor form is 0, 1 or 2");
+    if (option == FRGPU_OPT_BGK_TENSOR) p->bgk_tensor = value;
     if (option == FRGPU_OPT_BGK_CLOSURE) p->bgk_closure = value;
     if (option == FRGPU_OPT_GHOSTS_PER_STEP) p->ghosts_per_step = value != 0;
     if (option == FRGPU_OPT_FUSED_INDICATOR) p->fuse_indicator = value != 0;

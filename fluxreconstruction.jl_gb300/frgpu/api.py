@@ -485,7 +485,8 @@ class ODEProblem:
 
     def set_option(self, option: int, value: int) -> None:
         """Kernel choice for measurements (frgpu_problem_set_option), e.g.
-        ``set_option(L.OPT_BGK_TENSOR, 0)`` for the CUDA-core BGK transport."""
+        ``set_option(L.OPT_BGK_TENSOR, 0)`` for the CUDA-core BGK transport, 2 for
+        the tcgen05 form of the tensor-core product (1, the default, is mma.sync)."""
         check(L.lib().frgpu_problem_set_option(self._h, int(option), int(value)))
 
     def __del__(self):

@@ -281,7 +281,9 @@ FRGPU_API int frgpu_set_limiter(frgpu_problem *p, int on, const double *weights,
 FRGPU_API int frgpu_troubled_flags(frgpu_problem *p, int *flags, long n);
 /* Kernel choices for measurements; no counterpart in the reference.
  * FRGPU_OPT_BGK_TENSOR: 1 (default) runs the FP32 BGK transport as a TF32-split
- * tensor-core product, 0 on the CUDA cores.
+ * tensor-core product with warp-level mma.sync, 2 the same product on tcgen05
+ * (M = 128 velocities per CTA, accumulators in tensor memory; the same bits as
+ * 1, slower on small velocity grids), 0 on the CUDA cores.
  * FRGPU_OPT_FUSED_INDICATOR: 1 (default) runs the indicator (learned or plain)
  * + filter of an FP32K deg-3 2D Euler problem inside its third SSPRK3 stage, 0
  * as a kernel of its own after the step.

@@ -83,6 +83,35 @@ def test_bgk_tensor_and_cuda_core_forms_agree(frgpu, oracle):
     assert rel(outs[0], outs[1]) < 1e-5
 
 
+@pytest.mark.parametrize("deg", [1, 2, 3, 4, 5])
+def test_bgk_tcgen05_form_matches_mma_sync_form(frgpu, oracle, deg):
+    """The transport product on tcgen05 (FRGPU_OPT_BGK_TENSOR = 2: 128
+    velocities per CTA, TF32 operands in shared memory, FP32 accumulators in
+    tensor memory) accumulates the same split terms in the same order as the
+    mma.sync form: the same bits for one residual and after 25 steps, on a grid
+    whose 100 velocities fill one 128-velocity tile with both signs."""
+    from frgpu import _lib as L
+
+    ne, nv = 61, 100
+    dv = 0.16
+    v = -7 + (np.arange(nv) + 0.5) * dv
+    w = np.full(nv, dv)
+    dt = 0.1 * (1 / ne) / 9
+    outs = []
+    for form in (1, 2):
+        ps, f, prob, P = bgk_pair(frgpu, oracle, ne, deg, v, w, 1e-2)
+        prob.set_option(L.OPT_BGK_TENSOR, form)
+        r = prob.rhs(f)
+        itg = frgpu.init(prob, dt=dt)
+        l0 = itg.launches()
+        itg.step(25)
+        assert itg.launches() - l0 == 150  # a moments and a transport kernel per stage
+        outs.append((r, itg.u))
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])
+    assert rel(outs[1][1], P.ssprk3(f, dt, 25)) < 2e-5
+
+
 @pytest.mark.parametrize("kn", [1e-4, 1e-2])
 def test_bgk_workload_moments_match_oracle(frgpu, oracle, kn):
     """256 elements on periodic [0,1], p = 3, 512 velocity midpoints on [-8,8],
