@@ -83,7 +83,60 @@ __device__ __forceinline__ double final_value(const double *__restrict__ part, i
     return x;
 }
 
-template <class Real, bool DEV>
+// Warp tree of a thread's partials into red[v][warp] (fixed order: deterministic).
+// FP64 form: FP64 sums and maxima.  FP32K form: the sums stay double-float pairs
+// through the tree (TwoSum of the high parts, the low parts and the rounding
+// errors added in FP32), the maxima FP32 (exact), and only lane 0 converts to
+// FP64: the FP64 pipe (1/64 of the FP32 rate here) then carries one addition per
+// warp instead of 30 per thread, which had made the FP64 tree the kernel's bound.
+template <class Real>
+__device__ __forceinline__ void warp_partials(const SumAcc<Real> (&acc)[4], Real smax, Real rmax,
+                                              double (&red)[6][RED_THREADS / 32]) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if constexpr (sizeof(Real) == 8) {
+        double vals[6] = {acc[0].value(), acc[1].value(), acc[2].value(), acc[3].value(), smax, rmax};
+#pragma unroll
+        for (int v = 0; v < 6; ++v) {
+            double x = vals[v];
+            for (int off = 16; off > 0; off >>= 1) {
+                double y = __shfl_down_sync(0xffffffffu, x, off);
+                x = v < 4 ? x + y : fmax(x, y);
+            }
+            if (lane == 0) red[v][w] = x;
+        }
+    } else {
+        float hs[4], he[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            hs[m] = acc[m].s;
+            he[m] = acc[m].e;
+        }
+        float a = smax, b = rmax;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                const float s2 = __shfl_down_sync(0xffffffffu, hs[m], off);
+                const float e2 = __shfl_down_sync(0xffffffffu, he[m], off);
+                const float t = __fadd_rn(hs[m], s2);
+                const float bp = __fsub_rn(t, hs[m]);
+                const float err = __fadd_rn(__fsub_rn(hs[m], __fsub_rn(t, bp)), __fsub_rn(s2, bp));
+                hs[m] = t;
+                he[m] = __fadd_rn(he[m], __fadd_rn(e2, err));
+            }
+            a = fmaxf(a, __shfl_down_sync(0xffffffffu, a, off));
+            b = fmaxf(b, __shfl_down_sync(0xffffffffu, b, off));
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int m = 0; m < 4; ++m) red[m][w] = (double)hs[m] + (double)he[m];
+            red[4][w] = a;
+            red[5][w] = b;
+        }
+    }
+}
+
+template <class Real, bool DEV, bool MET = false>
 __global__ void __launch_bounds__(RED_THREADS, sizeof(Real) == 4 ? 4 : 2) k_reduce2d_partial(const Real *__restrict__ u, const Real *__restrict__ lo,
                                                              size_t plane, int nq, const double *__restrict__ wp,
                                                              double gamma, double idx_, double idy_,
@@ -113,7 +166,7 @@ __global__ void __launch_bounds__(RED_THREADS, sizeof(Real) == 4 ? 4 : 2) k_redu
                 const size_t at = frk::e2d_index(e, q, 0, plane);
                 frk::ldg4(u + at, W[t]);
                 if (lo != nullptr) frk::ldg4(lo + at, WL[t]);
-                if (met != nullptr) frk::ldg4(met + at, MT[t]);
+                if (MET) frk::ldg4(met + at, MT[t]);
             } else {
                 const size_t tt = e + plane * q;
 #pragma unroll
@@ -129,10 +182,10 @@ __global__ void __launch_bounds__(RED_THREADS, sizeof(Real) == 4 ? 4 : 2) k_redu
             if (eb + (size_t)t * blockDim.x >= e1) break;
             Real *w = W[t], *wl = WL[t], *mt = MT[t];
             Real jac = Real(1);
-            if (DEV && met != nullptr) jac = Real(1) / (mt[0] * mt[3] - mt[1] * mt[2]);
+            if (DEV && MET) jac = Real(1) / (mt[0] * mt[3] - mt[1] * mt[2]);
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
-                if (DEV && met != nullptr) acc[m].add(w[m] * jac, wl[m] * jac);
+                if (DEV && MET) acc[m].add(w[m] * jac, wl[m] * jac);
                 else acc[m].add(w[m], wl[m]);
                 w[m] += wl[m];
             }
@@ -142,7 +195,7 @@ __global__ void __launch_bounds__(RED_THREADS, sizeof(Real) == 4 ? 4 : 2) k_redu
             const Real c = frk::sqrtP<Real>(g * p * rinv);
             const Real a = fabs(U) + c, bb = fabs(V) + c;
             smax = fmax(smax, fmax(a, bb));
-            if (DEV && met != nullptr) {
+            if (DEV && MET) {
                 const Real lr = fabs(mt[0] * U + mt[1] * V) + c * frk::sqrtR<Real>(mt[0] * mt[0] + mt[1] * mt[1]);
                 const Real ls = fabs(mt[2] * U + mt[3] * V) + c * frk::sqrtR<Real>(mt[2] * mt[2] + mt[3] * mt[3]);
                 rmax = fmax(rmax, Real(0.5) * (lr + ls));
@@ -152,16 +205,7 @@ __global__ void __launch_bounds__(RED_THREADS, sizeof(Real) == 4 ? 4 : 2) k_redu
         }
     }
     __shared__ double red[6][RED_THREADS / 32];
-    double vals[6] = {acc[0].value(), acc[1].value(), acc[2].value(), acc[3].value(), (double)smax, (double)rmax};
-#pragma unroll
-    for (int v = 0; v < 6; ++v) {
-        double x = vals[v];
-        for (int off = 16; off > 0; off >>= 1) {
-            double y = __shfl_down_sync(0xffffffffu, x, off);
-            x = v < 4 ? x + y : fmax(x, y);
-        }
-        if ((threadIdx.x & 31) == 0) red[v][threadIdx.x >> 5] = x;
-    }
+    warp_partials<Real>(acc, smax, rmax, red);
     __syncthreads();
     if (threadIdx.x < 6) {
         const int v = threadIdx.x;
@@ -237,14 +281,18 @@ static int enqueue_reduce(frgpu_problem *p, const void *state, const void *lo, d
     unsigned *cnt = reinterpret_cast<unsigned *>(fin + 7);
     frgpu_problem::host_words *hw = nullptr;
     FR_CUDA(cudaHostGetDevicePointer((void **)&hw, p->h_words, 0));
-    if (p->d.precision == FRGPU_FP64)
-        k_reduce2d_partial<double, true><<<grid, RED_THREADS, 0, p->stream>>>(
-            (const double *)state, (const double *)lo, plane, nq, wp, p->d.gamma, cfl_dx, cfl_dy, part,
-            (const double *)p->d_met, cnt, fin, hw->red, p->d_status, &hw->status);
-    else
-        k_reduce2d_partial<float, true><<<grid, RED_THREADS, 0, p->stream>>>(
-            (const float *)state, (const float *)lo, plane, nq, wp, p->d.gamma, cfl_dx, cfl_dy, part,
-            (const float *)p->d_met, cnt, fin, hw->red, p->d_status, &hw->status);
+    const bool met = p->d_met != nullptr;
+    if (p->d.precision == FRGPU_FP64) {
+        auto k = met ? k_reduce2d_partial<double, true, true> : k_reduce2d_partial<double, true, false>;
+        k<<<grid, RED_THREADS, 0, p->stream>>>((const double *)state, (const double *)lo, plane, nq, wp, p->d.gamma,
+                                               cfl_dx, cfl_dy, part, (const double *)p->d_met, cnt, fin, hw->red,
+                                               p->d_status, &hw->status);
+    } else {
+        auto k = met ? k_reduce2d_partial<float, true, true> : k_reduce2d_partial<float, true, false>;
+        k<<<grid, RED_THREADS, 0, p->stream>>>((const float *)state, (const float *)lo, plane, nq, wp, p->d.gamma,
+                                               cfl_dx, cfl_dy, part, (const float *)p->d_met, cnt, fin, hw->red,
+                                               p->d_status, &hw->status);
+    }
     FR_CUDA(cudaGetLastError());
     return FRGPU_OK;
 }
