@@ -5,6 +5,7 @@
 #include <atomic>
 #include <cstdint>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "../../include/frgpu.h"
@@ -115,6 +116,8 @@ struct frgpu_problem {
     void *d_eig = nullptr; // 4 n values: direction, v, f(u), f(v)
     bool have_eig = false;
     double *d_eig_red = nullptr; // FR_RED_BLOCKS partials + the last-block counter
+    std::map<int, std::vector<double>> rkc2_cache; // frgpu_step_rkc2: s -> alpha, beta, mu, delta, bound
+    double rkc2_eps = -1.0;
     float *d_bgk_prim = nullptr;    // FP32 BGK: (rho, U, lambda) per (element, point), from the moments
     uint32_t *d_bgk_frag = nullptr; // FP32 BGK: TF32 A fragments of the transport operator (both signs, split)
     // captured step graph

@@ -996,6 +996,99 @@ FRGPU_API int frgpu_spectral_radius(frgpu_problem *p, int maxiter, double *rho, 
     FR_CATCH
 }
 
+// RKC2 coefficients (the closed forms of Sommeijer, Shampine and Verwer, J.
+// Comput. Appl. Math. 88 (1997) 315-326): Chebyshev T_j and its first two
+// derivatives at w0 = 1 + eps/s^2, w1 = T_s'/T_s'', b_j = T_j''/T_j'^2 (b_0 = b_1
+// = b_2), a_j = 1 - b_j T_j; in the increment form D_j = alpha_j D_{j-1} +
+// beta_j D_{j-2} + dt (mu_j f(u + D_{j-1}) + delta_j f(u)): mu_1 = b_1 w1 and for
+// j >= 2 alpha_j = 2 b_j w0 / b_{j-1}, beta_j = -b_j / b_{j-2}, mu_j = 2 b_j w1 /
+// b_{j-1}, delta_j = -a_{j-1} mu_j.  The operations and their order are those of
+// the Python restatement frgpu.rkc2_coefficients, so both give the same bits.
+static void rkc2_coeffs(int s, double eps, double *alpha, double *beta, double *mu, double *delta, double *bound) {
+    const double w0 = 1.0 + eps / (double)(s * s);
+    std::vector<double> T(s + 1, 0.0), dT(s + 1, 0.0), d2T(s + 1, 0.0), b(s + 1, 0.0), a(s + 1, 0.0);
+    T[0] = 1.0;
+    T[1] = w0;
+    dT[1] = 1.0;
+    for (int j = 2; j <= s; ++j) {
+        T[j] = 2 * w0 * T[j - 1] - T[j - 2];
+        dT[j] = 2 * T[j - 1] + 2 * w0 * dT[j - 1] - dT[j - 2];
+        d2T[j] = 4 * dT[j - 1] + 2 * w0 * d2T[j - 1] - d2T[j - 2];
+    }
+    const double w1 = dT[s] / d2T[s];
+    for (int j = 2; j <= s; ++j) b[j] = d2T[j] / (dT[j] * dT[j]);
+    b[0] = b[1] = b[2];
+    for (int j = 0; j <= s; ++j) a[j] = 1.0 - b[j] * T[j];
+    for (int j = 0; j < s; ++j) alpha[j] = beta[j] = mu[j] = delta[j] = 0.0;
+    mu[0] = b[1] * w1;
+    for (int j = 2; j <= s; ++j) {
+        alpha[j - 1] = 2 * b[j] * w0 / b[j - 1];
+        beta[j - 1] = -b[j] / b[j - 2];
+        mu[j - 1] = 2 * b[j] * w1 / b[j - 1];
+        delta[j - 1] = -a[j - 1] * mu[j - 1];
+    }
+    *bound = (w0 + 1) * d2T[s] / dT[s];
+}
+
+FRGPU_API int frgpu_rkc2_coefficients(int s, double eps, double *alpha, double *beta, double *mu, double *delta,
+                                      double *bound) {
+    FR_REQ(s >= 2 && s <= FR_ROCK_MAXM, "rkc2_coefficients: need 2 <= s <= 4096");
+    FR_REQ(std::isfinite(eps) && eps >= 0.0, "rkc2_coefficients: eps must be finite and >= 0");
+    FR_REQ(alpha && beta && mu && delta && bound, "rkc2_coefficients: null output");
+    FR_TRY
+    rkc2_coeffs(s, eps, alpha, beta, mu, delta, bound);
+    return FRGPU_OK;
+    FR_CATCH
+}
+
+FRGPU_API int frgpu_step_rkc2(frgpu_problem *p, double dt, int nsteps, double eps, int smax, int maxiter,
+                              int *stages) {
+    FR_REQ(p, "step_rkc2: null problem");
+    FR_REQ(nsteps >= 0, "step_rkc2: negative step count");
+    FR_REQ(smax >= 2 && smax <= FR_ROCK_MAXM, "step_rkc2: need 2 <= smax <= 4096");
+    FR_REQ(maxiter >= 1 && maxiter <= 10000, "step_rkc2: need 1 <= maxiter <= 10000");
+    FR_REQ(std::isfinite(eps) && eps >= 0.0, "step_rkc2: eps must be finite and >= 0");
+    if (!(dt > 0.0) || !std::isfinite(dt)) {
+        fr_set_error("step_rkc2: dt must be positive and finite");
+        return FRGPU_ERR_DT;
+    }
+    FR_TRY
+    if (p->rkc2_eps != eps) { // the cache of coefficient sets belongs to one damping
+        p->rkc2_cache.clear();
+        p->rkc2_eps = eps;
+    }
+    auto coeffs = [&](int s) -> const std::vector<double> & {
+        auto it = p->rkc2_cache.find(s);
+        if (it != p->rkc2_cache.end()) return it->second;
+        std::vector<double> c(4 * (size_t)s + 1);
+        rkc2_coeffs(s, eps, c.data(), c.data() + s, c.data() + 2 * s, c.data() + 3 * s, c.data() + 4 * s);
+        return p->rkc2_cache.emplace(s, std::move(c)).first->second;
+    };
+    for (int n = 0; n < nsteps; ++n) {
+        double rho = 0.0;
+        int it = 0;
+        int rc = frgpu_spectral_radius(p, maxiter, &rho, &it);
+        if (rc) return rc;
+        const double z = dt * rho;
+        int s = 2;
+        for (;;) {
+            if (coeffs(s)[4 * (size_t)s] >= z || s >= smax) break;
+            s = std::min(smax, std::max(s + 1, (int)(s * 1.1)));
+        }
+        const std::vector<double> &c = coeffs(s);
+        if (c[4 * (size_t)s] < z) {
+            fr_set_error("step_rkc2: dt * rho needs more than smax stages");
+            return FRGPU_ERR_DT;
+        }
+        rc = frgpu_step_rock(p, s, c.data(), c.data() + s, c.data() + 2 * s, c.data() + 3 * s, 0, nullptr, nullptr,
+                             dt, 1);
+        if (rc) return rc;
+        if (stages) stages[n] = s;
+    }
+    return FRGPU_OK;
+    FR_CATCH
+}
+
 FRGPU_API int frgpu_reduce(frgpu_problem *p, double *sums, double *maxspeed) {
     FR_REQ(p, "reduce: null problem");
     if (p->d.equation != FRGPU_EULER2D) {

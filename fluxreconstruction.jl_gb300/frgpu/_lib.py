@@ -75,6 +75,8 @@ SIGNATURES = {
     "frgpu_step_ssprk3_reduce": (C.c_int, [_VP, C.c_double, C.c_int, _D, _D]),
     "frgpu_step_rock": (C.c_int, [_VP, C.c_int, _D, _D, _D, _D, C.c_int, _D, _D, C.c_double, C.c_int]),
     "frgpu_spectral_radius": (C.c_int, [_VP, C.c_int, _D, _I]),
+    "frgpu_rkc2_coefficients": (C.c_int, [C.c_int, C.c_double, _D, _D, _D, _D, _D]),
+    "frgpu_step_rkc2": (C.c_int, [_VP, C.c_double, C.c_int, C.c_double, C.c_int, C.c_int, _I]),
     "frgpu_problem_set_metric": (C.c_int, [_VP, _D, _D, _D]),
     "frgpu_problem_set_face_jacobians": (C.c_int, [_VP, _D, _D, _D]),
     "frgpu_vandermonde_tri": (C.c_int, [C.c_int, _D, _D, C.c_int, _D, _D, _D]),

@@ -678,8 +678,10 @@ def rkc2_coefficients(s: int, eps: float = 2 / 13):
 
 
 def RKC2(eps: float = 2 / 13, smax: int = 4096, maxiter: int = 50) -> Stabilized:
-    """RKC2 with the fewest stages s >= 2 whose stability bound covers
-    dt * rho (rho from the power method, which includes the 1.2 safety factor)."""
+    """RKC2 with the fewest stages s >= 2 (s = 2, then max(s + 1, floor(1.1 s)),
+    at most smax) whose stability bound covers dt * rho (rho from the power
+    method, which includes the 1.2 safety factor).  Integrator.step runs it with
+    frgpu_step_rkc2, which makes the same choices in one call per n steps."""
     cache = {}
 
     def coefficients(z):
@@ -689,13 +691,15 @@ def RKC2(eps: float = 2 / 13, smax: int = 4096, maxiter: int = 50) -> Stabilized
                 cache[s] = rkc2_coefficients(s, eps)
             if cache[s][4] >= z or s >= smax:
                 break
-            s = max(s + 1, int(s * 1.1))
+            s = min(smax, max(s + 1, int(s * 1.1)))
         if cache[s][4] < z:
             raise ValueError(f"dt * rho = {z:.4g} needs more than {smax} RKC2 stages")
         al, be, mu, de, _ = cache[s]
         return al, be, mu, de, None, None
 
-    return Stabilized(coefficients, "RKC2", maxiter)
+    alg = Stabilized(coefficients, "RKC2", maxiter)
+    alg.rkc2 = (float(eps), int(smax))
+    return alg
 
 
 def ROCK(select, name: str = "ROCK", maxiter: int = 50) -> Stabilized:
@@ -756,6 +760,12 @@ class Integrator:
         dt = self.dt if dt is None else float(dt)
         if self.alg is None:
             check(L.lib().frgpu_step_ssprk3(self.prob._h, dt, int(n)))
+        elif isinstance(self.alg, Stabilized) and getattr(self.alg, "rkc2", None) is not None:
+            eps, smax = self.alg.rkc2
+            st = np.zeros(max(int(n), 1), dtype=np.int32)
+            check(L.lib().frgpu_step_rkc2(self.prob._h, dt, int(n), eps, smax, self.alg.maxiter,
+                                          st.ctypes.data_as(L._I)))
+            self.stages.extend(int(x) for x in st[:int(n)])
         elif isinstance(self.alg, Stabilized):
             for _ in range(int(n)):
                 rho, _ = self.spectral_radius(self.alg.maxiter)

@@ -279,16 +279,26 @@ struct ROCK
 end
 ROCK(select) = ROCK(select, 50)
 
+"""The built-in stabilised method: second-order Runge-Kutta-Chebyshev with damping
+`eps`, its stage count chosen from the device's spectral-radius estimate before every
+step, all inside `frgpu_step_rkc2` (one call per `step!(itg, n)`)."""
+struct RKC2
+    eps::Float64
+    smax::Int
+    maxiter::Int
+end
+RKC2(; eps=2 / 13, smax=4096, maxiter=50) = RKC2(eps, smax, maxiter)
+
 mutable struct Integrator
     p::Problem
     t::Float64
     dt::Float64
-    alg::Union{Nothing,ExplicitRK,ROCK}
+    alg::Union{Nothing,ExplicitRK,ROCK,RKC2}
 end
 
 """init(prob, SSPRK33(); dt) or init(prob, Midpoint(); dt): upload u0 once; the state
 stays on the device."""
-function init(prob::ODEProblem, alg::Union{SSPRK33,ExplicitRK,ROCK}; dt, adaptive=false, kwargs...)
+function init(prob::ODEProblem, alg::Union{SSPRK33,ExplicitRK,ROCK,RKC2}; dt, adaptive=false, kwargs...)
     adaptive && error("FRGPU integrates with fixed dt")
     p = prob.p::Problem
     check(ccall((:frgpu_state_upload, libfrgpu), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), p.h, Array{Float64}(prob.u0)))
@@ -321,6 +331,9 @@ function step!(itg::Integrator, n::Integer=1)
         for _ in 1:n
             rock_step!(itg, a)
         end
+    elseif a isa RKC2
+        check(ccall((:frgpu_step_rkc2, libfrgpu), Cint, (Ptr{Cvoid}, Cdouble, Cint, Cdouble, Cint, Cint, Ptr{Cint}),
+                    itg.p.h, itg.dt, n, a.eps, a.smax, a.maxiter, C_NULL))
     else
         A = Matrix{Float64}(permutedims(a.A))   # row-major for the C ABI
         check(ccall((:frgpu_step_erk, libfrgpu), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Cdouble, Cint),

@@ -212,6 +212,21 @@ FRGPU_API int frgpu_step_rock(frgpu_problem *p, int m, const double *alpha, cons
  * is kept for the next call.  iters receives the iterations used (negative when
  * the estimate did not settle within maxiter; rho is then the last estimate). */
 FRGPU_API int frgpu_spectral_radius(frgpu_problem *p, int maxiter, double *rho, int *iters);
+/* Coefficients of the second-order Runge-Kutta-Chebyshev method with s >= 2
+ * stages and damping eps (Sommeijer, Shampine, Verwer 1997) in the increment
+ * form of frgpu_step_rock (alpha, beta, mu, delta: s entries each), and its real
+ * stability bound.  Host arithmetic only. */
+FRGPU_API int frgpu_rkc2_coefficients(int s, double eps, double *alpha, double *beta, double *mu, double *delta,
+                                      double *bound);
+/* nsteps of RKC2 in one call, as the ROCK methods step (example/advection_kinetic.jl:135
+ * uses ROCK4): before every step the spectral radius (frgpu_spectral_radius,
+ * maxiter), then the fewest stages s >= 2 (s = 2, then max(s + 1, floor(1.1 s)))
+ * whose stability bound covers dt rho, at most smax, and the step
+ * (frgpu_step_rock with frgpu_rkc2_coefficients(s, eps), cached per s).
+ * stages (nsteps entries, may be NULL) receives each step's s.  Fails with
+ * FRGPU_ERR_DT when dt rho needs more than smax stages. */
+FRGPU_API int frgpu_step_rkc2(frgpu_problem *p, double dt, int nsteps, double eps, int smax, int maxiter,
+                              int *stages);
 /* dt = cfl / max over points of sum_d (|u_d| + c)/dx_d (FP64 max-reduction on the GPU);
  * with a per-point metric (frgpu_problem_set_metric) the rate at a point is
  * (lambda_r + lambda_s)/2 with the contravariant speeds lambda_r = |a11 u + a12 v|

@@ -72,6 +72,27 @@ def test_rkc2_and_rock_adapters(frgpu):
     np.testing.assert_array_equal(de, 0.0)
 
 
+@pytest.mark.parametrize("eps", [2 / 13, 0.0, 0.05])
+def test_library_rkc2_coefficients_equal_the_restatement(frgpu, eps):
+    """frgpu_rkc2_coefficients (host C++, used by frgpu_step_rkc2) gives the
+    bits of the numpy restatement rkc2_coefficients: the same operations in the
+    same order."""
+    import ctypes as C
+
+    from frgpu import _lib as L
+
+    for s in (2, 3, 4, 7, 16, 100, 1000):
+        out = [np.zeros(s) for _ in range(4)]
+        bound = C.c_double()
+        L.check(L.lib().frgpu_rkc2_coefficients(s, eps, *(x.ctypes.data_as(C.POINTER(C.c_double)) for x in out),
+                                                C.byref(bound)))
+        ref = frgpu.rkc2_coefficients(s, eps)
+        for a, b in zip(out, ref[:4]):
+            assert np.array_equal(a, b), s
+        assert bound.value == ref[4], s
+    assert L.lib().frgpu_rkc2_coefficients(1, eps, None, None, None, None, None) != 0
+
+
 def _advection(frgpu, oracle, ne=16, deg=2):
     ps = frgpu.FRPSpace1D(0, 1, ne, deg)
     po = oracle_space1d(ps, 0, 1, ne, deg)

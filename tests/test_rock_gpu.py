@@ -161,6 +161,22 @@ def test_rkc2_integrator_on_advection_kinetic(frgpu, oracle, tau):
     assert blown
 
 
+def test_step_rkc2_equals_the_host_driven_loop(frgpu, oracle):
+    """frgpu_step_rkc2 (spectral radius, stage count and coefficients chosen in
+    the library, n steps per call) against the same method driven step by step
+    from the host (frgpu_spectral_radius, the Python stage choice and
+    coefficients, frgpu_step_rock): the same stage counts and the same bits."""
+    dt, n = 5e-4, 40
+    a = frgpu.init(kinetic_pair(frgpu, oracle, 1e-4)[1], frgpu.RKC2(), dt=dt)
+    a.step(n)
+    rk = frgpu.RKC2()
+    generic = frgpu.Stabilized(rk.coefficients, "RKC2 from the host", rk.maxiter)
+    b = frgpu.init(kinetic_pair(frgpu, oracle, 1e-4)[1], generic, dt=dt)
+    b.step(n)
+    assert a.stages == b.stages and len(a.stages) == n
+    assert np.array_equal(a.u, b.u)
+
+
 def test_rock_graphs_follow_coefficients(frgpu, oracle):
     """Alternating coefficient sets replay their own captured graphs; the
     result equals stepping each set in turn on the oracle."""
