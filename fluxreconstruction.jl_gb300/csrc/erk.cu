@@ -355,7 +355,140 @@ template <class Real> __global__ void __launch_bounds__(256) k_fill(Real *__rest
 // flip one component of v about u: v[i] = u[i] - (v[i] - u[i])
 template <class Real> __global__ void k_flip(Real *v, const Real *u, size_t i) { v[i] = u[i] - (v[i] - u[i]); }
 
+// ---- the power method's scalar logic on the device (its graph form) ----
+// The same double arithmetic and tests as frgpu_spectral_radius's host loop
+// (this file is built without multiply-add contraction), so both forms take the
+// same iterations to the same bits.
+__global__ void k_pm_start(fr_power_ctl *c, size_t n, double uround, double sq, int maxiter) {
+    const double ynrm = c->ynrm, vnrm = c->vnrm;
+    double dynrm;
+    if (ynrm != 0.0 && vnrm != 0.0) {
+        dynrm = ynrm * sq;
+        c->mode = 0; // v = u + (dynrm / vnrm) d0
+        c->coef = dynrm / vnrm;
+    } else if (ynrm != 0.0) {
+        dynrm = ynrm * sq;
+        c->mode = 1; // v = u + sq u
+        c->coef = sq;
+    } else if (vnrm != 0.0) {
+        dynrm = uround;
+        c->mode = 0;
+        c->coef = dynrm / vnrm;
+    } else {
+        dynrm = uround;
+        c->mode = 2; // v = dynrm / sqrt(n)
+        c->coef = dynrm / sqrt((double)n);
+    }
+    c->dynrm = dynrm;
+    c->sigma = 0.0;
+    c->it = 0;
+    c->done = 0;
+    c->converged = 0;
+    c->maxiter = maxiter;
+}
+
+template <class Real>
+__global__ void __launch_bounds__(256) k_pm_vinit(Real *__restrict__ v, const Real *__restrict__ u,
+                                                  const Real *__restrict__ d0, const fr_power_ctl *c, size_t n) {
+    const int mode = c->mode;
+    const double coef = c->coef;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        if (mode == 2)
+            v[q] = (Real)coef;
+        else
+            v[q] = u[q] + (Real)coef * (mode == 1 ? u[q] : d0[q]);
+    }
+}
+
+// One iteration's estimate and test; ends the loop (condition 0) when it
+// settled or reached maxiter, else prepares the update of v.
+__global__ void k_pm_step(fr_power_ctl *c, size_t n, cudaGraphConditionalHandle h) {
+    const int it = ++c->it;
+    const double dfnrm = c->dfnrm;
+    const double sigmal = c->sigma;
+    const double sigma = dfnrm / c->dynrm;
+    c->sigma = sigma;
+    if (it >= 2 && fabs(sigma - sigmal) <= fmax(sigma, 1e-300) * 0.01) {
+        c->converged = 1;
+        c->done = 1;
+    } else if (it >= c->maxiter) {
+        c->done = 1;
+    } else if (dfnrm != 0.0) {
+        c->mode = 0; // v = u + (dynrm / dfnrm) (f(v) - f(u))
+        c->coef = c->dynrm / dfnrm;
+    } else {
+        c->mode = 1; // flip component it % n of v about u
+        c->flip = (long)((size_t)it % n);
+    }
+    cudaGraphSetConditional(h, c->done ? 0u : 1u);
+}
+
+template <class Real>
+__global__ void __launch_bounds__(256) k_pm_update(Real *__restrict__ v, const Real *__restrict__ u,
+                                                   const Real *__restrict__ fv, const Real *__restrict__ fu,
+                                                   const fr_power_ctl *c, size_t n) {
+    if (c->done) return;
+    if (c->mode == 1) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            const size_t i = (size_t)c->flip;
+            v[i] = u[i] - (v[i] - u[i]);
+        }
+        return;
+    }
+    const double coef = c->coef;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+        v[q] = u[q] + (Real)coef * (fv[q] - fu[q]);
+}
+
+__global__ void k_pm_finish(const fr_power_ctl *c, double *host_rho, int *host_iters) {
+    *host_rho = 1.2 * c->sigma;
+    *host_iters = c->converged ? c->it : -c->it;
+}
+
 } // namespace
+
+int fr_pm_start(cudaStream_t st, fr_power_ctl *ctl, size_t n, double uround, double sq, int maxiter) {
+    k_pm_start<<<1, 1, 0, st>>>(ctl, n, uround, sq, maxiter);
+    FR_CUDA(cudaGetLastError());
+    return FRGPU_OK;
+}
+
+int fr_pm_vinit(cudaStream_t st, bool f32, size_t n, void *v, const void *u, const void *d0, const fr_power_ctl *ctl) {
+    if (f32)
+        k_pm_vinit<float><<<grid_for(n), 256, 0, st>>>((float *)v, (const float *)u, (const float *)d0, ctl, n);
+    else
+        k_pm_vinit<double><<<grid_for(n), 256, 0, st>>>((double *)v, (const double *)u, (const double *)d0, ctl, n);
+    FR_CUDA(cudaGetLastError());
+    return FRGPU_OK;
+}
+
+int fr_pm_step(cudaStream_t st, fr_power_ctl *ctl, size_t n, cudaGraphConditionalHandle h) {
+    k_pm_step<<<1, 1, 0, st>>>(ctl, n, h);
+    FR_CUDA(cudaGetLastError());
+    return FRGPU_OK;
+}
+
+int fr_pm_update(cudaStream_t st, bool f32, size_t n, void *v, const void *u, const void *fv, const void *fu,
+                 const fr_power_ctl *ctl) {
+    if (f32)
+        k_pm_update<float><<<grid_for(n), 256, 0, st>>>((float *)v, (const float *)u, (const float *)fv,
+                                                        (const float *)fu, ctl, n);
+    else
+        k_pm_update<double><<<grid_for(n), 256, 0, st>>>((double *)v, (const double *)u, (const double *)fv,
+                                                         (const double *)fu, ctl, n);
+    FR_CUDA(cudaGetLastError());
+    return FRGPU_OK;
+}
+
+int fr_pm_finish(cudaStream_t st, const fr_power_ctl *ctl, double *host_rho, int *host_iters) {
+    double *dr = nullptr;
+    int *di = nullptr;
+    FR_CUDA(cudaHostGetDevicePointer((void **)&dr, host_rho, 0));
+    FR_CUDA(cudaHostGetDevicePointer((void **)&di, host_iters, 0));
+    k_pm_finish<<<1, 1, 0, st>>>(ctl, dr, di);
+    FR_CUDA(cudaGetLastError());
+    return FRGPU_OK;
+}
 
 int fr_rock_enqueue_raw(const fr_rock_raw &r, int (*residual)(void *, const void *, void *), void *ctx) {
     return r.f32 ? rock_enqueue_t<float>(r, residual, ctx) : rock_enqueue_t<double>(r, residual, ctx);
@@ -407,8 +540,14 @@ int fr_vec_flip(cudaStream_t st, bool f32, void *v, const void *u, size_t i) {
 int fr_vec_norm2(cudaStream_t st, bool f32, size_t n, const void *x, const void *y, double *d_part, unsigned *cnt,
                  double *host_out, const int *d_status, int *host_status) {
     double *dev_out = nullptr;
-    int *dev_status = nullptr;
     FR_CUDA(cudaHostGetDevicePointer((void **)&dev_out, host_out, 0));
+    return fr_vec_norm2_to(st, f32, n, x, y, d_part, cnt, dev_out, d_status, host_status);
+}
+
+// the same with the norm written to device memory (dev_out)
+int fr_vec_norm2_to(cudaStream_t st, bool f32, size_t n, const void *x, const void *y, double *d_part, unsigned *cnt,
+                    double *dev_out, const int *d_status, int *host_status) {
+    int *dev_status = nullptr;
     FR_CUDA(cudaHostGetDevicePointer((void **)&dev_status, host_status, 0));
     const int nb = grid_for(n) < FR_RED_BLOCKS ? grid_for(n) : FR_RED_BLOCKS;
     if (f32)

@@ -76,6 +76,8 @@ struct frgpu_problem {
     struct host_words {
         double red[6];
         double norm[2]; // power-method norms
+        double pm_rho;  // the graph form of the power method: 1.2 x the estimate
+        int pm_iters;   // and its iterations (negative: not settled)
         int status;
     } *h_words = nullptr;
     // captured reductions (kernels + copies of the results and the status word),
@@ -114,6 +116,16 @@ struct frgpu_problem {
     std::vector<rock_graph> rock_graphs; // most recently used last
     // nonlinear power method: direction of the last estimate, work vectors, norm partials
     void *d_eig = nullptr; // 4 n values: direction, v, f(u), f(v)
+    // the warm-started power method as one graph (a while-loop node over the
+    // iterations), per state buffer and iteration limit
+    struct pm_graph {
+        const void *u;
+        int maxiter;
+        cudaGraphExec_t gexec;
+        long pro, body, epi; // kernels of the prologue, of one iteration, of the epilogue
+    };
+    std::vector<pm_graph> pm_graphs;
+    struct fr_power_ctl *d_pm = nullptr;
     bool have_eig = false;
     double *d_eig_red = nullptr; // FR_RED_BLOCKS partials + the last-block counter
     std::map<int, std::vector<double>> rkc2_cache; // frgpu_step_rkc2: s -> alpha, beta, mu, delta, bound
@@ -282,5 +294,19 @@ int fr_vec_axpy_diff(cudaStream_t st, bool f32, size_t n, void *out, const void 
                      double c); // out = x + c (a - b)
 int fr_vec_fill(cudaStream_t st, bool f32, size_t n, void *v, double c);
 int fr_vec_flip(cudaStream_t st, bool f32, void *v, const void *u, size_t i);
+// Device state of the graph form of the power method (erk.cu).
+struct fr_power_ctl {
+    double ynrm, vnrm, dfnrm, dynrm, sigma, coef;
+    long flip;
+    int it, done, converged, maxiter, mode;
+};
+int fr_pm_start(cudaStream_t st, fr_power_ctl *ctl, size_t n, double uround, double sq, int maxiter);
+int fr_pm_vinit(cudaStream_t st, bool f32, size_t n, void *v, const void *u, const void *d0, const fr_power_ctl *ctl);
+int fr_pm_step(cudaStream_t st, fr_power_ctl *ctl, size_t n, cudaGraphConditionalHandle h);
+int fr_pm_update(cudaStream_t st, bool f32, size_t n, void *v, const void *u, const void *fv, const void *fu,
+                 const fr_power_ctl *ctl);
+int fr_pm_finish(cudaStream_t st, const fr_power_ctl *ctl, double *host_rho, int *host_iters);
 int fr_vec_norm2(cudaStream_t st, bool f32, size_t n, const void *x, const void *y, double *d_part, unsigned *cnt,
                  double *host_out, const int *d_status, int *host_status);
+int fr_vec_norm2_to(cudaStream_t st, bool f32, size_t n, const void *x, const void *y, double *d_part, unsigned *cnt,
+                    double *dev_out, const int *d_status, int *host_status);

@@ -286,6 +286,9 @@ static void drop_rock_graphs(frgpu_problem *p) {
     for (auto &g : p->rock_graphs)
         if (g.gexec) cudaGraphExecDestroy(g.gexec);
     p->rock_graphs.clear();
+    for (auto &g : p->pm_graphs)
+        if (g.gexec) cudaGraphExecDestroy(g.gexec);
+    p->pm_graphs.clear();
 }
 
 static void free_problem(frgpu_problem *p) {
@@ -302,7 +305,8 @@ static void free_problem(frgpu_problem *p) {
     void *bufs[] = {p->s0,     p->s1,      p->s2,         p->s3,      p->d_dt,      p->d_status, p->d_red,
                     p->d_flags, p->d_count, p->d_velo,     p->d_w,     p->d_J,       p->d_V,      p->d_iV,
                     p->rhs_in, p->rhs_out, p->d_bgk_prim, p->d_bgk_frag, p->d_stage, p->d_erk,   p->d_met,
-                    p->d_nfx,  p->d_nfy,   p->d_fsc,      p->d_rock,  p->d_eig,     p->d_eig_red, p->d_c2};
+                    p->d_nfx,  p->d_nfy,   p->d_fsc,      p->d_rock,  p->d_eig,     p->d_eig_red, p->d_c2,
+                    p->d_pm};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -917,6 +921,137 @@ FRGPU_API int frgpu_step_rock(frgpu_problem *p, int m, const double *alpha, cons
 // the ROCK methods use): v = u + dynrm d / |d|, sigma = |f(v) - f(u)| / dynrm,
 // v <- u + (f(v) - f(u)) dynrm / |f(v) - f(u)| until sigma changes by at most
 // 1 %, rho = 1.2 sigma.  d starts from the previous call's direction, else f(u).
+// The warm-started power method (a direction from the previous call) as one
+// graph: the prologue (f(u), the norms of u and of the direction, the start
+// vector), a while-loop node whose body is one iteration (f(v), ||f(v) - f(u)||,
+// the estimate and its test on the device, which ends the loop, and the update
+// of v), and the epilogue (the next direction, rho and the iteration count into
+// page-locked host words).  One host synchronisation per call instead of one per
+// iteration; the same operations as the host loop, so the same bits.
+static int build_pm_graph(frgpu_problem *p, int maxiter, const void *u, frgpu_problem::pm_graph &out) {
+    const bool f32 = p->d.precision == FRGPU_FP32K;
+    const size_t n = (size_t)p->ndof, es = p->esize;
+    char *base = (char *)p->d_eig;
+    void *dir = base, *v = base + n * es, *fu = base + 2 * n * es, *fv = base + 3 * n * es;
+    cudaStream_t st = p->stream;
+    unsigned *cnt = reinterpret_cast<unsigned *>(p->d_eig_red + FR_RED_BLOCKS);
+    fr_power_ctl *c = p->d_pm;
+    const double uround = f32 ? 0x1p-24 : 0x1p-53, sq = std::sqrt(uround);
+    auto norm_to = [&](const void *x, const void *y, double *dev_out) {
+        return fr_vec_norm2_to(st, f32, n, x, y, p->d_eig_red, cnt, dev_out, p->d_status, &p->h_words->status);
+    };
+    cudaGraph_t gp = nullptr, ge = nullptr, g = nullptr;
+    auto cleanup = [&]() {
+        for (cudaGraph_t x : {gp, ge, g})
+            if (x) cudaGraphDestroy(x);
+    };
+    const long l0 = p->launches;
+    int rc = FRGPU_OK;
+    cudaError_t ce;
+    // prologue
+    FR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    rc = residual_into(p, u, fu);
+    if (!rc) rc = norm_to(u, nullptr, &c->ynrm);
+    if (!rc) rc = norm_to(dir, nullptr, &c->vnrm);
+    if (!rc) rc = fr_pm_start(st, c, n, uround, sq, maxiter);
+    if (!rc) rc = fr_pm_vinit(st, f32, n, v, u, dir, c);
+    ce = cudaStreamEndCapture(st, &gp);
+    const long pro = p->launches - l0 + 4;
+    if (rc || ce != cudaSuccess) {
+        p->launches = l0;
+        cleanup();
+        return rc ? rc : fr_cuda_fail(ce, "power method graph: prologue capture");
+    }
+    // the while-loop over the iterations
+    cudaGraphNode_t npro = nullptr, ncond = nullptr, nepi = nullptr;
+    cudaGraphConditionalHandle h;
+    cudaGraphNodeParams cp = {};
+    if ((ce = cudaGraphCreate(&g, 0)) != cudaSuccess ||
+        (ce = cudaGraphAddChildGraphNode(&npro, g, nullptr, 0, gp)) != cudaSuccess ||
+        (ce = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess) {
+        p->launches = l0;
+        cleanup();
+        return fr_cuda_fail(ce, "power method graph: loop node");
+    }
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    if ((ce = cudaGraphAddNode(&ncond, g, &npro, nullptr, 1, &cp)) != cudaSuccess) {
+        p->launches = l0;
+        cleanup();
+        return fr_cuda_fail(ce, "power method graph: loop node");
+    }
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    const long l1 = p->launches;
+    if ((ce = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
+        cudaSuccess) {
+        p->launches = l0;
+        cleanup();
+        return fr_cuda_fail(ce, "power method graph: body capture");
+    }
+    rc = residual_into(p, v, fv);
+    if (!rc) rc = norm_to(fv, fu, &c->dfnrm);
+    if (!rc) rc = fr_pm_step(st, c, n, h);
+    if (!rc) rc = fr_pm_update(st, f32, n, v, u, fv, fu, c);
+    ce = cudaStreamEndCapture(st, &body);
+    const long bodyk = p->launches - l1 + 3;
+    if (rc || ce != cudaSuccess) {
+        p->launches = l0;
+        cleanup();
+        return rc ? rc : fr_cuda_fail(ce, "power method graph: body capture");
+    }
+    // epilogue
+    FR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    rc = fr_vec_axpy_diff(st, f32, n, dir, nullptr, v, u, 1.0);
+    if (!rc) rc = fr_pm_finish(st, c, &p->h_words->pm_rho, &p->h_words->pm_iters);
+    ce = cudaStreamEndCapture(st, &ge);
+    p->launches = l0;
+    if (rc || ce != cudaSuccess) {
+        cleanup();
+        return rc ? rc : fr_cuda_fail(ce, "power method graph: epilogue capture");
+    }
+    if ((ce = cudaGraphAddChildGraphNode(&nepi, g, &ncond, 1, ge)) != cudaSuccess ||
+        (ce = cudaGraphInstantiate(&out.gexec, g, 0)) != cudaSuccess) {
+        cleanup();
+        return fr_cuda_fail(ce, "power method graph: instantiate");
+    }
+    cleanup();
+    out.u = u;
+    out.maxiter = maxiter;
+    out.pro = pro;
+    out.body = bodyk;
+    out.epi = 2;
+    return FRGPU_OK;
+}
+
+static int spectral_radius_graph(frgpu_problem *p, int maxiter, double *rho, int *iters) {
+    const void *u = fr_state_hi(p);
+    if (!p->d_pm) FR_CUDA(cudaMalloc((void **)&p->d_pm, sizeof(fr_power_ctl)));
+    frgpu_problem::pm_graph *g = nullptr;
+    for (auto &x : p->pm_graphs)
+        if (x.u == u && x.maxiter == maxiter) g = &x;
+    if (!g) {
+        if (p->pm_graphs.size() >= 4) {
+            FR_CUDA(cudaStreamSynchronize(p->stream));
+            cudaGraphExecDestroy(p->pm_graphs.front().gexec);
+            p->pm_graphs.erase(p->pm_graphs.begin());
+        }
+        frgpu_problem::pm_graph ng{};
+        int rc = build_pm_graph(p, maxiter, u, ng);
+        if (rc) return rc;
+        p->pm_graphs.push_back(ng);
+        g = &p->pm_graphs.back();
+    }
+    FR_CUDA(cudaGraphLaunch(g->gexec, p->stream));
+    FR_CUDA(cudaStreamSynchronize(p->stream));
+    const int it = p->h_words->pm_iters;
+    p->launches += g->pro + (long)(it < 0 ? -it : it) * g->body + g->epi;
+    *rho = p->h_words->pm_rho;
+    if (iters) *iters = it;
+    return status_error(p, p->h_words->status);
+}
+
 FRGPU_API int frgpu_spectral_radius(frgpu_problem *p, int maxiter, double *rho, int *iters) {
     FR_REQ(p && rho, "spectral_radius: null argument");
     FR_REQ(maxiter >= 1 && maxiter <= 10000, "spectral_radius: need 1 <= maxiter <= 10000");
@@ -929,6 +1064,7 @@ FRGPU_API int frgpu_spectral_radius(frgpu_problem *p, int maxiter, double *rho, 
         FR_CUDA(cudaMemset(p->d_eig_red + FR_RED_BLOCKS, 0, sizeof(double))); // the norms' last-block counter
         p->have_eig = false;
     }
+    if (p->have_eig) return spectral_radius_graph(p, maxiter, rho, iters);
     char *base = (char *)p->d_eig;
     void *dir = base, *v = base + n * es, *fu = base + 2 * n * es, *fv = base + 3 * n * es;
     const void *u = fr_state_hi(p);

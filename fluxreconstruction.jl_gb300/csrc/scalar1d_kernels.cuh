@@ -271,13 +271,118 @@ template <class Real, int NP> struct BGKArgs {
     int *status;
 };
 
+// Transport, relaxation and stage update of velocity v of element i (neighbours
+// il, ir), given the element's (rho, U, lambda) per solution point.
+template <class Real, int NP, int MODE, int STAGE, class Prim>
+__device__ __forceinline__ int bgk_velocity(const BGKArgs<Real, NP> &a, int i, int il, int ir, int v,
+                                            const Prim &prim) {
+    const int nv = a.nvel;
+    const Ops<Real, NP> &op = a.ops;
+    const Real J = a.J[i], JL = a.J[il], JR = a.J[ir];
+    const Real dt = (Real)(*a.dtp);
+    const Real pi_inv = Real(0.31830988618379067154);
+    int bad = 0;
+    const Real vel = a.velo[v];
+    const bool up = vel > Real(0); // heaviside(v)
+    Real u[NP], f[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        u[k] = ld_state(a.uin, a.din, ((size_t)i * NP + k) * nv + v);
+        f[k] = divR<Real>(vel * u[k], J);
+    }
+    const Real fL = dotw<Real, NP>(f, op.ll), fR = dotw<Real, NP>(f, op.lr);
+    // upwind face fluxes: from the left neighbour's right trace when v > 0,
+    // else from this element's left trace (and likewise on the right face)
+    Real Fl, Fr;
+    {
+        Real g[NP];
+        const int nb = up ? il : ir;
+        const Real Jn = up ? JL : JR;
+#pragma unroll
+        for (int k = 0; k < NP; ++k) g[k] = vel * ld_state(a.uin, a.din, ((size_t)nb * NP + k) * nv + v) / Jn;
+        if (up) {
+            Fl = dotw<Real, NP>(g, op.lr);
+            Fr = fR;
+        } else {
+            Fl = fL;
+            Fr = dotw<Real, NP>(g, op.ll);
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < NP; ++m) {
+        const Real rho = prim[m][0], U = prim[m][1], lam = prim[m][2];
+        const Real dv = vel - U;
+        const Real M = rho * sqrtP<Real>(lam * pi_inv) * exp(-lam * dv * dv);
+        const Real r = dotw<Real, NP>(f, op.D[m]);
+        const Real du = -fmaR<Real>(Fr - fR, op.dgr[m], fmaR<Real>(Fl - fL, op.dgl[m], r)) + (M - u[m]) / a.tau;
+        const size_t idx = ((size_t)i * NP + m) * nv + v;
+        const Real res = stage_update<Real, MODE, STAGE>(du, u[m], dt, idx, a.un, a.uin, a.din, a.out, a.ul);
+        if (!isfinite(res)) bad |= ST_NONFINITE;
+    }
+    return bad;
+}
+
+// (rho, U, lambda) of one solution point from its FP64 moments (rho, m, 2E):
+// closure 0: conserve_prim(w, gamma = 3) (1D): lambda = 0.5 rho / (gamma - 1) / (E - m^2 / (2 rho));
+// closure 1: prim = [rho, a, 1] (example/advection_kinetic.jl:80-86)
+template <class Real, int NP>
+__device__ __forceinline__ bool bgk_prim(const BGKArgs<Real, NP> &a, double w0, double w1, double w2, Real (&pr)[3]) {
+    w2 *= 0.5;
+    const double U = a.closure ? a.a_adv : w1 / w0;
+    const double lam = a.closure ? 1.0 : 0.5 * w0 / 2.0 / (w2 - 0.5 * w1 * w1 / w0);
+    pr[0] = (Real)w0;
+    pr[1] = (Real)U;
+    pr[2] = (Real)lam;
+    return w0 > 0.0 && lam > 0.0;
+}
+
+// Small velocity sets (nvel <= 64): one warp per element and per block, the
+// moments reduced by a fixed butterfly inside the warp (no idle warps and no
+// block barrier; the block-per-element form leaves 7 of its 8 warps without
+// velocities at 28 of them, yet runs their FP64 reductions).  One warp per block
+// spreads the elements over the SMs: the FP64 work of an element is bound by
+// its SM's FP64 pipe (GB300: 1/64 of the FP32 rate), so four elements on one SM
+// took four times as long.
+template <class Real, int NP, int MODE, int STAGE>
+__global__ void __launch_bounds__(32) k_bgk1d_warp(const BGKArgs<Real, NP> a) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x;
+    const int ne = a.ne, nv = a.nvel;
+    if (i >= ne) return; // whole warp
+    const int il = i == 0 ? ne - 1 : i - 1, ir = i == ne - 1 ? 0 : i + 1;
+    double mom[NP][3];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) mom[k][0] = mom[k][1] = mom[k][2] = 0.0;
+    for (int v = lane; v < nv; v += 32) {
+        const double vel = (double)a.velo[v], wv = (double)a.w[v];
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+            const double x = (double)ld_state(a.uin, a.din, ((size_t)i * NP + k) * nv + v);
+            mom[k][0] += wv * x;
+            mom[k][1] += wv * vel * x;
+            mom[k][2] += wv * (vel * vel) * x;
+        }
+    }
+    Real prim[NP][3];
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+            for (int off = 16; off > 0; off >>= 1) mom[k][q] += __shfl_xor_sync(0xffffffffu, mom[k][q], off);
+        ok = bgk_prim<Real, NP>(a, mom[k][0], mom[k][1], mom[k][2], prim[k]) && ok;
+    }
+    if (!ok && lane == 0) atomicOr(a.status, ST_UNPHYSICAL);
+    int bad = 0;
+    for (int v = lane; v < nv; v += 32) bad |= bgk_velocity<Real, NP, MODE, STAGE>(a, i, il, ir, v, prim);
+    if (bad) atomicOr(a.status, bad);
+}
+
 template <class Real, int NP, int MODE, int STAGE>
 __global__ void __launch_bounds__(NTB) k_bgk1d(const BGKArgs<Real, NP> a) {
     const int i = blockIdx.x;
     const int ne = a.ne, nv = a.nvel;
     const int il = i == 0 ? ne - 1 : i - 1, ir = i == ne - 1 ? 0 : i + 1;
-    const Ops<Real, NP> &op = a.ops;
-    const Real J = a.J[i], JL = a.J[il], JR = a.J[ir];
     __shared__ double s_red[3 * NP][NTB / 32];
     __shared__ Real s_prim[NP][3];
     // moments: sum_v w_v [1, v, v^2/2] u(v) per solution point (FP64 accumulation)
@@ -311,59 +416,11 @@ __global__ void __launch_bounds__(NTB) k_bgk1d(const BGKArgs<Real, NP> a) {
             w1 += s_red[k * 3 + 1][wq];
             w2 += s_red[k * 3 + 2][wq];
         }
-        w2 *= 0.5;
-        // closure 0: conserve_prim(w, gamma = 3) (1D): lambda = 0.5 rho / (gamma - 1) / (E - m^2 / (2 rho));
-        // closure 1: prim = [rho, a, 1] (example/advection_kinetic.jl:80-86)
-        const double U = a.closure ? a.a_adv : w1 / w0;
-        const double lam = a.closure ? 1.0 : 0.5 * w0 / 2.0 / (w2 - 0.5 * w1 * w1 / w0);
-        s_prim[k][0] = (Real)w0;
-        s_prim[k][1] = (Real)U;
-        s_prim[k][2] = (Real)lam;
-        if (!(w0 > 0.0) || !(lam > 0.0)) atomicOr(a.status, ST_UNPHYSICAL);
+        if (!bgk_prim<Real, NP>(a, w0, w1, w2, s_prim[k])) atomicOr(a.status, ST_UNPHYSICAL);
     }
     __syncthreads();
-    const Real dt = (Real)(*a.dtp);
-    const Real pi_inv = Real(0.31830988618379067154);
     int bad = 0;
-    for (int v = threadIdx.x; v < nv; v += NTB) {
-        const Real vel = a.velo[v];
-        const bool up = vel > Real(0); // heaviside(v)
-        Real u[NP], f[NP];
-#pragma unroll
-        for (int k = 0; k < NP; ++k) {
-            u[k] = ld_state(a.uin, a.din, ((size_t)i * NP + k) * nv + v);
-            f[k] = divR<Real>(vel * u[k], J);
-        }
-        const Real fL = dotw<Real, NP>(f, op.ll), fR = dotw<Real, NP>(f, op.lr);
-        // upwind face fluxes: from the left neighbour's right trace when v > 0,
-        // else from this element's left trace (and likewise on the right face)
-        Real Fl, Fr;
-        {
-            Real g[NP];
-            const int nb = up ? il : ir;
-            const Real Jn = up ? JL : JR;
-#pragma unroll
-            for (int k = 0; k < NP; ++k) g[k] = vel * ld_state(a.uin, a.din, ((size_t)nb * NP + k) * nv + v) / Jn;
-            if (up) {
-                Fl = dotw<Real, NP>(g, op.lr);
-                Fr = fR;
-            } else {
-                Fl = fL;
-                Fr = dotw<Real, NP>(g, op.ll);
-            }
-        }
-#pragma unroll
-        for (int m = 0; m < NP; ++m) {
-            const Real rho = s_prim[m][0], U = s_prim[m][1], lam = s_prim[m][2];
-            const Real dv = vel - U;
-            const Real M = rho * sqrtP<Real>(lam * pi_inv) * exp(-lam * dv * dv);
-            const Real r = dotw<Real, NP>(f, op.D[m]);
-            const Real du = -fmaR<Real>(Fr - fR, op.dgr[m], fmaR<Real>(Fl - fL, op.dgl[m], r)) + (M - u[m]) / a.tau;
-            const size_t idx = ((size_t)i * NP + m) * nv + v;
-            const Real res = stage_update<Real, MODE, STAGE>(du, u[m], dt, idx, a.un, a.uin, a.din, a.out, a.ul);
-            if (!isfinite(res)) bad |= ST_NONFINITE;
-        }
-    }
+    for (int v = threadIdx.x; v < nv; v += NTB) bad |= bgk_velocity<Real, NP, MODE, STAGE>(a, i, il, ir, v, s_prim);
     if (bad) atomicOr(a.status, bad);
 }
 
@@ -447,7 +504,10 @@ int launch_bgk_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     a.a_adv = p->d.a;
     a.ops = make_ops1<Real, NP>(p->sp);
     a.status = p->d_status;
-    k_bgk1d<Real, NP, MODE, STAGE><<<a.ne, NTB, 0, p->stream>>>(a);
+    if (a.nvel <= 64)
+        k_bgk1d_warp<Real, NP, MODE, STAGE><<<a.ne, 32, 0, p->stream>>>(a);
+    else
+        k_bgk1d<Real, NP, MODE, STAGE><<<a.ne, NTB, 0, p->stream>>>(a);
     FR_CUDA(cudaGetLastError());
     p->launches += 1;
     return FRGPU_OK;
