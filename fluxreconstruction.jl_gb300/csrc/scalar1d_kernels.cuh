@@ -275,7 +275,7 @@ template <class Real, int NP> struct BGKArgs {
 // il, ir), given the element's (rho, U, lambda) per solution point.
 template <class Real, int NP, int MODE, int STAGE, class Prim>
 __device__ __forceinline__ int bgk_velocity(const BGKArgs<Real, NP> &a, int i, int il, int ir, int v,
-                                            const Prim &prim) {
+                                            const Prim &prim, int mfirst = 0, int mcount = NP) {
     const int nv = a.nvel;
     const Ops<Real, NP> &op = a.ops;
     const Real J = a.J[i], JL = a.J[il], JR = a.J[ir];
@@ -309,8 +309,10 @@ __device__ __forceinline__ int bgk_velocity(const BGKArgs<Real, NP> &a, int i, i
         }
     }
 #pragma unroll
-    for (int m = 0; m < NP; ++m) {
-        const Real rho = prim[m][0], U = prim[m][1], lam = prim[m][2];
+    for (int mm = 0; mm < NP; ++mm) {
+        if (mm >= mcount) break;
+        const int m = mfirst + mm;
+        const Real rho = prim[mm][0], U = prim[mm][1], lam = prim[mm][2];
         const Real dv = vel - U;
         const Real M = rho * sqrtP<Real>(lam * pi_inv) * exp(-lam * dv * dv);
         const Real r = dotw<Real, NP>(f, op.D[m]);
@@ -336,45 +338,35 @@ __device__ __forceinline__ bool bgk_prim(const BGKArgs<Real, NP> &a, double w0, 
     return w0 > 0.0 && lam > 0.0;
 }
 
-// Small velocity sets (nvel <= 64): one warp per element and per block, the
-// moments reduced by a fixed butterfly inside the warp (no idle warps and no
-// block barrier; the block-per-element form leaves 7 of its 8 warps without
-// velocities at 28 of them, yet runs their FP64 reductions).  One warp per block
-// spreads the elements over the SMs: the FP64 work of an element is bound by
-// its SM's FP64 pipe (GB300: 1/64 of the FP32 rate), so four elements on one SM
-// took four times as long.
+// Small velocity sets (nvel <= 64): one warp per (element, solution point m),
+// the NP warps of an element in one block.  A warp reduces the moments of its
+// point m by a fixed butterfly and updates the values of point m only, so that
+// each thread's dependent FP64 chain (the Maxwellian's exp, the divisions, the
+// stage update) covers one point instead of NP: the form is bound by that chain
+// (GB300's FP64 pipe runs at 1/64 of the FP32 rate), not by the FP64 work.  The
+// block-per-element form would leave 7 of its 8 warps without velocities at 28
+// of them, yet run their FP64 reductions.
 template <class Real, int NP, int MODE, int STAGE>
-__global__ void __launch_bounds__(32) k_bgk1d_warp(const BGKArgs<Real, NP> a) {
-    const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(32 * NP) k_bgk1d_warp(const BGKArgs<Real, NP> a) {
+    const int lane = threadIdx.x & 31, m = threadIdx.x >> 5;
     const int i = blockIdx.x;
     const int ne = a.ne, nv = a.nvel;
-    if (i >= ne) return; // whole warp
     const int il = i == 0 ? ne - 1 : i - 1, ir = i == ne - 1 ? 0 : i + 1;
-    double mom[NP][3];
-#pragma unroll
-    for (int k = 0; k < NP; ++k) mom[k][0] = mom[k][1] = mom[k][2] = 0.0;
+    double mom[3] = {0.0, 0.0, 0.0};
     for (int v = lane; v < nv; v += 32) {
         const double vel = (double)a.velo[v], wv = (double)a.w[v];
-#pragma unroll
-        for (int k = 0; k < NP; ++k) {
-            const double x = (double)ld_state(a.uin, a.din, ((size_t)i * NP + k) * nv + v);
-            mom[k][0] += wv * x;
-            mom[k][1] += wv * vel * x;
-            mom[k][2] += wv * (vel * vel) * x;
-        }
+        const double x = (double)ld_state(a.uin, a.din, ((size_t)i * NP + m) * nv + v);
+        mom[0] += wv * x;
+        mom[1] += wv * vel * x;
+        mom[2] += wv * (vel * vel) * x;
     }
-    Real prim[NP][3];
-    bool ok = true;
 #pragma unroll
-    for (int k = 0; k < NP; ++k) {
-#pragma unroll
-        for (int q = 0; q < 3; ++q)
-            for (int off = 16; off > 0; off >>= 1) mom[k][q] += __shfl_xor_sync(0xffffffffu, mom[k][q], off);
-        ok = bgk_prim<Real, NP>(a, mom[k][0], mom[k][1], mom[k][2], prim[k]) && ok;
-    }
-    if (!ok && lane == 0) atomicOr(a.status, ST_UNPHYSICAL);
+    for (int q = 0; q < 3; ++q)
+        for (int off = 16; off > 0; off >>= 1) mom[q] += __shfl_xor_sync(0xffffffffu, mom[q], off);
+    Real prim[1][3];
+    if (!bgk_prim<Real, NP>(a, mom[0], mom[1], mom[2], prim[0]) && lane == 0) atomicOr(a.status, ST_UNPHYSICAL);
     int bad = 0;
-    for (int v = lane; v < nv; v += 32) bad |= bgk_velocity<Real, NP, MODE, STAGE>(a, i, il, ir, v, prim);
+    for (int v = lane; v < nv; v += 32) bad |= bgk_velocity<Real, NP, MODE, STAGE>(a, i, il, ir, v, prim, m, 1);
     if (bad) atomicOr(a.status, bad);
 }
 
@@ -505,7 +497,7 @@ int launch_bgk_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     a.ops = make_ops1<Real, NP>(p->sp);
     a.status = p->d_status;
     if (a.nvel <= 64)
-        k_bgk1d_warp<Real, NP, MODE, STAGE><<<a.ne, 32, 0, p->stream>>>(a);
+        k_bgk1d_warp<Real, NP, MODE, STAGE><<<a.ne, 32 * NP, 0, p->stream>>>(a);
     else
         k_bgk1d<Real, NP, MODE, STAGE><<<a.ne, NTB, 0, p->stream>>>(a);
     FR_CUDA(cudaGetLastError());
