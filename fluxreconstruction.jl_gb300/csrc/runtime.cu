@@ -805,8 +805,20 @@ static int enqueue_rock(frgpu_problem *p, fr_rock_raw r) {
     return FRGPU_OK;
 }
 
+static int step_rock_impl(frgpu_problem *p, int m, const double *alpha, const double *beta, const double *mu,
+                          const double *delta, int sf, const double *A, const double *b, double dt, int nsteps,
+                          bool wait);
+
 FRGPU_API int frgpu_step_rock(frgpu_problem *p, int m, const double *alpha, const double *beta, const double *mu,
                               const double *delta, int sf, const double *A, const double *b, double dt, int nsteps) {
+    return step_rock_impl(p, m, alpha, beta, mu, delta, sf, A, b, dt, nsteps, true);
+}
+
+// wait = false: the steps are queued and their status is left in the device
+// status word for the next synchronising call
+static int step_rock_impl(frgpu_problem *p, int m, const double *alpha, const double *beta, const double *mu,
+                          const double *delta, int sf, const double *A, const double *b, double dt, int nsteps,
+                          bool wait) {
     FR_REQ(p && alpha && beta && mu && delta, "step_rock: null coefficient array");
     FR_REQ(m >= 1 && m <= FR_ROCK_MAXM, "step_rock: need 1 <= recurrence stages <= 4096");
     FR_REQ(sf >= 0 && sf <= FR_ERK_MAXS, "step_rock: need 0 <= finishing stages <= 16");
@@ -911,7 +923,7 @@ FRGPU_API int frgpu_step_rock(frgpu_problem *p, int m, const double *alpha, cons
         FR_CUDA(cudaGraphLaunch(g.gexec, p->stream));
         p->launches += g.launches;
     }
-    return check_status(p);
+    return wait ? check_status(p) : FRGPU_OK;
     FR_CATCH
 }
 
@@ -1216,12 +1228,14 @@ FRGPU_API int frgpu_step_rkc2(frgpu_problem *p, double dt, int nsteps, double ep
             fr_set_error("step_rkc2: dt * rho needs more than smax stages");
             return FRGPU_ERR_DT;
         }
-        rc = frgpu_step_rock(p, s, c.data(), c.data() + s, c.data() + 2 * s, c.data() + 3 * s, 0, nullptr, nullptr,
-                             dt, 1);
+        // queued without a wait: the next spectral radius (or the check below)
+        // synchronises and reports the step's status
+        rc = step_rock_impl(p, s, c.data(), c.data() + s, c.data() + 2 * s, c.data() + 3 * s, 0, nullptr, nullptr,
+                            dt, 1, false);
         if (rc) return rc;
         if (stages) stages[n] = s;
     }
-    return FRGPU_OK;
+    return check_status(p);
     FR_CATCH
 }
 
