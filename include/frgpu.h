@@ -224,7 +224,10 @@ FRGPU_API int frgpu_rkc2_coefficients(int s, double eps, double *alpha, double *
  * whose stability bound covers dt rho, at most smax, and the step
  * (frgpu_step_rock with frgpu_rkc2_coefficients(s, eps), cached per s).
  * stages (nsteps entries, may be NULL) receives each step's s.  Fails with
- * FRGPU_ERR_DT when dt rho needs more than smax stages. */
+ * FRGPU_ERR_DT when dt rho needs more than smax stages.  A step's device status
+ * (non-finite or unphysical values) is read with the next step's spectral
+ * radius, or after the last step: the call returns at the first failed step,
+ * whose stage count is the last one written to stages. */
 FRGPU_API int frgpu_step_rkc2(frgpu_problem *p, double dt, int nsteps, double eps, int smax, int maxiter,
                               int *stages);
 /* dt = cfl / max over points of sum_d (|u_d| + c)/dx_d (FP64 max-reduction on the GPU);
