@@ -199,6 +199,15 @@ template <class Real, int NP, int FLUX, int MODE, int STAGE, int FUSE = FUSE_NON
 __global__ void __launch_bounds__(Tile<Real, NP, FUSE, STAGE>::TX * NP * Tile<Real, NP, FUSE, STAGE>::TY,
                                   sizeof(Real) == 4 && Tile<Real, NP, FUSE, STAGE>::TX * NP * Tile<Real, NP, FUSE, STAGE>::TY <= 256 ? 3 : 1)
     k_euler2d(const E2DArgs<Real, NP> a) {
+    // programmatic dependent launch: wait for the previous kernel of the stream
+    // (all its writes visible) before touching global memory, and let the next
+    // stage's grid be scheduled as soon as every CTA of this one has started
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    // stage 1 of a step whose third stage runs the fused indicator zeroes that
+    // indicator's counters (a.stats), so that no memset separates the stages
+    if (STAGE == 1 && a.stats != nullptr && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 4)
+        a.stats[threadIdx.x] = 0;
     constexpr int TX = Tile<Real, NP, FUSE, STAGE>::TX, TY = Tile<Real, NP, FUSE, STAGE>::TY;
     constexpr int NT = TX * NP * TY;
     constexpr int NST = Stash<MODE, STAGE>::n;
@@ -756,6 +765,7 @@ int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     a.mlp = frmlp::MLPDev{nullptr, nullptr, nullptr, nullptr, nullptr};
     a.V = a.iV = nullptr;
     a.flags = a.stats = nullptr;
+    if (STAGE == 1 && fr_fused_indicator(p) != FRGPU_IND_NONE) a.stats = p->d_count;
     if (FUSE == FUSE_LEARNED) {
         const fr_mlp_ptrs m = fr_mlp_device(p->mlp);
         a.mlp = frmlp::MLPDev{m.P, (const __nv_bfloat16 *)m.W1, (const __nv_bfloat16 *)m.W2,
@@ -791,10 +801,19 @@ int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     static fr_smem_optin optin;
     if (int rc = fr_raise_smem(kern, S::bytes, optin, p->prepare_only)) return rc;
     if (p->prepare_only) return FRGPU_OK;
-    if (FUSE != FUSE_NONE) FR_CUDA(cudaMemsetAsync(p->d_count, 0, sizeof(int) * 4, p->stream));
-    dim3 grid((a.nx + T::TX - 1) / T::TX, (a.ny + T::TY - 1) / T::TY);
-    kern<<<grid, T::TX * NP * T::TY, S::bytes, p->stream>>>(a);
-    FR_CUDA(cudaGetLastError());
+    // launched with programmatic stream serialisation (the kernel waits at its
+    // top with griddepcontrol.wait)
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((a.nx + T::TX - 1) / T::TX, (a.ny + T::TY - 1) / T::TY);
+    cfg.blockDim = dim3(T::TX * NP * T::TY);
+    cfg.dynamicSmemBytes = S::bytes;
+    cfg.stream = p->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    FR_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
     p->launches += 1;
     return FRGPU_OK;
 }
