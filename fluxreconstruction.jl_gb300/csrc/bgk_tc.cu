@@ -83,6 +83,7 @@ __global__ void __launch_bounds__(32 * MW) k_bgk_moments(const float *__restrict
                                                         const float *__restrict__ velo, const float *__restrict__ w,
                                                         int ne, int nv, float *__restrict__ prim, int *status,
                                                         int closure, double a_adv) {
+    FR_PDL_ENTRY();
     const int row = blockIdx.x * MW + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (row >= ne * NP) return; // whole warp
     const size_t base = (size_t)row * nv;
@@ -150,6 +151,7 @@ __host__ __device__ constexpr int ucore(int r, int k, int K) {
 
 template <int NP, int STAGE>
 __global__ void __launch_bounds__(UT) k_bgk1d_umma(const TCArgs a) {
+    FR_PDL_ENTRY();
     constexpr BTile T = btile(NP);
     constexpr int K = 8 * T.KS;
     constexpr int RG = (T.ROWS + 3) / 4; // rows per warp group in the epilogue
@@ -256,6 +258,7 @@ __global__ void __launch_bounds__(UT) k_bgk1d_umma(const TCArgs a) {
 
 template <int NP, int STAGE>
 __global__ void __launch_bounds__(32 * TCW) k_bgk1d_tc(const TCArgs a) {
+    FR_PDL_ENTRY();
     constexpr BTile T = btile(NP);
     const int ne = a.ne, nv = a.nvel;
     const int i0 = blockIdx.x * T.EB;
@@ -332,9 +335,9 @@ int launch_tc(frgpu_problem *p, int stage, const void *in, const void *din, void
     constexpr BTile T = btile(NP);
     const int ne = p->sp.nx, nv = p->d.nvel;
     const float *uin = (const float *)in, *dn = (const float *)din;
-    k_bgk_moments<NP><<<(ne * NP + MW - 1) / MW, 32 * MW, 0, p->stream>>>(
+    FR_CUDA(fr_launch_opt(false, k_bgk_moments<NP>, (ne * NP + MW - 1) / MW, 32 * MW, 0, p->stream,
         uin, dn, (const float *)p->d_velo, (const float *)p->d_w, ne, nv, p->d_bgk_prim, p->d_status, p->bgk_closure,
-        p->d.a);
+        p->d.a));
     FR_CUDA(cudaGetLastError());
     TCArgs a;
     a.ne = ne;
@@ -355,10 +358,10 @@ int launch_tc(frgpu_problem *p, int stage, const void *in, const void *din, void
     if (p->bgk_tensor == 2) {
         const dim3 ug((ne + T.EB - 1) / T.EB, (nv + UM - 1) / UM);
         switch (stage) {
-        case 0: k_bgk1d_umma<NP, 0><<<ug, UT, 0, p->stream>>>(a); break;
-        case 1: k_bgk1d_umma<NP, 1><<<ug, UT, 0, p->stream>>>(a); break;
-        case 2: k_bgk1d_umma<NP, 2><<<ug, UT, 0, p->stream>>>(a); break;
-        case 3: k_bgk1d_umma<NP, 3><<<ug, UT, 0, p->stream>>>(a); break;
+        case 0: FR_CUDA(fr_launch_opt(false, k_bgk1d_umma<NP, 0>, ug, UT, 0, p->stream, a)); break;
+        case 1: FR_CUDA(fr_launch_opt(false, k_bgk1d_umma<NP, 1>, ug, UT, 0, p->stream, a)); break;
+        case 2: FR_CUDA(fr_launch_opt(false, k_bgk1d_umma<NP, 2>, ug, UT, 0, p->stream, a)); break;
+        case 3: FR_CUDA(fr_launch_opt(false, k_bgk1d_umma<NP, 3>, ug, UT, 0, p->stream, a)); break;
         default: fr_set_error("BGK residual: bad stage"); return FRGPU_ERR_ARG;
         }
         FR_CUDA(cudaGetLastError());
@@ -367,10 +370,10 @@ int launch_tc(frgpu_problem *p, int stage, const void *in, const void *din, void
     }
     const dim3 grid((ne + T.EB - 1) / T.EB, (nv + 8 * TCW - 1) / (8 * TCW));
     switch (stage) {
-    case 0: k_bgk1d_tc<NP, 0><<<grid, 32 * TCW, 0, p->stream>>>(a); break;
-    case 1: k_bgk1d_tc<NP, 1><<<grid, 32 * TCW, 0, p->stream>>>(a); break;
-    case 2: k_bgk1d_tc<NP, 2><<<grid, 32 * TCW, 0, p->stream>>>(a); break;
-    case 3: k_bgk1d_tc<NP, 3><<<grid, 32 * TCW, 0, p->stream>>>(a); break;
+    case 0: FR_CUDA(fr_launch_opt(false, k_bgk1d_tc<NP, 0>, grid, 32 * TCW, 0, p->stream, a)); break;
+    case 1: FR_CUDA(fr_launch_opt(false, k_bgk1d_tc<NP, 1>, grid, 32 * TCW, 0, p->stream, a)); break;
+    case 2: FR_CUDA(fr_launch_opt(false, k_bgk1d_tc<NP, 2>, grid, 32 * TCW, 0, p->stream, a)); break;
+    case 3: FR_CUDA(fr_launch_opt(false, k_bgk1d_tc<NP, 3>, grid, 32 * TCW, 0, p->stream, a)); break;
     default: fr_set_error("BGK residual: bad stage"); return FRGPU_ERR_ARG;
     }
     FR_CUDA(cudaGetLastError());

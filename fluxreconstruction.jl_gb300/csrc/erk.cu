@@ -36,6 +36,7 @@ template <class Real>
 __global__ void __launch_bounds__(256) k_erk_stage(const Real *__restrict__ u, const Real *__restrict__ k,
                                                    size_t kstride, size_t n, const Comb<Real> c,
                                                    const double *dtp, Real *__restrict__ out) {
+    FR_PDL_ENTRY();
     const Real dt = (Real)*dtp;
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
         out[q] = frk::fmaR<Real>(dt, comb_acc<Real>(k, kstride, q, c), __ldg(u + q));
@@ -46,6 +47,7 @@ template <class Real>
 __global__ void __launch_bounds__(256) k_erk_update(Real *__restrict__ u, Real *__restrict__ lo,
                                                     const Real *__restrict__ k, size_t kstride, size_t n, const Comb<Real> c,
                                                     const double *dtp, int *status) {
+    FR_PDL_ENTRY();
     const Real dt = (Real)*dtp;
     bool bad = false;
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
@@ -99,12 +101,12 @@ int fr_erk_enqueue_raw(const fr_erk_raw &r, int (*residual)(void *, const void *
         if (nt > 0) {
             if (!r.prepare_only) {
                 if (r.f32)
-                    k_erk_stage<float><<<grid_for(n), 256, 0, r.stream>>>(
-                        (const float *)r.u, (const float *)kb, kstride, n, comb_of<float>(Ai, i), r.d_dt, (float *)stage);
+                    FR_CUDA(fr_launch(k_erk_stage<float>, grid_for(n), 256, 0, r.stream,
+                        (const float *)r.u, (const float *)kb, kstride, n, comb_of<float>(Ai, i), r.d_dt, (float *)stage));
                 else
-                    k_erk_stage<double><<<grid_for(n), 256, 0, r.stream>>>((const double *)r.u, (const double *)kb,
+                    FR_CUDA(fr_launch(k_erk_stage<double>, grid_for(n), 256, 0, r.stream, (const double *)r.u, (const double *)kb,
                                                                            kstride, n, comb_of<double>(Ai, i),
-                                                                           r.d_dt, (double *)stage);
+                                                                           r.d_dt, (double *)stage));
                 FR_CUDA(cudaGetLastError());
                 *r.launches += 1;
             }
@@ -114,11 +116,11 @@ int fr_erk_enqueue_raw(const fr_erk_raw &r, int (*residual)(void *, const void *
     }
     if (comb_of<double>(r.b, s).nt == 0 || r.prepare_only) return FRGPU_OK;
     if (r.f32)
-        k_erk_update<float><<<grid_for(n), 256, 0, r.stream>>>((float *)r.u, (float *)r.lo, (const float *)kb, kstride,
-                                                               n, comb_of<float>(r.b, s), r.d_dt, r.d_status);
+        FR_CUDA(fr_launch(k_erk_update<float>, grid_for(n), 256, 0, r.stream, (float *)r.u, (float *)r.lo, (const float *)kb, kstride,
+                                                               n, comb_of<float>(r.b, s), r.d_dt, r.d_status));
     else
-        k_erk_update<double><<<grid_for(n), 256, 0, r.stream>>>((double *)r.u, nullptr, (const double *)kb, kstride,
-                                                                n, comb_of<double>(r.b, s), r.d_dt, r.d_status);
+        FR_CUDA(fr_launch(k_erk_update<double>, grid_for(n), 256, 0, r.stream, (double *)r.u, nullptr, (const double *)kb, kstride,
+                                                                n, comb_of<double>(r.b, s), r.d_dt, r.d_status));
     FR_CUDA(cudaGetLastError());
     *r.launches += 1;
     return FRGPU_OK;
@@ -179,6 +181,7 @@ __global__ void __launch_bounds__(256) k_rock_rec(const Real *__restrict__ u, co
                                                   const Real *__restrict__ d2, size_t n, Real alpha, Real beta,
                                                   Real mu, Real delta, const double *dtp, Real *__restrict__ dout,
                                                   Real *__restrict__ yout) {
+    FR_PDL_ENTRY();
     const Real dt = (Real)*dtp;
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
         Real t = mu * __ldg(F + q);
@@ -195,6 +198,7 @@ template <class Real>
 __global__ void __launch_bounds__(256) k_rock_fin(const Real *__restrict__ u, const Real *__restrict__ dm,
                                                   const Real *__restrict__ k, size_t kstride, size_t n,
                                                   const Comb<Real> c, const double *dtp, Real *__restrict__ out) {
+    FR_PDL_ENTRY();
     const Real dt = (Real)*dtp;
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
         out[q] = __ldg(u + q) + frk::fmaR<Real>(dt, comb_acc<Real>(k, kstride, q, c), __ldg(dm + q));
@@ -205,6 +209,7 @@ __global__ void __launch_bounds__(256) k_rock_update(Real *__restrict__ u, Real 
                                                      const Real *__restrict__ dm, const Real *__restrict__ k,
                                                      size_t kstride, size_t n, const Comb<Real> c,
                                                      const double *dtp, int *status) {
+    FR_PDL_ENTRY();
     const Real dt = (Real)*dtp;
     bool bad = false;
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
@@ -238,10 +243,10 @@ int rock_enqueue_t(const fr_rock_raw &r, int (*residual)(void *, const void *, v
         if (j >= 2 && (rc = residual(ctx, Y, F))) return rc;
         if (!r.prepare_only) {
             const double al = r.alpha[j - 1], be = r.beta[j - 1], mu = r.mu[j - 1], de = r.delta[j - 1];
-            k_rock_rec<Real><<<g, 256, 0, r.stream>>>(u, j == 1 ? F0 : F, de != 0.0 ? F0 : nullptr,
+            FR_CUDA(fr_launch(k_rock_rec<Real>, g, 256, 0, r.stream, u, j == 1 ? F0 : F, de != 0.0 ? F0 : nullptr,
                                                       (j >= 2 && al != 0.0) ? Dj(j - 1) : nullptr,
                                                       (j >= 3 && be != 0.0) ? Dj(j - 2) : nullptr, n, (Real)al,
-                                                      (Real)be, (Real)mu, (Real)de, r.d_dt, Dj(j), Y);
+                                                      (Real)be, (Real)mu, (Real)de, r.d_dt, Dj(j), Y));
             FR_CUDA(cudaGetLastError());
             *r.launches += 1;
         }
@@ -253,7 +258,7 @@ int rock_enqueue_t(const fr_rock_raw &r, int (*residual)(void *, const void *, v
         const Real *in = Y;
         if (c.nt > 0) {
             if (!r.prepare_only) {
-                k_rock_fin<Real><<<g, 256, 0, r.stream>>>(u, Dm, K, n, n, c, r.d_dt, S);
+                FR_CUDA(fr_launch(k_rock_fin<Real>, g, 256, 0, r.stream, u, Dm, K, n, n, c, r.d_dt, S));
                 FR_CUDA(cudaGetLastError());
                 *r.launches += 1;
             }
@@ -263,7 +268,7 @@ int rock_enqueue_t(const fr_rock_raw &r, int (*residual)(void *, const void *, v
     }
     if (r.prepare_only) return FRGPU_OK;
     const Comb<Real> cb = r.sf > 0 ? comb_of<Real>(r.b, r.sf) : Comb<Real>{};
-    k_rock_update<Real><<<g, 256, 0, r.stream>>>(u, (Real *)r.lo, Dm, K, n, n, cb, r.d_dt, r.d_status);
+    FR_CUDA(fr_launch(k_rock_update<Real>, g, 256, 0, r.stream, u, (Real *)r.lo, Dm, K, n, n, cb, r.d_dt, r.d_status));
     FR_CUDA(cudaGetLastError());
     *r.launches += 1;
     return FRGPU_OK;
@@ -274,6 +279,7 @@ int rock_enqueue_t(const fr_rock_raw &r, int (*residual)(void *, const void *, v
 template <class Real>
 __global__ void __launch_bounds__(256) k_axpy(Real *__restrict__ out, const Real *__restrict__ x,
                                               const Real *__restrict__ y, double c, size_t n) {
+    FR_PDL_ENTRY();
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
         const Real yq = y ? y[q] : x[q];
         out[q] = x[q] + (Real)c * yq;
@@ -293,6 +299,7 @@ template <class Real>
 __global__ void __launch_bounds__(256) k_axpy_diff(Real *__restrict__ out, const Real *__restrict__ x,
                                                    const Real *__restrict__ a, const Real *__restrict__ b, double c,
                                                    size_t n) {
+    FR_PDL_ENTRY();
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
         out[q] = (x ? x[q] : Real(0)) + (Real)c * (a[q] - b[q]);
 }
@@ -304,6 +311,7 @@ template <class Real>
 __global__ void __launch_bounds__(256) k_norm2(const Real *__restrict__ x, const Real *__restrict__ y, size_t n,
                                                double *__restrict__ part, unsigned *cnt, double *host_out,
                                                const int *dstatus, int *host_status) {
+    FR_PDL_ENTRY();
     __shared__ double s[8];
     __shared__ bool last;
     double acc = 0.0;
@@ -348,18 +356,23 @@ __global__ void __launch_bounds__(256) k_norm2(const Real *__restrict__ x, const
 }
 
 template <class Real> __global__ void __launch_bounds__(256) k_fill(Real *__restrict__ v, double c, size_t n) {
+    FR_PDL_ENTRY();
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
         v[q] = (Real)c;
 }
 
 // flip one component of v about u: v[i] = u[i] - (v[i] - u[i])
-template <class Real> __global__ void k_flip(Real *v, const Real *u, size_t i) { v[i] = u[i] - (v[i] - u[i]); }
+template <class Real> __global__ void k_flip(Real *v, const Real *u, size_t i) {
+    FR_PDL_ENTRY();
+    v[i] = u[i] - (v[i] - u[i]);
+}
 
 // ---- the power method's scalar logic on the device (its graph form) ----
 // The same double arithmetic and tests as frgpu_spectral_radius's host loop
 // (this file is built without multiply-add contraction), so both forms take the
 // same iterations to the same bits.
 __global__ void k_pm_start(fr_power_ctl *c, size_t n, double uround, double sq, int maxiter) {
+    FR_PDL_ENTRY();
     const double ynrm = c->ynrm, vnrm = c->vnrm;
     double dynrm;
     if (ynrm != 0.0 && vnrm != 0.0) {
@@ -390,6 +403,7 @@ __global__ void k_pm_start(fr_power_ctl *c, size_t n, double uround, double sq, 
 template <class Real>
 __global__ void __launch_bounds__(256) k_pm_vinit(Real *__restrict__ v, const Real *__restrict__ u,
                                                   const Real *__restrict__ d0, const fr_power_ctl *c, size_t n) {
+    FR_PDL_ENTRY();
     const int mode = c->mode;
     const double coef = c->coef;
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
@@ -403,6 +417,7 @@ __global__ void __launch_bounds__(256) k_pm_vinit(Real *__restrict__ v, const Re
 // One iteration's estimate and test; ends the loop (condition 0) when it
 // settled or reached maxiter, else prepares the update of v.
 __global__ void k_pm_step(fr_power_ctl *c, size_t n, cudaGraphConditionalHandle h) {
+    FR_PDL_ENTRY();
     const int it = ++c->it;
     const double dfnrm = c->dfnrm;
     const double sigmal = c->sigma;
@@ -427,6 +442,7 @@ template <class Real>
 __global__ void __launch_bounds__(256) k_pm_update(Real *__restrict__ v, const Real *__restrict__ u,
                                                    const Real *__restrict__ fv, const Real *__restrict__ fu,
                                                    const fr_power_ctl *c, size_t n) {
+    FR_PDL_ENTRY();
     if (c->done) return;
     if (c->mode == 1) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -441,6 +457,7 @@ __global__ void __launch_bounds__(256) k_pm_update(Real *__restrict__ v, const R
 }
 
 __global__ void k_pm_finish(const fr_power_ctl *c, double *host_rho, int *host_iters) {
+    FR_PDL_ENTRY();
     *host_rho = 1.2 * c->sigma;
     *host_iters = c->converged ? c->it : -c->it;
 }
@@ -448,22 +465,22 @@ __global__ void k_pm_finish(const fr_power_ctl *c, double *host_rho, int *host_i
 } // namespace
 
 int fr_pm_start(cudaStream_t st, fr_power_ctl *ctl, size_t n, double uround, double sq, int maxiter) {
-    k_pm_start<<<1, 1, 0, st>>>(ctl, n, uround, sq, maxiter);
+    FR_CUDA(fr_launch(k_pm_start, 1, 1, 0, st, ctl, n, uround, sq, maxiter));
     FR_CUDA(cudaGetLastError());
     return FRGPU_OK;
 }
 
 int fr_pm_vinit(cudaStream_t st, bool f32, size_t n, void *v, const void *u, const void *d0, const fr_power_ctl *ctl) {
     if (f32)
-        k_pm_vinit<float><<<grid_for(n), 256, 0, st>>>((float *)v, (const float *)u, (const float *)d0, ctl, n);
+        FR_CUDA(fr_launch(k_pm_vinit<float>, grid_for(n), 256, 0, st, (float *)v, (const float *)u, (const float *)d0, ctl, n));
     else
-        k_pm_vinit<double><<<grid_for(n), 256, 0, st>>>((double *)v, (const double *)u, (const double *)d0, ctl, n);
+        FR_CUDA(fr_launch(k_pm_vinit<double>, grid_for(n), 256, 0, st, (double *)v, (const double *)u, (const double *)d0, ctl, n));
     FR_CUDA(cudaGetLastError());
     return FRGPU_OK;
 }
 
 int fr_pm_step(cudaStream_t st, fr_power_ctl *ctl, size_t n, cudaGraphConditionalHandle h) {
-    k_pm_step<<<1, 1, 0, st>>>(ctl, n, h);
+    FR_CUDA(fr_launch(k_pm_step, 1, 1, 0, st, ctl, n, h));
     FR_CUDA(cudaGetLastError());
     return FRGPU_OK;
 }
@@ -471,11 +488,11 @@ int fr_pm_step(cudaStream_t st, fr_power_ctl *ctl, size_t n, cudaGraphConditiona
 int fr_pm_update(cudaStream_t st, bool f32, size_t n, void *v, const void *u, const void *fv, const void *fu,
                  const fr_power_ctl *ctl) {
     if (f32)
-        k_pm_update<float><<<grid_for(n), 256, 0, st>>>((float *)v, (const float *)u, (const float *)fv,
-                                                        (const float *)fu, ctl, n);
+        FR_CUDA(fr_launch(k_pm_update<float>, grid_for(n), 256, 0, st, (float *)v, (const float *)u, (const float *)fv,
+                                                        (const float *)fu, ctl, n));
     else
-        k_pm_update<double><<<grid_for(n), 256, 0, st>>>((double *)v, (const double *)u, (const double *)fv,
-                                                         (const double *)fu, ctl, n);
+        FR_CUDA(fr_launch(k_pm_update<double>, grid_for(n), 256, 0, st, (double *)v, (const double *)u, (const double *)fv,
+                                                         (const double *)fu, ctl, n));
     FR_CUDA(cudaGetLastError());
     return FRGPU_OK;
 }
@@ -485,7 +502,7 @@ int fr_pm_finish(cudaStream_t st, const fr_power_ctl *ctl, double *host_rho, int
     int *di = nullptr;
     FR_CUDA(cudaHostGetDevicePointer((void **)&dr, host_rho, 0));
     FR_CUDA(cudaHostGetDevicePointer((void **)&di, host_iters, 0));
-    k_pm_finish<<<1, 1, 0, st>>>(ctl, dr, di);
+    FR_CUDA(fr_launch(k_pm_finish, 1, 1, 0, st, ctl, dr, di));
     FR_CUDA(cudaGetLastError());
     return FRGPU_OK;
 }
@@ -496,9 +513,9 @@ int fr_rock_enqueue_raw(const fr_rock_raw &r, int (*residual)(void *, const void
 
 int fr_vec_axpy(cudaStream_t st, bool f32, size_t n, void *out, const void *x, const void *y, double c) {
     if (f32)
-        k_axpy<float><<<grid_for(n), 256, 0, st>>>((float *)out, (const float *)x, (const float *)y, c, n);
+        FR_CUDA(fr_launch(k_axpy<float>, grid_for(n), 256, 0, st, (float *)out, (const float *)x, (const float *)y, c, n));
     else
-        k_axpy<double><<<grid_for(n), 256, 0, st>>>((double *)out, (const double *)x, (const double *)y, c, n);
+        FR_CUDA(fr_launch(k_axpy<double>, grid_for(n), 256, 0, st, (double *)out, (const double *)x, (const double *)y, c, n));
     FR_CUDA(cudaGetLastError());
     return FRGPU_OK;
 }
@@ -506,29 +523,29 @@ int fr_vec_axpy(cudaStream_t st, bool f32, size_t n, void *out, const void *x, c
 int fr_vec_axpy_diff(cudaStream_t st, bool f32, size_t n, void *out, const void *x, const void *a, const void *b,
                      double c) {
     if (f32)
-        k_axpy_diff<float><<<grid_for(n), 256, 0, st>>>((float *)out, (const float *)x, (const float *)a,
-                                                        (const float *)b, c, n);
+        FR_CUDA(fr_launch(k_axpy_diff<float>, grid_for(n), 256, 0, st, (float *)out, (const float *)x, (const float *)a,
+                                                        (const float *)b, c, n));
     else
-        k_axpy_diff<double><<<grid_for(n), 256, 0, st>>>((double *)out, (const double *)x, (const double *)a,
-                                                         (const double *)b, c, n);
+        FR_CUDA(fr_launch(k_axpy_diff<double>, grid_for(n), 256, 0, st, (double *)out, (const double *)x, (const double *)a,
+                                                         (const double *)b, c, n));
     FR_CUDA(cudaGetLastError());
     return FRGPU_OK;
 }
 
 int fr_vec_fill(cudaStream_t st, bool f32, size_t n, void *v, double c) {
     if (f32)
-        k_fill<float><<<grid_for(n), 256, 0, st>>>((float *)v, c, n);
+        FR_CUDA(fr_launch(k_fill<float>, grid_for(n), 256, 0, st, (float *)v, c, n));
     else
-        k_fill<double><<<grid_for(n), 256, 0, st>>>((double *)v, c, n);
+        FR_CUDA(fr_launch(k_fill<double>, grid_for(n), 256, 0, st, (double *)v, c, n));
     FR_CUDA(cudaGetLastError());
     return FRGPU_OK;
 }
 
 int fr_vec_flip(cudaStream_t st, bool f32, void *v, const void *u, size_t i) {
     if (f32)
-        k_flip<float><<<1, 1, 0, st>>>((float *)v, (const float *)u, i);
+        FR_CUDA(fr_launch(k_flip<float>, 1, 1, 0, st, (float *)v, (const float *)u, i));
     else
-        k_flip<double><<<1, 1, 0, st>>>((double *)v, (const double *)u, i);
+        FR_CUDA(fr_launch(k_flip<double>, 1, 1, 0, st, (double *)v, (const double *)u, i));
     FR_CUDA(cudaGetLastError());
     return FRGPU_OK;
 }
@@ -551,11 +568,11 @@ int fr_vec_norm2_to(cudaStream_t st, bool f32, size_t n, const void *x, const vo
     FR_CUDA(cudaHostGetDevicePointer((void **)&dev_status, host_status, 0));
     const int nb = grid_for(n) < FR_RED_BLOCKS ? grid_for(n) : FR_RED_BLOCKS;
     if (f32)
-        k_norm2<float><<<nb, 256, 0, st>>>((const float *)x, (const float *)y, n, d_part, cnt, dev_out, d_status,
-                                           dev_status);
+        FR_CUDA(fr_launch(k_norm2<float>, nb, 256, 0, st, (const float *)x, (const float *)y, n, d_part, cnt, dev_out, d_status,
+                                           dev_status));
     else
-        k_norm2<double><<<nb, 256, 0, st>>>((const double *)x, (const double *)y, n, d_part, cnt, dev_out,
-                                            d_status, dev_status);
+        FR_CUDA(fr_launch(k_norm2<double>, nb, 256, 0, st, (const double *)x, (const double *)y, n, d_part, cnt, dev_out,
+                                            d_status, dev_status));
     FR_CUDA(cudaGetLastError());
     return FRGPU_OK;
 }

@@ -199,11 +199,7 @@ template <class Real, int NP, int FLUX, int MODE, int STAGE, int FUSE = FUSE_NON
 __global__ void __launch_bounds__(Tile<Real, NP, FUSE, STAGE>::TX * NP * Tile<Real, NP, FUSE, STAGE>::TY,
                                   sizeof(Real) == 4 && Tile<Real, NP, FUSE, STAGE>::TX * NP * Tile<Real, NP, FUSE, STAGE>::TY <= 256 ? 3 : 1)
     k_euler2d(const E2DArgs<Real, NP> a) {
-    // programmatic dependent launch: wait for the previous kernel of the stream
-    // (all its writes visible) before touching global memory, and let the next
-    // stage's grid be scheduled as soon as every CTA of this one has started
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    FR_PDL_ENTRY(); // launched by fr_launch: the previous kernel's writes are visible from here on
     // stage 1 of a step whose third stage runs the fused indicator zeroes that
     // indicator's counters (a.stats), so that no memset separates the stages
     if (STAGE == 1 && a.stats != nullptr && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 4)
@@ -801,19 +797,8 @@ int launch_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     static fr_smem_optin optin;
     if (int rc = fr_raise_smem(kern, S::bytes, optin, p->prepare_only)) return rc;
     if (p->prepare_only) return FRGPU_OK;
-    // launched with programmatic stream serialisation (the kernel waits at its
-    // top with griddepcontrol.wait)
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((a.nx + T::TX - 1) / T::TX, (a.ny + T::TY - 1) / T::TY);
-    cfg.blockDim = dim3(T::TX * NP * T::TY);
-    cfg.dynamicSmemBytes = S::bytes;
-    cfg.stream = p->stream;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    FR_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
+    FR_CUDA(fr_launch(kern, dim3((a.nx + T::TX - 1) / T::TX, (a.ny + T::TY - 1) / T::TY), dim3(T::TX * NP * T::TY),
+                      S::bytes, p->stream, a));
     p->launches += 1;
     return FRGPU_OK;
 }

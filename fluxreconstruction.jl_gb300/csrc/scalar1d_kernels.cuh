@@ -63,6 +63,7 @@ __device__ __forceinline__ Real roe_scalar(Real uL, Real fL, Real uR, Real fR, R
 
 template <class Real, int NP, int MODE, int STAGE, bool BURGERS>
 __global__ void __launch_bounds__(NT1) k_scalar1d(const S1DArgs<Real, NP> a) {
+    FR_PDL_ENTRY();
     __shared__ Real s_uR[NT1], s_fR[NT1], s_F[NT1 + 1], s_h[4];
     const int t = threadIdx.x;
     const int i0 = blockIdx.x * NT1;
@@ -174,6 +175,7 @@ __device__ __forceinline__ void trace3(const Real (&u)[NP][3], const Real *w, Re
 
 template <class Real, int NP, int MODE, int STAGE>
 __global__ void __launch_bounds__(NT1) k_euler1d(const S1DArgs<Real, NP> a) {
+    FR_PDL_ENTRY();
     __shared__ Real s_uR[3][NT1], s_F[3][NT1 + 1], s_h[2][3];
     const int t = threadIdx.x;
     const int i0 = blockIdx.x * NT1;
@@ -348,6 +350,7 @@ __device__ __forceinline__ bool bgk_prim(const BGKArgs<Real, NP> &a, double w0, 
 // of them, yet run their FP64 reductions.
 template <class Real, int NP, int MODE, int STAGE>
 __global__ void __launch_bounds__(32 * NP) k_bgk1d_warp(const BGKArgs<Real, NP> a) {
+    FR_PDL_ENTRY();
     const int lane = threadIdx.x & 31, m = threadIdx.x >> 5;
     const int i = blockIdx.x;
     const int ne = a.ne, nv = a.nvel;
@@ -372,6 +375,7 @@ __global__ void __launch_bounds__(32 * NP) k_bgk1d_warp(const BGKArgs<Real, NP> 
 
 template <class Real, int NP, int MODE, int STAGE>
 __global__ void __launch_bounds__(NTB) k_bgk1d(const BGKArgs<Real, NP> a) {
+    FR_PDL_ENTRY();
     const int i = blockIdx.x;
     const int ne = a.ne, nv = a.nvel;
     const int il = i == 0 ? ne - 1 : i - 1, ir = i == ne - 1 ? 0 : i + 1;
@@ -457,9 +461,9 @@ int launch_scalar_t(frgpu_problem *p, const void *in, const void *din, void *out
     auto a = make_args1<Real, NP>(p, in, din, out);
     const int grid = (a.ne + NT1 - 1) / NT1;
     if (p->d.equation == FRGPU_BURGERS)
-        k_scalar1d<Real, NP, MODE, STAGE, true><<<grid, NT1, 0, p->stream>>>(a);
+        FR_CUDA(fr_launch(k_scalar1d<Real, NP, MODE, STAGE, true>, grid, NT1, 0, p->stream, a));
     else
-        k_scalar1d<Real, NP, MODE, STAGE, false><<<grid, NT1, 0, p->stream>>>(a);
+        FR_CUDA(fr_launch(k_scalar1d<Real, NP, MODE, STAGE, false>, grid, NT1, 0, p->stream, a));
     FR_CUDA(cudaGetLastError());
     p->launches += 1;
     return FRGPU_OK;
@@ -470,7 +474,7 @@ int launch_euler1d_t(frgpu_problem *p, const void *in, const void *din, void *ou
     if (p->prepare_only) return FRGPU_OK;
     auto a = make_args1<Real, NP>(p, in, din, out);
     const int grid = (a.ne + NT1 - 1) / NT1;
-    k_euler1d<Real, NP, MODE, STAGE><<<grid, NT1, 0, p->stream>>>(a);
+    FR_CUDA(fr_launch(k_euler1d<Real, NP, MODE, STAGE>, grid, NT1, 0, p->stream, a));
     FR_CUDA(cudaGetLastError());
     p->launches += 1;
     return FRGPU_OK;
@@ -497,9 +501,9 @@ int launch_bgk_t(frgpu_problem *p, const void *in, const void *din, void *out) {
     a.ops = make_ops1<Real, NP>(p->sp);
     a.status = p->d_status;
     if (a.nvel <= 64)
-        k_bgk1d_warp<Real, NP, MODE, STAGE><<<a.ne, 32 * NP, 0, p->stream>>>(a);
+        FR_CUDA(fr_launch(k_bgk1d_warp<Real, NP, MODE, STAGE>, a.ne, 32 * NP, 0, p->stream, a));
     else
-        k_bgk1d<Real, NP, MODE, STAGE><<<a.ne, NTB, 0, p->stream>>>(a);
+        FR_CUDA(fr_launch_opt(false, k_bgk1d<Real, NP, MODE, STAGE>, a.ne, NTB, 0, p->stream, a));
     FR_CUDA(cudaGetLastError());
     p->launches += 1;
     return FRGPU_OK;
