@@ -16,8 +16,8 @@ Measured, and asserted here:
 * at the shipped decision threshold (0.97) the network filters fewer elements
   than the plain test over the run, with an L2 error within 0.5 % of the plain
   test's.
-It costs time: the fused network adds about 8 % to the step on this workload
-(bench.py reports both forms).
+It costs time: the fused network adds a few per cent to the step on this
+workload (bench.py reports both forms).
 """
 import numpy as np
 import pytest
