@@ -432,6 +432,20 @@ def test_async_steps_report_through_reduce(frgpu, oracle, precision):
     b.step(3)
     sb, mb = b.reduce()
     assert np.array_equal(sa, sb) and ma == mb and np.array_equal(a.u, b.u)
+    # one step per call (the step and its reduction as one graph, both state buffers)
+    for _ in range(3):
+        sa, ma = a.step_reduce(1)
+        b.step(1)
+        sb, mb = b.reduce()
+        assert np.array_equal(sa, sb) and ma == mb
+    assert np.array_equal(a.u, b.u)
+    # an unphysical state is reported by the call that steps it
+    a.u = neg
+    with pytest.raises(frgpu.FRGPUError) as e:
+        a.step_reduce(1)
+    assert e.value.code in (-3, -4)
+    a.u = u
+    a.step_reduce(1)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32k"])
