@@ -38,6 +38,7 @@ template <class Real, int NP> struct C2Ops {
 template <class Real, int NP>
 __global__ void __launch_bounds__(256) k_c2_flux(const Real *__restrict__ u, const Real *__restrict__ met, int ne,
                                                  Real gm1, Real *__restrict__ fv, int *status) {
+    FR_PDL_ENTRY();
     const long n = (long)ne * NP * NP;
     const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -63,6 +64,7 @@ template <class Real, int NP>
 __global__ void __launch_bounds__(256) k_c2_traces(const Real *__restrict__ u, const Real *__restrict__ fv, int ne,
                                                    const C2Ops<Real, NP> op, Real *__restrict__ tu,
                                                    Real *__restrict__ tf) {
+    FR_PDL_ENTRY();
     const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (t >= (long)ne * NP) return;
     const int q = (int)(t / ne);
@@ -102,6 +104,7 @@ template <class Real, int NP> struct C2Args {
 
 template <class Real, int NP>
 __global__ void __launch_bounds__(256) k_c2_rhs(const C2Args<Real, NP> a) {
+    FR_PDL_ENTRY();
     const int nx = a.nx, ny = a.ny;
     const long ne = (long)nx * ny;
     const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -168,11 +171,11 @@ template <class Real, int NP> int launch_c2(frgpu_problem *p, const void *in, vo
         op.dgr[q] = (Real)p->sp.dhr[q];
         for (int r = 0; r < NP; ++r) op.D[q][r] = (Real)p->sp.dl[q + NP * r];
     }
-    k_c2_flux<Real, NP><<<(unsigned)((n + 255) / 256), 256, 0, p->stream>>>(
-        (const Real *)in, (const Real *)p->d_met, (int)ne, (Real)(p->d.gamma - 1.0), fv, p->d_status);
+    FR_CUDA(fr_launch(k_c2_flux<Real, NP>, (unsigned)((n + 255) / 256), 256, 0, p->stream,
+        (const Real *)in, (const Real *)p->d_met, (int)ne, (Real)(p->d.gamma - 1.0), fv, p->d_status));
     FR_CUDA(cudaGetLastError());
-    k_c2_traces<Real, NP><<<(unsigned)((ne * NP + 255) / 256), 256, 0, p->stream>>>((const Real *)in, fv, (int)ne, op,
-                                                                                     tu, tf);
+    FR_CUDA(fr_launch(k_c2_traces<Real, NP>, (unsigned)((ne * NP + 255) / 256), 256, 0, p->stream, (const Real *)in, fv, (int)ne, op,
+                                                                                     tu, tf));
     FR_CUDA(cudaGetLastError());
     C2Args<Real, NP> a;
     a.nx = nx;
@@ -184,7 +187,7 @@ template <class Real, int NP> int launch_c2(frgpu_problem *p, const void *in, vo
     a.tf = tf;
     a.out = (Real *)out;
     a.op = op;
-    k_c2_rhs<Real, NP><<<(unsigned)((n + 255) / 256), 256, 0, p->stream>>>(a);
+    FR_CUDA(fr_launch(k_c2_rhs<Real, NP>, (unsigned)((n + 255) / 256), 256, 0, p->stream, a));
     FR_CUDA(cudaGetLastError());
     p->launches += 3;
     return FRGPU_OK;
